@@ -1,0 +1,381 @@
+#!/usr/bin/env python
+"""Benchmark: milliseconds per pressure projection solved to FP64 relative
+residual 1e-8, on the 2048x2048 two-phase cut-cell workload (three seeded
+circles, density ratio 1000:1.2), one GB300.
+
+One step = one full projection of SIMCOFlow's UpdatePUV projection part:
+operator assembly + multigrid setup, right-hand side, PCG solve to
+||b - A x||_2 <= 1e-8 ||b||_2, velocity correction, mass residual.
+
+  value  device-resident: every input already in HBM (device pointers
+         through the C-ABI), CUDA events on the solver's stream
+  e2e    the same projection through the C-ABI with pinned host buffers:
+         host->device copies of all inputs and device->host copies of all
+         outputs inside the timed region
+  --impl reference  the CPU restatement of the reference path (the oracle,
+         C + OpenMP on all host cores), same workload and metric
+
+Prints one JSON line (rank 0).  Under torchrun each rank solves its own
+seeded instance (replicas, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "ms/projection to FP64 rel. residual 1e-8: learned+mixed FPCG vs plain MG-PCG"
+UNIT = "ms/projection"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_case(name: str, rank: int):
+    from simcoflow_gb300 import synth
+    return synth.make_case(name, instance=rank)
+
+
+WORKLOADS = {
+    "c2": "2048x2048 cut-cell two-phase projection, 3 seeded circles, density 1000:1.2, "
+          "32-mode u*, dt 5e-4 (plain FP64 MG-PCG)",
+    "c1": "128x128 cut-cell two-phase projection, circle r=0.1, density 1000:1.2",
+    "c3": "4096x4096 y-stretched grid, rotated plate, density 1000:1.2 (plain FP64 MG-PCG)",
+}
+
+# compulsory bytes per fine cell of each measured kernel (kernel table)
+KERNEL_BYTES = {"smooth": 48, "pupdate_spmv": 56, "update_xr": 48, "resid_restrict": 40,
+                "prolong": 18}
+
+
+def kernels_per_iteration(levels: int, npre: int, npost: int) -> int:
+    if levels == 1:
+        return 2 + 2
+    return (levels - 1) * (2 * npre + 2 * npost + 2) + 1 + 2
+
+
+def cpu_projection_ms(case, threads: int) -> tuple[float, dict]:
+    """One projection through the oracle's C restatement (assembly, RHS,
+    FP64 MG-PCG to 1e-8, correction) on `threads` host threads."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    O.lib().oracle_set_threads(threads)
+    t0 = time.perf_counter()
+    pc = O.pocoef(case)
+    matr, A = O.matrix(case, pc)
+    rhm, b = O.rhs(case)
+    xi, it, rel, nlev = O.mgpcg(case, matr, rhm, rtol=1e-8, maxit=500, npre=2, npost=2,
+                                omega=1.9, threads=threads)
+    x = O.x_from_interior(case, xi)
+    Pp = O.scatter(case, x)
+    O.correct(case, Pp)
+    ms = (time.perf_counter() - t0) * 1e3
+    return ms, {"iters": it, "relres": rel, "levels": nlev}
+
+
+def run_reference(args):
+    world, rank, local = _dist()
+    if rank != 0:
+        return 0
+    case = make_case(args.config, 0)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_projection_ms(case, threads)
+    times, info = [], {}
+    for _ in range(args.steps):
+        ms, info = cpu_projection_ms(case, threads)
+        times.append(ms)
+    ms = float(np.mean(times))
+    line = {"impl": "reference", "metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded, shapes and distributions of the named config)",
+            "config": {"workload": WORKLOADS.get(args.config, args.config), "name": args.config,
+                       "nx": case.nx, "ny": case.ny},
+            "cpu_baseline": {"value": ms, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"one full {case.nx}x{case.ny} projection per step "
+                                       f"(C restatement + OpenMP; Fortran+HYPRE reference "
+                                       f"unbuildable: no Fortran compiler, MPI or HYPRE)",
+                             "iters": info.get("iters")},
+            "e2e": {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = _dist()
+    from simcoflow_gb300 import build as B
+    B.build_all()
+    from simcoflow_gb300 import projection as P
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+    case = make_case(args.config, rank)
+    A = case.arrays
+    nx, ny = case.nx, case.ny
+    stream = torch.cuda.Stream(device=dev)
+
+    def barrier():
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize(dev)
+
+    # ---- device-resident arm ----
+    tdev = {k: torch.from_numpy(np.ascontiguousarray(v.ravel(order="F"))).to(dev)
+            for k, v in A.items() if isinstance(v, np.ndarray)}
+    s = P.ProjectionSolver(nx, ny, device=local, device_ptrs=True, rtol=1e-8, maxit=200)
+    s.set_stream(stream.cuda_stream)
+    s.set_grid(tdev["dx"], tdev["dy"], tdev["dxU"], tdev["dyV"])
+    s.set_geometry(**{k: tdev[k] for k in P.GEOMETRY_ARGS})
+    u, v, p = tdev["u0"].clone(), tdev["v0"].clone(), tdev["p0"].clone()
+    Pp = torch.zeros_like(tdev["p0"])
+    mres = torch.zeros(nx * ny, dtype=torch.float64, device=dev)
+
+    def step():
+        s.assemble(tdev["DpU"], tdev["DpV"], case.betaP, case.betaM, case.bc)
+        _, _, st = s.update_puv(tdev["ustar"], tdev["vstar"], u, v, p, case.vb, Pp=Pp,
+                                mres=mres)
+        return st
+
+    for _ in range(args.warmup):
+        st = step()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    iters, relres = [], []
+    with ClockSampler(local) as clk:
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            st = step()
+            iters.append(st.iters)
+            relres.append(st.relres_true)
+        e1.record(stream)
+        barrier()
+    ms_total = e0.elapsed_time(e1)
+    if pg:
+        t = torch.tensor([ms_total], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    levels = st.levels
+
+    # per-kernel live timing on the same data (back-to-back launches)
+    kt = {}
+    for name, kid in (("smooth", 0), ("pupdate_spmv", 1), ("update_xr", 2),
+                      ("resid_restrict", 3), ("prolong", 4)):
+        import ctypes
+        out = ctypes.c_double(0.0)
+        rc = P.load().scf_proj_time_kernel(s._h, kid, 50, ctypes.byref(out))
+        if rc == 0:
+            kt[name] = out.value
+    s.close()
+
+    # ---- end-to-end arm: host (pinned) buffers through the C-ABI ----
+    def pinned(a):
+        t = torch.empty(a.size, dtype=torch.float64 if a.dtype == np.float64 else torch.int32)
+        t = t.pin_memory()
+        arr = t.numpy().reshape(a.shape, order="F")
+        arr[...] = a
+        return arr, t
+
+    hp = {k: pinned(v) for k, v in A.items() if isinstance(v, np.ndarray)}
+    H = {k: v[0] for k, v in hp.items()}
+    hs = P.ProjectionSolver(nx, ny, device=local, rtol=1e-8, maxit=200)
+    hs.set_stream(stream.cuda_stream)
+    hu, hv, hpp = pinned(A["u0"])[0], pinned(A["v0"])[0], pinned(A["p0"])[0]
+    hPp = pinned(np.zeros((nx + 2, ny + 2), order="F"))[0]
+    hm = pinned(np.zeros((nx, ny), order="F"))[0]
+    in_keys = ["dx", "dy", "dxU", "dyV", *P.GEOMETRY_ARGS, "DpU", "DpV", "ustar", "vstar"]
+    h2d = sum(H[k].nbytes for k in in_keys) + hu.nbytes + hv.nbytes + hpp.nbytes
+    d2h = hPp.nbytes + hu.nbytes + hv.nbytes + hpp.nbytes + hm.nbytes
+
+    def e2e_step():
+        hs.set_grid(H["dx"], H["dy"], H["dxU"], H["dyV"])
+        hs.set_geometry(**{k: H[k] for k in P.GEOMETRY_ARGS})
+        hs.assemble(H["DpU"], H["DpV"], case.betaP, case.betaM, case.bc)
+        hs.update_puv(H["ustar"], H["vstar"], hu, hv, hpp, case.vb, Pp=hPp, mres=hm)
+        return float(np.abs(hm).max())  # read of the step's result on the host
+
+    for _ in range(args.warmup):
+        e2e_step()
+    barrier()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    f1.record(stream)
+    barrier()
+    e2e_ms = f0.elapsed_time(f1) / args.steps
+    if pg:
+        t = torch.tensor([e2e_ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    hs.close()
+
+    if rank != 0:
+        if pg:
+            pg.destroy_process_group()
+        return 0
+
+    peak, peak_kind = _peaks()
+    cells = nx * ny
+    dom = "smooth"
+    roof = None
+    if dom in kt and kt[dom] > 0:
+        bytes_launch = KERNEL_BYTES[dom] * cells
+        achieved = bytes_launch / (kt[dom] * 1e-3) / 1e9
+        traffic = None
+        tf = ROOT / "profiles" / "traffic.json"
+        if tf.exists():
+            try:
+                traffic = json.loads(tf.read_text()).get(f"{dom}_{args.config}")
+            except Exception:
+                traffic = None
+        roof = {"bound": "hbm", "kernel": "k_smooth (red-black Gauss-Seidel half sweep, fine grid)",
+                "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                "bytes_per_launch": bytes_launch, "ms_per_launch": kt[dom],
+                "traffic": traffic,
+                "kernel_timing": "CUDA events around 50 back-to-back launches on the solver "
+                                 "stream, right after the timed region, same data"}
+    kernels = {k: {"ms": round(v, 5), "GBps": round(KERNEL_BYTES[k] * cells / (v * 1e-3) / 1e9, 1)}
+               for k, v in kt.items()}
+    per_it = kernels_per_iteration(levels, 2, 2)
+    launches = 0
+    for it in iters:
+        launches += (levels - 1) + 3 + 1 + 3  # assemble, excess, coarsen, coarse setup, rhs, final x3
+        launches += ((it + 1) // 2) * 2 * per_it
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        ms_cpu, info = cpu_projection_ms(case, threads)
+        cpu = {"value": round(ms_cpu, 2), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"one full {nx}x{ny} projection (C restatement of the reference path, "
+                         f"OpenMP, {info['iters']} MG-PCG iterations)"}
+    line = {
+        "metric": METRIC, "value": round(ms_step, 4), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded; shapes and distributions of the named config)",
+        "config": {"workload": WORKLOADS.get(args.config, args.config), "name": args.config,
+                   "nx": nx, "ny": ny, "path": "plain FP64 MG-PCG",
+                   "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (about 1.3 GB of arrays per projection)"},
+        "solves_per_s": round(1e3 * world / ms_step, 2),
+        "iters": iters[-1], "relres_true": relres[-1], "levels": levels,
+        "e2e": {"value": round(e2e_ms, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "roofline": roof, "kernels": kernels, "gpu_launches": int(launches),
+        "cpu_baseline": cpu, "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    if pg:
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,178 @@
+/*
+ * scf_proj.h -- C-ABI of the GB300 pressure-projection library
+ * (libscf_proj.so, CUDA kernels for sm_103a).
+ *
+ * Drop-in replacement for the projection step of SIMCOFlow:
+ *   PoissonEquationSolver   src/ProjectionP_Mod.f90:26-99
+ *   (ComputePossionMatrixCoefficient :395-580, SetBasicSolver :101-135,
+ *    SetPoissonMatrix :137-273, SetPoissonVectors :275-354,
+ *    HYPRE_ParCSRPCGSetup/Solve :57-58, DeltaPressureGetValues :356-393,
+ *    DeltaPressureBoundaryCondition :582-595)
+ *   UpdatePUV, projection part   src/ComputePUV_Mod.f90:56-218
+ *    (velocity correction :59-152, pressure copy :163-169, top-row
+ *     continuity :177-182, mass residual :184-217,
+ *     VariablesInternalCellCondition :227-245)
+ * The HYPRE IJ / ParCSR-PCG / BoomerAMG calls are replaced by a matrix-free
+ * FP64 PCG preconditioned by a geometric multigrid V-cycle on the GPU.
+ *
+ * Arrays are passed exactly as the Fortran caller holds them: column-major,
+ * i fastest, with the bounds given beside each argument:
+ *   (nx,ny)     means (1:Isize,1:Jsize)
+ *   (nx+2,ny+2) means (0:Isize+1,0:Jsize+1)
+ * Pointers are host pointers unless the handle was created with
+ * SCF_FLAG_DEVICE_PTRS, in which case every array argument is a device
+ * pointer (cudaMalloc'd) on the handle's device.  With device pointers,
+ * set_grid / set_geometry keep the pointers (no copy): the arrays must stay
+ * alive and unchanged until the next set_* call.
+ *
+ * Threading: one handle per host thread; calls on one handle are not
+ * re-entrant.  All work is ordered on the handle's CUDA stream; every call
+ * returns after its results are on the host (host mode) or after its work
+ * has been enqueued and completed (device mode).
+ * Errors: every function returns SCF_OK (0) or a negative SCF_ERR_* code;
+ * nothing aborts, exits or pauses (the reference pauses on NaN,
+ * src/ProjectionP_Mod.f90:209-213, :322-325, :383-386).
+ */
+#ifndef SCF_PROJ_H
+#define SCF_PROJ_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SCF_OK 0
+#define SCF_ERR_ARG (-1)           /* bad argument or size */
+#define SCF_ERR_CUDA (-2)          /* a CUDA call failed */
+#define SCF_ERR_NAN (-3)           /* NaN or Inf in the operator, RHS or iterate */
+#define SCF_ERR_NOT_CONVERGED (-4) /* maxit reached before rtol */
+#define SCF_ERR_STALL (-5)         /* residual stopped decreasing */
+#define SCF_ERR_TIMEOUT (-6)       /* a bounded device-side wait ran out */
+#define SCF_ERR_STATE (-7)         /* call order: e.g. solve before assemble */
+#define SCF_ERR_NOMEM (-8)         /* device allocation failed */
+
+#define SCF_PREC_FP64 0  /* FP64 MG preconditioner inside FP64 PCG */
+#define SCF_PREC_MIXED 1 /* FP32 MG with BF16 couplings inside FP64 flexible PCG */
+
+#define SCF_FLAG_DEVICE_PTRS 1 /* array arguments are device pointers */
+#define SCF_FLAG_NO_GRAPH 2    /* launch kernels one by one, no CUDA graph */
+
+typedef struct scf_opts {
+    int precision;   /* SCF_PREC_FP64 or SCF_PREC_MIXED */
+    int flags;       /* SCF_FLAG_* */
+    int device;      /* CUDA device ordinal */
+    int maxit;       /* outer PCG iterations (reference: 50, :108) */
+    double rtol;     /* stop at ||b-Ax||_2 <= rtol ||b||_2 (reference: 1e-20, :111) */
+    int npre, npost; /* red-black Gauss-Seidel sweeps before / after coarse correction */
+    double omega;    /* scale of the coarse-grid correction */
+    int coarse_max;  /* coarsest level has at most this many cells (<= 64) */
+    int reserved[8];
+} scf_opts;
+
+typedef struct scf_stats {
+    int iters;          /* outer PCG iterations taken */
+    int status;         /* SCF_OK or SCF_ERR_NOT_CONVERGED / _NAN / _STALL */
+    int levels;         /* multigrid levels */
+    int fallbacks;      /* preconditioner fallbacks taken */
+    double bnorm;       /* ||b||_2 */
+    double relres;      /* recursive ||r||_2/||b||_2 at exit */
+    double relres_true; /* FP64 recomputed ||b - A x||_2/||b||_2 */
+    double mres_max;    /* max |mres| over cells with Posnu /= -1 (update_puv) */
+    double ms_h2d, ms_assemble, ms_solve, ms_correct, ms_d2h, ms_total;
+} scf_stats;
+
+typedef struct scf_proj scf_proj;
+
+/* Fill opts with defaults: FP64, host pointers, device 0, maxit 200,
+ * rtol 1e-8, 2 pre / 2 post sweeps, omega 1.9, coarse_max 64. */
+void scf_opts_default(scf_opts *opts);
+
+/* Create a solver for an nx-by-ny pressure grid (Isize, Jsize).  Allocates
+ * all device memory for the operator, the multigrid hierarchy and the PCG
+ * vectors once; the handle is reused across time steps (the reference
+ * rebuilds its HYPRE objects on every call, src/ProjectionP_Mod.f90:52-69). */
+int scf_proj_create(scf_proj **h, int nx, int ny, const scf_opts *opts);
+int scf_proj_destroy(scf_proj *h);
+
+/* Use the given cudaStream_t (passed as void*) for all later work. */
+int scf_proj_set_stream(scf_proj *h, void *stream);
+
+/* Grid spacings: PGrid%dx, PGrid%dy, UGrid%dx, VGrid%dy, each (nx,ny)
+ * (TYPE(Grid), src/Mesh_Mod.f90:11-15). */
+int scf_proj_set_grid(scf_proj *h, const double *dx, const double *dy, const double *dxU,
+                      const double *dyV);
+
+/* Cut-cell and interface geometry (TYPE(Cell), src/Mesh_Mod.f90:17-41):
+ *   vof, phi, vofS, nyS, WlLh         PCell fields, (nx,ny)
+ *   aE, aW, aN, aS                    PCell%E/W/N/SEdge_Area, (nx+2,ny+2)
+ *   posnu_p                           PCell%Posnu, (nx+2,ny+2)
+ *   posnu_u, posnu_v                  UCell%Posnu, VCell%Posnu, (nx+2,ny+2)
+ *   moex_u, moex_v                    UCell%MoExCell, VCell%MoExCell, (nx,ny)
+ *   vofS_u, vofS_v                    UCell%vofS, VCell%vofS, (nx,ny) */
+int scf_proj_set_geometry(scf_proj *h, const double *vof, const double *phi,
+                          const double *vofS, const double *nyS, const double *WlLh,
+                          const double *aE, const double *aW, const double *aN,
+                          const double *aS, const int32_t *posnu_p, const int32_t *posnu_u,
+                          const int32_t *moex_u, const double *vofS_u,
+                          const int32_t *posnu_v, const int32_t *moex_v,
+                          const double *vofS_v);
+
+/* Assemble the variable-density cut-cell operator and set up the multigrid
+ * hierarchy.  Replaces ComputePossionMatrixCoefficient + SetPoissonMatrix +
+ * HYPRE_ParCSRPCGSetup (src/ProjectionP_Mod.f90:50-57).
+ *   DpU, DpV   PU%Dp, PV%Dp, (nx+2,ny+2) (src/PredictorUV_mod.f90:700)
+ *   betaP, betaM  1/(row/Roref), 1/(roa/Roref) (src/ComputePUV_Mod.f90:42-43)
+ *   wb, eb, sb, nb  1 = Neumann, 0 = Dirichlet (the reference passes 1,1,1,0) */
+int scf_proj_assemble(scf_proj *h, const double *DpU, const double *DpV, double betaP,
+                      double betaM, int wb, int eb, int sb, int nb);
+
+/* PoissonEquationSolver: right-hand side from the predicted velocities
+ * ustar = Pred%u, vstar = Pred%v (nx+2,ny+2) and the body velocity vb,
+ * then the PCG solve, then Pp = Proj%Pp (nx+2,ny+2) with the ghost
+ * conditions of DeltaPressureBoundaryCondition.  st may be NULL. */
+int scf_proj_poisson_solve(scf_proj *h, const double *ustar, const double *vstar, double vb,
+                           double *Pp, scf_stats *st);
+
+/* The projection part of UpdatePUV (src/ComputePUV_Mod.f90:56-218):
+ * poisson_solve, then the pressure-gradient correction of the faces,
+ * p = Pp on cells with an unknown, top-row continuity, the mass residual
+ * and the zeroing of solid cells.
+ *   u, v, p  TVar%u, TVar%v, TVar%p (nx+2,ny+2): in = old values (faces that
+ *            the reference does not correct keep them), out = new values
+ *   mres     TVar%mres (nx,ny), out
+ *   Pp       Proj%Pp (nx+2,ny+2), out; may be NULL */
+int scf_proj_update_puv(scf_proj *h, const double *ustar, const double *vstar, double vb,
+                        double *Pp, double *p, double *u, double *v, double *mres,
+                        scf_stats *st);
+
+/* Diagnostics: the assembled symmetric operator in Fortran (nx,ny) layout.
+ * cE(i,j) = -A(row(i,j), row(i+1,j)), cN(i,j) = -A(row(i,j), row(i,j+1)),
+ * diag(i,j) = A(row(i,j), row(i,j)) (-1 where Posnu = -1); rhs (nx,ny) is
+ * the last right-hand side (0 where Posnu = -1).  Any pointer may be NULL;
+ * always host pointers. */
+int scf_proj_get_operator(scf_proj *h, double *cE, double *cN, double *diag, double *rhs);
+
+/* Diagnostics: apply one multigrid V-cycle (the preconditioner) to b and
+ * return x, both host arrays in Fortran (nx,ny) layout. */
+int scf_proj_vcycle(scf_proj *h, const double *b, double *x);
+
+/* Measurement: launch one kernel of the path `reps` times back to back on
+ * the handle's stream, bracketed by CUDA events, and store the average
+ * milliseconds per launch.  Overwrites the solver's work vectors (call it
+ * between solves, after assemble).  No counterpart in the reference; it
+ * exists so that per-kernel bandwidth can be measured live. */
+#define SCF_K_SMOOTH 0         /* one red-black half sweep on the fine grid */
+#define SCF_K_PUPDATE_SPMV 1   /* p = z + beta p, q = A p, p.q */
+#define SCF_K_UPDATE_XR 2      /* x += alpha p, r -= alpha q, r.r */
+#define SCF_K_RESID_RESTRICT 3 /* fine residual summed onto the first coarse level */
+#define SCF_K_PROLONG 4        /* fine x += omega * coarse x */
+#define SCF_K_ASSEMBLE 5       /* operator assembly from the Fortran arrays */
+int scf_proj_time_kernel(scf_proj *h, int kernel, int reps, double *ms_per_launch);
+
+/* Human-readable text for a status code. */
+const char *scf_strerror(int code);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

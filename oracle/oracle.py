@@ -1,0 +1,377 @@
+"""Oracle of the projection path -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py may
+import this module.  The simcoflow_gb300 package never does.
+
+Parity status: UNPINNED.  The reference (Fortran 90 + HYPRE + MPI) cannot be
+compiled here or on the GPU host (no Fortran compiler, MPI or HYPRE) and ships
+no tests or golden vectors.  The restatement is pinned instead against the
+reference's built-in identities (per-row |A p - b| <= 1e-10,
+src/ProjectionP_Mod.f90:70-93; mass residual, src/ComputePUV_Mod.f90:184-216)
+and analytic known-answer cases (tests/test_oracle.py).
+
+Pieces:
+  C restatement (scf_oracle.c, via ctypes)
+    pocoef      ComputePossionMatrixCoefficient  src/ProjectionP_Mod.f90:395-580
+    matrix      SetPoissonMatrix                 src/ProjectionP_Mod.f90:137-273
+    rhs         SetPoissonVectors                src/ProjectionP_Mod.f90:275-354
+    scatter     DeltaPressureGetValues + BC      src/ProjectionP_Mod.f90:356-393, 582-595
+    correct     UpdatePUV correction .. zeroing  src/ComputePUV_Mod.f90:59-245
+    mgpcg       CPU FP64 MG-PCG (same algorithm as the CUDA path)
+  solve_direct  the HYPRE PCG/BoomerAMG solve replaced by SuperLU on the same
+                CSR matrix (an exact FP64 solve; HYPRE is not available)
+  geometry_literal  pure-Python restatement of Cell_Geo_Cal, frac, numbering
+                and DefineMomentumExchangeCell for small grids, to check the
+                package's geometry builder.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+import build as _build  # noqa: E402
+
+_P = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int32)
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(str(path))
+        L.oracle_pocoef.argtypes = [C.c_int, C.c_int, C.c_int] + [_P] * 9 + [C.c_double, C.c_double, _P]
+        L.oracle_matrix.restype = C.c_int
+        L.oracle_matrix.argtypes = [C.c_int, C.c_int, _P, _P, _P, _P, _P, _I, C.c_int, C.c_int,
+                                    C.c_int, C.c_int, _P, _I, _I, _P]
+        L.oracle_rhs.argtypes = [C.c_int, C.c_int] + [_P] * 10 + [_I, C.c_double, _P, _P]
+        L.oracle_scatter.argtypes = [C.c_int, C.c_int, _I, _P, C.c_int, C.c_int, C.c_int,
+                                     C.c_int, _P]
+        L.oracle_correct.argtypes = ([C.c_int, C.c_int] + [_P] * 3 + [_P] * 3 + [_P] * 2 +
+                                     [_P] * 4 + [_I, _I, _I, _P, _I, _I, _P] + [_P] * 6 +
+                                     [C.c_double, C.c_double, C.c_double, _P, _P, _P, _P])
+        L.oracle_row_residual.restype = C.c_double
+        L.oracle_row_residual.argtypes = [C.c_int, C.c_int, _P, _P, _P, _I]
+        L.oracle_mgpcg.restype = C.c_int
+        L.oracle_mgpcg.argtypes = [C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_double, C.c_int,
+                                   C.c_int, C.c_int, C.c_double, C.c_int, _P, C.POINTER(C.c_int)]
+        L.oracle_vcycle.argtypes = [C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_int, C.c_int,
+                                    C.c_double, C.c_int]
+        L.oracle_num_threads.restype = C.c_int
+        L.oracle_set_threads.argtypes = [C.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    if a is None:
+        return None
+    assert a.flags["F_CONTIGUOUS"] or a.ndim == 1, "arrays must be Fortran ordered"
+    return a.ctypes.data_as(_P if a.dtype == np.float64 else _I)
+
+
+def pocoef(case, literal=False) -> np.ndarray:
+    a = case.arrays
+    pc = np.zeros((case.nx, case.ny, 4), order="F")
+    lib().oracle_pocoef(case.nx, case.ny, int(literal), _p(a["vof"]), _p(a["phi"]), _p(a["vofS"]),
+                        _p(a["dx"]), _p(a["dy"]), _p(a["dxU"]), _p(a["dyV"]), _p(a["DpU"]),
+                        _p(a["DpV"]), case.betaP, case.betaM, _p(pc))
+    return pc
+
+
+def matrix(case, pc=None):
+    """Returns (matr (nx,ny,5), scipy CSR in Posnu numbering)."""
+    import scipy.sparse as sp
+    a = case.arrays
+    if pc is None:
+        pc = pocoef(case)
+    nx, ny = case.nx, case.ny
+    nmax = nx * ny
+    matr = np.zeros((nx, ny, 5), order="F")
+    rowptr = np.zeros(nmax + 1, dtype=np.int32)
+    cols = np.zeros(5 * nmax, dtype=np.int32)
+    vals = np.zeros(5 * nmax)
+    wb, eb, sb, nb = case.bc
+    nrows = lib().oracle_matrix(nx, ny, _p(pc), _p(a["aE"]), _p(a["aW"]), _p(a["aN"]), _p(a["aS"]),
+                                _p(a["posnu_p"]), wb, eb, sb, nb, _p(matr), _p(rowptr), _p(cols),
+                                _p(vals))
+    nnz = rowptr[nrows]
+    A = sp.csr_matrix((vals[:nnz], cols[:nnz], rowptr[: nrows + 1]), shape=(nrows, nrows))
+    return matr, A
+
+
+def rhs(case, ustar=None, vstar=None, vb=None):
+    a = case.arrays
+    nx, ny = case.nx, case.ny
+    us = a["ustar"] if ustar is None else ustar
+    vs = a["vstar"] if vstar is None else vstar
+    vb = case.vb if vb is None else vb
+    rhm = np.zeros((nx, ny), order="F")
+    n = int((a["posnu_p"][1:nx + 1, 1:ny + 1] != -1).sum())
+    b = np.zeros(max(n, 1))
+    lib().oracle_rhs(nx, ny, _p(us), _p(vs), _p(a["aE"]), _p(a["aW"]), _p(a["aN"]), _p(a["aS"]),
+                     _p(a["dx"]), _p(a["dy"]), _p(a["nyS"]), _p(a["WlLh"]), _p(a["posnu_p"]), vb,
+                     _p(rhm), _p(b))
+    return rhm, b[:n]
+
+
+def scatter(case, x) -> np.ndarray:
+    Pp = np.zeros((case.nx + 2, case.ny + 2), order="F")
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    wb, eb, sb, nb = case.bc
+    lib().oracle_scatter(case.nx, case.ny, _p(case["posnu_p"]), x.ctypes.data_as(_P), wb, eb, sb,
+                         nb, _p(Pp))
+    return Pp
+
+
+def correct(case, Pp, u0=None, v0=None, p0=None, vb=None):
+    a = case.arrays
+    nx, ny = case.nx, case.ny
+    u = (a["u0"] if u0 is None else u0).copy(order="F")
+    v = (a["v0"] if v0 is None else v0).copy(order="F")
+    p = (a["p0"] if p0 is None else p0).copy(order="F")
+    mres = np.zeros((nx, ny), order="F")
+    vb = case.vb if vb is None else vb
+    lib().oracle_correct(nx, ny, _p(Pp), _p(a["ustar"]), _p(a["vstar"]), _p(a["vof"]),
+                         _p(a["phi"]), _p(a["vofS"]), _p(a["nyS"]), _p(a["WlLh"]), _p(a["aE"]),
+                         _p(a["aW"]), _p(a["aN"]), _p(a["aS"]), _p(a["posnu_p"]),
+                         _p(a["posnu_u"]), _p(a["moex_u"]), _p(a["vofS_u"]), _p(a["posnu_v"]),
+                         _p(a["moex_v"]), _p(a["vofS_v"]), _p(a["dx"]), _p(a["dy"]),
+                         _p(a["dxU"]), _p(a["dyV"]), _p(a["DpU"]), _p(a["DpV"]), case.betaP,
+                         case.betaM, vb, _p(u), _p(v), _p(p), _p(mres))
+    return u, v, p, mres
+
+
+def row_residual(case, matr, Pp, rhm) -> float:
+    return lib().oracle_row_residual(case.nx, case.ny, _p(matr), _p(Pp), _p(rhm),
+                                     _p(case["posnu_p"]))
+
+
+def solve_direct(A, b) -> np.ndarray:
+    """FP64 direct solve of the reference's own matrix (SuperLU)."""
+    import scipy.sparse.linalg as spla
+    if A.shape[0] == 0:
+        return np.zeros(0)
+    return spla.spsolve(A.tocsc(), b)
+
+
+def symmetric_operator(case, matr):
+    """The symmetric 5-point storage of the CUDA path built from matr:
+    cE = -matr(.,.,4), cN = -matr(.,.,5), dg = matr(.,.,3) (-1 without an
+    unknown), in 0-based C order (ny, nx) flattened."""
+    nx, ny = case.nx, case.ny
+    act = case["posnu_p"][1:nx + 1, 1:ny + 1] != -1
+    cE = np.where(act, -matr[:, :, 3], 0.0) + 0.0
+    cN = np.where(act, -matr[:, :, 4], 0.0) + 0.0
+    dg = np.where(act, matr[:, :, 2], -1.0)
+    f = lambda a: np.ascontiguousarray(a.T).ravel()
+    return f(cE), f(cN), f(dg)
+
+
+def mgpcg(case, matr, rhm, rtol=1e-13, maxit=500, npre=1, npost=1, omega=1.0, coarse_max=64,
+          threads=0):
+    """CPU FP64 MG-PCG on the symmetric operator.  Returns (Pp-interior x as
+    (nx,ny) Fortran array, iterations, true relres, levels)."""
+    nx, ny = case.nx, case.ny
+    cE, cN, dg = symmetric_operator(case, matr)
+    b = np.ascontiguousarray(rhm.T).ravel()
+    x = np.zeros(nx * ny)
+    rel = C.c_double(0.0)
+    nlev = C.c_int(0)
+    if threads:
+        lib().oracle_set_threads(threads)
+    it = lib().oracle_mgpcg(nx, ny, cE.ctypes.data_as(_P), cN.ctypes.data_as(_P),
+                            dg.ctypes.data_as(_P), b.ctypes.data_as(_P), x.ctypes.data_as(_P),
+                            rtol, maxit, npre, npost, omega, coarse_max, C.byref(rel),
+                            C.byref(nlev))
+    return np.asfortranarray(x.reshape(ny, nx).T), it, rel.value, nlev.value
+
+
+def vcycle(case, matr, b_f, npre=1, npost=1, omega=1.0, coarse_max=64) -> np.ndarray:
+    nx, ny = case.nx, case.ny
+    cE, cN, dg = symmetric_operator(case, matr)
+    b = np.ascontiguousarray(b_f.T).ravel()
+    x = np.zeros(nx * ny)
+    lib().oracle_vcycle(nx, ny, cE.ctypes.data_as(_P), cN.ctypes.data_as(_P),
+                        dg.ctypes.data_as(_P), b.ctypes.data_as(_P), x.ctypes.data_as(_P), npre,
+                        npost, omega, coarse_max)
+    return np.asfortranarray(x.reshape(ny, nx).T)
+
+
+def x_from_interior(case, xint):
+    """Posnu-ordered vector from an (nx,ny) interior field."""
+    pn = case["posnu_p"][1:case.nx + 1, 1:case.ny + 1]
+    n = int((pn != -1).sum())
+    x = np.zeros(n)
+    m = pn != -1
+    x[pn[m]] = xint[m]
+    return x
+
+
+def project(case, solver="direct", **kw) -> dict:
+    """The whole reference projection on the CPU: assembly, RHS, FP64 solve,
+    scatter, correction.  solver='direct' (SuperLU) or 'mg' (CPU MG-PCG)."""
+    pc = pocoef(case)
+    matr, A = matrix(case, pc)
+    rhm, b = rhs(case)
+    if solver == "direct":
+        x = solve_direct(A, b)
+    else:
+        xi, it, rel, nlev = mgpcg(case, matr, rhm, **kw)
+        x = x_from_interior(case, xi)
+    Pp = scatter(case, x)
+    u, v, p, mres = correct(case, Pp)
+    res = row_residual(case, matr, Pp, rhm)
+    bn = float(np.linalg.norm(b))
+    relres = float(np.linalg.norm(A @ x - b) / bn) if bn > 0 else 0.0
+    return {"pocoef": pc, "matr": matr, "A": A, "rhm": rhm, "b": b, "x": x, "Pp": Pp, "u": u,
+            "v": v, "p": p, "mres": mres, "row_residual": res, "relres": relres}
+
+
+# ---------------------------------------------------------------------------
+# Literal pure-Python restatement of the geometry pipeline (small grids only)
+# ---------------------------------------------------------------------------
+
+def frac_literal(nx, ny, diss, dx, dy):
+    """frac, src/Clsvof_Mod.f90:1371-1404."""
+    slop_eps = 1.0e-20
+    tnx, tny = abs(nx), abs(ny)
+    if diss + 0.5 * (tnx * dx + tny * dy) <= 0.0:
+        return 1.0
+    if diss - 0.5 * (tnx * dx + tny * dy) >= 0.0:
+        return 0.0
+    if tnx <= slop_eps:
+        return 0.5 - diss / dy
+    if tny <= slop_eps:
+        return 0.5 - diss / dx
+    xx = (0.5 * tny * dy - diss) / dx / tnx + 0.5
+    yy = (0.5 * tnx * dx - diss) / dy / tny + 0.5
+    totalarea = 0.5 * xx * yy
+    topvf = ((yy - 1.0) / yy) ** 2.0 if yy > 1.0 else 0.0
+    rightvf = ((xx - 1.0) / xx) ** 2.0 if xx > 1.0 else 0.0
+    return totalarea * (1.0 - topvf - rightvf)
+
+
+def _edge(p1, p2, nxx, nyy, diss):
+    """Edge_Geo_Cal, src/Cutcell_Mod.f90:302-337 (edge solid fraction)."""
+    l1 = nxx * p1[0] + nyy * p1[1] + diss
+    l2 = nxx * p2[0] + nyy * p2[1] + diss
+    e = 1.0e-14
+    if l1 >= e and l2 >= e:
+        return 0.0
+    if l1 < e and l2 < e:
+        return 1.0
+    if l1 >= e and l2 < e:
+        return abs(l2) / (abs(l1) + abs(l2))
+    return abs(l1) / (abs(l1) + abs(l2))
+
+
+def geometry_literal(nx, ny, dxP, dyP, vofS_in, phiS, nxS, nyS, vofS_u_in, vofS_v_in,
+                     icorprob=True):
+    """Cell_Geo_Cal (P, U, V), DefineMomentumExchangeCell and
+    NumberExternalCell (src/Cutcell_Mod.f90:34-358) on (nx,ny) inputs given
+    as dicts/arrays indexed [i, j] 1-based via helper.  Returns a dict with
+    the same keys and layouts as simcoflow_gb300.geometry.build."""
+    epsi, epsiF, rnd = 1.0e-3, 1.0e-2, 1.0e-24
+    E = np.zeros((nx + 2, ny + 2)); W = np.zeros_like(E); N = np.zeros_like(E); S = np.zeros_like(E)
+    vs = np.array(vofS_in, dtype=float).copy()
+    ny_s = np.array(nyS, dtype=float).copy()
+    nx_s = np.array(nxS, dtype=float).copy()
+    WL = np.zeros((nx, ny))
+    for i in range(1, nx + 1):
+        for j in range(1, ny + 1):
+            dx, dy = dxP[i - 1, j - 1], dyP[i - 1, j - 1]
+            a, b, p = nx_s[i - 1, j - 1], ny_s[i - 1, j - 1], phiS[i - 1, j - 1]
+            P00, P01, P10, P11 = (-dx * 0.5, -dy * 0.5), (-dx * 0.5, dy * 0.5), (dx * 0.5, -dy * 0.5), (dx * 0.5, dy * 0.5)
+            W[i, j] = _edge(P00, P01, a, b, p)
+            N[i, j] = _edge(P01, P11, a, b, p)
+            E[i, j] = _edge(P11, P10, a, b, p)
+            S[i, j] = _edge(P10, P00, a, b, p)
+    for i in range(1, nx + 1):
+        for j in range(1, ny + 1):
+            WL[i - 1, j - 1] = math.sqrt(((E[i, j] - W[i, j]) * dxP[i - 1, j - 1]) ** 2.0 +
+                                         ((N[i, j] - S[i, j]) * dyP[i - 1, j - 1]) ** 2.0)
+    for i in range(1, nx + 1):
+        for j in range(1, ny + 1):
+            W[i, j] = 1.0 - W[i, j]; E[i, j] = 1.0 - E[i, j]
+            N[i, j] = 1.0 - N[i, j]; S[i, j] = 1.0 - S[i, j]
+    for i in range(2, nx):
+        for j in range(2, ny):
+            av = 2.0 * N[i, j] * S[i, j + 1] / (N[i, j] + S[i, j + 1] + rnd)
+            N[i, j] = av; S[i, j + 1] = av
+            av = 2.0 * E[i, j] * W[i + 1, j] / (E[i, j] + W[i + 1, j] + rnd)
+            E[i, j] = av; W[i + 1, j] = av
+    V = lambda i, j: vs[i - 1, j - 1]
+    for i in range(1, nx + 1):
+        for j in range(1, ny + 1):
+            if V(i, j) > 1.0 - epsi:
+                vs[i - 1, j - 1] = 1.0
+                W[i, j] = E[i, j] = N[i, j] = S[i, j] = 0.0
+                E[i - 1, j] = 0.0; N[i, j - 1] = 0.0; W[i + 1, j] = 0.0; S[i, j + 1] = 0.0
+            if (W[i, j] + E[i, j] < rnd or S[i, j] + N[i, j] < rnd) and V(i, j) < 1.0 - epsi:
+                vs[i - 1, j - 1] = 1.0
+                W[i, j] = E[i, j] = N[i, j] = S[i, j] = 0.0
+                E[i - 1, j] = 0.0; N[i, j - 1] = 0.0; W[i + 1, j] = 0.0; S[i, j + 1] = 0.0
+    for i in range(1, nx + 1):
+        for j in range(1, ny + 1):
+            if abs(V(i, j) - 1.0) < rnd:
+                if W[i, j] == 0.0 or E[i, j] == 0.0:
+                    WL[i - 1, j - 1] = dyP[i - 1, j - 1]
+                if N[i, j] == 0.0 or S[i, j] == 0.0:
+                    WL[i - 1, j - 1] = dxP[i - 1, j - 1]
+    if icorprob:
+        for i in range(1, nx + 1):
+            for j in range(1, ny - 3):
+                if -epsi < V(i, j) < epsi:
+                    if 0.6 - epsi < V(i, j + 1) < 0.6 + epsi and 0.6 - epsi < V(i, j + 2) < 0.6 + epsi:
+                        N[i, j] = 0.4; S[i, j + 1] = 0.4
+                        WL[i - 1, j - 1] = 0.6 * dxP[i - 1, j - 1]
+                        ny_s[i - 1, j - 1] = -1.0; nx_s[i - 1, j - 1] = 0.0
+                    if 1.0 - epsi < V(i, j + 1) < 1.0 + epsi:
+                        WL[i - 1, j - 1] = dxP[i - 1, j - 1]
+                        ny_s[i - 1, j - 1] = -1.0; nx_s[i - 1, j - 1] = 0.0
+    vsu = np.where(np.asarray(vofS_u_in) > 1.0 - epsi, 1.0, vofS_u_in)
+    vsv = np.where(np.asarray(vofS_v_in) > 1.0 - epsi, 1.0, vofS_v_in)
+    mu = np.zeros((nx, ny), dtype=np.int32); mv = np.zeros((nx, ny), dtype=np.int32)
+    for i in range(1, nx + 1):
+        for j in range(1, ny + 1):
+            if epsi <= vsu[i - 1, j - 1] < 1.0 - epsi:
+                if i < nx:
+                    if V(i, j) >= 1.0 - epsi or V(i + 1, j) >= 1.0 - epsi or E[i, j] < epsiF:
+                        mu[i - 1, j - 1] = 1; E[i, j] = 0.0; W[i + 1, j] = 0.0
+                elif V(i, j) >= 1.0 - epsi:
+                    mu[i - 1, j - 1] = 1
+            if epsi <= vsv[i - 1, j - 1] < 1.0 - epsi:
+                if j < ny:
+                    if V(i, j) >= 1.0 - epsi or V(i, j + 1) >= 1.0 - epsi or N[i, j] < epsiF:
+                        mv[i - 1, j - 1] = 1; N[i, j] = 0.0; S[i, j + 1] = 0.0
+                elif V(i, j) >= 1.0 - epsi:
+                    mv[i - 1, j - 1] = 1
+    pp = -np.ones((nx + 2, ny + 2), dtype=np.int32)
+    pu = -np.ones_like(pp); pv = -np.ones_like(pp)
+    c = 0
+    for i in range(1, nx + 1):
+        for j in range(1, ny + 1):
+            if V(i, j) < 1.0 - epsi:
+                pp[i, j] = c; c += 1
+    c = 0
+    for i in range(1, nx):
+        for j in range(1, ny + 1):
+            if vsu[i - 1, j - 1] < 1.0 - epsi:
+                pu[i, j] = c; c += 1
+    c = 0
+    for i in range(1, nx + 1):
+        for j in range(1, ny):
+            if vsv[i - 1, j - 1] < 1.0 - epsi:
+                pv[i, j] = c; c += 1
+    return {"aE": E, "aW": W, "aN": N, "aS": S, "WlLh": WL, "vofS": vs, "nyS": ny_s, "nxS": nx_s,
+            "posnu_p": pp, "posnu_u": pu, "posnu_v": pv, "moex_u": mu, "moex_v": mv,
+            "vofS_u": vsu, "vofS_v": vsv}

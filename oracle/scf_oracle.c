@@ -1,0 +1,804 @@
+/*
+ * scf_oracle.c -- CPU restatement of the SIMCOFlow pressure-projection path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle that the CUDA path is
+ * checked against.  Only tests/, __graft_entry__.smoke() and the CPU
+ * baseline leg of bench.py load it.  Nothing in the simcoflow_gb300 package
+ * links or calls it, and the product path never falls back to it.
+ *
+ * Parity status: UNPINNED.  The reference (Fortran 90 + HYPRE + MPI) cannot
+ * be compiled here (no Fortran compiler, no MPI, no HYPRE) and ships no golden
+ * vectors or tests.  The restatement is pinned instead against the
+ * reference's own built-in identities (the per-row |A p - b| <= 1e-10 check of
+ * src/ProjectionP_Mod.f90:70-93 and the mass residual of
+ * src/ComputePUV_Mod.f90:184-216) and against analytic known-answer cases.
+ *
+ * Every routine follows the reference loop by loop, in the same loop order
+ * and with the same floating-point operation order (compile with
+ * -ffp-contract=off so that no multiply-add is fused; the reference is built
+ * by mpif77 without FMA-generating flags).
+ *
+ * Array conventions are the reference's (Fortran, column-major, i fastest):
+ *   F1(a,i,j)  arrays dimensioned (1:nx,1:ny)
+ *   F0(a,i,j)  arrays dimensioned (0:nx+1,0:ny+1)
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define F1(a, i, j) (a)[(size_t)((i)-1) + (size_t)((j)-1) * (size_t)nx]
+#define F0(a, i, j) (a)[(size_t)(i) + (size_t)(j) * (size_t)(nx + 2)]
+#define PC(f, i, j) pocoef[(size_t)((i)-1) + (size_t)((j)-1) * (size_t)nx + (size_t)((f)-1) * (size_t)nx * (size_t)ny]
+#define MT(f, i, j) matr[(size_t)((i)-1) + (size_t)((j)-1) * (size_t)nx + (size_t)((f)-1) * (size_t)nx * (size_t)ny]
+
+static const double EPSI = 1.0e-3; /* src/StateVariables.f90:26 */
+
+/* wet / dry predicates, src/ProjectionP_Mod.f90:409-410 and :493-494 */
+static inline int is_wet(double vof, double phi, double vofS) {
+    return (vof >= 0.5 && vofS < EPSI) || (phi < 0.0 && vofS >= EPSI);
+}
+static inline int is_dry(double vof, double phi, double vofS) {
+    return (vof < 0.5 && vofS < EPSI) || (phi >= 0.0 && vofS >= EPSI);
+}
+
+/*
+ * ComputePossionMatrixCoefficient, src/ProjectionP_Mod.f90:395-580.
+ * pocoef is (nx,ny,4) with faces S=1, W=2, E=3, N=4 (comment at :45).
+ * literal=1 keeps the reference's loop-carried BetaW/BetaD variables,
+ * including the dry-cell / dry-south branch (:504-508) that assigns BetaW
+ * but divides by the BetaD left over from the previous cell; literal=0
+ * uses the intended rule (BetaD = BetaP in that branch).
+ */
+void oracle_pocoef(int nx, int ny, int literal, const double *vof, const double *phi,
+                   const double *vofS, const double *dxP, const double *dyP,
+                   const double *dxU, const double *dyV, const double *DpU,
+                   const double *DpV, double betaP, double betaM, double *pocoef) {
+    const double tol = 1.0e-24;
+    double BetaW = NAN, BetaD = NAN, Lamda;
+    for (size_t k = 0; k < (size_t)nx * ny * 4; ++k) pocoef[k] = 0.0;
+    for (int i = 1; i <= nx; ++i) {
+        for (int j = 1; j <= ny; ++j) {
+#define WET(ii, jj) is_wet(F1(vof, ii, jj), F1(phi, ii, jj), F1(vofS, ii, jj))
+#define DRY(ii, jj) is_dry(F1(vof, ii, jj), F1(phi, ii, jj), F1(vofS, ii, jj))
+#define LAM(ii, jj) (fabs(F1(phi, i, j)) / ((fabs(F1(phi, i, j)) + fabs(F1(phi, ii, jj))) + tol))
+            if (WET(i, j)) {
+                /* south */
+                if (j > 1) {
+                    if (DRY(i, j - 1)) {
+                        Lamda = LAM(i, j - 1);
+                        BetaW = Lamda * betaM + (1.0 - Lamda) * betaP;
+                        PC(1, i, j) = F0(DpV, i, j - 1) * F1(dxP, i, j) / F1(dyV, i, j - 1) * betaP * betaM / BetaW;
+                    } else if (WET(i, j - 1)) {
+                        BetaW = betaM;
+                        PC(1, i, j) = F0(DpV, i, j - 1) * F1(dxP, i, j) / F1(dyV, i, j - 1) * betaP * betaM / BetaW;
+                    }
+                } else {
+                    BetaW = betaM;
+                    PC(1, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaW;
+                }
+                /* west */
+                if (i > 1) {
+                    if (DRY(i - 1, j)) {
+                        Lamda = LAM(i - 1, j);
+                        BetaW = Lamda * betaM + (1.0 - Lamda) * betaP;
+                        PC(2, i, j) = F0(DpU, i - 1, j) * F1(dyP, i, j) / F1(dxU, i - 1, j) * betaP * betaM / BetaW;
+                    } else if (WET(i - 1, j)) {
+                        BetaW = betaM;
+                        PC(2, i, j) = F0(DpU, i - 1, j) * F1(dyP, i, j) / F1(dxU, i - 1, j) * betaP * betaM / BetaW;
+                    }
+                } else {
+                    BetaW = betaM;
+                    PC(2, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaW;
+                }
+                /* east */
+                if (i < nx) {
+                    if (DRY(i + 1, j)) {
+                        Lamda = LAM(i + 1, j);
+                        BetaW = Lamda * betaM + (1.0 - Lamda) * betaP;
+                        PC(3, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaW;
+                    } else if (WET(i + 1, j)) {
+                        BetaW = betaM;
+                        PC(3, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaW;
+                    }
+                } else {
+                    BetaW = betaM;
+                    PC(3, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaW;
+                }
+                /* north */
+                if (j < ny) {
+                    if (DRY(i, j + 1)) {
+                        Lamda = LAM(i, j + 1);
+                        BetaW = Lamda * betaM + (1.0 - Lamda) * betaP;
+                        PC(4, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaW;
+                    } else if (WET(i, j + 1)) {
+                        BetaW = betaM;
+                        PC(4, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaW;
+                    }
+                } else {
+                    BetaW = betaM;
+                    PC(4, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaW;
+                }
+            } else if (DRY(i, j)) {
+                /* south */
+                if (j > 1) {
+                    if (WET(i, j - 1)) {
+                        Lamda = LAM(i, j - 1);
+                        BetaD = Lamda * betaP + (1.0 - Lamda) * betaM;
+                        PC(1, i, j) = F0(DpV, i, j - 1) * F1(dxP, i, j) / F1(dyV, i, j - 1) * betaP * betaM / BetaD;
+                    } else if (DRY(i, j - 1)) {
+                        if (literal) BetaW = betaP; /* :506 assigns BetaW, :507 divides by BetaD */
+                        else BetaD = betaP;
+                        PC(1, i, j) = F0(DpV, i, j - 1) * F1(dxP, i, j) / F1(dyV, i, j - 1) * betaP * betaM / BetaD;
+                    }
+                } else {
+                    BetaD = betaP;
+                    PC(1, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaD;
+                }
+                /* west */
+                if (i > 1) {
+                    if (WET(i - 1, j)) {
+                        Lamda = LAM(i - 1, j);
+                        BetaD = Lamda * betaP + (1.0 - Lamda) * betaM;
+                        PC(2, i, j) = F0(DpU, i - 1, j) * F1(dyP, i, j) / F1(dxU, i - 1, j) * betaP * betaM / BetaD;
+                    } else if (DRY(i - 1, j)) {
+                        BetaD = betaP;
+                        PC(2, i, j) = F0(DpU, i - 1, j) * F1(dyP, i, j) / F1(dxU, i - 1, j) * betaP * betaM / BetaD;
+                    }
+                } else {
+                    BetaD = betaP;
+                    PC(2, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaD;
+                }
+                /* east */
+                if (i < nx) {
+                    if (WET(i + 1, j)) {
+                        Lamda = LAM(i + 1, j);
+                        BetaD = Lamda * betaP + (1.0 - Lamda) * betaM;
+                        PC(3, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaD;
+                    } else if (DRY(i + 1, j)) {
+                        BetaD = betaP;
+                        PC(3, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaD;
+                    }
+                } else {
+                    BetaD = betaP;
+                    PC(3, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaD;
+                }
+                /* north */
+                if (j < ny) {
+                    if (WET(i, j + 1)) {
+                        Lamda = LAM(i, j + 1);
+                        BetaD = Lamda * betaP + (1.0 - Lamda) * betaM;
+                        PC(4, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaD;
+                    } else if (DRY(i, j + 1)) {
+                        BetaD = betaP;
+                        PC(4, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaD;
+                    }
+                } else {
+                    BetaD = betaP;
+                    PC(4, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaD;
+                }
+            }
+#undef WET
+#undef DRY
+#undef LAM
+        }
+    }
+    (void)BetaW;
+}
+
+/*
+ * SetPoissonMatrix, src/ProjectionP_Mod.f90:137-273.
+ * Fills matr(nx,ny,5) (S,W,diag,E,N; zero where the reference leaves no
+ * entry) and the CSR matrix in the reference's row numbering (Posnu) with
+ * the reference's column order within a row (S, W, diag, E, N).
+ * rowptr has n_rows+1 entries, cols/vals room for 5*n_rows.
+ * Returns the number of rows (ExtCell+1).
+ */
+int oracle_matrix(int nx, int ny, const double *pocoef, const double *aE, const double *aW,
+                  const double *aN, const double *aS, const int32_t *posnu, int wb, int eb,
+                  int sb, int nbc, double *matr, int32_t *rowptr, int32_t *cols, double *vals) {
+    const double tol = 1.0e-24;
+    int nrows = 0;
+    for (int i = 1; i <= nx; ++i)
+        for (int j = 1; j <= ny; ++j)
+            if (F0(posnu, i, j) != -1) nrows++;
+    for (size_t k = 0; k < (size_t)nx * ny * 5; ++k) matr[k] = 0.0;
+    /* rows are numbered with j fastest (src/Cutcell_Mod.f90:347-351), which is
+       also the visiting order here, so CSR rows are written in order */
+    int nnz_total = 0;
+    rowptr[0] = 0;
+    for (int i = 1; i <= nx; ++i) {
+        for (int j = 1; j <= ny; ++j) {
+            int row = F0(posnu, i, j);
+            if (row == -1) continue;
+            double values[5];
+            int cc[5];
+            int nnz = 0;
+            if (j > 1 && F0(posnu, i, j - 1) != -1) {
+                cc[nnz] = F0(posnu, i, j - 1);
+                values[nnz] = -PC(1, i, j) * F0(aS, i, j);
+                MT(1, i, j) = values[nnz];
+                nnz++;
+            }
+            if (i > 1 && F0(posnu, i - 1, j) != -1) {
+                cc[nnz] = F0(posnu, i - 1, j);
+                values[nnz] = -PC(2, i, j) * F0(aW, i, j);
+                MT(2, i, j) = values[nnz];
+                nnz++;
+            }
+            cc[nnz] = row;
+            double d = PC(1, i, j) * F0(aS, i, j) + PC(2, i, j) * F0(aW, i, j) +
+                       PC(3, i, j) * F0(aE, i, j) + PC(4, i, j) * F0(aN, i, j);
+            if (sb == 1 && j == 1) d = d - PC(1, i, j) * F0(aS, i, j);
+            if (wb == 1 && i == 1) d = d - PC(2, i, j) * F0(aW, i, j);
+            if (eb == 1 && i == nx) d = d - PC(3, i, j) * F0(aE, i, j);
+            if (nbc == 1 && j == ny) d = d - PC(4, i, j) * F0(aN, i, j);
+            d = d + copysign(1.0, d) * tol;
+            values[nnz] = d;
+            MT(3, i, j) = d;
+            nnz++;
+            if (i < nx && F0(posnu, i + 1, j) != -1) {
+                cc[nnz] = F0(posnu, i + 1, j);
+                values[nnz] = -PC(3, i, j) * F0(aE, i, j);
+                MT(4, i, j) = values[nnz];
+                nnz++;
+            }
+            if (j < ny && F0(posnu, i, j + 1) != -1) {
+                cc[nnz] = F0(posnu, i, j + 1);
+                values[nnz] = -PC(4, i, j) * F0(aN, i, j);
+                MT(5, i, j) = values[nnz];
+                nnz++;
+            }
+            for (int k = 0; k < nnz; ++k) {
+                cols[nnz_total + k] = cc[k];
+                vals[nnz_total + k] = values[k];
+            }
+            nnz_total += nnz;
+            rowptr[row + 1] = nnz_total;
+        }
+    }
+    return nrows;
+}
+
+/*
+ * SetPoissonVectors, src/ProjectionP_Mod.f90:275-354 (formula :313-317).
+ * u, v are the predicted velocities (0:nx+1,0:ny+1); rhm is (nx,ny) and is
+ * zero where the cell has no row; rhs is in Posnu order.
+ */
+void oracle_rhs(int nx, int ny, const double *u, const double *v, const double *aE,
+                const double *aW, const double *aN, const double *aS, const double *dxP,
+                const double *dyP, const double *nyS, const double *WlLh, const int32_t *posnu,
+                double vb, double *rhm, double *rhs) {
+    for (int i = 1; i <= nx; ++i) {
+        for (int j = 1; j <= ny; ++j) {
+            int ictr = F0(posnu, i, j);
+            F1(rhm, i, j) = 0.0;
+            if (ictr == -1) continue;
+            double dx = F1(dxP, i, j), dy = F1(dyP, i, j);
+            double r = -((F0(u, i, j) * F0(aE, i, j) - F0(u, i - 1, j) * F0(aW, i, j)) * dy) -
+                       (F0(v, i, j) * F0(aN, i, j) - F0(v, i, j - 1) * F0(aS, i, j)) * dx +
+                       vb * F1(nyS, i, j) * F1(WlLh, i, j);
+            if (rhs) rhs[ictr] = r;
+            F1(rhm, i, j) = r;
+        }
+    }
+}
+
+/*
+ * DeltaPressureGetValues + DeltaPressureBoundaryCondition,
+ * src/ProjectionP_Mod.f90:356-393 and :582-595.  x is in Posnu order;
+ * Pp is (0:nx+1,0:ny+1) and its four corners stay zero as in UpdatePUV
+ * (src/ComputePUV_Mod.f90:50).
+ */
+void oracle_scatter(int nx, int ny, const int32_t *posnu, const double *x, int wb, int eb,
+                    int sb, int nbc, double *Pp) {
+    for (size_t k = 0; k < (size_t)(nx + 2) * (ny + 2); ++k) Pp[k] = 0.0;
+    for (int i = 1; i <= nx; ++i)
+        for (int j = 1; j <= ny; ++j) {
+            int c = F0(posnu, i, j);
+            F0(Pp, i, j) = (c != -1) ? x[c] : 0.0;
+        }
+    for (int i = 1; i <= nx; ++i) {
+        F0(Pp, i, 0) = (double)sb * F0(Pp, i, 1);
+        F0(Pp, i, ny + 1) = (double)nbc * F0(Pp, i, ny);
+    }
+    for (int j = 1; j <= ny; ++j) {
+        F0(Pp, 0, j) = (double)wb * F0(Pp, 1, j);
+        F0(Pp, nx + 1, j) = (double)eb * F0(Pp, nx, j);
+    }
+}
+
+/*
+ * Velocity correction, pressure copy, top-row continuity, mass residual and
+ * solid-cell zeroing: UpdatePUV src/ComputePUV_Mod.f90:59-100 (u), :111-152
+ * (v), :163-169 (p), :177-182 (top v), :184-217 (mres) and
+ * VariablesInternalCellCondition :227-245.
+ * u, v, p are TVar fields (0:nx+1,0:ny+1): in = old values, out = new.
+ * ustar, vstar are Pred%u, Pred%v; mres is (nx,ny).
+ */
+void oracle_correct(int nx, int ny, const double *Pp, const double *ustar, const double *vstar,
+                    const double *vof, const double *phi, const double *vofS, const double *nyS,
+                    const double *WlLh, const double *aE, const double *aW, const double *aN,
+                    const double *aS, const int32_t *posnu_p, const int32_t *posnu_u,
+                    const int32_t *moex_u, const double *vofS_u, const int32_t *posnu_v,
+                    const int32_t *moex_v, const double *vofS_v, const double *dxP,
+                    const double *dyP, const double *dxU, const double *dyV, const double *DpU,
+                    const double *DpV, double betaP, double betaM, double vb, double *u,
+                    double *v, double *p, double *mres) {
+    const double tol = 1.0e-24;
+#define WET(ii, jj) is_wet(F1(vof, ii, jj), F1(phi, ii, jj), F1(vofS, ii, jj))
+#define DRY(ii, jj) is_dry(F1(vof, ii, jj), F1(phi, ii, jj), F1(vofS, ii, jj))
+    for (int i = 1; i <= nx - 1; ++i) {
+        for (int j = 1; j <= ny; ++j) {
+            if (F0(posnu_u, i, j) != -1 && F1(moex_u, i, j) != 1) {
+                double BetaW, Lamda, G;
+                int set = 0;
+                if (WET(i, j)) {
+                    if (DRY(i + 1, j)) {
+                        Lamda = fabs(F1(phi, i, j)) / ((fabs(F1(phi, i, j)) + fabs(F1(phi, i + 1, j))) + tol);
+                        BetaW = Lamda * betaM + (1.0 - Lamda) * betaP;
+                        set = 1;
+                    } else if (WET(i + 1, j)) {
+                        BetaW = betaM;
+                        set = 1;
+                    }
+                } else if (DRY(i, j)) {
+                    if (WET(i + 1, j)) {
+                        Lamda = fabs(F1(phi, i, j)) / ((fabs(F1(phi, i, j)) + fabs(F1(phi, i + 1, j))) + tol);
+                        BetaW = Lamda * betaP + (1.0 - Lamda) * betaM;
+                        set = 1;
+                    } else if (DRY(i + 1, j)) {
+                        BetaW = betaP;
+                        set = 1;
+                    }
+                }
+                if (set) {
+                    G = (F0(Pp, i + 1, j) - F0(Pp, i, j)) * betaM * betaP / BetaW * F0(DpU, i, j) / F1(dxU, i, j);
+                    F0(u, i, j) = F0(ustar, i, j) - G;
+                }
+            }
+        }
+    }
+    for (int i = 1; i <= nx; ++i) {
+        for (int j = 1; j <= ny - 1; ++j) {
+            if (F0(posnu_v, i, j) != -1 && F1(moex_v, i, j) != 1) {
+                double BetaW, Lamda, G;
+                int set = 0;
+                if (WET(i, j)) {
+                    if (DRY(i, j + 1)) {
+                        Lamda = fabs(F1(phi, i, j)) / ((fabs(F1(phi, i, j)) + fabs(F1(phi, i, j + 1))) + tol);
+                        BetaW = Lamda * betaM + (1.0 - Lamda) * betaP;
+                        set = 1;
+                    } else if (WET(i, j + 1)) {
+                        BetaW = betaM;
+                        set = 1;
+                    }
+                } else if (DRY(i, j)) {
+                    if (WET(i, j + 1)) {
+                        Lamda = fabs(F1(phi, i, j)) / ((fabs(F1(phi, i, j)) + fabs(F1(phi, i, j + 1))) + tol);
+                        BetaW = Lamda * betaP + (1.0 - Lamda) * betaM;
+                        set = 1;
+                    } else if (DRY(i, j + 1)) {
+                        BetaW = betaP;
+                        set = 1;
+                    }
+                }
+                if (set) {
+                    G = (F0(Pp, i, j + 1) - F0(Pp, i, j)) * betaM * betaP / BetaW * F0(DpV, i, j) / F1(dyV, i, j);
+                    F0(v, i, j) = F0(vstar, i, j) - G;
+                }
+            }
+        }
+    }
+#undef WET
+#undef DRY
+    for (int i = 1; i <= nx; ++i)
+        for (int j = 1; j <= ny; ++j)
+            if (F0(posnu_p, i, j) != -1) F0(p, i, j) = F0(Pp, i, j);
+    for (int i = 1; i <= nx; ++i) {
+        int j = ny;
+        F0(v, i, j) = ((-(F0(u, i, j) * F0(aE, i, j)) + F0(u, i - 1, j) * F0(aW, i, j)) * F1(dyP, i, j) +
+                       F0(v, i, j - 1) * F0(aS, i, j) * F1(dxP, i, j)) /
+                      F1(dxP, i, j) / F0(aN, i, j);
+    }
+    for (int i = 1; i <= nx; ++i) {
+        for (int j = 1; j <= ny; ++j) {
+            F1(mres, i, j) = (F0(u, i, j) * F0(aE, i, j) - F0(u, i - 1, j) * F0(aW, i, j)) * F1(dyP, i, j) +
+                             (F0(v, i, j) * F0(aN, i, j) - F0(v, i, j - 1) * F0(aS, i, j)) * F1(dxP, i, j) -
+                             vb * F1(nyS, i, j) * F1(WlLh, i, j);
+            if (F1(vofS, i, j) > 1.0 - EPSI) F1(mres, i, j) = 0.0;
+        }
+    }
+    for (int i = 1; i <= nx; ++i) {
+        for (int j = 1; j <= ny; ++j) {
+            if (F1(vofS, i, j) > 1.0 - EPSI) F0(p, i, j) = 0.0;
+            if (F1(vofS_u, i, j) >= 1.0 - EPSI) F0(u, i, j) = 0.0;
+            if (F1(vofS_v, i, j) >= 1.0 - EPSI) F0(v, i, j) = 0.0;
+        }
+    }
+}
+
+/* The per-row residual self-check of src/ProjectionP_Mod.f90:70-93:
+ * returns max |A Pp - rhm| over rows with Posnu /= -1. */
+double oracle_row_residual(int nx, int ny, const double *matr, const double *Pp,
+                           const double *rhm, const int32_t *posnu) {
+    double worst = 0.0;
+    for (int i = 1; i <= nx; ++i)
+        for (int j = 1; j <= ny; ++j) {
+            double resi = 0.0;
+            if (j > 1) resi = resi + MT(1, i, j) * F0(Pp, i, j - 1);
+            if (i > 1) resi = resi + MT(2, i, j) * F0(Pp, i - 1, j);
+            resi = resi + MT(3, i, j) * F0(Pp, i, j);
+            if (i < nx) resi = resi + MT(4, i, j) * F0(Pp, i + 1, j);
+            if (j < ny) resi = resi + MT(5, i, j) * F0(Pp, i, j + 1);
+            double d = fabs(resi - F1(rhm, i, j));
+            if (F0(posnu, i, j) != -1 && d > worst) worst = d;
+        }
+    return worst;
+}
+
+/* ------------------------------------------------------------------------
+ * CPU FP64 MG-PCG: the same algorithm as the CUDA path, restated on the CPU.
+ * Used as the FP64 oracle solve at sizes the direct solver cannot reach and
+ * as the timed CPU baseline.  Symmetric 5-point storage per level:
+ *   cE(i,j): coupling of (i,j) and (i+1,j); cN(i,j): of (i,j) and (i,j+1);
+ *   dg(i,j): diagonal; a cell without an unknown has dg = -1 and no couplings.
+ * The fine level is taken from matr: cE = -matr(.,.,4), cN = -matr(.,.,5),
+ * dg = matr(.,.,3).  Coarse levels are the Galerkin product P^T A P with
+ * piecewise-constant 2x2 aggregation, computed as summed couplings plus the
+ * summed diagonal excess (dg - sum of couplings, clamped at 0).
+ * V-cycle: x=0; pre-smooth red then black; residual; restrict (sum);
+ * recurse; x += omega * P e (not into cells without an unknown); post-smooth
+ * black then red.  Coarsest level: dense Cholesky.
+ * Arrays are 0-based, x fastest: a[ix + iy*nx].
+ * ------------------------------------------------------------------------ */
+typedef struct {
+    int nx, ny;
+    double *cE, *cN, *dg, *ex;
+    double *x, *b, *r;
+} olevel;
+
+typedef struct {
+    int nlev;
+    olevel lev[32];
+    double omega;
+    int npre, npost;
+    int nc;          /* coarsest unknowns */
+    double *chol;    /* nc x nc lower Cholesky factor */
+    int *cmap;       /* coarsest cell -> dense index or -1 */
+} omg;
+
+static double *dalloc(size_t n) { return (double *)calloc(n ? n : 1, sizeof(double)); }
+
+static void level_alloc(olevel *L, int nx, int ny) {
+    size_t n = (size_t)nx * ny;
+    L->nx = nx; L->ny = ny;
+    L->cE = dalloc(n); L->cN = dalloc(n); L->dg = dalloc(n); L->ex = dalloc(n);
+    L->x = dalloc(n); L->b = dalloc(n); L->r = dalloc(n);
+}
+static void level_free(olevel *L) {
+    free(L->cE); free(L->cN); free(L->dg); free(L->ex); free(L->x); free(L->b); free(L->r);
+}
+
+static void compute_excess(olevel *L) {
+    int nx = L->nx, ny = L->ny;
+#pragma omp parallel for schedule(static)
+    for (int iy = 0; iy < ny; ++iy)
+        for (int ix = 0; ix < nx; ++ix) {
+            size_t k = (size_t)iy * nx + ix;
+            if (L->dg[k] < 0.0) { L->ex[k] = 0.0; continue; }
+            double s = L->cE[k] + (ix > 0 ? L->cE[k - 1] : 0.0) + L->cN[k] + (iy > 0 ? L->cN[k - nx] : 0.0);
+            double e = L->dg[k] - s;
+            L->ex[k] = e > 0.0 ? e : 0.0;
+        }
+}
+
+static void coarsen(const olevel *F, olevel *C) {
+    int nxf = F->nx, nyf = F->ny, nxc = (nxf + 1) / 2, nyc = (nyf + 1) / 2;
+    level_alloc(C, nxc, nyc);
+#pragma omp parallel for schedule(static)
+    for (int J = 0; J < nyc; ++J)
+        for (int I = 0; I < nxc; ++I) {
+            double ce = 0.0, cn = 0.0, ex = 0.0;
+            int active = 0;
+            for (int dj = 0; dj < 2; ++dj)
+                for (int di = 0; di < 2; ++di) {
+                    int ix = 2 * I + di, iy = 2 * J + dj;
+                    if (ix >= nxf || iy >= nyf) continue;
+                    size_t k = (size_t)iy * nxf + ix;
+                    if (F->dg[k] >= 0.0) active = 1;
+                    ex += F->ex[k];
+                    if (di == 1) ce += F->cE[k];
+                    if (dj == 1) cn += F->cN[k];
+                }
+            size_t kc = (size_t)J * nxc + I;
+            C->cE[kc] = ce;
+            C->cN[kc] = cn;
+            C->ex[kc] = active ? ex : 0.0;
+            C->dg[kc] = active ? 0.0 : -1.0;
+        }
+#pragma omp parallel for schedule(static)
+    for (int J = 0; J < nyc; ++J)
+        for (int I = 0; I < nxc; ++I) {
+            size_t kc = (size_t)J * nxc + I;
+            if (C->dg[kc] < 0.0) continue;
+            double s = C->cE[kc] + (I > 0 ? C->cE[kc - 1] : 0.0) + C->cN[kc] + (J > 0 ? C->cN[kc - nxc] : 0.0);
+            C->dg[kc] = s + C->ex[kc];
+            if (!(C->dg[kc] > 0.0)) C->dg[kc] = -1.0;
+        }
+}
+
+static void coarse_factor(omg *M) {
+    olevel *L = &M->lev[M->nlev - 1];
+    int nx = L->nx, ny = L->ny, n = 0;
+    M->cmap = (int *)malloc(sizeof(int) * (size_t)nx * ny);
+    for (int k = 0; k < nx * ny; ++k) M->cmap[k] = L->dg[k] >= 0.0 ? n++ : -1;
+    M->nc = n;
+    M->chol = dalloc((size_t)n * n);
+    double *A = M->chol;
+    for (int iy = 0; iy < ny; ++iy)
+        for (int ix = 0; ix < nx; ++ix) {
+            int k = iy * nx + ix, r = M->cmap[k];
+            if (r < 0) continue;
+            A[(size_t)r * n + r] = L->dg[k];
+            if (ix + 1 < nx && M->cmap[k + 1] >= 0) {
+                int c = M->cmap[k + 1];
+                A[(size_t)r * n + c] = -L->cE[k]; A[(size_t)c * n + r] = -L->cE[k];
+            }
+            if (iy + 1 < ny && M->cmap[k + nx] >= 0) {
+                int c = M->cmap[k + nx];
+                A[(size_t)r * n + c] = -L->cN[k]; A[(size_t)c * n + r] = -L->cN[k];
+            }
+        }
+    /* in-place lower Cholesky */
+    for (int j = 0; j < n; ++j) {
+        double d = A[(size_t)j * n + j];
+        for (int k = 0; k < j; ++k) d -= A[(size_t)j * n + k] * A[(size_t)j * n + k];
+        d = d > 0.0 ? sqrt(d) : 1e-300;
+        A[(size_t)j * n + j] = d;
+        for (int i = j + 1; i < n; ++i) {
+            double s = A[(size_t)i * n + j];
+            for (int k = 0; k < j; ++k) s -= A[(size_t)i * n + k] * A[(size_t)j * n + k];
+            A[(size_t)i * n + j] = s / d;
+        }
+    }
+}
+
+static void coarse_solve(omg *M) {
+    olevel *L = &M->lev[M->nlev - 1];
+    int n = M->nc, N = L->nx * L->ny;
+    double *y = dalloc((size_t)n);
+    for (int k = 0; k < N; ++k) if (M->cmap[k] >= 0) y[M->cmap[k]] = L->b[k];
+    const double *A = M->chol;
+    for (int i = 0; i < n; ++i) {
+        double s = y[i];
+        for (int k = 0; k < i; ++k) s -= A[(size_t)i * n + k] * y[k];
+        y[i] = s / A[(size_t)i * n + i];
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        double s = y[i];
+        for (int k = i + 1; k < n; ++k) s -= A[(size_t)k * n + i] * y[k];
+        y[i] = s / A[(size_t)i * n + i];
+    }
+    for (int k = 0; k < N; ++k) L->x[k] = M->cmap[k] >= 0 ? y[M->cmap[k]] : 0.0;
+    free(y);
+}
+
+/* one red-black half sweep: color 0 updates cells with (ix+iy) even */
+static void rbgs_half(olevel *L, int color) {
+    int nx = L->nx, ny = L->ny;
+    const double *cE = L->cE, *cN = L->cN, *dg = L->dg, *b = L->b;
+    double *x = L->x;
+#pragma omp parallel for schedule(static)
+    for (int iy = 0; iy < ny; ++iy) {
+        int ix0 = (iy + color) & 1;
+        for (int ix = ix0; ix < nx; ix += 2) {
+            size_t k = (size_t)iy * nx + ix;
+            double s = b[k];
+            if (ix + 1 < nx) s = s + cE[k] * x[k + 1];
+            if (ix > 0) s = s + cE[k - 1] * x[k - 1];
+            if (iy + 1 < ny) s = s + cN[k] * x[k + nx];
+            if (iy > 0) s = s + cN[k - nx] * x[k - nx];
+            x[k] = dg[k] > 0.0 ? s / dg[k] : 0.0;
+        }
+    }
+}
+
+static void residual(olevel *L) {
+    int nx = L->nx, ny = L->ny;
+#pragma omp parallel for schedule(static)
+    for (int iy = 0; iy < ny; ++iy)
+        for (int ix = 0; ix < nx; ++ix) {
+            size_t k = (size_t)iy * nx + ix;
+            if (L->dg[k] < 0.0) { L->r[k] = 0.0; continue; }
+            double s = L->b[k] - L->dg[k] * L->x[k];
+            if (ix + 1 < nx) s = s + L->cE[k] * L->x[k + 1];
+            if (ix > 0) s = s + L->cE[k - 1] * L->x[k - 1];
+            if (iy + 1 < ny) s = s + L->cN[k] * L->x[k + nx];
+            if (iy > 0) s = s + L->cN[k - nx] * L->x[k - nx];
+            L->r[k] = s;
+        }
+}
+
+static void restrict_sum(const olevel *F, olevel *C) {
+    int nxf = F->nx, nyf = F->ny, nxc = C->nx, nyc = C->ny;
+#pragma omp parallel for schedule(static)
+    for (int J = 0; J < nyc; ++J)
+        for (int I = 0; I < nxc; ++I) {
+            double s = 0.0;
+            for (int dj = 0; dj < 2; ++dj)
+                for (int di = 0; di < 2; ++di) {
+                    int ix = 2 * I + di, iy = 2 * J + dj;
+                    if (ix < nxf && iy < nyf) s = s + F->r[(size_t)iy * nxf + ix];
+                }
+            C->b[(size_t)J * nxc + I] = s;
+        }
+}
+
+static void prolong_add(olevel *F, const olevel *C, double omega) {
+    int nxf = F->nx, nyf = F->ny, nxc = C->nx;
+#pragma omp parallel for schedule(static)
+    for (int iy = 0; iy < nyf; ++iy)
+        for (int ix = 0; ix < nxf; ++ix) {
+            size_t k = (size_t)iy * nxf + ix;
+            if (F->dg[k] < 0.0) continue;
+            F->x[k] = F->x[k] + omega * C->x[(size_t)(iy / 2) * nxc + (ix / 2)];
+        }
+}
+
+static void vcycle(omg *M, int l) {
+    olevel *L = &M->lev[l];
+    size_t n = (size_t)L->nx * L->ny;
+    if (l == M->nlev - 1) { coarse_solve(M); return; }
+    memset(L->x, 0, n * sizeof(double));
+    for (int s = 0; s < M->npre; ++s) { rbgs_half(L, 0); rbgs_half(L, 1); }
+    residual(L);
+    restrict_sum(L, &M->lev[l + 1]);
+    vcycle(M, l + 1);
+    prolong_add(L, &M->lev[l + 1], M->omega);
+    for (int s = 0; s < M->npost; ++s) { rbgs_half(L, 1); rbgs_half(L, 0); }
+}
+
+static double dot(const double *a, const double *b, size_t n) {
+    double s = 0.0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+    for (size_t k = 0; k < n; ++k) s += a[k] * b[k];
+    return s;
+}
+
+static void apply_A(const olevel *L, const double *p, double *q) {
+    int nx = L->nx, ny = L->ny;
+#pragma omp parallel for schedule(static)
+    for (int iy = 0; iy < ny; ++iy)
+        for (int ix = 0; ix < nx; ++ix) {
+            size_t k = (size_t)iy * nx + ix;
+            double s = (L->dg[k] > 0.0 ? L->dg[k] : 0.0) * p[k];
+            if (ix + 1 < nx) s = s - L->cE[k] * p[k + 1];
+            if (ix > 0) s = s - L->cE[k - 1] * p[k - 1];
+            if (iy + 1 < ny) s = s - L->cN[k] * p[k + nx];
+            if (iy > 0) s = s - L->cN[k - nx] * p[k - nx];
+            q[k] = s;
+        }
+}
+
+/*
+ * Solve A x = b by MG-preconditioned CG.  cE, cN, dg, b, x are 0-based
+ * (nx*ny, x fastest); x is output (initial guess zero).  Returns iterations;
+ * *relres gets the recomputed ||b - A x|| / ||b||.
+ * maxit<0 selects a fixed number of V-cycles per application (the HYPRE
+ * setting of 10 cycles, src/ProjectionP_Mod.f90:130): ncyc = -maxit/1000,
+ * iterations = (-maxit)%1000.
+ */
+int oracle_mgpcg(int nx, int ny, const double *cE, const double *cN, const double *dg,
+                 const double *b, double *x, double rtol, int maxit, int npre, int npost,
+                 double omega, int coarse_max, double *relres, int *nlev_out) {
+    omg M;
+    memset(&M, 0, sizeof(M));
+    M.omega = omega; M.npre = npre; M.npost = npost;
+    int ncyc = 1;
+    if (maxit < 0) { ncyc = (-maxit) / 1000; maxit = (-maxit) % 1000; if (ncyc < 1) ncyc = 1; }
+    size_t n = (size_t)nx * ny;
+    level_alloc(&M.lev[0], nx, ny);
+    memcpy(M.lev[0].cE, cE, n * sizeof(double));
+    memcpy(M.lev[0].cN, cN, n * sizeof(double));
+    memcpy(M.lev[0].dg, dg, n * sizeof(double));
+    compute_excess(&M.lev[0]);
+    M.nlev = 1;
+    while (M.lev[M.nlev - 1].nx * M.lev[M.nlev - 1].ny > coarse_max && M.nlev < 32 &&
+           (M.lev[M.nlev - 1].nx > 1 || M.lev[M.nlev - 1].ny > 1)) {
+        coarsen(&M.lev[M.nlev - 1], &M.lev[M.nlev]);
+        M.nlev++;
+    }
+    coarse_factor(&M);
+    if (nlev_out) *nlev_out = M.nlev;
+    olevel *F = &M.lev[0];
+    double *r = dalloc(n), *z = dalloc(n), *p = dalloc(n), *q = dalloc(n);
+    for (size_t k = 0; k < n; ++k) { x[k] = 0.0; r[k] = b[k]; }
+    double bnorm = sqrt(dot(b, b, n));
+    int it = 0;
+    if (bnorm == 0.0) { *relres = 0.0; goto done; }
+    double rz = 0.0;
+    for (it = 0; it < maxit; ++it) {
+        /* z = M^{-1} r (ncyc V-cycles, each on the current residual) */
+        memcpy(F->b, r, n * sizeof(double));
+        vcycle(&M, 0);
+        memcpy(z, F->x, n * sizeof(double));
+        for (int c = 1; c < ncyc; ++c) {
+            apply_A(F, z, q);
+            for (size_t k = 0; k < n; ++k) F->b[k] = r[k] - q[k];
+            vcycle(&M, 0);
+            for (size_t k = 0; k < n; ++k) z[k] += F->x[k];
+        }
+        double rz_new = dot(r, z, n);
+        if (it == 0) memcpy(p, z, n * sizeof(double));
+        else {
+            double beta = rz_new / rz;
+#pragma omp parallel for schedule(static)
+            for (size_t k = 0; k < n; ++k) p[k] = z[k] + beta * p[k];
+        }
+        rz = rz_new;
+        apply_A(F, p, q);
+        double alpha = rz / dot(p, q, n);
+#pragma omp parallel for schedule(static)
+        for (size_t k = 0; k < n; ++k) { x[k] += alpha * p[k]; r[k] -= alpha * q[k]; }
+        double rn = sqrt(dot(r, r, n));
+        if (rn <= rtol * bnorm) { it++; break; }
+    }
+    apply_A(F, x, q);
+    {
+        double s = 0.0;
+        for (size_t k = 0; k < n; ++k) { double d = b[k] - q[k]; s += d * d; }
+        *relres = sqrt(s) / bnorm;
+    }
+done:
+    free(r); free(z); free(p); free(q);
+    for (int l = 0; l < M.nlev; ++l) level_free(&M.lev[l]);
+    free(M.chol); free(M.cmap);
+    return it;
+}
+
+/* one V-cycle on b (0-based), output x; exposed for bitwise tests */
+void oracle_vcycle(int nx, int ny, const double *cE, const double *cN, const double *dg,
+                   const double *b, double *x, int npre, int npost, double omega,
+                   int coarse_max) {
+    omg M;
+    memset(&M, 0, sizeof(M));
+    M.omega = omega; M.npre = npre; M.npost = npost;
+    size_t n = (size_t)nx * ny;
+    level_alloc(&M.lev[0], nx, ny);
+    memcpy(M.lev[0].cE, cE, n * sizeof(double));
+    memcpy(M.lev[0].cN, cN, n * sizeof(double));
+    memcpy(M.lev[0].dg, dg, n * sizeof(double));
+    compute_excess(&M.lev[0]);
+    M.nlev = 1;
+    while (M.lev[M.nlev - 1].nx * M.lev[M.nlev - 1].ny > coarse_max && M.nlev < 32 &&
+           (M.lev[M.nlev - 1].nx > 1 || M.lev[M.nlev - 1].ny > 1)) {
+        coarsen(&M.lev[M.nlev - 1], &M.lev[M.nlev]);
+        M.nlev++;
+    }
+    coarse_factor(&M);
+    memcpy(M.lev[0].b, b, n * sizeof(double));
+    vcycle(&M, 0);
+    memcpy(x, M.lev[0].x, n * sizeof(double));
+    for (int l = 0; l < M.nlev; ++l) level_free(&M.lev[l]);
+    free(M.chol); free(M.cmap);
+}
+
+int oracle_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void oracle_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}

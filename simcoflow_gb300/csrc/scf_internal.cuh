@@ -1,0 +1,110 @@
+// scf_internal.cuh -- data layout and kernel interfaces shared by the CUDA
+// translation units of libscf_proj.so.
+//
+// Padded level layout (all multigrid levels and PCG vectors):
+//   element (ix,iy), 0-based interior cell, at base[iy*pitch + ix];
+//   ix in [-1,nx] and iy in [-1,ny] are valid addresses (one ghost ring);
+//   pitch = round_up(nx+2, 32), so every row starts 256-byte aligned for
+//   FP64 and the ghost ix=-1 of row iy is the last padding column of row iy-1.
+//   Ghosts and padding are zeroed once at allocation and never written, so
+//   stencils read them without branches (their couplings are zero too).
+// Cells without an unknown (Posnu = -1) carry dg = -1 and zero couplings.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace scf {
+
+constexpr double kEpsi = 1.0e-3;  // src/StateVariables.f90:26
+constexpr int kBX = 32;           // threads per block in x (2 cells each)
+constexpr int kBY = 8;            // threads per block in y
+constexpr int kThreads = kBX * kBY;
+constexpr int kMaxCoarse = 64;    // largest coarsest level (dense inverse)
+
+struct LevelView {
+  int nx, ny, pitch;
+  double* cE;  // coupling to east neighbour (>= 0)
+  double* cN;  // coupling to north neighbour (>= 0)
+  double* dg;  // diagonal, -1 for cells without an unknown
+  double* ex;  // diagonal excess dg - sum of couplings, clamped at 0
+  double* x;   // iterate / correction
+  double* b;   // right-hand side
+};
+
+// Fortran-layout inputs of the assembly, right-hand side and correction.
+struct FortranIn {
+  int nx, ny;
+  const double *dx, *dy, *dxU, *dyV;                 // (nx,ny)
+  const double *vof, *phi, *vofS, *nyS, *WlLh;       // (nx,ny)
+  const double *aE, *aW, *aN, *aS;                   // (nx+2,ny+2)
+  const int32_t *posnu_p, *posnu_u, *posnu_v;        // (nx+2,ny+2)
+  const int32_t *moex_u, *moex_v;                    // (nx,ny)
+  const double *vofS_u, *vofS_v;                     // (nx,ny)
+  const double *DpU, *DpV;                           // (nx+2,ny+2)
+  double betaP, betaM;
+  int wb, eb, sb, nb;
+};
+
+// Device-resident scalars of one PCG solve.
+struct Scalars {
+  double bnorm2, rr, rz, pq, alpha, beta, rtol2, res_true2, mres_max, rr_prev;
+  int iter, maxit, done, status, nan;
+  int pad[3];
+  unsigned tickets[8];  // last-block counters, one per reduction site
+};
+
+enum Ticket { T_RHS = 0, T_RZ, T_PQ, T_RR, T_RES, T_MRES, T_DOT };
+
+// status codes written by the device (mirror scf_proj.h)
+constexpr int kOk = 0, kErrNaN = -3, kErrNotConverged = -4;
+
+__host__ __device__ inline size_t fo1(int nx, int i, int j) {  // (1:nx,1:ny)
+  return (size_t)(i - 1) + (size_t)(j - 1) * (size_t)nx;
+}
+__host__ __device__ inline size_t fo0(int nx, int i, int j) {  // (0:nx+1,0:ny+1)
+  return (size_t)i + (size_t)j * (size_t)(nx + 2);
+}
+
+inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
+
+// launch geometry: 2 cells per thread in x, rows looped with a grid stride
+inline dim3 grid_for(int nx, int ny, int cells_per_thread_x = 2) {
+  int gx = (nx + kBX * cells_per_thread_x - 1) / (kBX * cells_per_thread_x);
+  int gy_full = (ny + kBY - 1) / kBY;
+  int cap = (152 * 16 + gx - 1) / gx;
+  int gy = gy_full < cap ? gy_full : cap;
+  if (gy < 1) gy = 1;
+  return dim3(gx, gy);
+}
+
+// ---- kernel launchers (scf_kernels.cu) ----
+void launch_assemble(const FortranIn& in, LevelView L0, Scalars* sc, cudaStream_t s);
+void launch_excess(LevelView L, cudaStream_t s);
+void launch_coarsen(LevelView F, LevelView C, cudaStream_t s);
+void launch_coarse_setup(LevelView C, double* Ainv, int* cmap, int* nc, cudaStream_t s);
+void launch_rhs(const FortranIn& in, const double* ustar, const double* vstar, double vb,
+                LevelView L0, double* bvec, double* r, double* x, Scalars* sc, double* part,
+                double rtol, int maxit, cudaStream_t s);
+void launch_smooth(LevelView L, int color, int zero_init, int do_rz, Scalars* sc, double* part,
+                   cudaStream_t s);
+void launch_resid_restrict(LevelView F, LevelView C, Scalars* sc, cudaStream_t s);
+void launch_prolong(LevelView F, LevelView C, double omega, Scalars* sc, cudaStream_t s);
+void launch_coarse_solve(LevelView C, const double* Ainv, const int* cmap, const int* nc,
+                         Scalars* sc, cudaStream_t s);
+void launch_dot_rz(LevelView L0, Scalars* sc, double* part, cudaStream_t s);
+void launch_pupdate_spmv(LevelView L0, const double* z, const double* pold, double* pnew,
+                         double* q, Scalars* sc, double* part, cudaStream_t s);
+void launch_update_xr(LevelView L0, double* x, const double* p, double* r, const double* q,
+                      Scalars* sc, double* part, unsigned long long cond, cudaStream_t s);
+void launch_final_solution(const FortranIn& in, LevelView L0, const double* x,
+                           const double* bvec, const double* ustar, const double* vstar,
+                           double* Pp, double* p, double* u, double* v, int correct,
+                           Scalars* sc, double* part, cudaStream_t s);
+void launch_final_mres(const FortranIn& in, double vb, double* u, double* v, double* mres,
+                       Scalars* sc, double* part, cudaStream_t s);
+void launch_final_zero(const FortranIn& in, double* p, double* u, double* v, cudaStream_t s);
+void launch_to_fortran(LevelView L, const double* src, double* dst, cudaStream_t s);
+void launch_from_fortran(LevelView L, const double* src, double* dst, cudaStream_t s);
+
+}  // namespace scf

@@ -1,0 +1,814 @@
+// scf_kernels.cu -- CUDA kernels (sm_103a) of the FP64 projection path:
+// operator assembly, multigrid setup and V-cycle, PCG vector kernels with
+// fused FP64 reductions, and the velocity correction.
+//
+// Arithmetic in the assembly, the multigrid kernels and the correction uses
+// explicitly rounded operations (__dmul_rn/__dadd_rn/...) in the reference's
+// operation order, so that no multiply-add is fused and results match a
+// CPU restatement bit for bit.  The PCG vector updates use FMA freely.
+#include "scf_internal.cuh"
+
+namespace scf {
+namespace {
+
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
+
+__device__ __forceinline__ int tid2() { return threadIdx.y * blockDim.x + threadIdx.x; }
+__device__ __forceinline__ bool block00() {
+  return blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0;
+}
+
+// Sum over a 256-thread block; the result is valid in thread 0.
+__device__ double block_sum(double v) {
+  __shared__ double sm[kThreads / 32];
+  __syncthreads();
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  int t = tid2();
+  if ((t & 31) == 0) sm[t >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (t == 0)
+    for (int w = 0; w < kThreads / 32; ++w) s += sm[w];
+  return s;
+}
+__device__ double block_max(double v) {
+  __shared__ double sm[kThreads / 32];
+  __syncthreads();
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  int t = tid2();
+  if ((t & 31) == 0) sm[t >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (t == 0)
+    for (int w = 0; w < kThreads / 32; ++w) s = fmax(s, sm[w]);
+  return s;
+}
+
+// Deterministic grid reduction: each block stores its partial, the last
+// block to arrive combines all partials in block order.  Returns true in all
+// threads of the last block; *total is valid in its thread 0.  The ticket is
+// reset by the last block, so the kernel can be relaunched (graph replay).
+template <bool kMax>
+__device__ bool grid_reduce(double v, double* part, unsigned* ticket, double* total) {
+  __shared__ bool last;
+  const int t = tid2();
+  const unsigned nb = gridDim.x * gridDim.y;
+  const unsigned bid = blockIdx.y * gridDim.x + blockIdx.x;
+  double s = kMax ? block_max(v) : block_sum(v);
+  if (t == 0) {
+    part[bid] = s;
+    __threadfence();
+    unsigned tk = atomicAdd(ticket, 1u);
+    last = (tk == nb - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double acc = 0.0;
+  for (unsigned k = t; k < nb; k += kThreads) {
+    double pv = __ldcg(&part[k]);
+    acc = kMax ? fmax(acc, pv) : acc + pv;
+  }
+  double tot = kMax ? block_max(acc) : block_sum(acc);
+  if (t == 0) {
+    *total = tot;
+    *ticket = 0u;
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Assembly: ComputePossionMatrixCoefficient + SetPoissonMatrix
+// (src/ProjectionP_Mod.f90:395-580, :137-273).
+// ---------------------------------------------------------------------------
+
+// 1 = wet, 2 = dry, 0 = neither (NaN input); src/ProjectionP_Mod.f90:409-410, :493-494
+__device__ __forceinline__ int cell_class(double vof, double phi, double vofS) {
+  if ((vof >= 0.5 && vofS < kEpsi) || (phi < 0.0 && vofS >= kEpsi)) return 1;
+  if ((vof < 0.5 && vofS < kEpsi) || (phi >= 0.0 && vofS >= kEpsi)) return 2;
+  return 0;
+}
+
+// Weighted density of the face between a cell of class cs and its neighbour
+// of class cn (BetaW on wet cells, BetaD on dry cells).  Returns false where
+// the reference leaves the coefficient unset.
+__device__ __forceinline__ bool face_beta(int cs, int cn, double phis, double phin, double bP,
+                                          double bM, double* B) {
+  const double tol = 1.0e-24;
+  if (cs == 1) {
+    if (cn == 2) {
+      double l = dvd(fabs(phis), add(add(fabs(phis), fabs(phin)), tol));
+      *B = add(mul(l, bM), mul(sub(1.0, l), bP));
+      return true;
+    }
+    if (cn == 1) { *B = bM; return true; }
+    return false;
+  }
+  if (cs == 2) {
+    if (cn == 1) {
+      double l = dvd(fabs(phis), add(add(fabs(phis), fabs(phin)), tol));
+      *B = add(mul(l, bP), mul(sub(1.0, l), bM));
+      return true;
+    }
+    if (cn == 2) { *B = bP; return true; }
+  }
+  return false;
+}
+// face on the domain boundary: wet cells use BetaM, dry cells BetaP
+__device__ __forceinline__ bool boundary_beta(int cs, double bP, double bM, double* B) {
+  if (cs == 1) { *B = bM; return true; }
+  if (cs == 2) { *B = bP; return true; }
+  return false;
+}
+// PoCoef = Dp*len/dist*BetaP*BetaM/B, evaluated left to right
+__device__ __forceinline__ double pocoef(double Dp, double len, double dist, double bP,
+                                         double bM, double B) {
+  return dvd(mul(mul(dvd(mul(Dp, len), dist), bP), bM), B);
+}
+
+__global__ void k_assemble(FortranIn in, LevelView L, Scalars* sc) {
+  const int nx = in.nx, ny = in.ny;
+  const int ix = blockIdx.x * kBX + threadIdx.x;
+  if (ix >= nx) return;
+  for (int iy = blockIdx.y * kBY + threadIdx.y; iy < ny; iy += gridDim.y * kBY) {
+    const int i = ix + 1, j = iy + 1;
+    const size_t k1 = fo1(nx, i, j), k0 = fo0(nx, i, j);
+    const size_t kl = (size_t)iy * L.pitch + ix;
+    if (in.posnu_p[k0] == -1) {
+      L.cE[kl] = 0.0; L.cN[kl] = 0.0; L.dg[kl] = -1.0;
+      continue;
+    }
+    const double bP = in.betaP, bM = in.betaM;
+    const double phis = in.phi[k1];
+    const int cs = cell_class(in.vof[k1], phis, in.vofS[k1]);
+    const double dxP = in.dx[k1], dyP = in.dy[k1];
+    double pc[4] = {0.0, 0.0, 0.0, 0.0};  // S, W, E, N
+    double B;
+    if (j > 1) {
+      size_t kn = fo1(nx, i, j - 1);
+      if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B))
+        pc[0] = pocoef(in.DpV[fo0(nx, i, j - 1)], dxP, in.dyV[kn], bP, bM, B);
+    } else if (boundary_beta(cs, bP, bM, &B)) {
+      pc[0] = pocoef(in.DpV[k0], dxP, in.dyV[k1], bP, bM, B);
+    }
+    if (i > 1) {
+      size_t kn = fo1(nx, i - 1, j);
+      if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B))
+        pc[1] = pocoef(in.DpU[fo0(nx, i - 1, j)], dyP, in.dxU[kn], bP, bM, B);
+    } else if (boundary_beta(cs, bP, bM, &B)) {
+      pc[1] = pocoef(in.DpU[k0], dyP, in.dxU[k1], bP, bM, B);
+    }
+    if (i < nx) {
+      size_t kn = fo1(nx, i + 1, j);
+      if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B))
+        pc[2] = pocoef(in.DpU[k0], dyP, in.dxU[k1], bP, bM, B);
+    } else if (boundary_beta(cs, bP, bM, &B)) {
+      pc[2] = pocoef(in.DpU[k0], dyP, in.dxU[k1], bP, bM, B);
+    }
+    if (j < ny) {
+      size_t kn = fo1(nx, i, j + 1);
+      if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B))
+        pc[3] = pocoef(in.DpV[k0], dxP, in.dyV[k1], bP, bM, B);
+    } else if (boundary_beta(cs, bP, bM, &B)) {
+      pc[3] = pocoef(in.DpV[k0], dxP, in.dyV[k1], bP, bM, B);
+    }
+    const double aS = in.aS[k0], aW = in.aW[k0], aE = in.aE[k0], aN = in.aN[k0];
+    const double tS = mul(pc[0], aS), tW = mul(pc[1], aW), tE = mul(pc[2], aE), tN = mul(pc[3], aN);
+    double d = add(add(add(tS, tW), tE), tN);
+    if (in.sb == 1 && j == 1) d = sub(d, tS);
+    if (in.wb == 1 && i == 1) d = sub(d, tW);
+    if (in.eb == 1 && i == nx) d = sub(d, tE);
+    if (in.nb == 1 && j == ny) d = sub(d, tN);
+    d = add(d, mul(copysign(1.0, d), 1.0e-24));
+    if (!isfinite(d) || cs == 0) sc->nan = 1;
+    L.dg[kl] = d;
+    L.cE[kl] = (i < nx && in.posnu_p[fo0(nx, i + 1, j)] != -1) ? tE : 0.0;
+    L.cN[kl] = (j < ny && in.posnu_p[fo0(nx, i, j + 1)] != -1) ? tN : 0.0;
+  }
+}
+
+// diagonal excess dg - (cE + cW + cN + cS), clamped at zero
+__global__ void k_excess(LevelView L) {
+  const int ix = blockIdx.x * kBX + threadIdx.x;
+  if (ix >= L.nx) return;
+  for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY) {
+    const size_t k = (size_t)iy * L.pitch + ix;
+    const double d = L.dg[k];
+    if (d < 0.0) { L.ex[k] = 0.0; continue; }
+    double s = add(add(add(L.cE[k], L.cE[k - 1]), L.cN[k]), L.cN[k - L.pitch]);
+    double e = sub(d, s);
+    L.ex[k] = e > 0.0 ? e : 0.0;
+  }
+}
+
+// Galerkin coarse operator for piecewise-constant 2x2 aggregation
+__global__ void k_coarsen(LevelView F, LevelView C) {
+  const int I = blockIdx.x * kBX + threadIdx.x;
+  if (I >= C.nx) return;
+  const int nxf = F.nx, nyf = F.ny, pf = F.pitch;
+  for (int J = blockIdx.y * kBY + threadIdx.y; J < C.ny; J += gridDim.y * kBY) {
+    double ce = 0.0, cn = 0.0, ex = 0.0;
+    int active = 0;
+    for (int dj = 0; dj < 2; ++dj)
+      for (int di = 0; di < 2; ++di) {
+        int ix = 2 * I + di, iy = 2 * J + dj;
+        if (ix >= nxf || iy >= nyf) continue;
+        size_t k = (size_t)iy * pf + ix;
+        if (F.dg[k] >= 0.0) active = 1;
+        ex = add(ex, F.ex[k]);
+        if (di == 1) ce = add(ce, F.cE[k]);
+        if (dj == 1) cn = add(cn, F.cN[k]);
+      }
+    // couplings of the west and south coarse neighbours, same sums
+    double cw = 0.0, cs = 0.0;
+    if (I > 0)
+      for (int dj = 0; dj < 2; ++dj) {
+        int ix = 2 * I - 1, iy = 2 * J + dj;
+        if (iy < nyf) cw = add(cw, F.cE[(size_t)iy * pf + ix]);
+      }
+    if (J > 0)
+      for (int di = 0; di < 2; ++di) {
+        int ix = 2 * I + di, iy = 2 * J - 1;
+        if (ix < nxf) cs = add(cs, F.cN[(size_t)iy * pf + ix]);
+      }
+    const size_t kc = (size_t)J * C.pitch + I;
+    C.cE[kc] = ce;
+    C.cN[kc] = cn;
+    C.ex[kc] = active ? ex : 0.0;
+    double d = -1.0;
+    if (active) {
+      d = add(add(add(add(ce, cw), cn), cs), ex);
+      if (!(d > 0.0)) d = -1.0;
+    }
+    C.dg[kc] = d;
+  }
+}
+
+// Dense inverse of the coarsest operator (at most kMaxCoarse unknowns) by
+// Gauss-Jordan elimination without pivoting (the matrix is SPD).
+__global__ void k_coarse_setup(LevelView C, double* Ainv, int* cmap, int* nc_out) {
+  __shared__ double A[kMaxCoarse * kMaxCoarse];
+  __shared__ double rowp[kMaxCoarse], colp[kMaxCoarse];
+  __shared__ int map[kMaxCoarse];
+  __shared__ int n;
+  const int t = threadIdx.x, NT = blockDim.x;
+  const int ncell = C.nx * C.ny;
+  if (t == 0) {
+    int c = 0;
+    for (int k = 0; k < ncell; ++k) {
+      int ix = k % C.nx, iy = k / C.nx;
+      map[k] = C.dg[(size_t)iy * C.pitch + ix] >= 0.0 ? c++ : -1;
+    }
+    n = c;
+  }
+  __syncthreads();
+  const int nn = n;
+  for (int e = t; e < nn * nn; e += NT) A[e] = 0.0;
+  __syncthreads();
+  if (t == 0) {
+    for (int k = 0; k < ncell; ++k) {
+      int r = map[k];
+      if (r < 0) continue;
+      int ix = k % C.nx, iy = k / C.nx;
+      size_t kk = (size_t)iy * C.pitch + ix;
+      A[r * nn + r] = C.dg[kk];
+      if (ix + 1 < C.nx && map[k + 1] >= 0) {
+        int c = map[k + 1];
+        A[r * nn + c] = -C.cE[kk]; A[c * nn + r] = -C.cE[kk];
+      }
+      if (iy + 1 < C.ny && map[k + C.nx] >= 0) {
+        int c = map[k + C.nx];
+        A[r * nn + c] = -C.cN[kk]; A[c * nn + r] = -C.cN[kk];
+      }
+    }
+  }
+  __syncthreads();
+  for (int p = 0; p < nn; ++p) {
+    const double piv = A[p * nn + p];
+    for (int j = t; j < nn; j += NT) {
+      rowp[j] = (j == p) ? 1.0 / piv : A[p * nn + j] / piv;
+      colp[j] = A[j * nn + p];
+    }
+    __syncthreads();
+    for (int e = t; e < nn * nn; e += NT) {
+      int i = e / nn, j = e % nn;
+      if (i == p) A[e] = rowp[j];
+      else A[e] = ((j == p) ? 0.0 : A[e]) - colp[i] * rowp[j];
+    }
+    __syncthreads();
+  }
+  for (int e = t; e < nn * nn; e += NT) Ainv[e] = A[e];
+  for (int k = t; k < ncell; k += NT) cmap[k] = map[k];
+  if (t == 0) *nc_out = nn;
+}
+
+__global__ void k_coarse_solve(LevelView C, const double* Ainv, const int* cmap, const int* ncp,
+                               Scalars* sc) {
+  if (sc && sc->done) return;
+  __shared__ double bd[kMaxCoarse];
+  const int t = threadIdx.x;
+  const int ncell = C.nx * C.ny, nn = *ncp;
+  for (int k = t; k < ncell; k += blockDim.x) {
+    int r = cmap[k];
+    if (r >= 0) bd[r] = C.b[(size_t)(k / C.nx) * C.pitch + (k % C.nx)];
+  }
+  __syncthreads();
+  for (int k = t; k < ncell; k += blockDim.x) {
+    int r = cmap[k];
+    double y = 0.0;
+    if (r >= 0)
+      for (int c = 0; c < nn; ++c) y = fma(Ainv[r * nn + c], bd[c], y);
+    C.x[(size_t)(k / C.nx) * C.pitch + (k % C.nx)] = y;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Right-hand side: SetPoissonVectors (src/ProjectionP_Mod.f90:306-337).
+// Also starts the PCG: r = b, x = 0, scalars reset.
+// ---------------------------------------------------------------------------
+__global__ void k_rhs(FortranIn in, const double* us, const double* vs, double vb, int pitch,
+                      double* bvec, double* r, double* x, Scalars* sc, double* part, double rtol,
+                      int maxit) {
+  const int nx = in.nx, ny = in.ny;
+  const int ix = blockIdx.x * kBX + threadIdx.x;
+  double acc = 0.0;
+  bool bad = false;
+  if (ix < nx) {
+    for (int iy = blockIdx.y * kBY + threadIdx.y; iy < ny; iy += gridDim.y * kBY) {
+      const int i = ix + 1, j = iy + 1;
+      const size_t k1 = fo1(nx, i, j), k0 = fo0(nx, i, j);
+      const size_t kl = (size_t)iy * pitch + ix;
+      double bv = 0.0;
+      if (in.posnu_p[k0] != -1) {
+        const double dx = in.dx[k1], dy = in.dy[k1];
+        double tx = mul(sub(mul(us[k0], in.aE[k0]), mul(us[fo0(nx, i - 1, j)], in.aW[k0])), dy);
+        double ty = mul(sub(mul(vs[k0], in.aN[k0]), mul(vs[fo0(nx, i, j - 1)], in.aS[k0])), dx);
+        bv = add(sub(-tx, ty), mul(mul(vb, in.nyS[k1]), in.WlLh[k1]));
+        if (!isfinite(bv)) bad = true;
+      }
+      bvec[kl] = bv;
+      r[kl] = bv;
+      x[kl] = 0.0;
+      acc = fma(bv, bv, acc);
+    }
+  }
+  if (bad) sc->nan = 1;
+  double tot;
+  if (grid_reduce<false>(acc, part, &sc->tickets[T_RHS], &tot) && tid2() == 0) {
+    sc->bnorm2 = tot;
+    sc->rr = tot;
+    sc->rr_prev = tot;
+    sc->rtol2 = rtol * rtol * tot;
+    sc->rz = 0.0; sc->pq = 0.0; sc->alpha = 0.0; sc->beta = 0.0;
+    sc->iter = 0;
+    sc->maxit = maxit;
+    sc->status = kOk;
+    sc->done = 0;
+    if (!(tot > 0.0)) sc->done = 1;  // b = 0: x = 0 is the solution
+    if (!isfinite(tot) || sc->nan) { sc->status = kErrNaN; sc->done = 1; }
+    sc->pad[0] = 0;  // guard counter of the graph loop
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Multigrid V-cycle kernels.
+// ---------------------------------------------------------------------------
+
+// One red-black Gauss-Seidel half sweep updating cells with (ix+iy)%2 == color.
+// zero_init: the iterate starts at zero (the other colour is written as 0).
+// do_rz: also reduce r.z over the level (level 0 is the PCG: b = r, x = z)
+// and compute the PCG beta.
+__global__ void k_smooth(LevelView L, int color, int zero_init, int do_rz, Scalars* sc,
+                         double* part) {
+  if (sc->done) return;
+  const int ix0 = 2 * (blockIdx.x * kBX + threadIdx.x);
+  const int P = L.pitch;
+  double acc = 0.0;
+  if (ix0 < L.nx) {
+    for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY) {
+      const int ix = ix0 + ((iy + color) & 1);
+      const int io = ix0 + ((iy + color + 1) & 1);
+      const size_t row = (size_t)iy * P;
+      if (zero_init && io < L.nx) L.x[row + io] = 0.0;
+      if (ix < L.nx) {
+        const size_t k = row + ix;
+        const double d = L.dg[k];
+        double s = L.b[k];
+        if (!zero_init) {
+          s = add(s, mul(L.cE[k], L.x[k + 1]));
+          s = add(s, mul(L.cE[k - 1], L.x[k - 1]));
+          s = add(s, mul(L.cN[k], L.x[k + P]));
+          s = add(s, mul(L.cN[k - P], L.x[k - P]));
+        }
+        const double xn = d > 0.0 ? dvd(s, d) : 0.0;
+        L.x[k] = xn;
+        if (do_rz) acc = fma(L.b[k], xn, acc);
+      }
+      if (do_rz && io < L.nx) acc = fma(L.b[row + io], L.x[row + io], acc);
+    }
+  }
+  if (!do_rz) return;
+  double tot;
+  if (grid_reduce<false>(acc, part, &sc->tickets[T_RZ], &tot) && tid2() == 0) {
+    sc->beta = (sc->iter == 0) ? 0.0 : tot / sc->rz;
+    sc->rz = tot;
+  }
+}
+
+// residual of the fine level, summed over each 2x2 aggregate into C.b
+__global__ void k_resid_restrict(LevelView F, LevelView C, Scalars* sc) {
+  if (sc && sc->done) return;
+  const int I = blockIdx.x * kBX + threadIdx.x;
+  if (I >= C.nx) return;
+  const int nxf = F.nx, nyf = F.ny, P = F.pitch;
+  for (int J = blockIdx.y * kBY + threadIdx.y; J < C.ny; J += gridDim.y * kBY) {
+    double s = 0.0;
+    for (int dj = 0; dj < 2; ++dj)
+      for (int di = 0; di < 2; ++di) {
+        int ix = 2 * I + di, iy = 2 * J + dj;
+        if (ix >= nxf || iy >= nyf) continue;
+        size_t k = (size_t)iy * P + ix;
+        double r = 0.0;
+        if (F.dg[k] >= 0.0) {
+          r = sub(F.b[k], mul(F.dg[k], F.x[k]));
+          r = add(r, mul(F.cE[k], F.x[k + 1]));
+          r = add(r, mul(F.cE[k - 1], F.x[k - 1]));
+          r = add(r, mul(F.cN[k], F.x[k + P]));
+          r = add(r, mul(F.cN[k - P], F.x[k - P]));
+        }
+        s = add(s, r);
+      }
+    C.b[(size_t)J * C.pitch + I] = s;
+  }
+}
+
+// x_f += omega * x_c(parent) on cells with an unknown
+__global__ void k_prolong(LevelView F, LevelView C, double omega, Scalars* sc) {
+  if (sc && sc->done) return;
+  const int ix0 = 2 * (blockIdx.x * kBX + threadIdx.x);
+  if (ix0 >= F.nx) return;
+  for (int iy = blockIdx.y * kBY + threadIdx.y; iy < F.ny; iy += gridDim.y * kBY) {
+    const double xc = C.x[(size_t)(iy >> 1) * C.pitch + (ix0 >> 1)];
+    const double corr = mul(omega, xc);
+    for (int c = 0; c < 2; ++c) {
+      int ix = ix0 + c;
+      if (ix >= F.nx) break;
+      size_t k = (size_t)iy * F.pitch + ix;
+      if (F.dg[k] >= 0.0) F.x[k] = add(F.x[k], corr);
+    }
+  }
+}
+
+// r.z when the V-cycle does not end with a smoothing sweep
+__global__ void k_dot_rz(LevelView L, Scalars* sc, double* part) {
+  if (sc->done) return;
+  const int ix0 = 2 * (blockIdx.x * kBX + threadIdx.x);
+  double acc = 0.0;
+  if (ix0 < L.nx)
+    for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY)
+      for (int c = 0; c < 2 && ix0 + c < L.nx; ++c) {
+        size_t k = (size_t)iy * L.pitch + ix0 + c;
+        acc = fma(L.b[k], L.x[k], acc);
+      }
+  double tot;
+  if (grid_reduce<false>(acc, part, &sc->tickets[T_RZ], &tot) && tid2() == 0) {
+    sc->beta = (sc->iter == 0) ? 0.0 : tot / sc->rz;
+    sc->rz = tot;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// PCG vector kernels.
+// ---------------------------------------------------------------------------
+
+// p_new = z + beta p_old (p_new = z on the first iteration), q = A p_new,
+// reduce p.q and set alpha = r.z / p.q.  Neighbour values of p_new are
+// recomputed from z and p_old, so p_old and p_new must be different buffers.
+__global__ void k_pupdate_spmv(LevelView L, const double* __restrict__ z,
+                               const double* __restrict__ pold, double* __restrict__ pnew,
+                               double* __restrict__ q, Scalars* sc, double* part) {
+  if (sc->done) return;
+  const int ix0 = 2 * (blockIdx.x * kBX + threadIdx.x);
+  const int P = L.pitch;
+  const bool first = sc->iter == 0;
+  const double beta = sc->beta;
+  double acc = 0.0;
+  if (ix0 < L.nx) {
+    for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY) {
+      const size_t k0 = (size_t)iy * P + ix0;
+      auto pn = [&](size_t k) { return first ? z[k] : fma(beta, pold[k], z[k]); };
+      double pw = pn(k0 - 1), pc0 = pn(k0), pc1 = pn(k0 + 1), pe = pn(k0 + 2);
+      double ps0 = pn(k0 - P), ps1 = pn(k0 - P + 1), pn0 = pn(k0 + P), pn1 = pn(k0 + P + 1);
+      const double2 dg = *reinterpret_cast<const double2*>(L.dg + k0);
+      const double2 ce = *reinterpret_cast<const double2*>(L.cE + k0);
+      const double2 cn = *reinterpret_cast<const double2*>(L.cN + k0);
+      const double2 cs = *reinterpret_cast<const double2*>(L.cN + k0 - P);
+      const double cw = L.cE[k0 - 1];
+      double q0 = fmax(dg.x, 0.0) * pc0 - ce.x * pc1 - cw * pw - cn.x * pn0 - cs.x * ps0;
+      double q1 = fmax(dg.y, 0.0) * pc1 - ce.y * pe - ce.x * pc0 - cn.y * pn1 - cs.y * ps1;
+      pnew[k0] = pc0;
+      q[k0] = q0;
+      acc = fma(pc0, q0, acc);
+      if (ix0 + 1 < L.nx) {
+        pnew[k0 + 1] = pc1;
+        q[k0 + 1] = q1;
+        acc = fma(pc1, q1, acc);
+      }
+    }
+  }
+  double tot;
+  if (grid_reduce<false>(acc, part, &sc->tickets[T_PQ], &tot) && tid2() == 0) {
+    sc->pq = tot;
+    sc->alpha = sc->rz / tot;
+  }
+}
+
+// x += alpha p, r -= alpha q, reduce r.r; the last block advances the
+// iteration count, tests convergence and, inside a graph loop, clears the
+// loop condition.  Block (0,0) also counts body executions and stops the
+// loop after maxit+2 of them whatever else happens.
+__global__ void k_update_xr(LevelView L, double* __restrict__ x, const double* __restrict__ p,
+                            double* __restrict__ r, const double* __restrict__ q, Scalars* sc,
+                            double* part, unsigned long long cond) {
+  if (cond && block00()) {
+    int g = atomicAdd(&sc->pad[0], 1);
+    if (g + 1 >= sc->maxit + 2) cudaGraphSetConditional(cond, 0u);
+  }
+  if (sc->done) {
+    if (cond && block00()) cudaGraphSetConditional(cond, 0u);
+    return;
+  }
+  const int ix0 = 2 * (blockIdx.x * kBX + threadIdx.x);
+  const double alpha = sc->alpha;
+  double acc = 0.0;
+  if (ix0 < L.nx) {
+    for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY) {
+      const size_t k = (size_t)iy * L.pitch + ix0;
+      double2 xv = *reinterpret_cast<double2*>(x + k);
+      double2 rv = *reinterpret_cast<double2*>(r + k);
+      const double2 pv = *reinterpret_cast<const double2*>(p + k);
+      const double2 qv = *reinterpret_cast<const double2*>(q + k);
+      xv.x = fma(alpha, pv.x, xv.x);
+      rv.x = fma(-alpha, qv.x, rv.x);
+      acc = fma(rv.x, rv.x, acc);
+      if (ix0 + 1 < L.nx) {
+        xv.y = fma(alpha, pv.y, xv.y);
+        rv.y = fma(-alpha, qv.y, rv.y);
+        acc = fma(rv.y, rv.y, acc);
+        *reinterpret_cast<double2*>(x + k) = xv;
+        *reinterpret_cast<double2*>(r + k) = rv;
+      } else {
+        x[k] = xv.x;
+        r[k] = rv.x;
+      }
+    }
+  }
+  double tot;
+  if (grid_reduce<false>(acc, part, &sc->tickets[T_RR], &tot) && tid2() == 0) {
+    sc->rr_prev = sc->rr;
+    sc->rr = tot;
+    sc->iter += 1;
+    if (!isfinite(tot) || !isfinite(sc->alpha)) {
+      sc->status = kErrNaN;
+      sc->done = 1;
+    } else if (tot <= sc->rtol2) {
+      sc->done = 1;
+    } else if (sc->iter >= sc->maxit) {
+      sc->status = kErrNotConverged;
+      sc->done = 1;
+    }
+    if (sc->done && cond) cudaGraphSetConditional(cond, 0u);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Solution scatter, FP64 residual check and velocity correction:
+// DeltaPressureGetValues / DeltaPressureBoundaryCondition
+// (src/ProjectionP_Mod.f90:356-393, :582-595) and UpdatePUV
+// (src/ComputePUV_Mod.f90:59-169).
+// ---------------------------------------------------------------------------
+
+// Pressure-gradient correction of one face between cells s (self) and n
+// (east or north neighbour): returns false when the reference leaves the
+// face alone.  G = (Pp_n - Pp_s)*BetaM*BetaP/BetaW*Dp/dist.
+__device__ __forceinline__ bool face_grad(int cs, int cn, double phis, double phin, double pps,
+                                          double ppn, double bP, double bM, double Dp,
+                                          double dist, double* G) {
+  const double tol = 1.0e-24;
+  double BW;
+  if (cs == 1) {
+    if (cn == 2) {
+      double l = dvd(fabs(phis), add(add(fabs(phis), fabs(phin)), tol));
+      BW = add(mul(l, bM), mul(sub(1.0, l), bP));
+    } else if (cn == 1) {
+      BW = bM;
+    } else {
+      return false;
+    }
+  } else if (cs == 2) {
+    if (cn == 1) {
+      double l = dvd(fabs(phis), add(add(fabs(phis), fabs(phin)), tol));
+      BW = add(mul(l, bP), mul(sub(1.0, l), bM));
+    } else if (cn == 2) {
+      BW = bP;
+    } else {
+      return false;
+    }
+  } else {
+    return false;
+  }
+  *G = dvd(mul(dvd(mul(mul(sub(ppn, pps), bM), bP), BW), Dp), dist);
+  return true;
+}
+
+__global__ void k_final_solution(FortranIn in, LevelView L, const double* __restrict__ x,
+                                 const double* __restrict__ bvec, const double* __restrict__ us,
+                                 const double* __restrict__ vs, double* Pp, double* p, double* u,
+                                 double* v, int correct, Scalars* sc, double* part) {
+  const int nx = in.nx, ny = in.ny;
+  const int ix = blockIdx.x * kBX + threadIdx.x;
+  const int P = L.pitch;
+  double acc = 0.0;
+  if (ix < nx) {
+    for (int iy = blockIdx.y * kBY + threadIdx.y; iy < ny; iy += gridDim.y * kBY) {
+      const int i = ix + 1, j = iy + 1;
+      const size_t k1 = fo1(nx, i, j), k0 = fo0(nx, i, j);
+      const size_t kl = (size_t)iy * P + ix;
+      const bool act = in.posnu_p[k0] != -1;
+      const double ppc = act ? x[kl] : 0.0;
+      if (Pp) {
+        Pp[k0] = ppc;
+        if (i == 1) Pp[fo0(nx, 0, j)] = (double)in.wb * ppc;
+        if (i == nx) Pp[fo0(nx, nx + 1, j)] = (double)in.eb * ppc;
+        if (j == 1) Pp[fo0(nx, i, 0)] = (double)in.sb * ppc;
+        if (j == ny) Pp[fo0(nx, i, ny + 1)] = (double)in.nb * ppc;
+        if (i == 1 && j == 1) {
+          Pp[fo0(nx, 0, 0)] = 0.0; Pp[fo0(nx, nx + 1, 0)] = 0.0;
+          Pp[fo0(nx, 0, ny + 1)] = 0.0; Pp[fo0(nx, nx + 1, ny + 1)] = 0.0;
+        }
+      }
+      if (act) {
+        double ax = fmax(L.dg[kl], 0.0) * x[kl] - L.cE[kl] * x[kl + 1] - L.cE[kl - 1] * x[kl - 1] -
+                    L.cN[kl] * x[kl + P] - L.cN[kl - P] * x[kl - P];
+        double rr = bvec[kl] - ax;
+        acc = fma(rr, rr, acc);
+      }
+      if (!correct) continue;
+      const double bP = in.betaP, bM = in.betaM;
+      const double phis = in.phi[k1];
+      const int cs = cell_class(in.vof[k1], phis, in.vofS[k1]);
+      if (i <= nx - 1 && in.posnu_u[k0] != -1 && in.moex_u[k1] != 1) {
+        const size_t kn = fo1(nx, i + 1, j);
+        const double ppn = in.posnu_p[fo0(nx, i + 1, j)] != -1 ? x[kl + 1] : 0.0;
+        double G;
+        if (face_grad(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], ppc,
+                      ppn, bP, bM, in.DpU[k0], in.dxU[k1], &G))
+          u[k0] = sub(us[k0], G);
+      }
+      if (j <= ny - 1 && in.posnu_v[k0] != -1 && in.moex_v[k1] != 1) {
+        const size_t kn = fo1(nx, i, j + 1);
+        const double ppn = in.posnu_p[fo0(nx, i, j + 1)] != -1 ? x[kl + P] : 0.0;
+        double G;
+        if (face_grad(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], ppc,
+                      ppn, bP, bM, in.DpV[k0], in.dyV[k1], &G))
+          v[k0] = sub(vs[k0], G);
+      }
+      if (act) p[k0] = ppc;
+    }
+  }
+  double tot;
+  if (grid_reduce<false>(acc, part, &sc->tickets[T_RES], &tot) && tid2() == 0)
+    sc->res_true2 = tot;
+}
+
+// top-row continuity (src/ComputePUV_Mod.f90:177-182) and mass residual (:184-216)
+__global__ void k_final_mres(FortranIn in, double vb, double* u, double* v, double* mres,
+                             Scalars* sc, double* part) {
+  const int nx = in.nx, ny = in.ny;
+  const int ix = blockIdx.x * kBX + threadIdx.x;
+  double acc = 0.0;
+  if (ix < nx) {
+    for (int iy = blockIdx.y * kBY + threadIdx.y; iy < ny; iy += gridDim.y * kBY) {
+      const int i = ix + 1, j = iy + 1;
+      const size_t k1 = fo1(nx, i, j), k0 = fo0(nx, i, j);
+      const double dx = in.dx[k1], dy = in.dy[k1];
+      const double aE = in.aE[k0], aW = in.aW[k0], aN = in.aN[k0], aS = in.aS[k0];
+      const double ue = u[k0], uw = u[fo0(nx, i - 1, j)], vsb = v[fo0(nx, i, j - 1)];
+      double vn = v[k0];
+      if (j == ny) {
+        vn = dvd(dvd(add(mul(add(-mul(ue, aE), mul(uw, aW)), dy), mul(mul(vsb, aS), dx)), dx), aN);
+        v[k0] = vn;
+      }
+      double m = sub(add(mul(sub(mul(ue, aE), mul(uw, aW)), dy), mul(sub(mul(vn, aN), mul(vsb, aS)), dx)),
+                     mul(mul(vb, in.nyS[k1]), in.WlLh[k1]));
+      if (in.vofS[k1] > 1.0 - kEpsi) m = 0.0;
+      mres[k1] = m;
+      if (in.posnu_p[k0] != -1) acc = fmax(acc, fabs(m));
+    }
+  }
+  double tot;
+  if (grid_reduce<true>(acc, part, &sc->tickets[T_MRES], &tot) && tid2() == 0) sc->mres_max = tot;
+}
+
+// VariablesInternalCellCondition (src/ComputePUV_Mod.f90:227-245)
+__global__ void k_final_zero(FortranIn in, double* p, double* u, double* v) {
+  const int nx = in.nx, ny = in.ny;
+  const int ix = blockIdx.x * kBX + threadIdx.x;
+  if (ix >= nx) return;
+  for (int iy = blockIdx.y * kBY + threadIdx.y; iy < ny; iy += gridDim.y * kBY) {
+    const int i = ix + 1, j = iy + 1;
+    const size_t k1 = fo1(nx, i, j), k0 = fo0(nx, i, j);
+    if (in.vofS[k1] > 1.0 - kEpsi) p[k0] = 0.0;
+    if (in.vofS_u[k1] >= 1.0 - kEpsi) u[k0] = 0.0;
+    if (in.vofS_v[k1] >= 1.0 - kEpsi) v[k0] = 0.0;
+  }
+}
+
+__global__ void k_to_fortran(LevelView L, const double* src, double* dst) {
+  const int ix = blockIdx.x * kBX + threadIdx.x;
+  if (ix >= L.nx) return;
+  for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY)
+    dst[(size_t)ix + (size_t)iy * L.nx] = src[(size_t)iy * L.pitch + ix];
+}
+__global__ void k_from_fortran(LevelView L, const double* src, double* dst) {
+  const int ix = blockIdx.x * kBX + threadIdx.x;
+  if (ix >= L.nx) return;
+  for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY)
+    dst[(size_t)iy * L.pitch + ix] = src[(size_t)ix + (size_t)iy * L.nx];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static const dim3 kBlock(kBX, kBY);
+
+void launch_assemble(const FortranIn& in, LevelView L0, Scalars* sc, cudaStream_t s) {
+  k_assemble<<<grid_for(in.nx, in.ny, 1), kBlock, 0, s>>>(in, L0, sc);
+}
+void launch_excess(LevelView L, cudaStream_t s) {
+  k_excess<<<grid_for(L.nx, L.ny, 1), kBlock, 0, s>>>(L);
+}
+void launch_coarsen(LevelView F, LevelView C, cudaStream_t s) {
+  k_coarsen<<<grid_for(C.nx, C.ny, 1), kBlock, 0, s>>>(F, C);
+}
+void launch_coarse_setup(LevelView C, double* Ainv, int* cmap, int* nc, cudaStream_t s) {
+  k_coarse_setup<<<1, 256, 0, s>>>(C, Ainv, cmap, nc);
+}
+void launch_rhs(const FortranIn& in, const double* ustar, const double* vstar, double vb,
+                LevelView L0, double* bvec, double* r, double* x, Scalars* sc, double* part,
+                double rtol, int maxit, cudaStream_t s) {
+  k_rhs<<<grid_for(in.nx, in.ny, 1), kBlock, 0, s>>>(in, ustar, vstar, vb, L0.pitch, bvec, r, x,
+                                                      sc, part, rtol, maxit);
+}
+void launch_smooth(LevelView L, int color, int zero_init, int do_rz, Scalars* sc, double* part,
+                   cudaStream_t s) {
+  k_smooth<<<grid_for(L.nx, L.ny), kBlock, 0, s>>>(L, color, zero_init, do_rz, sc, part);
+}
+void launch_resid_restrict(LevelView F, LevelView C, Scalars* sc, cudaStream_t s) {
+  k_resid_restrict<<<grid_for(C.nx, C.ny, 1), kBlock, 0, s>>>(F, C, sc);
+}
+void launch_prolong(LevelView F, LevelView C, double omega, Scalars* sc, cudaStream_t s) {
+  k_prolong<<<grid_for(F.nx, F.ny), kBlock, 0, s>>>(F, C, omega, sc);
+}
+void launch_coarse_solve(LevelView C, const double* Ainv, const int* cmap, const int* nc,
+                         Scalars* sc, cudaStream_t s) {
+  k_coarse_solve<<<1, 64, 0, s>>>(C, Ainv, cmap, nc, sc);
+}
+void launch_dot_rz(LevelView L0, Scalars* sc, double* part, cudaStream_t s) {
+  k_dot_rz<<<grid_for(L0.nx, L0.ny), kBlock, 0, s>>>(L0, sc, part);
+}
+void launch_pupdate_spmv(LevelView L0, const double* z, const double* pold, double* pnew,
+                         double* q, Scalars* sc, double* part, cudaStream_t s) {
+  k_pupdate_spmv<<<grid_for(L0.nx, L0.ny), kBlock, 0, s>>>(L0, z, pold, pnew, q, sc, part);
+}
+void launch_update_xr(LevelView L0, double* x, const double* p, double* r, const double* q,
+                      Scalars* sc, double* part, unsigned long long cond, cudaStream_t s) {
+  k_update_xr<<<grid_for(L0.nx, L0.ny), kBlock, 0, s>>>(L0, x, p, r, q, sc, part, cond);
+}
+void launch_final_solution(const FortranIn& in, LevelView L0, const double* x,
+                           const double* bvec, const double* ustar, const double* vstar,
+                           double* Pp, double* p, double* u, double* v, int correct,
+                           Scalars* sc, double* part, cudaStream_t s) {
+  k_final_solution<<<grid_for(in.nx, in.ny, 1), kBlock, 0, s>>>(in, L0, x, bvec, ustar, vstar, Pp,
+                                                                 p, u, v, correct, sc, part);
+}
+void launch_final_mres(const FortranIn& in, double vb, double* u, double* v, double* mres,
+                       Scalars* sc, double* part, cudaStream_t s) {
+  k_final_mres<<<grid_for(in.nx, in.ny, 1), kBlock, 0, s>>>(in, vb, u, v, mres, sc, part);
+}
+void launch_final_zero(const FortranIn& in, double* p, double* u, double* v, cudaStream_t s) {
+  k_final_zero<<<grid_for(in.nx, in.ny, 1), kBlock, 0, s>>>(in, p, u, v);
+}
+void launch_to_fortran(LevelView L, const double* src, double* dst, cudaStream_t s) {
+  k_to_fortran<<<grid_for(L.nx, L.ny, 1), kBlock, 0, s>>>(L, src, dst);
+}
+void launch_from_fortran(LevelView L, const double* src, double* dst, cudaStream_t s) {
+  k_from_fortran<<<grid_for(L.nx, L.ny, 1), kBlock, 0, s>>>(L, src, dst);
+}
+
+}  // namespace scf

@@ -1,0 +1,269 @@
+"""Python host API over libscf_proj.so (include/scf_proj.h).
+
+Mirrors the reference's projection entry points:
+
+  ProjectionSolver.poisson_equation_solver  PoissonEquationSolver
+                                            (src/ProjectionP_Mod.f90:26-99)
+  ProjectionSolver.update_puv               projection part of UpdatePUV
+                                            (src/ComputePUV_Mod.f90:56-218)
+
+Arguments are the arrays the Fortran code holds, in the same layouts
+((nx,ny) for (1:Isize,1:Jsize), (nx+2,ny+2) for (0:Isize+1,0:Jsize+1),
+Fortran order).  numpy arrays are passed as host pointers; with
+device_ptrs=True every array must be a CUDA torch tensor (Fortran-ordered
+data, i.e. a tensor whose storage is the transpose (ny, nx) in C order, or
+any 1-D tensor with the right element count) and stays on the GPU.
+
+There is no CPU fallback: if libscf_proj.so cannot be loaded or a CUDA call
+fails, an exception is raised.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+_LIB = Path(__file__).resolve().parent / "_lib" / "libscf_proj.so"
+_lib = None
+
+SCF_OK = 0
+ERRORS = {-1: "SCF_ERR_ARG", -2: "SCF_ERR_CUDA", -3: "SCF_ERR_NAN", -4: "SCF_ERR_NOT_CONVERGED",
+          -5: "SCF_ERR_STALL", -6: "SCF_ERR_TIMEOUT", -7: "SCF_ERR_STATE", -8: "SCF_ERR_NOMEM"}
+PREC = {"fp64": 0, "mixed": 1}
+FLAG_DEVICE_PTRS = 1
+FLAG_NO_GRAPH = 2
+
+# every symbol declared in include/scf_proj.h
+EXPORTS = ["scf_opts_default", "scf_proj_create", "scf_proj_destroy", "scf_proj_set_stream",
+           "scf_proj_set_grid", "scf_proj_set_geometry", "scf_proj_assemble",
+           "scf_proj_poisson_solve", "scf_proj_update_puv", "scf_proj_get_operator",
+           "scf_proj_vcycle", "scf_proj_time_kernel", "scf_strerror"]
+
+
+class Opts(C.Structure):
+    _fields_ = [("precision", C.c_int), ("flags", C.c_int), ("device", C.c_int),
+                ("maxit", C.c_int), ("rtol", C.c_double), ("npre", C.c_int),
+                ("npost", C.c_int), ("omega", C.c_double), ("coarse_max", C.c_int),
+                ("reserved", C.c_int * 8)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("iters", C.c_int), ("status", C.c_int), ("levels", C.c_int),
+                ("fallbacks", C.c_int), ("bnorm", C.c_double), ("relres", C.c_double),
+                ("relres_true", C.c_double), ("mres_max", C.c_double), ("ms_h2d", C.c_double),
+                ("ms_assemble", C.c_double), ("ms_solve", C.c_double),
+                ("ms_correct", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ProjectionError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        self.code = code
+        msg = load().scf_strerror(code).decode() if _lib is not None else ERRORS.get(code, "?")
+        super().__init__(f"{where}: {ERRORS.get(code, code)} ({msg})")
+
+
+def load():
+    """Load libscf_proj.so (built by simcoflow_gb300.build); raises if absent."""
+    global _lib
+    if _lib is None:
+        if not _LIB.exists():
+            raise ImportError(f"{_LIB} is missing: run simcoflow_gb300.build.build_all() "
+                              "(there is no CPU fallback)")
+        L = C.CDLL(str(_LIB))
+        vp, dp, ip = C.c_void_p, C.c_void_p, C.c_void_p
+        L.scf_opts_default.argtypes = [C.POINTER(Opts)]
+        L.scf_opts_default.restype = None
+        L.scf_strerror.argtypes = [C.c_int]
+        L.scf_strerror.restype = C.c_char_p
+        L.scf_proj_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.POINTER(Opts)]
+        L.scf_proj_destroy.argtypes = [vp]
+        L.scf_proj_set_stream.argtypes = [vp, vp]
+        L.scf_proj_set_grid.argtypes = [vp, dp, dp, dp, dp]
+        L.scf_proj_set_geometry.argtypes = [vp] + [dp] * 9 + [ip, ip, ip, dp, ip, ip, dp]
+        L.scf_proj_assemble.argtypes = [vp, dp, dp, C.c_double, C.c_double, C.c_int, C.c_int,
+                                        C.c_int, C.c_int]
+        L.scf_proj_poisson_solve.argtypes = [vp, dp, dp, C.c_double, dp, C.POINTER(Stats)]
+        L.scf_proj_update_puv.argtypes = [vp, dp, dp, C.c_double, dp, dp, dp, dp, dp,
+                                          C.POINTER(Stats)]
+        L.scf_proj_get_operator.argtypes = [vp, dp, dp, dp, dp]
+        L.scf_proj_vcycle.argtypes = [vp, dp, dp]
+        L.scf_proj_time_kernel.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]
+        for name in EXPORTS:
+            f = getattr(L, name)
+            if f.restype is C.c_int or name.startswith("scf_proj"):
+                f.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _check(rc: int, where: str):
+    if rc != SCF_OK:
+        raise ProjectionError(rc, where)
+
+
+GEOMETRY_ARGS = ("vof", "phi", "vofS", "nyS", "WlLh", "aE", "aW", "aN", "aS", "posnu_p",
+                 "posnu_u", "moex_u", "vofS_u", "posnu_v", "moex_v", "vofS_v")
+
+
+class ProjectionSolver:
+    """One projection solver for an nx-by-ny grid (a handle of the C-ABI)."""
+
+    def __init__(self, nx: int, ny: int, precision: str = "fp64", device: int = 0,
+                 device_ptrs: bool = False, use_graph: bool = True, maxit: int = 200,
+                 rtol: float = 1e-8, npre: int = 2, npost: int = 2, omega: float = 1.9,
+                 coarse_max: int = 64):
+        L = load()
+        o = Opts()
+        L.scf_opts_default(C.byref(o))
+        o.precision = PREC[precision]
+        o.flags = (FLAG_DEVICE_PTRS if device_ptrs else 0) | (0 if use_graph else FLAG_NO_GRAPH)
+        o.device, o.maxit, o.rtol = device, maxit, rtol
+        o.npre, o.npost, o.omega, o.coarse_max = npre, npost, omega, coarse_max
+        self.nx, self.ny, self.device_ptrs = nx, ny, device_ptrs
+        self.opts = o
+        h = C.c_void_p()
+        _check(L.scf_proj_create(C.byref(h), nx, ny, C.byref(o)), "scf_proj_create")
+        self._h = h
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().scf_proj_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- pointers ---------------------------------------------------------
+    def _ptr(self, a, shape, dtype, name, writable=False):
+        if a is None:
+            return None
+        if self.device_ptrs:
+            import torch
+            if not (isinstance(a, torch.Tensor) and a.is_cuda):
+                raise TypeError(f"{name}: device_ptrs=True needs a CUDA tensor")
+            if a.numel() != int(np.prod(shape)):
+                raise ValueError(f"{name}: expected {np.prod(shape)} elements, got {a.numel()}")
+            tdt = {np.float64: torch.float64, np.int32: torch.int32}[dtype]
+            if a.dtype != tdt or not a.is_contiguous():
+                raise TypeError(f"{name}: needs a contiguous {tdt} tensor")
+            return a.data_ptr()
+        if not isinstance(a, np.ndarray):
+            raise TypeError(f"{name}: expected a numpy array")
+        if a.shape != tuple(shape) or a.dtype != dtype or not a.flags["F_CONTIGUOUS"]:
+            raise ValueError(f"{name}: expected Fortran-ordered {dtype.__name__}{tuple(shape)}, "
+                             f"got {a.dtype}{a.shape}")
+        if writable and not a.flags["WRITEABLE"]:
+            raise ValueError(f"{name}: array is read-only")
+        return a.ctypes.data
+
+    def _n1(self):
+        return (self.nx, self.ny)
+
+    def _n0(self):
+        return (self.nx + 2, self.ny + 2)
+
+    # -- API --------------------------------------------------------------
+    def set_stream(self, stream_ptr: int):
+        _check(load().scf_proj_set_stream(self._h, C.c_void_p(stream_ptr)), "scf_proj_set_stream")
+
+    def set_grid(self, dx, dy, dxU, dyV):
+        f = lambda a, n: self._ptr(a, self._n1(), np.float64, n)
+        self._keep["grid"] = (dx, dy, dxU, dyV)
+        _check(load().scf_proj_set_grid(self._h, f(dx, "dx"), f(dy, "dy"), f(dxU, "dxU"),
+                                        f(dyV, "dyV")), "scf_proj_set_grid")
+
+    def set_geometry(self, **g):
+        shapes = {"aE": 0, "aW": 0, "aN": 0, "aS": 0, "posnu_p": 0, "posnu_u": 0, "posnu_v": 0}
+        ptrs = []
+        for k in GEOMETRY_ARGS:
+            dt = np.int32 if k.startswith(("posnu", "moex")) else np.float64
+            shp = self._n0() if k in shapes else self._n1()
+            ptrs.append(self._ptr(g[k], shp, dt, k))
+        self._keep["geom"] = [g[k] for k in GEOMETRY_ARGS]
+        _check(load().scf_proj_set_geometry(self._h, *ptrs), "scf_proj_set_geometry")
+
+    def assemble(self, DpU, DpV, betaP: float, betaM: float, bc=(1, 1, 1, 0)):
+        f = lambda a, n: self._ptr(a, self._n0(), np.float64, n)
+        self._keep["dp"] = (DpU, DpV)
+        _check(load().scf_proj_assemble(self._h, f(DpU, "DpU"), f(DpV, "DpV"), betaP, betaM,
+                                        *bc), "scf_proj_assemble")
+
+    def poisson_equation_solver(self, ustar, vstar, vb: float = 0.0, Pp=None,
+                                check: bool = True):
+        """PoissonEquationSolver: returns (Pp, stats)."""
+        if Pp is None:
+            Pp = np.zeros(self._n0(), order="F")
+        st = Stats()
+        rc = load().scf_proj_poisson_solve(
+            self._h, self._ptr(ustar, self._n0(), np.float64, "ustar"),
+            self._ptr(vstar, self._n0(), np.float64, "vstar"), vb,
+            self._ptr(Pp, self._n0(), np.float64, "Pp", True), C.byref(st))
+        if check:
+            _check(rc, "scf_proj_poisson_solve")
+        return Pp, st
+
+    def update_puv(self, ustar, vstar, u, v, p, vb: float = 0.0, Pp=None, mres=None,
+                   check: bool = True):
+        """Projection part of UpdatePUV: corrects u, v, p in place and returns
+        (Pp, mres, stats)."""
+        if Pp is None and not self.device_ptrs:
+            Pp = np.zeros(self._n0(), order="F")
+        if mres is None:
+            mres = np.zeros(self._n1(), order="F")
+        st = Stats()
+        rc = load().scf_proj_update_puv(
+            self._h, self._ptr(ustar, self._n0(), np.float64, "ustar"),
+            self._ptr(vstar, self._n0(), np.float64, "vstar"), vb,
+            self._ptr(Pp, self._n0(), np.float64, "Pp", True),
+            self._ptr(p, self._n0(), np.float64, "p", True),
+            self._ptr(u, self._n0(), np.float64, "u", True),
+            self._ptr(v, self._n0(), np.float64, "v", True),
+            self._ptr(mres, self._n1(), np.float64, "mres", True), C.byref(st))
+        if check:
+            _check(rc, "scf_proj_update_puv")
+        return Pp, mres, st
+
+    def get_operator(self):
+        n1 = self._n1()
+        out = [np.zeros(n1, order="F") for _ in range(4)]
+        _check(load().scf_proj_get_operator(self._h, *[a.ctypes.data for a in out]),
+               "scf_proj_get_operator")
+        return dict(zip(("cE", "cN", "diag", "rhs"), out))
+
+    def vcycle(self, b):
+        x = np.zeros(self._n1(), order="F")
+        b = np.asfortranarray(b, dtype=np.float64)
+        _check(load().scf_proj_vcycle(self._h, b.ctypes.data, x.ctypes.data), "scf_proj_vcycle")
+        return x
+
+    # -- convenience --------------------------------------------------------
+    def setup_case(self, case):
+        """set_grid + set_geometry + assemble from a synth.Case (host arrays)."""
+        a = case.arrays
+        self.set_grid(a["dx"], a["dy"], a["dxU"], a["dyV"])
+        self.set_geometry(**{k: a[k] for k in GEOMETRY_ARGS})
+        self.assemble(a["DpU"], a["DpV"], case.betaP, case.betaM, case.bc)
+
+
+def project_case(case, **opts):
+    """Full projection of a synth.Case through the C-ABI with host arrays:
+    returns dict(Pp, u, v, p, mres, stats)."""
+    s = ProjectionSolver(case.nx, case.ny, **opts)
+    try:
+        s.setup_case(case)
+        a = case.arrays
+        u, v, p = a["u0"].copy(order="F"), a["v0"].copy(order="F"), a["p0"].copy(order="F")
+        Pp, mres, st = s.update_puv(a["ustar"], a["vstar"], u, v, p, case.vb)
+        return {"Pp": Pp, "u": u, "v": v, "p": p, "mres": mres, "stats": st.as_dict(),
+                "operator": s.get_operator()}
+    finally:
+        s.close()

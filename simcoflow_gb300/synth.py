@@ -1,0 +1,212 @@
+"""Seeded synthetic projection workloads.
+
+The reference publishes no benchmark inputs; every workload here is built
+from seeded random numbers with the shapes, sizes and value distributions of
+the five configurations the projection is measured on:
+
+  c1  128x128, one circle r=0.1 at (0.5,0.35), surface y=0.5+0.02 sin(2 pi x),
+      8 velocity modes, dt=1e-3 (the CPU-runnable case)
+  c2  2048x2048, three circles (centres U(0.15,0.85)^2, r U(0.04,0.1)),
+      surface y=0.5+0.03 sin(4 pi x + theta), 32 modes, dt=5e-4
+  c3  4096x4096 stretched in y (ratio 1.01 outside y in [0.45,0.55]), a
+      0.3x0.02 plate rotated 10 degrees at (0.5,0.35), two-mode surface,
+      64 modes plus a Gaussian vortex (strength 0.5, sigma 0.05), dt=2.5e-4
+  c4  learned-preconditioner cases: 512^2 training, 1024^2 / 4096^2 evaluation;
+      0-4 circles r U(0.03,0.12), amplitude U(0,0.05), wavenumber 1-6,
+      density ratio log-uniform in [10,1000]
+  c5  batch of 64 instances, sides 32*round(exp(U(ln 256, ln 1024))/32),
+      density ratio log-uniform in [10,1000], 0-4 circles, 16 modes, dt=1e-3
+
+Densities are water 1000 and air 1000/ratio (1.2 for ratio 1000:1.2); as in
+src/ComputePUV_Mod.f90:42-43 with Roref = row (src/Main.f90:148),
+betaP = 1 and betaM = rho_w/rho_a.  Dp = dt everywhere (the commented
+alternative of src/PredictorUV_mod.f90:699).  Walls W/E/S are no-slip with
+Neumann pressure; the top is open with Dirichlet p=0 (BC flags 1,1,1,0 as in
+src/ProjectionP_Mod.f90:55).  Seeds are 1000*config + instance.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import geometry as G
+
+RHO_W = 1000.0
+
+
+@dataclass
+class Case:
+    name: str
+    nx: int
+    ny: int
+    arrays: dict
+    betaP: float
+    betaM: float
+    vb: float = 0.0
+    dt: float = 1e-3
+    bc: tuple = (1, 1, 1, 0)
+    rtol: float = 1e-8
+    meta: dict = field(default_factory=dict)
+
+    def __getitem__(self, k):
+        return self.arrays[k]
+
+
+def _rng(config: int, instance: int, seed=None) -> np.random.Generator:
+    s = 1000 * config + instance if seed is None else seed
+    return np.random.Generator(np.random.PCG64(s))
+
+
+def _modes(rng, K, kmax=4):
+    a = rng.normal(0.0, 0.1, K)
+    kx = rng.integers(1, kmax + 1, K)
+    ky = rng.integers(1, kmax + 1, K)
+    th = rng.uniform(0.0, 2.0 * np.pi, K)
+    return a, kx, ky, th
+
+
+def _field(xs: np.ndarray, ys: np.ndarray, modes) -> np.ndarray:
+    """sum_k a_k sin(2 pi (kx x + ky y) + th_k) on the tensor grid xs x ys,
+    Fortran order (len(xs), len(ys)), as one matrix product."""
+    a, kx, ky, th = modes
+    ax = 2.0 * np.pi * np.outer(xs, kx) + th
+    by = 2.0 * np.pi * np.outer(ys, ky)
+    A = np.concatenate([a * np.sin(ax), a * np.cos(ax)], axis=1)
+    B = np.concatenate([np.cos(by), np.sin(by)], axis=1)
+    return np.asfortranarray(A @ B.T)
+
+
+def _velocities(g, modes_u, modes_v, vortex=None):
+    """u* at U faces (xf[i], y_j), i = 0..nx; v* at V faces (x_i, yf[j]), j = 0..ny;
+    (0:nx+1,0:ny+1) arrays with no-slip W/E/S walls and zero ghosts."""
+    xf, yf = g["xf"], g["yf"]
+    nx, ny = len(xf) - 1, len(yf) - 1
+    xc = 0.5 * (xf[1:] + xf[:-1])
+    yc = 0.5 * (yf[1:] + yf[:-1])
+    xu = np.concatenate([xf, [xf[-1]]])          # i = 0..nx+1 (ghost reuses the wall)
+    yu = np.concatenate([[yc[0]], yc, [yc[-1]]])  # j = 0..ny+1
+    xv = np.concatenate([[xc[0]], xc, [xc[-1]]])
+    yv = np.concatenate([yf, [yf[-1]]])
+    u = _field(xu, yu, modes_u)
+    v = _field(xv, yv, modes_v)
+    if vortex is not None:
+        gam, sig, x0, y0 = vortex
+        X, Y = np.meshgrid(xu, yu, indexing="ij")
+        r2 = (X - x0) ** 2 + (Y - y0) ** 2 + 1e-300
+        u += np.asfortranarray(-gam / (2 * np.pi) * (Y - y0) / r2 * (1 - np.exp(-r2 / sig**2)))
+        X, Y = np.meshgrid(xv, yv, indexing="ij")
+        r2 = (X - x0) ** 2 + (Y - y0) ** 2 + 1e-300
+        v += np.asfortranarray(gam / (2 * np.pi) * (X - x0) / r2 * (1 - np.exp(-r2 / sig**2)))
+    # ghosts and walls
+    u[:, 0] = 0.0; u[:, ny + 1] = 0.0; u[nx + 1, :] = 0.0
+    u[0, :] = 0.0; u[nx, :] = 0.0
+    v[0, :] = 0.0; v[nx + 1, :] = 0.0; v[:, ny + 1] = 0.0
+    v[:, 0] = 0.0
+    return np.asfortranarray(u), np.asfortranarray(v)
+
+
+def build_case(name, xf, yf, solids, surface, modes_u, modes_v, dt, ratio, vortex=None,
+               vb=0.0, rtol=1e-8, meta=None) -> Case:
+    g = G.build(xf, yf, solids, surface)
+    nx, ny = len(xf) - 1, len(yf) - 1
+    us, vs = _velocities(g, modes_u, modes_v, vortex)
+    arrays = {k: g[k] for k in ("dx", "dy", "dxU", "dyV", "vof", "phi", "vofS", "nyS", "WlLh",
+                                "aE", "aW", "aN", "aS", "posnu_p", "posnu_u", "moex_u",
+                                "vofS_u", "posnu_v", "moex_v", "vofS_v", "x", "y", "phiS",
+                                "nxS")}
+    arrays["DpU"] = np.full((nx + 2, ny + 2), dt, order="F")
+    arrays["DpV"] = np.full((nx + 2, ny + 2), dt, order="F")
+    arrays["ustar"], arrays["vstar"] = us, vs
+    arrays["u0"], arrays["v0"] = us.copy(order="F"), vs.copy(order="F")
+    arrays["p0"] = np.zeros((nx + 2, ny + 2), order="F")
+    m = {"n_unknowns": g["n_unknowns"], "solids": solids, "surface": surface,
+         "xf": g["xf"], "yf": g["yf"]}
+    if meta:
+        m.update(meta)
+    return Case(name, nx, ny, arrays, betaP=1.0, betaM=float(ratio), vb=vb, dt=dt, rtol=rtol,
+                meta=m)
+
+
+def _circles(rng, n, rlo, rhi):
+    out = []
+    for _ in range(n):
+        cx, cy = rng.uniform(0.15, 0.85, 2)
+        out.append(G.Solid(G.SOLID_CIRCLE, float(cx), float(cy), r=float(rng.uniform(rlo, rhi))))
+    return out
+
+
+def c1(n: int = 128, instance: int = 0, seed=None) -> Case:
+    rng = _rng(1, instance, seed)
+    xf = G.axis(n + 1, 0.0, 1.0)
+    yf = G.axis(n + 1, 0.0, 1.0)
+    solids = [G.Solid(G.SOLID_CIRCLE, 0.5, 0.35, r=0.1)]
+    surf = G.Surface(0.5, [0.02], [2 * np.pi], [0.0])
+    mu, mv = _modes(rng, 8), _modes(rng, 8)
+    return build_case("c1", xf, yf, solids, surf, mu, mv, 1e-3, RHO_W / 1.2, rtol=1e-10)
+
+
+def c2(n: int = 2048, instance: int = 0, seed=None) -> Case:
+    rng = _rng(2, instance, seed)
+    xf = G.axis(n + 1, 0.0, 1.0)
+    yf = G.axis(n + 1, 0.0, 1.0)
+    solids = _circles(rng, 3, 0.04, 0.1)
+    surf = G.Surface(0.5, [0.03], [4 * np.pi], [float(rng.uniform(0, 2 * np.pi))])
+    mu, mv = _modes(rng, 32), _modes(rng, 32)
+    return build_case("c2", xf, yf, solids, surf, mu, mv, 5e-4, RHO_W / 1.2)
+
+
+def c3(n: int = 4096, instance: int = 0, seed=None) -> Case:
+    rng = _rng(3, instance, seed)
+    xf = G.axis(n + 1, 0.0, 1.0)
+    # uniform band [0.45, 0.55] holding n - 2*round(n*496/4096) cells, geometric
+    # growth (Newton ratio ~1.01 at n=4096) outside, as Initial_Grid with
+    # NonUniformMesh=1
+    nout = int(round(n * 496 / 4096))
+    nrec = n + 1 - 2 * nout
+    yf = G.axis(n + 1, 0.0, 1.0, True, 0.45, 0.55, nrec)
+    solids = [G.Solid(G.SOLID_BOX, 0.5, 0.35, hw=0.15, hh=0.01, angle=np.deg2rad(10.0))]
+    th = rng.uniform(0, 2 * np.pi, 2)
+    surf = G.Surface(0.5, [0.02, 0.01], [2 * np.pi, 6 * np.pi], [float(th[0]), float(th[1])])
+    mu, mv = _modes(rng, 64), _modes(rng, 64)
+    return build_case("c3", xf, yf, solids, surf, mu, mv, 2.5e-4, RHO_W / 1.2,
+                      vortex=(0.5, 0.05, 0.5, 0.5))
+
+
+def random_instance(config: int, n: int, instance: int, nmodes: int = 16, dt: float = 1e-3,
+                    seed=None) -> Case:
+    """c4 / c5 style instance: 0-4 circles, sinusoidal surface, log-uniform density ratio."""
+    rng = _rng(config, instance, seed)
+    xf = G.axis(n + 1, 0.0, 1.0)
+    yf = G.axis(n + 1, 0.0, 1.0)
+    ncirc = int(rng.integers(0, 5))
+    solids = _circles(rng, ncirc, 0.03, 0.12)
+    amp = float(rng.uniform(0.0, 0.05))
+    kw = int(rng.integers(1, 7))
+    surf = G.Surface(0.5, [amp], [2 * np.pi * kw], [float(rng.uniform(0, 2 * np.pi))])
+    ratio = float(np.exp(rng.uniform(np.log(10.0), np.log(1000.0))))
+    mu, mv = _modes(rng, nmodes), _modes(rng, nmodes)
+    return build_case(f"c{config}", xf, yf, solids, surf, mu, mv, dt, ratio,
+                      meta={"ratio": ratio, "ncirc": ncirc})
+
+
+def c4(n: int = 512, instance: int = 0, seed=None) -> Case:
+    return random_instance(4, n, instance, seed=seed)
+
+
+def c5_sides(count: int = 64, seed=None) -> list[int]:
+    rng = _rng(5, 9999, seed)
+    s = np.exp(rng.uniform(np.log(256.0), np.log(1024.0), count))
+    return [int(32 * round(v / 32.0)) for v in s]
+
+
+def c5(instance: int = 0, n: int | None = None, seed=None) -> Case:
+    side = n if n is not None else c5_sides()[instance]
+    return random_instance(5, side, instance, nmodes=16, dt=1e-3, seed=seed)
+
+
+CONFIGS = {"c1": c1, "c2": c2, "c3": c3, "c4": c4, "c5": c5}
+
+
+def make_case(name: str, **kw) -> Case:
+    return CONFIGS[name](**kw)

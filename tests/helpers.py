@@ -1,0 +1,24 @@
+"""Shared helpers of the test suite."""
+from pathlib import Path
+
+import numpy as np
+
+from simcoflow_gb300 import synth
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+GOLDEN_CASES = ("c1_n16", "box25x19")
+
+
+def load_golden(name):
+    """(Case, expected outputs) of a committed golden fixture."""
+    z = np.load(GOLDEN / f"{name}.npz")
+    arrays = {k: np.asfortranarray(z[k]) for k in z.files}
+    c = synth.Case(name, int(z["nx"]), int(z["ny"]), arrays, float(z["betaP"]),
+                   float(z["betaM"]), vb=float(z["vb"]), bc=tuple(int(b) for b in z["bc"]))
+    return c, arrays
+
+
+def rel_l2(a, b):
+    d = np.linalg.norm(np.asarray(a) - np.asarray(b))
+    n = np.linalg.norm(np.asarray(b))
+    return d / n if n > 0 else d

@@ -1,0 +1,49 @@
+"""The C-ABI libraries load and export every symbol their headers declare
+(no GPU needed: no compute call is made)."""
+import ctypes
+import re
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _declared(header):
+    text = (ROOT / "include" / header).read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(scf_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_proj_library_exports_header_symbols(built):
+    from simcoflow_gb300 import build
+    lib = ctypes.CDLL(str(build.build_proj()))
+    names = _declared("scf_proj.h")
+    assert "scf_proj_update_puv" in names and "scf_proj_create" in names
+    for n in names:
+        assert hasattr(lib, n), n
+    from simcoflow_gb300 import projection
+    assert sorted(projection.EXPORTS) == sorted(n for n in names)
+
+
+def test_geom_library_exports_header_symbols(built):
+    from simcoflow_gb300 import build
+    lib = ctypes.CDLL(str(build.build_geom()))
+    for n in _declared("scf_geom.h"):
+        assert hasattr(lib, n), n
+
+
+def test_host_only_entry_points(built):
+    from simcoflow_gb300 import projection
+    L = projection.load()
+    assert L.scf_strerror(0) == b"ok"
+    assert b"NaN" in L.scf_strerror(-3)
+    o = projection.Opts()
+    L.scf_opts_default(ctypes.byref(o))
+    assert o.maxit == 200 and o.rtol == 1e-8 and o.coarse_max == 64
+    # argument checks happen before any CUDA call
+    h = ctypes.c_void_p()
+    assert L.scf_proj_create(ctypes.byref(h), 1, 5, ctypes.byref(o)) == -1
+    bad = projection.Opts()
+    L.scf_opts_default(ctypes.byref(bad))
+    bad.coarse_max = 1000
+    assert L.scf_proj_create(ctypes.byref(h), 8, 8, ctypes.byref(bad)) == -1
+    assert L.scf_proj_destroy(None) == 0

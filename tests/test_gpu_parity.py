@@ -1,0 +1,192 @@
+"""GPU parity of the projection path against the oracle, through the C-ABI.
+
+Tolerances (spec bar): pressure rel-L2 <= 1e-8, corrected velocity
+rel-L2 <= 1e-9, when both sides are driven to the FP64 floor; assembly and
+right-hand side bit for bit.
+"""
+import numpy as np
+import pytest
+
+from helpers import GOLDEN_CASES, load_golden, rel_l2
+from simcoflow_gb300 import synth
+from simcoflow_gb300 import projection as P
+
+pytestmark = pytest.mark.gpu
+
+TOL_P = 1e-8
+TOL_UV = 1e-9
+
+
+def _active(c):
+    return c["posnu_p"][1:c.nx + 1, 1:c.ny + 1] != -1
+
+
+def _gpu_project(c, **kw):
+    kw.setdefault("rtol", 1e-13)
+    kw.setdefault("maxit", 500)
+    return P.project_case(c, **kw)
+
+
+def _check_operator(c, op, matr, rhm):
+    act = _active(c)
+    cE = np.where(act, -matr[:, :, 3], 0.0) + 0.0
+    cN = np.where(act, -matr[:, :, 4], 0.0) + 0.0
+    dg = np.where(act, matr[:, :, 2], -1.0)
+    assert np.array_equal(op["cE"], cE)
+    assert np.array_equal(op["cN"], cN)
+    assert np.array_equal(op["diag"], dg)
+    assert np.array_equal(op["rhs"], rhm)
+
+
+def _check_solution(c, g, exp):
+    assert rel_l2(g["Pp"], exp["Pp"]) <= TOL_P
+    assert rel_l2(g["u"], exp["u"]) <= TOL_UV
+    assert rel_l2(g["v"], exp["v"]) <= TOL_UV
+    assert rel_l2(g["p"], exp["p"]) <= TOL_P
+    act = _active(c)
+    assert np.abs(g["mres"][act]).max() <= 1e-10
+    assert np.abs(g["mres"] - exp["mres"]).max() <= 1e-10
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_golden_fixture(cuda, name):
+    c, exp = load_golden(name)
+    g = _gpu_project(c)
+    _check_operator(c, g["operator"], exp["matr"], exp["rhm"])
+    _check_solution(c, g, exp)
+    assert g["stats"]["relres_true"] < 1e-11
+
+
+@pytest.mark.parametrize("maker", [
+    lambda: synth.c1(),
+    lambda: synth.c1(n=33),
+    lambda: synth.c4(n=40, instance=7),
+    lambda: synth.random_instance(5, 9, 3),
+    lambda: synth.c5(instance=1, n=96),
+], ids=["c1_128", "c1_33", "c4_40", "r9", "c5_96"])
+def test_parity_vs_oracle(cuda, oracle, maker):
+    c = maker()
+    exp = oracle.project(c)
+    g = _gpu_project(c)
+    _check_operator(c, g["operator"], exp["matr"], exp["rhm"])
+    _check_solution(c, g, exp)
+
+
+def test_odd_rectangular_grid(cuda, oracle):
+    from simcoflow_gb300 import geometry as G
+    rng = np.random.Generator(np.random.PCG64(11))
+    xf = G.axis(34, 0.0, 1.7)
+    yf = G.axis(18, 0.0, 0.9)
+    solids = [G.Solid(G.SOLID_CIRCLE, 0.8, 0.3, r=0.12)]
+    surf = G.Surface(0.5, [0.04], [2 * np.pi / 1.7], [0.2])
+    c = synth.build_case("odd", xf, yf, solids, surf, synth._modes(rng, 8), synth._modes(rng, 8),
+                         1e-3, 50.0, vb=-0.02)
+    exp = oracle.project(c)
+    g = _gpu_project(c)
+    _check_operator(c, g["operator"], exp["matr"], exp["rhm"])
+    _check_solution(c, g, exp)
+
+
+def test_vcycle_matches_oracle(cuda, oracle):
+    c = synth.c4(n=128, instance=4)
+    matr, _ = oracle.matrix(c)
+    rng = np.random.Generator(np.random.PCG64(5))
+    b = np.asfortranarray(rng.normal(size=(c.nx, c.ny)) * _active(c))
+    s = P.ProjectionSolver(c.nx, c.ny)
+    try:
+        s.setup_case(c)
+        xg = s.vcycle(b)
+    finally:
+        s.close()
+    xo = oracle.vcycle(c, matr, b, npre=2, npost=2, omega=1.9)
+    assert rel_l2(xg, xo) < 1e-11
+
+
+def test_deterministic_and_graph_free_path_agree(cuda):
+    c = synth.c4(n=96, instance=9)
+    a = _gpu_project(c)
+    b = _gpu_project(c)
+    n = _gpu_project(c, use_graph=False)
+    for k in ("Pp", "u", "v", "p", "mres"):
+        assert np.array_equal(a[k], b[k]), k
+        assert np.array_equal(a[k], n[k]), k
+    assert a["stats"]["iters"] == n["stats"]["iters"]
+
+
+def test_device_pointers_match_host(cuda):
+    import torch
+    c = synth.c1(n=64)
+    host = _gpu_project(c, rtol=1e-10)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a.ravel(order="F"))).to(cuda)
+    s = P.ProjectionSolver(c.nx, c.ny, device_ptrs=True, rtol=1e-10, maxit=500)
+    try:
+        A = {k: dev(v) for k, v in c.arrays.items() if isinstance(v, np.ndarray)}
+        s.set_grid(A["dx"], A["dy"], A["dxU"], A["dyV"])
+        s.set_geometry(**{k: A[k] for k in P.GEOMETRY_ARGS})
+        s.assemble(A["DpU"], A["DpV"], c.betaP, c.betaM, c.bc)
+        u, v, p = A["u0"].clone(), A["v0"].clone(), A["p0"].clone()
+        Pp = torch.zeros_like(A["p0"])
+        mres = torch.zeros(c.nx * c.ny, dtype=torch.float64, device=cuda)
+        _, _, st = s.update_puv(A["ustar"], A["vstar"], u, v, p, c.vb, Pp=Pp, mres=mres)
+        torch.cuda.synchronize()
+    finally:
+        s.close()
+    f = lambda t, shp: t.cpu().numpy().reshape(shp, order="F")
+    n0 = (c.nx + 2, c.ny + 2)
+    assert np.array_equal(f(Pp, n0), host["Pp"])
+    assert np.array_equal(f(u, n0), host["u"])
+    assert np.array_equal(f(v, n0), host["v"])
+    assert np.array_equal(f(mres, (c.nx, c.ny)), host["mres"])
+
+
+def test_zero_rhs_and_errors(cuda):
+    c = synth.c1(n=32)
+    s = P.ProjectionSolver(c.nx, c.ny)
+    try:
+        # solve before assemble: call-order error, nothing runs
+        z = np.zeros((c.nx + 2, c.ny + 2), order="F")
+        with pytest.raises(P.ProjectionError) as e:
+            s.poisson_equation_solver(z, z)
+        assert e.value.code == -7
+        s.setup_case(c)
+        Pp, st = s.poisson_equation_solver(z, z)
+        assert st.iters == 0 and np.all(Pp == 0.0)
+        bad = c["ustar"].copy(order="F")
+        bad[5, 7] = np.nan
+        with pytest.raises(P.ProjectionError) as e:
+            s.poisson_equation_solver(bad, c["vstar"])
+        assert e.value.code == -3
+        # the handle stays usable after an error
+        Pp, st = s.poisson_equation_solver(c["ustar"], c["vstar"])
+        assert st.status == 0 and st.relres_true < 1e-8
+    finally:
+        s.close()
+    s = P.ProjectionSolver(c.nx, c.ny, maxit=2, rtol=1e-14)
+    try:
+        s.setup_case(c)
+        Pp, st = s.poisson_equation_solver(c["ustar"], c["vstar"], check=False)
+        assert st.status == -4 and st.iters == 2
+    finally:
+        s.close()
+
+
+@pytest.mark.slow
+def test_full_size_c2(cuda, oracle):
+    """2048^2 at the benchmark tolerance: FP64 relative residual 1e-8, mass
+    residual at the reference's 1e-10 bound, and the pressure against a CPU
+    FP64 MG-PCG oracle solve driven to 1e-13."""
+    c = synth.c2()
+    g = _gpu_project(c, rtol=1e-8, maxit=200)
+    st = g["stats"]
+    assert st["status"] == 0
+    assert st["relres_true"] <= 1.5e-8
+    act = _active(c)
+    assert np.abs(g["mres"][act]).max() <= 1e-10
+    matr, _ = oracle.matrix(c)
+    rhm, _ = oracle.rhs(c)
+    xi, it, rel, nlev = oracle.mgpcg(c, matr, rhm, rtol=1e-13, npre=2, npost=2, omega=1.9)
+    assert rel < 1e-12
+    err = rel_l2(g["Pp"][1:-1, 1:-1], xi)
+    assert err < 1e-6, err
+    g2 = _gpu_project(c, rtol=1e-12, maxit=400)
+    assert rel_l2(g2["Pp"][1:-1, 1:-1], xi) <= TOL_P
