@@ -307,6 +307,8 @@ int solve_common(scf_proj* h, const double* ustar, const double* vstar, double v
   }
   CK(cudaEventRecord(h->ev[1], s));
   LevelView L0 = h->lev[0];
+  // the NaN flag of a previous solve must not leak into this one
+  CK(cudaMemsetAsync(&h->sc->nan, 0, sizeof(int), s));
   launch_rhs(h->fin, dus, dvs, vb, L0, h->bvec, L0.b, h->xsol, h->sc, h->part, h->opts.rtol,
              h->opts.maxit, s);
   CK(cudaGetLastError());
