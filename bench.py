@@ -212,7 +212,8 @@ def run_ours(args):
     # ---- device-resident arm ----
     tdev = {k: torch.from_numpy(np.ascontiguousarray(v.ravel(order="F"))).to(dev)
             for k, v in A.items() if isinstance(v, np.ndarray)}
-    s = P.ProjectionSolver(nx, ny, device=local, device_ptrs=True, rtol=1e-8, maxit=200)
+    s = P.ProjectionSolver(nx, ny, device=local, device_ptrs=True, rtol=1e-8, maxit=200,
+                           use_graph=not args.no_graph)
     s.set_stream(stream.cuda_stream)
     s.set_grid(tdev["dx"], tdev["dy"], tdev["dxU"], tdev["dyV"])
     s.set_geometry(**{k: tdev[k] for k in P.GEOMETRY_ARGS})
@@ -269,7 +270,8 @@ def run_ours(args):
 
     hp = {k: pinned(v) for k, v in A.items() if isinstance(v, np.ndarray)}
     H = {k: v[0] for k, v in hp.items()}
-    hs = P.ProjectionSolver(nx, ny, device=local, rtol=1e-8, maxit=200)
+    hs = P.ProjectionSolver(nx, ny, device=local, rtol=1e-8, maxit=200,
+                            use_graph=not args.no_graph)
     hs.set_stream(stream.cuda_stream)
     hu, hv, hpp = pinned(A["u0"])[0], pinned(A["v0"])[0], pinned(A["p0"])[0]
     hPp = pinned(np.zeros((nx + 2, ny + 2), order="F"))[0]
@@ -349,6 +351,7 @@ def run_ours(args):
         "config": {"workload": WORKLOADS.get(args.config, args.config), "name": args.config,
                    "nx": nx, "ny": ny, "path": "plain FP64 MG-PCG",
                    "parallelism": f"replicas x{world}",
+                   "launch": "direct launches" if args.no_graph else "CUDA graph (conditional while)",
                    "l2": "inputs larger than L2 (about 1.3 GB of arrays per projection)"},
         "solves_per_s": round(1e3 * world / ms_step, 2),
         "iters": iters[-1], "relres_true": relres[-1], "levels": levels,
@@ -371,6 +374,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="c2")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="launch the same kernels one by one instead of through the CUDA graph "
+                         "(profilers cannot see kernel nodes of graphs with conditional nodes)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
