@@ -169,6 +169,38 @@ int scf_proj_vcycle(scf_proj *h, const double *b, double *x);
 #define SCF_K_ASSEMBLE 5       /* operator assembly from the Fortran arrays */
 int scf_proj_time_kernel(scf_proj *h, int kernel, int reps, double *ms_per_launch);
 
+/* Allocation-free right-hand side.  Computes the right-hand side of the
+ * pressure equation exactly as SetPoissonVectors does
+ * (src/ProjectionP_Mod.f90:313-317) into rhs (nx,ny) (0 where Posnu = -1)
+ * and its 2-norm into *bnorm, without allocating any memory.
+ * No counterpart in the reference (SIMCOFlow builds the right-hand side on
+ * the CPU inside PoissonEquationSolver).  It is meant for callers that cannot
+ * allocate device memory where they need this value: a Fortran host that
+ * keeps all of its GPU memory in its own arena and forbids hidden
+ * cudaMalloc calls, or a time loop that must not pay the device-wide
+ * synchronisation that cudaMalloc and cudaFree can cause.
+ *  - Every array argument is a device pointer owned by the caller, in the
+ *    layouts of scf_proj_set_grid / scf_proj_set_geometry; ustar and vstar
+ *    are (nx+2,ny+2); rhs (nx,ny) and bnorm (one double) are outputs.
+ *  - Its only scratch is one fixed array inside the library (about 33 KB,
+ *    kept on every GPU that loads the library until the process exits).
+ *    nx and ny must not exceed SCF_NOALLOC_MAX_SIDE; larger grids are
+ *    rejected with SCF_ERR_ARG before anything runs.
+ *  - Asynchronous on `stream` (a cudaStream_t; NULL = default stream): the
+ *    outputs are valid once the stream has passed this call.
+ *  - The first call on each device looks up the scratch array's device
+ *    address (cudaGetSymbolAddress); make that first call on a device before
+ *    any stream capture.
+ *  - All calls share the one scratch array, which keeps the last call's
+ *    contents: calls that overlap on the GPU (different streams or host
+ *    threads) race, so the caller must serialise them. */
+#define SCF_NOALLOC_MAX_SIDE 16384
+int scf_rhs_norm_noalloc(int nx, int ny, const double *ustar, const double *vstar,
+                         const double *aE, const double *aW, const double *aN, const double *aS,
+                         const double *dx, const double *dy, const double *nyS,
+                         const double *WlLh, const int32_t *posnu_p, double vb, double *rhs,
+                         double *bnorm, void *stream);
+
 /* Human-readable text for a status code. */
 const char *scf_strerror(int code);
 

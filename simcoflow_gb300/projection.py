@@ -39,7 +39,7 @@ FLAG_NO_GRAPH = 2
 EXPORTS = ["scf_opts_default", "scf_proj_create", "scf_proj_destroy", "scf_proj_set_stream",
            "scf_proj_set_grid", "scf_proj_set_geometry", "scf_proj_assemble",
            "scf_proj_poisson_solve", "scf_proj_update_puv", "scf_proj_get_operator",
-           "scf_proj_vcycle", "scf_proj_time_kernel", "scf_strerror"]
+           "scf_proj_vcycle", "scf_proj_time_kernel", "scf_rhs_norm_noalloc", "scf_strerror"]
 
 
 class Opts(C.Structure):
@@ -93,6 +93,9 @@ def load():
         L.scf_proj_get_operator.argtypes = [vp, dp, dp, dp, dp]
         L.scf_proj_vcycle.argtypes = [vp, dp, dp]
         L.scf_proj_time_kernel.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]
+        L.scf_rhs_norm_noalloc.argtypes = [C.c_int, C.c_int] + [dp] * 10 + [ip, C.c_double, dp,
+                                                                            dp, vp]
+        L.scf_rhs_norm_noalloc.restype = C.c_int
         for name in EXPORTS:
             f = getattr(L, name)
             if f.restype is C.c_int or name.startswith("scf_proj"):
