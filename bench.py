@@ -127,15 +127,25 @@ WORKLOADS = {
     "c3": "4096x4096 y-stretched grid, rotated plate, density 1000:1.2 (plain FP64 MG-PCG)",
 }
 
-# compulsory bytes per fine cell of each measured kernel (kernel table)
-KERNEL_BYTES = {"smooth": 48, "pupdate_spmv": 56, "update_xr": 48, "resid_restrict": 40,
-                "prolong": 18}
+# compulsory bytes per fine cell of each measured kernel, per precision
+# (kernel table).  sweep = one red-black iteration (both colours)
+# in one pass; resid_restrict = sweep + residual + 2x2 restriction;
+# prolong = prolongation fused into a sweep.
+KERNEL_BYTES = {
+    "fp64": {"sweep": 48, "pupdate_spmv": 56, "update_xr": 48, "resid_restrict": 58,
+             "prolong": 50},
+    # fine level of the mixed path: x, di FP32; b is the FP64 residual; BF16 couplings
+    "mixed": {"sweep": 24, "pupdate_spmv": 52, "update_xr": 48, "resid_restrict": 29,
+              "prolong": 25},
+}
+KERNEL_IDS = (("sweep", 0), ("pupdate_spmv", 1), ("update_xr", 2), ("resid_restrict", 3),
+              ("prolong", 4))
 
 
 def kernels_per_iteration(levels: int, npre: int, npost: int) -> int:
     if levels == 1:
         return 2 + 2
-    return (levels - 1) * (2 * npre + 2 * npost + 2) + 1 + 2
+    return (levels - 1) * (npre + npost) + 1 + 2
 
 
 def cpu_projection_ms(case, threads: int) -> tuple[float, dict]:
@@ -187,6 +197,7 @@ def run_reference(args):
 
 
 def run_ours(args):
+    import ctypes
     import torch
     world, rank, local = _dist()
     from simcoflow_gb300 import build as B
@@ -202,6 +213,7 @@ def run_ours(args):
     case = make_case(args.config, rank)
     A = case.arrays
     nx, ny = case.nx, case.ny
+    cells = nx * ny
     stream = torch.cuda.Stream(device=dev)
 
     def barrier():
@@ -209,30 +221,41 @@ def run_ours(args):
             pg.barrier()
         torch.cuda.synchronize(dev)
 
-    # ---- device-resident arm ----
+    def max_over_ranks(x):
+        if pg:
+            t = torch.tensor([x], device=dev)
+            pg.all_reduce(t, op=pg.ReduceOp.MAX)
+            return float(t.item())
+        return x
+
     tdev = {k: torch.from_numpy(np.ascontiguousarray(v.ravel(order="F"))).to(dev)
             for k, v in A.items() if isinstance(v, np.ndarray)}
-    s = P.ProjectionSolver(nx, ny, device=local, device_ptrs=True, rtol=1e-8, maxit=200,
-                           use_graph=not args.no_graph)
-    s.set_stream(stream.cuda_stream)
-    s.set_grid(tdev["dx"], tdev["dy"], tdev["dxU"], tdev["dyV"])
-    s.set_geometry(**{k: tdev[k] for k in P.GEOMETRY_ARGS})
-    u, v, p = tdev["u0"].clone(), tdev["v0"].clone(), tdev["p0"].clone()
-    Pp = torch.zeros_like(tdev["p0"])
-    mres = torch.zeros(nx * ny, dtype=torch.float64, device=dev)
 
-    def step():
-        s.assemble(tdev["DpU"], tdev["DpV"], case.betaP, case.betaM, case.bc)
-        _, _, st = s.update_puv(tdev["ustar"], tdev["vstar"], u, v, p, case.vb, Pp=Pp,
-                                mres=mres)
-        return st
+    def device_arm(precision, sample_clocks):
+        """Device-resident projections: inputs in HBM, device pointers."""
+        s = P.ProjectionSolver(nx, ny, precision=precision, device=local, device_ptrs=True,
+                               rtol=1e-8, maxit=200, use_graph=not args.no_graph)
+        s.set_stream(stream.cuda_stream)
+        s.set_grid(tdev["dx"], tdev["dy"], tdev["dxU"], tdev["dyV"])
+        s.set_geometry(**{k: tdev[k] for k in P.GEOMETRY_ARGS})
+        u, v, p = tdev["u0"].clone(), tdev["v0"].clone(), tdev["p0"].clone()
+        Pp = torch.zeros_like(tdev["p0"])
+        mres = torch.zeros(cells, dtype=torch.float64, device=dev)
 
-    for _ in range(args.warmup):
-        st = step()
-    barrier()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    iters, relres = [], []
-    with ClockSampler(local) as clk:
+        def step():
+            s.assemble(tdev["DpU"], tdev["DpV"], case.betaP, case.betaM, case.bc)
+            _, _, st = s.update_puv(tdev["ustar"], tdev["vstar"], u, v, p, case.vb, Pp=Pp,
+                                    mres=mres)
+            return st
+
+        for _ in range(args.warmup):
+            st = step()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        iters, relres = [], []
+        clk = ClockSampler(local) if sample_clocks else None
+        if clk:
+            clk.__enter__()
         barrier()
         e0.record(stream)
         for _ in range(args.steps):
@@ -241,26 +264,22 @@ def run_ours(args):
             relres.append(st.relres_true)
         e1.record(stream)
         barrier()
-    ms_total = e0.elapsed_time(e1)
-    if pg:
-        t = torch.tensor([ms_total], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms_total = float(t.item())
-    ms_step = ms_total / args.steps
-    levels = st.levels
+        if clk:
+            clk.__exit__()
+        ms = max_over_ranks(e0.elapsed_time(e1)) / args.steps
+        kt = {}
+        for name, kid in KERNEL_IDS:  # live per-kernel timing on the same data
+            out = ctypes.c_double(0.0)
+            if P.load().scf_proj_time_kernel(s._h, kid, 50, ctypes.byref(out)) == 0:
+                kt[name] = out.value
+        s.close()
+        return {"ms": ms, "iters": iters, "relres": relres, "levels": st.levels, "kt": kt,
+                "clk": clk.summary() if clk else None}
 
-    # per-kernel live timing on the same data (back-to-back launches)
-    kt = {}
-    for name, kid in (("smooth", 0), ("pupdate_spmv", 1), ("update_xr", 2),
-                      ("resid_restrict", 3), ("prolong", 4)):
-        import ctypes
-        out = ctypes.c_double(0.0)
-        rc = P.load().scf_proj_time_kernel(s._h, kid, 50, ctypes.byref(out))
-        if rc == 0:
-            kt[name] = out.value
-    s.close()
+    plain = device_arm("fp64", False)
+    mixed = device_arm("mixed", True)
 
-    # ---- end-to-end arm: host (pinned) buffers through the C-ABI ----
+    # ---- end-to-end: the headline (mixed) path through host (pinned) buffers ----
     def pinned(a):
         t = torch.empty(a.size, dtype=torch.float64 if a.dtype == np.float64 else torch.int32)
         t = t.pin_memory()
@@ -270,7 +289,7 @@ def run_ours(args):
 
     hp = {k: pinned(v) for k, v in A.items() if isinstance(v, np.ndarray)}
     H = {k: v[0] for k, v in hp.items()}
-    hs = P.ProjectionSolver(nx, ny, device=local, rtol=1e-8, maxit=200,
+    hs = P.ProjectionSolver(nx, ny, precision="mixed", device=local, rtol=1e-8, maxit=200,
                             use_graph=not args.no_graph)
     hs.set_stream(stream.cuda_stream)
     hu, hv, hpp = pinned(A["u0"])[0], pinned(A["v0"])[0], pinned(A["p0"])[0]
@@ -296,11 +315,7 @@ def run_ours(args):
         e2e_step()
     f1.record(stream)
     barrier()
-    e2e_ms = f0.elapsed_time(f1) / args.steps
-    if pg:
-        t = torch.tensor([e2e_ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(f0.elapsed_time(f1)) / args.steps
     hs.close()
 
     if rank != 0:
@@ -309,33 +324,40 @@ def run_ours(args):
         return 0
 
     peak, peak_kind = _peaks()
-    cells = nx * ny
-    dom = "smooth"
+
+    def kernel_table(arm, prec):
+        return {k: {"ms": round(v, 5),
+                    "GBps": round(KERNEL_BYTES[prec][k] * cells / (v * 1e-3) / 1e9, 1)}
+                for k, v in arm["kt"].items()}
+
+    # dominant kernel of the headline path: the fine-level sweep (4 of them per
+    # V-cycle on the fine grid, plus the fused restrict / prolong variants)
+    dom = "sweep"
     roof = None
-    if dom in kt and kt[dom] > 0:
-        bytes_launch = KERNEL_BYTES[dom] * cells
-        achieved = bytes_launch / (kt[dom] * 1e-3) / 1e9
+    if dom in mixed["kt"] and mixed["kt"][dom] > 0:
+        bytes_launch = KERNEL_BYTES["mixed"][dom] * cells
+        achieved = bytes_launch / (mixed["kt"][dom] * 1e-3) / 1e9
         traffic = None
         tf = ROOT / "profiles" / "traffic.json"
         if tf.exists():
             try:
-                traffic = json.loads(tf.read_text()).get(f"{dom}_{args.config}")
+                traffic = json.loads(tf.read_text()).get(f"mixed_{dom}_{args.config}")
             except Exception:
                 traffic = None
-        roof = {"bound": "hbm", "kernel": "k_smooth (red-black Gauss-Seidel half sweep, fine grid)",
+        roof = {"bound": "hbm",
+                "kernel": "k_sweep<float,bf16,double> (fused red-black iteration, fine grid)",
                 "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                "bytes_per_launch": bytes_launch, "ms_per_launch": kt[dom],
+                "bytes_per_launch": bytes_launch, "ms_per_launch": mixed["kt"][dom],
                 "traffic": traffic,
                 "kernel_timing": "CUDA events around 50 back-to-back launches on the solver "
                                  "stream, right after the timed region, same data"}
-    kernels = {k: {"ms": round(v, 5), "GBps": round(KERNEL_BYTES[k] * cells / (v * 1e-3) / 1e9, 1)}
-               for k, v in kt.items()}
-    per_it = kernels_per_iteration(levels, 2, 2)
     launches = 0
-    for it in iters:
-        launches += (levels - 1) + 3 + 1 + 3  # assemble, excess, coarsen, coarse setup, rhs, final x3
-        launches += ((it + 1) // 2) * 2 * per_it
+    for arm in (mixed,):
+        per_it = kernels_per_iteration(arm["levels"], 2, 2)
+        for it in arm["iters"]:
+            launches += arm["levels"] + 3 + 1 + 3 + 2 * arm["levels"]  # setup, rhs, final
+            launches += ((it + 1) // 2) * 2 * per_it
     cpu = None
     if world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -343,22 +365,29 @@ def run_ours(args):
         cpu = {"value": round(ms_cpu, 2), "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"one full {nx}x{ny} projection (C restatement of the reference path, "
                          f"OpenMP, {info['iters']} MG-PCG iterations)"}
+    ms_step = mixed["ms"]
     line = {
         "metric": METRIC, "value": round(ms_step, 4), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded; shapes and distributions of the named config)",
         "config": {"workload": WORKLOADS.get(args.config, args.config), "name": args.config,
-                   "nx": nx, "ny": ny, "path": "plain FP64 MG-PCG",
+                   "nx": nx, "ny": ny,
+                   "path": "FP64 flexible PCG + FP32/BF16 multigrid (mixed)",
                    "parallelism": f"replicas x{world}",
                    "launch": "direct launches" if args.no_graph else "CUDA graph (conditional while)",
                    "l2": "inputs larger than L2 (about 1.3 GB of arrays per projection)"},
         "solves_per_s": round(1e3 * world / ms_step, 2),
-        "iters": iters[-1], "relres_true": relres[-1], "levels": levels,
+        "iters": mixed["iters"][-1], "relres_true": mixed["relres"][-1],
+        "levels": mixed["levels"],
+        "plain_fp64_mg_pcg": {"ms": round(plain["ms"], 4), "iters": plain["iters"][-1],
+                              "relres_true": plain["relres"][-1],
+                              "kernels": kernel_table(plain, "fp64")},
+        "speedup_vs_plain": round(plain["ms"] / ms_step, 3),
         "e2e": {"value": round(e2e_ms, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
-        "roofline": roof, "kernels": kernels, "gpu_launches": int(launches),
-        "cpu_baseline": cpu, "clocks": clk.summary(),
+        "roofline": roof, "kernels": kernel_table(mixed, "mixed"),
+        "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": mixed["clk"],
     }
     print(json.dumps(line), flush=True)
     if pg:

@@ -86,15 +86,6 @@ void launch_coarse_setup(LevelView C, double* Ainv, int* cmap, int* nc, cudaStre
 void launch_rhs(const FortranIn& in, const double* ustar, const double* vstar, double vb,
                 LevelView L0, double* bvec, double* r, double* x, Scalars* sc, double* part,
                 double rtol, int maxit, cudaStream_t s);
-void launch_smooth(LevelView L, int color, int zero_init, int do_rz, Scalars* sc, double* part,
-                   cudaStream_t s);
-void launch_resid_restrict(LevelView F, LevelView C, Scalars* sc, cudaStream_t s);
-void launch_prolong(LevelView F, LevelView C, double omega, Scalars* sc, cudaStream_t s);
-void launch_coarse_solve(LevelView C, const double* Ainv, const int* cmap, const int* nc,
-                         Scalars* sc, cudaStream_t s);
-void launch_dot_rz(LevelView L0, Scalars* sc, double* part, cudaStream_t s);
-void launch_pupdate_spmv(LevelView L0, const double* z, const double* pold, double* pnew,
-                         double* q, Scalars* sc, double* part, cudaStream_t s);
 void launch_update_xr(LevelView L0, double* x, const double* p, double* r, const double* q,
                       Scalars* sc, double* part, unsigned long long cond, cudaStream_t s);
 void launch_final_solution(const FortranIn& in, LevelView L0, const double* x,
@@ -106,5 +97,6 @@ void launch_final_mres(const FortranIn& in, double vb, double* u, double* v, dou
 void launch_final_zero(const FortranIn& in, double* p, double* u, double* v, cudaStream_t s);
 void launch_to_fortran(LevelView L, const double* src, double* dst, cudaStream_t s);
 void launch_from_fortran(LevelView L, const double* src, double* dst, cudaStream_t s);
+void launch_to_fortran_f(LevelView L, const float* src, double* dst, cudaStream_t s);
 
 }  // namespace scf

@@ -305,26 +305,6 @@ __global__ void k_coarse_setup(LevelView C, double* Ainv, int* cmap, int* nc_out
   if (t == 0) *nc_out = nn;
 }
 
-__global__ void k_coarse_solve(LevelView C, const double* Ainv, const int* cmap, const int* ncp,
-                               Scalars* sc) {
-  if (sc && sc->done) return;
-  __shared__ double bd[kMaxCoarse];
-  const int t = threadIdx.x;
-  const int ncell = C.nx * C.ny, nn = *ncp;
-  for (int k = t; k < ncell; k += blockDim.x) {
-    int r = cmap[k];
-    if (r >= 0) bd[r] = C.b[(size_t)(k / C.nx) * C.pitch + (k % C.nx)];
-  }
-  __syncthreads();
-  for (int k = t; k < ncell; k += blockDim.x) {
-    int r = cmap[k];
-    double y = 0.0;
-    if (r >= 0)
-      for (int c = 0; c < nn; ++c) y = fma(Ainv[r * nn + c], bd[c], y);
-    C.x[(size_t)(k / C.nx) * C.pitch + (k % C.nx)] = y;
-  }
-}
-
 // ---------------------------------------------------------------------------
 // Right-hand side: SetPoissonVectors (src/ProjectionP_Mod.f90:306-337).
 // Also starts the PCG: r = b, x = 0, scalars reset.
@@ -374,157 +354,8 @@ __global__ void k_rhs(FortranIn in, const double* us, const double* vs, double v
 }
 
 // ---------------------------------------------------------------------------
-// Multigrid V-cycle kernels.
+// PCG vector update.
 // ---------------------------------------------------------------------------
-
-// One red-black Gauss-Seidel half sweep updating cells with (ix+iy)%2 == color.
-// zero_init: the iterate starts at zero (the other colour is written as 0).
-// do_rz: also reduce r.z over the level (level 0 is the PCG: b = r, x = z)
-// and compute the PCG beta.
-__global__ void k_smooth(LevelView L, int color, int zero_init, int do_rz, Scalars* sc,
-                         double* part) {
-  if (sc->done) return;
-  const int ix0 = 2 * (blockIdx.x * kBX + threadIdx.x);
-  const int P = L.pitch;
-  double acc = 0.0;
-  if (ix0 < L.nx) {
-    for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY) {
-      const int ix = ix0 + ((iy + color) & 1);
-      const int io = ix0 + ((iy + color + 1) & 1);
-      const size_t row = (size_t)iy * P;
-      if (zero_init && io < L.nx) L.x[row + io] = 0.0;
-      if (ix < L.nx) {
-        const size_t k = row + ix;
-        const double d = L.dg[k];
-        double s = L.b[k];
-        if (!zero_init) {
-          s = add(s, mul(L.cE[k], L.x[k + 1]));
-          s = add(s, mul(L.cE[k - 1], L.x[k - 1]));
-          s = add(s, mul(L.cN[k], L.x[k + P]));
-          s = add(s, mul(L.cN[k - P], L.x[k - P]));
-        }
-        const double xn = d > 0.0 ? dvd(s, d) : 0.0;
-        L.x[k] = xn;
-        if (do_rz) acc = fma(L.b[k], xn, acc);
-      }
-      if (do_rz && io < L.nx) acc = fma(L.b[row + io], L.x[row + io], acc);
-    }
-  }
-  if (!do_rz) return;
-  double tot;
-  if (grid_reduce<false>(acc, part, &sc->tickets[T_RZ], &tot) && tid2() == 0) {
-    sc->beta = (sc->iter == 0) ? 0.0 : tot / sc->rz;
-    sc->rz = tot;
-  }
-}
-
-// residual of the fine level, summed over each 2x2 aggregate into C.b
-__global__ void k_resid_restrict(LevelView F, LevelView C, Scalars* sc) {
-  if (sc && sc->done) return;
-  const int I = blockIdx.x * kBX + threadIdx.x;
-  if (I >= C.nx) return;
-  const int nxf = F.nx, nyf = F.ny, P = F.pitch;
-  for (int J = blockIdx.y * kBY + threadIdx.y; J < C.ny; J += gridDim.y * kBY) {
-    double s = 0.0;
-    for (int dj = 0; dj < 2; ++dj)
-      for (int di = 0; di < 2; ++di) {
-        int ix = 2 * I + di, iy = 2 * J + dj;
-        if (ix >= nxf || iy >= nyf) continue;
-        size_t k = (size_t)iy * P + ix;
-        double r = 0.0;
-        if (F.dg[k] >= 0.0) {
-          r = sub(F.b[k], mul(F.dg[k], F.x[k]));
-          r = add(r, mul(F.cE[k], F.x[k + 1]));
-          r = add(r, mul(F.cE[k - 1], F.x[k - 1]));
-          r = add(r, mul(F.cN[k], F.x[k + P]));
-          r = add(r, mul(F.cN[k - P], F.x[k - P]));
-        }
-        s = add(s, r);
-      }
-    C.b[(size_t)J * C.pitch + I] = s;
-  }
-}
-
-// x_f += omega * x_c(parent) on cells with an unknown
-__global__ void k_prolong(LevelView F, LevelView C, double omega, Scalars* sc) {
-  if (sc && sc->done) return;
-  const int ix0 = 2 * (blockIdx.x * kBX + threadIdx.x);
-  if (ix0 >= F.nx) return;
-  for (int iy = blockIdx.y * kBY + threadIdx.y; iy < F.ny; iy += gridDim.y * kBY) {
-    const double xc = C.x[(size_t)(iy >> 1) * C.pitch + (ix0 >> 1)];
-    const double corr = mul(omega, xc);
-    for (int c = 0; c < 2; ++c) {
-      int ix = ix0 + c;
-      if (ix >= F.nx) break;
-      size_t k = (size_t)iy * F.pitch + ix;
-      if (F.dg[k] >= 0.0) F.x[k] = add(F.x[k], corr);
-    }
-  }
-}
-
-// r.z when the V-cycle does not end with a smoothing sweep
-__global__ void k_dot_rz(LevelView L, Scalars* sc, double* part) {
-  if (sc->done) return;
-  const int ix0 = 2 * (blockIdx.x * kBX + threadIdx.x);
-  double acc = 0.0;
-  if (ix0 < L.nx)
-    for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY)
-      for (int c = 0; c < 2 && ix0 + c < L.nx; ++c) {
-        size_t k = (size_t)iy * L.pitch + ix0 + c;
-        acc = fma(L.b[k], L.x[k], acc);
-      }
-  double tot;
-  if (grid_reduce<false>(acc, part, &sc->tickets[T_RZ], &tot) && tid2() == 0) {
-    sc->beta = (sc->iter == 0) ? 0.0 : tot / sc->rz;
-    sc->rz = tot;
-  }
-}
-
-// ---------------------------------------------------------------------------
-// PCG vector kernels.
-// ---------------------------------------------------------------------------
-
-// p_new = z + beta p_old (p_new = z on the first iteration), q = A p_new,
-// reduce p.q and set alpha = r.z / p.q.  Neighbour values of p_new are
-// recomputed from z and p_old, so p_old and p_new must be different buffers.
-__global__ void k_pupdate_spmv(LevelView L, const double* __restrict__ z,
-                               const double* __restrict__ pold, double* __restrict__ pnew,
-                               double* __restrict__ q, Scalars* sc, double* part) {
-  if (sc->done) return;
-  const int ix0 = 2 * (blockIdx.x * kBX + threadIdx.x);
-  const int P = L.pitch;
-  const bool first = sc->iter == 0;
-  const double beta = sc->beta;
-  double acc = 0.0;
-  if (ix0 < L.nx) {
-    for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY) {
-      const size_t k0 = (size_t)iy * P + ix0;
-      auto pn = [&](size_t k) { return first ? z[k] : fma(beta, pold[k], z[k]); };
-      double pw = pn(k0 - 1), pc0 = pn(k0), pc1 = pn(k0 + 1), pe = pn(k0 + 2);
-      double ps0 = pn(k0 - P), ps1 = pn(k0 - P + 1), pn0 = pn(k0 + P), pn1 = pn(k0 + P + 1);
-      const double2 dg = *reinterpret_cast<const double2*>(L.dg + k0);
-      const double2 ce = *reinterpret_cast<const double2*>(L.cE + k0);
-      const double2 cn = *reinterpret_cast<const double2*>(L.cN + k0);
-      const double2 cs = *reinterpret_cast<const double2*>(L.cN + k0 - P);
-      const double cw = L.cE[k0 - 1];
-      double q0 = fmax(dg.x, 0.0) * pc0 - ce.x * pc1 - cw * pw - cn.x * pn0 - cs.x * ps0;
-      double q1 = fmax(dg.y, 0.0) * pc1 - ce.y * pe - ce.x * pc0 - cn.y * pn1 - cs.y * ps1;
-      pnew[k0] = pc0;
-      q[k0] = q0;
-      acc = fma(pc0, q0, acc);
-      if (ix0 + 1 < L.nx) {
-        pnew[k0 + 1] = pc1;
-        q[k0 + 1] = q1;
-        acc = fma(pc1, q1, acc);
-      }
-    }
-  }
-  double tot;
-  if (grid_reduce<false>(acc, part, &sc->tickets[T_PQ], &tot) && tid2() == 0) {
-    sc->pq = tot;
-    sc->alpha = sc->rz / tot;
-  }
-}
 
 // x += alpha p, r -= alpha q, reduce r.r; the last block advances the
 // iteration count, tests convergence and, inside a graph loop, clears the
@@ -733,6 +564,12 @@ __global__ void k_to_fortran(LevelView L, const double* src, double* dst) {
   for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY)
     dst[(size_t)ix + (size_t)iy * L.nx] = src[(size_t)iy * L.pitch + ix];
 }
+__global__ void k_to_fortran_f(LevelView L, const float* src, double* dst) {
+  const int ix = blockIdx.x * kBX + threadIdx.x;
+  if (ix >= L.nx) return;
+  for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY)
+    dst[(size_t)ix + (size_t)iy * L.nx] = (double)src[(size_t)iy * L.pitch + ix];
+}
 __global__ void k_from_fortran(LevelView L, const double* src, double* dst) {
   const int ix = blockIdx.x * kBX + threadIdx.x;
   if (ix >= L.nx) return;
@@ -765,27 +602,6 @@ void launch_rhs(const FortranIn& in, const double* ustar, const double* vstar, d
   k_rhs<<<grid_for(in.nx, in.ny, 1), kBlock, 0, s>>>(in, ustar, vstar, vb, L0.pitch, bvec, r, x,
                                                       sc, part, rtol, maxit);
 }
-void launch_smooth(LevelView L, int color, int zero_init, int do_rz, Scalars* sc, double* part,
-                   cudaStream_t s) {
-  k_smooth<<<grid_for(L.nx, L.ny), kBlock, 0, s>>>(L, color, zero_init, do_rz, sc, part);
-}
-void launch_resid_restrict(LevelView F, LevelView C, Scalars* sc, cudaStream_t s) {
-  k_resid_restrict<<<grid_for(C.nx, C.ny, 1), kBlock, 0, s>>>(F, C, sc);
-}
-void launch_prolong(LevelView F, LevelView C, double omega, Scalars* sc, cudaStream_t s) {
-  k_prolong<<<grid_for(F.nx, F.ny), kBlock, 0, s>>>(F, C, omega, sc);
-}
-void launch_coarse_solve(LevelView C, const double* Ainv, const int* cmap, const int* nc,
-                         Scalars* sc, cudaStream_t s) {
-  k_coarse_solve<<<1, 64, 0, s>>>(C, Ainv, cmap, nc, sc);
-}
-void launch_dot_rz(LevelView L0, Scalars* sc, double* part, cudaStream_t s) {
-  k_dot_rz<<<grid_for(L0.nx, L0.ny), kBlock, 0, s>>>(L0, sc, part);
-}
-void launch_pupdate_spmv(LevelView L0, const double* z, const double* pold, double* pnew,
-                         double* q, Scalars* sc, double* part, cudaStream_t s) {
-  k_pupdate_spmv<<<grid_for(L0.nx, L0.ny), kBlock, 0, s>>>(L0, z, pold, pnew, q, sc, part);
-}
 void launch_update_xr(LevelView L0, double* x, const double* p, double* r, const double* q,
                       Scalars* sc, double* part, unsigned long long cond, cudaStream_t s) {
   k_update_xr<<<grid_for(L0.nx, L0.ny), kBlock, 0, s>>>(L0, x, p, r, q, sc, part, cond);
@@ -806,6 +622,9 @@ void launch_final_zero(const FortranIn& in, double* p, double* u, double* v, cud
 }
 void launch_to_fortran(LevelView L, const double* src, double* dst, cudaStream_t s) {
   k_to_fortran<<<grid_for(L.nx, L.ny, 1), kBlock, 0, s>>>(L, src, dst);
+}
+void launch_to_fortran_f(LevelView L, const float* src, double* dst, cudaStream_t s) {
+  k_to_fortran_f<<<grid_for(L.nx, L.ny, 1), kBlock, 0, s>>>(L, src, dst);
 }
 void launch_from_fortran(LevelView L, const double* src, double* dst, cudaStream_t s) {
   k_from_fortran<<<grid_for(L.nx, L.ny, 1), kBlock, 0, s>>>(L, src, dst);

@@ -1,0 +1,442 @@
+// scf_mg.cu -- multigrid V-cycle kernels, templated on precision:
+//   <double, double, double>           plain FP64 preconditioner
+//   <float, bf16, double | float>      mixed: FP32 state, BF16 couplings; the
+//                                      fine level reads the FP64 residual
+// and the PCG direction update, templated on the type of z.
+//
+// Every smoothing pass is a temporally blocked red-black Gauss-Seidel sweep:
+// one CTA owns a 64x32 tile, loads x with a halo into shared memory, updates
+// the first colour on the tile plus a ring, syncs, updates the second colour
+// on the tile (plus a ring when the residual follows), and writes the tile
+// back once.  Ring cells are recomputed from the same inputs as the
+// neighbouring CTA computes them, so the result equals the two half sweeps
+// of a global red-black iteration.  Optional fusions:
+//   ZERO      the iterate starts at zero (no x read)
+//   PROLONG   x += omega * x_coarse(parent) while loading (cells with an unknown)
+//   RESTRICT  after the sweep, the residual of the tile is summed 2x2 onto
+//             the coarse right-hand side (needs a 3-cell halo)
+//   RZ        r.z (and r.z_old for the flexible PCG) reduced over the grid,
+//             then the PCG beta
+#include "scf_mg.cuh"
+
+namespace scf {
+namespace {
+
+constexpr int SX = 64, SY = 32, NT = 256;
+
+template <class CT, class T>
+__device__ __forceinline__ T cload(const CT* p, size_t k, float cs);
+template <>
+__device__ __forceinline__ double cload<double, double>(const double* p, size_t k, float) {
+  return p[k];
+}
+template <>
+__device__ __forceinline__ float cload<__nv_bfloat16, float>(const __nv_bfloat16* p, size_t k,
+                                                               float cs) {
+  return __bfloat162float(p[k]) * cs;
+}
+
+__device__ __forceinline__ int tlin() { return threadIdx.y * blockDim.x + threadIdx.x; }
+
+__device__ double block_sum256(double v) {
+  __shared__ double sm[NT / 32];
+  __syncthreads();
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int t = tlin();
+  if ((t & 31) == 0) sm[t >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (t == 0)
+    for (int w = 0; w < NT / 32; ++w) s += sm[w];
+  return s;
+}
+
+// two sums over the grid, last-block combine in block order (deterministic)
+__device__ bool grid_sum2(double a, double b, double* part, unsigned* ticket, double* ta,
+                          double* tb) {
+  __shared__ bool last;
+  const int t = tlin();
+  const unsigned nb = gridDim.x * gridDim.y;
+  const unsigned bid = blockIdx.y * gridDim.x + blockIdx.x;
+  const double sa = block_sum256(a);
+  const double sb = block_sum256(b);
+  if (t == 0) {
+    part[2 * bid] = sa;
+    part[2 * bid + 1] = sb;
+    __threadfence();
+    last = (atomicAdd(ticket, 1u) == nb - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double xa = 0.0, xb = 0.0;
+  for (unsigned k = t; k < nb; k += NT) {
+    xa += __ldcg(&part[2 * k]);
+    xb += __ldcg(&part[2 * k + 1]);
+  }
+  xa = block_sum256(xa);
+  xb = block_sum256(xb);
+  if (t == 0) {
+    *ta = xa;
+    *tb = xb;
+    *ticket = 0u;
+  }
+  return true;
+}
+
+// PCG beta from r.z_new (and r.z_old): plain beta = rz_new / rz_old;
+// flexible (Polak-Ribiere) beta = (r.z_new - r.z_old) / rz_old
+__device__ __forceinline__ void set_beta(Scalars* sc, double rz_new, double rz_cross,
+                                         int flexible) {
+  if (sc->iter == 0) sc->beta = 0.0;
+  else sc->beta = (flexible ? (rz_new - rz_cross) : rz_new) / sc->rz;
+  sc->rz = rz_new;
+}
+
+template <class T, class CT, class BT, int FIRST, bool ZERO, bool PROLONG, bool RESTRICT, bool RZ>
+__global__ void __launch_bounds__(NT)
+k_sweep(MgView<T, CT, BT> L, MgView<T, CT, T> C, T omega, const T* __restrict__ zold,
+        int flexible, Scalars* sc, double* part) {
+  if (sc->done) return;
+  constexpr int H = RESTRICT ? 3 : 2;  // x halo
+  constexpr int WX = SX + 2 * H, WY = SY + 2 * H;
+  __shared__ T xs[WY][WX];
+  const int nx = L.nx, ny = L.ny, P = L.pitch;
+  const int x0 = blockIdx.x * SX, y0 = blockIdx.y * SY;
+  const int t = tlin();
+  const float cs = L.csp ? __ldg(L.csp) : 1.0f;
+
+  // phase 0: x with halo; outside the grid the value is zero
+  for (int e = t; e < WX * WY; e += NT) {
+    const int ex = e % WX, ey = e / WX;
+    const int gx = x0 - H + ex, gy = y0 - H + ey;
+    T v = T(0);
+    if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
+      const size_t g = (size_t)gy * P + gx;
+      if (!ZERO) v = L.x[g];
+      if (PROLONG) {
+        if (L.di[g] > T(0)) v = fma(omega, C.x[(size_t)(gy >> 1) * C.pitch + (gx >> 1)], v);
+      }
+    }
+    xs[ey][ex] = v;
+  }
+  __syncthreads();
+
+  auto relax = [&](int gx, int gy) {
+    const size_t g = (size_t)gy * P + gx;
+    const int lx = gx - x0 + H, ly = gy - y0 + H;
+    T s = (T)L.b[g];
+    s = fma(cload<CT, T>(L.cE, g, cs), xs[ly][lx + 1], s);
+    s = fma(cload<CT, T>(L.cE, g - 1, cs), xs[ly][lx - 1], s);
+    s = fma(cload<CT, T>(L.cN, g, cs), xs[ly + 1][lx], s);
+    s = fma(cload<CT, T>(L.cN, g - P, cs), xs[ly - 1][lx], s);
+    xs[ly][lx] = s * L.di[g];
+  };
+
+  // phase 1: first colour on the tile plus a ring of width H-1
+  {
+    constexpr int R = H - 1;
+    constexpr int CW = (SX + 2 * R) / 2, RH = SY + 2 * R;
+    for (int e = t; e < CW * RH; e += NT) {
+      const int k = e % CW, ey = e / CW;
+      const int gy = y0 - R + ey;
+      const int gx = x0 - R + ((x0 - R + gy + FIRST) & 1) + 2 * k;
+      if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) relax(gx, gy);
+    }
+  }
+  __syncthreads();
+  // phase 2: second colour on the tile plus a ring of width H-2
+  {
+    constexpr int R = H - 2;
+    constexpr int CW = (SX + 2 * R) / 2, RH = SY + 2 * R;
+    for (int e = t; e < CW * RH; e += NT) {
+      const int k = e % CW, ey = e / CW;
+      const int gy = y0 - R + ey;
+      const int gx = x0 - R + ((x0 - R + gy + (1 - FIRST)) & 1) + 2 * k;
+      if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) relax(gx, gy);
+    }
+  }
+  __syncthreads();
+
+  // phase 3: write the tile; optional r.z
+  double a1 = 0.0, a2 = 0.0;
+  for (int e = t; e < SX * SY; e += NT) {
+    const int ex = e % SX, ey = e / SX;
+    const int gx = x0 + ex, gy = y0 + ey;
+    if (gx < nx && gy < ny) {
+      const size_t g = (size_t)gy * P + gx;
+      const T v = xs[ey + H][ex + H];
+      L.x[g] = v;
+      if (RZ) {
+        const double rb = (double)L.b[g];
+        a1 = fma(rb, (double)v, a1);
+        if (flexible) a2 = fma(rb, (double)zold[g], a2);
+      }
+    }
+  }
+
+  if (RESTRICT) {
+    // residual of each tile cell, summed 2x2 onto the coarse level
+    const int I0 = x0 >> 1, J0 = y0 >> 1;
+    for (int e = t; e < (SX / 2) * (SY / 2); e += NT) {
+      const int ci = e % (SX / 2), cj = e / (SX / 2);
+      const int I = I0 + ci, J = J0 + cj;
+      if (I >= C.nx || J >= C.ny) continue;
+      T s = T(0);
+      for (int dj = 0; dj < 2; ++dj)
+        for (int dq = 0; dq < 2; ++dq) {
+          const int gx = 2 * I + dq, gy = 2 * J + dj;
+          if (gx >= nx || gy >= ny) continue;
+          const size_t g = (size_t)gy * P + gx;
+          const int lx = gx - x0 + H, ly = gy - y0 + H;
+          const T d = L.dg[g];
+          if (d < T(0)) continue;
+          T r = fma(-d, xs[ly][lx], (T)L.b[g]);
+          r = fma(cload<CT, T>(L.cE, g, cs), xs[ly][lx + 1], r);
+          r = fma(cload<CT, T>(L.cE, g - 1, cs), xs[ly][lx - 1], r);
+          r = fma(cload<CT, T>(L.cN, g, cs), xs[ly + 1][lx], r);
+          r = fma(cload<CT, T>(L.cN, g - P, cs), xs[ly - 1][lx], r);
+          s += r;
+        }
+      C.b[(size_t)J * C.pitch + I] = s;
+    }
+  }
+
+  if (RZ) {
+    double tot1, tot2;
+    if (grid_sum2(a1, a2, part, &sc->tickets[T_RZ], &tot1, &tot2) && t == 0)
+      set_beta(sc, tot1, tot2, flexible);
+  }
+}
+
+template <class T, class CT, class BT>
+__global__ void k_coarse_solve_t(MgView<T, CT, BT> C, const double* Ainv, const int* cmap,
+                                 const int* ncp, Scalars* sc) {
+  if (sc->done) return;
+  __shared__ double bd[kMaxCoarse];
+  const int t = threadIdx.x;
+  const int ncell = C.nx * C.ny, nn = *ncp;
+  for (int k = t; k < ncell; k += blockDim.x) {
+    const int r = cmap[k];
+    if (r >= 0) bd[r] = (double)C.b[(size_t)(k / C.nx) * C.pitch + (k % C.nx)];
+  }
+  __syncthreads();
+  for (int k = t; k < ncell; k += blockDim.x) {
+    const int r = cmap[k];
+    double y = 0.0;
+    if (r >= 0)
+      for (int c = 0; c < nn; ++c) y = fma(Ainv[r * nn + c], bd[c], y);
+    C.x[(size_t)(k / C.nx) * C.pitch + (k % C.nx)] = (T)y;
+  }
+}
+
+// r.z (and r.z_old) when the V-cycle does not end with a sweep
+template <class T, class BT>
+__global__ void k_dot_rz_t(int nx, int ny, int pitch, const BT* r, const T* z, const T* zold,
+                           int flexible, Scalars* sc, double* part) {
+  if (sc->done) return;
+  double a1 = 0.0, a2 = 0.0;
+  const int ix = blockIdx.x * 32 + threadIdx.x;
+  if (ix < nx)
+    for (int iy = blockIdx.y * 8 + threadIdx.y; iy < ny; iy += gridDim.y * 8) {
+      const size_t k = (size_t)iy * pitch + ix;
+      a1 = fma((double)r[k], (double)z[k], a1);
+      if (flexible) a2 = fma((double)r[k], (double)zold[k], a2);
+    }
+  double t1, t2;
+  if (grid_sum2(a1, a2, part, &sc->tickets[T_RZ], &t1, &t2) && tlin() == 0)
+    set_beta(sc, t1, t2, flexible);
+}
+
+// p_new = z + beta p_old (= z on the first iteration), q = A p_new, p.q and
+// alpha = r.z / p.q.  A 64x32 tile of p_new with a one-cell halo is built in
+// shared memory, so each p_new is formed once per CTA.
+template <class ZT>
+__global__ void __launch_bounds__(NT)
+k_pupdate_spmv_t(LevelView L, const ZT* __restrict__ z, const double* __restrict__ pold,
+                 double* __restrict__ pnew, double* __restrict__ q, Scalars* sc, double* part) {
+  if (sc->done) return;
+  constexpr int WX = SX + 2, WY = SY + 2;
+  __shared__ double ps[WY][WX];
+  const int nx = L.nx, ny = L.ny, P = L.pitch;
+  const int x0 = blockIdx.x * SX, y0 = blockIdx.y * SY;
+  const int t = tlin();
+  const bool first = sc->iter == 0;
+  const double beta = sc->beta;
+  for (int e = t; e < WX * WY; e += NT) {
+    const int ex = e % WX, ey = e / WX;
+    const int gx = x0 - 1 + ex, gy = y0 - 1 + ey;
+    double v = 0.0;
+    if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
+      const size_t g = (size_t)gy * P + gx;
+      v = first ? (double)z[g] : fma(beta, pold[g], (double)z[g]);
+    }
+    ps[ey][ex] = v;
+  }
+  __syncthreads();
+  double acc = 0.0;
+  for (int e = t; e < SX * SY; e += NT) {
+    const int ex = e % SX, ey = e / SX;
+    const int gx = x0 + ex, gy = y0 + ey;
+    if (gx < nx && gy < ny) {
+      const size_t g = (size_t)gy * P + gx;
+      const int lx = ex + 1, ly = ey + 1;
+      const double pc = ps[ly][lx];
+      double qv = fmax(L.dg[g], 0.0) * pc;
+      qv = fma(-L.cE[g], ps[ly][lx + 1], qv);
+      qv = fma(-L.cE[g - 1], ps[ly][lx - 1], qv);
+      qv = fma(-L.cN[g], ps[ly + 1][lx], qv);
+      qv = fma(-L.cN[g - P], ps[ly - 1][lx], qv);
+      pnew[g] = pc;
+      q[g] = qv;
+      acc = fma(pc, qv, acc);
+    }
+  }
+  double tot, dummy;
+  if (grid_sum2(acc, 0.0, part, &sc->tickets[T_PQ], &tot, &dummy) && t == 0) {
+    sc->pq = tot;
+    sc->alpha = sc->rz / tot;
+  }
+}
+
+// inverse diagonal of an FP64 level (0 where the cell has no unknown)
+__global__ void k_inv_diag(int nx, int ny, int pitch, const double* dg, double* di) {
+  const int ix = blockIdx.x * 32 + threadIdx.x;
+  if (ix >= nx) return;
+  for (int iy = blockIdx.y * 8 + threadIdx.y; iy < ny; iy += gridDim.y * 8) {
+    const size_t k = (size_t)iy * pitch + ix;
+    const double d = dg[k];
+    di[k] = d > 0.0 ? 1.0 / d : 0.0;
+  }
+}
+
+// largest coupling of a level, as the bits of a non-negative float
+__global__ void k_max_coupling(LevelView F, unsigned* out_bits) {
+  float m = 0.0f;
+  const int ix = blockIdx.x * 32 + threadIdx.x;
+  if (ix < F.nx)
+    for (int iy = blockIdx.y * 8 + threadIdx.y; iy < F.ny; iy += gridDim.y * 8) {
+      const size_t k = (size_t)iy * F.pitch + ix;
+      m = fmaxf(m, (float)fabs(F.cE[k]));
+      m = fmaxf(m, (float)fabs(F.cN[k]));
+    }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out_bits, __float_as_uint(m));
+}
+
+// Mixed level from the FP64 level: BF16 couplings divided by a power-of-two
+// scale near the level's largest coupling, FP32 diagonal rebuilt from the
+// rounded couplings plus the FP64 excess (so the level stays a diagonally
+// dominant M-matrix), FP32 inverse diagonal.
+__global__ void k_to_mixed(LevelView F, MgView<float, __nv_bfloat16, float> M,
+                           const unsigned* max_bits, float* cscale_out) {
+  const float mx = __uint_as_float(*max_bits);
+  int ex = 0;
+  frexpf(mx > 0.0f ? mx : 1.0f, &ex);
+  const float cs = ldexpf(1.0f, ex);  // power of two >= the largest coupling
+  const float inv = 1.0f / cs;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) *cscale_out = cs;
+  const int ix = blockIdx.x * 32 + threadIdx.x;
+  if (ix >= F.nx) return;
+  const int P = F.pitch;
+  auto rb = [&](double c) { return __float2bfloat16_rn((float)c * inv); };
+  for (int iy = blockIdx.y * 8 + threadIdx.y; iy < F.ny; iy += gridDim.y * 8) {
+    const size_t k = (size_t)iy * P + ix;
+    const __nv_bfloat16 e16 = rb(F.cE[k]), n16 = rb(F.cN[k]);
+    const_cast<__nv_bfloat16*>(M.cE)[k] = e16;
+    const_cast<__nv_bfloat16*>(M.cN)[k] = n16;
+    float d = -1.0f, di = 0.0f;
+    if (F.dg[k] > 0.0) {
+      const float sum = (__bfloat162float(e16) + __bfloat162float(rb(F.cE[k - 1])) +
+                         __bfloat162float(n16) + __bfloat162float(rb(F.cN[k - P]))) * cs;
+      d = sum + (float)F.ex[k];
+      if (d > 0.0f) di = 1.0f / d;
+      else d = -1.0f;
+    }
+    const_cast<float*>(M.dg)[k] = d;
+    const_cast<float*>(M.di)[k] = di;
+  }
+}
+
+}  // namespace
+
+static dim3 tiles(int nx, int ny) { return dim3((nx + SX - 1) / SX, (ny + SY - 1) / SY); }
+static dim3 small_grid(int nx, int ny) {
+  int gy = (ny + 7) / 8;
+  return dim3((nx + 31) / 32, gy < 1024 ? gy : 1024);
+}
+
+template <class T, class CT, class BT>
+void launch_sweep(const MgView<T, CT, BT>& L, const MgView<T, CT, T>& C, int first, bool zero,
+                  bool prolong, bool restrict_, bool rz, double omega, const T* zold,
+                  int flexible, Scalars* sc, double* part, cudaStream_t s) {
+  const dim3 g = tiles(L.nx, L.ny);
+  const T om = (T)omega;
+#define SCF_SWEEP(F, Z, PR, RS, R) \
+  k_sweep<T, CT, BT, F, Z, PR, RS, R><<<g, NT, 0, s>>>(L, C, om, zold, flexible, sc, part)
+  // the combinations the V-cycle uses (pre: red first; post: black first)
+  if (first == 0 && zero && !prolong && !restrict_ && !rz) SCF_SWEEP(0, true, false, false, false);
+  else if (first == 0 && zero && !prolong && restrict_ && !rz) SCF_SWEEP(0, true, false, true, false);
+  else if (first == 0 && !zero && !prolong && restrict_ && !rz) SCF_SWEEP(0, false, false, true, false);
+  else if (first == 0 && !zero && !prolong && !restrict_ && !rz) SCF_SWEEP(0, false, false, false, false);
+  else if (first == 1 && !zero && prolong && !restrict_ && !rz) SCF_SWEEP(1, false, true, false, false);
+  else if (first == 1 && !zero && prolong && !restrict_ && rz) SCF_SWEEP(1, false, true, false, true);
+  else if (first == 1 && !zero && !prolong && !restrict_ && !rz) SCF_SWEEP(1, false, false, false, false);
+  else if (first == 1 && !zero && !prolong && !restrict_ && rz) SCF_SWEEP(1, false, false, false, true);
+#undef SCF_SWEEP
+}
+
+template <class T, class CT, class BT>
+void launch_coarse_solve_t(const MgView<T, CT, BT>& C, const double* Ainv, const int* cmap,
+                           const int* nc, Scalars* sc, cudaStream_t s) {
+  k_coarse_solve_t<T, CT, BT><<<1, 64, 0, s>>>(C, Ainv, cmap, nc, sc);
+}
+
+template <class T, class BT>
+void launch_dot_rz_t(int nx, int ny, int pitch, const BT* r, const T* z, const T* zold,
+                     int flexible, Scalars* sc, double* part, cudaStream_t s) {
+  k_dot_rz_t<T, BT><<<small_grid(nx, ny), dim3(32, 8), 0, s>>>(nx, ny, pitch, r, z, zold,
+                                                                 flexible, sc, part);
+}
+
+template <class ZT>
+void launch_pupdate_spmv_t(LevelView L0, const ZT* z, const double* pold, double* pnew,
+                           double* q, Scalars* sc, double* part, cudaStream_t s) {
+  k_pupdate_spmv_t<ZT><<<tiles(L0.nx, L0.ny), NT, 0, s>>>(L0, z, pold, pnew, q, sc, part);
+}
+
+void launch_inv_diag(const LevelView& L, double* di, cudaStream_t s) {
+  k_inv_diag<<<small_grid(L.nx, L.ny), dim3(32, 8), 0, s>>>(L.nx, L.ny, L.pitch, L.dg, di);
+}
+
+void launch_max_coupling(const LevelView& L, unsigned* out_bits, cudaStream_t s) {
+  cudaMemsetAsync(out_bits, 0, sizeof(unsigned), s);
+  k_max_coupling<<<small_grid(L.nx, L.ny), dim3(32, 8), 0, s>>>(L, out_bits);
+}
+
+void launch_to_mixed(const LevelView& F, const MgView<float, __nv_bfloat16, float>& M,
+                     const unsigned* max_bits, float* cscale_out, cudaStream_t s) {
+  k_to_mixed<<<small_grid(F.nx, F.ny), dim3(32, 8), 0, s>>>(F, M, max_bits, cscale_out);
+}
+
+#define SCF_INST(T, CT, BT)                                                                   \
+  template void launch_sweep<T, CT, BT>(const MgView<T, CT, BT>&, const MgView<T, CT, T>&, int, \
+                                        bool, bool, bool, bool, double, const T*, int,          \
+                                        Scalars*, double*, cudaStream_t);                       \
+  template void launch_coarse_solve_t<T, CT, BT>(const MgView<T, CT, BT>&, const double*,      \
+                                                 const int*, const int*, Scalars*, cudaStream_t);
+SCF_INST(double, double, double)
+SCF_INST(float, __nv_bfloat16, float)
+SCF_INST(float, __nv_bfloat16, double)
+#undef SCF_INST
+template void launch_dot_rz_t<double, double>(int, int, int, const double*, const double*,
+                                              const double*, int, Scalars*, double*,
+                                              cudaStream_t);
+template void launch_dot_rz_t<float, double>(int, int, int, const double*, const float*,
+                                             const float*, int, Scalars*, double*, cudaStream_t);
+template void launch_pupdate_spmv_t<double>(LevelView, const double*, const double*, double*,
+                                            double*, Scalars*, double*, cudaStream_t);
+template void launch_pupdate_spmv_t<float>(LevelView, const float*, const double*, double*,
+                                           double*, Scalars*, double*, cudaStream_t);
+
+}  // namespace scf

@@ -4,9 +4,10 @@
 //
 // The PCG loop runs entirely on the device: one CUDA graph holds a
 // conditional WHILE node whose body is two PCG iterations (the direction
-// vector ping-pongs between two buffers); the convergence test in the last
-// kernel of each iteration clears the loop condition.  No host round trip
-// happens between the right-hand side and the final correction.
+// vector, and in the flexible mixed-precision variant also z, ping-pong
+// between two buffers); the convergence test in the last kernel of each
+// iteration clears the loop condition.  No host round trip happens between
+// the right-hand side and the final correction.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -15,18 +16,14 @@
 #include <vector>
 
 #include "../../include/scf_proj.h"
-#include "scf_internal.cuh"
+#include "scf_mg.cuh"
 
 using namespace scf;
 
-namespace {
-
-struct DevBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-};
-
-}  // namespace
+using bf16 = __nv_bfloat16;
+using MgD = MgView<double, double, double>;
+using MgF = MgView<float, bf16, float>;
+using MgF0 = MgView<float, bf16, double>;
 
 struct scf_proj {
   int nx = 0, ny = 0;
@@ -35,10 +32,18 @@ struct scf_proj {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   bool devptrs = false;
+  bool mixed = false;
 
-  // multigrid levels (level 0 is the fine grid; its b is the PCG residual r
-  // and its x the preconditioned residual z)
+  // FP64 multigrid levels (setup hierarchy; level 0 is the fine operator of
+  // the PCG, its b is the PCG residual r and its x the FP64 z)
   std::vector<LevelView> lev;
+  std::vector<double*> di64;  // FP64 inverse diagonals
+  // mixed levels (FP32 state, BF16 couplings), built from lev at assemble
+  std::vector<MgF> mix;
+  float* zA = nullptr;  // mixed fine-level z, ping-pong pair
+  float* zB = nullptr;
+  float* cscale = nullptr;      // device, one BF16 scale per level
+  unsigned* maxbits = nullptr;  // device, one per level
   std::vector<void*> allocs;
   // PCG vectors (padded layout)
   double *xsol = nullptr, *pA = nullptr, *pB = nullptr, *q = nullptr, *bvec = nullptr;
@@ -70,7 +75,7 @@ struct scf_proj {
   // graph of the PCG loop
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
-  bool graph_cond = false;     // true: conditional while-node graph
+  bool graph_cond = false;              // true: conditional while-node graph
   cudaGraph_t body_graph = nullptr;
   cudaGraphExec_t body_exec = nullptr;  // fallback: body only, host-polled
 
@@ -79,14 +84,15 @@ struct scf_proj {
 
 namespace {
 
-#define CK(call)                                                                   \
-  do {                                                                             \
-    cudaError_t e_ = (call);                                                       \
-    if (e_ != cudaSuccess) {                                                       \
-      if (getenv("SCF_DEBUG")) fprintf(stderr, "scf: %s failed: %s (%s:%d)\n", #call, \
-                                       cudaGetErrorString(e_), __FILE__, __LINE__); \
-      return e_ == cudaErrorMemoryAllocation ? SCF_ERR_NOMEM : SCF_ERR_CUDA;       \
-    }                                                                              \
+#define CK(call)                                                                       \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) {                                                           \
+      if (getenv("SCF_DEBUG"))                                                         \
+        fprintf(stderr, "scf: %s failed: %s (%s:%d)\n", #call, cudaGetErrorString(e_), \
+                __FILE__, __LINE__);                                                   \
+      return e_ == cudaErrorMemoryAllocation ? SCF_ERR_NOMEM : SCF_ERR_CUDA;           \
+    }                                                                                  \
   } while (0)
 
 int dev_alloc(scf_proj* h, void** p, size_t bytes) {
@@ -98,18 +104,14 @@ int dev_alloc(scf_proj* h, void** p, size_t bytes) {
 }
 
 // padded array for a level: (ny+3)*pitch elements, base at row 2
-int level_array(scf_proj* h, int ny, int pitch, double** base) {
+template <class T>
+int level_array(scf_proj* h, int ny, int pitch, T** base) {
   void* p = nullptr;
   size_t n = (size_t)(ny + 3) * pitch;
-  int rc = dev_alloc(h, &p, n * sizeof(double));
+  int rc = dev_alloc(h, &p, n * sizeof(T));
   if (rc) return rc;
-  *base = reinterpret_cast<double*>(p) + 2 * (size_t)pitch;
+  *base = reinterpret_cast<T*>(p) + 2 * (size_t)pitch;
   return SCF_OK;
-}
-
-void fill_fin(scf_proj* h) {
-  FortranIn& f = h->fin;
-  f.nx = h->nx; f.ny = h->ny;
 }
 
 void destroy_graph(scf_proj* h) {
@@ -120,48 +122,76 @@ void destroy_graph(scf_proj* h) {
   h->gexec = nullptr; h->graph = nullptr; h->body_exec = nullptr; h->body_graph = nullptr;
 }
 
-// Enqueue one multigrid V-cycle on level 0 (b -> x).  do_rz: the last
-// kernel also reduces r.z and sets the PCG beta.
-void enqueue_vcycle(scf_proj* h, Scalars* sc, bool do_rz, cudaStream_t s) {
+MgD view64(scf_proj* h, int l) {
+  const LevelView& L = h->lev[l];
+  return MgD{L.nx, L.ny, L.pitch, L.cE, L.cN, L.dg, h->di64[l], L.x, L.b, nullptr};
+}
+
+// Enqueue one V-cycle.  Level 0 has right-hand side b0 (the PCG residual)
+// and iterate x0 (z); coarse levels are `coarse(l)`.  do_rz: the last
+// kernel reduces r.z (and r.z_old when flexible) and sets the PCG beta.
+template <class T, class CT, class BT, class CoarseFn>
+void enqueue_vcycle_t(scf_proj* h, MgView<T, CT, BT> L0, CoarseFn coarse, Scalars* sc,
+                      bool do_rz, const T* zold, int flexible, cudaStream_t s) {
   const int L = (int)h->lev.size();
   const int npre = h->opts.npre, npost = h->opts.npost;
+  const double om = h->opts.omega;
   if (L == 1) {
-    launch_coarse_solve(h->lev[0], h->Ainv, h->cmap, h->ncoarse, sc, s);
-    if (do_rz) launch_dot_rz(h->lev[0], sc, h->part, s);
+    launch_coarse_solve_t(L0, h->Ainv, h->cmap, h->ncoarse, sc, s);
+    if (do_rz)
+      launch_dot_rz_t<T, BT>(L0.nx, L0.ny, L0.pitch, L0.b, L0.x, zold, flexible, sc, h->part, s);
     return;
   }
-  for (int l = 0; l < L - 1; ++l) {
-    for (int it = 0; it < npre; ++it) {
-      launch_smooth(h->lev[l], 0, it == 0 ? 1 : 0, 0, sc, h->part, s);
-      launch_smooth(h->lev[l], 1, 0, 0, sc, h->part, s);
-    }
-    if (npre == 0) {
-      // iterate starts at zero without a smoothing sweep
-      cudaMemsetAsync(h->lev[l].x - 2 * (size_t)h->lev[l].pitch, 0,
-                      sizeof(double) * (size_t)(h->lev[l].ny + 3) * h->lev[l].pitch, s);
-    }
-    launch_resid_restrict(h->lev[l], h->lev[l + 1], sc, s);
-  }
-  launch_coarse_solve(h->lev[L - 1], h->Ainv, h->cmap, h->ncoarse, sc, s);
-  for (int l = L - 2; l >= 0; --l) {
-    launch_prolong(h->lev[l], h->lev[l + 1], h->opts.omega, sc, s);
+  // down leg
+  auto down = [&](auto V, const MgView<T, CT, T>& C) {
+    for (int it = 0; it < npre; ++it)
+      launch_sweep(V, C, 0, it == 0, false, it == npre - 1, false, om, (const T*)nullptr, 0, sc,
+                   h->part, s);
+  };
+  down(L0, coarse(1));
+  for (int l = 1; l < L - 1; ++l) down(coarse(l), coarse(l + 1));
+  launch_coarse_solve_t(coarse(L - 1), h->Ainv, h->cmap, h->ncoarse, sc, s);
+  // up leg
+  auto up = [&](auto V, const MgView<T, CT, T>& C, bool fine) {
     for (int it = 0; it < npost; ++it) {
-      bool last = (l == 0 && it == npost - 1);
-      launch_smooth(h->lev[l], 1, 0, 0, sc, h->part, s);
-      launch_smooth(h->lev[l], 0, 0, (last && do_rz) ? 1 : 0, sc, h->part, s);
+      const bool rz = fine && do_rz && it == npost - 1;
+      launch_sweep(V, C, 1, false, it == 0, false, rz, om, zold, flexible, sc, h->part, s);
     }
+  };
+  for (int l = L - 2; l >= 1; --l) up(coarse(l), coarse(l + 1), false);
+  up(L0, coarse(1), true);
+}
+
+// V-cycle of the handle's precision on level 0: b0 = r (FP64), x = z
+void enqueue_vcycle(scf_proj* h, Scalars* sc, bool do_rz, bool ping, cudaStream_t s) {
+  if (!h->mixed) {
+    auto coarse = [h](int l) { return view64(h, l); };
+    enqueue_vcycle_t(h, view64(h, 0), coarse, sc, do_rz, (const double*)nullptr, 0, s);
+  } else {
+    const MgF& m0 = h->mix[0];
+    MgF0 L0{m0.nx, m0.ny, m0.pitch, m0.cE, m0.cN, m0.dg, m0.di, ping ? h->zB : h->zA,
+            h->lev[0].b, m0.csp};
+    auto coarse = [h](int l) { return h->mix[l]; };
+    enqueue_vcycle_t(h, L0, coarse, sc, do_rz, ping ? h->zA : h->zB, 1, s);
   }
-  if (npost == 0 && do_rz) launch_dot_rz(h->lev[0], sc, h->part, s);
 }
 
 // one PCG iteration: z = M r, beta, p = z + beta p_old, q = A p, alpha,
 // x += alpha p, r -= alpha q, convergence test
-void enqueue_iteration(scf_proj* h, const double* pold, double* pnew, unsigned long long cond,
-                       cudaStream_t s) {
+void enqueue_iteration(scf_proj* h, const double* pold, double* pnew, bool ping,
+                       unsigned long long cond, cudaStream_t s) {
   LevelView L0 = h->lev[0];
-  enqueue_vcycle(h, h->sc, true, s);
-  launch_pupdate_spmv(L0, L0.x, pold, pnew, h->q, h->sc, h->part, s);
+  enqueue_vcycle(h, h->sc, true, ping, s);
+  if (!h->mixed)
+    launch_pupdate_spmv_t<double>(L0, L0.x, pold, pnew, h->q, h->sc, h->part, s);
+  else
+    launch_pupdate_spmv_t<float>(L0, ping ? h->zB : h->zA, pold, pnew, h->q, h->sc, h->part, s);
   launch_update_xr(L0, h->xsol, pnew, L0.b, h->q, h->sc, h->part, cond, s);
+}
+
+void enqueue_body(scf_proj* h, unsigned long long cond, cudaStream_t s) {
+  enqueue_iteration(h, h->pA, h->pB, false, cond, s);
+  enqueue_iteration(h, h->pB, h->pA, true, cond, s);
 }
 
 int build_graph(scf_proj* h) {
@@ -169,9 +199,8 @@ int build_graph(scf_proj* h) {
   if (h->opts.flags & SCF_FLAG_NO_GRAPH) return SCF_OK;
   cudaStream_t cs = nullptr;
   CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-  // preferred: conditional while node
   bool ok = false;
-  do {
+  do {  // preferred: conditional while node
     cudaGraph_t g = nullptr;
     if (cudaGraphCreate(&g, 0) != cudaSuccess) break;
     cudaGraphConditionalHandle handle;
@@ -196,11 +225,9 @@ int build_graph(scf_proj* h) {
       cudaGraphDestroy(g);
       break;
     }
-    enqueue_iteration(h, h->pA, h->pB, (unsigned long long)handle, cs);
-    enqueue_iteration(h, h->pB, h->pA, (unsigned long long)handle, cs);
+    enqueue_body(h, (unsigned long long)handle, cs);
     cudaGraph_t captured = nullptr;
-    cudaError_t e = cudaStreamEndCapture(cs, &captured);
-    if (e != cudaSuccess) {
+    if (cudaStreamEndCapture(cs, &captured) != cudaSuccess) {
       cudaGetLastError();
       cudaGraphDestroy(g);
       break;
@@ -216,12 +243,10 @@ int build_graph(scf_proj* h) {
     h->graph_cond = true;
     ok = true;
   } while (0);
-  if (!ok) {
-    // fallback: graph of the loop body, relaunched and polled from the host
+  if (!ok) {  // fallback: graph of the loop body, relaunched and polled from the host
     cudaGetLastError();
     CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed));
-    enqueue_iteration(h, h->pA, h->pB, 0ull, cs);
-    enqueue_iteration(h, h->pB, h->pA, 0ull, cs);
+    enqueue_body(h, 0ull, cs);
     CK(cudaStreamEndCapture(cs, &h->body_graph));
     CK(cudaGraphInstantiate(&h->body_exec, h->body_graph, 0));
     h->graph_cond = false;
@@ -250,8 +275,7 @@ int run_pcg(scf_proj* h) {
       if (h->body_exec) {
         CK(cudaGraphLaunch(h->body_exec, h->stream));
       } else {
-        enqueue_iteration(h, h->pA, h->pB, 0ull, h->stream);
-        enqueue_iteration(h, h->pB, h->pA, 0ull, h->stream);
+        enqueue_body(h, 0ull, h->stream);
         CK(cudaGetLastError());
       }
       launched += 2;
@@ -397,7 +421,8 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
   scf_opts o;
   if (opts) o = *opts; else scf_opts_default(&o);
   if (o.precision != SCF_PREC_FP64 && o.precision != SCF_PREC_MIXED) return SCF_ERR_ARG;
-  if (o.maxit < 1 || o.npre < 0 || o.npost < 0 || !(o.rtol >= 0.0)) return SCF_ERR_ARG;
+  if (o.maxit < 1 || o.npre < 1 || o.npost < 1 || o.npre > 8 || o.npost > 8 || !(o.rtol >= 0.0))
+    return SCF_ERR_ARG;
   if (o.coarse_max < 1 || o.coarse_max > kMaxCoarse) return SCF_ERR_ARG;
   if (!(o.omega > 0.0 && o.omega < 2.0)) return SCF_ERR_ARG;
   scf_proj* h = new (std::nothrow) scf_proj();
@@ -405,6 +430,7 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
   h->nx = nx; h->ny = ny; h->opts = o;
   h->device = o.device;
   h->devptrs = (o.flags & SCF_FLAG_DEVICE_PTRS) != 0;
+  h->mixed = o.precision == SCF_PREC_MIXED;
   int rc = SCF_OK;
   auto fail = [&](int code) { scf_proj_destroy(h); return code; };
   if (cudaSetDevice(h->device) != cudaSuccess) return fail(SCF_ERR_CUDA);
@@ -413,7 +439,7 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
   h->own_stream = true;
   for (auto& e : h->ev)
     if (cudaEventCreate(&e) != cudaSuccess) return fail(SCF_ERR_CUDA);
-  // multigrid levels
+  // FP64 multigrid levels
   int lx = nx, ly = ny;
   while (true) {
     LevelView L{};
@@ -421,9 +447,29 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
     double** arrs[6] = {&L.cE, &L.cN, &L.dg, &L.ex, &L.x, &L.b};
     for (auto a : arrs)
       if ((rc = level_array(h, ly, L.pitch, a))) return fail(rc);
+    double* di = nullptr;
+    if ((rc = level_array(h, ly, L.pitch, &di))) return fail(rc);
     h->lev.push_back(L);
+    h->di64.push_back(di);
     if ((long)lx * ly <= o.coarse_max || (lx == 1 && ly == 1) || h->lev.size() >= 30) break;
     lx = (lx + 1) / 2; ly = (ly + 1) / 2;
+  }
+  const int nlev = (int)h->lev.size();
+  if ((rc = dev_alloc(h, (void**)&h->cscale, sizeof(float) * nlev))) return fail(rc);
+  if ((rc = dev_alloc(h, (void**)&h->maxbits, sizeof(unsigned) * nlev))) return fail(rc);
+  if (h->mixed) {
+    for (int l = 0; l < nlev; ++l) {
+      const LevelView& F = h->lev[l];
+      bf16 *ce = nullptr, *cn = nullptr;
+      float *dg = nullptr, *di = nullptr, *x = nullptr, *b = nullptr;
+      if ((rc = level_array(h, F.ny, F.pitch, &ce)) || (rc = level_array(h, F.ny, F.pitch, &cn)) ||
+          (rc = level_array(h, F.ny, F.pitch, &dg)) || (rc = level_array(h, F.ny, F.pitch, &di)) ||
+          (rc = level_array(h, F.ny, F.pitch, &x)) || (rc = level_array(h, F.ny, F.pitch, &b)))
+        return fail(rc);
+      h->mix.push_back(MgF{F.nx, F.ny, F.pitch, ce, cn, dg, di, x, b, h->cscale + l});
+    }
+    h->zA = h->mix[0].x;
+    if ((rc = level_array(h, ny, h->lev[0].pitch, &h->zB))) return fail(rc);
   }
   const int P0 = h->lev[0].pitch;
   double** pv[5] = {&h->xsol, &h->pA, &h->pB, &h->q, &h->bvec};
@@ -439,12 +485,13 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
     dim3 g1 = grid_for(nx, ny, 1), g2 = grid_for(nx, ny, 2);
     nblk = (size_t)g1.x * g1.y;
     if ((size_t)g2.x * g2.y > nblk) nblk = (size_t)g2.x * g2.y;
+    size_t tb = (size_t)((nx + 63) / 64) * ((ny + 31) / 32);
+    if (tb > nblk) nblk = tb;
   }
-  if ((rc = dev_alloc(h, (void**)&h->part, sizeof(double) * (nblk + 32)))) return fail(rc);
+  if ((rc = dev_alloc(h, (void**)&h->part, sizeof(double) * (2 * nblk + 64)))) return fail(rc);
   if (cudaMallocHost((void**)&h->sc_host, sizeof(Scalars)) != cudaSuccess) return fail(SCF_ERR_NOMEM);
   memset(h->sc_host, 0, sizeof(Scalars));
-  // Fortran-layout staging (host mode only)
-  if (!h->devptrs) {
+  if (!h->devptrs) {  // Fortran-layout staging
     const size_t n0 = (size_t)(nx + 2) * (ny + 2), n1 = (size_t)nx * ny;
     struct { void** p; size_t b; } st[] = {
         {(void**)&h->st_dx, n1 * 8},  {(void**)&h->st_dy, n1 * 8},  {(void**)&h->st_dxU, n1 * 8},
@@ -460,7 +507,7 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
     for (auto& e : st)
       if ((rc = dev_alloc(h, e.p, e.b))) return fail(rc);
   }
-  fill_fin(h);
+  h->fin.nx = nx; h->fin.ny = ny;
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) return fail(SCF_ERR_CUDA);
   *out = h;
   return SCF_OK;
@@ -556,6 +603,12 @@ int scf_proj_assemble(scf_proj* h, const double* DpU, const double* DpV, double 
   launch_excess(h->lev[0], s);
   for (size_t l = 1; l < h->lev.size(); ++l) launch_coarsen(h->lev[l - 1], h->lev[l], s);
   launch_coarse_setup(h->lev.back(), h->Ainv, h->cmap, h->ncoarse, s);
+  for (size_t l = 0; l < h->lev.size(); ++l) launch_inv_diag(h->lev[l], h->di64[l], s);
+  if (h->mixed)
+    for (size_t l = 0; l < h->lev.size(); ++l) {
+      launch_max_coupling(h->lev[l], h->maxbits + l, s);
+      launch_to_mixed(h->lev[l], h->mix[l], h->maxbits + l, h->cscale + l, s);
+    }
   CK(cudaGetLastError());
   int nanflag = 0;
   CK(cudaMemcpyAsync(&nanflag, &h->sc->nan, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -613,23 +666,36 @@ int scf_proj_time_kernel(scf_proj* h, int kernel, int reps, double* ms) {
   init.rtol2 = -1.0;
   CK(cudaMemcpyAsync(h->sc_diag, &init, sizeof(init), cudaMemcpyHostToDevice, s));
   LevelView L0 = h->lev[0];
+  const bool two = h->lev.size() > 1;
+  const double om = h->opts.omega;
   auto launch = [&]() {
-    switch (kernel) {
-      case SCF_K_SMOOTH: launch_smooth(L0, 1, 0, 0, h->sc_diag, h->part, s); break;
-      case SCF_K_PUPDATE_SPMV:
-        launch_pupdate_spmv(L0, L0.x, h->pA, h->pB, h->q, h->sc_diag, h->part, s);
-        break;
-      case SCF_K_UPDATE_XR:
-        launch_update_xr(L0, h->xsol, h->pB, L0.b, h->q, h->sc_diag, h->part, 0ull, s);
-        break;
-      case SCF_K_RESID_RESTRICT:
-        if (h->lev.size() > 1) launch_resid_restrict(L0, h->lev[1], h->sc_diag, s);
-        break;
-      case SCF_K_PROLONG:
-        if (h->lev.size() > 1) launch_prolong(L0, h->lev[1], h->opts.omega, h->sc_diag, s);
-        break;
-      case SCF_K_ASSEMBLE: launch_assemble(h->fin, L0, h->sc_diag, s); break;
+    if (kernel == SCF_K_PUPDATE_SPMV) {
+      if (h->mixed) launch_pupdate_spmv_t<float>(L0, h->zA, h->pA, h->pB, h->q, h->sc_diag, h->part, s);
+      else launch_pupdate_spmv_t<double>(L0, L0.x, h->pA, h->pB, h->q, h->sc_diag, h->part, s);
+      return;
     }
+    if (kernel == SCF_K_UPDATE_XR) {
+      launch_update_xr(L0, h->xsol, h->pB, L0.b, h->q, h->sc_diag, h->part, 0ull, s);
+      return;
+    }
+    if (kernel == SCF_K_ASSEMBLE) {
+      launch_assemble(h->fin, L0, h->sc_diag, s);
+      return;
+    }
+    if (!two) return;
+    const bool smooth = kernel == SCF_K_SMOOTH, restr = kernel == SCF_K_RESID_RESTRICT,
+               prol = kernel == SCF_K_PROLONG;
+    const int first = restr ? 0 : 1;
+    if (!h->mixed) {
+      launch_sweep(view64(h, 0), view64(h, 1), first, false, prol, restr, false, om,
+                   (const double*)nullptr, 0, h->sc_diag, h->part, s);
+    } else {
+      const MgF& m0 = h->mix[0];
+      MgF0 V{m0.nx, m0.ny, m0.pitch, m0.cE, m0.cN, m0.dg, m0.di, h->zA, L0.b, m0.csp};
+      launch_sweep(V, h->mix[1], first, false, prol, restr, false, om, (const float*)nullptr, 0,
+                   h->sc_diag, h->part, s);
+    }
+    (void)smooth;
   };
   launch();  // warm-up
   CK(cudaEventRecord(h->ev[5], s));
@@ -652,8 +718,9 @@ int scf_proj_vcycle(scf_proj* h, const double* b, double* x) {
   CK(cudaMemcpyAsync(tmp, b, n1 * 8, cudaMemcpyHostToDevice, s));
   launch_from_fortran(h->lev[0], tmp, h->lev[0].b, s);
   CK(cudaMemsetAsync(h->sc_diag, 0, sizeof(Scalars), s));
-  enqueue_vcycle(h, h->sc_diag, false, s);
-  launch_to_fortran(h->lev[0], h->lev[0].x, tmp, s);
+  enqueue_vcycle(h, h->sc_diag, false, false, s);
+  if (h->mixed) launch_to_fortran_f(h->lev[0], h->zA, tmp, s);
+  else launch_to_fortran(h->lev[0], h->lev[0].x, tmp, s);
   CK(cudaMemcpyAsync(x, tmp, n1 * 8, cudaMemcpyDeviceToHost, s));
   cudaFreeAsync(tmp, s);
   CK(cudaGetLastError());

@@ -48,10 +48,11 @@ def _check_solution(c, g, exp):
     assert np.abs(g["mres"] - exp["mres"]).max() <= 1e-10
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("name", GOLDEN_CASES)
-def test_golden_fixture(cuda, name):
+def test_golden_fixture(cuda, name, precision):
     c, exp = load_golden(name)
-    g = _gpu_project(c)
+    g = _gpu_project(c, precision=precision)
     _check_operator(c, g["operator"], exp["matr"], exp["rhm"])
     _check_solution(c, g, exp)
     assert g["stats"]["relres_true"] < 1e-11
@@ -64,10 +65,11 @@ def test_golden_fixture(cuda, name):
     lambda: synth.random_instance(5, 9, 3),
     lambda: synth.c5(instance=1, n=96),
 ], ids=["c1_128", "c1_33", "c4_40", "r9", "c5_96"])
-def test_parity_vs_oracle(cuda, oracle, maker):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_parity_vs_oracle(cuda, oracle, maker, precision):
     c = maker()
     exp = oracle.project(c)
-    g = _gpu_project(c)
+    g = _gpu_project(c, precision=precision)
     _check_operator(c, g["operator"], exp["matr"], exp["rhm"])
     _check_solution(c, g, exp)
 
@@ -102,11 +104,12 @@ def test_vcycle_matches_oracle(cuda, oracle):
     assert rel_l2(xg, xo) < 1e-11
 
 
-def test_deterministic_and_graph_free_path_agree(cuda):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_deterministic_and_graph_free_path_agree(cuda, precision):
     c = synth.c4(n=96, instance=9)
-    a = _gpu_project(c)
-    b = _gpu_project(c)
-    n = _gpu_project(c, use_graph=False)
+    a = _gpu_project(c, precision=precision)
+    b = _gpu_project(c, precision=precision)
+    n = _gpu_project(c, use_graph=False, precision=precision)
     for k in ("Pp", "u", "v", "p", "mres"):
         assert np.array_equal(a[k], b[k]), k
         assert np.array_equal(a[k], n[k]), k
@@ -170,6 +173,34 @@ def test_zero_rhs_and_errors(cuda):
         s.close()
 
 
+def test_mixed_vcycle_is_close_to_fp64(cuda, oracle):
+    """The FP32/BF16 V-cycle approximates the FP64 one to BF16 accuracy."""
+    c = synth.c4(n=128, instance=4)
+    rng = np.random.Generator(np.random.PCG64(6))
+    b = np.asfortranarray(rng.normal(size=(c.nx, c.ny)) * _active(c))
+    out = {}
+    for prec in ("fp64", "mixed"):
+        s = P.ProjectionSolver(c.nx, c.ny, precision=prec)
+        try:
+            s.setup_case(c)
+            out[prec] = s.vcycle(b)
+        finally:
+            s.close()
+    assert rel_l2(out["mixed"], out["fp64"]) < 3e-2
+
+
+def test_mixed_preconditioner_iterations(cuda):
+    """The mixed preconditioner inside flexible PCG needs about as many
+    iterations as the FP64 one."""
+    c = synth.c4(n=256, instance=2)
+    it = {}
+    for prec in ("fp64", "mixed"):
+        g = _gpu_project(c, precision=prec, rtol=1e-8, maxit=200)
+        assert g["stats"]["status"] == 0 and g["stats"]["relres_true"] < 1.5e-8
+        it[prec] = g["stats"]["iters"]
+    assert it["mixed"] <= it["fp64"] + 3, it
+
+
 @pytest.mark.slow
 def test_full_size_c2(cuda, oracle):
     """2048^2 at the benchmark tolerance: FP64 relative residual 1e-8, mass
@@ -188,5 +219,8 @@ def test_full_size_c2(cuda, oracle):
     assert rel < 1e-10  # the recomputed FP64 residual floors near 3e-12 at 2048^2
     err = rel_l2(g["Pp"][1:-1, 1:-1], xi)
     assert err < 1e-6, err
-    g2 = _gpu_project(c, rtol=1e-12, maxit=400)
-    assert rel_l2(g2["Pp"][1:-1, 1:-1], xi) <= TOL_P
+    for prec in ("fp64", "mixed"):
+        g2 = _gpu_project(c, rtol=1e-12, maxit=400, precision=prec)
+        assert rel_l2(g2["Pp"][1:-1, 1:-1], xi) <= TOL_P, prec
+    gm = _gpu_project(c, rtol=1e-8, maxit=200, precision="mixed")
+    assert gm["stats"]["status"] == 0 and gm["stats"]["relres_true"] <= 1.5e-8
