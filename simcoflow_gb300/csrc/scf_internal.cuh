@@ -49,6 +49,7 @@ struct FortranIn {
 // Device-resident scalars of one PCG solve.
 struct Scalars {
   double bnorm2, rr, rz, pq, alpha, beta, rtol2, res_true2, mres_max, rr_prev;
+  double rz_cross;  // r_{k+1}.z_k of the flexible PCG, reduced by the x/r update
   int iter, maxit, done, status, nan;
   int pad[3];
   unsigned tickets[8];  // last-block counters, one per reduction site
@@ -68,6 +69,36 @@ __host__ __device__ inline size_t fo0(int nx, int i, int j) {  // (0:nx+1,0:ny+1
 
 inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
 
+// Programmatic dependent launch.  Kernels are launched with
+// cudaLaunchAttributeProgrammaticStreamSerialization, so a kernel's CTAs may
+// be scheduled while its predecessor in the stream (or graph) drains; every
+// kernel first waits here for the predecessor's completion and memory
+// flush, then signals that its own successor may start scheduling.  For a
+// kernel launched without the attribute both calls are no-ops.
+__device__ __forceinline__ void pdl_wait() {
+  cudaGridDependencySynchronize();
+  cudaTriggerProgrammaticLaunchCompletion();
+}
+
+// PDL is on unless SCF_NO_PDL is set in the environment.
+bool pdl_enabled();
+
+template <typename... KArgs, typename... Args>
+inline void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                     cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // launch geometry: 2 cells per thread in x, rows looped with a grid stride
 inline dim3 grid_for(int nx, int ny, int cells_per_thread_x = 2) {
   int gx = (nx + kBX * cells_per_thread_x - 1) / (kBX * cells_per_thread_x);
@@ -84,10 +115,11 @@ void launch_excess(LevelView L, cudaStream_t s);
 void launch_coarsen(LevelView F, LevelView C, cudaStream_t s);
 void launch_coarse_setup(LevelView C, double* Ainv, int* cmap, int* nc, cudaStream_t s);
 void launch_rhs(const FortranIn& in, const double* ustar, const double* vstar, double vb,
-                LevelView L0, double* bvec, double* r, double* x, Scalars* sc, double* part,
-                double rtol, int maxit, cudaStream_t s);
-void launch_update_xr(LevelView L0, double* x, const double* p, double* r, const double* q,
-                      Scalars* sc, double* part, unsigned long long cond, cudaStream_t s);
+                LevelView L0, double* bvec, double* r, float* r32, double* x, Scalars* sc,
+                double* part, double rtol, int maxit, cudaStream_t s);
+void launch_update_xr(LevelView L0, double* x, const double* p, double* r, float* r32,
+                      const float* z32, const double* q, Scalars* sc, double* part,
+                      unsigned long long cond, cudaStream_t s);
 void launch_final_solution(const FortranIn& in, LevelView L0, const double* x,
                            const double* bvec, const double* ustar, const double* vstar,
                            double* Pp, double* p, double* u, double* v, int correct,
@@ -98,5 +130,6 @@ void launch_final_zero(const FortranIn& in, double* p, double* u, double* v, cud
 void launch_to_fortran(LevelView L, const double* src, double* dst, cudaStream_t s);
 void launch_from_fortran(LevelView L, const double* src, double* dst, cudaStream_t s);
 void launch_to_fortran_f(LevelView L, const float* src, double* dst, cudaStream_t s);
+void launch_from_fortran_f(LevelView L, const double* src, float* dst, cudaStream_t s);
 
 }  // namespace scf

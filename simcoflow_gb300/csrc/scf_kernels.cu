@@ -80,6 +80,39 @@ __device__ bool grid_reduce(double v, double* part, unsigned* ticket, double* to
   return true;
 }
 
+// Two sums at once, same scheme (two partial slots per block).
+__device__ bool grid_reduce2(double a, double b, double* part, unsigned* ticket, double* ta,
+                             double* tb) {
+  __shared__ bool last;
+  const int t = tid2();
+  const unsigned nb = gridDim.x * gridDim.y;
+  const unsigned bid = blockIdx.y * gridDim.x + blockIdx.x;
+  const double sa = block_sum(a);
+  const double sb = block_sum(b);
+  if (t == 0) {
+    part[2 * bid] = sa;
+    part[2 * bid + 1] = sb;
+    __threadfence();
+    last = (atomicAdd(ticket, 1u) == nb - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double xa = 0.0, xb = 0.0;
+  for (unsigned k = t; k < nb; k += kThreads) {
+    xa += __ldcg(&part[2 * k]);
+    xb += __ldcg(&part[2 * k + 1]);
+  }
+  xa = block_sum(xa);
+  xb = block_sum(xb);
+  if (t == 0) {
+    *ta = xa;
+    *tb = xb;
+    *ticket = 0u;
+  }
+  return true;
+}
+
 // ---------------------------------------------------------------------------
 // Assembly: ComputePossionMatrixCoefficient + SetPoissonMatrix
 // (src/ProjectionP_Mod.f90:395-580, :137-273).
@@ -130,6 +163,7 @@ __device__ __forceinline__ double pocoef(double Dp, double len, double dist, dou
 }
 
 __global__ void k_assemble(FortranIn in, LevelView L, Scalars* sc) {
+  pdl_wait();
   const int nx = in.nx, ny = in.ny;
   const int ix = blockIdx.x * kBX + threadIdx.x;
   if (ix >= nx) return;
@@ -192,6 +226,7 @@ __global__ void k_assemble(FortranIn in, LevelView L, Scalars* sc) {
 
 // diagonal excess dg - (cE + cW + cN + cS), clamped at zero
 __global__ void k_excess(LevelView L) {
+  pdl_wait();
   const int ix = blockIdx.x * kBX + threadIdx.x;
   if (ix >= L.nx) return;
   for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY) {
@@ -206,6 +241,7 @@ __global__ void k_excess(LevelView L) {
 
 // Galerkin coarse operator for piecewise-constant 2x2 aggregation
 __global__ void k_coarsen(LevelView F, LevelView C) {
+  pdl_wait();
   const int I = blockIdx.x * kBX + threadIdx.x;
   if (I >= C.nx) return;
   const int nxf = F.nx, nyf = F.ny, pf = F.pitch;
@@ -250,6 +286,7 @@ __global__ void k_coarsen(LevelView F, LevelView C) {
 // Dense inverse of the coarsest operator (at most kMaxCoarse unknowns) by
 // Gauss-Jordan elimination without pivoting (the matrix is SPD).
 __global__ void k_coarse_setup(LevelView C, double* Ainv, int* cmap, int* nc_out) {
+  pdl_wait();
   __shared__ double A[kMaxCoarse * kMaxCoarse];
   __shared__ double rowp[kMaxCoarse], colp[kMaxCoarse];
   __shared__ int map[kMaxCoarse];
@@ -310,8 +347,9 @@ __global__ void k_coarse_setup(LevelView C, double* Ainv, int* cmap, int* nc_out
 // Also starts the PCG: r = b, x = 0, scalars reset.
 // ---------------------------------------------------------------------------
 __global__ void k_rhs(FortranIn in, const double* us, const double* vs, double vb, int pitch,
-                      double* bvec, double* r, double* x, Scalars* sc, double* part, double rtol,
-                      int maxit) {
+                      double* bvec, double* r, float* r32, double* x, Scalars* sc, double* part,
+                      double rtol, int maxit) {
+  pdl_wait();
   const int nx = in.nx, ny = in.ny;
   const int ix = blockIdx.x * kBX + threadIdx.x;
   double acc = 0.0;
@@ -331,6 +369,7 @@ __global__ void k_rhs(FortranIn in, const double* us, const double* vs, double v
       }
       bvec[kl] = bv;
       r[kl] = bv;
+      if (r32) r32[kl] = (float)bv;
       x[kl] = 0.0;
       acc = fma(bv, bv, acc);
     }
@@ -357,13 +396,17 @@ __global__ void k_rhs(FortranIn in, const double* us, const double* vs, double v
 // PCG vector update.
 // ---------------------------------------------------------------------------
 
-// x += alpha p, r -= alpha q, reduce r.r; the last block advances the
+// x += alpha p, r -= alpha q, reduce r.r (and, for the flexible PCG, the
+// cross term r_new.z of the next beta, with z the preconditioned residual of
+// this iteration, in FP32 per thread); the last block advances the
 // iteration count, tests convergence and, inside a graph loop, clears the
 // loop condition.  Block (0,0) also counts body executions and stops the
 // loop after maxit+2 of them whatever else happens.
 __global__ void k_update_xr(LevelView L, double* __restrict__ x, const double* __restrict__ p,
-                            double* __restrict__ r, const double* __restrict__ q, Scalars* sc,
-                            double* part, unsigned long long cond) {
+                            double* __restrict__ r, float* __restrict__ r32,
+                            const float* __restrict__ z32, const double* __restrict__ q,
+                            Scalars* sc, double* part, unsigned long long cond) {
+  pdl_wait();
   if (cond && block00()) {
     int g = atomicAdd(&sc->pad[0], 1);
     if (g + 1 >= sc->maxit + 2) cudaGraphSetConditional(cond, 0u);
@@ -375,6 +418,7 @@ __global__ void k_update_xr(LevelView L, double* __restrict__ x, const double* _
   const int ix0 = 2 * (blockIdx.x * kBX + threadIdx.x);
   const double alpha = sc->alpha;
   double acc = 0.0;
+  float crs = 0.0f;
   if (ix0 < L.nx) {
     for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY) {
       const size_t k = (size_t)iy * L.pitch + ix0;
@@ -391,14 +435,28 @@ __global__ void k_update_xr(LevelView L, double* __restrict__ x, const double* _
         acc = fma(rv.y, rv.y, acc);
         *reinterpret_cast<double2*>(x + k) = xv;
         *reinterpret_cast<double2*>(r + k) = rv;
+        if (r32) {
+          const float2 rf = make_float2((float)rv.x, (float)rv.y);
+          *reinterpret_cast<float2*>(r32 + k) = rf;
+          if (z32) {
+            const float2 zf = *reinterpret_cast<const float2*>(z32 + k);
+            crs = fmaf(rf.x, zf.x, crs);
+            crs = fmaf(rf.y, zf.y, crs);
+          }
+        }
       } else {
         x[k] = xv.x;
         r[k] = rv.x;
+        if (r32) {
+          r32[k] = (float)rv.x;
+          if (z32) crs = fmaf((float)rv.x, z32[k], crs);
+        }
       }
     }
   }
-  double tot;
-  if (grid_reduce<false>(acc, part, &sc->tickets[T_RR], &tot) && tid2() == 0) {
+  double tot, cross;
+  if (grid_reduce2(acc, (double)crs, part, &sc->tickets[T_RR], &tot, &cross) && tid2() == 0) {
+    sc->rz_cross = cross;
     sc->rr_prev = sc->rr;
     sc->rr = tot;
     sc->iter += 1;
@@ -459,6 +517,7 @@ __global__ void k_final_solution(FortranIn in, LevelView L, const double* __rest
                                  const double* __restrict__ bvec, const double* __restrict__ us,
                                  const double* __restrict__ vs, double* Pp, double* p, double* u,
                                  double* v, int correct, Scalars* sc, double* part) {
+  pdl_wait();
   const int nx = in.nx, ny = in.ny;
   const int ix = blockIdx.x * kBX + threadIdx.x;
   const int P = L.pitch;
@@ -518,6 +577,7 @@ __global__ void k_final_solution(FortranIn in, LevelView L, const double* __rest
 // top-row continuity (src/ComputePUV_Mod.f90:177-182) and mass residual (:184-216)
 __global__ void k_final_mres(FortranIn in, double vb, double* u, double* v, double* mres,
                              Scalars* sc, double* part) {
+  pdl_wait();
   const int nx = in.nx, ny = in.ny;
   const int ix = blockIdx.x * kBX + threadIdx.x;
   double acc = 0.0;
@@ -546,6 +606,7 @@ __global__ void k_final_mres(FortranIn in, double vb, double* u, double* v, doub
 
 // VariablesInternalCellCondition (src/ComputePUV_Mod.f90:227-245)
 __global__ void k_final_zero(FortranIn in, double* p, double* u, double* v) {
+  pdl_wait();
   const int nx = in.nx, ny = in.ny;
   const int ix = blockIdx.x * kBX + threadIdx.x;
   if (ix >= nx) return;
@@ -559,18 +620,28 @@ __global__ void k_final_zero(FortranIn in, double* p, double* u, double* v) {
 }
 
 __global__ void k_to_fortran(LevelView L, const double* src, double* dst) {
+  pdl_wait();
   const int ix = blockIdx.x * kBX + threadIdx.x;
   if (ix >= L.nx) return;
   for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY)
     dst[(size_t)ix + (size_t)iy * L.nx] = src[(size_t)iy * L.pitch + ix];
 }
 __global__ void k_to_fortran_f(LevelView L, const float* src, double* dst) {
+  pdl_wait();
   const int ix = blockIdx.x * kBX + threadIdx.x;
   if (ix >= L.nx) return;
   for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY)
     dst[(size_t)ix + (size_t)iy * L.nx] = (double)src[(size_t)iy * L.pitch + ix];
 }
+__global__ void k_from_fortran_f(LevelView L, const double* src, float* dst) {
+  pdl_wait();
+  const int ix = blockIdx.x * kBX + threadIdx.x;
+  if (ix >= L.nx) return;
+  for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY)
+    dst[(size_t)iy * L.pitch + ix] = (float)src[(size_t)ix + (size_t)iy * L.nx];
+}
 __global__ void k_from_fortran(LevelView L, const double* src, double* dst) {
+  pdl_wait();
   const int ix = blockIdx.x * kBX + threadIdx.x;
   if (ix >= L.nx) return;
   for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY)
@@ -585,49 +656,54 @@ __global__ void k_from_fortran(LevelView L, const double* src, double* dst) {
 static const dim3 kBlock(kBX, kBY);
 
 void launch_assemble(const FortranIn& in, LevelView L0, Scalars* sc, cudaStream_t s) {
-  k_assemble<<<grid_for(in.nx, in.ny, 1), kBlock, 0, s>>>(in, L0, sc);
+  launch_k(k_assemble, grid_for(in.nx, in.ny, 1), kBlock, 0, s, in, L0, sc);
 }
 void launch_excess(LevelView L, cudaStream_t s) {
-  k_excess<<<grid_for(L.nx, L.ny, 1), kBlock, 0, s>>>(L);
+  launch_k(k_excess, grid_for(L.nx, L.ny, 1), kBlock, 0, s, L);
 }
 void launch_coarsen(LevelView F, LevelView C, cudaStream_t s) {
-  k_coarsen<<<grid_for(C.nx, C.ny, 1), kBlock, 0, s>>>(F, C);
+  launch_k(k_coarsen, grid_for(C.nx, C.ny, 1), kBlock, 0, s, F, C);
 }
 void launch_coarse_setup(LevelView C, double* Ainv, int* cmap, int* nc, cudaStream_t s) {
-  k_coarse_setup<<<1, 256, 0, s>>>(C, Ainv, cmap, nc);
+  launch_k(k_coarse_setup, 1, dim3(256), 0, s, C, Ainv, cmap, nc);
 }
 void launch_rhs(const FortranIn& in, const double* ustar, const double* vstar, double vb,
-                LevelView L0, double* bvec, double* r, double* x, Scalars* sc, double* part,
-                double rtol, int maxit, cudaStream_t s) {
-  k_rhs<<<grid_for(in.nx, in.ny, 1), kBlock, 0, s>>>(in, ustar, vstar, vb, L0.pitch, bvec, r, x,
-                                                      sc, part, rtol, maxit);
+                LevelView L0, double* bvec, double* r, float* r32, double* x, Scalars* sc,
+                double* part, double rtol, int maxit, cudaStream_t s) {
+  launch_k(k_rhs, grid_for(in.nx, in.ny, 1), kBlock, 0, s, in, ustar, vstar, vb, L0.pitch, bvec,
+           r, r32, x, sc, part, rtol, maxit);
 }
-void launch_update_xr(LevelView L0, double* x, const double* p, double* r, const double* q,
-                      Scalars* sc, double* part, unsigned long long cond, cudaStream_t s) {
-  k_update_xr<<<grid_for(L0.nx, L0.ny), kBlock, 0, s>>>(L0, x, p, r, q, sc, part, cond);
+void launch_update_xr(LevelView L0, double* x, const double* p, double* r, float* r32,
+                      const float* z32, const double* q, Scalars* sc, double* part,
+                      unsigned long long cond, cudaStream_t s) {
+  launch_k(k_update_xr, grid_for(L0.nx, L0.ny), kBlock, 0, s, L0, x, p, r, r32, z32, q, sc, part,
+           cond);
 }
 void launch_final_solution(const FortranIn& in, LevelView L0, const double* x,
                            const double* bvec, const double* ustar, const double* vstar,
                            double* Pp, double* p, double* u, double* v, int correct,
                            Scalars* sc, double* part, cudaStream_t s) {
-  k_final_solution<<<grid_for(in.nx, in.ny, 1), kBlock, 0, s>>>(in, L0, x, bvec, ustar, vstar, Pp,
+  launch_k(k_final_solution, grid_for(in.nx, in.ny, 1), kBlock, 0, s, in, L0, x, bvec, ustar, vstar, Pp,
                                                                  p, u, v, correct, sc, part);
 }
 void launch_final_mres(const FortranIn& in, double vb, double* u, double* v, double* mres,
                        Scalars* sc, double* part, cudaStream_t s) {
-  k_final_mres<<<grid_for(in.nx, in.ny, 1), kBlock, 0, s>>>(in, vb, u, v, mres, sc, part);
+  launch_k(k_final_mres, grid_for(in.nx, in.ny, 1), kBlock, 0, s, in, vb, u, v, mres, sc, part);
 }
 void launch_final_zero(const FortranIn& in, double* p, double* u, double* v, cudaStream_t s) {
-  k_final_zero<<<grid_for(in.nx, in.ny, 1), kBlock, 0, s>>>(in, p, u, v);
+  launch_k(k_final_zero, grid_for(in.nx, in.ny, 1), kBlock, 0, s, in, p, u, v);
 }
 void launch_to_fortran(LevelView L, const double* src, double* dst, cudaStream_t s) {
-  k_to_fortran<<<grid_for(L.nx, L.ny, 1), kBlock, 0, s>>>(L, src, dst);
+  launch_k(k_to_fortran, grid_for(L.nx, L.ny, 1), kBlock, 0, s, L, src, dst);
 }
 void launch_to_fortran_f(LevelView L, const float* src, double* dst, cudaStream_t s) {
-  k_to_fortran_f<<<grid_for(L.nx, L.ny, 1), kBlock, 0, s>>>(L, src, dst);
+  launch_k(k_to_fortran_f, grid_for(L.nx, L.ny, 1), kBlock, 0, s, L, src, dst);
+}
+void launch_from_fortran_f(LevelView L, const double* src, float* dst, cudaStream_t s) {
+  launch_k(k_from_fortran_f, grid_for(L.nx, L.ny, 1), kBlock, 0, s, L, src, dst);
 }
 void launch_from_fortran(LevelView L, const double* src, double* dst, cudaStream_t s) {
-  k_from_fortran<<<grid_for(L.nx, L.ny, 1), kBlock, 0, s>>>(L, src, dst);
+  launch_k(k_from_fortran, grid_for(L.nx, L.ny, 1), kBlock, 0, s, L, src, dst);
 }
 
 }  // namespace scf

@@ -1,7 +1,7 @@
 // scf_mg.cu -- multigrid V-cycle kernels, templated on precision:
-//   <double, double, double>           plain FP64 preconditioner
-//   <float, bf16, double | float>      mixed: FP32 state, BF16 couplings; the
-//                                      fine level reads the FP64 residual
+//   <double, double, double>  plain FP64 preconditioner
+//   <float, bf16, float>      mixed: FP32 state, BF16 couplings (the fine level
+//                             reads the FP32 copy of the PCG residual)
 // and the PCG direction update, templated on the type of z.
 //
 // Every smoothing pass is a temporally blocked red-black Gauss-Seidel sweep:
@@ -17,6 +17,8 @@
 //             the coarse right-hand side (needs a 3-cell halo)
 //   RZ        r.z (and r.z_old for the flexible PCG) reduced over the grid,
 //             then the PCG beta
+#include <cstdlib>
+
 #include "scf_mg.cuh"
 
 namespace scf {
@@ -84,19 +86,20 @@ __device__ bool grid_sum2(double a, double b, double* part, unsigned* ticket, do
   return true;
 }
 
-// PCG beta from r.z_new (and r.z_old): plain beta = rz_new / rz_old;
-// flexible (Polak-Ribiere) beta = (r.z_new - r.z_old) / rz_old
-__device__ __forceinline__ void set_beta(Scalars* sc, double rz_new, double rz_cross,
-                                         int flexible) {
+// PCG beta: plain beta = r_k.z_k / r_{k-1}.z_{k-1}; flexible (Polak-Ribiere)
+// beta = (r_k.z_k - r_k.z_{k-1}) / r_{k-1}.z_{k-1}, where the cross term
+// r_k.z_{k-1} was reduced by the previous iteration's x/r update
+__device__ __forceinline__ void set_beta(Scalars* sc, double rz_new, int flexible) {
   if (sc->iter == 0) sc->beta = 0.0;
-  else sc->beta = (flexible ? (rz_new - rz_cross) : rz_new) / sc->rz;
+  else sc->beta = (flexible ? (rz_new - sc->rz_cross) : rz_new) / sc->rz;
   sc->rz = rz_new;
 }
 
 template <class T, class CT, class BT, int FIRST, bool ZERO, bool PROLONG, bool RESTRICT, bool RZ>
 __global__ void __launch_bounds__(NT)
-k_sweep(MgView<T, CT, BT> L, MgView<T, CT, T> C, T omega, const T* __restrict__ zold,
-        int flexible, Scalars* sc, double* part) {
+k_sweep(MgView<T, CT, BT> L, MgView<T, CT, T> C, T omega, int flexible, Scalars* sc,
+        double* part) {
+  pdl_wait();
   if (sc->done) return;
   constexpr int H = RESTRICT ? 3 : 2;  // x halo
   constexpr int WX = SX + 2 * H, WY = SY + 2 * H;
@@ -113,7 +116,7 @@ k_sweep(MgView<T, CT, BT> L, MgView<T, CT, T> C, T omega, const T* __restrict__ 
     T v = T(0);
     if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
       const size_t g = (size_t)gy * P + gx;
-      if (!ZERO) v = L.x[g];
+      if (!ZERO) v = L.xin[g];
       if (PROLONG) {
         if (L.di[g] > T(0)) v = fma(omega, C.x[(size_t)(gy >> 1) * C.pitch + (gx >> 1)], v);
       }
@@ -158,8 +161,9 @@ k_sweep(MgView<T, CT, BT> L, MgView<T, CT, T> C, T omega, const T* __restrict__ 
   }
   __syncthreads();
 
-  // phase 3: write the tile; optional r.z
-  double a1 = 0.0, a2 = 0.0;
+  // phase 3: write the tile; optional r.z (accumulated in T per thread, then
+  // combined in FP64)
+  T a1 = T(0);
   for (int e = t; e < SX * SY; e += NT) {
     const int ex = e % SX, ey = e / SX;
     const int gx = x0 + ex, gy = y0 + ey;
@@ -167,11 +171,7 @@ k_sweep(MgView<T, CT, BT> L, MgView<T, CT, T> C, T omega, const T* __restrict__ 
       const size_t g = (size_t)gy * P + gx;
       const T v = xs[ey + H][ex + H];
       L.x[g] = v;
-      if (RZ) {
-        const double rb = (double)L.b[g];
-        a1 = fma(rb, (double)v, a1);
-        if (flexible) a2 = fma(rb, (double)zold[g], a2);
-      }
+      if (RZ) a1 = fma((T)L.b[g], v, a1);
     }
   }
 
@@ -204,14 +204,15 @@ k_sweep(MgView<T, CT, BT> L, MgView<T, CT, T> C, T omega, const T* __restrict__ 
 
   if (RZ) {
     double tot1, tot2;
-    if (grid_sum2(a1, a2, part, &sc->tickets[T_RZ], &tot1, &tot2) && t == 0)
-      set_beta(sc, tot1, tot2, flexible);
+    if (grid_sum2((double)a1, 0.0, part, &sc->tickets[T_RZ], &tot1, &tot2) && t == 0)
+      set_beta(sc, tot1, flexible);
   }
 }
 
 template <class T, class CT, class BT>
 __global__ void k_coarse_solve_t(MgView<T, CT, BT> C, const double* Ainv, const int* cmap,
                                  const int* ncp, Scalars* sc) {
+  pdl_wait();
   if (sc->done) return;
   __shared__ double bd[kMaxCoarse];
   const int t = threadIdx.x;
@@ -232,8 +233,9 @@ __global__ void k_coarse_solve_t(MgView<T, CT, BT> C, const double* Ainv, const 
 
 // r.z (and r.z_old) when the V-cycle does not end with a sweep
 template <class T, class BT>
-__global__ void k_dot_rz_t(int nx, int ny, int pitch, const BT* r, const T* z, const T* zold,
-                           int flexible, Scalars* sc, double* part) {
+__global__ void k_dot_rz_t(int nx, int ny, int pitch, const BT* r, const T* z, int flexible,
+                           Scalars* sc, double* part) {
+  pdl_wait();
   if (sc->done) return;
   double a1 = 0.0, a2 = 0.0;
   const int ix = blockIdx.x * 32 + threadIdx.x;
@@ -241,11 +243,11 @@ __global__ void k_dot_rz_t(int nx, int ny, int pitch, const BT* r, const T* z, c
     for (int iy = blockIdx.y * 8 + threadIdx.y; iy < ny; iy += gridDim.y * 8) {
       const size_t k = (size_t)iy * pitch + ix;
       a1 = fma((double)r[k], (double)z[k], a1);
-      if (flexible) a2 = fma((double)r[k], (double)zold[k], a2);
+
     }
   double t1, t2;
   if (grid_sum2(a1, a2, part, &sc->tickets[T_RZ], &t1, &t2) && tlin() == 0)
-    set_beta(sc, t1, t2, flexible);
+    set_beta(sc, t1, flexible);
 }
 
 // p_new = z + beta p_old (= z on the first iteration), q = A p_new, p.q and
@@ -255,6 +257,7 @@ template <class ZT>
 __global__ void __launch_bounds__(NT)
 k_pupdate_spmv_t(LevelView L, const ZT* __restrict__ z, const double* __restrict__ pold,
                  double* __restrict__ pnew, double* __restrict__ q, Scalars* sc, double* part) {
+  pdl_wait();
   if (sc->done) return;
   constexpr int WX = SX + 2, WY = SY + 2;
   __shared__ double ps[WY][WX];
@@ -301,6 +304,7 @@ k_pupdate_spmv_t(LevelView L, const ZT* __restrict__ z, const double* __restrict
 
 // inverse diagonal of an FP64 level (0 where the cell has no unknown)
 __global__ void k_inv_diag(int nx, int ny, int pitch, const double* dg, double* di) {
+  pdl_wait();
   const int ix = blockIdx.x * 32 + threadIdx.x;
   if (ix >= nx) return;
   for (int iy = blockIdx.y * 8 + threadIdx.y; iy < ny; iy += gridDim.y * 8) {
@@ -312,6 +316,7 @@ __global__ void k_inv_diag(int nx, int ny, int pitch, const double* dg, double* 
 
 // largest coupling of a level, as the bits of a non-negative float
 __global__ void k_max_coupling(LevelView F, unsigned* out_bits) {
+  pdl_wait();
   float m = 0.0f;
   const int ix = blockIdx.x * 32 + threadIdx.x;
   if (ix < F.nx)
@@ -330,6 +335,7 @@ __global__ void k_max_coupling(LevelView F, unsigned* out_bits) {
 // dominant M-matrix), FP32 inverse diagonal.
 __global__ void k_to_mixed(LevelView F, MgView<float, __nv_bfloat16, float> M,
                            const unsigned* max_bits, float* cscale_out) {
+  pdl_wait();
   const float mx = __uint_as_float(*max_bits);
   int ex = 0;
   frexpf(mx > 0.0f ? mx : 1.0f, &ex);
@@ -358,7 +364,168 @@ __global__ void k_to_mixed(LevelView F, MgView<float, __nv_bfloat16, float> M,
   }
 }
 
+// The coarse end of the V-cycle in one CTA: every level of at most
+// kTailMaxCells cells, down to the dense coarsest solve and back up, with x
+// and b of all those levels in shared memory (each level padded by a zero
+// ghost ring) and the operators read through L1.  Replaces four kernel
+// launches per level, which on such small grids cost launch latency only.
+// The arithmetic is that of k_sweep / k_coarse_solve_t, cell for cell.
+template <class T, class CT>
+__global__ void __launch_bounds__(1024) k_tail(TailDesc<T, CT> d, Scalars* sc) {
+  pdl_wait();
+  if (sc->done) return;
+  extern __shared__ __align__(16) unsigned char tail_smem[];
+  T* sm = reinterpret_cast<T*>(tail_smem);
+  double* bd = reinterpret_cast<double*>(tail_smem + d.bd_off);
+  const int t = threadIdx.x, NTT = blockDim.x;
+  for (int i = t; i < d.total; i += NTT) sm[i] = T(0);
+  __syncthreads();
+  auto W = [&](int l) { return d.lv[l].nx + 2; };
+  auto xs = [&](int l) { return sm + d.off[l]; };
+  auto bs = [&](int l) { return sm + d.off[l] + W(l) * (d.lv[l].ny + 2); };
+  {  // right-hand side of the first tail level (restricted by the previous kernel)
+    const MgView<T, CT, T>& L = d.lv[0];
+    T* b = bs(0);
+    for (int k = t; k < L.nx * L.ny; k += NTT) {
+      const int ix = k % L.nx, iy = k / L.nx;
+      b[(iy + 1) * W(0) + ix + 1] = L.b[(size_t)iy * L.pitch + ix];
+    }
+  }
+  __syncthreads();
+  auto relax = [&](int l, int colour) {
+    const MgView<T, CT, T>& L = d.lv[l];
+    const float cs = L.csp ? __ldg(L.csp) : 1.0f;
+    T* x = xs(l);
+    const T* b = bs(l);
+    const int w = W(l), P = L.pitch;
+    for (int k = t; k < L.nx * L.ny; k += NTT) {
+      const int ix = k % L.nx, iy = k / L.nx;
+      if (((ix + iy) & 1) != colour) continue;
+      const size_t g = (size_t)iy * P + ix;
+      const int si = (iy + 1) * w + ix + 1;
+      T s = b[si];
+      s = fma(cload<CT, T>(L.cE, g, cs), x[si + 1], s);
+      s = fma(cload<CT, T>(L.cE, g - 1, cs), x[si - 1], s);
+      s = fma(cload<CT, T>(L.cN, g, cs), x[si + w], s);
+      s = fma(cload<CT, T>(L.cN, g - P, cs), x[si - w], s);
+      x[si] = s * L.di[g];
+    }
+    __syncthreads();
+  };
+  const int n = d.n;
+  for (int l = 0; l < n - 1; ++l) {
+    for (int it = 0; it < d.npre; ++it) { relax(l, 0); relax(l, 1); }
+    // residual summed 2x2 onto level l+1
+    const MgView<T, CT, T>& L = d.lv[l];
+    const MgView<T, CT, T>& C = d.lv[l + 1];
+    const float cs = L.csp ? __ldg(L.csp) : 1.0f;
+    const T* x = xs(l);
+    const T* b = bs(l);
+    T* bc = bs(l + 1);
+    const int w = W(l), wc = W(l + 1), P = L.pitch;
+    for (int k = t; k < C.nx * C.ny; k += NTT) {
+      const int I = k % C.nx, J = k / C.nx;
+      T s = T(0);
+      for (int dj = 0; dj < 2; ++dj)
+        for (int dq = 0; dq < 2; ++dq) {
+          const int gx = 2 * I + dq, gy = 2 * J + dj;
+          if (gx >= L.nx || gy >= L.ny) continue;
+          const size_t g = (size_t)gy * P + gx;
+          const T dgv = L.dg[g];
+          if (dgv < T(0)) continue;
+          const int si = (gy + 1) * w + gx + 1;
+          T r = fma(-dgv, x[si], b[si]);
+          r = fma(cload<CT, T>(L.cE, g, cs), x[si + 1], r);
+          r = fma(cload<CT, T>(L.cE, g - 1, cs), x[si - 1], r);
+          r = fma(cload<CT, T>(L.cN, g, cs), x[si + w], r);
+          r = fma(cload<CT, T>(L.cN, g - P, cs), x[si - w], r);
+          s += r;
+        }
+      bc[(J + 1) * wc + I + 1] = s;
+    }
+    __syncthreads();
+  }
+  {  // dense FP64 solve on the coarsest level
+    const MgView<T, CT, T>& C = d.lv[n - 1];
+    const int ncell = C.nx * C.ny, nn = *d.nc, w = W(n - 1);
+    const T* b = bs(n - 1);
+    T* x = xs(n - 1);
+    for (int k = t; k < ncell; k += NTT) {
+      const int r = d.cmap[k];
+      if (r >= 0) bd[r] = (double)b[(k / C.nx + 1) * w + (k % C.nx) + 1];
+    }
+    __syncthreads();
+    for (int k = t; k < ncell; k += NTT) {
+      const int r = d.cmap[k];
+      double y = 0.0;
+      if (r >= 0)
+        for (int c = 0; c < nn; ++c) y = fma(d.Ainv[r * nn + c], bd[c], y);
+      x[(k / C.nx + 1) * w + (k % C.nx) + 1] = (T)y;
+    }
+    __syncthreads();
+  }
+  for (int l = n - 2; l >= 0; --l) {
+    const MgView<T, CT, T>& L = d.lv[l];
+    T* x = xs(l);
+    const T* xc = xs(l + 1);
+    const int w = W(l), wc = W(l + 1);
+    for (int k = t; k < L.nx * L.ny; k += NTT) {
+      const int ix = k % L.nx, iy = k / L.nx;
+      if (L.di[(size_t)iy * L.pitch + ix] > T(0)) {
+        const int si = (iy + 1) * w + ix + 1;
+        x[si] = fma(d.omega, xc[((iy >> 1) + 1) * wc + (ix >> 1) + 1], x[si]);
+      }
+    }
+    __syncthreads();
+    for (int it = 0; it < d.npost; ++it) { relax(l, 1); relax(l, 0); }
+  }
+  {  // x of the first tail level back to global memory
+    const MgView<T, CT, T>& L = d.lv[0];
+    const T* x = xs(0);
+    for (int k = t; k < L.nx * L.ny; k += NTT) {
+      const int ix = k % L.nx, iy = k / L.nx;
+      L.x[(size_t)iy * L.pitch + ix] = x[(iy + 1) * W(0) + ix + 1];
+    }
+  }
+}
+
 }  // namespace
+
+template <class T, class CT>
+int tail_prepare(TailDesc<T, CT>& d) {
+  int off = 0;
+  for (int l = 0; l < d.n; ++l) {
+    d.off[l] = off;
+    off += 2 * (d.lv[l].nx + 2) * (d.lv[l].ny + 2);
+  }
+  d.total = off;
+  size_t bytes = (size_t)off * sizeof(T);
+  bytes = (bytes + 15) / 16 * 16;
+  d.bd_off = (int)bytes;
+  bytes += kMaxCoarse * sizeof(double);
+  d.smem = (int)bytes;
+  if (cudaFuncSetAttribute(k_tail<T, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           d.smem) != cudaSuccess)
+    return -1;
+  return 0;
+}
+
+template <class T, class CT>
+void launch_tail(const TailDesc<T, CT>& d, Scalars* sc, cudaStream_t s) {
+  launch_k(k_tail<T, CT>, dim3(1), dim3(1024), (size_t)d.smem, s, d, sc);
+}
+
+template int tail_prepare<double, double>(TailDesc<double, double>&);
+template int tail_prepare<float, __nv_bfloat16>(TailDesc<float, __nv_bfloat16>&);
+template void launch_tail<double, double>(const TailDesc<double, double>&, Scalars*,
+                                          cudaStream_t);
+template void launch_tail<float, __nv_bfloat16>(const TailDesc<float, __nv_bfloat16>&, Scalars*,
+                                                cudaStream_t);
+
+bool pdl_enabled() {
+  static const bool on = getenv("SCF_NO_PDL") == nullptr;
+  return on;
+}
 
 static dim3 tiles(int nx, int ny) { return dim3((nx + SX - 1) / SX, (ny + SY - 1) / SY); }
 static dim3 small_grid(int nx, int ny) {
@@ -368,12 +535,12 @@ static dim3 small_grid(int nx, int ny) {
 
 template <class T, class CT, class BT>
 void launch_sweep(const MgView<T, CT, BT>& L, const MgView<T, CT, T>& C, int first, bool zero,
-                  bool prolong, bool restrict_, bool rz, double omega, const T* zold,
-                  int flexible, Scalars* sc, double* part, cudaStream_t s) {
+                  bool prolong, bool restrict_, bool rz, double omega, int flexible, Scalars* sc,
+                  double* part, cudaStream_t s) {
   const dim3 g = tiles(L.nx, L.ny);
   const T om = (T)omega;
 #define SCF_SWEEP(F, Z, PR, RS, R) \
-  k_sweep<T, CT, BT, F, Z, PR, RS, R><<<g, NT, 0, s>>>(L, C, om, zold, flexible, sc, part)
+  launch_k(k_sweep<T, CT, BT, F, Z, PR, RS, R>, g, dim3(NT), 0, s, L, C, om, flexible, sc, part)
   // the combinations the V-cycle uses (pre: red first; post: black first)
   if (first == 0 && zero && !prolong && !restrict_ && !rz) SCF_SWEEP(0, true, false, false, false);
   else if (first == 0 && zero && !prolong && restrict_ && !rz) SCF_SWEEP(0, true, false, true, false);
@@ -389,51 +556,49 @@ void launch_sweep(const MgView<T, CT, BT>& L, const MgView<T, CT, T>& C, int fir
 template <class T, class CT, class BT>
 void launch_coarse_solve_t(const MgView<T, CT, BT>& C, const double* Ainv, const int* cmap,
                            const int* nc, Scalars* sc, cudaStream_t s) {
-  k_coarse_solve_t<T, CT, BT><<<1, 64, 0, s>>>(C, Ainv, cmap, nc, sc);
+  launch_k(k_coarse_solve_t<T, CT, BT>, dim3(1), dim3(64), 0, s, C, Ainv, cmap, nc, sc);
 }
 
 template <class T, class BT>
-void launch_dot_rz_t(int nx, int ny, int pitch, const BT* r, const T* z, const T* zold,
-                     int flexible, Scalars* sc, double* part, cudaStream_t s) {
-  k_dot_rz_t<T, BT><<<small_grid(nx, ny), dim3(32, 8), 0, s>>>(nx, ny, pitch, r, z, zold,
-                                                                 flexible, sc, part);
+void launch_dot_rz_t(int nx, int ny, int pitch, const BT* r, const T* z, int flexible,
+                     Scalars* sc, double* part, cudaStream_t s) {
+  launch_k(k_dot_rz_t<T, BT>, small_grid(nx, ny), dim3(32, 8), 0, s, nx, ny, pitch, r, z,
+           flexible, sc, part);
 }
 
 template <class ZT>
 void launch_pupdate_spmv_t(LevelView L0, const ZT* z, const double* pold, double* pnew,
                            double* q, Scalars* sc, double* part, cudaStream_t s) {
-  k_pupdate_spmv_t<ZT><<<tiles(L0.nx, L0.ny), NT, 0, s>>>(L0, z, pold, pnew, q, sc, part);
+  launch_k(k_pupdate_spmv_t<ZT>, tiles(L0.nx, L0.ny), dim3(NT), 0, s, L0, z, pold, pnew, q, sc, part);
 }
 
 void launch_inv_diag(const LevelView& L, double* di, cudaStream_t s) {
-  k_inv_diag<<<small_grid(L.nx, L.ny), dim3(32, 8), 0, s>>>(L.nx, L.ny, L.pitch, L.dg, di);
+  launch_k(k_inv_diag, small_grid(L.nx, L.ny), dim3(32, 8), 0, s, L.nx, L.ny, L.pitch, (const double*)L.dg, di);
 }
 
 void launch_max_coupling(const LevelView& L, unsigned* out_bits, cudaStream_t s) {
   cudaMemsetAsync(out_bits, 0, sizeof(unsigned), s);
-  k_max_coupling<<<small_grid(L.nx, L.ny), dim3(32, 8), 0, s>>>(L, out_bits);
+  launch_k(k_max_coupling, small_grid(L.nx, L.ny), dim3(32, 8), 0, s, L, out_bits);
 }
 
 void launch_to_mixed(const LevelView& F, const MgView<float, __nv_bfloat16, float>& M,
                      const unsigned* max_bits, float* cscale_out, cudaStream_t s) {
-  k_to_mixed<<<small_grid(F.nx, F.ny), dim3(32, 8), 0, s>>>(F, M, max_bits, cscale_out);
+  launch_k(k_to_mixed, small_grid(F.nx, F.ny), dim3(32, 8), 0, s, F, M, max_bits, cscale_out);
 }
 
 #define SCF_INST(T, CT, BT)                                                                   \
   template void launch_sweep<T, CT, BT>(const MgView<T, CT, BT>&, const MgView<T, CT, T>&, int, \
-                                        bool, bool, bool, bool, double, const T*, int,          \
-                                        Scalars*, double*, cudaStream_t);                       \
+                                        bool, bool, bool, bool, double, int, Scalars*, double*, \
+                                        cudaStream_t);                                          \
   template void launch_coarse_solve_t<T, CT, BT>(const MgView<T, CT, BT>&, const double*,      \
                                                  const int*, const int*, Scalars*, cudaStream_t);
 SCF_INST(double, double, double)
 SCF_INST(float, __nv_bfloat16, float)
-SCF_INST(float, __nv_bfloat16, double)
 #undef SCF_INST
-template void launch_dot_rz_t<double, double>(int, int, int, const double*, const double*,
-                                              const double*, int, Scalars*, double*,
-                                              cudaStream_t);
-template void launch_dot_rz_t<float, double>(int, int, int, const double*, const float*,
-                                             const float*, int, Scalars*, double*, cudaStream_t);
+template void launch_dot_rz_t<double, double>(int, int, int, const double*, const double*, int,
+                                              Scalars*, double*, cudaStream_t);
+template void launch_dot_rz_t<float, float>(int, int, int, const float*, const float*, int,
+                                            Scalars*, double*, cudaStream_t);
 template void launch_pupdate_spmv_t<double>(LevelView, const double*, const double*, double*,
                                             double*, Scalars*, double*, cudaStream_t);
 template void launch_pupdate_spmv_t<float>(LevelView, const float*, const double*, double*,

@@ -17,25 +17,51 @@ struct MgView {
   const CT* cN;
   const T* dg;  // diagonal, negative where the cell has no unknown
   const T* di;  // inverse diagonal, 0 where the cell has no unknown
-  T* x;
+  T* x;         // iterate written by a sweep
   BT* b;
+  const T* xin;  // iterate read by a sweep: the other buffer of the level's pair.
+                 // A fused sweep reads its halo from neighbouring tiles, which
+                 // other CTAs of the same kernel overwrite, so input and output
+                 // must never alias.
   const float* csp;  // device pointer to the BF16 coupling scale (power of two);
                      // null for FP64 levels.  Kept in device memory so that a
                      // captured graph stays valid when the operator is reassembled.
 };
 
+// The coarse end of a V-cycle in one CTA (levels of at most kTailMaxCells
+// cells, the last of them the coarsest).
+constexpr int kTailMaxCells = 4096;
+constexpr int kTailMaxLevels = 12;
+template <class T, class CT>
+struct TailDesc {
+  int n;  // number of tail levels
+  MgView<T, CT, T> lv[kTailMaxLevels];
+  int off[kTailMaxLevels];  // shared-memory offset of each level's x (b follows)
+  int total;                // elements of T in shared memory
+  int bd_off, smem;         // byte offset of the coarse gather buffer, total bytes
+  int npre, npost;
+  T omega;
+  const double* Ainv;
+  const int* cmap;
+  const int* nc;
+};
+template <class T, class CT>
+int tail_prepare(TailDesc<T, CT>& d);  // fills offsets and sizes; 0 on success
+template <class T, class CT>
+void launch_tail(const TailDesc<T, CT>& d, Scalars* sc, cudaStream_t s);
+
 template <class T, class CT, class BT>
 void launch_sweep(const MgView<T, CT, BT>& L, const MgView<T, CT, T>& C, int first, bool zero,
-                  bool prolong, bool restrict_, bool rz, double omega, const T* zold,
-                  int flexible, Scalars* sc, double* part, cudaStream_t s);
+                  bool prolong, bool restrict_, bool rz, double omega, int flexible, Scalars* sc,
+                  double* part, cudaStream_t s);
 
 template <class T, class CT, class BT>
 void launch_coarse_solve_t(const MgView<T, CT, BT>& C, const double* Ainv, const int* cmap,
                            const int* nc, Scalars* sc, cudaStream_t s);
 
 template <class T, class BT>
-void launch_dot_rz_t(int nx, int ny, int pitch, const BT* r, const T* z, const T* zold,
-                     int flexible, Scalars* sc, double* part, cudaStream_t s);
+void launch_dot_rz_t(int nx, int ny, int pitch, const BT* r, const T* z, int flexible,
+                     Scalars* sc, double* part, cudaStream_t s);
 
 template <class ZT>
 void launch_pupdate_spmv_t(LevelView L0, const ZT* z, const double* pold, double* pnew,

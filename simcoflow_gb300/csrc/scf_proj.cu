@@ -23,7 +23,6 @@ using namespace scf;
 using bf16 = __nv_bfloat16;
 using MgD = MgView<double, double, double>;
 using MgF = MgView<float, bf16, float>;
-using MgF0 = MgView<float, bf16, double>;
 
 struct scf_proj {
   int nx = 0, ny = 0;
@@ -38,10 +37,15 @@ struct scf_proj {
   // the PCG, its b is the PCG residual r and its x the FP64 z)
   std::vector<LevelView> lev;
   std::vector<double*> di64;  // FP64 inverse diagonals
+  std::vector<double*> x2_64; // second iterate buffer of each FP64 level
+  std::vector<float*> x2_32;  // second iterate buffer of each mixed level
   // mixed levels (FP32 state, BF16 couplings), built from lev at assemble
   std::vector<MgF> mix;
-  float* zA = nullptr;  // mixed fine-level z, ping-pong pair
-  float* zB = nullptr;
+  float* r32 = nullptr;  // FP32 copy of the PCG residual (mixed)
+  // single-CTA tail of the V-cycle: levels tail0 .. L-1 (tail0 = 0: none)
+  int tail0 = 0;
+  TailDesc<double, double> tail64{};
+  TailDesc<float, bf16> tail32{};
   float* cscale = nullptr;      // device, one BF16 scale per level
   unsigned* maxbits = nullptr;  // device, one per level
   std::vector<void*> allocs;
@@ -124,74 +128,116 @@ void destroy_graph(scf_proj* h) {
 
 MgD view64(scf_proj* h, int l) {
   const LevelView& L = h->lev[l];
-  return MgD{L.nx, L.ny, L.pitch, L.cE, L.cN, L.dg, h->di64[l], L.x, L.b, nullptr};
+  MgD v{};
+  v.nx = L.nx; v.ny = L.ny; v.pitch = L.pitch;
+  v.cE = L.cE; v.cN = L.cN; v.dg = L.dg; v.di = h->di64[l];
+  v.x = L.x; v.b = L.b; v.xin = nullptr; v.csp = nullptr;
+  return v;
 }
 
-// Enqueue one V-cycle.  Level 0 has right-hand side b0 (the PCG residual)
-// and iterate x0 (z); coarse levels are `coarse(l)`.  do_rz: the last
-// kernel reduces r.z (and r.z_old when flexible) and sets the PCG beta.
-template <class T, class CT, class BT, class CoarseFn>
-void enqueue_vcycle_t(scf_proj* h, MgView<T, CT, BT> L0, CoarseFn coarse, Scalars* sc,
-                      bool do_rz, const T* zold, int flexible, cudaStream_t s) {
+// the two iterate buffers of a level; buffer 0 is the one in the base view
+double* buf64(scf_proj* h, int l, int i) { return i == 0 ? h->lev[l].x : h->x2_64[l]; }
+float* buf32(scf_proj* h, int l, int i) { return i == 0 ? h->mix[l].x : h->x2_32[l]; }
+
+// Buffer holding a level's result after its part of the V-cycle: sweeps
+// alternate buffers (npre down, npost up, starting from buffer 0), the tail
+// and the coarse solve write buffer 0.
+int final_buf(scf_proj* h, int l) {
+  const int L = (int)h->lev.size();
+  const int lk = h->tail0 > 0 ? h->tail0 : L - 1;
+  if (L == 1 || l >= lk) return 0;
+  return (h->opts.npre - 1 + h->opts.npost) % 2;
+}
+
+// Enqueue one V-cycle.  `view(l)` is the base view of level l (level 0's b
+// is the PCG residual), `buf(l, i)` its two iterate buffers.  do_rz: the
+// last kernel reduces r.z and sets the PCG beta.
+template <class T, class CT, class ViewFn, class BufFn>
+void enqueue_vcycle_t(scf_proj* h, ViewFn view, BufFn buf, const TailDesc<T, CT>& tail,
+                      Scalars* sc, bool do_rz, int flexible, cudaStream_t s) {
+  using V = MgView<T, CT, T>;
   const int L = (int)h->lev.size();
   const int npre = h->opts.npre, npost = h->opts.npost;
   const double om = h->opts.omega;
   if (L == 1) {
-    launch_coarse_solve_t(L0, h->Ainv, h->cmap, h->ncoarse, sc, s);
-    if (do_rz)
-      launch_dot_rz_t<T, BT>(L0.nx, L0.ny, L0.pitch, L0.b, L0.x, zold, flexible, sc, h->part, s);
+    V c = view(0);
+    c.x = buf(0, 0);
+    launch_coarse_solve_t(c, h->Ainv, h->cmap, h->ncoarse, sc, s);
+    if (do_rz) launch_dot_rz_t<T, T>(c.nx, c.ny, c.pitch, c.b, c.x, flexible, sc, h->part, s);
     return;
   }
-  // down leg
-  auto down = [&](auto V, const MgView<T, CT, T>& C) {
-    for (int it = 0; it < npre; ++it)
-      launch_sweep(V, C, 0, it == 0, false, it == npre - 1, false, om, (const T*)nullptr, 0, sc,
-                   h->part, s);
+  // levels 0 .. lk-1 run as kernels; the tail (or the coarse solve) covers lk .. L-1
+  const int lk = h->tail0 > 0 ? h->tail0 : L - 1;
+  auto coarse_result = [&](int l) {  // level l with x = its final buffer
+    V c = view(l);
+    c.x = buf(l, final_buf(h, l));
+    return c;
   };
-  down(L0, coarse(1));
-  for (int l = 1; l < L - 1; ++l) down(coarse(l), coarse(l + 1));
-  launch_coarse_solve_t(coarse(L - 1), h->Ainv, h->cmap, h->ncoarse, sc, s);
-  // up leg
-  auto up = [&](auto V, const MgView<T, CT, T>& C, bool fine) {
-    for (int it = 0; it < npost; ++it) {
-      const bool rz = fine && do_rz && it == npost - 1;
-      launch_sweep(V, C, 1, false, it == 0, false, rz, om, zold, flexible, sc, h->part, s);
+  for (int l = 0; l < lk; ++l) {
+    V f = view(l);
+    const V c = view(l + 1);  // restriction target (its b)
+    for (int it = 0; it < npre; ++it) {
+      f.xin = it > 0 ? buf(l, (it - 1) % 2) : nullptr;
+      f.x = buf(l, it % 2);
+      launch_sweep(f, c, 0, it == 0, false, it == npre - 1, false, om, flexible, sc, h->part, s);
     }
-  };
-  for (int l = L - 2; l >= 1; --l) up(coarse(l), coarse(l + 1), false);
-  up(L0, coarse(1), true);
+  }
+  if (h->tail0 > 0) {
+    launch_tail(tail, sc, s);
+  } else {
+    V c = view(L - 1);
+    c.x = buf(L - 1, 0);
+    launch_coarse_solve_t(c, h->Ainv, h->cmap, h->ncoarse, sc, s);
+  }
+  for (int l = lk - 1; l >= 0; --l) {
+    V f = view(l);
+    const V c = coarse_result(l + 1);
+    for (int it = 0; it < npost; ++it) {
+      f.xin = buf(l, (npre - 1 + it) % 2);
+      f.x = buf(l, (npre + it) % 2);
+      const bool rz = l == 0 && do_rz && it == npost - 1;
+      launch_sweep(f, c, 1, false, it == 0, false, rz, om, flexible, sc, h->part, s);
+    }
+  }
 }
 
-// V-cycle of the handle's precision on level 0: b0 = r (FP64), x = z
-void enqueue_vcycle(scf_proj* h, Scalars* sc, bool do_rz, bool ping, cudaStream_t s) {
+// V-cycle of the handle's precision on level 0: b = r (or its FP32 copy), x = z
+void enqueue_vcycle(scf_proj* h, Scalars* sc, bool do_rz, cudaStream_t s) {
   if (!h->mixed) {
-    auto coarse = [h](int l) { return view64(h, l); };
-    enqueue_vcycle_t(h, view64(h, 0), coarse, sc, do_rz, (const double*)nullptr, 0, s);
+    auto view = [h](int l) { return view64(h, l); };
+    auto buf = [h](int l, int i) { return buf64(h, l, i); };
+    enqueue_vcycle_t(h, view, buf, h->tail64, sc, do_rz, 0, s);
   } else {
-    const MgF& m0 = h->mix[0];
-    MgF0 L0{m0.nx, m0.ny, m0.pitch, m0.cE, m0.cN, m0.dg, m0.di, ping ? h->zB : h->zA,
-            h->lev[0].b, m0.csp};
-    auto coarse = [h](int l) { return h->mix[l]; };
-    enqueue_vcycle_t(h, L0, coarse, sc, do_rz, ping ? h->zA : h->zB, 1, s);
+    auto view = [h](int l) {
+      MgF v = h->mix[l];
+      if (l == 0) v.b = h->r32;
+      return v;
+    };
+    auto buf = [h](int l, int i) { return buf32(h, l, i); };
+    enqueue_vcycle_t(h, view, buf, h->tail32, sc, do_rz, 1, s);
   }
 }
 
 // one PCG iteration: z = M r, beta, p = z + beta p_old, q = A p, alpha,
-// x += alpha p, r -= alpha q, convergence test
-void enqueue_iteration(scf_proj* h, const double* pold, double* pnew, bool ping,
-                       unsigned long long cond, cudaStream_t s) {
+// x += alpha p, r -= alpha q (and the flexible cross term), convergence test
+void enqueue_iteration(scf_proj* h, const double* pold, double* pnew, unsigned long long cond,
+                       cudaStream_t s) {
   LevelView L0 = h->lev[0];
-  enqueue_vcycle(h, h->sc, true, ping, s);
-  if (!h->mixed)
-    launch_pupdate_spmv_t<double>(L0, L0.x, pold, pnew, h->q, h->sc, h->part, s);
-  else
-    launch_pupdate_spmv_t<float>(L0, ping ? h->zB : h->zA, pold, pnew, h->q, h->sc, h->part, s);
-  launch_update_xr(L0, h->xsol, pnew, L0.b, h->q, h->sc, h->part, cond, s);
+  const int zf = final_buf(h, 0);
+  enqueue_vcycle(h, h->sc, true, s);
+  if (!h->mixed) {
+    launch_pupdate_spmv_t<double>(L0, buf64(h, 0, zf), pold, pnew, h->q, h->sc, h->part, s);
+    launch_update_xr(L0, h->xsol, pnew, L0.b, nullptr, nullptr, h->q, h->sc, h->part, cond, s);
+  } else {
+    const float* z = buf32(h, 0, zf);
+    launch_pupdate_spmv_t<float>(L0, z, pold, pnew, h->q, h->sc, h->part, s);
+    launch_update_xr(L0, h->xsol, pnew, L0.b, h->r32, z, h->q, h->sc, h->part, cond, s);
+  }
 }
 
 void enqueue_body(scf_proj* h, unsigned long long cond, cudaStream_t s) {
-  enqueue_iteration(h, h->pA, h->pB, false, cond, s);
-  enqueue_iteration(h, h->pB, h->pA, true, cond, s);
+  enqueue_iteration(h, h->pA, h->pB, cond, s);
+  enqueue_iteration(h, h->pB, h->pA, cond, s);
 }
 
 int build_graph(scf_proj* h) {
@@ -333,8 +379,8 @@ int solve_common(scf_proj* h, const double* ustar, const double* vstar, double v
   LevelView L0 = h->lev[0];
   // the NaN flag of a previous solve must not leak into this one
   CK(cudaMemsetAsync(&h->sc->nan, 0, sizeof(int), s));
-  launch_rhs(h->fin, dus, dvs, vb, L0, h->bvec, L0.b, h->xsol, h->sc, h->part, h->opts.rtol,
-             h->opts.maxit, s);
+  launch_rhs(h->fin, dus, dvs, vb, L0, h->bvec, L0.b, h->r32, h->xsol, h->sc, h->part,
+             h->opts.rtol, h->opts.maxit, s);
   CK(cudaGetLastError());
   int rc = run_pcg(h);
   if (rc) return rc;
@@ -449,8 +495,11 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
       if ((rc = level_array(h, ly, L.pitch, a))) return fail(rc);
     double* di = nullptr;
     if ((rc = level_array(h, ly, L.pitch, &di))) return fail(rc);
+    double* x2 = nullptr;
+    if ((rc = level_array(h, ly, L.pitch, &x2))) return fail(rc);
     h->lev.push_back(L);
     h->di64.push_back(di);
+    h->x2_64.push_back(x2);
     if ((long)lx * ly <= o.coarse_max || (lx == 1 && ly == 1) || h->lev.size() >= 30) break;
     lx = (lx + 1) / 2; ly = (ly + 1) / 2;
   }
@@ -461,15 +510,20 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
     for (int l = 0; l < nlev; ++l) {
       const LevelView& F = h->lev[l];
       bf16 *ce = nullptr, *cn = nullptr;
-      float *dg = nullptr, *di = nullptr, *x = nullptr, *b = nullptr;
+      float *dg = nullptr, *di = nullptr, *x = nullptr, *x2 = nullptr, *b = nullptr;
       if ((rc = level_array(h, F.ny, F.pitch, &ce)) || (rc = level_array(h, F.ny, F.pitch, &cn)) ||
           (rc = level_array(h, F.ny, F.pitch, &dg)) || (rc = level_array(h, F.ny, F.pitch, &di)) ||
-          (rc = level_array(h, F.ny, F.pitch, &x)) || (rc = level_array(h, F.ny, F.pitch, &b)))
+          (rc = level_array(h, F.ny, F.pitch, &x)) || (rc = level_array(h, F.ny, F.pitch, &x2)) ||
+          (rc = level_array(h, F.ny, F.pitch, &b)))
         return fail(rc);
-      h->mix.push_back(MgF{F.nx, F.ny, F.pitch, ce, cn, dg, di, x, b, h->cscale + l});
+      MgF v{};
+      v.nx = F.nx; v.ny = F.ny; v.pitch = F.pitch;
+      v.cE = ce; v.cN = cn; v.dg = dg; v.di = di;
+      v.x = x; v.b = b; v.xin = nullptr; v.csp = h->cscale + l;
+      h->mix.push_back(v);
+      h->x2_32.push_back(x2);
     }
-    h->zA = h->mix[0].x;
-    if ((rc = level_array(h, ny, h->lev[0].pitch, &h->zB))) return fail(rc);
+    if ((rc = level_array(h, ny, h->lev[0].pitch, &h->r32))) return fail(rc);
   }
   const int P0 = h->lev[0].pitch;
   double** pv[5] = {&h->xsol, &h->pA, &h->pB, &h->q, &h->bvec};
@@ -478,6 +532,24 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
   if ((rc = dev_alloc(h, (void**)&h->Ainv, sizeof(double) * kMaxCoarse * kMaxCoarse))) return fail(rc);
   if ((rc = dev_alloc(h, (void**)&h->cmap, sizeof(int) * kMaxCoarse))) return fail(rc);
   if ((rc = dev_alloc(h, (void**)&h->ncoarse, sizeof(int)))) return fail(rc);
+  // the single-CTA tail: first level >= 1 with at most kTailMaxCells cells
+  for (int l = 1; l < nlev; ++l)
+    if ((long)h->lev[l].nx * h->lev[l].ny <= kTailMaxCells) { h->tail0 = l; break; }
+  if (h->tail0 > 0 && nlev - h->tail0 > kTailMaxLevels) h->tail0 = 0;
+  if (h->tail0 > 0 && getenv("SCF_NO_TAIL")) h->tail0 = 0;
+  if (h->tail0 > 0) {
+    auto fill = [&](auto& d, auto view) {
+      d.n = nlev - h->tail0;
+      for (int l = 0; l < d.n; ++l) d.lv[l] = view(h->tail0 + l);
+      d.npre = o.npre; d.npost = o.npost;
+      d.omega = (decltype(d.omega))o.omega;
+      d.Ainv = h->Ainv; d.cmap = h->cmap; d.nc = h->ncoarse;
+      return tail_prepare(d);
+    };
+    int bad = fill(h->tail64, [h](int l) { return view64(h, l); });
+    if (h->mixed) bad |= fill(h->tail32, [h](int l) { return h->mix[l]; });
+    if (bad) h->tail0 = 0;
+  }
   if ((rc = dev_alloc(h, (void**)&h->sc, sizeof(Scalars)))) return fail(rc);
   if ((rc = dev_alloc(h, (void**)&h->sc_diag, sizeof(Scalars)))) return fail(rc);
   size_t nblk = 0;
@@ -670,12 +742,15 @@ int scf_proj_time_kernel(scf_proj* h, int kernel, int reps, double* ms) {
   const double om = h->opts.omega;
   auto launch = [&]() {
     if (kernel == SCF_K_PUPDATE_SPMV) {
-      if (h->mixed) launch_pupdate_spmv_t<float>(L0, h->zA, h->pA, h->pB, h->q, h->sc_diag, h->part, s);
-      else launch_pupdate_spmv_t<double>(L0, L0.x, h->pA, h->pB, h->q, h->sc_diag, h->part, s);
+      if (h->mixed)
+        launch_pupdate_spmv_t<float>(L0, buf32(h, 0, 0), h->pA, h->pB, h->q, h->sc_diag, h->part, s);
+      else
+        launch_pupdate_spmv_t<double>(L0, L0.x, h->pA, h->pB, h->q, h->sc_diag, h->part, s);
       return;
     }
     if (kernel == SCF_K_UPDATE_XR) {
-      launch_update_xr(L0, h->xsol, h->pB, L0.b, h->q, h->sc_diag, h->part, 0ull, s);
+      launch_update_xr(L0, h->xsol, h->pB, L0.b, h->r32, h->mixed ? buf32(h, 0, 0) : nullptr, h->q,
+                       h->sc_diag, h->part, 0ull, s);
       return;
     }
     if (kernel == SCF_K_ASSEMBLE) {
@@ -687,13 +762,17 @@ int scf_proj_time_kernel(scf_proj* h, int kernel, int reps, double* ms) {
                prol = kernel == SCF_K_PROLONG;
     const int first = restr ? 0 : 1;
     if (!h->mixed) {
-      launch_sweep(view64(h, 0), view64(h, 1), first, false, prol, restr, false, om,
-                   (const double*)nullptr, 0, h->sc_diag, h->part, s);
+      MgD V = view64(h, 0);
+      V.xin = buf64(h, 0, 0);
+      V.x = buf64(h, 0, 1);
+      launch_sweep(V, view64(h, 1), first, false, prol, restr, false, om, 0, h->sc_diag, h->part,
+                   s);
     } else {
-      const MgF& m0 = h->mix[0];
-      MgF0 V{m0.nx, m0.ny, m0.pitch, m0.cE, m0.cN, m0.dg, m0.di, h->zA, L0.b, m0.csp};
-      launch_sweep(V, h->mix[1], first, false, prol, restr, false, om, (const float*)nullptr, 0,
-                   h->sc_diag, h->part, s);
+      MgF V = h->mix[0];
+      V.xin = buf32(h, 0, 0);
+      V.x = buf32(h, 0, 1);
+      V.b = h->r32;
+      launch_sweep(V, h->mix[1], first, false, prol, restr, false, om, 1, h->sc_diag, h->part, s);
     }
     (void)smooth;
   };
@@ -717,10 +796,12 @@ int scf_proj_vcycle(scf_proj* h, const double* b, double* x) {
   CK(cudaMallocAsync((void**)&tmp, n1 * 8, s));
   CK(cudaMemcpyAsync(tmp, b, n1 * 8, cudaMemcpyHostToDevice, s));
   launch_from_fortran(h->lev[0], tmp, h->lev[0].b, s);
+  if (h->mixed) launch_from_fortran_f(h->lev[0], tmp, h->r32, s);
   CK(cudaMemsetAsync(h->sc_diag, 0, sizeof(Scalars), s));
-  enqueue_vcycle(h, h->sc_diag, false, false, s);
-  if (h->mixed) launch_to_fortran_f(h->lev[0], h->zA, tmp, s);
-  else launch_to_fortran(h->lev[0], h->lev[0].x, tmp, s);
+  enqueue_vcycle(h, h->sc_diag, false, s);
+  const int zf = final_buf(h, 0);
+  if (h->mixed) launch_to_fortran_f(h->lev[0], buf32(h, 0, zf), tmp, s);
+  else launch_to_fortran(h->lev[0], buf64(h, 0, zf), tmp, s);
   CK(cudaMemcpyAsync(x, tmp, n1 * 8, cudaMemcpyDeviceToHost, s));
   cudaFreeAsync(tmp, s);
   CK(cudaGetLastError());

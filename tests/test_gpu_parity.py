@@ -116,6 +116,37 @@ def test_deterministic_and_graph_free_path_agree(cuda, precision):
     assert a["stats"]["iters"] == n["stats"]["iters"]
 
 
+_PDL_PROBE = r'''
+import sys, numpy as np
+sys.path.insert(0, sys.argv[1])
+from simcoflow_gb300 import synth, projection as P
+c = synth.c4(n=320, instance=3)
+for prec in ("fp64", "mixed"):
+    g = P.project_case(c, precision=prec, rtol=1e-10, maxit=300)
+    np.save(sys.argv[2] + "_" + prec + ".npy", g["Pp"])
+'''
+
+
+def test_programmatic_launch_does_not_change_results(cuda, tmp_path):
+    """Kernels overlap their predecessors' tails under programmatic dependent
+    launch; the results must be bit-identical to strictly serial launches."""
+    import os
+    import subprocess
+    import sys
+    from helpers import GOLDEN
+    root = str(GOLDEN.parent.parent)
+    for tag, env in (("on", {}), ("off", {"SCF_NO_PDL": "1"})):
+        e = dict(os.environ)
+        e.update(env)
+        r = subprocess.run([sys.executable, "-c", _PDL_PROBE, root, str(tmp_path / tag)], env=e,
+                           capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr[-2000:]
+    for prec in ("fp64", "mixed"):
+        a = np.load(tmp_path / f"on_{prec}.npy")
+        b = np.load(tmp_path / f"off_{prec}.npy")
+        assert np.array_equal(a, b), prec
+
+
 def test_device_pointers_match_host(cuda):
     import torch
     c = synth.c1(n=64)
@@ -224,3 +255,8 @@ def test_full_size_c2(cuda, oracle):
         assert rel_l2(g2["Pp"][1:-1, 1:-1], xi) <= TOL_P, prec
     gm = _gpu_project(c, rtol=1e-8, maxit=200, precision="mixed")
     assert gm["stats"]["status"] == 0 and gm["stats"]["relres_true"] <= 1.5e-8
+    # full size, many CTAs per kernel: repeated solves are bit-identical
+    gm2 = _gpu_project(c, rtol=1e-8, maxit=200, precision="mixed")
+    assert np.array_equal(gm["Pp"], gm2["Pp"]) and gm["stats"]["iters"] == gm2["stats"]["iters"]
+    g3 = _gpu_project(c, rtol=1e-8, maxit=200)
+    assert np.array_equal(g["Pp"], g3["Pp"])
