@@ -84,7 +84,7 @@ typedef struct scf_stats {
 typedef struct scf_proj scf_proj;
 
 /* Fill opts with defaults: FP64, host pointers, device 0, maxit 200,
- * rtol 1e-8, 2 pre / 2 post sweeps, omega 1.9, coarse_max 64. */
+ * rtol 1e-8, 2 pre / 2 post sweeps, omega 1.9, coarse_max 16. */
 void scf_opts_default(scf_opts *opts);
 
 /* Create a solver for an nx-by-ny pressure grid (Isize, Jsize).  Allocates
@@ -167,6 +167,8 @@ int scf_proj_vcycle(scf_proj *h, const double *b, double *x);
 #define SCF_K_RESID_RESTRICT 3 /* fine residual summed onto the first coarse level */
 #define SCF_K_PROLONG 4        /* fine x += omega * coarse x */
 #define SCF_K_ASSEMBLE 5       /* operator assembly from the Fortran arrays */
+#define SCF_K_VCYCLE 6         /* one whole V-cycle, captured as a CUDA graph */
+#define SCF_K_SETUP 7          /* assembly + multigrid hierarchy setup (device work only) */
 int scf_proj_time_kernel(scf_proj *h, int kernel, int reps, double *ms_per_launch);
 
 /* Allocation-free right-hand side.  Computes the right-hand side of the

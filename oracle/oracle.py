@@ -176,7 +176,7 @@ def symmetric_operator(case, matr):
     return f(cE), f(cN), f(dg)
 
 
-def mgpcg(case, matr, rhm, rtol=1e-13, maxit=500, npre=1, npost=1, omega=1.0, coarse_max=64,
+def mgpcg(case, matr, rhm, rtol=1e-13, maxit=500, npre=2, npost=2, omega=1.9, coarse_max=16,
           threads=0):
     """CPU FP64 MG-PCG on the symmetric operator.  Returns (Pp-interior x as
     (nx,ny) Fortran array, iterations, true relres, levels)."""
@@ -195,7 +195,7 @@ def mgpcg(case, matr, rhm, rtol=1e-13, maxit=500, npre=1, npost=1, omega=1.0, co
     return np.asfortranarray(x.reshape(ny, nx).T), it, rel.value, nlev.value
 
 
-def vcycle(case, matr, b_f, npre=1, npost=1, omega=1.0, coarse_max=64) -> np.ndarray:
+def vcycle(case, matr, b_f, npre=2, npost=2, omega=1.9, coarse_max=16) -> np.ndarray:
     nx, ny = case.nx, case.ny
     cE, cN, dg = symmetric_operator(case, matr)
     b = np.ascontiguousarray(b_f.T).ravel()

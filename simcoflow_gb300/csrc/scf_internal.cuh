@@ -111,8 +111,8 @@ inline dim3 grid_for(int nx, int ny, int cells_per_thread_x = 2) {
 
 // ---- kernel launchers (scf_kernels.cu) ----
 void launch_assemble(const FortranIn& in, LevelView L0, Scalars* sc, cudaStream_t s);
-void launch_excess(LevelView L, cudaStream_t s);
-void launch_coarsen(LevelView F, LevelView C, cudaStream_t s);
+void launch_excess(LevelView L, double* di, cudaStream_t s);
+void launch_coarsen(LevelView F, LevelView C, double* di, cudaStream_t s);
 void launch_coarse_setup(LevelView C, double* Ainv, int* cmap, int* nc, cudaStream_t s);
 void launch_rhs(const FortranIn& in, const double* ustar, const double* vstar, double vb,
                 LevelView L0, double* bvec, double* r, float* r32, double* x, Scalars* sc,

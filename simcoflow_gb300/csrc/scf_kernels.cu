@@ -162,52 +162,93 @@ __device__ __forceinline__ double pocoef(double Dp, double len, double dist, dou
   return dvd(mul(mul(dvd(mul(Dp, len), dist), bP), bM), B);
 }
 
+// PoCoef of one face for every lane of a converged warp.  Away from the
+// interface and the solids the inputs (Dp, face length, node distance,
+// density factor) are the same across a warp, which spans one grid row; the
+// two IEEE divisions are then done once and broadcast, so the FP64 pipe
+// (slow on GB300) is spared while every lane gets the bits it would have
+// computed itself.
+__device__ __forceinline__ double pocoef_warp(bool valid, double Dp, double len, double dist,
+                                              double bP, double bM, double B) {
+  const unsigned full = 0xffffffffu;
+  const unsigned vmask = __ballot_sync(full, valid);
+  if (vmask == 0u) return 0.0;
+  const int leader = __ffs(vmask) - 1;
+  const long long a = __double_as_longlong(Dp), b = __double_as_longlong(len);
+  const long long c = __double_as_longlong(dist), d = __double_as_longlong(B);
+  // every lane takes part in every shuffle (no short-circuit around them)
+  const long long a0 = __shfl_sync(full, a, leader), b0 = __shfl_sync(full, b, leader);
+  const long long c0 = __shfl_sync(full, c, leader), d0 = __shfl_sync(full, d, leader);
+  const bool same = !valid || (a == a0 && b == b0 && c == c0 && d == d0);
+  if (__all_sync(full, same)) {
+    double r = 0.0;
+    if ((int)(threadIdx.x & 31) == leader) r = pocoef(Dp, len, dist, bP, bM, B);
+    return __shfl_sync(full, r, leader);
+  }
+  return valid ? pocoef(Dp, len, dist, bP, bM, B) : 0.0;
+}
+
 __global__ void k_assemble(FortranIn in, LevelView L, Scalars* sc) {
   pdl_wait();
   const int nx = in.nx, ny = in.ny;
   const int ix = blockIdx.x * kBX + threadIdx.x;
-  if (ix >= nx) return;
+  const bool in_x = ix < nx;
+  // every lane of a warp walks the same rows (blockDim.x == 32), so the warp
+  // stays converged for the shuffles in pocoef_warp
   for (int iy = blockIdx.y * kBY + threadIdx.y; iy < ny; iy += gridDim.y * kBY) {
     const int i = ix + 1, j = iy + 1;
-    const size_t k1 = fo1(nx, i, j), k0 = fo0(nx, i, j);
+    const size_t k1 = in_x ? fo1(nx, i, j) : 0, k0 = in_x ? fo0(nx, i, j) : 0;
     const size_t kl = (size_t)iy * L.pitch + ix;
-    if (in.posnu_p[k0] == -1) {
+    const bool act = in_x && in.posnu_p[k0] != -1;
+    const double bP = in.betaP, bM = in.betaM;
+    const double phis = act ? in.phi[k1] : 0.0;
+    const int cs = act ? cell_class(in.vof[k1], phis, in.vofS[k1]) : 0;
+    const double dxP = act ? in.dx[k1] : 1.0, dyP = act ? in.dy[k1] : 1.0;
+    // per face: whether the reference sets it, and the inputs of PoCoef
+    bool ok[4] = {false, false, false, false};
+    double Dp[4] = {0, 0, 0, 0}, len[4] = {1, 1, 1, 1}, dist[4] = {1, 1, 1, 1}, Bf[4] = {1, 1, 1, 1};
+    if (act) {
+      double B;
+      if (j > 1) {
+        const size_t kn = fo1(nx, i, j - 1);
+        if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B)) {
+          ok[0] = true; Dp[0] = in.DpV[fo0(nx, i, j - 1)]; len[0] = dxP; dist[0] = in.dyV[kn]; Bf[0] = B;
+        }
+      } else if (boundary_beta(cs, bP, bM, &B)) {
+        ok[0] = true; Dp[0] = in.DpV[k0]; len[0] = dxP; dist[0] = in.dyV[k1]; Bf[0] = B;
+      }
+      if (i > 1) {
+        const size_t kn = fo1(nx, i - 1, j);
+        if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B)) {
+          ok[1] = true; Dp[1] = in.DpU[fo0(nx, i - 1, j)]; len[1] = dyP; dist[1] = in.dxU[kn]; Bf[1] = B;
+        }
+      } else if (boundary_beta(cs, bP, bM, &B)) {
+        ok[1] = true; Dp[1] = in.DpU[k0]; len[1] = dyP; dist[1] = in.dxU[k1]; Bf[1] = B;
+      }
+      if (i < nx) {
+        const size_t kn = fo1(nx, i + 1, j);
+        if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B)) {
+          ok[2] = true; Dp[2] = in.DpU[k0]; len[2] = dyP; dist[2] = in.dxU[k1]; Bf[2] = B;
+        }
+      } else if (boundary_beta(cs, bP, bM, &B)) {
+        ok[2] = true; Dp[2] = in.DpU[k0]; len[2] = dyP; dist[2] = in.dxU[k1]; Bf[2] = B;
+      }
+      if (j < ny) {
+        const size_t kn = fo1(nx, i, j + 1);
+        if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B)) {
+          ok[3] = true; Dp[3] = in.DpV[k0]; len[3] = dxP; dist[3] = in.dyV[k1]; Bf[3] = B;
+        }
+      } else if (boundary_beta(cs, bP, bM, &B)) {
+        ok[3] = true; Dp[3] = in.DpV[k0]; len[3] = dxP; dist[3] = in.dyV[k1]; Bf[3] = B;
+      }
+    }
+    double pc[4];  // S, W, E, N
+#pragma unroll
+    for (int f = 0; f < 4; ++f) pc[f] = pocoef_warp(ok[f], Dp[f], len[f], dist[f], bP, bM, Bf[f]);
+    if (!in_x) continue;
+    if (!act) {
       L.cE[kl] = 0.0; L.cN[kl] = 0.0; L.dg[kl] = -1.0;
       continue;
-    }
-    const double bP = in.betaP, bM = in.betaM;
-    const double phis = in.phi[k1];
-    const int cs = cell_class(in.vof[k1], phis, in.vofS[k1]);
-    const double dxP = in.dx[k1], dyP = in.dy[k1];
-    double pc[4] = {0.0, 0.0, 0.0, 0.0};  // S, W, E, N
-    double B;
-    if (j > 1) {
-      size_t kn = fo1(nx, i, j - 1);
-      if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B))
-        pc[0] = pocoef(in.DpV[fo0(nx, i, j - 1)], dxP, in.dyV[kn], bP, bM, B);
-    } else if (boundary_beta(cs, bP, bM, &B)) {
-      pc[0] = pocoef(in.DpV[k0], dxP, in.dyV[k1], bP, bM, B);
-    }
-    if (i > 1) {
-      size_t kn = fo1(nx, i - 1, j);
-      if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B))
-        pc[1] = pocoef(in.DpU[fo0(nx, i - 1, j)], dyP, in.dxU[kn], bP, bM, B);
-    } else if (boundary_beta(cs, bP, bM, &B)) {
-      pc[1] = pocoef(in.DpU[k0], dyP, in.dxU[k1], bP, bM, B);
-    }
-    if (i < nx) {
-      size_t kn = fo1(nx, i + 1, j);
-      if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B))
-        pc[2] = pocoef(in.DpU[k0], dyP, in.dxU[k1], bP, bM, B);
-    } else if (boundary_beta(cs, bP, bM, &B)) {
-      pc[2] = pocoef(in.DpU[k0], dyP, in.dxU[k1], bP, bM, B);
-    }
-    if (j < ny) {
-      size_t kn = fo1(nx, i, j + 1);
-      if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B))
-        pc[3] = pocoef(in.DpV[k0], dxP, in.dyV[k1], bP, bM, B);
-    } else if (boundary_beta(cs, bP, bM, &B)) {
-      pc[3] = pocoef(in.DpV[k0], dxP, in.dyV[k1], bP, bM, B);
     }
     const double aS = in.aS[k0], aW = in.aW[k0], aE = in.aE[k0], aN = in.aN[k0];
     const double tS = mul(pc[0], aS), tW = mul(pc[1], aW), tE = mul(pc[2], aE), tN = mul(pc[3], aN);
@@ -224,14 +265,16 @@ __global__ void k_assemble(FortranIn in, LevelView L, Scalars* sc) {
   }
 }
 
-// diagonal excess dg - (cE + cW + cN + cS), clamped at zero
-__global__ void k_excess(LevelView L) {
+// diagonal excess dg - (cE + cW + cN + cS), clamped at zero, and the
+// inverse diagonal (0 where the cell has no unknown)
+__global__ void k_excess(LevelView L, double* di) {
   pdl_wait();
   const int ix = blockIdx.x * kBX + threadIdx.x;
   if (ix >= L.nx) return;
   for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY) {
     const size_t k = (size_t)iy * L.pitch + ix;
     const double d = L.dg[k];
+    di[k] = d > 0.0 ? 1.0 / d : 0.0;
     if (d < 0.0) { L.ex[k] = 0.0; continue; }
     double s = add(add(add(L.cE[k], L.cE[k - 1]), L.cN[k]), L.cN[k - L.pitch]);
     double e = sub(d, s);
@@ -239,8 +282,9 @@ __global__ void k_excess(LevelView L) {
   }
 }
 
-// Galerkin coarse operator for piecewise-constant 2x2 aggregation
-__global__ void k_coarsen(LevelView F, LevelView C) {
+// Galerkin coarse operator for piecewise-constant 2x2 aggregation (and the
+// coarse inverse diagonal)
+__global__ void k_coarsen(LevelView F, LevelView C, double* di) {
   pdl_wait();
   const int I = blockIdx.x * kBX + threadIdx.x;
   if (I >= C.nx) return;
@@ -280,6 +324,7 @@ __global__ void k_coarsen(LevelView F, LevelView C) {
       if (!(d > 0.0)) d = -1.0;
     }
     C.dg[kc] = d;
+    di[kc] = d > 0.0 ? 1.0 / d : 0.0;
   }
 }
 
@@ -658,14 +703,14 @@ static const dim3 kBlock(kBX, kBY);
 void launch_assemble(const FortranIn& in, LevelView L0, Scalars* sc, cudaStream_t s) {
   launch_k(k_assemble, grid_for(in.nx, in.ny, 1), kBlock, 0, s, in, L0, sc);
 }
-void launch_excess(LevelView L, cudaStream_t s) {
-  launch_k(k_excess, grid_for(L.nx, L.ny, 1), kBlock, 0, s, L);
+void launch_excess(LevelView L, double* di, cudaStream_t s) {
+  launch_k(k_excess, grid_for(L.nx, L.ny, 1), kBlock, 0, s, L, di);
 }
-void launch_coarsen(LevelView F, LevelView C, cudaStream_t s) {
-  launch_k(k_coarsen, grid_for(C.nx, C.ny, 1), kBlock, 0, s, F, C);
+void launch_coarsen(LevelView F, LevelView C, double* di, cudaStream_t s) {
+  launch_k(k_coarsen, grid_for(C.nx, C.ny, 1), kBlock, 0, s, F, C, di);
 }
 void launch_coarse_setup(LevelView C, double* Ainv, int* cmap, int* nc, cudaStream_t s) {
-  launch_k(k_coarse_setup, 1, dim3(256), 0, s, C, Ainv, cmap, nc);
+  launch_k(k_coarse_setup, dim3(1), dim3(1024), 0, s, C, Ainv, cmap, nc);
 }
 void launch_rhs(const FortranIn& in, const double* ustar, const double* vstar, double vb,
                 LevelView L0, double* bvec, double* r, float* r32, double* x, Scalars* sc,

@@ -326,7 +326,15 @@ __global__ void k_max_coupling(LevelView F, unsigned* out_bits) {
       m = fmaxf(m, (float)fabs(F.cN[k]));
     }
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(out_bits, __float_as_uint(m));
+  __shared__ float wm[8];
+  const int t = threadIdx.y * 32 + threadIdx.x;
+  if ((t & 31) == 0) wm[t >> 5] = m;
+  __syncthreads();
+  if (t == 0) {
+    float b = wm[0];
+    for (int w = 1; w < 8; ++w) b = fmaxf(b, wm[w]);
+    atomicMax(out_bits, __float_as_uint(b));  // one atomic per block
+  }
 }
 
 // Mixed level from the FP64 level: BF16 couplings divided by a power-of-two

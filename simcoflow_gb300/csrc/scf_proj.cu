@@ -218,6 +218,20 @@ void enqueue_vcycle(scf_proj* h, Scalars* sc, bool do_rz, cudaStream_t s) {
   }
 }
 
+// assembly of the fine operator and setup of the whole hierarchy
+void enqueue_setup(scf_proj* h, Scalars* sc, cudaStream_t s) {
+  launch_assemble(h->fin, h->lev[0], sc, s);
+  launch_excess(h->lev[0], h->di64[0], s);
+  for (size_t l = 1; l < h->lev.size(); ++l)
+    launch_coarsen(h->lev[l - 1], h->lev[l], h->di64[l], s);
+  launch_coarse_setup(h->lev.back(), h->Ainv, h->cmap, h->ncoarse, s);
+  if (h->mixed)
+    for (size_t l = 0; l < h->lev.size(); ++l) {
+      launch_max_coupling(h->lev[l], h->maxbits + l, s);
+      launch_to_mixed(h->lev[l], h->mix[l], h->maxbits + l, h->cscale + l, s);
+    }
+}
+
 // one PCG iteration: z = M r, beta, p = z + beta p_old, q = A p, alpha,
 // x += alpha p, r -= alpha q (and the flexible cross term), convergence test
 void enqueue_iteration(scf_proj* h, const double* pold, double* pnew, unsigned long long cond,
@@ -442,7 +456,7 @@ void scf_opts_default(scf_opts* o) {
   o->npre = 2;
   o->npost = 2;
   o->omega = 1.9;
-  o->coarse_max = 64;
+  o->coarse_max = 16;
 }
 
 const char* scf_strerror(int code) {
@@ -671,16 +685,7 @@ int scf_proj_assemble(scf_proj* h, const double* DpU, const double* DpV, double 
   f.wb = wb; f.eb = eb; f.sb = sb; f.nb = nb;
   cudaStream_t s = h->stream;
   CK(cudaMemsetAsync(h->sc, 0, sizeof(Scalars), s));
-  launch_assemble(f, h->lev[0], h->sc, s);
-  launch_excess(h->lev[0], s);
-  for (size_t l = 1; l < h->lev.size(); ++l) launch_coarsen(h->lev[l - 1], h->lev[l], s);
-  launch_coarse_setup(h->lev.back(), h->Ainv, h->cmap, h->ncoarse, s);
-  for (size_t l = 0; l < h->lev.size(); ++l) launch_inv_diag(h->lev[l], h->di64[l], s);
-  if (h->mixed)
-    for (size_t l = 0; l < h->lev.size(); ++l) {
-      launch_max_coupling(h->lev[l], h->maxbits + l, s);
-      launch_to_mixed(h->lev[l], h->mix[l], h->maxbits + l, h->cscale + l, s);
-    }
+  enqueue_setup(h, h->sc, s);
   CK(cudaGetLastError());
   int nanflag = 0;
   CK(cudaMemcpyAsync(&nanflag, &h->sc->nan, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -727,7 +732,7 @@ int scf_proj_get_operator(scf_proj* h, double* cE, double* cN, double* diag, dou
 }
 
 int scf_proj_time_kernel(scf_proj* h, int kernel, int reps, double* ms) {
-  if (!h || !ms || reps < 1 || kernel < 0 || kernel > SCF_K_ASSEMBLE) return SCF_ERR_ARG;
+  if (!h || !ms || reps < 1 || kernel < 0 || kernel > SCF_K_SETUP) return SCF_ERR_ARG;
   if (!h->assembled) return SCF_ERR_STATE;
   CK(cudaSetDevice(h->device));
   cudaStream_t s = h->stream;
@@ -740,7 +745,27 @@ int scf_proj_time_kernel(scf_proj* h, int kernel, int reps, double* ms) {
   LevelView L0 = h->lev[0];
   const bool two = h->lev.size() > 1;
   const double om = h->opts.omega;
+  cudaGraphExec_t vexec = nullptr;
+  if (kernel == SCF_K_VCYCLE) {  // one V-cycle as a graph, replayed
+    cudaStream_t cs = nullptr;
+    CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed));
+    enqueue_vcycle(h, h->sc_diag, false, cs);
+    CK(cudaStreamEndCapture(cs, &g));
+    CK(cudaGraphInstantiate(&vexec, g, 0));
+    cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+  }
   auto launch = [&]() {
+    if (kernel == SCF_K_VCYCLE) {
+      cudaGraphLaunch(vexec, s);
+      return;
+    }
+    if (kernel == SCF_K_SETUP) {
+      enqueue_setup(h, h->sc_diag, s);
+      return;
+    }
     if (kernel == SCF_K_PUPDATE_SPMV) {
       if (h->mixed)
         launch_pupdate_spmv_t<float>(L0, buf32(h, 0, 0), h->pA, h->pB, h->q, h->sc_diag, h->part, s);
@@ -782,6 +807,7 @@ int scf_proj_time_kernel(scf_proj* h, int kernel, int reps, double* ms) {
   CK(cudaEventRecord(h->ev[6], s));
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(s));
+  if (vexec) cudaGraphExecDestroy(vexec);
   *ms = (double)elapsed(h->ev[5], h->ev[6]) / reps;
   return SCF_OK;
 }
