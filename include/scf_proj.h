@@ -57,6 +57,16 @@ extern "C" {
 #define SCF_FLAG_DEVICE_PTRS 1 /* array arguments are device pointers */
 #define SCF_FLAG_NO_GRAPH 2    /* launch kernels one by one, no CUDA graph */
 
+/* Multigrid smoother.  POINT: red-black Gauss-Seidel.  LINE: alternating
+ * zebra line Gauss-Seidel (exact tridiagonal solves along x, then along y),
+ * robust on stretched grids; lines of at most 16384 cells.  AUTO: LINE when
+ * some cell's aspect ratio max(dx/dy, dy/dx) exceeds 2, else POINT.
+ * BoomerAMG, which this replaces (src/ProjectionP_Mod.f90:116-133), adapts
+ * to anisotropy through its strength-of-connection coarsening. */
+#define SCF_SMOOTH_AUTO 0
+#define SCF_SMOOTH_POINT 1
+#define SCF_SMOOTH_LINE 2
+
 typedef struct scf_opts {
     int precision;   /* SCF_PREC_FP64 or SCF_PREC_MIXED */
     int flags;       /* SCF_FLAG_* */
@@ -66,7 +76,8 @@ typedef struct scf_opts {
     int npre, npost; /* red-black Gauss-Seidel sweeps before / after coarse correction */
     double omega;    /* scale of the coarse-grid correction */
     int coarse_max;  /* coarsest level has at most this many cells (<= 64) */
-    int reserved[8];
+    int smoother;    /* SCF_SMOOTH_AUTO (default), SCF_SMOOTH_POINT or SCF_SMOOTH_LINE */
+    int reserved[7];
 } scf_opts;
 
 typedef struct scf_stats {
@@ -79,6 +90,7 @@ typedef struct scf_stats {
     double relres_true; /* FP64 recomputed ||b - A x||_2/||b||_2 */
     double mres_max;    /* max |mres| over cells with Posnu /= -1 (update_puv) */
     double ms_h2d, ms_assemble, ms_solve, ms_correct, ms_d2h, ms_total;
+    int smoother;       /* SCF_SMOOTH_POINT or SCF_SMOOTH_LINE: the smoother used */
 } scf_stats;
 
 typedef struct scf_proj scf_proj;

@@ -62,9 +62,10 @@ def lib():
         L.oracle_row_residual.argtypes = [C.c_int, C.c_int, _P, _P, _P, _I]
         L.oracle_mgpcg.restype = C.c_int
         L.oracle_mgpcg.argtypes = [C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_double, C.c_int,
-                                   C.c_int, C.c_int, C.c_double, C.c_int, _P, C.POINTER(C.c_int)]
+                                   C.c_int, C.c_int, C.c_double, C.c_int, _P, C.POINTER(C.c_int),
+                                   C.c_int]
         L.oracle_vcycle.argtypes = [C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_int, C.c_int,
-                                    C.c_double, C.c_int]
+                                    C.c_double, C.c_int, C.c_int]
         L.oracle_num_threads.restype = C.c_int
         L.oracle_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -176,10 +177,14 @@ def symmetric_operator(case, matr):
     return f(cE), f(cN), f(dg)
 
 
+SMOOTHERS = {"point": 0, "line": 1}
+
+
 def mgpcg(case, matr, rhm, rtol=1e-13, maxit=500, npre=2, npost=2, omega=1.9, coarse_max=16,
-          threads=0):
+          threads=0, smoother="point"):
     """CPU FP64 MG-PCG on the symmetric operator.  Returns (Pp-interior x as
-    (nx,ny) Fortran array, iterations, true relres, levels)."""
+    (nx,ny) Fortran array, iterations, true relres, levels).  smoother:
+    'point' (red-black Gauss-Seidel) or 'line' (alternating zebra lines)."""
     nx, ny = case.nx, case.ny
     cE, cN, dg = symmetric_operator(case, matr)
     b = np.ascontiguousarray(rhm.T).ravel()
@@ -191,18 +196,19 @@ def mgpcg(case, matr, rhm, rtol=1e-13, maxit=500, npre=2, npost=2, omega=1.9, co
     it = lib().oracle_mgpcg(nx, ny, cE.ctypes.data_as(_P), cN.ctypes.data_as(_P),
                             dg.ctypes.data_as(_P), b.ctypes.data_as(_P), x.ctypes.data_as(_P),
                             rtol, maxit, npre, npost, omega, coarse_max, C.byref(rel),
-                            C.byref(nlev))
+                            C.byref(nlev), SMOOTHERS[smoother])
     return np.asfortranarray(x.reshape(ny, nx).T), it, rel.value, nlev.value
 
 
-def vcycle(case, matr, b_f, npre=2, npost=2, omega=1.9, coarse_max=16) -> np.ndarray:
+def vcycle(case, matr, b_f, npre=2, npost=2, omega=1.9, coarse_max=16,
+           smoother="point") -> np.ndarray:
     nx, ny = case.nx, case.ny
     cE, cN, dg = symmetric_operator(case, matr)
     b = np.ascontiguousarray(b_f.T).ravel()
     x = np.zeros(nx * ny)
     lib().oracle_vcycle(nx, ny, cE.ctypes.data_as(_P), cN.ctypes.data_as(_P),
                         dg.ctypes.data_as(_P), b.ctypes.data_as(_P), x.ctypes.data_as(_P), npre,
-                        npost, omega, coarse_max)
+                        npost, omega, coarse_max, SMOOTHERS[smoother])
     return np.asfortranarray(x.reshape(ny, nx).T)
 
 

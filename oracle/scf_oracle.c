@@ -452,7 +452,9 @@ double oracle_row_residual(int nx, int ny, const double *matr, const double *Pp,
  * summed diagonal excess (dg - sum of couplings, clamped at 0).
  * V-cycle: x=0; pre-smooth red then black; residual; restrict (sum);
  * recurse; x += omega * P e (not into cells without an unknown); post-smooth
- * black then red.  Coarsest level: dense Cholesky.
+ * black then red.  Coarsest level: dense Cholesky.  With the line smoother a
+ * pre-smoothing step is: even rows, odd rows, even columns, odd columns,
+ * each line solved exactly; post-smoothing runs the reverse order.
  * Arrays are 0-based, x fastest: a[ix + iy*nx].
  * ------------------------------------------------------------------------ */
 typedef struct {
@@ -466,6 +468,7 @@ typedef struct {
     olevel lev[32];
     double omega;
     int npre, npost;
+    int line;        /* 1: alternating zebra line smoother */
     int nc;          /* coarsest unknowns */
     double *chol;    /* nc x nc lower Cholesky factor */
     int *cmap;       /* coarsest cell -> dense index or -1 */
@@ -607,6 +610,63 @@ static void rbgs_half(olevel *L, int color) {
     }
 }
 
+/* Exact solves of the lines of one parity: dir 0 rows (iy % 2 == color),
+ * dir 1 columns (ix % 2 == color).  Each line is the tridiagonal system of
+ * its in-line couplings, with the couplings to the neighbouring lines of the
+ * other parity on the right-hand side; Thomas algorithm.  Cells without an
+ * unknown get x = 0. */
+static void line_half(olevel *L, int dir, int color) {
+    int nx = L->nx, ny = L->ny;
+    const double *cE = L->cE, *cN = L->cN, *dg = L->dg, *b = L->b;
+    double *x = L->x;
+    int nlines = dir == 0 ? ny : nx, len = dir == 0 ? nx : ny;
+#pragma omp parallel
+    {
+        double *cp = dalloc((size_t)len), *dp = dalloc((size_t)len);
+#pragma omp for schedule(static)
+        for (int q = color; q < nlines; q += 2) {
+            /* cell k of line q: index and its in-line / cross couplings */
+            for (int k = 0; k < len; ++k) {
+                int ix = dir == 0 ? k : q, iy = dir == 0 ? q : k;
+                size_t c = (size_t)iy * nx + ix;
+                double a = 0.0, up = 0.0, d = 1.0, r = 0.0;
+                if (dg[c] > 0.0) {
+                    d = dg[c];
+                    r = b[c];
+                    if (dir == 0) {
+                        a = ix > 0 ? -cE[c - 1] : 0.0;
+                        up = ix + 1 < nx ? -cE[c] : 0.0;
+                        if (iy + 1 < ny) r = r + cN[c] * x[c + nx];
+                        if (iy > 0) r = r + cN[c - nx] * x[c - nx];
+                    } else {
+                        a = iy > 0 ? -cN[c - nx] : 0.0;
+                        up = iy + 1 < ny ? -cN[c] : 0.0;
+                        if (ix + 1 < nx) r = r + cE[c] * x[c + 1];
+                        if (ix > 0) r = r + cE[c - 1] * x[c - 1];
+                    }
+                }
+                double den = k > 0 ? d - a * cp[k - 1] : d;
+                cp[k] = up / den;
+                dp[k] = (k > 0 ? r - a * dp[k - 1] : r) / den;
+            }
+            double xn = 0.0;
+            for (int k = len - 1; k >= 0; --k) {
+                int ix = dir == 0 ? k : q, iy = dir == 0 ? q : k;
+                size_t c = (size_t)iy * nx + ix;
+                xn = dp[k] - (k + 1 < len ? cp[k] * xn : 0.0);
+                x[c] = dg[c] > 0.0 ? xn : 0.0;
+            }
+        }
+        free(cp); free(dp);
+    }
+}
+
+/* one smoothing step of the line smoother; post: the reverse order */
+static void line_step(olevel *L, int post) {
+    if (!post) { line_half(L, 0, 0); line_half(L, 0, 1); line_half(L, 1, 0); line_half(L, 1, 1); }
+    else { line_half(L, 1, 1); line_half(L, 1, 0); line_half(L, 0, 1); line_half(L, 0, 0); }
+}
+
 static void residual(olevel *L) {
     int nx = L->nx, ny = L->ny;
 #pragma omp parallel for schedule(static)
@@ -654,12 +714,21 @@ static void vcycle(omg *M, int l) {
     size_t n = (size_t)L->nx * L->ny;
     if (l == M->nlev - 1) { coarse_solve(M); return; }
     memset(L->x, 0, n * sizeof(double));
-    for (int s = 0; s < M->npre; ++s) { rbgs_half(L, 0); rbgs_half(L, 1); }
+    if (M->line) {
+        /* a line step (x-lines and y-lines) counts as two sweeps */
+        for (int s = 0; s < (M->npre + 1) / 2; ++s) line_step(L, 0);
+    } else {
+        for (int s = 0; s < M->npre; ++s) { rbgs_half(L, 0); rbgs_half(L, 1); }
+    }
     residual(L);
     restrict_sum(L, &M->lev[l + 1]);
     vcycle(M, l + 1);
     prolong_add(L, &M->lev[l + 1], M->omega);
-    for (int s = 0; s < M->npost; ++s) { rbgs_half(L, 1); rbgs_half(L, 0); }
+    if (M->line) {
+        for (int s = 0; s < (M->npost + 1) / 2; ++s) line_step(L, 1);
+    } else {
+        for (int s = 0; s < M->npost; ++s) { rbgs_half(L, 1); rbgs_half(L, 0); }
+    }
 }
 
 static double dot(const double *a, const double *b, size_t n) {
@@ -694,10 +763,10 @@ static void apply_A(const olevel *L, const double *p, double *q) {
  */
 int oracle_mgpcg(int nx, int ny, const double *cE, const double *cN, const double *dg,
                  const double *b, double *x, double rtol, int maxit, int npre, int npost,
-                 double omega, int coarse_max, double *relres, int *nlev_out) {
+                 double omega, int coarse_max, double *relres, int *nlev_out, int smoother) {
     omg M;
     memset(&M, 0, sizeof(M));
-    M.omega = omega; M.npre = npre; M.npost = npost;
+    M.omega = omega; M.npre = npre; M.npost = npost; M.line = smoother == 1;
     int ncyc = 1;
     if (maxit < 0) { ncyc = (-maxit) / 1000; maxit = (-maxit) % 1000; if (ncyc < 1) ncyc = 1; }
     size_t n = (size_t)nx * ny;
@@ -763,10 +832,10 @@ done:
 /* one V-cycle on b (0-based), output x; exposed for bitwise tests */
 void oracle_vcycle(int nx, int ny, const double *cE, const double *cN, const double *dg,
                    const double *b, double *x, int npre, int npost, double omega,
-                   int coarse_max) {
+                   int coarse_max, int smoother) {
     omg M;
     memset(&M, 0, sizeof(M));
-    M.omega = omega; M.npre = npre; M.npost = npost;
+    M.omega = omega; M.npre = npre; M.npost = npost; M.line = smoother == 1;
     size_t n = (size_t)nx * ny;
     level_alloc(&M.lev[0], nx, ny);
     memcpy(M.lev[0].cE, cE, n * sizeof(double));

@@ -18,6 +18,7 @@
 //   RZ        r.z (and r.z_old for the flexible PCG) reduced over the grid,
 //             then the PCG beta
 #include <cstdlib>
+#include <type_traits>
 
 #include "scf_mg.cuh"
 
@@ -375,13 +376,17 @@ __global__ void k_to_mixed(LevelView F, MgView<float, __nv_bfloat16, float> M,
 // The coarse end of the V-cycle in one CTA: every level of at most
 // kTailMaxCells cells, down to the dense coarsest solve and back up, with x
 // and b of all those levels in shared memory (each level padded by a zero
-// ghost ring) and the operators read through L1.  Replaces four kernel
+// ghost ring); FP32 tails stage the operators there too, FP64 tails read
+// them through L1.  Replaces four kernel
 // launches per level, which on such small grids cost launch latency only.
 // The arithmetic is that of k_sweep / k_coarse_solve_t, cell for cell.
 template <class T, class CT>
 __global__ void __launch_bounds__(1024) k_tail(TailDesc<T, CT> d, Scalars* sc) {
   pdl_wait();
   if (sc->done) return;
+  // FP32 tails also stage the operators (couplings scaled to FP32, inverse
+  // diagonal, diagonal) so that no phase after the first touches global memory
+  constexpr bool STAGE = std::is_same<T, float>::value;
   extern __shared__ __align__(16) unsigned char tail_smem[];
   T* sm = reinterpret_cast<T*>(tail_smem);
   double* bd = reinterpret_cast<double*>(tail_smem + d.bd_off);
@@ -389,8 +394,13 @@ __global__ void __launch_bounds__(1024) k_tail(TailDesc<T, CT> d, Scalars* sc) {
   for (int i = t; i < d.total; i += NTT) sm[i] = T(0);
   __syncthreads();
   auto W = [&](int l) { return d.lv[l].nx + 2; };
+  auto WH = [&](int l) { return (d.lv[l].nx + 2) * (d.lv[l].ny + 2); };
   auto xs = [&](int l) { return sm + d.off[l]; };
-  auto bs = [&](int l) { return sm + d.off[l] + W(l) * (d.lv[l].ny + 2); };
+  auto bs = [&](int l) { return sm + d.off[l] + WH(l); };
+  auto dis = [&](int l) { return sm + d.off[l] + 2 * WH(l); };
+  auto dgs = [&](int l) { return sm + d.off[l] + 3 * WH(l); };
+  auto ces = [&](int l) { return sm + d.off[l] + 4 * WH(l); };
+  auto cns = [&](int l) { return sm + d.off[l] + 5 * WH(l); };
   {  // right-hand side of the first tail level (restricted by the previous kernel)
     const MgView<T, CT, T>& L = d.lv[0];
     T* b = bs(0);
@@ -399,10 +409,34 @@ __global__ void __launch_bounds__(1024) k_tail(TailDesc<T, CT> d, Scalars* sc) {
       b[(iy + 1) * W(0) + ix + 1] = L.b[(size_t)iy * L.pitch + ix];
     }
   }
+  if (STAGE) {
+    for (int l = 0; l < d.n; ++l) {
+      const MgView<T, CT, T>& L = d.lv[l];
+      const float cs = L.csp ? __ldg(L.csp) : 1.0f;
+      for (int k = t; k < L.nx * L.ny; k += NTT) {
+        const int ix = k % L.nx, iy = k / L.nx;
+        const size_t g = (size_t)iy * L.pitch + ix;
+        const int si = (iy + 1) * W(l) + ix + 1;
+        dis(l)[si] = L.di[g];
+        dgs(l)[si] = L.dg[g];
+        ces(l)[si] = cload<CT, T>(L.cE, g, cs);
+        cns(l)[si] = cload<CT, T>(L.cN, g, cs);
+      }
+    }
+  }
   __syncthreads();
+  // operator access: staged copies or the global arrays
+  auto opE = [&](int l, int si, size_t g, float cs) {
+    return STAGE ? ces(l)[si] : cload<CT, T>(d.lv[l].cE, g, cs);
+  };
+  auto opN = [&](int l, int si, size_t g, float cs) {
+    return STAGE ? cns(l)[si] : cload<CT, T>(d.lv[l].cN, g, cs);
+  };
+  auto opDi = [&](int l, int si, size_t g) { return STAGE ? dis(l)[si] : d.lv[l].di[g]; };
+  auto opDg = [&](int l, int si, size_t g) { return STAGE ? dgs(l)[si] : d.lv[l].dg[g]; };
   auto relax = [&](int l, int colour) {
     const MgView<T, CT, T>& L = d.lv[l];
-    const float cs = L.csp ? __ldg(L.csp) : 1.0f;
+    const float cs = (!STAGE && L.csp) ? __ldg(L.csp) : 1.0f;
     T* x = xs(l);
     const T* b = bs(l);
     const int w = W(l), P = L.pitch;
@@ -412,11 +446,11 @@ __global__ void __launch_bounds__(1024) k_tail(TailDesc<T, CT> d, Scalars* sc) {
       const size_t g = (size_t)iy * P + ix;
       const int si = (iy + 1) * w + ix + 1;
       T s = b[si];
-      s = fma(cload<CT, T>(L.cE, g, cs), x[si + 1], s);
-      s = fma(cload<CT, T>(L.cE, g - 1, cs), x[si - 1], s);
-      s = fma(cload<CT, T>(L.cN, g, cs), x[si + w], s);
-      s = fma(cload<CT, T>(L.cN, g - P, cs), x[si - w], s);
-      x[si] = s * L.di[g];
+      s = fma(opE(l, si, g, cs), x[si + 1], s);
+      s = fma(opE(l, si - 1, g - 1, cs), x[si - 1], s);
+      s = fma(opN(l, si, g, cs), x[si + w], s);
+      s = fma(opN(l, si - w, g - P, cs), x[si - w], s);
+      x[si] = s * opDi(l, si, g);
     }
     __syncthreads();
   };
@@ -426,7 +460,7 @@ __global__ void __launch_bounds__(1024) k_tail(TailDesc<T, CT> d, Scalars* sc) {
     // residual summed 2x2 onto level l+1
     const MgView<T, CT, T>& L = d.lv[l];
     const MgView<T, CT, T>& C = d.lv[l + 1];
-    const float cs = L.csp ? __ldg(L.csp) : 1.0f;
+    const float cs = (!STAGE && L.csp) ? __ldg(L.csp) : 1.0f;
     const T* x = xs(l);
     const T* b = bs(l);
     T* bc = bs(l + 1);
@@ -439,14 +473,14 @@ __global__ void __launch_bounds__(1024) k_tail(TailDesc<T, CT> d, Scalars* sc) {
           const int gx = 2 * I + dq, gy = 2 * J + dj;
           if (gx >= L.nx || gy >= L.ny) continue;
           const size_t g = (size_t)gy * P + gx;
-          const T dgv = L.dg[g];
-          if (dgv < T(0)) continue;
           const int si = (gy + 1) * w + gx + 1;
+          const T dgv = opDg(l, si, g);
+          if (dgv < T(0)) continue;
           T r = fma(-dgv, x[si], b[si]);
-          r = fma(cload<CT, T>(L.cE, g, cs), x[si + 1], r);
-          r = fma(cload<CT, T>(L.cE, g - 1, cs), x[si - 1], r);
-          r = fma(cload<CT, T>(L.cN, g, cs), x[si + w], r);
-          r = fma(cload<CT, T>(L.cN, g - P, cs), x[si - w], r);
+          r = fma(opE(l, si, g, cs), x[si + 1], r);
+          r = fma(opE(l, si - 1, g - 1, cs), x[si - 1], r);
+          r = fma(opN(l, si, g, cs), x[si + w], r);
+          r = fma(opN(l, si - w, g - P, cs), x[si - w], r);
           s += r;
         }
       bc[(J + 1) * wc + I + 1] = s;
@@ -479,10 +513,9 @@ __global__ void __launch_bounds__(1024) k_tail(TailDesc<T, CT> d, Scalars* sc) {
     const int w = W(l), wc = W(l + 1);
     for (int k = t; k < L.nx * L.ny; k += NTT) {
       const int ix = k % L.nx, iy = k / L.nx;
-      if (L.di[(size_t)iy * L.pitch + ix] > T(0)) {
-        const int si = (iy + 1) * w + ix + 1;
+      const int si = (iy + 1) * w + ix + 1;
+      if (opDi(l, si, (size_t)iy * L.pitch + ix) > T(0))
         x[si] = fma(d.omega, xc[((iy >> 1) + 1) * wc + (ix >> 1) + 1], x[si]);
-      }
     }
     __syncthreads();
     for (int it = 0; it < d.npost; ++it) { relax(l, 1); relax(l, 0); }
@@ -501,10 +534,12 @@ __global__ void __launch_bounds__(1024) k_tail(TailDesc<T, CT> d, Scalars* sc) {
 
 template <class T, class CT>
 int tail_prepare(TailDesc<T, CT>& d) {
+  // x and b per level; FP32 tails also stage di, dg, cE, cN
+  const int arrays = std::is_same<T, float>::value ? 6 : 2;
   int off = 0;
   for (int l = 0; l < d.n; ++l) {
     d.off[l] = off;
-    off += 2 * (d.lv[l].nx + 2) * (d.lv[l].ny + 2);
+    off += arrays * (d.lv[l].nx + 2) * (d.lv[l].ny + 2);
   }
   d.total = off;
   size_t bytes = (size_t)off * sizeof(T);
@@ -512,9 +547,16 @@ int tail_prepare(TailDesc<T, CT>& d) {
   d.bd_off = (int)bytes;
   bytes += kMaxCoarse * sizeof(double);
   d.smem = (int)bytes;
-  if (cudaFuncSetAttribute(k_tail<T, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           d.smem) != cudaSuccess)
+  int dev = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+      bytes > (size_t)optin)
     return -1;
+  if (cudaFuncSetAttribute(k_tail<T, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           d.smem) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return -1;
+  }
   return 0;
 }
 

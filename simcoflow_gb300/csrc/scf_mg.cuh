@@ -36,7 +36,7 @@ template <class T, class CT>
 struct TailDesc {
   int n;  // number of tail levels
   MgView<T, CT, T> lv[kTailMaxLevels];
-  int off[kTailMaxLevels];  // shared-memory offset of each level's x (b follows)
+  int off[kTailMaxLevels];  // shared-memory offset of each level's x (b, then di, dg, cE, cN in FP32)
   int total;                // elements of T in shared memory
   int bd_off, smem;         // byte offset of the coarse gather buffer, total bytes
   int npre, npost;
@@ -66,6 +66,25 @@ void launch_dot_rz_t(int nx, int ny, int pitch, const BT* r, const T* z, int fle
 template <class ZT>
 void launch_pupdate_spmv_t(LevelView L0, const ZT* z, const double* pold, double* pnew,
                            double* q, Scalars* sc, double* part, cudaStream_t s);
+
+// Line relaxation (scf_line.cu).  Lines longer than kLineMaxLen cells are
+// not supported by the line smoother.
+constexpr int kLineMaxLen = 16384;
+int line_threads(int len, int* chunk);  // CTA size for a line; 0 if too long
+template <class T, class CT>
+void launch_line(const MgView<T, CT, T>& L, int colour, bool zero, const Scalars* sc,
+                 cudaStream_t s);
+template <class E>
+void launch_transpose(const E* src, int nx, int ny, int ps, E* dst, int pd, const Scalars* sc,
+                      cudaStream_t s);
+template <class T, class CT>
+void launch_resid_restrict_l(const MgView<T, CT, T>& L, const MgView<T, CT, T>& C,
+                             const Scalars* sc, cudaStream_t s);
+template <class T, class CT>
+void launch_prolong_l(const MgView<T, CT, T>& L, const T* xc, int pc, double omega,
+                      const Scalars* sc, cudaStream_t s);
+void launch_aspect(const double* dx, const double* dy, size_t n, unsigned* out_bits,
+                   cudaStream_t s);
 
 void launch_inv_diag(const LevelView& L, double* di, cudaStream_t s);
 void launch_max_coupling(const LevelView& L, unsigned* out_bits, cudaStream_t s);

@@ -46,6 +46,13 @@ struct scf_proj {
   int tail0 = 0;
   TailDesc<double, double> tail64{};
   TailDesc<float, bf16> tail32{};
+  // line smoother: transposed copy of each level (cE and cN swapped), used
+  // for the lines along y; allocated when the line smoother is selected
+  bool line = false;
+  bool line_alloc = false;
+  std::vector<MgD> t64;
+  std::vector<MgF> t32;
+  unsigned* aspect_bits = nullptr;  // device: largest cell aspect ratio (float bits)
   float* cscale = nullptr;      // device, one BF16 scale per level
   unsigned* maxbits = nullptr;  // device, one per level
   std::vector<void*> allocs;
@@ -143,6 +150,7 @@ float* buf32(scf_proj* h, int l, int i) { return i == 0 ? h->mix[l].x : h->x2_32
 // alternate buffers (npre down, npost up, starting from buffer 0), the tail
 // and the coarse solve write buffer 0.
 int final_buf(scf_proj* h, int l) {
+  if (h->line) return 0;  // line passes update in place
   const int L = (int)h->lev.size();
   const int lk = h->tail0 > 0 ? h->tail0 : L - 1;
   if (L == 1 || l >= lk) return 0;
@@ -201,12 +209,77 @@ void enqueue_vcycle_t(scf_proj* h, ViewFn view, BufFn buf, const TailDesc<T, CT>
   }
 }
 
+// V-cycle with the alternating zebra line smoother.  A smoothing step is
+// x-lines (even rows, odd rows), then y-lines (even columns, odd columns) on
+// the transposed level; the post-smoothing steps run the same passes in
+// reverse order, so the V-cycle stays symmetric.  A step counts as two
+// sweeps of npre / npost.  x and b move to the transposed layout by tiled
+// transposes (b once per level and V-cycle).  Every pass updates x in place.
+template <class T, class CT, class ViewFn, class TViewFn>
+void enqueue_vcycle_line_t(scf_proj* h, ViewFn view, TViewFn tview, Scalars* sc, bool do_rz,
+                           int flexible, cudaStream_t s) {
+  using V = MgView<T, CT, T>;
+  const int L = (int)h->lev.size();
+  const int npre = (h->opts.npre + 1) / 2, npost = (h->opts.npost + 1) / 2;
+  const double om = h->opts.omega;
+  auto to_t = [&](const V& f, const V& ft) {
+    launch_transpose<T>(f.x, f.nx, f.ny, f.pitch, ft.x, ft.pitch, sc, s);
+  };
+  auto from_t = [&](const V& f, const V& ft) {
+    launch_transpose<T>(ft.x, ft.nx, ft.ny, ft.pitch, f.x, f.pitch, sc, s);
+  };
+  auto step = [&](int l, bool post, bool zero) {
+    const V f = view(l), ft = tview(l);
+    if (!post) {
+      launch_line(f, 0, zero, sc, s);
+      launch_line(f, 1, false, sc, s);
+      to_t(f, ft);
+      launch_line(ft, 0, false, sc, s);
+      launch_line(ft, 1, false, sc, s);
+      from_t(f, ft);
+    } else {
+      to_t(f, ft);
+      launch_line(ft, 1, false, sc, s);
+      launch_line(ft, 0, false, sc, s);
+      from_t(f, ft);
+      launch_line(f, 1, false, sc, s);
+      launch_line(f, 0, false, sc, s);
+    }
+  };
+  if (L > 1) {
+    for (int l = 0; l < L - 1; ++l) {
+      const V f = view(l), ft = tview(l);
+      launch_transpose<T>(f.b, f.nx, f.ny, f.pitch, ft.b, ft.pitch, sc, s);
+      for (int it = 0; it < npre; ++it) step(l, false, it == 0);
+      launch_resid_restrict_l(f, view(l + 1), sc, s);
+    }
+  }
+  {
+    V c = view(L - 1);
+    launch_coarse_solve_t(c, h->Ainv, h->cmap, h->ncoarse, sc, s);
+  }
+  for (int l = L - 2; l >= 0; --l) {
+    const V f = view(l), c = view(l + 1);
+    launch_prolong_l(f, c.x, c.pitch, om, sc, s);
+    for (int it = 0; it < npost; ++it) step(l, true, false);
+  }
+  if (do_rz) {
+    const V f = view(0);
+    launch_dot_rz_t<T, T>(f.nx, f.ny, f.pitch, f.b, f.x, flexible, sc, h->part, s);
+  }
+}
+
 // V-cycle of the handle's precision on level 0: b = r (or its FP32 copy), x = z
 void enqueue_vcycle(scf_proj* h, Scalars* sc, bool do_rz, cudaStream_t s) {
   if (!h->mixed) {
     auto view = [h](int l) { return view64(h, l); };
     auto buf = [h](int l, int i) { return buf64(h, l, i); };
-    enqueue_vcycle_t(h, view, buf, h->tail64, sc, do_rz, 0, s);
+    if (h->line) {
+      auto tview = [h](int l) { return h->t64[l]; };
+      enqueue_vcycle_line_t<double, double>(h, view, tview, sc, do_rz, 0, s);
+    } else {
+      enqueue_vcycle_t(h, view, buf, h->tail64, sc, do_rz, 0, s);
+    }
   } else {
     auto view = [h](int l) {
       MgF v = h->mix[l];
@@ -214,7 +287,26 @@ void enqueue_vcycle(scf_proj* h, Scalars* sc, bool do_rz, cudaStream_t s) {
       return v;
     };
     auto buf = [h](int l, int i) { return buf32(h, l, i); };
-    enqueue_vcycle_t(h, view, buf, h->tail32, sc, do_rz, 1, s);
+    if (h->line) {
+      auto tview = [h](int l) { return h->t32[l]; };
+      enqueue_vcycle_line_t<float, bf16>(h, view, tview, sc, do_rz, 1, s);
+    } else {
+      enqueue_vcycle_t(h, view, buf, h->tail32, sc, do_rz, 1, s);
+    }
+  }
+}
+
+// transposed operator of every level for the line smoother
+template <class T, class CT>
+void enqueue_line_setup_t(const std::vector<MgView<T, CT, T>>& nat,
+                          const std::vector<MgView<T, CT, T>>& tr, cudaStream_t s) {
+  for (size_t l = 0; l < nat.size(); ++l) {
+    const MgView<T, CT, T>& f = nat[l];
+    const MgView<T, CT, T>& t = tr[l];
+    launch_transpose<CT>(f.cN, f.nx, f.ny, f.pitch, const_cast<CT*>(t.cE), t.pitch, nullptr, s);
+    launch_transpose<CT>(f.cE, f.nx, f.ny, f.pitch, const_cast<CT*>(t.cN), t.pitch, nullptr, s);
+    launch_transpose<T>(f.dg, f.nx, f.ny, f.pitch, const_cast<T*>(t.dg), t.pitch, nullptr, s);
+    launch_transpose<T>(f.di, f.nx, f.ny, f.pitch, const_cast<T*>(t.di), t.pitch, nullptr, s);
   }
 }
 
@@ -230,6 +322,51 @@ void enqueue_setup(scf_proj* h, Scalars* sc, cudaStream_t s) {
       launch_max_coupling(h->lev[l], h->maxbits + l, s);
       launch_to_mixed(h->lev[l], h->mix[l], h->maxbits + l, h->cscale + l, s);
     }
+  if (h->line) {
+    if (h->mixed) {
+      enqueue_line_setup_t(h->mix, h->t32, s);
+    } else {
+      std::vector<MgD> nat;
+      for (size_t l = 0; l < h->lev.size(); ++l) nat.push_back(view64(h, l));
+      enqueue_line_setup_t(nat, h->t64, s);
+    }
+  }
+}
+
+// transposed levels of the line smoother (allocated once, on first use)
+int alloc_line(scf_proj* h) {
+  if (h->line_alloc) return SCF_OK;
+  int rc;
+  for (size_t l = 0; l < h->lev.size(); ++l) {
+    const int nx = h->lev[l].nx, ny = h->lev[l].ny;
+    const int pt = (ny + 2 + 31) / 32 * 32;  // transposed: ny columns, nx rows
+    if (!h->mixed) {
+      MgD v{};
+      v.nx = ny; v.ny = nx; v.pitch = pt;
+      double *ce, *cn, *dg, *di, *x, *b;
+      if ((rc = level_array(h, nx, pt, &ce)) || (rc = level_array(h, nx, pt, &cn)) ||
+          (rc = level_array(h, nx, pt, &dg)) || (rc = level_array(h, nx, pt, &di)) ||
+          (rc = level_array(h, nx, pt, &x)) || (rc = level_array(h, nx, pt, &b)))
+        return rc;
+      v.cE = ce; v.cN = cn; v.dg = dg; v.di = di; v.x = x; v.b = b;
+      v.xin = nullptr; v.csp = nullptr;
+      h->t64.push_back(v);
+    } else {
+      MgF v{};
+      v.nx = ny; v.ny = nx; v.pitch = pt;
+      bf16 *ce, *cn;
+      float *dg, *di, *x, *b;
+      if ((rc = level_array(h, nx, pt, &ce)) || (rc = level_array(h, nx, pt, &cn)) ||
+          (rc = level_array(h, nx, pt, &dg)) || (rc = level_array(h, nx, pt, &di)) ||
+          (rc = level_array(h, nx, pt, &x)) || (rc = level_array(h, nx, pt, &b)))
+        return rc;
+      v.cE = ce; v.cN = cn; v.dg = dg; v.di = di; v.x = x; v.b = b;
+      v.xin = nullptr; v.csp = h->mix[l].csp;
+      h->t32.push_back(v);
+    }
+  }
+  h->line_alloc = true;
+  return SCF_OK;
 }
 
 // one PCG iteration: z = M r, beta, p = z + beta p_old, q = A p, alpha,
@@ -427,6 +564,7 @@ int solve_common(scf_proj* h, const double* ustar, const double* vstar, double v
     st->status = status;
     st->levels = (int)h->lev.size();
     st->fallbacks = 0;
+    st->smoother = h->line ? SCF_SMOOTH_LINE : SCF_SMOOTH_POINT;
     st->bnorm = sqrt(S.bnorm2);
     st->relres = S.bnorm2 > 0 ? sqrt(S.rr / S.bnorm2) : 0.0;
     st->relres_true = S.bnorm2 > 0 ? sqrt(S.res_true2 / S.bnorm2) : 0.0;
@@ -457,6 +595,7 @@ void scf_opts_default(scf_opts* o) {
   o->npost = 2;
   o->omega = 1.9;
   o->coarse_max = 16;
+  o->smoother = SCF_SMOOTH_AUTO;
 }
 
 const char* scf_strerror(int code) {
@@ -485,6 +624,10 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
     return SCF_ERR_ARG;
   if (o.coarse_max < 1 || o.coarse_max > kMaxCoarse) return SCF_ERR_ARG;
   if (!(o.omega > 0.0 && o.omega < 2.0)) return SCF_ERR_ARG;
+  if (o.smoother != SCF_SMOOTH_AUTO && o.smoother != SCF_SMOOTH_POINT &&
+      o.smoother != SCF_SMOOTH_LINE)
+    return SCF_ERR_ARG;
+  if (o.smoother == SCF_SMOOTH_LINE && (nx > kLineMaxLen || ny > kLineMaxLen)) return SCF_ERR_ARG;
   scf_proj* h = new (std::nothrow) scf_proj();
   if (!h) return SCF_ERR_NOMEM;
   h->nx = nx; h->ny = ny; h->opts = o;
@@ -546,24 +689,25 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
   if ((rc = dev_alloc(h, (void**)&h->Ainv, sizeof(double) * kMaxCoarse * kMaxCoarse))) return fail(rc);
   if ((rc = dev_alloc(h, (void**)&h->cmap, sizeof(int) * kMaxCoarse))) return fail(rc);
   if ((rc = dev_alloc(h, (void**)&h->ncoarse, sizeof(int)))) return fail(rc);
-  // the single-CTA tail: first level >= 1 with at most kTailMaxCells cells
-  for (int l = 1; l < nlev; ++l)
-    if ((long)h->lev[l].nx * h->lev[l].ny <= kTailMaxCells) { h->tail0 = l; break; }
-  if (h->tail0 > 0 && nlev - h->tail0 > kTailMaxLevels) h->tail0 = 0;
-  if (h->tail0 > 0 && getenv("SCF_NO_TAIL")) h->tail0 = 0;
-  if (h->tail0 > 0) {
-    auto fill = [&](auto& d, auto view) {
-      d.n = nlev - h->tail0;
-      for (int l = 0; l < d.n; ++l) d.lv[l] = view(h->tail0 + l);
-      d.npre = o.npre; d.npost = o.npost;
-      d.omega = (decltype(d.omega))o.omega;
-      d.Ainv = h->Ainv; d.cmap = h->cmap; d.nc = h->ncoarse;
-      return tail_prepare(d);
-    };
-    int bad = fill(h->tail64, [h](int l) { return view64(h, l); });
-    if (h->mixed) bad |= fill(h->tail32, [h](int l) { return h->mix[l]; });
-    if (bad) h->tail0 = 0;
+  // the single-CTA tail: the first level >= 1 with at most kTailMaxCells cells
+  // whose levels fit one CTA's shared memory (ragged grids may need a later one)
+  if (!getenv("SCF_NO_TAIL")) {
+    for (int l = 1; l < nlev; ++l) {
+      if ((long)h->lev[l].nx * h->lev[l].ny > kTailMaxCells || nlev - l > kTailMaxLevels) continue;
+      auto fill = [&](auto& d, auto view) {
+        d.n = nlev - l;
+        for (int k = 0; k < d.n; ++k) d.lv[k] = view(l + k);
+        d.npre = o.npre; d.npost = o.npost;
+        d.omega = (decltype(d.omega))o.omega;
+        d.Ainv = h->Ainv; d.cmap = h->cmap; d.nc = h->ncoarse;
+        return tail_prepare(d);
+      };
+      int bad = fill(h->tail64, [h](int k) { return view64(h, k); });
+      if (h->mixed) bad |= fill(h->tail32, [h](int k) { return h->mix[k]; });
+      if (!bad) { h->tail0 = l; break; }
+    }
   }
+  if ((rc = dev_alloc(h, (void**)&h->aspect_bits, sizeof(unsigned)))) return fail(rc);
   if ((rc = dev_alloc(h, (void**)&h->sc, sizeof(Scalars)))) return fail(rc);
   if ((rc = dev_alloc(h, (void**)&h->sc_diag, sizeof(Scalars)))) return fail(rc);
   size_t nblk = 0;
@@ -573,6 +717,10 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
     if ((size_t)g2.x * g2.y > nblk) nblk = (size_t)g2.x * g2.y;
     size_t tb = (size_t)((nx + 63) / 64) * ((ny + 31) / 32);
     if (tb > nblk) nblk = tb;
+    // r.z reduction after a line-smoothed V-cycle: 32x8 blocks, at most 1024 rows of blocks
+    const size_t gy = (size_t)(ny + 7) / 8;
+    size_t rb = (size_t)((nx + 31) / 32) * (gy < 1024 ? gy : 1024);
+    if (rb > nblk) nblk = rb;
   }
   if ((rc = dev_alloc(h, (void**)&h->part, sizeof(double) * (2 * nblk + 64)))) return fail(rc);
   if (cudaMallocHost((void**)&h->sc_host, sizeof(Scalars)) != cudaSuccess) return fail(SCF_ERR_NOMEM);
@@ -633,6 +781,25 @@ int scf_proj_set_grid(scf_proj* h, const double* dx, const double* dy, const dou
       (rc = put(h, &h->st_dxU, dxU, n1)) || (rc = put(h, &h->st_dyV, dyV, n1)))
     return rc;
   h->fin.dx = h->st_dx; h->fin.dy = h->st_dy; h->fin.dxU = h->st_dxU; h->fin.dyV = h->st_dyV;
+  // smoother: lines when asked, or (auto) when some cell has an aspect ratio
+  // above 2 (couplings 4x stronger along one axis), where red-black point
+  // relaxation smooths poorly
+  bool want = h->opts.smoother == SCF_SMOOTH_LINE;
+  if (h->opts.smoother == SCF_SMOOTH_AUTO && h->nx <= kLineMaxLen && h->ny <= kLineMaxLen) {
+    unsigned bits = 0;
+    CK(cudaMemsetAsync(h->aspect_bits, 0, sizeof(unsigned), h->stream));
+    launch_aspect(h->st_dx, h->st_dy, n1, h->aspect_bits, h->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(&bits, h->aspect_bits, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                       h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    float aspect;
+    memcpy(&aspect, &bits, sizeof(aspect));
+    want = aspect > 2.0f;
+  }
+  if (want && (rc = alloc_line(h))) return rc;
+  if (want != h->line) destroy_graph(h);
+  h->line = want;
   CK(cudaStreamSynchronize(h->stream));
   h->have_grid = true;
   h->assembled = false;

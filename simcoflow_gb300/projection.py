@@ -46,7 +46,7 @@ class Opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("flags", C.c_int), ("device", C.c_int),
                 ("maxit", C.c_int), ("rtol", C.c_double), ("npre", C.c_int),
                 ("npost", C.c_int), ("omega", C.c_double), ("coarse_max", C.c_int),
-                ("reserved", C.c_int * 8)]
+                ("smoother", C.c_int), ("reserved", C.c_int * 7)]
 
 
 class Stats(C.Structure):
@@ -54,7 +54,8 @@ class Stats(C.Structure):
                 ("fallbacks", C.c_int), ("bnorm", C.c_double), ("relres", C.c_double),
                 ("relres_true", C.c_double), ("mres_max", C.c_double), ("ms_h2d", C.c_double),
                 ("ms_assemble", C.c_double), ("ms_solve", C.c_double),
-                ("ms_correct", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double)]
+                ("ms_correct", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double),
+                ("smoother", C.c_int)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -109,6 +110,9 @@ def _check(rc: int, where: str):
         raise ProjectionError(rc, where)
 
 
+# multigrid smoother (scf_opts.smoother / scf_stats.smoother)
+SMOOTHERS = {"auto": 0, "point": 1, "line": 2}
+
 GEOMETRY_ARGS = ("vof", "phi", "vofS", "nyS", "WlLh", "aE", "aW", "aN", "aS", "posnu_p",
                  "posnu_u", "moex_u", "vofS_u", "posnu_v", "moex_v", "vofS_v")
 
@@ -119,7 +123,7 @@ class ProjectionSolver:
     def __init__(self, nx: int, ny: int, precision: str = "fp64", device: int = 0,
                  device_ptrs: bool = False, use_graph: bool = True, maxit: int = 200,
                  rtol: float = 1e-8, npre: int = 2, npost: int = 2, omega: float = 1.9,
-                 coarse_max: int = 16):
+                 coarse_max: int = 16, smoother: str = "auto"):
         L = load()
         o = Opts()
         L.scf_opts_default(C.byref(o))
@@ -127,6 +131,7 @@ class ProjectionSolver:
         o.flags = (FLAG_DEVICE_PTRS if device_ptrs else 0) | (0 if use_graph else FLAG_NO_GRAPH)
         o.device, o.maxit, o.rtol = device, maxit, rtol
         o.npre, o.npost, o.omega, o.coarse_max = npre, npost, omega, coarse_max
+        o.smoother = SMOOTHERS[smoother]
         self.nx, self.ny, self.device_ptrs = nx, ny, device_ptrs
         self.opts = o
         h = C.c_void_p()

@@ -233,3 +233,22 @@ def test_geometry_top_row_keeps_open_faces(built):
     for inst in range(8):
         c = synth.c5(instance=inst, n=64)
         assert (c["aN"][1:-1, c.ny] > 0).all()
+
+
+def test_oracle_line_smoother_on_stretched_grid(oracle, built):
+    """The point smoother stalls on the stretched 4096^2 configuration's grid
+    (scaled down); the line smoother converges in a grid-independent number
+    of iterations and reaches the direct solution."""
+    its = {}
+    for n in (128, 256):
+        c = synth.c3(n=n)
+        r = oracle.project(c)
+        xp, itp, _, _ = oracle.mgpcg(c, r["matr"], r["rhm"], rtol=1e-8, maxit=1000)
+        xl, itl, rel, _ = oracle.mgpcg(c, r["matr"], r["rhm"], rtol=1e-12, maxit=200,
+                                       smoother="line")
+        pn = c["posnu_p"][1:n + 1, 1:n + 1] != -1
+        xd = r["Pp"][1:n + 1, 1:n + 1]
+        assert np.linalg.norm((xl - xd)[pn]) <= 1e-9 * np.linalg.norm(xd[pn])
+        its[n] = (itp, itl)
+    assert all(itl < 30 for _, itl in its.values())
+    assert all(itp > 3 * itl for itp, itl in its.values())
