@@ -40,6 +40,60 @@ __device__ __forceinline__ float lcoef<__nv_bfloat16, float>(const __nv_bfloat16
   return __bfloat162float(p[k]) * cs;
 }
 
+// M consecutive values from an aligned row position as T (16-byte vector
+// loads; a chunk never extends past the row's padded pitch).  The words of
+// each vector are unpacked by value, so nothing goes through local memory.
+__device__ __forceinline__ void unpack(const uint4& u, float* e) {
+  e[0] = __uint_as_float(u.x); e[1] = __uint_as_float(u.y);
+  e[2] = __uint_as_float(u.z); e[3] = __uint_as_float(u.w);
+}
+__device__ __forceinline__ void unpack(const uint4& u, double* e) {
+  e[0] = __hiloint2double((int)u.y, (int)u.x);
+  e[1] = __hiloint2double((int)u.w, (int)u.z);
+}
+__device__ __forceinline__ float bf_lo(unsigned w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf_hi(unsigned w) { return __uint_as_float(w & 0xffff0000u); }
+__device__ __forceinline__ uint4 pack(const float* e) {
+  return make_uint4(__float_as_uint(e[0]), __float_as_uint(e[1]), __float_as_uint(e[2]),
+                    __float_as_uint(e[3]));
+}
+__device__ __forceinline__ uint4 pack(const double* e) {
+  return make_uint4((unsigned)__double2loint(e[0]), (unsigned)__double2hiint(e[0]),
+                    (unsigned)__double2loint(e[1]), (unsigned)__double2hiint(e[1]));
+}
+
+template <class T, int M>
+__device__ __forceinline__ void vload(const T* p, T (&o)[M]) {
+  static_assert((M * sizeof(T)) % 16 == 0, "chunk must be whole 16-byte vectors");
+  constexpr int PER = 16 / sizeof(T);
+#pragma unroll
+  for (int v = 0; v < M / PER; ++v) unpack(__ldg(reinterpret_cast<const uint4*>(p) + v), o + v * PER);
+}
+template <int M>
+__device__ __forceinline__ void cvload(const double* p, double (&o)[M], float) {
+  vload<double, M>(p, o);
+}
+// BF16 couplings: 8 per vector, widened to FP32 and scaled
+template <int M>
+__device__ __forceinline__ void cvload(const __nv_bfloat16* p, float (&o)[M], float cs) {
+  static_assert((M * 2) % 16 == 0, "chunk must be whole 16-byte vectors");
+#pragma unroll
+  for (int v = 0; v < M / 8; ++v) {
+    const uint4 u = __ldg(reinterpret_cast<const uint4*>(p) + v);
+    float* e = o + v * 8;
+    e[0] = bf_lo(u.x) * cs; e[1] = bf_hi(u.x) * cs;
+    e[2] = bf_lo(u.y) * cs; e[3] = bf_hi(u.y) * cs;
+    e[4] = bf_lo(u.z) * cs; e[5] = bf_hi(u.z) * cs;
+    e[6] = bf_lo(u.w) * cs; e[7] = bf_hi(u.w) * cs;
+  }
+}
+template <class T, int M>
+__device__ __forceinline__ void vstore(T* p, const T (&o)[M]) {
+  constexpr int PER = 16 / sizeof(T);
+#pragma unroll
+  for (int v = 0; v < M / PER; ++v) reinterpret_cast<uint4*>(p)[v] = pack(o + v * PER);
+}
+
 // Relax the lines (rows) iy = 2*blockIdx.x + colour of level L.
 // ZERO: the iterate is zero on entry (the first pass of a V-cycle level):
 // the neighbouring rows are not read, and they are written as zero.
@@ -62,29 +116,43 @@ k_line(MgView<T, CT, T> L, int colour, const Scalars* sc) {
 
   T a[M], d[M], c[M], r[M];
   unsigned actm = 0;  // bit k: cell k has an unknown
-#pragma unroll
-  for (int k = 0; k < M; ++k) {
-    const int ix = t * M + k;
-    T dv = T(-1), aw = T(0), ce = T(0), rv = T(0);
-    if (ix < nx) {
-      const size_t g = g0 + ix;
-      dv = L.dg[g];
-      if (dv > T(0)) {
-        aw = lcoef<CT, T>(L.cE, g - 1, cs);
-        ce = lcoef<CT, T>(L.cE, g, cs);
-        rv = L.b[g];
-        if (!ZERO) {
-          rv = fma(lcoef<CT, T>(L.cN, g, cs), L.x[g + P], rv);
-          rv = fma(lcoef<CT, T>(L.cN, g - P, cs), L.x[g - P], rv);
-        }
-      }
+  const int ix0 = t * M;
+  if (ix0 < nx) {
+    // the chunk ends at or before round_up(nx, M) <= pitch: whole vectors
+    // stay inside the row (padding cells are zero and count as inactive)
+    const size_t g = g0 + ix0;
+    T dv[M], ce[M], bv[M];
+    vload<T, M>(L.dg + g, dv);
+    cvload<M>(L.cE + g, ce, cs);
+    vload<T, M>(L.b + g, bv);
+    const T aw0 = lcoef<CT, T>(L.cE, g - 1, cs);
+    T xn[M], xs[M], cn[M], cs_[M];
+    if (!ZERO) {
+      vload<T, M>(L.x + g + P, xn);
+      vload<T, M>(L.x + g - P, xs);
+      cvload<M>(L.cN + g, cn, cs);
+      cvload<M>(L.cN + g - P, cs_, cs);
     }
-    const bool act = dv > T(0);
-    actm |= act ? (1u << k) : 0u;
-    a[k] = act ? -aw : T(0);
-    c[k] = act ? -ce : T(0);
-    d[k] = act ? dv : T(1);
-    r[k] = act ? rv : T(0);
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+      const bool act = dv[k] > T(0) && ix0 + k < nx;
+      T rv = bv[k];
+      if (!ZERO) rv = fma(cs_[k], xs[k], fma(cn[k], xn[k], rv));
+      const T aw = k == 0 ? aw0 : ce[k - 1];
+      actm |= act ? (1u << k) : 0u;
+      a[k] = act ? -aw : T(0);
+      c[k] = act ? -ce[k] : T(0);
+      d[k] = act ? dv[k] : T(1);
+      r[k] = act ? rv : T(0);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+      a[k] = T(0);
+      c[k] = T(0);
+      d[k] = T(1);
+      r[k] = T(0);
+    }
   }
 
   // interior cells 0..M-2: forward elimination with three right-hand sides
@@ -128,15 +196,14 @@ k_line(MgView<T, CT, T> L, int colour, const Scalars* sc) {
   T ec = cI * Tn;
   T ed = fma(-cI, Dn, fma(-aI, D[M - 2], rI));
   // parallel cyclic reduction over the nth interface equations
-  T* buf[2] = {pa, pa + 4 * nth};
-  int cur = 0;
-  buf[0][t] = ea;
-  buf[0][nth + t] = eb;
-  buf[0][2 * nth + t] = ec;
-  buf[0][3 * nth + t] = ed;
+  int cur = 0;  // PCR buffer cur starts at pa + cur * 4 * nth
+  pa[t] = ea;
+  pa[nth + t] = eb;
+  pa[2 * nth + t] = ec;
+  pa[3 * nth + t] = ed;
   __syncthreads();
   for (int s = 1; s < nth; s <<= 1) {
-    const T* A_ = buf[cur];
+    const T* A_ = pa + cur * 4 * nth;
     const T* B_ = A_ + nth;
     const T* C_ = B_ + nth;
     const T* D_ = C_ + nth;
@@ -153,7 +220,7 @@ k_line(MgView<T, CT, T> L, int colour, const Scalars* sc) {
       nb = fma(-A_[t + s], k2, nb);
       nd = fma(-D_[t + s], k2, nd);
     }
-    T* W = buf[cur ^ 1];
+    T* W = pa + (cur ^ 1) * 4 * nth;
     W[t] = na;
     W[nth + t] = nb;
     W[2 * nth + t] = nc;
@@ -161,17 +228,27 @@ k_line(MgView<T, CT, T> L, int colour, const Scalars* sc) {
     cur ^= 1;
     __syncthreads();
   }
-  const T It = buf[cur][3 * nth + t] / buf[cur][nth + t];
+  const T It = pa[cur * 4 * nth + 3 * nth + t] / pa[cur * 4 * nth + nth + t];
   rD0[t] = It;  // rD0 is no longer read by anyone after the first barrier above
   __syncthreads();
   const T Il = t > 0 ? rD0[t - 1] : T(0);
+  if (ix0 >= nx) return;
+  T xo[M];
 #pragma unroll
   for (int k = 0; k < M; ++k) {
-    const int ix = t * M + k;
-    if (ix >= nx) break;
     const T v = (k == M - 1) ? It : fma(S[k], Il, fma(Tr[k], It, D[k]));
-    L.x[g0 + ix] = (actm >> k) & 1u ? v : T(0);
-    if (ZERO && iy + 1 < L.ny) L.x[g0 + P + ix] = T(0);
+    xo[k] = (actm >> k) & 1u ? v : T(0);
+  }
+  if (ix0 + M <= nx) {
+    vstore<T, M>(L.x + g0 + ix0, xo);
+  } else {  // the ghost columns past nx keep their zeros
+    for (int k = 0; k < nx - ix0; ++k) L.x[g0 + ix0 + k] = xo[k];
+  }
+  if (ZERO && iy + 1 < L.ny) {
+    T z[M];
+#pragma unroll
+    for (int k = 0; k < M; ++k) z[k] = T(0);
+    vstore<T, M>(L.x + g0 + P + ix0, z);
   }
 }
 
@@ -251,7 +328,205 @@ __global__ void k_aspect(const double* __restrict__ dx, const double* __restrict
   if ((threadIdx.x & 31) == 0) atomicMax(out_bits, __float_as_uint(m));
 }
 
+// The coarse end of a line-smoothed V-cycle in one CTA: every level of at
+// most kTailMaxCells cells, down to the dense coarsest solve and back up,
+// with x, b, the couplings and the diagonal of all those levels in shared
+// memory (each level padded by a zero ghost ring).  Each line is solved by
+// one thread with the Thomas algorithm (short lines: a serial solve per line
+// is cheaper than the partitioned one).  Same passes, in the same order, as
+// the per-level kernels.
+template <class T, class CT>
+__global__ void __launch_bounds__(1024) k_line_tail(TailDesc<T, CT> d, Scalars* sc) {
+  pdl_wait();
+  if (sc->done) return;
+  extern __shared__ __align__(16) unsigned char ltail_smem[];
+  T* sm = reinterpret_cast<T*>(ltail_smem);
+  double* bd = reinterpret_cast<double*>(ltail_smem + d.bd_off);
+  const int t = threadIdx.x, NTT = blockDim.x;
+  for (int i = t; i < d.total; i += NTT) sm[i] = T(0);
+  __syncthreads();
+  auto W = [&](int l) { return d.lv[l].nx + 2; };
+  auto WH = [&](int l) { return (d.lv[l].nx + 2) * (d.lv[l].ny + 2); };
+  auto X = [&](int l) { return sm + d.off[l]; };
+  auto B = [&](int l) { return sm + d.off[l] + WH(l); };
+  auto E = [&](int l) { return sm + d.off[l] + 2 * WH(l); };
+  auto N = [&](int l) { return sm + d.off[l] + 3 * WH(l); };
+  auto G = [&](int l) { return sm + d.off[l] + 4 * WH(l); };
+  T* CP = sm + d.off[d.n];  // line-solve scratch, the size of the first tail level
+  T* DP = CP + WH(0);
+  for (int l = 0; l < d.n; ++l) {
+    const MgView<T, CT, T>& L = d.lv[l];
+    const float cs = L.csp ? __ldg(L.csp) : 1.0f;
+    for (int k = t; k < L.nx * L.ny; k += NTT) {
+      const int ix = k % L.nx, iy = k / L.nx;
+      const size_t g = (size_t)iy * L.pitch + ix;
+      const int si = (iy + 1) * W(l) + ix + 1;
+      E(l)[si] = lcoef<CT, T>(L.cE, g, cs);
+      N(l)[si] = lcoef<CT, T>(L.cN, g, cs);
+      G(l)[si] = L.dg[g];
+      if (l == 0) B(0)[si] = L.b[g];
+    }
+  }
+  __syncthreads();
+  // lines of one parity: dir 0 rows, dir 1 columns; thread q solves line q
+  auto pass = [&](int l, int dir, int colour) {
+    const int nx = d.lv[l].nx, ny = d.lv[l].ny, w = W(l);
+    const int nlines = dir == 0 ? ny : nx, len = dir == 0 ? nx : ny;
+    const int step = dir == 0 ? 1 : w;  // cell stride along the line
+    const int cross = dir == 0 ? w : 1;  // stride to the neighbouring line
+    const T* Ax = dir == 0 ? E(l) : N(l);  // in-line couplings
+    const T* Cx = dir == 0 ? N(l) : E(l);  // cross couplings
+    const T* b = B(l);
+    const T* g = G(l);
+    T* x = X(l);
+    for (int q = colour + 2 * t; q < nlines; q += 2 * NTT) {
+      int si = (dir == 0 ? (q + 1) * w + 1 : w + q + 1);
+      T cpp = T(0), dpp = T(0);
+      for (int k = 0; k < len; ++k, si += step) {
+        T a = T(0), c = T(0), dd = T(1), r = T(0);
+        const T gv = g[si];
+        if (gv > T(0)) {
+          a = -Ax[si - step];
+          c = -Ax[si];
+          dd = gv;
+          r = fma(Cx[si], x[si + cross], b[si]);
+          r = fma(Cx[si - cross], x[si - cross], r);
+        }
+        const T inv = T(1) / fma(-a, cpp, dd);
+        cpp = c * inv;
+        dpp = fma(-a, dpp, r) * inv;
+        CP[si] = cpp;
+        DP[si] = dpp;
+      }
+      T xn = T(0);
+      for (int k = len - 1; k >= 0; --k) {
+        si -= step;
+        xn = fma(-CP[si], xn, DP[si]);
+        x[si] = g[si] > T(0) ? xn : T(0);
+      }
+    }
+    __syncthreads();
+  };
+  const int ns_pre = (d.npre + 1) / 2, ns_post = (d.npost + 1) / 2;
+  const int n = d.n;
+  for (int l = 0; l < n - 1; ++l) {
+    for (int it = 0; it < ns_pre; ++it) {
+      pass(l, 0, 0); pass(l, 0, 1); pass(l, 1, 0); pass(l, 1, 1);
+    }
+    // residual summed 2x2 onto level l+1
+    const MgView<T, CT, T>& L = d.lv[l];
+    const MgView<T, CT, T>& C = d.lv[l + 1];
+    const T* x = X(l);
+    const T* b = B(l);
+    T* bc = B(l + 1);
+    const int w = W(l), wc = W(l + 1);
+    for (int k = t; k < C.nx * C.ny; k += NTT) {
+      const int I = k % C.nx, J = k / C.nx;
+      T s = T(0);
+      for (int dj = 0; dj < 2; ++dj)
+        for (int dq = 0; dq < 2; ++dq) {
+          const int gx = 2 * I + dq, gy = 2 * J + dj;
+          if (gx >= L.nx || gy >= L.ny) continue;
+          const int si = (gy + 1) * w + gx + 1;
+          const T dgv = G(l)[si];
+          if (dgv < T(0)) continue;
+          T r = fma(-dgv, x[si], b[si]);
+          r = fma(E(l)[si], x[si + 1], r);
+          r = fma(E(l)[si - 1], x[si - 1], r);
+          r = fma(N(l)[si], x[si + w], r);
+          r = fma(N(l)[si - w], x[si - w], r);
+          s += r;
+        }
+      bc[(J + 1) * wc + I + 1] = s;
+    }
+    __syncthreads();
+  }
+  {  // dense FP64 solve on the coarsest level
+    const MgView<T, CT, T>& C = d.lv[n - 1];
+    const int ncell = C.nx * C.ny, nn = *d.nc, w = W(n - 1);
+    const T* b = B(n - 1);
+    T* x = X(n - 1);
+    for (int k = t; k < ncell; k += NTT) {
+      const int r = d.cmap[k];
+      if (r >= 0) bd[r] = (double)b[(k / C.nx + 1) * w + (k % C.nx) + 1];
+    }
+    __syncthreads();
+    for (int k = t; k < ncell; k += NTT) {
+      const int r = d.cmap[k];
+      double y = 0.0;
+      if (r >= 0)
+        for (int c = 0; c < nn; ++c) y = fma(d.Ainv[r * nn + c], bd[c], y);
+      x[(k / C.nx + 1) * w + (k % C.nx) + 1] = (T)y;
+    }
+    __syncthreads();
+  }
+  for (int l = n - 2; l >= 0; --l) {
+    const MgView<T, CT, T>& L = d.lv[l];
+    T* x = X(l);
+    const T* xc = X(l + 1);
+    const int w = W(l), wc = W(l + 1);
+    for (int k = t; k < L.nx * L.ny; k += NTT) {
+      const int ix = k % L.nx, iy = k / L.nx;
+      const int si = (iy + 1) * w + ix + 1;
+      if (G(l)[si] > T(0)) x[si] = fma(d.omega, xc[((iy >> 1) + 1) * wc + (ix >> 1) + 1], x[si]);
+    }
+    __syncthreads();
+    for (int it = 0; it < ns_post; ++it) {
+      pass(l, 1, 1); pass(l, 1, 0); pass(l, 0, 1); pass(l, 0, 0);
+    }
+  }
+  {  // x of the first tail level back to global memory
+    const MgView<T, CT, T>& L = d.lv[0];
+    const T* x = X(0);
+    for (int k = t; k < L.nx * L.ny; k += NTT) {
+      const int ix = k % L.nx, iy = k / L.nx;
+      L.x[(size_t)iy * L.pitch + ix] = x[(iy + 1) * W(0) + ix + 1];
+    }
+  }
+}
+
 }  // namespace
+
+template <class T, class CT>
+int line_tail_prepare(TailDesc<T, CT>& d) {
+  if (d.n < 1 || d.n + 1 > kTailMaxLevels) return -1;
+  int off = 0;
+  for (int l = 0; l < d.n; ++l) {
+    d.off[l] = off;
+    off += 5 * (d.lv[l].nx + 2) * (d.lv[l].ny + 2);
+  }
+  d.off[d.n] = off;  // scratch
+  off += 2 * (d.lv[0].nx + 2) * (d.lv[0].ny + 2);
+  d.total = off;
+  size_t bytes = (size_t)off * sizeof(T);
+  bytes = (bytes + 15) / 16 * 16;
+  d.bd_off = (int)bytes;
+  bytes += kMaxCoarse * sizeof(double);
+  d.smem = (int)bytes;
+  int dev = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+      bytes > (size_t)optin)
+    return -1;
+  if (cudaFuncSetAttribute(k_line_tail<T, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           d.smem) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return -1;
+  }
+  return 0;
+}
+
+template <class T, class CT>
+void launch_line_tail(const TailDesc<T, CT>& d, Scalars* sc, cudaStream_t s) {
+  launch_k(k_line_tail<T, CT>, dim3(1), dim3(1024), (size_t)d.smem, s, d, sc);
+}
+
+template int line_tail_prepare<double, double>(TailDesc<double, double>&);
+template int line_tail_prepare<float, __nv_bfloat16>(TailDesc<float, __nv_bfloat16>&);
+template void launch_line_tail<double, double>(const TailDesc<double, double>&, Scalars*,
+                                               cudaStream_t);
+template void launch_line_tail<float, __nv_bfloat16>(const TailDesc<float, __nv_bfloat16>&,
+                                                     Scalars*, cudaStream_t);
 
 int line_threads(int len, int* chunk) {
   int m = len <= 4096 ? 8 : len <= 8192 ? 16 : len <= kLineMaxLen ? 32 : 0;

@@ -238,14 +238,16 @@ __global__ void k_dot_rz_t(int nx, int ny, int pitch, const BT* r, const T* z, i
                            Scalars* sc, double* part) {
   pdl_wait();
   if (sc->done) return;
-  double a1 = 0.0, a2 = 0.0;
+  // each thread accumulates its column strip in T (FP32 for the mixed
+  // preconditioner, whose z is FP32 anyway), the grid combines in FP64
+  T acc = T(0);
   const int ix = blockIdx.x * 32 + threadIdx.x;
   if (ix < nx)
     for (int iy = blockIdx.y * 8 + threadIdx.y; iy < ny; iy += gridDim.y * 8) {
       const size_t k = (size_t)iy * pitch + ix;
-      a1 = fma((double)r[k], (double)z[k], a1);
-
+      acc = fma((T)r[k], z[k], acc);
     }
+  const double a1 = (double)acc, a2 = 0.0;
   double t1, t2;
   if (grid_sum2(a1, a2, part, &sc->tickets[T_RZ], &t1, &t2) && tlin() == 0)
     set_beta(sc, t1, flexible);
@@ -582,6 +584,13 @@ static dim3 small_grid(int nx, int ny) {
   int gy = (ny + 7) / 8;
   return dim3((nx + 31) / 32, gy < 1024 ? gy : 1024);
 }
+// grid-stride reductions: about 16 blocks of 256 threads per SM
+static dim3 reduce_grid(int nx, int ny) {
+  const int gx = (nx + 31) / 32;
+  int gy = (ny + 7) / 8;
+  const int cap = 2432 / gx > 1 ? 2432 / gx : 1;
+  return dim3(gx, gy < cap ? gy : cap);
+}
 
 template <class T, class CT, class BT>
 void launch_sweep(const MgView<T, CT, BT>& L, const MgView<T, CT, T>& C, int first, bool zero,
@@ -612,7 +621,7 @@ void launch_coarse_solve_t(const MgView<T, CT, BT>& C, const double* Ainv, const
 template <class T, class BT>
 void launch_dot_rz_t(int nx, int ny, int pitch, const BT* r, const T* z, int flexible,
                      Scalars* sc, double* part, cudaStream_t s) {
-  launch_k(k_dot_rz_t<T, BT>, small_grid(nx, ny), dim3(32, 8), 0, s, nx, ny, pitch, r, z,
+  launch_k(k_dot_rz_t<T, BT>, reduce_grid(nx, ny), dim3(32, 8), 0, s, nx, ny, pitch, r, z,
            flexible, sc, part);
 }
 

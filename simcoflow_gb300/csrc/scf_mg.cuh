@@ -47,6 +47,12 @@ struct TailDesc {
 };
 template <class T, class CT>
 int tail_prepare(TailDesc<T, CT>& d);  // fills offsets and sizes; 0 on success
+// the same for the line-smoother tail (scf_line.cu): per level x, b, cE, cN,
+// dg in shared memory, plus two line-solve scratch arrays of the first level
+template <class T, class CT>
+int line_tail_prepare(TailDesc<T, CT>& d);
+template <class T, class CT>
+void launch_line_tail(const TailDesc<T, CT>& d, Scalars* sc, cudaStream_t s);
 template <class T, class CT>
 void launch_tail(const TailDesc<T, CT>& d, Scalars* sc, cudaStream_t s);
 

@@ -50,6 +50,9 @@ struct scf_proj {
   // for the lines along y; allocated when the line smoother is selected
   bool line = false;
   bool line_alloc = false;
+  int ltail0 = 0;  // first level of the single-CTA line tail (0: none)
+  TailDesc<double, double> ltail64{};
+  TailDesc<float, bf16> ltail32{};
   std::vector<MgD> t64;
   std::vector<MgF> t32;
   unsigned* aspect_bits = nullptr;  // device: largest cell aspect ratio (float bits)
@@ -216,8 +219,8 @@ void enqueue_vcycle_t(scf_proj* h, ViewFn view, BufFn buf, const TailDesc<T, CT>
 // sweeps of npre / npost.  x and b move to the transposed layout by tiled
 // transposes (b once per level and V-cycle).  Every pass updates x in place.
 template <class T, class CT, class ViewFn, class TViewFn>
-void enqueue_vcycle_line_t(scf_proj* h, ViewFn view, TViewFn tview, Scalars* sc, bool do_rz,
-                           int flexible, cudaStream_t s) {
+void enqueue_vcycle_line_t(scf_proj* h, ViewFn view, TViewFn tview, const TailDesc<T, CT>& tail,
+                           Scalars* sc, bool do_rz, int flexible, cudaStream_t s) {
   using V = MgView<T, CT, T>;
   const int L = (int)h->lev.size();
   const int npre = (h->opts.npre + 1) / 2, npost = (h->opts.npost + 1) / 2;
@@ -246,19 +249,21 @@ void enqueue_vcycle_line_t(scf_proj* h, ViewFn view, TViewFn tview, Scalars* sc,
       launch_line(f, 0, false, sc, s);
     }
   };
-  if (L > 1) {
-    for (int l = 0; l < L - 1; ++l) {
-      const V f = view(l), ft = tview(l);
-      launch_transpose<T>(f.b, f.nx, f.ny, f.pitch, ft.b, ft.pitch, sc, s);
-      for (int it = 0; it < npre; ++it) step(l, false, it == 0);
-      launch_resid_restrict_l(f, view(l + 1), sc, s);
-    }
+  // levels 0 .. lk-1 run as kernels; the tail (or the coarse solve) covers lk .. L-1
+  const int lk = h->ltail0 > 0 ? h->ltail0 : L - 1;
+  for (int l = 0; l < lk; ++l) {
+    const V f = view(l), ft = tview(l);
+    launch_transpose<T>(f.b, f.nx, f.ny, f.pitch, ft.b, ft.pitch, sc, s);
+    for (int it = 0; it < npre; ++it) step(l, false, it == 0);
+    launch_resid_restrict_l(f, view(l + 1), sc, s);
   }
-  {
+  if (h->ltail0 > 0) {
+    launch_line_tail(tail, sc, s);
+  } else {
     V c = view(L - 1);
     launch_coarse_solve_t(c, h->Ainv, h->cmap, h->ncoarse, sc, s);
   }
-  for (int l = L - 2; l >= 0; --l) {
+  for (int l = lk - 1; l >= 0; --l) {
     const V f = view(l), c = view(l + 1);
     launch_prolong_l(f, c.x, c.pitch, om, sc, s);
     for (int it = 0; it < npost; ++it) step(l, true, false);
@@ -276,7 +281,7 @@ void enqueue_vcycle(scf_proj* h, Scalars* sc, bool do_rz, cudaStream_t s) {
     auto buf = [h](int l, int i) { return buf64(h, l, i); };
     if (h->line) {
       auto tview = [h](int l) { return h->t64[l]; };
-      enqueue_vcycle_line_t<double, double>(h, view, tview, sc, do_rz, 0, s);
+      enqueue_vcycle_line_t<double, double>(h, view, tview, h->ltail64, sc, do_rz, 0, s);
     } else {
       enqueue_vcycle_t(h, view, buf, h->tail64, sc, do_rz, 0, s);
     }
@@ -289,7 +294,7 @@ void enqueue_vcycle(scf_proj* h, Scalars* sc, bool do_rz, cudaStream_t s) {
     auto buf = [h](int l, int i) { return buf32(h, l, i); };
     if (h->line) {
       auto tview = [h](int l) { return h->t32[l]; };
-      enqueue_vcycle_line_t<float, bf16>(h, view, tview, sc, do_rz, 1, s);
+      enqueue_vcycle_line_t<float, bf16>(h, view, tview, h->ltail32, sc, do_rz, 1, s);
     } else {
       enqueue_vcycle_t(h, view, buf, h->tail32, sc, do_rz, 1, s);
     }
@@ -705,6 +710,24 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
       int bad = fill(h->tail64, [h](int k) { return view64(h, k); });
       if (h->mixed) bad |= fill(h->tail32, [h](int k) { return h->mix[k]; });
       if (!bad) { h->tail0 = l; break; }
+    }
+  }
+  // the single-CTA tail of the line smoother, chosen the same way
+  if (o.smoother != SCF_SMOOTH_POINT && !getenv("SCF_NO_TAIL")) {
+    for (int l = 1; l < nlev; ++l) {
+      if ((long)h->lev[l].nx * h->lev[l].ny > kTailMaxCells || nlev - l + 1 > kTailMaxLevels)
+        continue;
+      auto fill = [&](auto& d, auto view) {
+        d.n = nlev - l;
+        for (int k = 0; k < d.n; ++k) d.lv[k] = view(l + k);
+        d.npre = o.npre; d.npost = o.npost;
+        d.omega = (decltype(d.omega))o.omega;
+        d.Ainv = h->Ainv; d.cmap = h->cmap; d.nc = h->ncoarse;
+        return line_tail_prepare(d);
+      };
+      int bad = h->mixed ? fill(h->ltail32, [h](int k) { return h->mix[k]; })
+                         : fill(h->ltail64, [h](int k) { return view64(h, k); });
+      if (!bad) { h->ltail0 = l; break; }
     }
   }
   if ((rc = dev_alloc(h, (void**)&h->aspect_bits, sizeof(unsigned)))) return fail(rc);
