@@ -63,6 +63,15 @@ extern "C" {
  * some cell's aspect ratio max(dx/dy, dy/dx) exceeds 2, else POINT.
  * BoomerAMG, which this replaces (src/ProjectionP_Mod.f90:116-133), adapts
  * to anisotropy through its strength-of-connection coarsening. */
+/* Preconditioner of the flexible PCG.  MG: the multigrid V-cycle.  LEARNED
+ * (mixed precision only): the U-Net of scf_unet.h, given by
+ * scf_proj_set_network, for as long as each of its iterations reduces the
+ * residual norm by at least the factor 0.6; from the first iteration that
+ * does not, the V-cycle for the rest of the solve (stats.fallbacks = 1).
+ * The FP64 residual decides convergence either way. */
+#define SCF_PRECOND_MG 0
+#define SCF_PRECOND_LEARNED 1
+
 #define SCF_SMOOTH_AUTO 0
 #define SCF_SMOOTH_POINT 1
 #define SCF_SMOOTH_LINE 2
@@ -77,7 +86,8 @@ typedef struct scf_opts {
     double omega;    /* scale of the coarse-grid correction */
     int coarse_max;  /* coarsest level has at most this many cells (<= 64) */
     int smoother;    /* SCF_SMOOTH_AUTO (default), SCF_SMOOTH_POINT or SCF_SMOOTH_LINE */
-    int reserved[7];
+    int precond;     /* SCF_PRECOND_MG (default) or SCF_PRECOND_LEARNED */
+    int reserved[6];
 } scf_opts;
 
 typedef struct scf_stats {
@@ -91,9 +101,27 @@ typedef struct scf_stats {
     double mres_max;    /* max |mres| over cells with Posnu /= -1 (update_puv) */
     double ms_h2d, ms_assemble, ms_solve, ms_correct, ms_d2h, ms_total;
     int smoother;       /* SCF_SMOOTH_POINT or SCF_SMOOTH_LINE: the smoother used */
+    int learned_iters;  /* iterations preconditioned by the network (SCF_PRECOND_LEARNED) */
 } scf_stats;
 
 typedef struct scf_proj scf_proj;
+
+/* Network of SCF_PRECOND_LEARNED: params is a host array of
+ * scf_unet_num_params() floats in the order of scf_unet.h.  The handle keeps
+ * its own device copy.  No reference counterpart (the reference
+ * preconditions with BoomerAMG, src/ProjectionP_Mod.f90:116-133). */
+int scf_proj_set_network(struct scf_proj *h, const float *params, int nparams);
+
+/* Solve A x = b with the assembled operator for an arbitrary right-hand
+ * side b ((nx,ny), zero on cells without an unknown), at most maxit
+ * iterations (0 <= maxit <= opts.maxit; 0 gives x = 0).  x and, when not
+ * null, the final recursive residual r are (nx,ny) outputs.  Returns
+ * SCF_ERR_NOT_CONVERGED when maxit ran out before opts.rtol, with x and r
+ * written.  This is the same PCG as PoissonEquationSolver's (without the
+ * HYPRE vector setup of src/ProjectionP_Mod.f90:275-354); it generates the
+ * residual/error pairs that train the learned preconditioner. */
+int scf_proj_solve_rhs(struct scf_proj *h, const double *b, double *x, double *r, int maxit,
+                       struct scf_stats *st);
 
 /* Fill opts with defaults: FP64, host pointers, device 0, maxit 200,
  * rtol 1e-8, 2 pre / 2 post sweeps, omega 1.9, coarse_max 16. */

@@ -21,7 +21,8 @@ LIB = PKG / "_lib"
 INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["scf_kernels.cu", "scf_mg.cu", "scf_line.cu", "scf_proj.cu", "scf_noalloc.cu"]
+CUDA_SOURCES = ["scf_kernels.cu", "scf_mg.cu", "scf_line.cu", "scf_unet.cu", "scf_proj.cu",
+                "scf_noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -117,6 +117,9 @@ void launch_coarse_setup(LevelView C, double* Ainv, int* cmap, int* nc, cudaStre
 void launch_rhs(const FortranIn& in, const double* ustar, const double* vstar, double vb,
                 LevelView L0, double* bvec, double* r, float* r32, double* x, Scalars* sc,
                 double* part, double rtol, int maxit, cudaStream_t s);
+void launch_rhs_given(int nx, int ny, const double* bF, LevelView L0, double* bvec, double* r,
+                      float* r32, double* x, Scalars* sc, double* part, double rtol, int maxit,
+                      cudaStream_t s);
 void launch_update_xr(LevelView L0, double* x, const double* p, double* r, float* r32,
                       const float* z32, const double* q, Scalars* sc, double* part,
                       unsigned long long cond, cudaStream_t s);

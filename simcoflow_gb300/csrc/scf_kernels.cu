@@ -391,6 +391,9 @@ __global__ void k_coarse_setup(LevelView C, double* Ainv, int* cmap, int* nc_out
 // Right-hand side: SetPoissonVectors (src/ProjectionP_Mod.f90:306-337).
 // Also starts the PCG: r = b, x = 0, scalars reset.
 // ---------------------------------------------------------------------------
+__device__ void rhs_finish(double acc, bool bad, Scalars* sc, double* part, double rtol,
+                           int maxit);
+
 __global__ void k_rhs(FortranIn in, const double* us, const double* vs, double vb, int pitch,
                       double* bvec, double* r, float* r32, double* x, Scalars* sc, double* part,
                       double rtol, int maxit) {
@@ -419,6 +422,36 @@ __global__ void k_rhs(FortranIn in, const double* us, const double* vs, double v
       acc = fma(bv, bv, acc);
     }
   }
+  rhs_finish(acc, bad, sc, part, rtol, maxit);
+}
+
+// PCG start from a given right-hand side bF (Fortran (nx,ny) order; zero on
+// cells without an unknown): the same state as k_rhs leaves
+__global__ void k_rhs_given(int nx, int ny, const double* bF, LevelView L, double* bvec,
+                            double* r, float* r32, double* x, Scalars* sc, double* part,
+                            double rtol, int maxit) {
+  pdl_wait();
+  const int ix = blockIdx.x * kBX + threadIdx.x;
+  double acc = 0.0;
+  bool bad = false;
+  if (ix < nx) {
+    for (int iy = blockIdx.y * kBY + threadIdx.y; iy < ny; iy += gridDim.y * kBY) {
+      const size_t kl = (size_t)iy * L.pitch + ix;
+      const double bv = L.dg[kl] > 0.0 ? bF[(size_t)iy * nx + ix] : 0.0;
+      if (!isfinite(bv)) bad = true;
+      bvec[kl] = bv;
+      r[kl] = bv;
+      if (r32) r32[kl] = (float)bv;
+      x[kl] = 0.0;
+      acc = fma(bv, bv, acc);
+    }
+  }
+  rhs_finish(acc, bad, sc, part, rtol, maxit);
+}
+
+// last step of the right-hand side kernels: ||b||^2 and the PCG scalars
+__device__ void rhs_finish(double acc, bool bad, Scalars* sc, double* part, double rtol,
+                           int maxit) {
   if (bad) sc->nan = 1;
   double tot;
   if (grid_reduce<false>(acc, part, &sc->tickets[T_RHS], &tot) && tid2() == 0) {
@@ -717,6 +750,12 @@ void launch_rhs(const FortranIn& in, const double* ustar, const double* vstar, d
                 double* part, double rtol, int maxit, cudaStream_t s) {
   launch_k(k_rhs, grid_for(in.nx, in.ny, 1), kBlock, 0, s, in, ustar, vstar, vb, L0.pitch, bvec,
            r, r32, x, sc, part, rtol, maxit);
+}
+void launch_rhs_given(int nx, int ny, const double* bF, LevelView L0, double* bvec, double* r,
+                      float* r32, double* x, Scalars* sc, double* part, double rtol, int maxit,
+                      cudaStream_t s) {
+  launch_k(k_rhs_given, grid_for(nx, ny, 1), kBlock, 0, s, nx, ny, bF, L0, bvec, r, r32, x, sc,
+           part, rtol, maxit);
 }
 void launch_update_xr(LevelView L0, double* x, const double* p, double* r, float* r32,
                       const float* z32, const double* q, Scalars* sc, double* part,

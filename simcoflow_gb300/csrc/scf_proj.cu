@@ -13,10 +13,12 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <utility>
 #include <vector>
 
 #include "../../include/scf_proj.h"
 #include "scf_mg.cuh"
+#include "scf_unet.cuh"
 
 using namespace scf;
 
@@ -56,6 +58,9 @@ struct scf_proj {
   std::vector<MgD> t64;
   std::vector<MgF> t32;
   unsigned* aspect_bits = nullptr;  // device: largest cell aspect ratio (float bits)
+  // learned preconditioner (SCF_PRECOND_LEARNED): network and its residual scale
+  UNet* net = nullptr;
+  float* net_sigma = nullptr;
   float* cscale = nullptr;      // device, one BF16 scale per level
   unsigned* maxbits = nullptr;  // device, one per level
   std::vector<void*> allocs;
@@ -489,6 +494,52 @@ int run_pcg(scf_proj* h) {
   return SCF_OK;
 }
 
+// Flexible PCG with the learned preconditioner (mixed handles): z = sigma *
+// U-Net(r) while each iteration reduces ||r|| by at least kLearnedRatio,
+// then the mixed V-cycle for the rest of the solve.  Host-polled (one
+// scalar read per iteration decides the preconditioner of the next).
+constexpr double kLearnedRatio = 0.6;
+
+int run_learned(scf_proj* h, int* nn_iters, int* fell_back) {
+  cudaStream_t s = h->stream;
+  LevelView L0 = h->lev[0];
+  const int zf = final_buf(h, 0);
+  float* z = buf32(h, 0, zf);
+  int rc = read_scalars(h);
+  if (rc) return rc;
+  double rr_prev = h->sc_host->rr;
+  bool use_nn = true;
+  *nn_iters = 0;
+  *fell_back = 0;
+  double* pold = h->pA;
+  double* pnew = h->pB;
+  for (int it = 0; it < h->opts.maxit && !h->sc_host->done; ++it) {
+    if (use_nn) {
+      h->net->features(0, L0.nx, L0.ny, L0.pitch, L0.b, L0.cE, L0.cN, L0.dg, h->net_sigma, s);
+      h->net->forward(s);
+      h->net->correction(L0.nx, L0.ny, L0.pitch, L0.dg, h->net_sigma, z, s);
+      launch_dot_rz_t<float, float>(L0.nx, L0.ny, L0.pitch, h->r32, z, 1, h->sc, h->part, s);
+    } else {
+      enqueue_vcycle(h, h->sc, true, s);
+    }
+    launch_pupdate_spmv_t<float>(L0, z, pold, pnew, h->q, h->sc, h->part, s);
+    launch_update_xr(L0, h->xsol, pnew, L0.b, h->r32, z, h->q, h->sc, h->part, 0ull, s);
+    CK(cudaGetLastError());
+    std::swap(pold, pnew);
+    if ((rc = read_scalars(h))) return rc;
+    const double rr = h->sc_host->rr;
+    if (use_nn) {
+      ++*nn_iters;
+      if (!(rr <= kLearnedRatio * kLearnedRatio * rr_prev)) {
+        use_nn = false;
+        *fell_back = 1;
+      }
+    }
+    rr_prev = rr;
+  }
+  return SCF_OK;
+}
+
 float elapsed(cudaEvent_t a, cudaEvent_t b) {
   float ms = 0.f;
   if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) return 0.f;
@@ -506,10 +557,13 @@ int put(scf_proj* h, T** dst, const T* src, size_t n) {
   return SCF_OK;
 }
 
+bool learned(const scf_proj* h) { return h->opts.precond == SCF_PRECOND_LEARNED; }
+
 int solve_common(scf_proj* h, const double* ustar, const double* vstar, double vb, double* Pp,
                  double* p, double* u, double* v, double* mres, scf_stats* st, bool correct) {
   if (!h) return SCF_ERR_ARG;
   if (!h->assembled) return SCF_ERR_STATE;
+  if (learned(h) && !h->net) return SCF_ERR_STATE;
   if (!ustar || !vstar) return SCF_ERR_ARG;
   if (correct && (!p || !u || !v || !mres)) return SCF_ERR_ARG;
   CK(cudaSetDevice(h->device));
@@ -538,7 +592,8 @@ int solve_common(scf_proj* h, const double* ustar, const double* vstar, double v
   launch_rhs(h->fin, dus, dvs, vb, L0, h->bvec, L0.b, h->r32, h->xsol, h->sc, h->part,
              h->opts.rtol, h->opts.maxit, s);
   CK(cudaGetLastError());
-  int rc = run_pcg(h);
+  int nn_iters = 0, fell_back = 0;
+  int rc = learned(h) ? run_learned(h, &nn_iters, &fell_back) : run_pcg(h);
   if (rc) return rc;
   CK(cudaEventRecord(h->ev[2], s));
   launch_final_solution(h->fin, L0, h->xsol, h->bvec, dus, dvs, dPp, dp, du, dv, correct ? 1 : 0,
@@ -568,7 +623,8 @@ int solve_common(scf_proj* h, const double* ustar, const double* vstar, double v
     st->iters = S.iter;
     st->status = status;
     st->levels = (int)h->lev.size();
-    st->fallbacks = 0;
+    st->fallbacks = fell_back;
+    st->learned_iters = nn_iters;
     st->smoother = h->line ? SCF_SMOOTH_LINE : SCF_SMOOTH_POINT;
     st->bnorm = sqrt(S.bnorm2);
     st->relres = S.bnorm2 > 0 ? sqrt(S.rr / S.bnorm2) : 0.0;
@@ -633,6 +689,8 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
       o.smoother != SCF_SMOOTH_LINE)
     return SCF_ERR_ARG;
   if (o.smoother == SCF_SMOOTH_LINE && (nx > kLineMaxLen || ny > kLineMaxLen)) return SCF_ERR_ARG;
+  if (o.precond != SCF_PRECOND_MG && o.precond != SCF_PRECOND_LEARNED) return SCF_ERR_ARG;
+  if (o.precond == SCF_PRECOND_LEARNED && o.precision != SCF_PREC_MIXED) return SCF_ERR_ARG;
   scf_proj* h = new (std::nothrow) scf_proj();
   if (!h) return SCF_ERR_NOMEM;
   h->nx = nx; h->ny = ny; h->opts = o;
@@ -775,6 +833,7 @@ int scf_proj_destroy(scf_proj* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   destroy_graph(h);
+  delete h->net;
   for (void* p : h->allocs) cudaFree(p);
   if (h->sc_host) cudaFreeHost(h->sc_host);
   for (auto& e : h->ev)
@@ -1000,6 +1059,90 @@ int scf_proj_time_kernel(scf_proj* h, int kernel, int reps, double* ms) {
   if (vexec) cudaGraphExecDestroy(vexec);
   *ms = (double)elapsed(h->ev[5], h->ev[6]) / reps;
   return SCF_OK;
+}
+
+int scf_proj_set_network(scf_proj* h, const float* params, int nparams) {
+  if (!h || !params || nparams != UNet::num_params()) return SCF_ERR_ARG;
+  if (!h->mixed) return SCF_ERR_ARG;
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  if (!h->net) {
+    UNet* u = new (std::nothrow) UNet();
+    if (!u) return SCF_ERR_NOMEM;
+    const int H = (h->ny + 7) / 8 * 8, W = (h->nx + 7) / 8 * 8;
+    if (u->create(1, H, W, false, h->device) != 0) {
+      delete u;
+      return SCF_ERR_NOMEM;
+    }
+    h->net = u;
+    int rc;
+    if (!h->net_sigma && (rc = dev_alloc(h, (void**)&h->net_sigma, sizeof(float)))) return rc;
+  }
+  if (h->net->set_params_host(params) != 0) return SCF_ERR_CUDA;
+  return SCF_OK;
+}
+
+int scf_proj_solve_rhs(scf_proj* h, const double* b, double* x, double* r, int maxit,
+                       scf_stats* st) {
+  if (!h || !b || !x) return SCF_ERR_ARG;
+  if (!h->assembled) return SCF_ERR_STATE;
+  if (maxit < 0 || maxit > h->opts.maxit) return SCF_ERR_ARG;
+  if (learned(h) && !h->net) return SCF_ERR_STATE;
+  CK(cudaSetDevice(h->device));
+  cudaStream_t s = h->stream;
+  const size_t n1 = (size_t)h->nx * h->ny;
+  const double* db = b;
+  double *dx = x, *dr = r;
+  if (!h->devptrs) {  // the (nx+2)(ny+2) velocity staging buffers hold (nx,ny) arrays
+    CK(cudaMemcpyAsync(h->st_us, b, n1 * 8, cudaMemcpyHostToDevice, s));
+    db = h->st_us;
+    dx = h->st_vs;
+    dr = r ? h->st_Pp : nullptr;
+  }
+  CK(cudaEventRecord(h->ev[1], s));
+  LevelView L0 = h->lev[0];
+  CK(cudaMemsetAsync(&h->sc->nan, 0, sizeof(int), s));
+  launch_rhs_given(h->nx, h->ny, db, L0, h->bvec, L0.b, h->r32, h->xsol, h->sc, h->part,
+                   h->opts.rtol, maxit, s);
+  CK(cudaGetLastError());
+  int nn_iters = 0, fell_back = 0, rc = SCF_OK;
+  if (maxit > 0) {
+    const int saved = h->opts.maxit;
+    h->opts.maxit = maxit;  // bound of the host-polled loops
+    rc = learned(h) ? run_learned(h, &nn_iters, &fell_back) : run_pcg(h);
+    h->opts.maxit = saved;
+    if (rc) return rc;
+  }
+  CK(cudaEventRecord(h->ev[2], s));
+  launch_final_solution(h->fin, L0, h->xsol, h->bvec, nullptr, nullptr, nullptr, nullptr,
+                        nullptr, nullptr, 0, h->sc, h->part, s);
+  launch_to_fortran(L0, h->xsol, dx, s);
+  if (dr) launch_to_fortran(L0, L0.b, dr, s);
+  CK(cudaGetLastError());
+  if (!h->devptrs) {
+    CK(cudaMemcpyAsync(x, dx, n1 * 8, cudaMemcpyDeviceToHost, s));
+    if (r) CK(cudaMemcpyAsync(r, dr, n1 * 8, cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaMemcpyAsync(h->sc_host, h->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  const Scalars& S = *h->sc_host;
+  int status = S.status;
+  if (S.nan) status = SCF_ERR_NAN;
+  if (maxit == 0 && S.bnorm2 > 0) status = SCF_ERR_NOT_CONVERGED;
+  if (st) {
+    memset(st, 0, sizeof(*st));
+    st->iters = S.iter;
+    st->status = status;
+    st->levels = (int)h->lev.size();
+    st->fallbacks = fell_back;
+    st->learned_iters = nn_iters;
+    st->smoother = h->line ? SCF_SMOOTH_LINE : SCF_SMOOTH_POINT;
+    st->bnorm = sqrt(S.bnorm2);
+    st->relres = S.bnorm2 > 0 ? sqrt(S.rr / S.bnorm2) : 0.0;
+    st->relres_true = S.bnorm2 > 0 ? sqrt(S.res_true2 / S.bnorm2) : 0.0;
+    st->ms_solve = elapsed(h->ev[1], h->ev[2]);
+  }
+  return status == kOk ? SCF_OK : status;
 }
 
 int scf_proj_vcycle(scf_proj* h, const double* b, double* x) {

@@ -1,0 +1,67 @@
+// scf_unet.cuh -- the U-Net of include/scf_unet.h as a C++ object, used by the
+// C-ABI (training, tests) and by the projection solver (inference inside the
+// flexible PCG).
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <vector>
+
+namespace scf {
+
+struct UNetLayer {
+  int cin, cout;  // channels in / out
+  int level;      // resolution level of the output (0 = full)
+  bool ups;       // input read at half resolution (nearest upsampling)
+  bool relu;      // ReLU on the output
+  int skip;       // layer whose output is added to this one's (-1: none)
+  size_t woff, boff;  // offsets of W ([cout][9][cin]) and bias in the parameters
+};
+
+class UNet {
+ public:
+  // batch n of h x w images (multiples of 8); train: also the backward buffers
+  int create(int n, int h, int w, bool train, int device);
+  void destroy();
+  ~UNet() { destroy(); }
+
+  static int num_params();
+  static const std::vector<UNetLayer>& layers();
+
+  // parameters: host FP32 array in the order of include/scf_unet.h
+  int set_params_host(const float* p);
+  int get_params_host(float* p);
+
+  // input features of image i from FP64 device arrays with cell (x, y) at
+  // y * ld + x; sigma_out (device float) gets the residual scale
+  void features(int i, int nx, int ny, int ld, const double* r, const double* cE,
+                const double* cN, const double* dg, float* sigma_out, cudaStream_t s);
+  void forward(cudaStream_t s);  // leaves z (n*h*w FP32) in z_
+  // FP32 correction on a padded level layout: x[g] = sigma * z on cells with dg > 0
+  void correction(int nx, int ny, int pitch, const double* dg, const float* sigma, float* x,
+                  cudaStream_t s);
+  // training target of image i: t = e / sigma, mask = dg > 0 (Fortran (nx,ny) arrays)
+  void target(int i, int nx, int ny, const double* e, const double* dg, const float* sigma,
+              float* t, unsigned char* mask, cudaStream_t s);
+  void loss(const float* t, const unsigned char* mask, float* loss_dev, cudaStream_t s);
+  void backward(cudaStream_t s);
+  void adam(float lr, float b1, float b2, float eps, int step, cudaStream_t s);
+  void refresh_weights(cudaStream_t s);  // BF16 copies after a parameter change
+
+  int n_ = 0, h_ = 0, w_ = 0;
+  bool train_ = false;
+  int sms_ = 152;
+  float *params_ = nullptr, *grads_ = nullptr, *m_ = nullptr, *v_ = nullptr;
+  __nv_bfloat16 *wb_ = nullptr, *wt_ = nullptr;  // BF16 weights and flipped transposes
+  float *z_ = nullptr, *dz_ = nullptr, *red_ = nullptr;
+  __nv_bfloat16* in_ = nullptr;            // input features [n][h][w][16]
+  std::vector<__nv_bfloat16*> act_;        // layer outputs
+  std::vector<__nv_bfloat16*> pool_;       // pooled inputs of e1a, e2a, e3a
+  std::vector<__nv_bfloat16*> g_;          // scratch gradient buffers
+  std::vector<void*> allocs_;
+
+ private:
+  int alloc(void** p, size_t bytes);
+};
+
+}  // namespace scf

@@ -29,6 +29,7 @@ _LIB = Path(__file__).resolve().parent / "_lib" / "libscf_proj.so"
 _lib = None
 
 SCF_OK = 0
+SCF_ERR_NOT_CONVERGED = -4
 ERRORS = {-1: "SCF_ERR_ARG", -2: "SCF_ERR_CUDA", -3: "SCF_ERR_NAN", -4: "SCF_ERR_NOT_CONVERGED",
           -5: "SCF_ERR_STALL", -6: "SCF_ERR_TIMEOUT", -7: "SCF_ERR_STATE", -8: "SCF_ERR_NOMEM"}
 PREC = {"fp64": 0, "mixed": 1}
@@ -39,14 +40,21 @@ FLAG_NO_GRAPH = 2
 EXPORTS = ["scf_opts_default", "scf_proj_create", "scf_proj_destroy", "scf_proj_set_stream",
            "scf_proj_set_grid", "scf_proj_set_geometry", "scf_proj_assemble",
            "scf_proj_poisson_solve", "scf_proj_update_puv", "scf_proj_get_operator",
-           "scf_proj_vcycle", "scf_proj_time_kernel", "scf_rhs_norm_noalloc", "scf_strerror"]
+           "scf_proj_vcycle", "scf_proj_time_kernel", "scf_rhs_norm_noalloc", "scf_strerror",
+           "scf_proj_set_network", "scf_proj_solve_rhs"]
+# every symbol declared in include/scf_unet.h
+UNET_EXPORTS = ["scf_unet_num_params", "scf_unet_create", "scf_unet_destroy",
+                "scf_unet_set_stream", "scf_unet_set_params", "scf_unet_get_params",
+                "scf_unet_features", "scf_unet_target", "scf_unet_set_input", "scf_unet_forward",
+                "scf_unet_loss", "scf_unet_set_dz", "scf_unet_backward", "scf_unet_get_grads",
+                "scf_unet_adam"]
 
 
 class Opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("flags", C.c_int), ("device", C.c_int),
                 ("maxit", C.c_int), ("rtol", C.c_double), ("npre", C.c_int),
                 ("npost", C.c_int), ("omega", C.c_double), ("coarse_max", C.c_int),
-                ("smoother", C.c_int), ("reserved", C.c_int * 7)]
+                ("smoother", C.c_int), ("precond", C.c_int), ("reserved", C.c_int * 6)]
 
 
 class Stats(C.Structure):
@@ -55,7 +63,7 @@ class Stats(C.Structure):
                 ("relres_true", C.c_double), ("mres_max", C.c_double), ("ms_h2d", C.c_double),
                 ("ms_assemble", C.c_double), ("ms_solve", C.c_double),
                 ("ms_correct", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double),
-                ("smoother", C.c_int)]
+                ("smoother", C.c_int), ("learned_iters", C.c_int)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -97,6 +105,8 @@ def load():
         L.scf_rhs_norm_noalloc.argtypes = [C.c_int, C.c_int] + [dp] * 10 + [ip, C.c_double, dp,
                                                                             dp, vp]
         L.scf_rhs_norm_noalloc.restype = C.c_int
+        L.scf_proj_set_network.argtypes = [vp, vp, C.c_int]
+        L.scf_proj_solve_rhs.argtypes = [vp, dp, dp, dp, C.c_int, C.POINTER(Stats)]
         for name in EXPORTS:
             f = getattr(L, name)
             if f.restype is C.c_int or name.startswith("scf_proj"):
@@ -112,6 +122,8 @@ def _check(rc: int, where: str):
 
 # multigrid smoother (scf_opts.smoother / scf_stats.smoother)
 SMOOTHERS = {"auto": 0, "point": 1, "line": 2}
+# preconditioner (scf_opts.precond)
+PRECONDS = {"mg": 0, "learned": 1}
 
 GEOMETRY_ARGS = ("vof", "phi", "vofS", "nyS", "WlLh", "aE", "aW", "aN", "aS", "posnu_p",
                  "posnu_u", "moex_u", "vofS_u", "posnu_v", "moex_v", "vofS_v")
@@ -123,7 +135,7 @@ class ProjectionSolver:
     def __init__(self, nx: int, ny: int, precision: str = "fp64", device: int = 0,
                  device_ptrs: bool = False, use_graph: bool = True, maxit: int = 200,
                  rtol: float = 1e-8, npre: int = 2, npost: int = 2, omega: float = 1.9,
-                 coarse_max: int = 16, smoother: str = "auto"):
+                 coarse_max: int = 16, smoother: str = "auto", precond: str = "mg"):
         L = load()
         o = Opts()
         L.scf_opts_default(C.byref(o))
@@ -132,6 +144,7 @@ class ProjectionSolver:
         o.device, o.maxit, o.rtol = device, maxit, rtol
         o.npre, o.npost, o.omega, o.coarse_max = npre, npost, omega, coarse_max
         o.smoother = SMOOTHERS[smoother]
+        o.precond = PRECONDS[precond]
         self.nx, self.ny, self.device_ptrs = nx, ny, device_ptrs
         self.opts = o
         h = C.c_void_p()
@@ -246,6 +259,35 @@ class ProjectionSolver:
         _check(load().scf_proj_get_operator(self._h, *[a.ctypes.data for a in out]),
                "scf_proj_get_operator")
         return dict(zip(("cE", "cN", "diag", "rhs"), out))
+
+    def set_network(self, params):
+        """Weights of the learned preconditioner (float32 array of
+        scf_unet_num_params() values, order of include/scf_unet.h)."""
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        _check(load().scf_proj_set_network(self._h, p.ctypes.data, p.size), "scf_proj_set_network")
+
+    def solve_rhs(self, b, x=None, r=None, maxit=None, check=True):
+        """A x = b for an (nx,ny) right-hand side; returns (x, r, stats).  With
+        device_ptrs, b/x/r are CUDA float64 tensors of nx*ny elements (x and r
+        allocated when not given); else Fortran-ordered numpy arrays."""
+        maxit = self.opts.maxit if maxit is None else maxit
+        if self.device_ptrs:
+            import torch
+            if x is None:
+                x = torch.zeros(self.nx * self.ny, dtype=torch.float64, device=b.device)
+            if r is None:
+                r = torch.zeros(self.nx * self.ny, dtype=torch.float64, device=b.device)
+        else:
+            b = np.asfortranarray(b, dtype=np.float64)
+            x = np.zeros(self._n1(), order="F") if x is None else x
+            r = np.zeros(self._n1(), order="F") if r is None else r
+        st = Stats()
+        f = lambda a, n, w=False: self._ptr(a, self._n1(), np.float64, n, w)
+        rc = load().scf_proj_solve_rhs(self._h, f(b, "b"), f(x, "x", True), f(r, "r", True),
+                                       maxit, C.byref(st))
+        if check and rc != SCF_ERR_NOT_CONVERGED:
+            _check(rc, "scf_proj_solve_rhs")
+        return x, r, st
 
     def vcycle(self, b):
         x = np.zeros(self._n1(), order="F")

@@ -24,6 +24,15 @@ def test_proj_library_exports_header_symbols(built):
     assert sorted(projection.EXPORTS) == sorted(n for n in names)
 
 
+def test_proj_library_exports_unet_header_symbols(built):
+    from simcoflow_gb300 import build, projection
+    lib = ctypes.CDLL(str(build.build_proj()))
+    names = _declared("scf_unet.h")
+    for n in names:
+        assert hasattr(lib, n), n
+    assert sorted(projection.UNET_EXPORTS) == names
+
+
 def test_geom_library_exports_header_symbols(built):
     from simcoflow_gb300 import build
     lib = ctypes.CDLL(str(build.build_geom()))
