@@ -123,6 +123,27 @@ int scf_proj_set_network(struct scf_proj *h, const float *params, int nparams);
 int scf_proj_solve_rhs(struct scf_proj *h, const double *b, double *x, double *r, int maxit,
                        struct scf_stats *st);
 
+/* Change the V-cycle schedule of an existing handle (sweeps before / after
+ * the coarse correction, correction scale); rebuilds its graph.  Used by the
+ * autotuner. */
+int scf_proj_set_opts(struct scf_proj *h, int npre, int npost, double omega);
+
+/* Batched projections: many independent, assembled handles (device-pointer
+ * mode, one device, MG preconditioner, graphs on) solved by ONE graph
+ * launch.  Each instance is an independent branch of the graph: operator
+ * setup, right-hand side, the PCG loop as a conditional WHILE node, the
+ * correction (as scf_proj_update_puv) and its scalars.  The arrays given to
+ * scf_batch_set_io are baked into the graph; setting them again rebuilds it.
+ * stats: one entry per instance; ms_total is the whole batch.  Returns the
+ * first non-OK instance status.  The reference has no batched path: it
+ * solves one projection per HYPRE call (src/ProjectionP_Mod.f90:21-99). */
+typedef struct scf_batch scf_batch;
+int scf_batch_create(scf_batch **b, struct scf_proj *const *handles, int count);
+int scf_batch_set_io(scf_batch *b, int i, const double *ustar, const double *vstar, double vb,
+                     double *Pp, double *p, double *u, double *v, double *mres);
+int scf_batch_run(scf_batch *b, void *stream, struct scf_stats *stats);
+int scf_batch_destroy(scf_batch *b);
+
 /* Fill opts with defaults: FP64, host pointers, device 0, maxit 200,
  * rtol 1e-8, 2 pre / 2 post sweeps, omega 1.9, coarse_max 16. */
 void scf_opts_default(scf_opts *opts);

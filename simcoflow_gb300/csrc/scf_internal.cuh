@@ -83,6 +83,21 @@ __device__ __forceinline__ void pdl_wait() {
 // PDL is on unless SCF_NO_PDL is set in the environment.
 bool pdl_enabled();
 
+// Allow a kernel the device's whole opt-in dynamic shared memory.  The
+// attribute belongs to the function, not to a launch: graphs of several
+// handles capture launches of the same kernel with different sizes, so it
+// must only ever be raised, never set to one handle's size.
+template <typename F>
+inline cudaError_t allow_max_smem(F* kernel) {
+  int dev = 0, optin = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(reinterpret_cast<const void*>(kernel),
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  return e;
+}
+
 template <typename... KArgs, typename... Args>
 inline void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
                      cudaStream_t s, Args... args) {

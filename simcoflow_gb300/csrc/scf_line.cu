@@ -508,8 +508,7 @@ int line_tail_prepare(TailDesc<T, CT>& d) {
       cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
       bytes > (size_t)optin)
     return -1;
-  if (cudaFuncSetAttribute(k_line_tail<T, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           d.smem) != cudaSuccess) {
+  if (allow_max_smem(k_line_tail<T, CT>) != cudaSuccess) {
     (void)cudaGetLastError();
     return -1;
   }
@@ -549,11 +548,11 @@ void launch_line(const MgView<T, CT, T>& L, int colour, bool zero, const Scalars
   do {                                                                                         \
     if (zero) {                                                                                \
       auto k = k_line<T, CT, MM, true>;                                                        \
-      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);         \
+      allow_max_smem(k);                                                                       \
       launch_k(k, g, dim3(th), smem, s, L, colour, sc);                                        \
     } else {                                                                                   \
       auto k = k_line<T, CT, MM, false>;                                                       \
-      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);         \
+      allow_max_smem(k);                                                                       \
       launch_k(k, g, dim3(th), smem, s, L, colour, sc);                                        \
     }                                                                                          \
   } while (0)

@@ -554,8 +554,7 @@ int tail_prepare(TailDesc<T, CT>& d) {
       cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
       bytes > (size_t)optin)
     return -1;
-  if (cudaFuncSetAttribute(k_tail<T, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           d.smem) != cudaSuccess) {
+  if (allow_max_smem(k_tail<T, CT>) != cudaSuccess) {
     (void)cudaGetLastError();
     return -1;
   }

@@ -462,6 +462,86 @@ int build_graph(scf_proj* h) {
   return SCF_OK;
 }
 
+// Add one instance's whole projection to the batch graph g as an independent
+// branch: scalars reset, operator setup, right-hand side, the PCG loop as a
+// conditional WHILE node (body: two iterations, as in build_graph), the
+// correction and the copy of the scalars to pinned host memory.
+struct BatchIO {
+  const double *ustar = nullptr, *vstar = nullptr;
+  double vb = 0.0;
+  double *Pp = nullptr, *p = nullptr, *u = nullptr, *v = nullptr, *mres = nullptr;
+  bool set = false;
+};
+
+int add_batch_branch(scf_proj* h, const BatchIO& io, cudaGraph_t g, cudaStream_t cs,
+                     cudaStream_t cs2) {
+  if (cudaStreamBeginCaptureToGraph(cs, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) !=
+      cudaSuccess)
+    return SCF_ERR_CUDA;
+  int rc = SCF_OK;
+  do {
+    cudaMemsetAsync(h->sc, 0, sizeof(Scalars), cs);
+    enqueue_setup(h, h->sc, cs);
+    LevelView L0 = h->lev[0];
+    launch_rhs(h->fin, io.ustar, io.vstar, io.vb, L0, h->bvec, L0.b, h->r32, h->xsol, h->sc,
+               h->part, h->opts.rtol, h->opts.maxit, cs);
+    // the conditional node, added by hand at the capture's current position
+    cudaStreamCaptureStatus cst;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    cudaGraph_t cg = nullptr;
+    if (cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg, &deps, nullptr, &ndeps) != cudaSuccess ||
+        cst != cudaStreamCaptureStatusActive) {
+      rc = SCF_ERR_CUDA;
+      break;
+    }
+    cudaGraphConditionalHandle handle;
+    if (cudaGraphConditionalHandleCreate(&handle, cg, 1, cudaGraphCondAssignDefault) !=
+        cudaSuccess) {
+      rc = SCF_ERR_CUDA;
+      break;
+    }
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = handle;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (cudaGraphAddNode(&node, cg, deps, nullptr, ndeps, &np) != cudaSuccess) {
+      rc = SCF_ERR_CUDA;
+      break;
+    }
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    if (cudaStreamBeginCaptureToGraph(cs2, body, nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+      rc = SCF_ERR_CUDA;
+      break;
+    }
+    enqueue_body(h, (unsigned long long)handle, cs2);
+    cudaGraph_t captured = nullptr;
+    if (cudaStreamEndCapture(cs2, &captured) != cudaSuccess) {
+      rc = SCF_ERR_CUDA;
+      break;
+    }
+    if (cudaStreamUpdateCaptureDependencies(cs, &node, nullptr, 1,
+                                            cudaStreamSetCaptureDependencies) !=
+        cudaSuccess) {
+      rc = SCF_ERR_CUDA;
+      break;
+    }
+    launch_final_solution(h->fin, L0, h->xsol, h->bvec, io.ustar, io.vstar, io.Pp, io.p, io.u,
+                          io.v, 1, h->sc, h->part, cs);
+    launch_final_mres(h->fin, io.vb, io.u, io.v, io.mres, h->sc, h->part, cs);
+    launch_final_zero(h->fin, io.p, io.u, io.v, cs);
+    cudaMemcpyAsync(h->sc_host, h->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, cs);
+  } while (0);
+  cudaGraph_t out = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(cs, &out);
+  if (rc == SCF_OK && e != cudaSuccess) rc = SCF_ERR_CUDA;
+  if (rc != SCF_OK) cudaGetLastError();
+  return rc;
+}
+
 int read_scalars(scf_proj* h) {
   CK(cudaMemcpyAsync(h->sc_host, h->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
@@ -1058,6 +1138,141 @@ int scf_proj_time_kernel(scf_proj* h, int kernel, int reps, double* ms) {
   CK(cudaStreamSynchronize(s));
   if (vexec) cudaGraphExecDestroy(vexec);
   *ms = (double)elapsed(h->ev[5], h->ev[6]) / reps;
+  return SCF_OK;
+}
+
+struct scf_batch {
+  std::vector<scf_proj*> h;
+  std::vector<BatchIO> io;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  float last_ms = 0.0f;
+};
+
+int scf_batch_create(scf_batch** out, scf_proj* const* handles, int count) {
+  if (!out || !handles || count < 1) return SCF_ERR_ARG;
+  *out = nullptr;
+  for (int i = 0; i < count; ++i) {
+    scf_proj* h = handles[i];
+    if (!h || !h->devptrs || h->device != handles[0]->device || learned(h) ||
+        (h->opts.flags & SCF_FLAG_NO_GRAPH))
+      return SCF_ERR_ARG;
+    if (!h->assembled) return SCF_ERR_STATE;
+    for (int j = 0; j < i; ++j)
+      if (handles[j] == h) return SCF_ERR_ARG;
+  }
+  scf_batch* b = new (std::nothrow) scf_batch();
+  if (!b) return SCF_ERR_NOMEM;
+  b->h.assign(handles, handles + count);
+  b->io.resize(count);
+  CK(cudaSetDevice(handles[0]->device));
+  if (cudaEventCreate(&b->ev[0]) != cudaSuccess || cudaEventCreate(&b->ev[1]) != cudaSuccess) {
+    delete b;
+    return SCF_ERR_CUDA;
+  }
+  *out = b;
+  return SCF_OK;
+}
+
+int scf_batch_destroy(scf_batch* b) {
+  if (!b) return SCF_OK;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  for (auto e : b->ev)
+    if (e) cudaEventDestroy(e);
+  delete b;
+  return SCF_OK;
+}
+
+int scf_batch_set_io(scf_batch* b, int i, const double* ustar, const double* vstar, double vb,
+                     double* Pp, double* p, double* u, double* v, double* mres) {
+  if (!b || i < 0 || i >= (int)b->h.size() || !ustar || !vstar || !Pp || !p || !u || !v || !mres)
+    return SCF_ERR_ARG;
+  BatchIO& io = b->io[i];
+  io.ustar = ustar; io.vstar = vstar; io.vb = vb;
+  io.Pp = Pp; io.p = p; io.u = u; io.v = v; io.mres = mres;
+  io.set = true;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+  return SCF_OK;
+}
+
+int scf_batch_run(scf_batch* b, void* stream, scf_stats* stats) {
+  if (!b) return SCF_ERR_ARG;
+  for (const BatchIO& io : b->io)
+    if (!io.set) return SCF_ERR_STATE;
+  for (scf_proj* h : b->h)
+    if (!h->assembled) return SCF_ERR_STATE;
+  CK(cudaSetDevice(b->h[0]->device));
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!b->exec) {
+    CK(cudaDeviceSynchronize());
+    cudaGraph_t g = nullptr;
+    CK(cudaGraphCreate(&g, 0));
+    cudaStream_t cs = nullptr, cs2 = nullptr;
+    CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&cs2, cudaStreamNonBlocking));
+    int rc = SCF_OK;
+    for (size_t i = 0; i < b->h.size() && rc == SCF_OK; ++i)
+      rc = add_batch_branch(b->h[i], b->io[i], g, cs, cs2);
+    cudaStreamDestroy(cs);
+    cudaStreamDestroy(cs2);
+    if (rc == SCF_OK && cudaGraphInstantiate(&b->exec, g, 0) != cudaSuccess) rc = SCF_ERR_CUDA;
+    if (rc != SCF_OK) {
+      cudaGetLastError();
+      cudaGraphDestroy(g);
+      b->exec = nullptr;
+      return rc;
+    }
+    b->graph = g;
+  }
+  CK(cudaEventRecord(b->ev[0], s));
+  CK(cudaGraphLaunch(b->exec, s));
+  CK(cudaEventRecord(b->ev[1], s));
+  CK(cudaStreamSynchronize(s));
+  b->last_ms = elapsed(b->ev[0], b->ev[1]);
+  int worst = SCF_OK;
+  for (size_t i = 0; i < b->h.size(); ++i) {
+    const Scalars& S = *b->h[i]->sc_host;
+    int status = S.nan ? SCF_ERR_NAN : S.status;
+    if (status != kOk && worst == SCF_OK) worst = status;
+    if (stats) {
+      scf_stats& st = stats[i];
+      memset(&st, 0, sizeof(st));
+      st.iters = S.iter;
+      st.status = status;
+      st.levels = (int)b->h[i]->lev.size();
+      st.smoother = b->h[i]->line ? SCF_SMOOTH_LINE : SCF_SMOOTH_POINT;
+      st.bnorm = sqrt(S.bnorm2);
+      st.relres = S.bnorm2 > 0 ? sqrt(S.rr / S.bnorm2) : 0.0;
+      st.relres_true = S.bnorm2 > 0 ? sqrt(S.res_true2 / S.bnorm2) : 0.0;
+      st.mres_max = S.mres_max;
+      st.ms_total = b->last_ms;
+    }
+  }
+  return worst;
+}
+
+int scf_proj_set_opts(scf_proj* h, int npre, int npost, double omega) {
+  if (!h || npre < 1 || npost < 1 || npre > 8 || npost > 8 || !(omega > 0.0 && omega < 2.0))
+    return SCF_ERR_ARG;
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  h->opts.npre = npre;
+  h->opts.npost = npost;
+  h->opts.omega = omega;
+  // the tails carry their own copy of the schedule
+  h->tail64.npre = h->tail32.npre = h->ltail64.npre = h->ltail32.npre = npre;
+  h->tail64.npost = h->tail32.npost = h->ltail64.npost = h->ltail32.npost = npost;
+  h->tail64.omega = omega;
+  h->tail32.omega = (float)omega;
+  h->ltail64.omega = omega;
+  h->ltail32.omega = (float)omega;
+  destroy_graph(h);
+  if (h->assembled && !(h->opts.flags & SCF_FLAG_NO_GRAPH)) return build_graph(h);
   return SCF_OK;
 }
 

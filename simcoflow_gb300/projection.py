@@ -41,7 +41,8 @@ EXPORTS = ["scf_opts_default", "scf_proj_create", "scf_proj_destroy", "scf_proj_
            "scf_proj_set_grid", "scf_proj_set_geometry", "scf_proj_assemble",
            "scf_proj_poisson_solve", "scf_proj_update_puv", "scf_proj_get_operator",
            "scf_proj_vcycle", "scf_proj_time_kernel", "scf_rhs_norm_noalloc", "scf_strerror",
-           "scf_proj_set_network", "scf_proj_solve_rhs"]
+           "scf_proj_set_network", "scf_proj_solve_rhs", "scf_proj_set_opts",
+           "scf_batch_create", "scf_batch_set_io", "scf_batch_run", "scf_batch_destroy"]
 # every symbol declared in include/scf_unet.h
 UNET_EXPORTS = ["scf_unet_num_params", "scf_unet_create", "scf_unet_destroy",
                 "scf_unet_set_stream", "scf_unet_set_params", "scf_unet_get_params",
@@ -107,6 +108,11 @@ def load():
         L.scf_rhs_norm_noalloc.restype = C.c_int
         L.scf_proj_set_network.argtypes = [vp, vp, C.c_int]
         L.scf_proj_solve_rhs.argtypes = [vp, dp, dp, dp, C.c_int, C.POINTER(Stats)]
+        L.scf_proj_set_opts.argtypes = [vp, C.c_int, C.c_int, C.c_double]
+        L.scf_batch_create.argtypes = [C.POINTER(vp), C.POINTER(vp), C.c_int]
+        L.scf_batch_set_io.argtypes = [vp, C.c_int, dp, dp, C.c_double, dp, dp, dp, dp, dp]
+        L.scf_batch_run.argtypes = [vp, vp, C.POINTER(Stats)]
+        L.scf_batch_destroy.argtypes = [vp]
         for name in EXPORTS:
             f = getattr(L, name)
             if f.restype is C.c_int or name.startswith("scf_proj"):
@@ -259,6 +265,11 @@ class ProjectionSolver:
         _check(load().scf_proj_get_operator(self._h, *[a.ctypes.data for a in out]),
                "scf_proj_get_operator")
         return dict(zip(("cE", "cN", "diag", "rhs"), out))
+
+    def set_schedule(self, npre: int, npost: int, omega: float):
+        """V-cycle schedule of this handle (rebuilds its graph)."""
+        _check(load().scf_proj_set_opts(self._h, npre, npost, omega), "scf_proj_set_opts")
+        self.opts.npre, self.opts.npost, self.opts.omega = npre, npost, omega
 
     def set_network(self, params):
         """Weights of the learned preconditioner (float32 array of
