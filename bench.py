@@ -148,9 +148,10 @@ def kernels_per_iteration(levels: int, npre: int, npost: int) -> int:
     return (levels - 1) * (npre + npost) + 1 + 2
 
 
-def cpu_projection_ms(case, threads: int) -> tuple[float, dict]:
+def cpu_projection_ms(case, threads: int, rtol: float = 1e-8):
     """One projection through the oracle's C restatement (assembly, RHS,
-    FP64 MG-PCG to 1e-8, correction) on `threads` host threads."""
+    FP64 MG-PCG to rtol, correction) on `threads` host threads.  Returns
+    (ms, info, solution)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as O
     O.lib().oracle_set_threads(threads)
@@ -158,13 +159,121 @@ def cpu_projection_ms(case, threads: int) -> tuple[float, dict]:
     pc = O.pocoef(case)
     matr, A = O.matrix(case, pc)
     rhm, b = O.rhs(case)
-    xi, it, rel, nlev = O.mgpcg(case, matr, rhm, rtol=1e-8, maxit=500, npre=2, npost=2,
+    xi, it, rel, nlev = O.mgpcg(case, matr, rhm, rtol=rtol, maxit=500, npre=2, npost=2,
                                 omega=1.9, threads=threads)
     x = O.x_from_interior(case, xi)
     Pp = O.scatter(case, x)
-    O.correct(case, Pp)
+    u, v, p, mres = O.correct(case, Pp)
     ms = (time.perf_counter() - t0) * 1e3
-    return ms, {"iters": it, "relres": rel, "levels": nlev}
+    return ms, {"iters": it, "relres": rel, "levels": nlev}, {"Pp": Pp, "u": u, "v": v}
+
+
+def _rel(a, b):
+    d = np.linalg.norm(np.asarray(a) - np.asarray(b))
+    n = np.linalg.norm(np.asarray(b))
+    return float(d / n) if n > 0 else float(d)
+
+
+def extra_learned(case, tdev, dev, local, args):
+    """The headline case with the learned preconditioner (shipped weights)."""
+    import torch
+    from simcoflow_gb300 import learned as Lr, projection as P
+    params, meta = Lr.load_weights()
+    nx, ny = case.nx, case.ny
+    s = P.ProjectionSolver(nx, ny, precision="mixed", precond="learned", device=local,
+                           device_ptrs=True, rtol=1e-8, maxit=200)
+    try:
+        s.set_network(params)
+        s.set_grid(tdev["dx"], tdev["dy"], tdev["dxU"], tdev["dyV"])
+        s.set_geometry(**{k: tdev[k] for k in P.GEOMETRY_ARGS})
+        u, v, p = tdev["u0"].clone(), tdev["v0"].clone(), tdev["p0"].clone()
+        Pp = torch.zeros_like(tdev["p0"])
+        m = torch.zeros(nx * ny, dtype=torch.float64, device=dev)
+
+        def step():
+            s.assemble(tdev["DpU"], tdev["DpV"], case.betaP, case.betaM, case.bc)
+            return s.update_puv(tdev["ustar"], tdev["vstar"], u, v, p, case.vb, Pp=Pp, mres=m)[2]
+
+        step()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        reps = max(1, min(args.steps, 3))
+        for _ in range(reps):
+            st = step()
+        torch.cuda.synchronize(dev)
+        ms = (time.perf_counter() - t0) / reps * 1e3
+        return {"ms": round(ms, 3), "iters": st.iters, "learned_iters": st.learned_iters,
+                "fallback_to_vcycle": bool(st.fallbacks), "relres_true": st.relres_true,
+                "training": {k: meta.get(k) for k in ("instances", "iters", "size", "steps",
+                                                      "batch", "loss_first", "loss_last")}}
+    finally:
+        s.close()
+
+
+def extra_stretched(local, args):
+    """The 4096^2 y-stretched configuration (line smoother), mixed and plain FP64."""
+    import torch
+    from simcoflow_gb300 import synth, projection as P
+    case = synth.c3()
+    dev = torch.device("cuda", local)
+    t = {k: torch.from_numpy(np.ascontiguousarray(v.ravel(order="F"))).to(dev)
+         for k, v in case.arrays.items() if isinstance(v, np.ndarray)}
+    out = {"workload": WORKLOADS["c3"], "nx": case.nx, "ny": case.ny}
+    for prec in ("mixed", "fp64"):
+        s = P.ProjectionSolver(case.nx, case.ny, precision=prec, device=local, device_ptrs=True,
+                               rtol=1e-8, maxit=300)
+        try:
+            s.set_grid(t["dx"], t["dy"], t["dxU"], t["dyV"])
+            s.set_geometry(**{k: t[k] for k in P.GEOMETRY_ARGS})
+            u, v, p = t["u0"].clone(), t["v0"].clone(), t["p0"].clone()
+            Pp = torch.zeros_like(t["p0"])
+            m = torch.zeros(case.nx * case.ny, dtype=torch.float64, device=dev)
+
+            def step():
+                s.assemble(t["DpU"], t["DpV"], case.betaP, case.betaM, case.bc)
+                return s.update_puv(t["ustar"], t["vstar"], u, v, p, case.vb, Pp=Pp,
+                                    mres=m)[2]
+
+            step()
+            torch.cuda.synchronize(dev)
+            e0, e1 = torch.cuda.Event(True), torch.cuda.Event(True)
+            e0.record()
+            reps = 2
+            for _ in range(reps):
+                st = step()
+            e1.record()
+            torch.cuda.synchronize(dev)
+            out[prec] = {"ms": round(e0.elapsed_time(e1) / reps, 3), "iters": st.iters,
+                         "relres_true": st.relres_true,
+                         "smoother": {1: "point", 2: "line"}.get(st.smoother)}
+        finally:
+            s.close()
+    out["speedup_mixed_vs_plain"] = round(out["fp64"]["ms"] / out["mixed"]["ms"], 3)
+    return out
+
+
+def extra_batch(local):
+    """64 uneven instances in one graph launch with autotuned schedules."""
+    from simcoflow_gb300 import synth, batch as Bt
+    cases = [synth.c5(instance=i) for i in range(64)]
+    bp = Bt.BatchProjector(cases, precision="mixed", rtol=1e-8, maxit=300, device=local)
+    try:
+        bp.run()
+        times = []
+        for _ in range(3):
+            st, ms = bp.run()
+            times.append(ms)
+        ms = min(times)
+        return {"workload": "64 instances, sides 256..1024 (log-uniform, multiples of 32), "
+                            "density ratio log-U[10,1000], 0-4 circles, 16-mode u*, dt 1e-3",
+                "cells": int(sum(c.nx * c.ny for c in cases)), "ms_per_batch": round(ms, 3),
+                "solves_per_s": round(64 / (ms * 1e-3), 1),
+                "iters_min_max": [min(x["iters"] for x in st), max(x["iters"] for x in st)],
+                "max_relres_true": max(x["relres_true"] for x in st),
+                "launch": "one CUDA graph (64 branches, conditional-while PCG per branch)",
+                "autotune": json.loads(bp.table_json())}
+    finally:
+        bp.close()
 
 
 def run_reference(args):
@@ -177,7 +286,7 @@ def run_reference(args):
         cpu_projection_ms(case, threads)
     times, info = [], {}
     for _ in range(args.steps):
-        ms, info = cpu_projection_ms(case, threads)
+        ms, info, _ = cpu_projection_ms(case, threads)
         times.append(ms)
     ms = float(np.mean(times))
     line = {"impl": "reference", "metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": world,
@@ -362,12 +471,29 @@ def run_ours(args):
             launches += arm["levels"] + 3 + 1 + 3 + 2 * arm["levels"]  # setup, rhs, final
             launches += ((it + 1) // 2) * 2 * per_it
     cpu = None
+    err = None
     if world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        ms_cpu, info = cpu_projection_ms(case, threads)
+        ms_cpu, info, _ = cpu_projection_ms(case, threads)
         cpu = {"value": round(ms_cpu, 2), "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"one full {nx}x{ny} projection (C restatement of the reference path, "
                          f"OpenMP, {info['iters']} MG-PCG iterations)"}
+        # error statement of the headline result against the FP64 oracle driven
+        # to its floor (checker only; not timed)
+        _, info13, ref = cpu_projection_ms(case, threads, rtol=1e-13)
+        err = {"p_rel_l2": _rel(hPp, ref["Pp"]),
+               "uv_rel_l2": _rel(np.concatenate([hu.ravel(), hv.ravel()]),
+                                 np.concatenate([ref["u"].ravel(), ref["v"].ravel()])),
+               "oracle": f"C restatement, FP64 MG-PCG to relres {info13['relres']:.1e}"}
+    extras = {}
+    if world == 1 and not args.no_extras:
+        for name, fn in (("learned", lambda: extra_learned(case, tdev, dev, local, args)),
+                         ("stretched_4096", lambda: extra_stretched(local, args)),
+                         ("batch_64", lambda: extra_batch(local))):
+            try:
+                extras[name] = fn()
+            except Exception as e:  # an extra must not hide the headline line
+                extras[name] = {"error": f"{type(e).__name__}: {e}"}
     ms_step = mixed["ms"]
     line = {
         "metric": METRIC, "value": round(ms_step, 4), "unit": UNIT, "n_gpus": world,
@@ -391,6 +517,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(d2h)},
         "roofline": roof, "kernels": kernel_table(mixed, "mixed"),
         "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": mixed["clk"],
+        "err_vs_fp64_oracle": err, **extras,
     }
     print(json.dumps(line), flush=True)
     if pg:
@@ -406,6 +533,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="c2")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the learned, 4096^2 stretched and 64-instance batch lines")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch the same kernels one by one instead of through the CUDA graph "
                          "(profilers cannot see kernel nodes of graphs with conditional nodes)")
