@@ -96,13 +96,16 @@ __device__ __forceinline__ void set_beta(Scalars* sc, double rz_new, int flexibl
   sc->rz = rz_new;
 }
 
-template <class T, class CT, class BT, int FIRST, bool ZERO, bool PROLONG, bool RESTRICT, bool RZ>
+template <class T, class CT, class BT, int FIRST, bool ZERO, bool PROLONG, bool RESTRICT, bool RZ,
+          int ITER>
 __global__ void __launch_bounds__(NT)
 k_sweep(MgView<T, CT, BT> L, MgView<T, CT, T> C, T omega, int flexible, Scalars* sc,
         double* part) {
   pdl_wait();
   if (sc->done) return;
-  constexpr int H = RESTRICT ? 3 : 2;  // x halo
+  // x halo: one ring per colour phase (ITER red-black iterations), plus one
+  // for the residual of the restriction
+  constexpr int H = 2 * ITER + (RESTRICT ? 1 : 0);
   constexpr int WX = SX + 2 * H, WY = SY + 2 * H;
   __shared__ T xs[WY][WX];
   const int nx = L.nx, ny = L.ny, P = L.pitch;
@@ -137,30 +140,22 @@ k_sweep(MgView<T, CT, BT> L, MgView<T, CT, T> C, T omega, int flexible, Scalars*
     xs[ly][lx] = s * L.di[g];
   };
 
-  // phase 1: first colour on the tile plus a ring of width H-1
-  {
-    constexpr int R = H - 1;
-    constexpr int CW = (SX + 2 * R) / 2, RH = SY + 2 * R;
+  // colour phases q = 0 .. 2*ITER-1 (FIRST colour on even q): phase q
+  // updates its colour on the tile plus a ring of width H-1-q, from values
+  // that phase q-1 (or the load) left valid one ring further out
+#pragma unroll
+  for (int q = 0; q < 2 * ITER; ++q) {
+    const int colour = (q & 1) ? 1 - FIRST : FIRST;
+    const int R = H - 1 - q;
+    const int CW = (SX + 2 * R) / 2, RH = SY + 2 * R;
     for (int e = t; e < CW * RH; e += NT) {
       const int k = e % CW, ey = e / CW;
       const int gy = y0 - R + ey;
-      const int gx = x0 - R + ((x0 - R + gy + FIRST) & 1) + 2 * k;
+      const int gx = x0 - R + ((x0 - R + gy + colour) & 1) + 2 * k;
       if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) relax(gx, gy);
     }
+    __syncthreads();
   }
-  __syncthreads();
-  // phase 2: second colour on the tile plus a ring of width H-2
-  {
-    constexpr int R = H - 2;
-    constexpr int CW = (SX + 2 * R) / 2, RH = SY + 2 * R;
-    for (int e = t; e < CW * RH; e += NT) {
-      const int k = e % CW, ey = e / CW;
-      const int gy = y0 - R + ey;
-      const int gx = x0 - R + ((x0 - R + gy + (1 - FIRST)) & 1) + 2 * k;
-      if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) relax(gx, gy);
-    }
-  }
-  __syncthreads();
 
   // phase 3: write the tile; optional r.z (accumulated in T per thread, then
   // combined in FP64)
@@ -594,11 +589,18 @@ static dim3 reduce_grid(int nx, int ny) {
 template <class T, class CT, class BT>
 void launch_sweep(const MgView<T, CT, BT>& L, const MgView<T, CT, T>& C, int first, bool zero,
                   bool prolong, bool restrict_, bool rz, double omega, int flexible, Scalars* sc,
-                  double* part, cudaStream_t s) {
+                  double* part, cudaStream_t s, int iters) {
   const dim3 g = tiles(L.nx, L.ny);
   const T om = (T)omega;
-#define SCF_SWEEP(F, Z, PR, RS, R) \
-  launch_k(k_sweep<T, CT, BT, F, Z, PR, RS, R>, g, dim3(NT), 0, s, L, C, om, flexible, sc, part)
+#define SCF_SWEEP(F, Z, PR, RS, R)                                                              \
+  do {                                                                                          \
+    if (iters == 2)                                                                             \
+      launch_k(k_sweep<T, CT, BT, F, Z, PR, RS, R, 2>, g, dim3(NT), 0, s, L, C, om, flexible,  \
+               sc, part);                                                                       \
+    else                                                                                        \
+      launch_k(k_sweep<T, CT, BT, F, Z, PR, RS, R, 1>, g, dim3(NT), 0, s, L, C, om, flexible,  \
+               sc, part);                                                                       \
+  } while (0)
   // the combinations the V-cycle uses (pre: red first; post: black first)
   if (first == 0 && zero && !prolong && !restrict_ && !rz) SCF_SWEEP(0, true, false, false, false);
   else if (first == 0 && zero && !prolong && restrict_ && !rz) SCF_SWEEP(0, true, false, true, false);
@@ -647,7 +649,7 @@ void launch_to_mixed(const LevelView& F, const MgView<float, __nv_bfloat16, floa
 #define SCF_INST(T, CT, BT)                                                                   \
   template void launch_sweep<T, CT, BT>(const MgView<T, CT, BT>&, const MgView<T, CT, T>&, int, \
                                         bool, bool, bool, bool, double, int, Scalars*, double*, \
-                                        cudaStream_t);                                          \
+                                        cudaStream_t, int);                                     \
   template void launch_coarse_solve_t<T, CT, BT>(const MgView<T, CT, BT>&, const double*,      \
                                                  const int*, const int*, Scalars*, cudaStream_t);
 SCF_INST(double, double, double)

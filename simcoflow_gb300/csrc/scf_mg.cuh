@@ -56,10 +56,11 @@ void launch_line_tail(const TailDesc<T, CT>& d, Scalars* sc, cudaStream_t s);
 template <class T, class CT>
 void launch_tail(const TailDesc<T, CT>& d, Scalars* sc, cudaStream_t s);
 
+// One fused launch of `iters` (1 or 2) red-black iterations on level L.
 template <class T, class CT, class BT>
 void launch_sweep(const MgView<T, CT, BT>& L, const MgView<T, CT, T>& C, int first, bool zero,
                   bool prolong, bool restrict_, bool rz, double omega, int flexible, Scalars* sc,
-                  double* part, cudaStream_t s);
+                  double* part, cudaStream_t s, int iters = 1);
 
 template <class T, class CT, class BT>
 void launch_coarse_solve_t(const MgView<T, CT, BT>& C, const double* Ainv, const int* cmap,

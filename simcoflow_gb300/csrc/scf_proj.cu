@@ -13,6 +13,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -154,15 +155,30 @@ MgD view64(scf_proj* h, int l) {
 double* buf64(scf_proj* h, int l, int i) { return i == 0 ? h->lev[l].x : h->x2_64[l]; }
 float* buf32(scf_proj* h, int l, int i) { return i == 0 ? h->mix[l].x : h->x2_32[l]; }
 
-// Buffer holding a level's result after its part of the V-cycle: sweeps
-// alternate buffers (npre down, npost up, starting from buffer 0), the tail
-// and the coarse solve write buffer 0.
+// The sweeps of one side of a V-cycle level as fused launches.  FP32
+// levels: two red-black iterations per launch while two remain, then one
+// (the second iteration reuses the tile staged by the first, halving the
+// DRAM traffic; its extra halo work is cheap in FP32).  FP64 levels: one per
+// launch -- the FP64 pipe, not DRAM, bounds them, and the wider halo would
+// add FP64 work.
+std::vector<int> sweep_launches(int n, bool fused2) {
+  std::vector<int> c;
+  for (; fused2 && n >= 2; n -= 2) c.push_back(2);
+  for (; n > 0; --n) c.push_back(1);
+  return c;
+}
+
+// Buffer holding a level's result after its part of the V-cycle: sweep
+// launches alternate buffers (down, then up, starting from buffer 0), the
+// tail and the coarse solve write buffer 0.
 int final_buf(scf_proj* h, int l) {
   if (h->line) return 0;  // line passes update in place
   const int L = (int)h->lev.size();
   const int lk = h->tail0 > 0 ? h->tail0 : L - 1;
   if (L == 1 || l >= lk) return 0;
-  return (h->opts.npre - 1 + h->opts.npost) % 2;
+  const int npre = (int)sweep_launches(h->opts.npre, h->mixed).size();
+  const int npost = (int)sweep_launches(h->opts.npost, h->mixed).size();
+  return (npre - 1 + npost) % 2;
 }
 
 // Enqueue one V-cycle.  `view(l)` is the base view of level l (level 0's b
@@ -173,7 +189,10 @@ void enqueue_vcycle_t(scf_proj* h, ViewFn view, BufFn buf, const TailDesc<T, CT>
                       Scalars* sc, bool do_rz, int flexible, cudaStream_t s) {
   using V = MgView<T, CT, T>;
   const int L = (int)h->lev.size();
-  const int npre = h->opts.npre, npost = h->opts.npost;
+  const bool fused2 = std::is_same<T, float>::value;
+  const std::vector<int> pre = sweep_launches(h->opts.npre, fused2),
+                         post = sweep_launches(h->opts.npost, fused2);
+  const int npre = (int)pre.size(), npost = (int)post.size();
   const double om = h->opts.omega;
   if (L == 1) {
     V c = view(0);
@@ -195,7 +214,8 @@ void enqueue_vcycle_t(scf_proj* h, ViewFn view, BufFn buf, const TailDesc<T, CT>
     for (int it = 0; it < npre; ++it) {
       f.xin = it > 0 ? buf(l, (it - 1) % 2) : nullptr;
       f.x = buf(l, it % 2);
-      launch_sweep(f, c, 0, it == 0, false, it == npre - 1, false, om, flexible, sc, h->part, s);
+      launch_sweep(f, c, 0, it == 0, false, it == npre - 1, false, om, flexible, sc, h->part, s,
+                   pre[it]);
     }
   }
   if (h->tail0 > 0) {
@@ -212,7 +232,7 @@ void enqueue_vcycle_t(scf_proj* h, ViewFn view, BufFn buf, const TailDesc<T, CT>
       f.xin = buf(l, (npre - 1 + it) % 2);
       f.x = buf(l, (npre + it) % 2);
       const bool rz = l == 0 && do_rz && it == npost - 1;
-      launch_sweep(f, c, 1, false, it == 0, false, rz, om, flexible, sc, h->part, s);
+      launch_sweep(f, c, 1, false, it == 0, false, rz, om, flexible, sc, h->part, s, post[it]);
     }
   }
 }

