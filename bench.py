@@ -357,6 +357,25 @@ def run_ours(args):
                                     mres=mres)
             return st
 
+        # V-cycle schedule from the project's autotuner (same candidates as the
+        # batch path), chosen by time to the tolerance on this workload
+        schedule = None
+        if not args.no_tune:
+            from simcoflow_gb300 import batch as Bt
+            best = None
+            for sch in Bt.SCHEDULES:
+                s.set_schedule(*sch)
+                step()
+                torch.cuda.synchronize(dev)
+                t0 = time.perf_counter()
+                for _ in range(2):
+                    stt = step()
+                torch.cuda.synchronize(dev)
+                ms_t = (time.perf_counter() - t0) / 2
+                if stt.status == 0 and (best is None or ms_t < best[0]):
+                    best = (ms_t, sch)
+            schedule = best[1]
+            s.set_schedule(*schedule)
         for _ in range(args.warmup):
             st = step()
         barrier()
@@ -383,7 +402,7 @@ def run_ours(args):
                 kt[name] = out.value
         s.close()
         return {"ms": ms, "iters": iters, "relres": relres, "levels": st.levels, "kt": kt,
-                "clk": clk.summary() if clk else None}
+                "clk": clk.summary() if clk else None, "schedule": schedule}
 
     plain = device_arm("fp64", False)
     mixed = device_arm("mixed", True)
@@ -404,16 +423,18 @@ def run_ours(args):
     hu, hv, hpp = pinned(A["u0"])[0], pinned(A["v0"])[0], pinned(A["p0"])[0]
     hPp = pinned(np.zeros((nx + 2, ny + 2), order="F"))[0]
     hm = pinned(np.zeros((nx, ny), order="F"))[0]
-    in_keys = ["dx", "dy", "dxU", "dyV", *P.GEOMETRY_ARGS, "DpU", "DpV", "ustar", "vstar"]
+    # the grid is fixed for a whole run (Initial_Grid, src/Mesh_Mod.f90:54-175): set once;
+    # everything the time step changes is copied in and out every step
+    in_keys = [*P.GEOMETRY_ARGS, "DpU", "DpV", "ustar", "vstar"]
     h2d = sum(H[k].nbytes for k in in_keys) + hu.nbytes + hv.nbytes + hpp.nbytes
     d2h = hPp.nbytes + hu.nbytes + hv.nbytes + hpp.nbytes + hm.nbytes
+    hs.set_grid(H["dx"], H["dy"], H["dxU"], H["dyV"])
 
     def e2e_step():
-        hs.set_grid(H["dx"], H["dy"], H["dxU"], H["dyV"])
         hs.set_geometry(**{k: H[k] for k in P.GEOMETRY_ARGS})
         hs.assemble(H["DpU"], H["DpV"], case.betaP, case.betaM, case.bc)
-        hs.update_puv(H["ustar"], H["vstar"], hu, hv, hpp, case.vb, Pp=hPp, mres=hm)
-        return float(np.abs(hm).max())  # read of the step's result on the host
+        _, _, st_ = hs.update_puv(H["ustar"], H["vstar"], hu, hv, hpp, case.vb, Pp=hPp, mres=hm)
+        return st_.mres_max  # the step's result (max |mres|), read on the host
 
     for _ in range(args.warmup):
         e2e_step()
@@ -509,8 +530,11 @@ def run_ours(args):
         "solves_per_s": round(1e3 * world / ms_step, 2),
         "iters": mixed["iters"][-1], "relres_true": mixed["relres"][-1],
         "levels": mixed["levels"],
+        "schedule": {"npre_npost_omega": mixed["schedule"],
+                     "source": "autotuner (simcoflow_gb300.batch.SCHEDULES), per arm"},
         "plain_fp64_mg_pcg": {"ms": round(plain["ms"], 4), "iters": plain["iters"][-1],
                               "relres_true": plain["relres"][-1],
+                              "schedule": plain["schedule"],
                               "kernels": kernel_table(plain, "fp64")},
         "speedup_vs_plain": round(plain["ms"] / ms_step, 3),
         "e2e": {"value": round(e2e_ms, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
@@ -533,6 +557,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="c2")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="default V-cycle schedule instead of the autotuned one")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the learned, 4096^2 stretched and 64-instance batch lines")
     ap.add_argument("--no-graph", action="store_true",

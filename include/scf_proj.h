@@ -183,7 +183,10 @@ int scf_proj_set_geometry(scf_proj *h, const double *vof, const double *phi,
  * HYPRE_ParCSRPCGSetup (src/ProjectionP_Mod.f90:50-57).
  *   DpU, DpV   PU%Dp, PV%Dp, (nx+2,ny+2) (src/PredictorUV_mod.f90:700)
  *   betaP, betaM  1/(row/Roref), 1/(roa/Roref) (src/ComputePUV_Mod.f90:42-43)
- *   wb, eb, sb, nb  1 = Neumann, 0 = Dirichlet (the reference passes 1,1,1,0) */
+ *   wb, eb, sb, nb  1 = Neumann, 0 = Dirichlet (the reference passes 1,1,1,0)
+ * Asynchronous on the handle's stream: it returns once DpU/DpV are copied
+ * (host mode) and leaves the setup running; a NaN, Inf or invalid cell class
+ * met by the setup is reported by the next solve as SCF_ERR_NAN. */
 int scf_proj_assemble(scf_proj *h, const double *DpU, const double *DpV, double betaP,
                       double betaM, int wb, int eb, int sb, int nb);
 

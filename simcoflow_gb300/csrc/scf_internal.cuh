@@ -51,7 +51,8 @@ struct Scalars {
   double bnorm2, rr, rz, pq, alpha, beta, rtol2, res_true2, mres_max, rr_prev;
   double rz_cross;  // r_{k+1}.z_k of the flexible PCG, reduced by the x/r update
   int iter, maxit, done, status, nan;
-  int pad[3];
+  int pad[2];  // pad[0]: guard counter of the graph loop
+  int anan;    // NaN or Inf met by the operator setup (kept until the next assembly)
   unsigned tickets[8];  // last-block counters, one per reduction site
 };
 

@@ -258,7 +258,7 @@ __global__ void k_assemble(FortranIn in, LevelView L, Scalars* sc) {
     if (in.eb == 1 && i == nx) d = sub(d, tE);
     if (in.nb == 1 && j == ny) d = sub(d, tN);
     d = add(d, mul(copysign(1.0, d), 1.0e-24));
-    if (!isfinite(d) || cs == 0) sc->nan = 1;
+    if (!isfinite(d) || cs == 0) sc->anan = 1;
     L.dg[kl] = d;
     L.cE[kl] = (i < nx && in.posnu_p[fo0(nx, i + 1, j)] != -1) ? tE : 0.0;
     L.cN[kl] = (j < ny && in.posnu_p[fo0(nx, i, j + 1)] != -1) ? tN : 0.0;

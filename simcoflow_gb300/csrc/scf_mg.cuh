@@ -30,7 +30,7 @@ struct MgView {
 
 // The coarse end of a V-cycle in one CTA (levels of at most kTailMaxCells
 // cells, the last of them the coarsest).
-constexpr int kTailMaxCells = 4096;
+constexpr int kTailMaxCells = 1024;
 constexpr int kTailMaxLevels = 12;
 template <class T, class CT>
 struct TailDesc {

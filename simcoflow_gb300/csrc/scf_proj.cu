@@ -33,6 +33,10 @@ struct scf_proj {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  // host-pointer mode: the solve's input copies run here, beside the
+  // operator setup still running on `stream`
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_done = nullptr;
   bool devptrs = false;
   bool mixed = false;
 
@@ -154,6 +158,17 @@ MgD view64(scf_proj* h, int l) {
 // the two iterate buffers of a level; buffer 0 is the one in the base view
 double* buf64(scf_proj* h, int l, int i) { return i == 0 ? h->lev[l].x : h->x2_64[l]; }
 float* buf32(scf_proj* h, int l, int i) { return i == 0 ? h->mix[l].x : h->x2_32[l]; }
+
+// Largest level handled by the single-CTA tails (SCF_TAIL_CELLS overrides
+// kTailMaxCells, for tuning; shared memory bounds it in any case).
+long tail_cells() {
+  static const long v = [] {
+    const char* e = getenv("SCF_TAIL_CELLS");
+    const long n = e ? atol(e) : 0;
+    return n > 0 ? n : (long)kTailMaxCells;
+  }();
+  return v;
+}
 
 // The sweeps of one side of a V-cycle level as fused launches.  FP32
 // levels: two red-black iterations per launch while two remain, then one
@@ -670,22 +685,30 @@ int solve_common(scf_proj* h, const double* ustar, const double* vstar, double v
   const int nx = h->nx, ny = h->ny;
   const size_t n0 = (size_t)(nx + 2) * (ny + 2), n1 = (size_t)nx * ny;
   cudaStream_t s = h->stream;
-  CK(cudaEventRecord(h->ev[0], s));
+  // host mode: the input copies go on the copy stream, so they overlap the
+  // operator setup that assemble left running on the solver stream (the
+  // staging buffers are idle: every solve ends with a synchronisation)
+  cudaStream_t cs = h->devptrs ? s : h->copy_stream;
+  CK(cudaEventRecord(h->ev[0], cs));
   const double *dus = ustar, *dvs = vstar;
   double *dPp = Pp, *dp = p, *du = u, *dv = v, *dm = mres;
   if (!h->devptrs) {
-    CK(cudaMemcpyAsync(h->st_us, ustar, n0 * 8, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(h->st_vs, vstar, n0 * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->st_us, ustar, n0 * 8, cudaMemcpyHostToDevice, cs));
+    CK(cudaMemcpyAsync(h->st_vs, vstar, n0 * 8, cudaMemcpyHostToDevice, cs));
     dus = h->st_us; dvs = h->st_vs;
     dPp = Pp ? h->st_Pp : nullptr;
     if (correct) {
-      CK(cudaMemcpyAsync(h->st_p, p, n0 * 8, cudaMemcpyHostToDevice, s));
-      CK(cudaMemcpyAsync(h->st_u, u, n0 * 8, cudaMemcpyHostToDevice, s));
-      CK(cudaMemcpyAsync(h->st_v, v, n0 * 8, cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(h->st_p, p, n0 * 8, cudaMemcpyHostToDevice, cs));
+      CK(cudaMemcpyAsync(h->st_u, u, n0 * 8, cudaMemcpyHostToDevice, cs));
+      CK(cudaMemcpyAsync(h->st_v, v, n0 * 8, cudaMemcpyHostToDevice, cs));
       dp = h->st_p; du = h->st_u; dv = h->st_v; dm = h->st_mres;
     }
   }
-  CK(cudaEventRecord(h->ev[1], s));
+  CK(cudaEventRecord(h->ev[1], cs));
+  if (cs != s) {
+    CK(cudaEventRecord(h->copy_done, cs));
+    CK(cudaStreamWaitEvent(s, h->copy_done, 0));
+  }
   LevelView L0 = h->lev[0];
   // the NaN flag of a previous solve must not leak into this one
   CK(cudaMemsetAsync(&h->sc->nan, 0, sizeof(int), s));
@@ -718,7 +741,7 @@ int solve_common(scf_proj* h, const double* ustar, const double* vstar, double v
   CK(cudaStreamSynchronize(s));
   const Scalars& S = *h->sc_host;
   int status = S.status;
-  if (S.nan) status = SCF_ERR_NAN;
+  if (S.nan || S.anan) status = SCF_ERR_NAN;
   if (st) {
     st->iters = S.iter;
     st->status = status;
@@ -803,6 +826,9 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
     return fail(SCF_ERR_CUDA);
   h->own_stream = true;
+  if (cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->copy_done, cudaEventDisableTiming) != cudaSuccess)
+    return fail(SCF_ERR_CUDA);
   for (auto& e : h->ev)
     if (cudaEventCreate(&e) != cudaSuccess) return fail(SCF_ERR_CUDA);
   // FP64 multigrid levels
@@ -852,11 +878,11 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
   if ((rc = dev_alloc(h, (void**)&h->Ainv, sizeof(double) * kMaxCoarse * kMaxCoarse))) return fail(rc);
   if ((rc = dev_alloc(h, (void**)&h->cmap, sizeof(int) * kMaxCoarse))) return fail(rc);
   if ((rc = dev_alloc(h, (void**)&h->ncoarse, sizeof(int)))) return fail(rc);
-  // the single-CTA tail: the first level >= 1 with at most kTailMaxCells cells
+  // the single-CTA tail: the first level >= 1 with at most tail_cells() cells
   // whose levels fit one CTA's shared memory (ragged grids may need a later one)
   if (!getenv("SCF_NO_TAIL")) {
     for (int l = 1; l < nlev; ++l) {
-      if ((long)h->lev[l].nx * h->lev[l].ny > kTailMaxCells || nlev - l > kTailMaxLevels) continue;
+      if ((long)h->lev[l].nx * h->lev[l].ny > tail_cells() || nlev - l > kTailMaxLevels) continue;
       auto fill = [&](auto& d, auto view) {
         d.n = nlev - l;
         for (int k = 0; k < d.n; ++k) d.lv[k] = view(l + k);
@@ -873,7 +899,7 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
   // the single-CTA tail of the line smoother, chosen the same way
   if (o.smoother != SCF_SMOOTH_POINT && !getenv("SCF_NO_TAIL")) {
     for (int l = 1; l < nlev; ++l) {
-      if ((long)h->lev[l].nx * h->lev[l].ny > kTailMaxCells || nlev - l + 1 > kTailMaxLevels)
+      if ((long)h->lev[l].nx * h->lev[l].ny > tail_cells() || nlev - l + 1 > kTailMaxLevels)
         continue;
       auto fill = [&](auto& d, auto view) {
         d.n = nlev - l;
@@ -939,6 +965,8 @@ int scf_proj_destroy(scf_proj* h) {
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+  if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+  if (h->copy_done) cudaEventDestroy(h->copy_done);
   delete h;
   return SCF_OK;
 }
@@ -1033,16 +1061,15 @@ int scf_proj_assemble(scf_proj* h, const double* DpU, const double* DpV, double 
   f.betaP = betaP; f.betaM = betaM;
   f.wb = wb; f.eb = eb; f.sb = sb; f.nb = nb;
   cudaStream_t s = h->stream;
+  // host mode: the caller may reuse DpU/DpV once their copies are done
+  CK(cudaEventRecord(h->copy_done, s));
   CK(cudaMemsetAsync(h->sc, 0, sizeof(Scalars), s));
   enqueue_setup(h, h->sc, s);
   CK(cudaGetLastError());
-  int nanflag = 0;
-  CK(cudaMemcpyAsync(&nanflag, &h->sc->nan, sizeof(int), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
-  if (nanflag) return SCF_ERR_NAN;
   if (!h->gexec && !h->body_exec && !(h->opts.flags & SCF_FLAG_NO_GRAPH)) {
     if ((rc = build_graph(h))) return rc;
   }
+  if (!h->devptrs) CK(cudaEventSynchronize(h->copy_done));
   h->assembled = true;
   return SCF_OK;
 }
@@ -1257,7 +1284,7 @@ int scf_batch_run(scf_batch* b, void* stream, scf_stats* stats) {
   int worst = SCF_OK;
   for (size_t i = 0; i < b->h.size(); ++i) {
     const Scalars& S = *b->h[i]->sc_host;
-    int status = S.nan ? SCF_ERR_NAN : S.status;
+    int status = (S.nan || S.anan) ? SCF_ERR_NAN : S.status;
     if (status != kOk && worst == SCF_OK) worst = status;
     if (stats) {
       scf_stats& st = stats[i];
@@ -1362,7 +1389,7 @@ int scf_proj_solve_rhs(scf_proj* h, const double* b, double* x, double* r, int m
   CK(cudaStreamSynchronize(s));
   const Scalars& S = *h->sc_host;
   int status = S.status;
-  if (S.nan) status = SCF_ERR_NAN;
+  if (S.nan || S.anan) status = SCF_ERR_NAN;
   if (maxit == 0 && S.bnorm2 > 0) status = SCF_ERR_NOT_CONVERGED;
   if (st) {
     memset(st, 0, sizeof(*st));
