@@ -162,89 +162,106 @@ __device__ __forceinline__ double pocoef(double Dp, double len, double dist, dou
   return dvd(mul(mul(dvd(mul(Dp, len), dist), bP), bM), B);
 }
 
-// PoCoef of one face for every lane of a converged warp.  Away from the
-// interface and the solids the inputs (Dp, face length, node distance,
-// density factor) are the same across a warp, which spans one grid row; the
-// two IEEE divisions are then done once and broadcast, so the FP64 pipe
-// (slow on GB300) is spared while every lane gets the bits it would have
-// computed itself.
-__device__ __forceinline__ double pocoef_warp(bool valid, double Dp, double len, double dist,
-                                              double bP, double bM, double B) {
-  const unsigned full = 0xffffffffu;
-  const unsigned vmask = __ballot_sync(full, valid);
-  if (vmask == 0u) return 0.0;
-  const int leader = __ffs(vmask) - 1;
-  const long long a = __double_as_longlong(Dp), b = __double_as_longlong(len);
-  const long long c = __double_as_longlong(dist), d = __double_as_longlong(B);
-  // every lane takes part in every shuffle (no short-circuit around them)
-  const long long a0 = __shfl_sync(full, a, leader), b0 = __shfl_sync(full, b, leader);
-  const long long c0 = __shfl_sync(full, c, leader), d0 = __shfl_sync(full, d, leader);
-  const bool same = !valid || (a == a0 && b == b0 && c == c0 && d == d0);
-  if (__all_sync(full, same)) {
-    double r = 0.0;
-    if ((int)(threadIdx.x & 31) == leader) r = pocoef(Dp, len, dist, bP, bM, B);
-    return __shfl_sync(full, r, leader);
-  }
-  return valid ? pocoef(Dp, len, dist, bP, bM, B) : 0.0;
+// Inputs of one face's PoCoef, and whether the reference sets the face.
+struct FaceIn {
+  bool ok;
+  double Dp, len, dist, B;
+};
+__device__ __forceinline__ bool same_bits(double a, double b) {
+  return __double_as_longlong(a) == __double_as_longlong(b);
+}
+__device__ __forceinline__ bool same_face(const FaceIn& a, const FaceIn& b) {
+  return a.ok == b.ok && (!a.ok || (same_bits(a.Dp, b.Dp) && same_bits(a.len, b.len) &&
+                                    same_bits(a.dist, b.dist) && same_bits(a.B, b.B)));
+}
+__device__ __forceinline__ double face_pocoef(const FaceIn& f, double bP, double bM) {
+  return f.ok ? pocoef(f.Dp, f.len, f.dist, bP, bM, f.B) : 0.0;
+}
+__device__ __forceinline__ double shfl_up_d(double v, int lane_delta) {
+  return __shfl_up_sync(0xffffffffu, v, lane_delta);
 }
 
+// Operator assembly, one thread per cell column and a run of consecutive
+// rows.  Every cell evaluates PoCoef on its four faces in the reference's
+// order, but a face whose inputs (Dp, face length, node distance, density
+// factor) equal bit for bit those of the same face seen from the other cell
+// -- the east face of the west neighbour (one lane down the warp), the north
+// face of the row below (this thread's previous row) -- takes that value
+// instead of repeating the two IEEE FP64 divisions: the same function of the
+// same bits.  Away from the interface every face qualifies, which halves the
+// divisions on GB300's slow FP64 pipe.
 __global__ void k_assemble(FortranIn in, LevelView L, Scalars* sc) {
   pdl_wait();
   const int nx = in.nx, ny = in.ny;
   const int ix = blockIdx.x * kBX + threadIdx.x;
+  const int lane = threadIdx.x;  // blockDim.x == 32: a warp is 32 consecutive columns
   const bool in_x = ix < nx;
-  // every lane of a warp walks the same rows (blockDim.x == 32), so the warp
-  // stays converged for the shuffles in pocoef_warp
-  for (int iy = blockIdx.y * kBY + threadIdx.y; iy < ny; iy += gridDim.y * kBY) {
+  const int nthr_y = gridDim.y * kBY;
+  const int chunk = (ny + nthr_y - 1) / nthr_y;
+  const int r0 = (blockIdx.y * kBY + threadIdx.y) * chunk;
+  const int r1 = r0 + chunk < ny ? r0 + chunk : ny;
+  const double bP = in.betaP, bM = in.betaM;
+  FaceIn prevN = {false, 0.0, 1.0, 1.0, 1.0};
+  double prevNpc = 0.0;
+  // the row range is the same for the whole warp: it stays converged for the shuffles
+  for (int iy = r0; iy < r1; ++iy) {
     const int i = ix + 1, j = iy + 1;
     const size_t k1 = in_x ? fo1(nx, i, j) : 0, k0 = in_x ? fo0(nx, i, j) : 0;
     const size_t kl = (size_t)iy * L.pitch + ix;
     const bool act = in_x && in.posnu_p[k0] != -1;
-    const double bP = in.betaP, bM = in.betaM;
     const double phis = act ? in.phi[k1] : 0.0;
     const int cs = act ? cell_class(in.vof[k1], phis, in.vofS[k1]) : 0;
     const double dxP = act ? in.dx[k1] : 1.0, dyP = act ? in.dy[k1] : 1.0;
-    // per face: whether the reference sets it, and the inputs of PoCoef
-    bool ok[4] = {false, false, false, false};
-    double Dp[4] = {0, 0, 0, 0}, len[4] = {1, 1, 1, 1}, dist[4] = {1, 1, 1, 1}, Bf[4] = {1, 1, 1, 1};
+    FaceIn f[4];  // S, W, E, N
+#pragma unroll
+    for (int q = 0; q < 4; ++q) f[q] = {false, 0.0, 1.0, 1.0, 1.0};
     if (act) {
       double B;
       if (j > 1) {
         const size_t kn = fo1(nx, i, j - 1);
-        if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B)) {
-          ok[0] = true; Dp[0] = in.DpV[fo0(nx, i, j - 1)]; len[0] = dxP; dist[0] = in.dyV[kn]; Bf[0] = B;
-        }
+        if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B))
+          f[0] = {true, in.DpV[fo0(nx, i, j - 1)], dxP, in.dyV[kn], B};
       } else if (boundary_beta(cs, bP, bM, &B)) {
-        ok[0] = true; Dp[0] = in.DpV[k0]; len[0] = dxP; dist[0] = in.dyV[k1]; Bf[0] = B;
+        f[0] = {true, in.DpV[k0], dxP, in.dyV[k1], B};
       }
       if (i > 1) {
         const size_t kn = fo1(nx, i - 1, j);
-        if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B)) {
-          ok[1] = true; Dp[1] = in.DpU[fo0(nx, i - 1, j)]; len[1] = dyP; dist[1] = in.dxU[kn]; Bf[1] = B;
-        }
+        if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B))
+          f[1] = {true, in.DpU[fo0(nx, i - 1, j)], dyP, in.dxU[kn], B};
       } else if (boundary_beta(cs, bP, bM, &B)) {
-        ok[1] = true; Dp[1] = in.DpU[k0]; len[1] = dyP; dist[1] = in.dxU[k1]; Bf[1] = B;
+        f[1] = {true, in.DpU[k0], dyP, in.dxU[k1], B};
       }
       if (i < nx) {
         const size_t kn = fo1(nx, i + 1, j);
-        if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B)) {
-          ok[2] = true; Dp[2] = in.DpU[k0]; len[2] = dyP; dist[2] = in.dxU[k1]; Bf[2] = B;
-        }
+        if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B))
+          f[2] = {true, in.DpU[k0], dyP, in.dxU[k1], B};
       } else if (boundary_beta(cs, bP, bM, &B)) {
-        ok[2] = true; Dp[2] = in.DpU[k0]; len[2] = dyP; dist[2] = in.dxU[k1]; Bf[2] = B;
+        f[2] = {true, in.DpU[k0], dyP, in.dxU[k1], B};
       }
       if (j < ny) {
         const size_t kn = fo1(nx, i, j + 1);
-        if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B)) {
-          ok[3] = true; Dp[3] = in.DpV[k0]; len[3] = dxP; dist[3] = in.dyV[k1]; Bf[3] = B;
-        }
+        if (face_beta(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], bP, bM, &B))
+          f[3] = {true, in.DpV[k0], dxP, in.dyV[k1], B};
       } else if (boundary_beta(cs, bP, bM, &B)) {
-        ok[3] = true; Dp[3] = in.DpV[k0]; len[3] = dxP; dist[3] = in.dyV[k1]; Bf[3] = B;
+        f[3] = {true, in.DpV[k0], dxP, in.dyV[k1], B};
       }
     }
-    double pc[4];  // S, W, E, N
-#pragma unroll
-    for (int f = 0; f < 4; ++f) pc[f] = pocoef_warp(ok[f], Dp[f], len[f], dist[f], bP, bM, Bf[f]);
+    double pc[4];
+    pc[2] = face_pocoef(f[2], bP, bM);
+    pc[3] = face_pocoef(f[3], bP, bM);
+    // west face: the east face of the lane below (all lanes shuffle)
+    FaceIn wl;
+    wl.ok = __shfl_up_sync(0xffffffffu, (int)f[2].ok, 1) != 0;
+    wl.Dp = shfl_up_d(f[2].Dp, 1);
+    wl.len = shfl_up_d(f[2].len, 1);
+    wl.dist = shfl_up_d(f[2].dist, 1);
+    wl.B = shfl_up_d(f[2].B, 1);
+    const double pcl = shfl_up_d(pc[2], 1);
+    pc[1] = (lane > 0 && same_face(f[1], wl)) ? pcl : face_pocoef(f[1], bP, bM);
+    // south face: this thread's north face of the previous row
+    pc[0] = (iy > r0 && same_face(f[0], prevN)) ? prevNpc : face_pocoef(f[0], bP, bM);
+    prevN = f[3];
+    prevNpc = pc[3];
     if (!in_x) continue;
     if (!act) {
       L.cE[kl] = 0.0; L.cN[kl] = 0.0; L.dg[kl] = -1.0;
