@@ -94,6 +94,20 @@ __device__ __forceinline__ void vstore(T* p, const T (&o)[M]) {
   for (int v = 0; v < M / PER; ++v) reinterpret_cast<uint4*>(p)[v] = pack(o + v * PER);
 }
 
+// Reciprocal for the eliminations (a smoother needs no correctly rounded
+// quotient).  FP32: the hardware's correctly rounded reciprocal.  FP64: an
+// FP32 seed refined by two Newton-Raphson steps r <- r (2 - x r), each of
+// which doubles the correct bits (24 -> 48 -> full precision); far cheaper
+// than an IEEE FP64 division on GB300's FP64 pipe.  x is a positive pivot of
+// an M-matrix elimination, well inside FP32's range.
+__device__ __forceinline__ float lrcp(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double lrcp(double x) {
+  double r = (double)__frcp_rn((float)x);
+  r = r * fma(-x, r, 2.0);
+  r = r * fma(-x, r, 2.0);
+  return r;
+}
+
 // Relax the lines (rows) iy = 2*blockIdx.x + colour of level L.
 // ZERO: the iterate is zero on entry (the first pass of a V-cycle level):
 // the neighbouring rows are not read, and they are written as zero.
@@ -161,7 +175,7 @@ k_line(MgView<T, CT, T> L, int colour, const Scalars* sc) {
   //   x_k = D_k + S_k * I_{t-1} + T_k * I_t   (k < M-1).
   T cp[M], D[M], S[M], Tr[M];
   {
-    T inv = T(1) / d[0];
+    T inv = lrcp(d[0]);
     cp[0] = (M == 2) ? T(0) : c[0] * inv;
     D[0] = r[0] * inv;
     S[0] = -a[0] * inv;
@@ -169,7 +183,7 @@ k_line(MgView<T, CT, T> L, int colour, const Scalars* sc) {
 #pragma unroll
     for (int k = 1; k < M - 1; ++k) {
       const T den = fma(-a[k], cp[k - 1], d[k]);
-      inv = T(1) / den;
+      inv = lrcp(den);
       cp[k] = (k == M - 2) ? T(0) : c[k] * inv;
       D[k] = fma(-a[k], D[k - 1], r[k]) * inv;
       S[k] = -a[k] * S[k - 1] * inv;
@@ -209,13 +223,13 @@ k_line(MgView<T, CT, T> L, int colour, const Scalars* sc) {
     const T* D_ = C_ + nth;
     T na = T(0), nb = B_[t], nc = T(0), nd = D_[t];
     if (t - s >= 0) {
-      const T k1 = A_[t] / B_[t - s];
+      const T k1 = A_[t] * lrcp(B_[t - s]);
       na = -A_[t - s] * k1;
       nb = fma(-C_[t - s], k1, nb);
       nd = fma(-D_[t - s], k1, nd);
     }
     if (t + s < nth) {
-      const T k2 = C_[t] / B_[t + s];
+      const T k2 = C_[t] * lrcp(B_[t + s]);
       nc = -C_[t + s] * k2;
       nb = fma(-A_[t + s], k2, nb);
       nd = fma(-D_[t + s], k2, nd);
@@ -228,7 +242,7 @@ k_line(MgView<T, CT, T> L, int colour, const Scalars* sc) {
     cur ^= 1;
     __syncthreads();
   }
-  const T It = pa[cur * 4 * nth + 3 * nth + t] / pa[cur * 4 * nth + nth + t];
+  const T It = pa[cur * 4 * nth + 3 * nth + t] * lrcp(pa[cur * 4 * nth + nth + t]);
   rD0[t] = It;  // rD0 is no longer read by anyone after the first barrier above
   __syncthreads();
   const T Il = t > 0 ? rD0[t - 1] : T(0);
@@ -249,6 +263,216 @@ k_line(MgView<T, CT, T> L, int colour, const Scalars* sc) {
 #pragma unroll
     for (int k = 0; k < M; ++k) z[k] = T(0);
     vstore<T, M>(L.x + g0 + P + ix0, z);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Factored line relaxation (FP64 levels).  The line matrices do not change
+// between V-cycles, so everything that depends on them alone -- the interior
+// pivots, the responses S, T of every interior cell to its two interfaces,
+// the interface equations and every multiplier of the cyclic reduction -- is
+// computed once per assembly by k_line_factor.  A relaxation pass
+// (k_line_solve) is then a forward and a backward substitution, one
+// cyclic-reduction sweep of the right-hand side and the recovery: no
+// division, five FP64 operations per cell instead of about forty, which
+// matters on GB300's slow FP64 pipe.
+// Per cell (interior cells of each thread's chunk): INV (1/pivot, 0 where
+// the cell has no unknown), GA (sub-diagonal times INV), CP (super-diagonal
+// multiplier), S, TR (responses).  Per thread: aI, cI, 1/B of the reduced
+// equation (0 where the interface has no unknown), then k1, k2 per
+// reduction step.
+constexpr int kLineSlots = kLineThreadSlots;  // 3 + 2 x (up to 10 reduction steps)
+
+template <class T, class CT, int M>
+__global__ void __launch_bounds__(512, 1)
+k_line_factor(MgView<T, CT, T> L, LineFactors<T> F) {
+  pdl_wait();
+  extern __shared__ __align__(16) unsigned char lf_smem[];
+  const int nth = blockDim.x, t = threadIdx.x;
+  T* rS0 = reinterpret_cast<T*>(lf_smem);
+  T* rT0 = rS0 + nth;
+  T* pa = rT0 + nth;  // two buffers of A, B, C
+  const int iy = blockIdx.x;
+  if (iy >= L.ny) return;
+  const int P = L.pitch, nx = L.nx;
+  const size_t g0 = (size_t)iy * P;
+  const float cs = L.csp ? __ldg(L.csp) : 1.0f;
+  T a[M], d[M], c[M];
+  unsigned actm = 0;
+  const int ix0 = t * M;
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const int ix = ix0 + k;
+    T dv = T(-1), aw = T(0), ce = T(0);
+    if (ix < nx) {
+      const size_t g = g0 + ix;
+      dv = L.dg[g];
+      aw = lcoef<CT, T>(L.cE, g - 1, cs);
+      ce = lcoef<CT, T>(L.cE, g, cs);
+    }
+    const bool act = dv > T(0);
+    actm |= act ? (1u << k) : 0u;
+    a[k] = act ? -aw : T(0);
+    c[k] = act ? -ce : T(0);
+    d[k] = act ? dv : T(1);
+  }
+  T cp[M], iv[M], S[M], Tr[M];
+  {
+    T inv = lrcp(d[0]);
+    iv[0] = inv;
+    cp[0] = (M == 2) ? T(0) : c[0] * inv;
+    S[0] = -a[0] * inv;
+    Tr[0] = (M == 2) ? -c[0] * inv : T(0);
+#pragma unroll
+    for (int k = 1; k < M - 1; ++k) {
+      inv = lrcp(fma(-a[k], cp[k - 1], d[k]));
+      iv[k] = inv;
+      cp[k] = (k == M - 2) ? T(0) : c[k] * inv;
+      S[k] = -a[k] * S[k - 1] * inv;
+      Tr[k] = fma(-a[k], Tr[k - 1], (k == M - 2) ? -c[k] : T(0)) * inv;
+    }
+#pragma unroll
+    for (int k = M - 3; k >= 0; --k) {
+      S[k] = fma(-cp[k], S[k + 1], S[k]);
+      Tr[k] = fma(-cp[k], Tr[k + 1], Tr[k]);
+    }
+  }
+  if (ix0 < nx) {
+#pragma unroll
+    for (int k = 0; k < M - 1; ++k) {
+      const size_t g = g0 + ix0 + k;
+      const bool act = (actm >> k) & 1u;
+      F.inv[g] = act ? iv[k] : T(0);
+      F.ga[g] = act ? a[k] * iv[k] : T(0);
+      F.cp[g] = cp[k];
+      F.S[g] = S[k];
+      F.tr[g] = Tr[k];
+    }
+  }
+  rS0[t] = S[0];
+  rT0[t] = Tr[0];
+  __syncthreads();
+  const bool last = t == nth - 1;
+  const T aI = a[M - 1], dI = d[M - 1], cI = c[M - 1];
+  const T Sn = last ? T(0) : rS0[t + 1], Tn = last ? T(0) : rT0[t + 1];
+  T* th = F.thr + ((size_t)iy * F.nth + t) * kLineSlots;
+  th[0] = aI;
+  th[1] = cI;
+  pa[t] = aI * S[M - 2];
+  pa[nth + t] = fma(cI, Sn, fma(aI, Tr[M - 2], dI));
+  pa[2 * nth + t] = cI * Tn;
+  __syncthreads();
+  int cur = 0, step = 0;
+  for (int sdist = 1; sdist < nth; sdist <<= 1, ++step) {
+    const T* A_ = pa + cur * 3 * nth;
+    const T* B_ = A_ + nth;
+    const T* C_ = B_ + nth;
+    T na = T(0), nb = B_[t], nc = T(0), k1 = T(0), k2 = T(0);
+    if (t - sdist >= 0) {
+      k1 = A_[t] * lrcp(B_[t - sdist]);
+      na = -A_[t - sdist] * k1;
+      nb = fma(-C_[t - sdist], k1, nb);
+    }
+    if (t + sdist < nth) {
+      k2 = C_[t] * lrcp(B_[t + sdist]);
+      nc = -C_[t + sdist] * k2;
+      nb = fma(-A_[t + sdist], k2, nb);
+    }
+    th[3 + 2 * step] = k1;
+    th[4 + 2 * step] = k2;
+    T* W = pa + (cur ^ 1) * 3 * nth;
+    W[t] = na;
+    W[nth + t] = nb;
+    W[2 * nth + t] = nc;
+    cur ^= 1;
+    __syncthreads();
+  }
+  const bool actI = (actm >> (M - 1)) & 1u;
+  th[2] = actI ? lrcp(pa[cur * 3 * nth + nth + t]) : T(0);
+}
+
+// One relaxation pass with the factors of k_line_factor (lines iy = 2*blockIdx.x + colour)
+template <class T, class CT, int M, bool ZERO>
+__global__ void __launch_bounds__(512, 1)
+k_line_solve(MgView<T, CT, T> L, LineFactors<T> F, int colour, const Scalars* sc) {
+  pdl_wait();
+  if (sc && sc->done) return;
+  extern __shared__ __align__(16) unsigned char ls_smem[];
+  const int nth = blockDim.x, t = threadIdx.x;
+  T* rD0 = reinterpret_cast<T*>(ls_smem);
+  T* pd = rD0 + nth;  // two buffers of the reduced right-hand side
+  const int iy = 2 * blockIdx.x + colour;
+  if (iy >= L.ny) return;
+  const int P = L.pitch, nx = L.nx;
+  const size_t g0 = (size_t)iy * P;
+  const float cs = L.csp ? __ldg(L.csp) : 1.0f;
+  const int ix0 = t * M;
+  const bool has = ix0 < nx;  // chunks past the row are identity rows
+  T r[M], D[M];
+  if (has) {
+    const size_t g = g0 + ix0;
+    vload<T, M>(L.b + g, r);
+    if (!ZERO) {
+      T xn[M], xs[M], cn[M], cs_[M];
+      vload<T, M>(L.x + g + P, xn);
+      vload<T, M>(L.x + g - P, xs);
+      cvload<M>(L.cN + g, cn, cs);
+      cvload<M>(L.cN + g - P, cs_, cs);
+#pragma unroll
+      for (int k = 0; k < M; ++k) r[k] = fma(cs_[k], xs[k], fma(cn[k], xn[k], r[k]));
+    }
+    T iv[M], ga[M], cp[M];
+    vload<T, M>(F.inv + g, iv);
+    vload<T, M>(F.ga + g, ga);
+    vload<T, M>(F.cp + g, cp);
+    D[0] = r[0] * iv[0];
+#pragma unroll
+    for (int k = 1; k < M - 1; ++k) D[k] = fma(-ga[k], D[k - 1], r[k] * iv[k]);
+#pragma unroll
+    for (int k = M - 3; k >= 0; --k) D[k] = fma(-cp[k], D[k + 1], D[k]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < M; ++k) { r[k] = T(0); D[k] = T(0); }
+  }
+  rD0[t] = D[0];
+  const T* th = F.thr + ((size_t)iy * F.nth + t) * kLineSlots;
+  const T aI = th[0], cI = th[1], invB = th[2];
+  __syncthreads();
+  const T Dn = t == nth - 1 ? T(0) : rD0[t + 1];
+  pd[t] = fma(-cI, Dn, fma(-aI, D[M - 2], r[M - 1]));
+  __syncthreads();
+  int cur = 0, step = 0;
+  for (int sdist = 1; sdist < nth; sdist <<= 1, ++step) {
+    const T* Dc = pd + cur * nth;
+    T v = Dc[t];
+    if (t - sdist >= 0) v = fma(-th[3 + 2 * step], Dc[t - sdist], v);
+    if (t + sdist < nth) v = fma(-th[4 + 2 * step], Dc[t + sdist], v);
+    pd[(cur ^ 1) * nth + t] = v;
+    cur ^= 1;
+    __syncthreads();
+  }
+  const T It = pd[cur * nth + t] * invB;
+  rD0[t] = It;  // rD0's reads all happened before the reduction's first barrier
+  __syncthreads();
+  const T Il = t > 0 ? rD0[t - 1] : T(0);
+  if (!has) return;
+  const size_t g = g0 + ix0;
+  T S[M], Tr[M], xo[M];
+  vload<T, M>(F.S + g, S);
+  vload<T, M>(F.tr + g, Tr);
+#pragma unroll
+  for (int k = 0; k < M - 1; ++k) xo[k] = fma(S[k], Il, fma(Tr[k], It, D[k]));
+  xo[M - 1] = It;
+  if (ix0 + M <= nx) {
+    vstore<T, M>(L.x + g, xo);
+  } else {
+    for (int k = 0; k < nx - ix0; ++k) L.x[g + k] = xo[k];
+  }
+  if (ZERO && iy + 1 < L.ny) {
+    T z[M];
+#pragma unroll
+    for (int k = 0; k < M; ++k) z[k] = T(0);
+    vstore<T, M>(L.x + g + P, z);
   }
 }
 
@@ -392,7 +616,7 @@ __global__ void __launch_bounds__(1024) k_line_tail(TailDesc<T, CT> d, Scalars* 
           r = fma(Cx[si], x[si + cross], b[si]);
           r = fma(Cx[si - cross], x[si - cross], r);
         }
-        const T inv = T(1) / fma(-a, cpp, dd);
+        const T inv = lrcp(fma(-a, cpp, dd));
         cpp = c * inv;
         dpp = fma(-a, dpp, r) * inv;
         CP[si] = cpp;
@@ -562,6 +786,49 @@ void launch_line(const MgView<T, CT, T>& L, int colour, bool zero, const Scalars
 #undef SCF_LINE
 }
 
+template <class T, class CT>
+void launch_line_factor(const MgView<T, CT, T>& L, const LineFactors<T>& F, cudaStream_t s) {
+  int m = 0;
+  const int th = line_threads(L.nx, &m);
+  const size_t smem = (size_t)8 * th * sizeof(T);
+#define SCF_LF(MM)                                                            \
+  do {                                                                        \
+    auto k = k_line_factor<T, CT, MM>;                                        \
+    allow_max_smem(k);                                                        \
+    launch_k(k, dim3(L.ny), dim3(th), smem, s, L, F);                         \
+  } while (0)
+  if (m == 8) SCF_LF(8);
+  else if (m == 16) SCF_LF(16);
+  else SCF_LF(32);
+#undef SCF_LF
+}
+
+template <class T, class CT>
+void launch_line_solve(const MgView<T, CT, T>& L, const LineFactors<T>& F, int colour, bool zero,
+                       const Scalars* sc, cudaStream_t s) {
+  int m = 0;
+  const int th = line_threads(L.nx, &m);
+  const dim3 g((L.ny - colour + 1) / 2);
+  const size_t smem = (size_t)3 * th * sizeof(T);
+  if (g.x == 0) return;
+#define SCF_LS(MM)                                                             \
+  do {                                                                         \
+    if (zero) {                                                                \
+      auto k = k_line_solve<T, CT, MM, true>;                                  \
+      allow_max_smem(k);                                                       \
+      launch_k(k, g, dim3(th), smem, s, L, F, colour, sc);                     \
+    } else {                                                                   \
+      auto k = k_line_solve<T, CT, MM, false>;                                 \
+      allow_max_smem(k);                                                       \
+      launch_k(k, g, dim3(th), smem, s, L, F, colour, sc);                     \
+    }                                                                          \
+  } while (0)
+  if (m == 8) SCF_LS(8);
+  else if (m == 16) SCF_LS(16);
+  else SCF_LS(32);
+#undef SCF_LS
+}
+
 template <class E>
 void launch_transpose(const E* src, int nx, int ny, int ps, E* dst, int pd, const Scalars* sc,
                       cudaStream_t s) {
@@ -592,6 +859,11 @@ template void launch_line<double, double>(const MgView<double, double, double>&,
                                           const Scalars*, cudaStream_t);
 template void launch_line<float, __nv_bfloat16>(const MgView<float, __nv_bfloat16, float>&, int,
                                                 bool, const Scalars*, cudaStream_t);
+template void launch_line_factor<double, double>(const MgView<double, double, double>&,
+                                                const LineFactors<double>&, cudaStream_t);
+template void launch_line_solve<double, double>(const MgView<double, double, double>&,
+                                               const LineFactors<double>&, int, bool,
+                                               const Scalars*, cudaStream_t);
 template void launch_transpose<double>(const double*, int, int, int, double*, int,
                                        const Scalars*, cudaStream_t);
 template void launch_transpose<float>(const float*, int, int, int, float*, int, const Scalars*,

@@ -84,6 +84,20 @@ void launch_line(const MgView<T, CT, T>& L, int colour, bool zero, const Scalars
 template <class E>
 void launch_transpose(const E* src, int nx, int ny, int ps, E* dst, int pd, const Scalars* sc,
                       cudaStream_t s);
+// factored line relaxation (FP64 levels): factors of every line of a level
+// (per cell: level-shaped padded arrays; per thread: thr[row][nth][slots])
+template <class T>
+struct LineFactors {
+  T *inv, *ga, *cp, *S, *tr;
+  T* thr;
+  int nth;  // threads per line
+};
+constexpr int kLineThreadSlots = 23;  // 3 + 2 x 10 reduction steps
+template <class T, class CT>
+void launch_line_factor(const MgView<T, CT, T>& L, const LineFactors<T>& F, cudaStream_t s);
+template <class T, class CT>
+void launch_line_solve(const MgView<T, CT, T>& L, const LineFactors<T>& F, int colour, bool zero,
+                       const Scalars* sc, cudaStream_t s);
 template <class T, class CT>
 void launch_resid_restrict_l(const MgView<T, CT, T>& L, const MgView<T, CT, T>& C,
                              const Scalars* sc, cudaStream_t s);

@@ -62,6 +62,8 @@ struct scf_proj {
   TailDesc<float, bf16> ltail32{};
   std::vector<MgD> t64;
   std::vector<MgF> t32;
+  // FP64 line factors of the kernel levels: [level][0 natural, 1 transposed]
+  std::vector<LineFactors<double>> lf64n, lf64t;
   unsigned* aspect_bits = nullptr;  // device: largest cell aspect ratio (float bits)
   // learned preconditioner (SCF_PRECOND_LEARNED): network and its residual scale
   UNet* net = nullptr;
@@ -271,22 +273,33 @@ void enqueue_vcycle_line_t(scf_proj* h, ViewFn view, TViewFn tview, const TailDe
   auto from_t = [&](const V& f, const V& ft) {
     launch_transpose<T>(ft.x, ft.nx, ft.ny, ft.pitch, f.x, f.pitch, sc, s);
   };
+  // one pass: factored on FP64 levels that have factors, else the full solve
+  auto pass = [&](int l, bool tr, int colour, bool zero) {
+    const V L = tr ? tview(l) : view(l);
+    if constexpr (std::is_same<T, double>::value) {
+      if (l < (int)h->lf64n.size()) {
+        launch_line_solve<double, double>(L, tr ? h->lf64t[l] : h->lf64n[l], colour, zero, sc, s);
+        return;
+      }
+    }
+    launch_line(L, colour, zero, sc, s);
+  };
   auto step = [&](int l, bool post, bool zero) {
     const V f = view(l), ft = tview(l);
     if (!post) {
-      launch_line(f, 0, zero, sc, s);
-      launch_line(f, 1, false, sc, s);
+      pass(l, false, 0, zero);
+      pass(l, false, 1, false);
       to_t(f, ft);
-      launch_line(ft, 0, false, sc, s);
-      launch_line(ft, 1, false, sc, s);
+      pass(l, true, 0, false);
+      pass(l, true, 1, false);
       from_t(f, ft);
     } else {
       to_t(f, ft);
-      launch_line(ft, 1, false, sc, s);
-      launch_line(ft, 0, false, sc, s);
+      pass(l, true, 1, false);
+      pass(l, true, 0, false);
       from_t(f, ft);
-      launch_line(f, 1, false, sc, s);
-      launch_line(f, 0, false, sc, s);
+      pass(l, false, 1, false);
+      pass(l, false, 0, false);
     }
   };
   // levels 0 .. lk-1 run as kernels; the tail (or the coarse solve) covers lk .. L-1
@@ -374,6 +387,10 @@ void enqueue_setup(scf_proj* h, Scalars* sc, cudaStream_t s) {
       std::vector<MgD> nat;
       for (size_t l = 0; l < h->lev.size(); ++l) nat.push_back(view64(h, l));
       enqueue_line_setup_t(nat, h->t64, s);
+      for (size_t l = 0; l < h->lf64n.size(); ++l) {
+        launch_line_factor<double, double>(nat[l], h->lf64n[l], s);
+        launch_line_factor<double, double>(h->t64[l], h->lf64t[l], s);
+      }
     }
   }
 }
@@ -396,6 +413,23 @@ int alloc_line(scf_proj* h) {
       v.cE = ce; v.cN = cn; v.dg = dg; v.di = di; v.x = x; v.b = b;
       v.xin = nullptr; v.csp = nullptr;
       h->t64.push_back(v);
+      // factors of the levels relaxed by kernels (the tail solves its own lines)
+      const int lk = h->ltail0 > 0 ? h->ltail0 : (int)h->lev.size() - 1;
+      if ((int)l < lk) {
+        auto factors = [&](int rows, int len, int pitch, LineFactors<double>* F) {
+          F->nth = line_threads(len, nullptr);
+          double** arr[5] = {&F->inv, &F->ga, &F->cp, &F->S, &F->tr};
+          for (auto a : arr)
+            if (int e = level_array(h, rows, pitch, a)) return e;
+          return dev_alloc(h, (void**)&F->thr,
+                           sizeof(double) * (size_t)rows * F->nth * kLineThreadSlots);
+        };
+        LineFactors<double> fn{}, ft{};
+        if ((rc = factors(ny, nx, h->lev[l].pitch, &fn)) || (rc = factors(nx, ny, pt, &ft)))
+          return rc;
+        h->lf64n.push_back(fn);
+        h->lf64t.push_back(ft);
+      }
     } else {
       MgF v{};
       v.nx = ny; v.ny = nx; v.pitch = pt;
