@@ -59,7 +59,7 @@ struct Scalars {
 enum Ticket { T_RHS = 0, T_RZ, T_PQ, T_RR, T_RES, T_MRES, T_DOT };
 
 // status codes written by the device (mirror scf_proj.h)
-constexpr int kOk = 0, kErrNaN = -3, kErrNotConverged = -4;
+constexpr int kOk = 0, kErrNaN = -3, kErrNotConverged = -4, kErrTimeout = -6;
 
 __host__ __device__ inline size_t fo1(int nx, int i, int j) {  // (1:nx,1:ny)
   return (size_t)(i - 1) + (size_t)(j - 1) * (size_t)nx;
@@ -93,9 +93,14 @@ inline cudaError_t allow_max_smem(F* kernel) {
   int dev = 0, optin = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  // the kernel's own static shared memory counts against the same limit
+  cudaFuncAttributes fa;
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, reinterpret_cast<const void*>(kernel));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(reinterpret_cast<const void*>(kernel),
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             optin - (int)fa.sharedSizeBytes);
+  if (e != cudaSuccess) (void)cudaGetLastError();  // the launch reports what matters
   return e;
 }
 

@@ -17,6 +17,7 @@
 //             the coarse right-hand side (needs a 3-cell halo)
 //   RZ        r.z (and r.z_old for the flexible PCG) reduced over the grid,
 //             then the PCG beta
+#include <cstdio>
 #include <cstdlib>
 #include <type_traits>
 
@@ -198,6 +199,201 @@ k_sweep(MgView<T, CT, BT> L, MgView<T, CT, T> C, T omega, int flexible, Scalars*
     }
   }
 
+  if (RZ) {
+    double tot1, tot2;
+    if (grid_sum2((double)a1, 0.0, part, &sc->tickets[T_RZ], &tot1, &tot2) && t == 0)
+      set_beta(sc, tot1, flexible);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// TMA-staged sweep (FP32/BF16 levels).  The same fused red-black iterations
+// as k_sweep, in the same arithmetic order, but every operand of the tile's
+// window -- x, b, the inverse diagonal and both BF16 couplings over 80 x 42
+// cells around the 64 x 32 tile -- arrives by one bulk tensor copy per array
+// (cp.async.bulk.tensor, completion counted in bytes on an mbarrier), so the
+// whole window is in flight at once and the colour phases read shared
+// memory only.  Cells outside the grid arrive as zeros (the ghost values).
+// The wait on the mbarrier is bounded: past the limit the kernel records a
+// timeout, waits (bounded again) for its copies to land, and returns.
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// 2-D tile of the tensor map at `map` (generic address of global memory)
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
+      : "memory");
+}
+
+constexpr int kBoxCells = kSweepBoxX * kSweepBoxY;
+constexpr int kBoxF32 = kBoxCells * 4, kBoxBF16 = kBoxCells * 2;  // bytes per window copy
+constexpr int r128(int b) { return (b + 127) / 128 * 128; }
+// window regions at 128-byte aligned offsets from a 128-byte aligned base
+constexpr int kOffB = r128(kBoxF32), kOffD = 2 * r128(kBoxF32), kOffE = 3 * r128(kBoxF32);
+constexpr int kOffN = kOffE + r128(kBoxBF16), kOffBar = kOffN + r128(kBoxBF16);
+constexpr int kTmaSmem = 128 + kOffBar + 16;  // + slack to align the base
+constexpr int kMbarSpins = 1 << 20;
+
+template <int FIRST, bool ZERO, bool PROLONG, bool RESTRICT, bool RZ, int ITER>
+__global__ void __launch_bounds__(NT)
+k_sweep_tma(MgView<float, __nv_bfloat16, float> L, MgView<float, __nv_bfloat16, float> C,
+            float omega, int flexible, Scalars* sc, double* part, const CUtensorMap* maps,
+            int xin) {
+  pdl_wait();
+  if (sc->done) return;
+  constexpr int H = 2 * ITER + (RESTRICT ? 1 : 0);  // halo of the colour phases (<= 5)
+  constexpr int OX = 8, OY = 5;                     // window origin relative to the tile
+  extern __shared__ __align__(128) unsigned char tsm_raw[];
+  unsigned char* tsm = tsm_raw + ((128u - (smem_addr(tsm_raw) & 127u)) & 127u);
+  float* xw = reinterpret_cast<float*>(tsm);  // [kSweepBoxY][kSweepBoxX]
+  float* bw = reinterpret_cast<float*>(tsm + kOffB);
+  float* dw = reinterpret_cast<float*>(tsm + kOffD);
+  __nv_bfloat16* ew = reinterpret_cast<__nv_bfloat16*>(tsm + kOffE);
+  __nv_bfloat16* nw = reinterpret_cast<__nv_bfloat16*>(tsm + kOffN);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tsm + kOffBar);
+  const int nx = L.nx, ny = L.ny;
+  const int x0 = blockIdx.x * SX, y0 = blockIdx.y * SY;
+  const int wx0 = x0 - OX, wy0 = y0 - OY;  // window origin (x: a multiple of 8)
+  const int t = tlin();
+  const float cs = L.csp ? __ldg(L.csp) : 1.0f;
+  if (t == 0) {
+    mbar_init(bar, 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  if (t == 0) {
+    mbar_expect_tx(bar, (ZERO ? 0u : (unsigned)kBoxF32) + 2u * kBoxF32 + 2u * kBoxBF16);
+    if (!ZERO) tma_load_2d(xw, maps + xin, wx0, wy0, bar);
+    tma_load_2d(bw, maps + 2, wx0, wy0, bar);
+    tma_load_2d(dw, maps + 3, wx0, wy0, bar);
+    tma_load_2d(ew, maps + 4, wx0, wy0, bar);
+    tma_load_2d(nw, maps + 5, wx0, wy0, bar);
+  }
+  if (ZERO)
+    for (int e = t; e < kBoxCells; e += NT) xw[e] = 0.0f;
+  // PROLONG: the coarse values of the tile plus its H-cell ring, read while
+  // the window is in flight
+  constexpr int PW = SX + 2 * H, PH = SY + 2 * H, KP = PROLONG ? (PW * PH + NT - 1) / NT : 1;
+  float cx[KP];
+  if (PROLONG) {
+#pragma unroll
+    for (int k = 0; k < KP; ++k) {
+      const int e = t + k * NT;
+      const int gx = x0 - H + e % PW, gy = y0 - H + e / PW;
+      cx[k] = (e < PW * PH && gx >= 0 && gx < nx && gy >= 0 && gy < ny)
+                  ? C.x[(size_t)(gy >> 1) * C.pitch + (gx >> 1)]
+                  : 0.0f;
+    }
+  }
+  bool ok = false;
+  for (int it = 0; it < kMbarSpins && !ok; ++it) ok = mbar_try_wait(bar, 0);
+  if (!ok) {  // record, let the copies land (bounded), leave
+    if (t == 0) {
+      sc->status = kErrTimeout;
+      sc->done = 1;
+    }
+    for (int it = 0; it < kMbarSpins && !mbar_try_wait(bar, 0); ++it) {
+    }
+    return;
+  }
+  __syncthreads();
+  auto W = [&](int gx, int gy) { return (gy - wy0) * kSweepBoxX + (gx - wx0); };
+  if (PROLONG) {
+#pragma unroll
+    for (int k = 0; k < KP; ++k) {
+      const int e = t + k * NT;
+      const int gx = x0 - H + e % PW, gy = y0 - H + e / PW;
+      if (e < PW * PH && gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
+        const int w = W(gx, gy);
+        if (dw[w] > 0.0f) xw[w] = fmaf(omega, cx[k], xw[w]);
+      }
+    }
+    __syncthreads();
+  }
+  auto relax = [&](int gx, int gy) {
+    const int w = W(gx, gy);
+    float s = bw[w];
+    s = fmaf(__bfloat162float(ew[w]) * cs, xw[w + 1], s);
+    s = fmaf(__bfloat162float(ew[w - 1]) * cs, xw[w - 1], s);
+    s = fmaf(__bfloat162float(nw[w]) * cs, xw[w + kSweepBoxX], s);
+    s = fmaf(__bfloat162float(nw[w - kSweepBoxX]) * cs, xw[w - kSweepBoxX], s);
+    xw[w] = s * dw[w];
+  };
+#pragma unroll
+  for (int q = 0; q < 2 * ITER; ++q) {
+    const int colour = (q & 1) ? 1 - FIRST : FIRST;
+    const int R = H - 1 - q;
+    const int CW = (SX + 2 * R) / 2, RH = SY + 2 * R;
+    for (int e = t; e < CW * RH; e += NT) {
+      const int k = e % CW, ey = e / CW;
+      const int gy = y0 - R + ey;
+      const int gx = x0 - R + ((x0 - R + gy + colour) & 1) + 2 * k;
+      if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) relax(gx, gy);
+    }
+    __syncthreads();
+  }
+  const int P = L.pitch;
+  float a1 = 0.0f;
+  for (int e = t; e < SX * SY; e += NT) {
+    const int gx = x0 + e % SX, gy = y0 + e / SX;
+    if (gx < nx && gy < ny) {
+      const int w = W(gx, gy);
+      const float v = xw[w];
+      L.x[(size_t)gy * P + gx] = v;
+      if (RZ) a1 = fmaf(bw[w], v, a1);
+    }
+  }
+  if (RESTRICT) {
+    const int I0 = x0 >> 1, J0 = y0 >> 1;
+    for (int e = t; e < (SX / 2) * (SY / 2); e += NT) {
+      const int I = I0 + e % (SX / 2), J = J0 + e / (SX / 2);
+      if (I >= C.nx || J >= C.ny) continue;
+      float s = 0.0f;
+      for (int dj = 0; dj < 2; ++dj)
+        for (int dq = 0; dq < 2; ++dq) {
+          const int gx = 2 * I + dq, gy = 2 * J + dj;
+          if (gx >= nx || gy >= ny) continue;
+          const float d = L.dg[(size_t)gy * P + gx];
+          if (d < 0.0f) continue;
+          const int w = W(gx, gy);
+          float r = fmaf(-d, xw[w], bw[w]);
+          r = fmaf(__bfloat162float(ew[w]) * cs, xw[w + 1], r);
+          r = fmaf(__bfloat162float(ew[w - 1]) * cs, xw[w - 1], r);
+          r = fmaf(__bfloat162float(nw[w]) * cs, xw[w + kSweepBoxX], r);
+          r = fmaf(__bfloat162float(nw[w - kSweepBoxX]) * cs, xw[w - kSweepBoxX], r);
+          s += r;
+        }
+      C.b[(size_t)J * C.pitch + I] = s;
+    }
+  }
   if (RZ) {
     double tot1, tot2;
     if (grid_sum2((double)a1, 0.0, part, &sc->tickets[T_RZ], &tot1, &tot2) && t == 0)
@@ -644,6 +840,82 @@ void launch_max_coupling(const LevelView& L, unsigned* out_bits, cudaStream_t s)
 void launch_to_mixed(const LevelView& F, const MgView<float, __nv_bfloat16, float>& M,
                      const unsigned* max_bits, float* cscale_out, cudaStream_t s) {
   launch_k(k_to_mixed, small_grid(F.nx, F.ny), dim3(32, 8), 0, s, F, M, max_bits, cscale_out);
+}
+
+void launch_sweep_tma(const MgView<float, __nv_bfloat16, float>& L,
+                      const MgView<float, __nv_bfloat16, float>& C, const CUtensorMap* maps,
+                      int xin, int first, bool zero, bool prolong, bool restrict_, bool rz,
+                      double omega, int flexible, Scalars* sc, double* part, cudaStream_t s,
+                      int iters) {
+  const dim3 g = tiles(L.nx, L.ny);
+  const float om = (float)omega;
+#define SCF_TSWEEP(F, Z, PR, RS, R)                                                        \
+  do {                                                                                     \
+    if (iters == 2) {                                                                      \
+      auto k = k_sweep_tma<F, Z, PR, RS, R, 2>;                                            \
+      allow_max_smem(k);                                                                   \
+      launch_k(k, g, dim3(NT), (size_t)kTmaSmem, s, L, C, om, flexible, sc, part, maps, xin); \
+    } else {                                                                               \
+      auto k = k_sweep_tma<F, Z, PR, RS, R, 1>;                                            \
+      allow_max_smem(k);                                                                   \
+      launch_k(k, g, dim3(NT), (size_t)kTmaSmem, s, L, C, om, flexible, sc, part, maps, xin); \
+    }                                                                                      \
+  } while (0)
+  if (first == 0 && zero && !prolong && !restrict_ && !rz) SCF_TSWEEP(0, true, false, false, false);
+  else if (first == 0 && zero && !prolong && restrict_ && !rz) SCF_TSWEEP(0, true, false, true, false);
+  else if (first == 0 && !zero && !prolong && restrict_ && !rz) SCF_TSWEEP(0, false, false, true, false);
+  else if (first == 0 && !zero && !prolong && !restrict_ && !rz) SCF_TSWEEP(0, false, false, false, false);
+  else if (first == 1 && !zero && prolong && !restrict_ && !rz) SCF_TSWEEP(1, false, true, false, false);
+  else if (first == 1 && !zero && prolong && !restrict_ && rz) SCF_TSWEEP(1, false, true, false, true);
+  else if (first == 1 && !zero && !prolong && !restrict_ && !rz) SCF_TSWEEP(1, false, false, false, false);
+  else if (first == 1 && !zero && !prolong && !restrict_ && rz) SCF_TSWEEP(1, false, false, false, true);
+#undef SCF_TSWEEP
+}
+
+namespace {
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return (EncodeTiledFn) nullptr;
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+bool encode2d(CUtensorMap* m, const void* base, CUtensorMapDataType dt, int esize, int nx, int ny,
+              int pitch) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  // base 16-byte aligned, row stride a multiple of 16 bytes; the box rows are
+  // 80 x 4 and 80 x 2 bytes, multiples of 16
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || ((size_t)pitch * esize) % 16) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)nx, (cuuint64_t)ny};
+  const cuuint64_t strides[1] = {(cuuint64_t)pitch * esize};
+  const cuuint32_t box[2] = {(cuuint32_t)kSweepBoxX, (cuuint32_t)kSweepBoxY};
+  const cuuint32_t es[2] = {1, 1};
+  return fn(m, dt, 2, const_cast<void*>(base), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+         CUDA_SUCCESS;
+}
+}  // namespace
+
+bool make_sweep_maps(const MgView<float, __nv_bfloat16, float>& L, float* const xbuf[2],
+                     const float* b, CUtensorMap* m) {
+  const int nx = L.nx, ny = L.ny, P = L.pitch;
+  return encode2d(&m[0], xbuf[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, nx, ny, P) &&
+         encode2d(&m[1], xbuf[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, nx, ny, P) &&
+         encode2d(&m[2], b, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, nx, ny, P) &&
+         encode2d(&m[3], L.di, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, nx, ny, P) &&
+         encode2d(&m[4], L.cE, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nx, ny, P) &&
+         encode2d(&m[5], L.cN, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nx, ny, P);
 }
 
 #define SCF_INST(T, CT, BT)                                                                   \

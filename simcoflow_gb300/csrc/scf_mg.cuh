@@ -1,6 +1,8 @@
 // scf_mg.cuh -- multigrid level views and launchers shared by scf_mg.cu and
 // the host side.
 #pragma once
+#include <cuda.h>
+
 #include "scf_internal.cuh"
 
 namespace scf {
@@ -55,6 +57,22 @@ template <class T, class CT>
 void launch_line_tail(const TailDesc<T, CT>& d, Scalars* sc, cudaStream_t s);
 template <class T, class CT>
 void launch_tail(const TailDesc<T, CT>& d, Scalars* sc, cudaStream_t s);
+
+// TMA-staged sweep of FP32/BF16 levels.  Per level, six tensor maps live in
+// device memory (64-byte aligned): the two iterate buffers, b, the inverse
+// diagonal, cE, cN.  Dims (nx, ny), row stride = pitch, box kSweepBoxX x
+// kSweepBoxY; cells outside the grid read as zero.
+constexpr int kSweepBoxX = 80, kSweepBoxY = 42;  // 64x32 tile + 8 / 5 cells around
+constexpr int kSweepMaps = 6;                    // x0, x1, b, di, cE, cN
+// encodes the six maps into host memory; false when the driver has no tensor
+// maps or refuses one
+bool make_sweep_maps(const MgView<float, __nv_bfloat16, float>& L, float* const xbuf[2],
+                     const float* b, CUtensorMap* maps);
+void launch_sweep_tma(const MgView<float, __nv_bfloat16, float>& L,
+                      const MgView<float, __nv_bfloat16, float>& C, const CUtensorMap* maps,
+                      int xin, int first, bool zero, bool prolong, bool restrict_, bool rz,
+                      double omega, int flexible, Scalars* sc, double* part, cudaStream_t s,
+                      int iters);
 
 // One fused launch of `iters` (1 or 2) red-black iterations on level L.
 template <class T, class CT, class BT>

@@ -49,6 +49,10 @@ struct scf_proj {
   // mixed levels (FP32 state, BF16 couplings), built from lev at assemble
   std::vector<MgF> mix;
   float* r32 = nullptr;  // FP32 copy of the PCG residual (mixed)
+  // device tensor maps of the TMA-staged sweep, kSweepMaps per mixed level
+  // (tma[l]: the level uses it)
+  std::vector<CUtensorMap*> dmaps;
+  std::vector<char> tma;
   // single-CTA tail of the V-cycle: levels tail0 .. L-1 (tail0 = 0: none)
   int tail0 = 0;
   TailDesc<double, double> tail64{};
@@ -161,6 +165,13 @@ MgD view64(scf_proj* h, int l) {
 double* buf64(scf_proj* h, int l, int i) { return i == 0 ? h->lev[l].x : h->x2_64[l]; }
 float* buf32(scf_proj* h, int l, int i) { return i == 0 ? h->mix[l].x : h->x2_32[l]; }
 
+// the TMA-staged sweep runs on mixed levels of at least 128 x 64 cells whose
+// tensor maps were accepted (SCF_NO_TMA turns it off)
+bool tma_level(const scf_proj* h, int l) {
+  static const bool off = getenv("SCF_NO_TMA") != nullptr;
+  return !off && l < (int)h->tma.size() && h->tma[l];
+}
+
 // Largest level handled by the single-CTA tails (SCF_TAIL_CELLS overrides
 // kTailMaxCells, for tuning; shared memory bounds it in any case).
 long tail_cells() {
@@ -231,6 +242,13 @@ void enqueue_vcycle_t(scf_proj* h, ViewFn view, BufFn buf, const TailDesc<T, CT>
     for (int it = 0; it < npre; ++it) {
       f.xin = it > 0 ? buf(l, (it - 1) % 2) : nullptr;
       f.x = buf(l, it % 2);
+      if constexpr (std::is_same<T, float>::value) {
+        if (tma_level(h, l)) {
+          launch_sweep_tma(f, c, h->dmaps[l], it > 0 ? (it - 1) % 2 : 0, 0, it == 0, false,
+                           it == npre - 1, false, om, flexible, sc, h->part, s, pre[it]);
+          continue;
+        }
+      }
       launch_sweep(f, c, 0, it == 0, false, it == npre - 1, false, om, flexible, sc, h->part, s,
                    pre[it]);
     }
@@ -249,6 +267,13 @@ void enqueue_vcycle_t(scf_proj* h, ViewFn view, BufFn buf, const TailDesc<T, CT>
       f.xin = buf(l, (npre - 1 + it) % 2);
       f.x = buf(l, (npre + it) % 2);
       const bool rz = l == 0 && do_rz && it == npost - 1;
+      if constexpr (std::is_same<T, float>::value) {
+        if (tma_level(h, l)) {
+          launch_sweep_tma(f, c, h->dmaps[l], (npre - 1 + it) % 2, 1, false, it == 0, false, rz,
+                           om, flexible, sc, h->part, s, post[it]);
+          continue;
+        }
+      }
       launch_sweep(f, c, 1, false, it == 0, false, rz, om, flexible, sc, h->part, s, post[it]);
     }
   }
@@ -904,6 +929,23 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
       h->x2_32.push_back(x2);
     }
     if ((rc = level_array(h, ny, h->lev[0].pitch, &h->r32))) return fail(rc);
+    // tensor maps of the TMA-staged sweep (levels of at least 128 x 64 cells),
+    // encoded on the host, kept in device memory
+    h->dmaps.assign(nlev, nullptr);
+    h->tma.assign(nlev, 0);
+    for (int l = 0; l < nlev; ++l) {
+      const MgF& M = h->mix[l];
+      if (M.nx < 128 || M.ny < 64) continue;
+      alignas(64) CUtensorMap hm[kSweepMaps];
+      float* const xb[2] = {buf32(h, l, 0), buf32(h, l, 1)};
+      if (!make_sweep_maps(M, xb, l == 0 ? h->r32 : M.b, hm)) continue;
+      if ((rc = dev_alloc(h, (void**)&h->dmaps[l], sizeof(hm)))) return fail(rc);
+      if (cudaMemcpyAsync(h->dmaps[l], hm, sizeof(hm), cudaMemcpyHostToDevice, h->stream) !=
+              cudaSuccess ||
+          cudaStreamSynchronize(h->stream) != cudaSuccess)
+        return fail(SCF_ERR_CUDA);
+      h->tma[l] = 1;
+    }
   }
   const int P0 = h->lev[0].pitch;
   double** pv[5] = {&h->xsol, &h->pA, &h->pB, &h->q, &h->bvec};
@@ -1207,7 +1249,12 @@ int scf_proj_time_kernel(scf_proj* h, int kernel, int reps, double* ms) {
       V.xin = buf32(h, 0, 0);
       V.x = buf32(h, 0, 1);
       V.b = h->r32;
-      launch_sweep(V, h->mix[1], first, false, prol, restr, false, om, 1, h->sc_diag, h->part, s);
+      if (tma_level(h, 0))
+        launch_sweep_tma(V, h->mix[1], h->dmaps[0], 0, first, false, prol, restr, false, om, 1,
+                         h->sc_diag, h->part, s, 1);
+      else
+        launch_sweep(V, h->mix[1], first, false, prol, restr, false, om, 1, h->sc_diag, h->part,
+                     s);
     }
     (void)smooth;
   };

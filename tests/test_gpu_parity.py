@@ -260,3 +260,33 @@ def test_full_size_c2(cuda, oracle):
     assert np.array_equal(gm["Pp"], gm2["Pp"]) and gm["stats"]["iters"] == gm2["stats"]["iters"]
     g3 = _gpu_project(c, rtol=1e-8, maxit=200)
     assert np.array_equal(g["Pp"], g3["Pp"])
+
+
+_TMA_PROBE = r'''
+import sys, numpy as np
+sys.path.insert(0, sys.argv[1])
+from simcoflow_gb300 import synth, projection as P
+c = synth.c4(n=330, instance=5)
+g = P.project_case(c, precision="mixed", rtol=1e-10, maxit=300)
+np.save(sys.argv[2] + "_Pp.npy", g["Pp"])
+np.save(sys.argv[2] + "_it.npy", np.array([g["stats"]["iters"]]))
+'''
+
+
+def test_tma_staged_sweep_matches_plain_sweep(cuda, tmp_path):
+    """The TMA-staged sweep (bulk tensor copies of the tile window) computes
+    the same cell updates in the same order as the sweep that loads through
+    the cache hierarchy: results are bit-identical (330^2: partial tiles)."""
+    import os
+    import subprocess
+    import sys
+    from helpers import GOLDEN
+    root = str(GOLDEN.parent.parent)
+    for tag, env in (("tma", {}), ("plain", {"SCF_NO_TMA": "1"})):
+        e = dict(os.environ)
+        e.update(env)
+        r = subprocess.run([sys.executable, "-c", _TMA_PROBE, root, str(tmp_path / tag)], env=e,
+                           capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr[-2000:]
+    assert np.array_equal(np.load(tmp_path / "tma_Pp.npy"), np.load(tmp_path / "plain_Pp.npy"))
+    assert np.load(tmp_path / "tma_it.npy")[0] == np.load(tmp_path / "plain_it.npy")[0]
