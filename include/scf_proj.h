@@ -102,6 +102,9 @@ typedef struct scf_stats {
     double ms_h2d, ms_assemble, ms_solve, ms_correct, ms_d2h, ms_total;
     int smoother;       /* SCF_SMOOTH_POINT or SCF_SMOOTH_LINE: the smoother used */
     int learned_iters;  /* iterations preconditioned by the network (SCF_PRECOND_LEARNED) */
+    int launches;       /* kernel launches of this call, graph nodes counted per
+                           execution, including those of the assembly before it */
+    int reserved_i;
 } scf_stats;
 
 typedef struct scf_proj scf_proj;

@@ -84,6 +84,11 @@ __device__ __forceinline__ void pdl_wait() {
 // PDL is on unless SCF_NO_PDL is set in the environment.
 bool pdl_enabled();
 
+// Kernel launches issued by this host thread (direct launches and launches
+// recorded into a graph under capture); the solver reports per-call counts.
+extern thread_local long long g_launches;
+inline void note_launch() { ++g_launches; }
+
 // Allow a kernel the device's whole opt-in dynamic shared memory.  The
 // attribute belongs to the function, not to a launch: graphs of several
 // handles capture launches of the same kernel with different sizes, so it
@@ -118,6 +123,7 @@ inline void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t sme
   cfg.attrs = at;
   cfg.numAttrs = pdl_enabled() ? 1 : 0;
   cudaLaunchKernelEx(&cfg, kernel, args...);
+  note_launch();
 }
 
 // launch geometry: 2 cells per thread in x, rows looped with a grid stride

@@ -853,6 +853,7 @@ void launch_prolong_l(const MgView<T, CT, T>& L, const T* xc, int pc, double ome
 void launch_aspect(const double* dx, const double* dy, size_t n, unsigned* out_bits,
                    cudaStream_t s) {
   k_aspect<<<304, 256, 0, s>>>(dx, dy, n, out_bits);
+  note_launch();
 }
 
 template void launch_line<double, double>(const MgView<double, double, double>&, int, bool,

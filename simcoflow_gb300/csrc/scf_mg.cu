@@ -769,6 +769,8 @@ bool pdl_enabled() {
   return on;
 }
 
+thread_local long long g_launches = 0;
+
 static dim3 tiles(int nx, int ny) { return dim3((nx + SX - 1) / SX, (ny + SY - 1) / SY); }
 static dim3 small_grid(int nx, int ny) {
   int gy = (ny + 7) / 8;

@@ -108,6 +108,9 @@ struct scf_proj {
   bool graph_cond = false;              // true: conditional while-node graph
   cudaGraph_t body_graph = nullptr;
   cudaGraphExec_t body_exec = nullptr;  // fallback: body only, host-polled
+  long long body_launches = 0;          // kernel nodes of one loop body (two iterations)
+  long long body_runs = 0;              // host-polled body graph launches of this solve
+  long long pending_launches = 0;       // launches of an assembly not yet reported
 
   cudaEvent_t ev[8];
 };
@@ -526,7 +529,9 @@ int build_graph(scf_proj* h) {
       cudaGraphDestroy(g);
       break;
     }
+    const long long l0 = g_launches;
     enqueue_body(h, (unsigned long long)handle, cs);
+    h->body_launches = g_launches - l0;
     cudaGraph_t captured = nullptr;
     if (cudaStreamEndCapture(cs, &captured) != cudaSuccess) {
       cudaGetLastError();
@@ -547,7 +552,9 @@ int build_graph(scf_proj* h) {
   if (!ok) {  // fallback: graph of the loop body, relaunched and polled from the host
     cudaGetLastError();
     CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed));
+    const long long l0 = g_launches;
     enqueue_body(h, 0ull, cs);
+    h->body_launches = g_launches - l0;
     CK(cudaStreamEndCapture(cs, &h->body_graph));
     CK(cudaGraphInstantiate(&h->body_exec, h->body_graph, 0));
     h->graph_cond = false;
@@ -568,11 +575,13 @@ struct BatchIO {
 };
 
 int add_batch_branch(scf_proj* h, const BatchIO& io, cudaGraph_t g, cudaStream_t cs,
-                     cudaStream_t cs2) {
+                     cudaStream_t cs2, long long* once, long long* body_launches) {
   if (cudaStreamBeginCaptureToGraph(cs, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) !=
       cudaSuccess)
     return SCF_ERR_CUDA;
   int rc = SCF_OK;
+  const long long l0 = g_launches;
+  long long lb = 0;
   do {
     cudaMemsetAsync(h->sc, 0, sizeof(Scalars), cs);
     enqueue_setup(h, h->sc, cs);
@@ -611,7 +620,9 @@ int add_batch_branch(scf_proj* h, const BatchIO& io, cudaGraph_t g, cudaStream_t
       rc = SCF_ERR_CUDA;
       break;
     }
+    const long long b0 = g_launches;
     enqueue_body(h, (unsigned long long)handle, cs2);
+    lb = g_launches - b0;
     cudaGraph_t captured = nullptr;
     if (cudaStreamEndCapture(cs2, &captured) != cudaSuccess) {
       rc = SCF_ERR_CUDA;
@@ -629,6 +640,8 @@ int add_batch_branch(scf_proj* h, const BatchIO& io, cudaGraph_t g, cudaStream_t
     launch_final_zero(h->fin, io.p, io.u, io.v, cs);
     cudaMemcpyAsync(h->sc_host, h->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, cs);
   } while (0);
+  *body_launches = lb;
+  *once = g_launches - l0 - lb;
   cudaGraph_t out = nullptr;
   const cudaError_t e = cudaStreamEndCapture(cs, &out);
   if (rc == SCF_OK && e != cudaSuccess) rc = SCF_ERR_CUDA;
@@ -655,6 +668,7 @@ int run_pcg(scf_proj* h) {
     for (int c = 0; c < chunk && launched < maxit; ++c) {
       if (h->body_exec) {
         CK(cudaGraphLaunch(h->body_exec, h->stream));
+        ++h->body_runs;
       } else {
         enqueue_body(h, 0ull, h->stream);
         CK(cudaGetLastError());
@@ -744,6 +758,8 @@ int solve_common(scf_proj* h, const double* ustar, const double* vstar, double v
   const int nx = h->nx, ny = h->ny;
   const size_t n0 = (size_t)(nx + 2) * (ny + 2), n1 = (size_t)nx * ny;
   cudaStream_t s = h->stream;
+  const long long l0 = g_launches;
+  h->body_runs = 0;
   // host mode: the input copies go on the copy stream, so they overlap the
   // operator setup that assemble left running on the solver stream (the
   // staging buffers are idle: every solve ends with a synchronisation)
@@ -818,7 +834,14 @@ int solve_common(scf_proj* h, const double* ustar, const double* vstar, double v
     st->ms_d2h = elapsed(h->ev[3], h->ev[4]);
     st->ms_total = elapsed(h->ev[0], h->ev[4]);
     st->ms_assemble = 0.0;
+    // direct launches, plus the kernel nodes of every executed loop body
+    // (k_update_xr counts two per body execution in the loop guard)
+    long long n = h->pending_launches + (g_launches - l0);
+    if (h->graph_cond && h->gexec && !learned(h)) n += (long long)(S.pad[0] / 2) * h->body_launches;
+    n += h->body_runs * h->body_launches;
+    st->launches = (int)n;
   }
+  h->pending_launches = 0;
   return status == kOk ? SCF_OK : status;
 }
 
@@ -1140,7 +1163,9 @@ int scf_proj_assemble(scf_proj* h, const double* DpU, const double* DpV, double 
   // host mode: the caller may reuse DpU/DpV once their copies are done
   CK(cudaEventRecord(h->copy_done, s));
   CK(cudaMemsetAsync(h->sc, 0, sizeof(Scalars), s));
+  const long long l0 = g_launches;
   enqueue_setup(h, h->sc, s);
+  h->pending_launches += g_launches - l0;
   CK(cudaGetLastError());
   if (!h->gexec && !h->body_exec && !(h->opts.flags & SCF_FLAG_NO_GRAPH)) {
     if ((rc = build_graph(h))) return rc;
@@ -1276,6 +1301,7 @@ struct scf_batch {
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   float last_ms = 0.0f;
+  std::vector<long long> once, body;  // kernel nodes per branch: outside / inside the loop
 };
 
 int scf_batch_create(scf_batch** out, scf_proj* const* handles, int count) {
@@ -1344,8 +1370,10 @@ int scf_batch_run(scf_batch* b, void* stream, scf_stats* stats) {
     CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&cs2, cudaStreamNonBlocking));
     int rc = SCF_OK;
+    b->once.assign(b->h.size(), 0);
+    b->body.assign(b->h.size(), 0);
     for (size_t i = 0; i < b->h.size() && rc == SCF_OK; ++i)
-      rc = add_batch_branch(b->h[i], b->io[i], g, cs, cs2);
+      rc = add_batch_branch(b->h[i], b->io[i], g, cs, cs2, &b->once[i], &b->body[i]);
     cudaStreamDestroy(cs);
     cudaStreamDestroy(cs2);
     if (rc == SCF_OK && cudaGraphInstantiate(&b->exec, g, 0) != cudaSuccess) rc = SCF_ERR_CUDA;
@@ -1379,6 +1407,7 @@ int scf_batch_run(scf_batch* b, void* stream, scf_stats* stats) {
       st.relres_true = S.bnorm2 > 0 ? sqrt(S.res_true2 / S.bnorm2) : 0.0;
       st.mres_max = S.mres_max;
       st.ms_total = b->last_ms;
+      st.launches = (int)(b->once[i] + (long long)(S.pad[0] / 2) * b->body[i]);
     }
   }
   return worst;
@@ -1443,6 +1472,8 @@ int scf_proj_solve_rhs(scf_proj* h, const double* b, double* x, double* r, int m
     dr = r ? h->st_Pp : nullptr;
   }
   CK(cudaEventRecord(h->ev[1], s));
+  const long long l0 = g_launches;
+  h->body_runs = 0;
   LevelView L0 = h->lev[0];
   CK(cudaMemsetAsync(&h->sc->nan, 0, sizeof(int), s));
   launch_rhs_given(h->nx, h->ny, db, L0, h->bvec, L0.b, h->r32, h->xsol, h->sc, h->part,
@@ -1484,7 +1515,13 @@ int scf_proj_solve_rhs(scf_proj* h, const double* b, double* x, double* r, int m
     st->relres = S.bnorm2 > 0 ? sqrt(S.rr / S.bnorm2) : 0.0;
     st->relres_true = S.bnorm2 > 0 ? sqrt(S.res_true2 / S.bnorm2) : 0.0;
     st->ms_solve = elapsed(h->ev[1], h->ev[2]);
+    long long n = h->pending_launches + (g_launches - l0);
+    if (maxit > 0 && h->graph_cond && h->gexec && !learned(h))
+      n += (long long)(S.pad[0] / 2) * h->body_launches;
+    n += h->body_runs * h->body_launches;
+    st->launches = (int)n;
   }
+  h->pending_launches = 0;
   return status == kOk ? SCF_OK : status;
 }
 

@@ -25,6 +25,11 @@
 #include "scf_unet.cuh"
 
 namespace scf {
+extern thread_local long long g_launches;  // defined with the multigrid launchers
+inline void note_launch() { ++g_launches; }
+}  // namespace scf
+
+namespace scf {
 namespace {
 
 using bf16 = __nv_bfloat16;
@@ -613,6 +618,7 @@ void conv_t(const ConvP& p, int sms, cudaStream_t s) {
   const int tiles = ((p.W + TW - 1) / TW) * ((p.H + TH - 1) / TH) * p.n;
   const int g = tiles < 2 * sms ? tiles : 2 * sms;
   k<<<g, NTH, smem, s>>>(p);
+  note_launch();
 }
 
 // channel pairs of the upsampling decoder layers (64->64, 64->32, 32->16)
@@ -674,6 +680,7 @@ void wgrad_t(const WgP& p, int sms, cudaStream_t s) {
   int g = (2 * sms + 8) / 9;
   if (g > tiles) g = tiles;
   k<<<dim3(g, 9), NTH, smem, s>>>(p);
+  note_launch();
 }
 
 void wgrad_dispatch(int cin, int cout, const WgP& p, bool ups, bool relu, int sms,
@@ -760,6 +767,7 @@ void UNet::refresh_weights(cudaStream_t s) {
     const int nw = l.cout * 9 * l.cin;
     k_weights<<<grid_for(nw, sms_), 256, 0, s>>>(params_ + l.woff, l.cin, l.cout, wb_ + off,
                                                  wt_ + off);
+    note_launch();
     off += nw;
   }
 }
@@ -782,8 +790,10 @@ void UNet::features(int i, int nx, int ny, int ld, const double* r, const double
   float* sums = red_ + 2 * (i % 1024);
   cudaMemsetAsync(sums, 0, 8, s);
   k_feat_sums<<<grid_for((size_t)nx * ny, sms_), 256, 0, s>>>(nx, ny, ld, r, dg, sums);
+  note_launch();
   k_features<<<grid_for((size_t)h_ * w_, sms_), 256, 0, s>>>(
       nx, ny, ld, r, cE, cN, dg, sums, sigma_out, in_ + (size_t)i * h_ * w_ * 16, h_, w_);
+  note_launch();
 }
 
 void UNet::forward(cudaStream_t s) {
@@ -799,6 +809,7 @@ void UNet::forward(cudaStream_t s) {
       const UNetLayer& src = L[i - 1];
       k_pool<<<grid_for((size_t)n_ * H * W * src.cout / 8, sms_), 256, 0, s>>>(
           act_[i - 1], pool_[k], n_, H * 2, W * 2, src.cout);
+      note_launch();
       in = pool_[k];
     } else {
       in = act_[i - 1];
@@ -817,12 +828,14 @@ void UNet::forward(cudaStream_t s) {
   }
   k_head<<<grid_for((size_t)n_ * h_ * w_, sms_), 256, 0, s>>>(
       act_.back(), params_ + num_params() - 17, (size_t)n_ * h_ * w_, z_);
+  note_launch();
 }
 
 void UNet::correction(int nx, int ny, int pitch, const double* dg, const float* sigma, float* x,
                       cudaStream_t s) {
   k_correction<float><<<grid_for((size_t)nx * ny, sms_), 256, 0, s>>>(nx, ny, pitch, w_, dg,
                                                                       sigma, z_, x);
+  note_launch();
 }
 
 // target of image i for training: t = e / sigma (FP32) and the mask dg > 0;
@@ -853,6 +866,7 @@ void UNet::target(int i, int nx, int ny, const double* e, const double* dg, cons
   const size_t hw = (size_t)h_ * w_;
   k_target<<<grid_for(hw, sms_), 256, 0, s>>>(nx, ny, h_, w_, e, dg, sigma, t + i * hw,
                                              mask + i * hw);
+  note_launch();
 }
 
 void UNet::loss(const float* t, const unsigned char* mask, float* loss_dev, cudaStream_t s) {
@@ -861,8 +875,11 @@ void UNet::loss(const float* t, const unsigned char* mask, float* loss_dev, cuda
   cudaMemsetAsync(sums, 0, 2 * n_ * 4, s);
   const dim3 g((unsigned)((grid_for(hw, sms_) + n_ - 1) / n_ + 1), n_);
   k_loss_sums<<<g, 256, 0, s>>>(z_, t, mask, hw, sums);
+  note_launch();
   k_loss_grad<<<g, 256, 0, s>>>(z_, t, mask, hw, sums, dz_);
+  note_launch();
   k_loss_total<<<1, 1, 0, s>>>(sums, n_, loss_dev);
+  note_launch();
 }
 
 void UNet::backward(cudaStream_t s) {
@@ -876,6 +893,7 @@ void UNet::backward(cudaStream_t s) {
   // head: gradient of d0 into g_[0]
   k_head_bwd<<<grid_for(p0, sms_), 256, 0, s>>>(act_.back(), params_ + num_params() - 17, dz_, p0,
                                                 g_[0], grads_ + num_params() - 17);
+  note_launch();
   // g_[0..2] rotate through the layer gradients.  The skip gradients of
   // e0, e1, e2 (outputs of layers 1, 3, 5), set by the decoder's add layers
   // 12, 10, 8, live in g_[3] until the encoder adds them to the gradient of
@@ -930,6 +948,7 @@ void UNet::backward(cudaStream_t s) {
       const int c = other(a, b);
       k_sumpool<<<grid_for((size_t)n_ * H * W * l.cin / 32, sms_), 256, 0, s>>>(
           g_[b], g_[c], n_, H, W, l.cin);
+      note_launch();
       cur = c;
     }
     if (i == 2 || i == 4 || i == 6) {
@@ -939,6 +958,7 @@ void UNet::backward(cudaStream_t s) {
       const int c = other(cur, -1);
       k_unpool_add<<<grid_for((size_t)n_ * (H * 2) * (W * 2) * src.cout / 8, sms_), 256, 0, s>>>(
           gskip[i - 1], g_[cur], g_[c], n_, H * 2, W * 2, src.cout);
+      note_launch();
       cur = c;
     }
     a = cur;
@@ -949,6 +969,7 @@ void UNet::adam(float lr, float b1, float b2, float eps, int step, cudaStream_t 
   const int n = num_params();
   const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
   k_adam<<<grid_for(n, sms_), 256, 0, s>>>(params_, grads_, m_, v_, n, lr, b1, b2, eps, c1, c2);
+  note_launch();
   refresh_weights(s);
 }
 

@@ -64,7 +64,8 @@ class Stats(C.Structure):
                 ("relres_true", C.c_double), ("mres_max", C.c_double), ("ms_h2d", C.c_double),
                 ("ms_assemble", C.c_double), ("ms_solve", C.c_double),
                 ("ms_correct", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double),
-                ("smoother", C.c_int), ("learned_iters", C.c_int)]
+                ("smoother", C.c_int), ("learned_iters", C.c_int), ("launches", C.c_int),
+                ("reserved_i", C.c_int)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

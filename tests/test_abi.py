@@ -40,6 +40,31 @@ def test_geom_library_exports_header_symbols(built):
         assert hasattr(lib, n), n
 
 
+def test_struct_layouts_match_header(tmp_path):
+    """The ctypes mirrors of scf_opts and scf_stats have the header's layout."""
+    import shutil
+    import subprocess
+    if not shutil.which("gcc"):
+        import pytest
+        pytest.skip("no C compiler")
+    from simcoflow_gb300 import projection as P
+    src = tmp_path / "lay.c"
+    fields = [n for n, _ in P.Stats._fields_]
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "scf_proj.h"\n'
+        "int main(void) {\n"
+        '  printf("%zu %zu\\n", sizeof(scf_opts), sizeof(scf_stats));\n'
+        + "".join(f'  printf("%zu\\n", offsetof(scf_stats, {n}));\n' for n in fields)
+        + "  return 0;\n}\n")
+    exe = tmp_path / "lay"
+    subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    assert int(out[0]) == ctypes.sizeof(P.Opts)
+    assert int(out[1]) == ctypes.sizeof(P.Stats)
+    for n, off in zip(fields, out[2:]):
+        assert int(off) == getattr(P.Stats, n).offset, n
+
+
 def test_host_only_entry_points(built):
     from simcoflow_gb300 import projection
     L = projection.load()

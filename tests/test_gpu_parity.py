@@ -114,6 +114,12 @@ def test_deterministic_and_graph_free_path_agree(cuda, precision):
         assert np.array_equal(a[k], b[k]), k
         assert np.array_equal(a[k], n[k]), k
     assert a["stats"]["iters"] == n["stats"]["iters"]
+    # launch counts: the graph loop's executed bodies are counted node by
+    # node; the host-polled path runs whole chunks of bodies, so it launches
+    # at least as many kernels
+    la, ln = a["stats"]["launches"], n["stats"]["launches"]
+    assert la == b["stats"]["launches"]
+    assert 3 * a["stats"]["iters"] < la <= ln
 
 
 _PDL_PROBE = r'''
