@@ -81,6 +81,48 @@ __device__ __forceinline__ void pdl_wait() {
   cudaTriggerProgrammaticLaunchCompletion();
 }
 
+// Format conversions and selections done on the integer pipe.  On GB300 a
+// float <-> double conversion and an FP64 max issue on the FP64 pipe (about
+// two per SM and clock, like an FP64 FMA); the kernels that are bound by that
+// pipe use these bit-level equivalents instead.  Both conversions follow the
+// IEEE-754 binary32/binary64 encodings; the rare operands outside the normal
+// range (zero excepted) take the hardware conversion.
+
+// exact widening float -> double
+__device__ __forceinline__ double f2d_exact(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e - 1u < 254u) {  // normal: rebias the exponent, widen the fraction
+    const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0xfffffu);
+    return __hiloint2double((int)hi, (int)(u << 29));
+  }
+  if ((u << 1) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);  // +-0
+  return (double)f;  // subnormal, infinity, NaN
+}
+
+// double -> float, round to nearest even
+__device__ __forceinline__ float d2f_rn(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  // binary32 normal range before rounding: biased exponent 897 .. 1150
+  if (e - 897u < 254u) {
+    const unsigned sign = hi & 0x80000000u;
+    const unsigned frac = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 fraction bits
+    const unsigned rest = lo & 0x1fffffffu;                     // 29 bits dropped
+    unsigned f = sign | ((e - 896u) << 23) | frac;
+    // ties to even; a carry out of the fraction steps the exponent (up to inf)
+    if (rest > 0x10000000u || (rest == 0x10000000u && (frac & 1u))) f += 1u;
+    return __uint_as_float(f);
+  }
+  if (((hi << 1) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);  // +-0
+  return (float)d;  // below or above the binary32 normal range, infinity, NaN
+}
+
+// max(v, 0) for a v that is not NaN, by the sign bit (-0 gives +0)
+__device__ __forceinline__ double pos_part(double v) {
+  return __double2hiint(v) < 0 ? 0.0 : v;
+}
+
 // PDL is on unless SCF_NO_PDL is set in the environment.
 bool pdl_enabled();
 

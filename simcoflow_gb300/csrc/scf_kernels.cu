@@ -531,7 +531,7 @@ __global__ void k_update_xr(LevelView L, double* __restrict__ x, const double* _
         *reinterpret_cast<double2*>(x + k) = xv;
         *reinterpret_cast<double2*>(r + k) = rv;
         if (r32) {
-          const float2 rf = make_float2((float)rv.x, (float)rv.y);
+          const float2 rf = make_float2(d2f_rn(rv.x), d2f_rn(rv.y));
           *reinterpret_cast<float2*>(r32 + k) = rf;
           if (z32) {
             const float2 zf = *reinterpret_cast<const float2*>(z32 + k);
@@ -543,8 +543,9 @@ __global__ void k_update_xr(LevelView L, double* __restrict__ x, const double* _
         x[k] = xv.x;
         r[k] = rv.x;
         if (r32) {
-          r32[k] = (float)rv.x;
-          if (z32) crs = fmaf((float)rv.x, z32[k], crs);
+          const float rf = d2f_rn(rv.x);
+          r32[k] = rf;
+          if (z32) crs = fmaf(rf, z32[k], crs);
         }
       }
     }

@@ -9,6 +9,9 @@
 // along y run the same kernel on a transposed copy of the level (operator
 // transposed at setup, x and b transposed inside the V-cycle by tiled
 // shared-memory transposes), so every line kernel reads contiguous rows.
+// The residual restriction and the prolongation work on the transposed
+// copy, and the restriction writes both layouts of the coarse right-hand
+// side, so a level costs two transposes of x per V-cycle.
 //
 // A line is solved by one CTA.  Thread t owns M consecutive cells; the last
 // of them is an interface cell, the first M-1 are interior.  Each thread
@@ -497,46 +500,130 @@ k_transpose(const E* __restrict__ src, int nx, int ny, int ps, E* __restrict__ d
   }
 }
 
-// residual of level L summed 2x2 onto the right-hand side of level C
-template <class T, class CT>
+// Transpose of FP32 levels, 64 x 64 cells per CTA with 16-byte vector
+// loads and stores (4 cells).  A row of the padded layout starts on a
+// 128-byte boundary and its pitch is a multiple of 32 cells, so a vector
+// that starts at a multiple of its width stays inside its row; cells past
+// nx (padding and the next row's ghost) hold zeros, are read as such and
+// written back as zeros.
+template <class E>
 __global__ void __launch_bounds__(256)
-k_resid_restrict_l(MgView<T, CT, T> L, MgView<T, CT, T> C, const Scalars* sc) {
+k_transpose_v(const E* __restrict__ src, int nx, int ny, int ps, E* __restrict__ dst, int pd,
+              const Scalars* sc) {
   pdl_wait();
   if (sc && sc->done) return;
-  const int I = blockIdx.x * 32 + threadIdx.x, J = blockIdx.y * 8 + threadIdx.y;
-  if (I >= C.nx || J >= C.ny) return;
-  const float cs = L.csp ? __ldg(L.csp) : 1.0f;
-  const int P = L.pitch;
-  T s = T(0);
+  constexpr int V = 16 / sizeof(E), TS = 64, VR = TS / V;  // vectors per tile row
+  __shared__ E tile[TS][TS + 1];
+  const int bx = blockIdx.x * TS, by = blockIdx.y * TS;
+  const int t = threadIdx.y * 32 + threadIdx.x;
+  for (int e = t; e < TS * VR; e += 256) {
+    const int r = e / VR, c = (e % VR) * V;
+    const int ix = bx + c, iy = by + r;
+    E v[V];
+    if (iy < ny && ix < nx) {
+      const uint4 u = __ldg(reinterpret_cast<const uint4*>(src + (size_t)iy * ps + ix));
+      unpack(u, v);
+    } else {
 #pragma unroll
-  for (int dj = 0; dj < 2; ++dj)
-#pragma unroll
-    for (int dq = 0; dq < 2; ++dq) {
-      const int gx = 2 * I + dq, gy = 2 * J + dj;
-      if (gx >= L.nx || gy >= L.ny) continue;
-      const size_t g = (size_t)gy * P + gx;
-      const T dgv = L.dg[g];
-      if (dgv < T(0)) continue;
-      T rr = fma(-dgv, L.x[g], L.b[g]);
-      rr = fma(lcoef<CT, T>(L.cE, g, cs), L.x[g + 1], rr);
-      rr = fma(lcoef<CT, T>(L.cE, g - 1, cs), L.x[g - 1], rr);
-      rr = fma(lcoef<CT, T>(L.cN, g, cs), L.x[g + P], rr);
-      rr = fma(lcoef<CT, T>(L.cN, g - P, cs), L.x[g - P], rr);
-      s += rr;
+      for (int m = 0; m < V; ++m) v[m] = E(0);
     }
-  C.b[(size_t)J * C.pitch + I] = s;
+#pragma unroll
+    for (int m = 0; m < V; ++m) tile[r][c + m] = v[m];
+  }
+  __syncthreads();
+  for (int e = t; e < TS * VR; e += 256) {
+    const int o = e / VR, c = (e % VR) * V;  // dst row bx + o, dst cells by + c ..
+    const int oy = bx + o, ox = by + c;
+    if (oy >= nx || ox >= ny) continue;
+    E v[V];
+#pragma unroll
+    for (int m = 0; m < V; ++m) v[m] = tile[c + m][o];
+    *reinterpret_cast<uint4*>(dst + (size_t)oy * pd + ox) = pack(v);
+  }
 }
 
-// x += omega * x_coarse(parent) on cells with an unknown
+// Residual of a level summed 2x2 onto the right-hand side of the coarser
+// level, computed on the level's transposed copy Lt (where the last
+// relaxation of the pre-smoothing left the iterate) and written to the
+// coarse level in both layouts (C natural, Ct transposed), so neither needs
+// a transpose.  Lt cell (i, j) is natural cell (j, i); Ct cell (a, b) is C
+// cell (b, a).  Terms are summed in natural order (cells by natural row,
+// then column; couplings east, west, north, south): the result does not
+// depend on the layout the residual is computed in.
 template <class T, class CT>
 __global__ void __launch_bounds__(256)
-k_prolong_l(MgView<T, CT, T> L, const T* __restrict__ xc, int pc, T omega, const Scalars* sc) {
+k_resid_restrict_lt(MgView<T, CT, T> Lt, MgView<T, CT, T> C, MgView<T, CT, T> Ct,
+                    const Scalars* sc) {
   pdl_wait();
   if (sc && sc->done) return;
-  const int ix = blockIdx.x * 32 + threadIdx.x, iy = blockIdx.y * 8 + threadIdx.y;
-  if (ix >= L.nx || iy >= L.ny) return;
-  const size_t g = (size_t)iy * L.pitch + ix;
-  if (L.di[g] > T(0)) L.x[g] = fma(omega, xc[(size_t)(iy >> 1) * pc + (ix >> 1)], L.x[g]);
+  // one coarse cell per thread (a CTA: 32 x 8 coarse cells), so the FP64
+  // residual chains of different cells run side by side
+  __shared__ T tile[8][33];
+  const int a0 = blockIdx.x * 32, b0 = blockIdx.y * 8;
+  const float cs = Lt.csp ? __ldg(Lt.csp) : 1.0f;
+  const int P = Lt.pitch;
+  {
+    const int bb = threadIdx.y;
+    const int a = a0 + threadIdx.x, b = b0 + bb;
+    T s = T(0);
+    if (a < Ct.nx && b < Ct.ny) {
+#pragma unroll
+      for (int dj = 0; dj < 2; ++dj)
+#pragma unroll
+        for (int dq = 0; dq < 2; ++dq) {
+          const int gx = 2 * a + dj, gy = 2 * b + dq;  // natural (2b + dq, 2a + dj)
+          if (gx >= Lt.nx || gy >= Lt.ny) continue;
+          const size_t g = (size_t)gy * P + gx;
+          const T dgv = Lt.dg[g];
+          if (dgv < T(0)) continue;
+          T rr = fma(-dgv, Lt.x[g], Lt.b[g]);
+          rr = fma(lcoef<CT, T>(Lt.cN, g, cs), Lt.x[g + P], rr);
+          rr = fma(lcoef<CT, T>(Lt.cN, g - P, cs), Lt.x[g - P], rr);
+          rr = fma(lcoef<CT, T>(Lt.cE, g, cs), Lt.x[g + 1], rr);
+          rr = fma(lcoef<CT, T>(Lt.cE, g - 1, cs), Lt.x[g - 1], rr);
+          s += rr;
+        }
+      Ct.b[(size_t)b * Ct.pitch + a] = s;
+    }
+    tile[bb][threadIdx.x] = s;
+  }
+  __syncthreads();
+  {
+    const int t = threadIdx.y * 32 + threadIdx.x;
+    const int bb = t % 8, aa = t / 8;
+    const int ix = b0 + bb, iy = a0 + aa;  // C cell (ix, iy) = Ct cell (iy, ix)
+    if (ix < C.nx && iy < C.ny) C.b[(size_t)iy * C.pitch + ix] = tile[bb][aa];
+  }
+}
+
+// x += omega * x_coarse(parent) on cells with an unknown, applied to the
+// transposed copy Lt of a level (where the post-smoothing starts): Lt cell
+// (i, j) is natural cell (j, i), whose parent is coarse cell (j/2, i/2) of
+// the natural coarse level (nxc x nyc, pitch pc).  A 16 x 16 block of coarse
+// values is staged in shared memory for the CTA's 32 x 32 fine cells.
+template <class T, class CT>
+__global__ void __launch_bounds__(256)
+k_prolong_lt(MgView<T, CT, T> Lt, const T* __restrict__ xc, int pc, int nxc, int nyc, T omega,
+             const Scalars* sc) {
+  pdl_wait();
+  if (sc && sc->done) return;
+  __shared__ T ct[16][17];
+  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+  const int t = threadIdx.y * 32 + threadIdx.x;
+  {
+    const int cx = t % 16, cy = t / 16;  // coarse natural (y0/2 + cx, x0/2 + cy)
+    const int ix = (y0 >> 1) + cx, iy = (x0 >> 1) + cy;
+    ct[cy][cx] = (ix < nxc && iy < nyc) ? xc[(size_t)iy * pc + ix] : T(0);
+  }
+  __syncthreads();
+  const int i = x0 + threadIdx.x;
+  if (i >= Lt.nx) return;
+  for (int jj = threadIdx.y; jj < 32; jj += 8) {
+    const int j = y0 + jj;
+    if (j >= Lt.ny) break;
+    const size_t g = (size_t)j * Lt.pitch + i;
+    if (Lt.di[g] > T(0)) Lt.x[g] = fma(omega, ct[threadIdx.x >> 1][jj >> 1], Lt.x[g]);
+  }
 }
 
 // largest aspect ratio max(dx/dy, dy/dx) over the cells, as float bits
@@ -832,22 +919,33 @@ void launch_line_solve(const MgView<T, CT, T>& L, const LineFactors<T>& F, int c
 template <class E>
 void launch_transpose(const E* src, int nx, int ny, int ps, E* dst, int pd, const Scalars* sc,
                       cudaStream_t s) {
-  const dim3 g((nx + 31) / 32, (ny + 31) / 32);
-  launch_k(k_transpose<E>, g, dim3(32, 8), 0, s, src, nx, ny, ps, dst, pd, sc);
+  // FP32: 64 x 64 tiles with vector accesses.  FP64 keeps 32 x 32 scalar
+  // tiles: a 64 x 64 FP64 tile (33 KB of static shared memory) made the
+  // driver hold a shared-memory-heavy L1 split across the PDL-overlapped
+  // line relaxations that follow, whose L1 hit rate it cut (4096^2 stretched
+  // FP64 projection 90 -> 130 ms, with unchanged kernel times in isolation).
+  if constexpr (sizeof(E) == 4) {
+    const dim3 g((nx + 63) / 64, (ny + 63) / 64);
+    launch_k(k_transpose_v<E>, g, dim3(32, 8), 0, s, src, nx, ny, ps, dst, pd, sc);
+  } else {
+    const dim3 g((nx + 31) / 32, (ny + 31) / 32);
+    launch_k(k_transpose<E>, g, dim3(32, 8), 0, s, src, nx, ny, ps, dst, pd, sc);
+  }
 }
 
 template <class T, class CT>
-void launch_resid_restrict_l(const MgView<T, CT, T>& L, const MgView<T, CT, T>& C,
-                             const Scalars* sc, cudaStream_t s) {
-  const dim3 g((C.nx + 31) / 32, (C.ny + 7) / 8);
-  launch_k(k_resid_restrict_l<T, CT>, g, dim3(32, 8), 0, s, L, C, sc);
+void launch_resid_restrict_lt(const MgView<T, CT, T>& Lt, const MgView<T, CT, T>& C,
+                              const MgView<T, CT, T>& Ct, const Scalars* sc, cudaStream_t s) {
+  const dim3 g((Ct.nx + 31) / 32, (Ct.ny + 7) / 8);
+  launch_k(k_resid_restrict_lt<T, CT>, g, dim3(32, 8), 0, s, Lt, C, Ct, sc);
 }
 
 template <class T, class CT>
-void launch_prolong_l(const MgView<T, CT, T>& L, const T* xc, int pc, double omega,
-                      const Scalars* sc, cudaStream_t s) {
-  const dim3 g((L.nx + 31) / 32, (L.ny + 7) / 8);
-  launch_k(k_prolong_l<T, CT>, g, dim3(32, 8), 0, s, L, xc, pc, (T)omega, sc);
+void launch_prolong_lt(const MgView<T, CT, T>& Lt, const MgView<T, CT, T>& C, double omega,
+                       const Scalars* sc, cudaStream_t s) {
+  const dim3 g((Lt.nx + 31) / 32, (Lt.ny + 31) / 32);
+  launch_k(k_prolong_lt<T, CT>, g, dim3(32, 8), 0, s, Lt, (const T*)C.x, C.pitch, C.nx, C.ny,
+           (T)omega, sc);
 }
 
 void launch_aspect(const double* dx, const double* dy, size_t n, unsigned* out_bits,
@@ -871,17 +969,18 @@ template void launch_transpose<float>(const float*, int, int, int, float*, int, 
                                       cudaStream_t);
 template void launch_transpose<__nv_bfloat16>(const __nv_bfloat16*, int, int, int,
                                               __nv_bfloat16*, int, const Scalars*, cudaStream_t);
-template void launch_resid_restrict_l<double, double>(const MgView<double, double, double>&,
-                                                      const MgView<double, double, double>&,
-                                                      const Scalars*, cudaStream_t);
-template void launch_resid_restrict_l<float, __nv_bfloat16>(
+template void launch_resid_restrict_lt<double, double>(const MgView<double, double, double>&,
+                                                       const MgView<double, double, double>&,
+                                                       const MgView<double, double, double>&,
+                                                       const Scalars*, cudaStream_t);
+template void launch_resid_restrict_lt<float, __nv_bfloat16>(
     const MgView<float, __nv_bfloat16, float>&, const MgView<float, __nv_bfloat16, float>&,
-    const Scalars*, cudaStream_t);
-template void launch_prolong_l<double, double>(const MgView<double, double, double>&,
-                                               const double*, int, double, const Scalars*,
-                                               cudaStream_t);
-template void launch_prolong_l<float, __nv_bfloat16>(const MgView<float, __nv_bfloat16, float>&,
-                                                     const float*, int, double, const Scalars*,
-                                                     cudaStream_t);
+    const MgView<float, __nv_bfloat16, float>&, const Scalars*, cudaStream_t);
+template void launch_prolong_lt<double, double>(const MgView<double, double, double>&,
+                                                const MgView<double, double, double>&, double,
+                                                const Scalars*, cudaStream_t);
+template void launch_prolong_lt<float, __nv_bfloat16>(const MgView<float, __nv_bfloat16, float>&,
+                                                      const MgView<float, __nv_bfloat16, float>&,
+                                                      double, const Scalars*, cudaStream_t);
 
 }  // namespace scf

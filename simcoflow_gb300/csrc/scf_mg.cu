@@ -444,6 +444,9 @@ __global__ void k_dot_rz_t(int nx, int ny, int pitch, const BT* r, const T* z, i
     set_beta(sc, t1, flexible);
 }
 
+__device__ __forceinline__ double conv_z(float z) { return f2d_exact(z); }
+__device__ __forceinline__ double conv_z(double z) { return z; }
+
 // p_new = z + beta p_old (= z on the first iteration), q = A p_new, p.q and
 // alpha = r.z / p.q.  A 64x32 tile of p_new with a one-cell halo is built in
 // shared memory, so each p_new is formed once per CTA.
@@ -466,7 +469,8 @@ k_pupdate_spmv_t(LevelView L, const ZT* __restrict__ z, const double* __restrict
     double v = 0.0;
     if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
       const size_t g = (size_t)gy * P + gx;
-      v = first ? (double)z[g] : fma(beta, pold[g], (double)z[g]);
+      const double zd = conv_z(z[g]);
+      v = first ? zd : fma(beta, pold[g], zd);
     }
     ps[ey][ex] = v;
   }
@@ -479,7 +483,7 @@ k_pupdate_spmv_t(LevelView L, const ZT* __restrict__ z, const double* __restrict
       const size_t g = (size_t)gy * P + gx;
       const int lx = ex + 1, ly = ey + 1;
       const double pc = ps[ly][lx];
-      double qv = fmax(L.dg[g], 0.0) * pc;
+      double qv = pos_part(L.dg[g]) * pc;
       qv = fma(-L.cE[g], ps[ly][lx + 1], qv);
       qv = fma(-L.cE[g - 1], ps[ly][lx - 1], qv);
       qv = fma(-L.cN[g], ps[ly + 1][lx], qv);

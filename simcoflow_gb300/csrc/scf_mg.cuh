@@ -116,12 +116,16 @@ void launch_line_factor(const MgView<T, CT, T>& L, const LineFactors<T>& F, cuda
 template <class T, class CT>
 void launch_line_solve(const MgView<T, CT, T>& L, const LineFactors<T>& F, int colour, bool zero,
                        const Scalars* sc, cudaStream_t s);
+// residual restriction and prolongation of the line V-cycle, both on the
+// transposed copy Lt of a level; the restriction writes the coarse
+// right-hand side in both layouts (C, Ct), the prolongation reads the
+// natural coarse iterate C.x
 template <class T, class CT>
-void launch_resid_restrict_l(const MgView<T, CT, T>& L, const MgView<T, CT, T>& C,
-                             const Scalars* sc, cudaStream_t s);
+void launch_resid_restrict_lt(const MgView<T, CT, T>& Lt, const MgView<T, CT, T>& C,
+                              const MgView<T, CT, T>& Ct, const Scalars* sc, cudaStream_t s);
 template <class T, class CT>
-void launch_prolong_l(const MgView<T, CT, T>& L, const T* xc, int pc, double omega,
-                      const Scalars* sc, cudaStream_t s);
+void launch_prolong_lt(const MgView<T, CT, T>& Lt, const MgView<T, CT, T>& C, double omega,
+                       const Scalars* sc, cudaStream_t s);
 void launch_aspect(const double* dx, const double* dy, size_t n, unsigned* out_bits,
                    cudaStream_t s);
 

@@ -312,7 +312,12 @@ void enqueue_vcycle_line_t(scf_proj* h, ViewFn view, TViewFn tview, const TailDe
     }
     launch_line(L, colour, zero, sc, s);
   };
-  auto step = [&](int l, bool post, bool zero) {
+  // One alternating step.  The iterate lives in one layout at a time: a
+  // pre-smoothing step ends on the transposed copy (the restriction reads
+  // it there) unless another step follows; a post-smoothing step starts on
+  // the transposed copy (the prolongation wrote it there) when it is the
+  // first, and always ends in the natural layout.
+  auto step = [&](int l, bool post, bool zero, bool edge) {
     const V f = view(l), ft = tview(l);
     if (!post) {
       pass(l, false, 0, zero);
@@ -320,9 +325,9 @@ void enqueue_vcycle_line_t(scf_proj* h, ViewFn view, TViewFn tview, const TailDe
       to_t(f, ft);
       pass(l, true, 0, false);
       pass(l, true, 1, false);
-      from_t(f, ft);
+      if (!edge) from_t(f, ft);
     } else {
-      to_t(f, ft);
+      if (!edge) to_t(f, ft);
       pass(l, true, 1, false);
       pass(l, true, 0, false);
       from_t(f, ft);
@@ -334,9 +339,11 @@ void enqueue_vcycle_line_t(scf_proj* h, ViewFn view, TViewFn tview, const TailDe
   const int lk = h->ltail0 > 0 ? h->ltail0 : L - 1;
   for (int l = 0; l < lk; ++l) {
     const V f = view(l), ft = tview(l);
-    launch_transpose<T>(f.b, f.nx, f.ny, f.pitch, ft.b, ft.pitch, sc, s);
-    for (int it = 0; it < npre; ++it) step(l, false, it == 0);
-    launch_resid_restrict_l(f, view(l + 1), sc, s);
+    // level 0 gets b from the PCG; coarser levels get both layouts from the
+    // restriction
+    if (l == 0) launch_transpose<T>(f.b, f.nx, f.ny, f.pitch, ft.b, ft.pitch, sc, s);
+    for (int it = 0; it < npre; ++it) step(l, false, it == 0, it == npre - 1);
+    launch_resid_restrict_lt(ft, view(l + 1), tview(l + 1), sc, s);
   }
   if (h->ltail0 > 0) {
     launch_line_tail(tail, sc, s);
@@ -345,9 +352,8 @@ void enqueue_vcycle_line_t(scf_proj* h, ViewFn view, TViewFn tview, const TailDe
     launch_coarse_solve_t(c, h->Ainv, h->cmap, h->ncoarse, sc, s);
   }
   for (int l = lk - 1; l >= 0; --l) {
-    const V f = view(l), c = view(l + 1);
-    launch_prolong_l(f, c.x, c.pitch, om, sc, s);
-    for (int it = 0; it < npost; ++it) step(l, true, false);
+    launch_prolong_lt(tview(l), view(l + 1), om, sc, s);
+    for (int it = 0; it < npost; ++it) step(l, true, false, it == 0);
   }
   if (do_rz) {
     const V f = view(0);
