@@ -98,14 +98,19 @@ __device__ __forceinline__ void vstore(T* p, const T (&o)[M]) {
 }
 
 // Reciprocal for the eliminations (a smoother needs no correctly rounded
-// quotient).  FP32: the hardware's correctly rounded reciprocal.  FP64: an
-// FP32 seed refined by two Newton-Raphson steps r <- r (2 - x r), each of
-// which doubles the correct bits (24 -> 48 -> full precision); far cheaper
-// than an IEEE FP64 division on GB300's FP64 pipe.  x is a positive pivot of
-// an M-matrix elimination, well inside FP32's range.
-__device__ __forceinline__ float lrcp(float x) { return __frcp_rn(x); }
+// quotient).  FP32: the PTX approximate reciprocal (one special-function
+// instruction, relative error about 2^-23).  FP64: that FP32 value as a seed,
+// refined by two Newton-Raphson steps r <- r (2 - x r), each of which
+// doubles the correct bits (22 -> 44 -> full precision); far cheaper than an
+// IEEE FP64 division on GB300's FP64 pipe.  x is a positive pivot of an
+// M-matrix elimination, well inside FP32's normal range.
+__device__ __forceinline__ float lrcp(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
 __device__ __forceinline__ double lrcp(double x) {
-  double r = (double)__frcp_rn((float)x);
+  double r = (double)lrcp((float)x);
   r = r * fma(-x, r, 2.0);
   r = r * fma(-x, r, 2.0);
   return r;
