@@ -20,8 +20,10 @@
 // own interface), which leaves one equation per thread that couples only
 // the interfaces of threads t-1, t, t+1 -- the Schur complement, again a
 // symmetric diagonally dominant tridiagonal system.  That system is solved
-// by parallel cyclic reduction in shared memory, and every thread then
-// recovers its interior cells from its two interface values.  The
+// by the same splitting one level up (each warp's last lane is the warp's
+// interface; cyclic reduction by warp shuffles inside each warp, then over
+// the warps' interfaces), and every thread then recovers its interior cells
+// from its two interface values.  The
 // interfaces of an M-matrix keep every pivot positive, so no pivoting is
 // needed.
 #include <type_traits>
@@ -116,6 +118,8 @@ __device__ __forceinline__ double lrcp(double x) {
   return r;
 }
 
+constexpr int kWarpSlots = 16;  // per-warp values exchanged in k_line (13 used)
+
 // Relax the lines (rows) iy = 2*blockIdx.x + colour of level L.
 // ZERO: the iterate is zero on entry (the first pass of a V-cycle level):
 // the neighbouring rows are not read, and they are written as zero.
@@ -126,10 +130,6 @@ k_line(MgView<T, CT, T> L, int colour, const Scalars* sc) {
   if (sc && sc->done) return;
   extern __shared__ __align__(16) unsigned char line_smem[];
   const int nth = blockDim.x, t = threadIdx.x;
-  T* rD0 = reinterpret_cast<T*>(line_smem);  // responses of each thread's first interior cell
-  T* rS0 = rD0 + nth;
-  T* rT0 = rS0 + nth;
-  T* pa = rT0 + nth;  // two PCR buffers of 4 arrays each
   const int iy = 2 * blockIdx.x + colour;
   if (iy >= L.ny) return;
   const int P = L.pitch, nx = L.nx;
@@ -204,56 +204,98 @@ k_line(MgView<T, CT, T> L, int colour, const Scalars* sc) {
       Tr[k] = fma(-cp[k], Tr[k + 1], Tr[k]);
     }
   }
-  rD0[t] = D[0];
-  rS0[t] = S[0];
-  rT0[t] = Tr[0];
-  __syncthreads();
-  // interface equation of thread t: couples I_{t-1}, I_t, I_{t+1}
+  // Interface system: one equation per thread,
+  //   ea I_{t-1} + eb I_t + ec I_{t+1} = ed,
+  // solved in two stages without block-wide reduction steps.  (1) In each
+  // warp, lanes 0..30 are interior unknowns and lane 31's interface J_w is
+  // the warp's own interface: cyclic reduction over the lanes (shuffles,
+  // five steps) gives I_l = P_l + Q_l J_{w-1} + R_l J_w.  (2) Substituting
+  // that into lane 31's equation leaves one tridiagonal equation per warp in
+  // the J's; every warp forms all of them from shared memory (after the
+  // kernel's one block barrier) and reduces them by shuffles itself.
+  const int lane = t & 31, warp = t >> 5, nw = nth >> 5;
+  T* wsm = reinterpret_cast<T*>(line_smem);  // [nw][kWarpSlots]
   const T aI = a[M - 1], dI = d[M - 1], cI = c[M - 1], rI = r[M - 1];
-  const bool last = t == nth - 1;
-  const T Dn = last ? T(0) : rD0[t + 1], Sn = last ? T(0) : rS0[t + 1],
-          Tn = last ? T(0) : rT0[t + 1];
-  T ea = aI * S[M - 2];
-  T eb = fma(cI, Sn, fma(aI, Tr[M - 2], dI));
-  T ec = cI * Tn;
-  T ed = fma(-cI, Dn, fma(-aI, D[M - 2], rI));
-  // parallel cyclic reduction over the nth interface equations
-  int cur = 0;  // PCR buffer cur starts at pa + cur * 4 * nth
-  pa[t] = ea;
-  pa[nth + t] = eb;
-  pa[2 * nth + t] = ec;
-  pa[3 * nth + t] = ed;
-  __syncthreads();
-  for (int s = 1; s < nth; s <<= 1) {
-    const T* A_ = pa + cur * 4 * nth;
-    const T* B_ = A_ + nth;
-    const T* C_ = B_ + nth;
-    const T* D_ = C_ + nth;
-    T na = T(0), nb = B_[t], nc = T(0), nd = D_[t];
-    if (t - s >= 0) {
-      const T k1 = A_[t] * lrcp(B_[t - s]);
-      na = -A_[t - s] * k1;
-      nb = fma(-C_[t - s], k1, nb);
-      nd = fma(-D_[t - s], k1, nd);
-    }
-    if (t + s < nth) {
-      const T k2 = C_[t] * lrcp(B_[t + s]);
-      nc = -C_[t + s] * k2;
-      nb = fma(-A_[t + s], k2, nb);
-      nd = fma(-D_[t + s], k2, nd);
-    }
-    T* W = pa + (cur ^ 1) * 4 * nth;
-    W[t] = na;
-    W[nth + t] = nb;
-    W[2 * nth + t] = nc;
-    W[3 * nth + t] = nd;
-    cur ^= 1;
-    __syncthreads();
+  // first-cell responses of thread t+1 (lane 31: the next warp's, later)
+  const T Dn = __shfl_down_sync(0xffffffffu, D[0], 1);
+  const T Sn = __shfl_down_sync(0xffffffffu, S[0], 1);
+  const T Tn = __shfl_down_sync(0xffffffffu, Tr[0], 1);
+  const T ea = aI * S[M - 2];
+  const T ebp = fma(aI, Tr[M - 2], dI), edp = fma(-aI, D[M - 2], rI);
+  T pa_ = T(0), pb = T(1), pc = T(0), pd = T(0), pe = T(0), pf = T(0);
+  if (lane < 31) {
+    const T eb = fma(cI, Sn, ebp), ec = cI * Tn, ed = fma(-cI, Dn, edp);
+    pa_ = lane == 0 ? T(0) : ea;
+    pb = eb;
+    pc = lane == 30 ? T(0) : ec;
+    pd = ed;
+    pe = lane == 0 ? -ea : T(0);   // coefficient of J_{w-1}
+    pf = lane == 30 ? -ec : T(0);  // coefficient of J_w
   }
-  const T It = pa[cur * 4 * nth + 3 * nth + t] * lrcp(pa[cur * 4 * nth + nth + t]);
-  rD0[t] = It;  // rD0 is no longer read by anyone after the first barrier above
+#pragma unroll
+  for (int sh = 1; sh < 32; sh <<= 1) {
+    // lanes without a partner at distance sh have the matching coupling
+    // already zero, so the partner values (their own, from the shuffle)
+    // are multiplied by zero
+    const T am = __shfl_up_sync(0xffffffffu, pa_, sh), bm = __shfl_up_sync(0xffffffffu, pb, sh);
+    const T cm = __shfl_up_sync(0xffffffffu, pc, sh), dm = __shfl_up_sync(0xffffffffu, pd, sh);
+    const T em = __shfl_up_sync(0xffffffffu, pe, sh), fm = __shfl_up_sync(0xffffffffu, pf, sh);
+    const T ap = __shfl_down_sync(0xffffffffu, pa_, sh), bp = __shfl_down_sync(0xffffffffu, pb, sh);
+    const T cp2 = __shfl_down_sync(0xffffffffu, pc, sh), dp = __shfl_down_sync(0xffffffffu, pd, sh);
+    const T ep = __shfl_down_sync(0xffffffffu, pe, sh), fp = __shfl_down_sync(0xffffffffu, pf, sh);
+    const T k1 = pa_ * lrcp(bm), k2 = pc * lrcp(bp);
+    pa_ = -am * k1;
+    pc = -cp2 * k2;
+    pb = fma(-ap, k2, fma(-cm, k1, pb));
+    pd = fma(-dp, k2, fma(-dm, k1, pd));
+    pe = fma(-ep, k2, fma(-em, k1, pe));
+    pf = fma(-fp, k2, fma(-fm, k1, pf));
+  }
+  const T ib = lrcp(pb);
+  const T Pl = pd * ib, Ql = pe * ib, Rl = pf * ib;
+  const T P30 = __shfl_up_sync(0xffffffffu, Pl, 1), Q30 = __shfl_up_sync(0xffffffffu, Ql, 1),
+          R30 = __shfl_up_sync(0xffffffffu, Rl, 1);
+  T* ws = wsm + warp * kWarpSlots;
+  if (lane == 0) {
+    ws[0] = D[0]; ws[1] = S[0]; ws[2] = Tr[0];
+    ws[3] = Pl; ws[4] = Ql; ws[5] = Rl;
+  } else if (lane == 31) {
+    ws[6] = ea; ws[7] = ebp; ws[8] = cI; ws[9] = edp;
+    ws[10] = P30; ws[11] = Q30; ws[12] = R30;
+  }
   __syncthreads();
-  const T Il = t > 0 ? rD0[t - 1] : T(0);
+  // the warps' interface equations (lane k: warp k), reduced in every warp
+  T ja = T(0), jb = T(1), jc = T(0), jd = T(0);
+  if (lane < nw) {
+    const T* wk = wsm + lane * kWarpSlots;
+    const bool nx_ = lane + 1 < nw;
+    const T* wn = wk + kWarpSlots;
+    const T D0n = nx_ ? wn[0] : T(0), S0n = nx_ ? wn[1] : T(0), T0n = nx_ ? wn[2] : T(0);
+    const T P0n = nx_ ? wn[3] : T(0), Q0n = nx_ ? wn[4] : T(0), R0n = nx_ ? wn[5] : T(0);
+    const T eak = wk[6], cIk = wk[8];
+    const T ebk = fma(cIk, S0n, wk[7]), eck = cIk * T0n, edk = fma(-cIk, D0n, wk[9]);
+    ja = eak * wk[11];
+    jb = fma(eck, Q0n, fma(eak, wk[12], ebk));
+    jc = eck * R0n;
+    jd = fma(-eck, P0n, fma(-eak, wk[10], edk));
+  }
+  for (int sh = 1; sh < nw; sh <<= 1) {
+    const T am = __shfl_up_sync(0xffffffffu, ja, sh), bm = __shfl_up_sync(0xffffffffu, jb, sh);
+    const T cm = __shfl_up_sync(0xffffffffu, jc, sh), dm = __shfl_up_sync(0xffffffffu, jd, sh);
+    const T ap = __shfl_down_sync(0xffffffffu, ja, sh), bp = __shfl_down_sync(0xffffffffu, jb, sh);
+    const T cp2 = __shfl_down_sync(0xffffffffu, jc, sh), dp = __shfl_down_sync(0xffffffffu, jd, sh);
+    const T k1 = ja * lrcp(bm), k2 = jc * lrcp(bp);
+    ja = -am * k1;
+    jc = -cp2 * k2;
+    jb = fma(-ap, k2, fma(-cm, k1, jb));
+    jd = fma(-dp, k2, fma(-dm, k1, jd));
+  }
+  const T J = jd * lrcp(jb);
+  const T Jw = __shfl_sync(0xffffffffu, J, warp);
+  const T Jm = warp > 0 ? __shfl_sync(0xffffffffu, J, warp > 0 ? warp - 1 : 0) : T(0);
+  const T It = lane == 31 ? Jw : fma(Ql, Jm, fma(Rl, Jw, Pl));
+  const T Iup = __shfl_up_sync(0xffffffffu, It, 1);
+  const T Il = lane == 0 ? Jm : Iup;
   if (ix0 >= nx) return;
   T xo[M];
 #pragma unroll
@@ -858,7 +900,7 @@ void launch_line(const MgView<T, CT, T>& L, int colour, bool zero, const Scalars
   int m = 0;
   const int th = line_threads(L.nx, &m);
   const dim3 g((L.ny - colour + 1) / 2);
-  const size_t smem = (size_t)11 * th * sizeof(T);
+  const size_t smem = (size_t)(th / 32) * kWarpSlots * sizeof(T);
   if (g.x == 0) return;
 #define SCF_LINE(MM)                                                                           \
   do {                                                                                         \
