@@ -58,6 +58,15 @@ struct Scalars {
 
 enum Ticket { T_RHS = 0, T_RZ, T_PQ, T_RR, T_RES, T_MRES, T_DOT };
 
+// PCG beta: plain beta = r_k.z_k / r_{k-1}.z_{k-1}; flexible (Polak-Ribiere)
+// beta = (r_k.z_k - r_k.z_{k-1}) / r_{k-1}.z_{k-1}, where the cross term
+// r_k.z_{k-1} was reduced by the previous iteration's x/r update
+__device__ __forceinline__ void set_beta(Scalars* sc, double rz_new, int flexible) {
+  if (sc->iter == 0) sc->beta = 0.0;
+  else sc->beta = (flexible ? (rz_new - sc->rz_cross) : rz_new) / sc->rz;
+  sc->rz = rz_new;
+}
+
 // status codes written by the device (mirror scf_proj.h)
 constexpr int kOk = 0, kErrNaN = -3, kErrNotConverged = -4, kErrTimeout = -6;
 

@@ -123,9 +123,12 @@ constexpr int kWarpSlots = 16;  // per-warp values exchanged in k_line (13 used)
 // Relax the lines (rows) iy = 2*blockIdx.x + colour of level L.
 // ZERO: the iterate is zero on entry (the first pass of a V-cycle level):
 // the neighbouring rows are not read, and they are written as zero.
-template <class T, class CT, int M, bool ZERO>
+// RZ (colour 0 only, the last pass of the V-cycle on the finest level):
+// also reduce r.z over the whole level -- this CTA's row and the row above
+// it, whose iterate is final -- and set the PCG beta, as k_dot_rz_t would.
+template <class T, class CT, int M, bool ZERO, bool RZ>
 __global__ void __launch_bounds__(512, 1)
-k_line(MgView<T, CT, T> L, int colour, const Scalars* sc) {
+k_line(MgView<T, CT, T> L, int colour, Scalars* sc, int flexible, double* part) {
   pdl_wait();
   if (sc && sc->done) return;
   extern __shared__ __align__(16) unsigned char line_smem[];
@@ -296,23 +299,68 @@ k_line(MgView<T, CT, T> L, int colour, const Scalars* sc) {
   const T It = lane == 31 ? Jw : fma(Ql, Jm, fma(Rl, Jw, Pl));
   const T Iup = __shfl_up_sync(0xffffffffu, It, 1);
   const T Il = lane == 0 ? Jm : Iup;
-  if (ix0 >= nx) return;
-  T xo[M];
+  if (!RZ && ix0 >= nx) return;
+  T acc = T(0);
+  if (ix0 < nx) {
+    T xo[M];
 #pragma unroll
-  for (int k = 0; k < M; ++k) {
-    const T v = (k == M - 1) ? It : fma(S[k], Il, fma(Tr[k], It, D[k]));
-    xo[k] = (actm >> k) & 1u ? v : T(0);
-  }
-  if (ix0 + M <= nx) {
-    vstore<T, M>(L.x + g0 + ix0, xo);
-  } else {  // the ghost columns past nx keep their zeros
-    for (int k = 0; k < nx - ix0; ++k) L.x[g0 + ix0 + k] = xo[k];
-  }
-  if (ZERO && iy + 1 < L.ny) {
-    T z[M];
+    for (int k = 0; k < M; ++k) {
+      const T v = (k == M - 1) ? It : fma(S[k], Il, fma(Tr[k], It, D[k]));
+      xo[k] = (actm >> k) & 1u ? v : T(0);
+    }
+    if (ix0 + M <= nx) {
+      vstore<T, M>(L.x + g0 + ix0, xo);
+    } else {  // the ghost columns past nx keep their zeros
+      for (int k = 0; k < nx - ix0; ++k) L.x[g0 + ix0 + k] = xo[k];
+    }
+    if (ZERO && iy + 1 < L.ny) {
+      T z[M];
 #pragma unroll
-    for (int k = 0; k < M; ++k) z[k] = T(0);
-    vstore<T, M>(L.x + g0 + P + ix0, z);
+      for (int k = 0; k < M; ++k) z[k] = T(0);
+      vstore<T, M>(L.x + g0 + P + ix0, z);
+    }
+    if (RZ) {  // b and x past nx are zero padding
+      T bv[M];
+      vload<T, M>(L.b + g0 + ix0, bv);
+#pragma unroll
+      for (int k = 0; k < M; ++k) acc = fma(bv[k], xo[k], acc);
+      if (iy + 1 < L.ny) {
+        T xu[M];
+        vload<T, M>(L.b + g0 + P + ix0, bv);
+        vload<T, M>(L.x + g0 + P + ix0, xu);
+#pragma unroll
+        for (int k = 0; k < M; ++k) acc = fma(bv[k], xu[k], acc);
+      }
+    }
+  }
+  if (RZ) {  // per-thread FP32 sums, combined in FP64 in a fixed order
+    __shared__ double red[16];
+    __shared__ bool lastblk;
+    double v = (double)acc;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (t == 0) {
+      double sb = 0.0;
+      for (int w = 0; w < nw; ++w) sb += red[w];
+      part[blockIdx.x] = sb;
+      __threadfence();
+      lastblk = atomicAdd(&sc->tickets[T_RZ], 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!lastblk) return;
+    __threadfence();
+    double xs = 0.0;
+    for (unsigned k = t; k < gridDim.x; k += nth) xs += __ldcg(&part[k]);
+    for (int o = 16; o > 0; o >>= 1) xs += __shfl_down_sync(0xffffffffu, xs, o);
+    if (lane == 0) red[warp] = xs;
+    __syncthreads();
+    if (t == 0) {
+      double tot = 0.0;
+      for (int w = 0; w < nw; ++w) tot += red[w];
+      set_beta(sc, tot, flexible);
+      sc->tickets[T_RZ] = 0u;
+    }
   }
 }
 
@@ -895,8 +943,8 @@ int line_threads(int len, int* chunk) {
 }
 
 template <class T, class CT>
-void launch_line(const MgView<T, CT, T>& L, int colour, bool zero, const Scalars* sc,
-                 cudaStream_t s) {
+void launch_line(const MgView<T, CT, T>& L, int colour, bool zero, Scalars* sc, cudaStream_t s,
+                 bool rz, int flexible, double* part) {
   int m = 0;
   const int th = line_threads(L.nx, &m);
   const dim3 g((L.ny - colour + 1) / 2);
@@ -905,13 +953,17 @@ void launch_line(const MgView<T, CT, T>& L, int colour, bool zero, const Scalars
 #define SCF_LINE(MM)                                                                           \
   do {                                                                                         \
     if (zero) {                                                                                \
-      auto k = k_line<T, CT, MM, true>;                                                        \
+      auto k = k_line<T, CT, MM, true, false>;                                                 \
       allow_max_smem(k);                                                                       \
-      launch_k(k, g, dim3(th), smem, s, L, colour, sc);                                        \
+      launch_k(k, g, dim3(th), smem, s, L, colour, sc, flexible, part);                        \
+    } else if (rz) {                                                                           \
+      auto k = k_line<T, CT, MM, false, true>;                                                 \
+      allow_max_smem(k);                                                                       \
+      launch_k(k, g, dim3(th), smem, s, L, colour, sc, flexible, part);                        \
     } else {                                                                                   \
-      auto k = k_line<T, CT, MM, false>;                                                       \
+      auto k = k_line<T, CT, MM, false, false>;                                                \
       allow_max_smem(k);                                                                       \
-      launch_k(k, g, dim3(th), smem, s, L, colour, sc);                                        \
+      launch_k(k, g, dim3(th), smem, s, L, colour, sc, flexible, part);                        \
     }                                                                                          \
   } while (0)
   if (m == 8) SCF_LINE(8);
@@ -1002,9 +1054,9 @@ void launch_aspect(const double* dx, const double* dy, size_t n, unsigned* out_b
 }
 
 template void launch_line<double, double>(const MgView<double, double, double>&, int, bool,
-                                          const Scalars*, cudaStream_t);
+                                          Scalars*, cudaStream_t, bool, int, double*);
 template void launch_line<float, __nv_bfloat16>(const MgView<float, __nv_bfloat16, float>&, int,
-                                                bool, const Scalars*, cudaStream_t);
+                                                bool, Scalars*, cudaStream_t, bool, int, double*);
 template void launch_line_factor<double, double>(const MgView<double, double, double>&,
                                                 const LineFactors<double>&, cudaStream_t);
 template void launch_line_solve<double, double>(const MgView<double, double, double>&,

@@ -88,14 +88,6 @@ __device__ bool grid_sum2(double a, double b, double* part, unsigned* ticket, do
   return true;
 }
 
-// PCG beta: plain beta = r_k.z_k / r_{k-1}.z_{k-1}; flexible (Polak-Ribiere)
-// beta = (r_k.z_k - r_k.z_{k-1}) / r_{k-1}.z_{k-1}, where the cross term
-// r_k.z_{k-1} was reduced by the previous iteration's x/r update
-__device__ __forceinline__ void set_beta(Scalars* sc, double rz_new, int flexible) {
-  if (sc->iter == 0) sc->beta = 0.0;
-  else sc->beta = (flexible ? (rz_new - sc->rz_cross) : rz_new) / sc->rz;
-  sc->rz = rz_new;
-}
 
 template <class T, class CT, class BT, int FIRST, bool ZERO, bool PROLONG, bool RESTRICT, bool RZ,
           int ITER>

@@ -97,8 +97,8 @@ void launch_pupdate_spmv_t(LevelView L0, const ZT* z, const double* pold, double
 constexpr int kLineMaxLen = 16384;
 int line_threads(int len, int* chunk);  // CTA size for a line; 0 if too long
 template <class T, class CT>
-void launch_line(const MgView<T, CT, T>& L, int colour, bool zero, const Scalars* sc,
-                 cudaStream_t s);
+void launch_line(const MgView<T, CT, T>& L, int colour, bool zero, Scalars* sc, cudaStream_t s,
+                 bool rz = false, int flexible = 0, double* part = nullptr);
 template <class E>
 void launch_transpose(const E* src, int nx, int ny, int ps, E* dst, int pd, const Scalars* sc,
                       cudaStream_t s);

@@ -302,7 +302,9 @@ void enqueue_vcycle_line_t(scf_proj* h, ViewFn view, TViewFn tview, const TailDe
     launch_transpose<T>(ft.x, ft.nx, ft.ny, ft.pitch, f.x, f.pitch, sc, s);
   };
   // one pass: factored on FP64 levels that have factors, else the full solve
-  auto pass = [&](int l, bool tr, int colour, bool zero) {
+  // (which can also reduce the PCG's r.z on its last pass)
+  bool rz_done = false;
+  auto pass = [&](int l, bool tr, int colour, bool zero, bool rz = false) {
     const V L = tr ? tview(l) : view(l);
     if constexpr (std::is_same<T, double>::value) {
       if (l < (int)h->lf64n.size()) {
@@ -310,14 +312,15 @@ void enqueue_vcycle_line_t(scf_proj* h, ViewFn view, TViewFn tview, const TailDe
         return;
       }
     }
-    launch_line(L, colour, zero, sc, s);
+    launch_line(L, colour, zero, sc, s, rz, flexible, h->part);
+    rz_done = rz_done || rz;
   };
   // One alternating step.  The iterate lives in one layout at a time: a
   // pre-smoothing step ends on the transposed copy (the restriction reads
   // it there) unless another step follows; a post-smoothing step starts on
   // the transposed copy (the prolongation wrote it there) when it is the
   // first, and always ends in the natural layout.
-  auto step = [&](int l, bool post, bool zero, bool edge) {
+  auto step = [&](int l, bool post, bool zero, bool edge, bool rz = false) {
     const V f = view(l), ft = tview(l);
     if (!post) {
       pass(l, false, 0, zero);
@@ -332,7 +335,7 @@ void enqueue_vcycle_line_t(scf_proj* h, ViewFn view, TViewFn tview, const TailDe
       pass(l, true, 0, false);
       from_t(f, ft);
       pass(l, false, 1, false);
-      pass(l, false, 0, false);
+      pass(l, false, 0, false, rz);
     }
   };
   // levels 0 .. lk-1 run as kernels; the tail (or the coarse solve) covers lk .. L-1
@@ -353,9 +356,10 @@ void enqueue_vcycle_line_t(scf_proj* h, ViewFn view, TViewFn tview, const TailDe
   }
   for (int l = lk - 1; l >= 0; --l) {
     launch_prolong_lt(tview(l), view(l + 1), om, sc, s);
-    for (int it = 0; it < npost; ++it) step(l, true, false, it == 0);
+    for (int it = 0; it < npost; ++it)
+      step(l, true, false, it == 0, do_rz && l == 0 && it == npost - 1);
   }
-  if (do_rz) {
+  if (do_rz && !rz_done) {
     const V f = view(0);
     launch_dot_rz_t<T, T>(f.nx, f.ny, f.pitch, f.b, f.x, flexible, sc, h->part, s);
   }
@@ -1033,6 +1037,9 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
     const size_t gy = (size_t)(ny + 7) / 8;
     size_t rb = (size_t)((nx + 31) / 32) * (gy < 1024 ? gy : 1024);
     if (rb > nblk) nblk = rb;
+    // r.z fused into the last line relaxation: one block per pair of rows
+    const size_t lb = (size_t)(ny + 1) / 2;
+    if (lb > nblk) nblk = lb;
   }
   if ((rc = dev_alloc(h, (void**)&h->part, sizeof(double) * (2 * nblk + 64)))) return fail(rc);
   if (cudaMallocHost((void**)&h->sc_host, sizeof(Scalars)) != cudaSuccess) return fail(SCF_ERR_NOMEM);
