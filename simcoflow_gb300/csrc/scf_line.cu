@@ -694,30 +694,39 @@ k_resid_restrict_lt(MgView<T, CT, T> Lt, MgView<T, CT, T> C, MgView<T, CT, T> Ct
 // x += omega * x_coarse(parent) on cells with an unknown, applied to the
 // transposed copy Lt of a level (where the post-smoothing starts): Lt cell
 // (i, j) is natural cell (j, i), whose parent is coarse cell (j/2, i/2) of
-// the natural coarse level (nxc x nyc, pitch pc).  A 16 x 16 block of coarse
-// values is staged in shared memory for the CTA's 32 x 32 fine cells.
+// the natural coarse level (nxc x nyc, pitch pc).  A 32 x 16 block of coarse
+// values is staged in shared memory for the CTA's 64 x 32 fine cells.
 template <class T, class CT>
 __global__ void __launch_bounds__(256)
 k_prolong_lt(MgView<T, CT, T> Lt, const T* __restrict__ xc, int pc, int nxc, int nyc, T omega,
              const Scalars* sc) {
   pdl_wait();
   if (sc && sc->done) return;
-  __shared__ T ct[16][17];
-  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+  // CTA: 64 x 32 fine cells, 16-byte vectors along the rows
+  constexpr int V = 16 / sizeof(T), TPR = 64 / V, RPP = 256 / TPR;
+  __shared__ T ct[32][17];
+  const int x0 = blockIdx.x * 64, y0 = blockIdx.y * 32;
   const int t = threadIdx.y * 32 + threadIdx.x;
-  {
-    const int cx = t % 16, cy = t / 16;  // coarse natural (y0/2 + cx, x0/2 + cy)
+  for (int e = t; e < 32 * 16; e += 256) {
+    const int cx = e % 16, cy = e / 16;  // coarse natural (y0/2 + cx, x0/2 + cy)
     const int ix = (y0 >> 1) + cx, iy = (x0 >> 1) + cy;
     ct[cy][cx] = (ix < nxc && iy < nyc) ? xc[(size_t)iy * pc + ix] : T(0);
   }
   __syncthreads();
-  const int i = x0 + threadIdx.x;
+  const int li = (t % TPR) * V, i = x0 + li;
   if (i >= Lt.nx) return;
-  for (int jj = threadIdx.y; jj < 32; jj += 8) {
+  for (int jj = t / TPR; jj < 32; jj += RPP) {
     const int j = y0 + jj;
     if (j >= Lt.ny) break;
+    // a vector reaching past nx covers padding, whose inverse diagonal is 0
     const size_t g = (size_t)j * Lt.pitch + i;
-    if (Lt.di[g] > T(0)) Lt.x[g] = fma(omega, ct[threadIdx.x >> 1][jj >> 1], Lt.x[g]);
+    T dv[V], xv[V];
+    unpack(__ldg(reinterpret_cast<const uint4*>(Lt.di + g)), dv);
+    unpack(*reinterpret_cast<const uint4*>(Lt.x + g), xv);
+#pragma unroll
+    for (int m = 0; m < V; ++m)
+      if (dv[m] > T(0)) xv[m] = fma(omega, ct[(li + m) >> 1][jj >> 1], xv[m]);
+    *reinterpret_cast<uint4*>(Lt.x + g) = pack(xv);
   }
 }
 
@@ -1042,7 +1051,7 @@ void launch_resid_restrict_lt(const MgView<T, CT, T>& Lt, const MgView<T, CT, T>
 template <class T, class CT>
 void launch_prolong_lt(const MgView<T, CT, T>& Lt, const MgView<T, CT, T>& C, double omega,
                        const Scalars* sc, cudaStream_t s) {
-  const dim3 g((Lt.nx + 31) / 32, (Lt.ny + 31) / 32);
+  const dim3 g((Lt.nx + 63) / 64, (Lt.ny + 31) / 32);
   launch_k(k_prolong_lt<T, CT>, g, dim3(32, 8), 0, s, Lt, (const T*)C.x, C.pitch, C.nx, C.ny,
            (T)omega, sc);
 }
