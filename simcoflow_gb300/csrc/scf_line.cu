@@ -691,6 +691,80 @@ k_resid_restrict_lt(MgView<T, CT, T> Lt, MgView<T, CT, T> C, MgView<T, CT, T> Ct
   }
 }
 
+// The same restriction for FP32/BF16 levels with vector loads: a thread
+// owns two coarse cells (a0, a0 + 1) of coarse row b, i.e. four fine cells
+// (16 bytes of FP32, 8 bytes of BF16) in each of the fine rows 2b, 2b + 1;
+// a CTA owns 64 x 8 coarse cells.  Same terms in the same order as
+// k_resid_restrict_lt.
+__device__ __forceinline__ void bf4(const __nv_bfloat16* p, float cs, float (&o)[4]) {
+  const uint2 u = __ldg(reinterpret_cast<const uint2*>(p));
+  o[0] = bf_lo(u.x) * cs; o[1] = bf_hi(u.x) * cs;
+  o[2] = bf_lo(u.y) * cs; o[3] = bf_hi(u.y) * cs;
+}
+__device__ __forceinline__ void f4(const float* p, float (&o)[4]) {
+  unpack(__ldg(reinterpret_cast<const uint4*>(p)), o);
+}
+__global__ void __launch_bounds__(256)
+k_resid_restrict_lt4(MgView<float, __nv_bfloat16, float> Lt, MgView<float, __nv_bfloat16, float> C,
+                     MgView<float, __nv_bfloat16, float> Ct, const Scalars* sc) {
+  pdl_wait();
+  if (sc && sc->done) return;
+  __shared__ float tile[8][65];
+  const int a0 = blockIdx.x * 64 + 2 * threadIdx.x, b = blockIdx.y * 8 + threadIdx.y;
+  const float cs = Lt.csp ? __ldg(Lt.csp) : 1.0f;
+  const int P = Lt.pitch, nx = Lt.nx, ny = Lt.ny;
+  float s0 = 0.0f, s1 = 0.0f;
+  if (a0 < Ct.nx && b < Ct.ny) {
+    const int c0 = 2 * a0;
+    float rr[2][4];  // [fine row 2b + dq][fine column c0 + m]
+#pragma unroll
+    for (int dq = 0; dq < 2; ++dq) {
+      const int gy = 2 * b + dq;
+#pragma unroll
+      for (int m = 0; m < 4; ++m) rr[dq][m] = 0.0f;
+      if (gy >= ny) continue;
+      const size_t g = (size_t)gy * P + c0;
+      float xv[4], xu[4], xd[4], bv[4], dv[4], ce[4], cn[4], cs_[4];
+      f4(Lt.x + g, xv);
+      f4(Lt.x + g + P, xu);
+      f4(Lt.x + g - P, xd);
+      f4(Lt.b + g, bv);
+      f4(Lt.dg + g, dv);
+      bf4(Lt.cE + g, cs, ce);
+      bf4(Lt.cN + g, cs, cn);
+      bf4(Lt.cN + g - P, cs, cs_);
+      const float xw = Lt.x[g - 1];
+      const float cw = __bfloat162float(Lt.cE[g - 1]) * cs;
+      const float xe = c0 + 3 < nx ? Lt.x[g + 4] : 0.0f;
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        float r = fmaf(-dv[m], xv[m], bv[m]);
+        r = fmaf(cn[m], xu[m], r);
+        r = fmaf(cs_[m], xd[m], r);
+        r = fmaf(ce[m], m < 3 ? xv[m + 1] : xe, r);
+        r = fmaf(m > 0 ? ce[m - 1] : cw, m > 0 ? xv[m - 1] : xw, r);
+        // cells past nx and cells without an unknown add nothing
+        rr[dq][m] = (c0 + m < nx && dv[m] >= 0.0f) ? r : 0.0f;
+      }
+    }
+    // natural order: fine column (natural row) outer, fine row inner
+    s0 = rr[0][0]; s0 += rr[1][0]; s0 += rr[0][1]; s0 += rr[1][1];
+    s1 = rr[0][2]; s1 += rr[1][2]; s1 += rr[0][3]; s1 += rr[1][3];
+    float* o = Ct.b + (size_t)b * Ct.pitch + a0;
+    if (a0 + 1 < Ct.nx) *reinterpret_cast<float2*>(o) = make_float2(s0, s1);
+    else o[0] = s0;
+  }
+  tile[threadIdx.y][2 * threadIdx.x] = s0;
+  tile[threadIdx.y][2 * threadIdx.x + 1] = s1;
+  __syncthreads();
+  const int t = threadIdx.y * 32 + threadIdx.x;
+  for (int e = t; e < 64 * 8; e += 256) {
+    const int bl = e % 8, al = e / 8;
+    const int ix = blockIdx.y * 8 + bl, iy = blockIdx.x * 64 + al;  // C cell = Ct cell (iy, ix)
+    if (ix < C.nx && iy < C.ny) C.b[(size_t)iy * C.pitch + ix] = tile[bl][al];
+  }
+}
+
 // x += omega * x_coarse(parent) on cells with an unknown, applied to the
 // transposed copy Lt of a level (where the post-smoothing starts): Lt cell
 // (i, j) is natural cell (j, i), whose parent is coarse cell (j/2, i/2) of
@@ -1044,8 +1118,13 @@ void launch_transpose(const E* src, int nx, int ny, int ps, E* dst, int pd, cons
 template <class T, class CT>
 void launch_resid_restrict_lt(const MgView<T, CT, T>& Lt, const MgView<T, CT, T>& C,
                               const MgView<T, CT, T>& Ct, const Scalars* sc, cudaStream_t s) {
-  const dim3 g((Ct.nx + 31) / 32, (Ct.ny + 7) / 8);
-  launch_k(k_resid_restrict_lt<T, CT>, g, dim3(32, 8), 0, s, Lt, C, Ct, sc);
+  if constexpr (std::is_same<T, float>::value) {
+    const dim3 g((Ct.nx + 63) / 64, (Ct.ny + 7) / 8);
+    launch_k(k_resid_restrict_lt4, g, dim3(32, 8), 0, s, Lt, C, Ct, sc);
+  } else {
+    const dim3 g((Ct.nx + 31) / 32, (Ct.ny + 7) / 8);
+    launch_k(k_resid_restrict_lt<T, CT>, g, dim3(32, 8), 0, s, Lt, C, Ct, sc);
+  }
 }
 
 template <class T, class CT>
