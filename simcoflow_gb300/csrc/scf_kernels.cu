@@ -118,10 +118,28 @@ __device__ bool grid_reduce2(double a, double b, double* part, unsigned* ticket,
 // (src/ProjectionP_Mod.f90:395-580, :137-273).
 // ---------------------------------------------------------------------------
 
-// 1 = wet, 2 = dry, 0 = neither (NaN input); src/ProjectionP_Mod.f90:409-410, :493-494
+// 1 = wet, 2 = dry, 0 = neither (NaN input); src/ProjectionP_Mod.f90:409-410, :493-494.
+// The comparisons run on the integer pipe (an FP64 compare issues on GB300's
+// slow FP64 pipe): for a non-NaN double x and a constant c > 0, x >= c
+// exactly when the bit patterns compare so as signed 64-bit integers
+// (negative x, -0 included, have negative patterns), and x < 0 exactly when
+// the pattern is negative and not that of -0.  NaN operands make every
+// comparison false, as in IEEE arithmetic.
+__device__ __forceinline__ bool bits_nan(long long b) {
+  return (b & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+}
 __device__ __forceinline__ int cell_class(double vof, double phi, double vofS) {
-  if ((vof >= 0.5 && vofS < kEpsi) || (phi < 0.0 && vofS >= kEpsi)) return 1;
-  if ((vof < 0.5 && vofS < kEpsi) || (phi >= 0.0 && vofS >= kEpsi)) return 2;
+  constexpr long long kHalfBits = 0x3fe0000000000000ll;  // 0.5
+  constexpr long long kEpsiBits = 0x3f50624dd2f1a9fcll;  // 1.0e-3 (kEpsi)
+  const long long v = __double_as_longlong(vof), p = __double_as_longlong(phi),
+                  e = __double_as_longlong(vofS);
+  const bool vn = bits_nan(v), pn = bits_nan(p), en = bits_nan(e);
+  const bool v_ge = !vn && v >= kHalfBits, v_lt = !vn && v < kHalfBits;
+  const bool e_lt = !en && e < kEpsiBits, e_ge = !en && e >= kEpsiBits;
+  const bool p_neg = p < 0 && p != (long long)0x8000000000000000ull;
+  const bool p_lt = !pn && p_neg, p_ge = !pn && !p_neg;
+  if ((v_ge && e_lt) || (p_lt && e_ge)) return 1;
+  if ((v_lt && e_lt) || (p_ge && e_ge)) return 2;
   return 0;
 }
 
