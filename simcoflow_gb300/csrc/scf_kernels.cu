@@ -597,33 +597,39 @@ __global__ void k_update_xr(LevelView L, double* __restrict__ x, const double* _
 // Pressure-gradient correction of one face between cells s (self) and n
 // (east or north neighbour): returns false when the reference leaves the
 // face alone.  G = (Pp_n - Pp_s)*BetaM*BetaP/BetaW*Dp/dist.
+// Faces inside one phase divide by BetaM or BetaP; they multiply by the
+// reciprocal (rM = 1/BetaM, rP = 1/BetaP, each a correctly rounded FP64
+// division made once per thread) instead, which moves G by at most an ulp
+// of an FP64 division on the slow FP64 pipe (the velocities are compared
+// with the oracle to a tolerance, the operator bit for bit).
 __device__ __forceinline__ bool face_grad(int cs, int cn, double phis, double phin, double pps,
-                                          double ppn, double bP, double bM, double Dp,
-                                          double dist, double* G) {
+                                          double ppn, double bP, double bM, double rP, double rM,
+                                          double Dp, double dist, double* G) {
   const double tol = 1.0e-24;
-  double BW;
+  const double t = mul(mul(sub(ppn, pps), bM), bP);
+  double q;
   if (cs == 1) {
     if (cn == 2) {
       double l = dvd(fabs(phis), add(add(fabs(phis), fabs(phin)), tol));
-      BW = add(mul(l, bM), mul(sub(1.0, l), bP));
+      q = dvd(t, add(mul(l, bM), mul(sub(1.0, l), bP)));
     } else if (cn == 1) {
-      BW = bM;
+      q = mul(t, rM);
     } else {
       return false;
     }
   } else if (cs == 2) {
     if (cn == 1) {
       double l = dvd(fabs(phis), add(add(fabs(phis), fabs(phin)), tol));
-      BW = add(mul(l, bP), mul(sub(1.0, l), bM));
+      q = dvd(t, add(mul(l, bP), mul(sub(1.0, l), bM)));
     } else if (cn == 2) {
-      BW = bP;
+      q = mul(t, rP);
     } else {
       return false;
     }
   } else {
     return false;
   }
-  *G = dvd(mul(dvd(mul(mul(sub(ppn, pps), bM), bP), BW), Dp), dist);
+  *G = dvd(mul(q, Dp), dist);
   return true;
 }
 
@@ -636,6 +642,7 @@ __global__ void k_final_solution(FortranIn in, LevelView L, const double* __rest
   const int ix = blockIdx.x * kBX + threadIdx.x;
   const int P = L.pitch;
   double acc = 0.0;
+  const double rP = dvd(1.0, in.betaP), rM = dvd(1.0, in.betaM);
   if (ix < nx) {
     for (int iy = blockIdx.y * kBY + threadIdx.y; iy < ny; iy += gridDim.y * kBY) {
       const int i = ix + 1, j = iy + 1;
@@ -655,7 +662,7 @@ __global__ void k_final_solution(FortranIn in, LevelView L, const double* __rest
         }
       }
       if (act) {
-        double ax = fmax(L.dg[kl], 0.0) * x[kl] - L.cE[kl] * x[kl + 1] - L.cE[kl - 1] * x[kl - 1] -
+        double ax = pos_part(L.dg[kl]) * x[kl] - L.cE[kl] * x[kl + 1] - L.cE[kl - 1] * x[kl - 1] -
                     L.cN[kl] * x[kl + P] - L.cN[kl - P] * x[kl - P];
         double rr = bvec[kl] - ax;
         acc = fma(rr, rr, acc);
@@ -669,7 +676,7 @@ __global__ void k_final_solution(FortranIn in, LevelView L, const double* __rest
         const double ppn = in.posnu_p[fo0(nx, i + 1, j)] != -1 ? x[kl + 1] : 0.0;
         double G;
         if (face_grad(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], ppc,
-                      ppn, bP, bM, in.DpU[k0], in.dxU[k1], &G))
+                      ppn, bP, bM, rP, rM, in.DpU[k0], in.dxU[k1], &G))
           u[k0] = sub(us[k0], G);
       }
       if (j <= ny - 1 && in.posnu_v[k0] != -1 && in.moex_v[k1] != 1) {
@@ -677,7 +684,7 @@ __global__ void k_final_solution(FortranIn in, LevelView L, const double* __rest
         const double ppn = in.posnu_p[fo0(nx, i, j + 1)] != -1 ? x[kl + P] : 0.0;
         double G;
         if (face_grad(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], ppc,
-                      ppn, bP, bM, in.DpV[k0], in.dyV[k1], &G))
+                      ppn, bP, bM, rP, rM, in.DpV[k0], in.dyV[k1], &G))
           v[k0] = sub(vs[k0], G);
       }
       if (act) p[k0] = ppc;
