@@ -301,7 +301,8 @@ __global__ void k_assemble(FortranIn in, LevelView L, Scalars* sc) {
 }
 
 // diagonal excess dg - (cE + cW + cN + cS), clamped at zero, and the
-// inverse diagonal (0 where the cell has no unknown)
+// inverse diagonal (0 where the cell has no unknown; skipped when di is null:
+// the mixed-precision hierarchy builds its own FP32 inverse diagonals)
 __global__ void k_excess(LevelView L, double* di) {
   pdl_wait();
   const int ix = blockIdx.x * kBX + threadIdx.x;
@@ -309,7 +310,7 @@ __global__ void k_excess(LevelView L, double* di) {
   for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY) {
     const size_t k = (size_t)iy * L.pitch + ix;
     const double d = L.dg[k];
-    di[k] = d > 0.0 ? 1.0 / d : 0.0;
+    if (di) di[k] = d > 0.0 ? 1.0 / d : 0.0;
     if (d < 0.0) { L.ex[k] = 0.0; continue; }
     double s = add(add(add(L.cE[k], L.cE[k - 1]), L.cN[k]), L.cN[k - L.pitch]);
     double e = sub(d, s);
@@ -359,7 +360,7 @@ __global__ void k_coarsen(LevelView F, LevelView C, double* di) {
       if (!(d > 0.0)) d = -1.0;
     }
     C.dg[kc] = d;
-    di[kc] = d > 0.0 ? 1.0 / d : 0.0;
+    if (di) di[kc] = d > 0.0 ? 1.0 / d : 0.0;
   }
 }
 

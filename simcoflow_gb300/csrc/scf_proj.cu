@@ -409,9 +409,10 @@ void enqueue_line_setup_t(const std::vector<MgView<T, CT, T>>& nat,
 // assembly of the fine operator and setup of the whole hierarchy
 void enqueue_setup(scf_proj* h, Scalars* sc, cudaStream_t s) {
   launch_assemble(h->fin, h->lev[0], sc, s);
-  launch_excess(h->lev[0], h->di64[0], s);
+  // FP64 inverse diagonals serve the FP64 smoothers only
+  launch_excess(h->lev[0], h->mixed ? nullptr : h->di64[0], s);
   for (size_t l = 1; l < h->lev.size(); ++l)
-    launch_coarsen(h->lev[l - 1], h->lev[l], h->di64[l], s);
+    launch_coarsen(h->lev[l - 1], h->lev[l], h->mixed ? nullptr : h->di64[l], s);
   launch_coarse_setup(h->lev.back(), h->Ainv, h->cmap, h->ncoarse, s);
   if (h->mixed)
     for (size_t l = 0; l < h->lev.size(); ++l) {
