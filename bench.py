@@ -129,6 +129,17 @@ def _dist():
     return world, rank, local
 
 
+def reduce_max(x: float, pg, device) -> float:
+    """Max of x over the ranks of process group module pg (None: one rank).
+    The timed region's length is the slowest replica's."""
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
 def make_case(name: str, rank: int):
     from simcoflow_gb300 import synth
     return synth.make_case(name, instance=rank)
@@ -339,11 +350,7 @@ def run_ours(args):
         torch.cuda.synchronize(dev)
 
     def max_over_ranks(x):
-        if pg:
-            t = torch.tensor([x], device=dev)
-            pg.all_reduce(t, op=pg.ReduceOp.MAX)
-            return float(t.item())
-        return x
+        return reduce_max(x, pg, dev)
 
     tdev = {k: torch.from_numpy(np.ascontiguousarray(v.ravel(order="F"))).to(dev)
             for k, v in A.items() if isinstance(v, np.ndarray)}
