@@ -868,6 +868,44 @@ __global__ void __launch_bounds__(1024) k_line_tail(TailDesc<T, CT> d, Scalars* 
     const T* b = B(l);
     const T* g = G(l);
     T* x = X(l);
+    if (std::is_same<T, double>::value && len <= 32) {
+      // FP64: one warp per line, one cell per lane, cyclic reduction by
+      // shuffles -- log2 len steps instead of 2 len dependent elimination
+      // steps, which the FP64 pipe's latency makes long.  (FP32 keeps the
+      // serial elimination: with the approximate reciprocal the reduction
+      // costs the coarse correction enough accuracy for an extra PCG
+      // iteration.)
+      const int lane = t & 31, nwarp = NTT >> 5;
+      for (int q = colour + 2 * (t >> 5); q < nlines; q += 2 * nwarp) {
+        const int si = (dir == 0 ? (q + 1) * w + 1 : w + q + 1) + lane * step;
+        T a = T(0), c = T(0), dd = T(1), r = T(0);
+        const bool in = lane < len;
+        const T gv = in ? g[si] : T(0);
+        if (gv > T(0)) {
+          a = -Ax[si - step];
+          c = -Ax[si];
+          dd = gv;
+          r = fma(Cx[si], x[si + cross], b[si]);
+          r = fma(Cx[si - cross], x[si - cross], r);
+        }
+        if (lane == 0) a = T(0);        // the ghost before the line start
+        if (lane >= len - 1) c = T(0);  // and after its end
+        for (int sh = 1; sh < len; sh <<= 1) {
+          const T am = __shfl_up_sync(0xffffffffu, a, sh), bm = __shfl_up_sync(0xffffffffu, dd, sh);
+          const T cm = __shfl_up_sync(0xffffffffu, c, sh), rm = __shfl_up_sync(0xffffffffu, r, sh);
+          const T ap = __shfl_down_sync(0xffffffffu, a, sh), bp = __shfl_down_sync(0xffffffffu, dd, sh);
+          const T cp = __shfl_down_sync(0xffffffffu, c, sh), rp = __shfl_down_sync(0xffffffffu, r, sh);
+          const T k1 = a * lrcp(bm), k2 = c * lrcp(bp);
+          a = -am * k1;
+          c = -cp * k2;
+          dd = fma(-ap, k2, fma(-cm, k1, dd));
+          r = fma(-rp, k2, fma(-rm, k1, r));
+        }
+        if (in) x[si] = gv > T(0) ? r * lrcp(dd) : T(0);
+      }
+      __syncthreads();
+      return;
+    }
     for (int q = colour + 2 * t; q < nlines; q += 2 * NTT) {
       int si = (dir == 0 ? (q + 1) * w + 1 : w + q + 1);
       T cpp = T(0), dpp = T(0);
