@@ -1,6 +1,7 @@
 """Build recipe of the oracle (test infrastructure only).
 
-Compiles oracle/scf_oracle.c into oracle/_build/liboracle.so with gcc.
+Compiles oracle/scf_oracle.c (projection) and oracle/mom_oracle.c (momentum
+predictor solves) into oracle/_build/liboracle.so with gcc.
 -ffp-contract=off keeps every multiply and add separately rounded, as in
 the reference's Fortran build (mpif77 without FMA flags), so that the
 restatement gives the same bits on x86-64 and aarch64.
@@ -15,11 +16,12 @@ OUT = HERE / "_build" / "liboracle.so"
 
 
 def build(force: bool = False) -> Path:
-    src = HERE / "scf_oracle.c"
+    srcs = [HERE / "scf_oracle.c", HERE / "mom_oracle.c"]
     OUT.parent.mkdir(exist_ok=True)
-    if force or not OUT.exists() or OUT.stat().st_mtime < src.stat().st_mtime:
+    newest = max(p.stat().st_mtime for p in srcs)
+    if force or not OUT.exists() or OUT.stat().st_mtime < newest:
         cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-               str(src), "-o", str(OUT), "-lm"]
+               *map(str, srcs), "-o", str(OUT), "-lm"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"oracle build failed:\n{r.stderr}")

@@ -23,6 +23,10 @@ Pieces:
   geometry_literal  pure-Python restatement of Cell_Geo_Cal, frac, numbering
                 and DefineMomentumExchangeCell for small grids, to check the
                 package's geometry builder.
+  C restatement of the momentum predictor's implicit solves (mom_oracle.c)
+    mom_predict SetMatrix, SetVectors, solve, DeltaGetValues, gradient update,
+                Dp copies              src/PredictorUV_mod.f90:507-563, 622-885
+                (solve: SuperLU, or the C BiCGStab of the CPU baseline)
 """
 from __future__ import annotations
 
@@ -66,6 +70,16 @@ def lib():
                                    C.c_int]
         L.oracle_vcycle.argtypes = [C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_int, C.c_int,
                                     C.c_double, C.c_int, C.c_int]
+        L.oracle_mom_matrix.restype = C.c_int
+        L.oracle_mom_matrix.argtypes = ([C.c_int] * 4 + [_P, _P, _I] + [_P] * 10 +
+                                        [_P, _P, _P, _P, _P])
+        L.oracle_mom_vectors.argtypes = ([C.c_int] * 4 + [_I, _P, _P, _P, _P, _P, _P, _P,
+                                         C.c_double, _P])
+        L.oracle_mom_finish.argtypes = ([C.c_int] * 4 + [_I, _P, _P, _P, _P, C.c_double, _P,
+                                        _P])
+        L.oracle_mom_bicgstab.restype = C.c_int
+        L.oracle_mom_bicgstab.argtypes = ([C.c_int] * 4 + [_I, _P, _P, C.c_double, C.c_int, _P,
+                                          C.POINTER(C.c_double)])
         L.oracle_num_threads.restype = C.c_int
         L.oracle_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -381,3 +395,80 @@ def geometry_literal(nx, ny, dxP, dyP, vofS_in, phiS, nxS, nyS, vofS_u_in, vofS_
     return {"aE": E, "aW": W, "aN": N, "aS": S, "WlLh": WL, "vofS": vs, "nyS": ny_s, "nxS": nx_s,
             "posnu_p": pp, "posnu_u": pu, "posnu_v": pv, "moex_u": mu, "moex_v": mv,
             "vofS_u": vsu, "vofS_v": vsv}
+
+
+# ---------------------------------------------------------------------------
+# Momentum predictor: implicit solve of one velocity component
+# ---------------------------------------------------------------------------
+def mom_operator(mi) -> dict:
+    """SetMatrix + SetVectors on the inputs of synth.momentum_inputs:
+    matr (nx,ny,5: S,W,P,E,N), rhm, Dp (assembled cells), CWE, CSN."""
+    L = lib()
+    nx, ny, iu, iv = mi["nx"], mi["ny"], mi["iu"], mi["iv"]
+    cst = np.array([mi["dt"], mi["beta_vis"], mi["nua"], mi["nuw"], mi["nuref"], mi["rey"]])
+    matr = np.zeros((nx, ny, 5), order="F")
+    Dp = mi["Dp"].copy(order="F")
+    cwe = np.zeros((ny, 2), order="F")
+    csn = np.zeros((nx, 2), order="F")
+    rc = L.oracle_mom_matrix(nx, ny, iu, iv, _p(mi["dx"]), _p(mi["dy"]), _p(mi["posnu"]),
+                             _p(mi["vof"]), _p(mi["vofS"]), _p(mi["etaE"]), _p(mi["etaN"]),
+                             _p(mi["WlLh"]), _p(mi["delh"]), _p(mi["difEW"]), _p(mi["difNS"]),
+                             _p(mi["edEW"]), _p(mi["edNS"]), _p(cst), _p(Dp), _p(cwe),
+                             _p(csn), _p(matr))
+    rhm = np.zeros((nx, ny), order="F")
+    L.oracle_mom_vectors(nx, ny, iu, iv, _p(mi["posnu"]), _p(mi["dx"]), _p(mi["dy"]),
+                         _p(mi["flux"]), _p(cwe), _p(csn), _p(mi["u"]), _p(mi["v"]),
+                         mi["fr"], _p(rhm))
+    return {"matr": matr, "rhm": rhm, "Dp": Dp, "cwe": cwe, "csn": csn, "bad": rc != 0}
+
+
+def mom_csr(mi, matr):
+    """The system of the numbered cells (Posnu order) as a CSR matrix."""
+    import scipy.sparse as sp
+    nx, ny = mi["nx"], mi["ny"]
+    pn = mi["posnu"][1:nx + 1, 1:ny + 1]
+    act = pn != -1
+    n = int(act.sum())
+    rows, cols, vals = [], [], []
+    idx = np.argwhere(act)
+    r = pn[act]
+    I, J = idx[:, 0], idx[:, 1]
+    for f, (di, dj) in enumerate([(0, -1), (-1, 0), (0, 0), (1, 0), (0, 1)]):
+        ii, jj = I + di, J + dj
+        ok = (ii >= 0) & (ii < nx) & (jj >= 0) & (jj < ny)
+        c = np.full(len(I), -1)
+        c[ok] = pn[ii[ok], jj[ok]]
+        ok &= c != -1
+        rows.append(r[ok]); cols.append(c[ok]); vals.append(matr[I[ok], J[ok], f])
+    A = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                      shape=(n, n))
+    return A, r, I, J
+
+
+def mom_predict(mi, solver="direct", rtol=1e-14, maxit=500) -> dict:
+    """The whole implicit step of one component: operator, right-hand side,
+    solve (SuperLU, or the C BiCGStab), Pred and Dp with their boundary
+    copies.  Returns pred, Dp, matr, rhm, x (by unknown), iterations."""
+    L = lib()
+    op = mom_operator(mi)
+    nx, ny, iu, iv = mi["nx"], mi["ny"], mi["iu"], mi["iv"]
+    A, r, I, J = mom_csr(mi, op["matr"])
+    b = np.zeros(A.shape[0])
+    b[r] = op["rhm"][I, J]
+    its = 0
+    if solver == "direct":
+        x = solve_direct(A, b)
+    else:
+        xg = np.zeros((nx, ny), order="F")
+        rel = C.c_double(0.0)
+        its = L.oracle_mom_bicgstab(nx, ny, iu, iv, _p(mi["posnu"]), _p(op["matr"]),
+                                    _p(op["rhm"]), rtol, maxit, _p(xg), C.byref(rel))
+        x = np.zeros(A.shape[0])
+        x[r] = xg[I, J]
+    xv = np.ascontiguousarray(x, dtype=np.float64)
+    pred = mi["pred"].copy(order="F")
+    Dp = op["Dp"]
+    L.oracle_mom_finish(nx, ny, iu, iv, _p(mi["posnu"]), _p(xv), _p(mi["gradp"]),
+                        _p(mi["dx"]), _p(mi["dy"]), mi["dt"], _p(pred), _p(Dp))
+    return {"pred": pred, "Dp": Dp, "matr": op["matr"], "rhm": op["rhm"], "x": x,
+            "A": A, "b": b, "iters": its, "bad": op["bad"]}

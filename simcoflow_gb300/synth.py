@@ -210,3 +210,89 @@ CONFIGS = {"c1": c1, "c2": c2, "c3": c3, "c4": c4, "c5": c5}
 
 def make_case(name: str, **kw) -> Case:
     return CONFIGS[name](**kw)
+
+
+# ---------------------------------------------------------------------------
+# Momentum-predictor solves (one velocity component each): the inputs of
+# SetMatrix / SetVectors (src/PredictorUV_mod.f90:622-846) on the U or V
+# cells of a projection case.  The face fluxes are computed upstream by the
+# predictor's flux routines, which are not on this path: here they are
+# seeded fields of the same shapes and magnitudes -- diffusive conductances
+# nu_mix/nu_ref/Re * (face length / centre distance) * open face fraction
+# with the mixture viscosity of the cells' liquid fraction, skew ("ED")
+# fluxes of a fraction of that only in cut cells, smooth convective-flux
+# divergence and pressure-gradient fields, upwind weights Eta in [0.3, 0.7].
+# ---------------------------------------------------------------------------
+NU_W, NU_A = 1.0034e-6, 1.506e-5   # src/StateVariables.f90:26-27
+BETA_VIS = 0.5                       # src/StateVariables.f90:28
+
+
+def momentum_inputs(case: Case, comp: str, rey: float = 1.0e5, seed: int = 0) -> dict:
+    """Inputs of one component's implicit solve ('u' or 'v') for `case`.
+    Array layouts are the reference's (Fortran order): (nx,ny) for grid and
+    cell fields, (nx+2,ny+2) for Posnu/EtaE/EtaN/velocities/Dp/Pred,
+    (nx+1,ny) for the east-west face fluxes and (nx,ny+1) for north-south."""
+    if comp not in ("u", "v"):
+        raise ValueError("comp must be 'u' or 'v'")
+    A = case.arrays
+    nx, ny = case.nx, case.ny
+    iu, iv = (1, 0) if comp == "u" else (0, 1)
+    rng = _rng(7, seed + (0 if comp == "u" else 1))
+    F = lambda a: np.asfortranarray(a)
+    vofP, wlP = A["vof"], A["WlLh"]
+    if comp == "u":
+        dxc, dyc = A["dxU"], A["dy"]
+        vof = vofP.copy(order="F")
+        vof[:-1, :] = 0.5 * (vofP[:-1, :] + vofP[1:, :])
+        wl = wlP.copy(order="F")
+        wl[:-1, :] = 0.5 * (wlP[:-1, :] + wlP[1:, :])
+        vofS, posnu = A["vofS_u"], A["posnu_u"]
+    else:
+        dxc, dyc = A["dx"], A["dyV"]
+        vof = vofP.copy(order="F")
+        vof[:, :-1] = 0.5 * (vofP[:, :-1] + vofP[:, 1:])
+        wl = wlP.copy(order="F")
+        wl[:, :-1] = 0.5 * (wlP[:, :-1] + wlP[:, 1:])
+        vofS, posnu = A["vofS_v"], A["posnu_v"]
+    vof = np.asfortranarray(np.minimum(vof, 1.0 - vofS))  # liquid within the open part
+    vf = np.clip(vof / np.maximum(1.0 - vofS, 1e-3), 0.0, 1.0)
+    visc = ((1.0 - vf) * NU_A / NU_W + vf * NU_W / NU_W) / rey   # nu_mix / nu_ref / Re
+    cut = (vofS > 0.0) & (vofS < 1.0)
+    # east-west faces i = 1..nx+1 (face i is the west face of cell i)
+    vE = np.empty((nx + 1, ny)); vE[1:-1] = 0.5 * (visc[1:] + visc[:-1])
+    vE[0], vE[-1] = visc[0], visc[-1]
+    gE = np.empty((nx + 1, ny)); gE[1:-1] = dyc[1:] / (0.5 * (dxc[1:] + dxc[:-1]))
+    gE[0], gE[-1] = dyc[0] / dxc[0], dyc[-1] / dxc[-1]
+    vN = np.empty((nx, ny + 1)); vN[:, 1:-1] = 0.5 * (visc[:, 1:] + visc[:, :-1])
+    vN[:, 0], vN[:, -1] = visc[:, 0], visc[:, -1]
+    gN = np.empty((nx, ny + 1)); gN[:, 1:-1] = dxc[:, 1:] / (0.5 * (dyc[:, 1:] + dyc[:, :-1]))
+    gN[:, 0], gN[:, -1] = dxc[:, 0] / dyc[:, 0], dxc[:, -1] / dyc[:, -1]
+    # open fraction of each face (the lesser of its two cells' open fractions)
+    op = 1.0 - vofS
+    aE = np.empty((nx + 1, ny)); aE[1:-1] = np.minimum(op[1:], op[:-1])
+    aE[0], aE[-1] = op[0], op[-1]
+    aN = np.empty((nx, ny + 1)); aN[:, 1:-1] = np.minimum(op[:, 1:], op[:, :-1])
+    aN[:, 0], aN[:, -1] = op[:, 0], op[:, -1]
+    difEW, difNS = F(vE * gE * aE), F(vN * gN * aN)
+    cutE = np.zeros((nx + 1, ny), bool); cutE[1:] |= cut; cutE[:-1] |= cut
+    cutN = np.zeros((nx, ny + 1), bool); cutN[:, 1:] |= cut; cutN[:, :-1] |= cut
+    edEW = F(np.where(cutE, rng.uniform(-0.3, 0.3, (nx + 1, ny)) * difEW, 0.0))
+    edNS = F(np.where(cutN, rng.uniform(-0.3, 0.3, (nx, ny + 1)) * difNS, 0.0))
+    xs, ys = np.linspace(0, 1, nx + 2), np.linspace(0, 1, ny + 2)
+    eta_e = F(0.5 + 0.2 * _field(xs, ys, _modes(rng, 4)) / 0.4)
+    eta_n = F(0.5 + 0.2 * _field(xs, ys, _modes(rng, 4)) / 0.4)
+    eta_e, eta_n = F(np.clip(eta_e, 0.3, 0.7)), F(np.clip(eta_n, 0.3, 0.7))
+    area = dxc * dyc
+    xc, yc = np.linspace(0, 1, nx), np.linspace(0, 1, ny)
+    flux = F(_field(xc, yc, _modes(rng, 8)) * area)
+    gradp = F(_field(xc, yc, _modes(rng, 8)) * area * 10.0)
+    vel = A["u0"] if comp == "u" else A["v0"]
+    return {"comp": comp, "iu": iu, "iv": iv, "nx": nx, "ny": ny,
+            "dx": F(dxc), "dy": F(dyc), "posnu": posnu, "vof": F(vof), "vofS": vofS,
+            "etaE": eta_e, "etaN": eta_n, "WlLh": F(wl), "delh": F(0.5 * dxc),
+            "difEW": difEW, "difNS": difNS, "edEW": edEW, "edNS": edNS,
+            "flux": flux, "gradp": gradp, "u": A["u0"], "v": A["v0"],
+            "pred": vel.copy(order="F"),
+            "Dp": (A["DpU"] if comp == "u" else A["DpV"]).copy(order="F"),
+            "dt": case.dt, "beta_vis": BETA_VIS, "nua": NU_A, "nuw": NU_W, "nuref": NU_W,
+            "rey": rey, "fr": 1.0 / np.sqrt(9.81)}

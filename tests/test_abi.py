@@ -81,3 +81,36 @@ def test_host_only_entry_points(built):
     bad.coarse_max = 1000
     assert L.scf_proj_create(ctypes.byref(h), 8, 8, ctypes.byref(bad)) == -1
     assert L.scf_proj_destroy(None) == 0
+
+
+def test_proj_library_exports_momentum_header_symbols(built):
+    from simcoflow_gb300 import build, momentum
+    lib = ctypes.CDLL(str(build.build_proj()))
+    names = _declared("scf_mom.h")
+    for n in names:
+        assert hasattr(lib, n), n
+    assert sorted(momentum.EXPORTS) == names
+
+
+def test_momentum_input_struct_layout(tmp_path):
+    """The ctypes mirror of scf_mom_in has the header's layout."""
+    import shutil
+    import subprocess
+    if not shutil.which("gcc"):
+        import pytest
+        pytest.skip("no C compiler")
+    from simcoflow_gb300 import momentum as M
+    src = tmp_path / "lay.c"
+    fields = [n for n, _ in M.MomIn._fields_]
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "scf_mom.h"\n'
+        "int main(void) {\n"
+        '  printf("%zu\\n", sizeof(scf_mom_in));\n'
+        + "".join(f'  printf("%zu\\n", offsetof(scf_mom_in, {n}));\n' for n in fields)
+        + "  return 0;\n}\n")
+    exe = tmp_path / "lay"
+    subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    assert int(out[0]) == ctypes.sizeof(M.MomIn)
+    for n, off in zip(fields, out[1:]):
+        assert int(off) == getattr(M.MomIn, n).offset, n
