@@ -271,6 +271,59 @@ def extra_stretched(local, args):
     return out
 
 
+def extra_momentum(case, local, args):
+    """The momentum predictor's implicit solves (u and v) on the headline
+    workload's cells: device-resident GPU time against the C restatement
+    (operator, right-hand side, BiCGStab, scatter) on all host cores."""
+    import torch
+    from simcoflow_gb300 import momentum as M
+    from simcoflow_gb300 import synth
+    dev = torch.device("cuda", local)
+    out = {"workload": f"u and v implicit solves on the {case.nx}x{case.ny} cells of the "
+                       "headline workload (seeded face fluxes, Re 1e5)"}
+    T = lambda x: torch.from_numpy(np.ascontiguousarray(x.ravel(order="F"))).to(dev)
+    mis = {c: synth.momentum_inputs(case, c) for c in ("u", "v")}
+    s = M.MomentumSolver(case.nx, case.ny, device_ptrs=True, device=local)
+    try:
+        tin = {c: {k: (T(v) if isinstance(v, np.ndarray) else v) for k, v in mi.items()}
+               for c, mi in mis.items()}
+        work = {c: (T(mi["pred"]), T(mi["Dp"])) for c, mi in mis.items()}
+
+        def step():
+            sts = []
+            for c in ("u", "v"):
+                pred, Dp = work[c]
+                sts.append(s.solve(c, tin[c], pred, Dp, rtol=1e-13))
+            return sts
+
+        for _ in range(3):
+            step()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        reps = 10
+        for _ in range(reps):
+            sts = step()
+        torch.cuda.synchronize(dev)
+        ms = (time.perf_counter() - t0) / reps * 1e3
+    finally:
+        s.close()
+    out["gpu"] = {"ms_u_plus_v": round(ms, 3), "iters": [st.iters for st in sts],
+                  "relres": [st.relres for st in sts], "launches": sum(st.launches for st in sts),
+                  "timing": "host clock around 10 steps (each solve ends with a host poll)"}
+    if not args.no_cpu:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle as O
+        threads = os.cpu_count() or 1
+        O.lib().oracle_set_threads(threads)
+        t0 = time.perf_counter()
+        its = [O.mom_predict(mis[c], solver="bicgstab", rtol=1e-13)["iters"] for c in ("u", "v")]
+        cpu_ms = (time.perf_counter() - t0) * 1e3
+        out["cpu"] = {"ms_u_plus_v": round(cpu_ms, 1), "cores": threads, "kind": "port",
+                      "iters": its, "sample": "one u and one v solve (C restatement, OpenMP)"}
+        out["speedup_vs_cpu"] = round(cpu_ms / ms, 1)
+    return out
+
+
 def extra_batch(local):
     """64 uneven instances in one graph launch with autotuned schedules."""
     from simcoflow_gb300 import synth, batch as Bt
@@ -527,7 +580,8 @@ def run_ours(args):
     if world == 1 and not args.no_extras:
         for name, fn in (("learned", lambda: extra_learned(case, tdev, dev, local, args)),
                          ("stretched_4096", lambda: extra_stretched(local, args)),
-                         ("batch_64", lambda: extra_batch(local))):
+                         ("batch_64", lambda: extra_batch(local)),
+                         ("momentum_2048", lambda: extra_momentum(case, local, args))):
             try:
                 extras[name] = fn()
             except Exception as e:  # an extra must not hide the headline line
