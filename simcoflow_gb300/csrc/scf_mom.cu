@@ -97,6 +97,20 @@ __device__ bool gsum2(double a, double b, double* part, unsigned* ticket, double
   return true;
 }
 
+// x / d where d is 1.0 in most cells (an open cell's 1 - vofS): IEEE
+// division by one is exact, so the FP64 division (slow on GB300's FP64
+// pipe) is skipped there without changing a bit
+__device__ __forceinline__ double div_open(double x, double d, bool one) {
+  return one ? x : dvd(x, d);
+}
+// approximate 1/x for the Jacobi preconditioner (x > 0): an FP32 seed refined
+// by two Newton-Raphson steps r <- r (2 - x r) (22 -> 44 -> ~53 correct bits)
+__device__ __forceinline__ double rcp_newton(double x) {
+  double r = (double)__frcp_rn((float)x);
+  r = r * fma(-x, r, 2.0);
+  return r * fma(-x, r, 2.0);
+}
+
 #define MF1(a, i, j) (a)[(size_t)((i)-1) + (size_t)((j)-1) * (size_t)nx]
 #define MF0(a, i, j) (a)[(size_t)(i) + (size_t)(j) * (size_t)(nx + 2)]
 #define MFE(a, i, j) (a)[(size_t)((i)-1) + (size_t)((j)-1) * (size_t)(nx + 1)]
@@ -113,6 +127,8 @@ __global__ void k_mom_assemble(MomIn in, int iu, int iv, MomOp M, double* Dp, do
   const int ix = blockIdx.x * 32 + threadIdx.x;
   double acc = 0.0;
   bool bad = false;
+  const double ob = sub(1.0, in.beta_vis);
+  const double ifr2 = dvd(1.0, mul(in.fr, in.fr));  // 1/Fr**2, the same for every cell
   if (ix < nx) {
     for (int iy = blockIdx.y * 8 + threadIdx.y; iy < ny; iy += gridDim.y * 8) {
       const int i = ix + 1, j = iy + 1;
@@ -120,23 +136,23 @@ __global__ void k_mom_assemble(MomIn in, int iu, int iv, MomOp M, double* Dp, do
       double cP = 0.0, cW = 0.0, cE = 0.0, cS = 0.0, cN = 0.0, rhs = 0.0, dinv = 0.0;
       if (i <= nx - iu && j <= ny - iv && MF0(in.posnu, i, j) != -1) {
         const double VofAF = sub(1.0, MF1(in.vofS, i, j));
-        const double ob = sub(1.0, in.beta_vis);
-        double De = dvd(mul(ob, MFE(in.difEW, i + 1, j)), VofAF);
-        double Dw = dvd(mul(ob, MFE(in.difEW, i, j)), VofAF);
-        double Dn = dvd(mul(ob, MFN(in.difNS, i, j + 1)), VofAF);
-        const double Ds = dvd(mul(ob, MFN(in.difNS, i, j)), VofAF);
+        const bool one = __double_as_longlong(VofAF) == 0x3ff0000000000000ll;  // 1.0
+        double De = div_open(mul(ob, MFE(in.difEW, i + 1, j)), VofAF, one);
+        double Dw = div_open(mul(ob, MFE(in.difEW, i, j)), VofAF, one);
+        double Dn = div_open(mul(ob, MFN(in.difNS, i, j + 1)), VofAF, one);
+        const double Ds = div_open(mul(ob, MFN(in.difNS, i, j)), VofAF, one);
         const double ee = MF0(in.etaE, i, j), ew = MF0(in.etaE, i - 1, j);
         const double en = MF0(in.etaN, i, j), es = MF0(in.etaN, i, j - 1);
         const double fe = MFE(in.edEW, i + 1, j), fw = MFE(in.edEW, i, j);
         const double fn = MFN(in.edNS, i, j + 1), fs = MFN(in.edNS, i, j);
-        const double Fep = dvd(mul(fe, sub(1.0, ee)), VofAF);
-        const double Fem = dvd(mul(fe, ee), VofAF);
-        const double Fwp = dvd(mul(fw, ew), VofAF);
-        const double Fwm = dvd(mul(fw, sub(1.0, ew)), VofAF);
-        const double Fnp = dvd(mul(fn, sub(1.0, en)), VofAF);
-        const double Fnm = dvd(mul(fn, en), VofAF);
-        const double Fsp = dvd(mul(fs, es), VofAF);
-        const double Fsm = dvd(mul(fs, sub(1.0, es)), VofAF);
+        const double Fep = div_open(mul(fe, sub(1.0, ee)), VofAF, one);
+        const double Fem = div_open(mul(fe, ee), VofAF, one);
+        const double Fwp = div_open(mul(fw, ew), VofAF, one);
+        const double Fwm = div_open(mul(fw, sub(1.0, ew)), VofAF, one);
+        const double Fnp = div_open(mul(fn, sub(1.0, en)), VofAF, one);
+        const double Fnm = div_open(mul(fn, en), VofAF, one);
+        const double Fsp = div_open(mul(fs, es), VofAF, one);
+        const double Fsm = div_open(mul(fs, sub(1.0, es)), VofAF, one);
         if (iu == 1) {
           if (j == ny) Dn = 0.0;
           if (i == nx - iu) De = 0.0;
@@ -147,12 +163,18 @@ __global__ void k_mom_assemble(MomIn in, int iu, int iv, MomOp M, double* Dp, do
         double aE = De, aW = Dw, aN = Dn, aS = Ds;
         const double cwe1 = aW, cwe2 = aE, csn1 = aS;  // CWE(j,1), CWE(j,2), CSN(i,1)
         const double dxy = mul(MF1(in.dx, i, j), MF1(in.dy, i, j));
-        const double rv = dvd(MF1(in.vof, i, j), sub(1.0, MF1(in.vofS, i, j)));
-        const double visc = add(dvd(mul(sub(1.0, rv), in.nua), in.nuref),
-                                dvd(mul(rv, in.nuw), in.nuref));
-        const double wall =
-            dvd(dvd(mul(dvd(visc, in.rey), MF1(in.WlLh, i, j)), MF1(in.delh, i, j)), VofAF);
-        double aP = add(add(add(add(add(dvd(dxy, in.dt), aE), aW), aN), aS), wall);
+        double aP = add(add(add(add(dvd(dxy, in.dt), aE), aW), aN), aS);
+        const double wl = MF1(in.WlLh, i, j), dh = MF1(in.delh, i, j);
+        // the wall-shear term: without a wall (WlLh = 0, finite vof, finite
+        // nonzero delh) it is a signed zero added to the positive sum above,
+        // which leaves aP unchanged; otherwise (NaN included) it is evaluated
+        const bool nowall = wl == 0.0 && isfinite(MF1(in.vof, i, j)) && isfinite(dh) && dh != 0.0;
+        if (!nowall) {
+          const double rv = dvd(MF1(in.vof, i, j), sub(1.0, MF1(in.vofS, i, j)));
+          const double visc = add(dvd(mul(sub(1.0, rv), in.nua), in.nuref),
+                                  dvd(mul(rv, in.nuw), in.nuref));
+          aP = add(aP, div_open(dvd(mul(dvd(visc, in.rey), wl), dh), VofAF, one));
+        }
         aP = sub(add(sub(add(aP, Fep), Fwp), Fnp), Fsp);
         aE = sub(aE, Fem);
         aW = add(aW, Fwm);
@@ -171,8 +193,7 @@ __global__ void k_mom_assemble(MomIn in, int iu, int iv, MomOp M, double* Dp, do
         // does not set are undefined, so the term is +0 times the ghost.
         const double diu = (double)iu, dv = (double)iv;
         rhs = sub(0.0, MF1(in.flux, i, j));
-        if (iv == 1) rhs = sub(rhs, mul(mul(dvd(1.0, mul(in.fr, in.fr)), MF1(in.dx, i, j)),
-                                        MF1(in.dy, i, j)));
+        if (iv == 1) rhs = sub(rhs, mul(mul(ifr2, MF1(in.dx, i, j)), MF1(in.dy, i, j)));
         if (i == 1)
           rhs = add(rhs, mul(cwe1, add(mul(diu, MF0(in.u, i - 1, j)), mul(dv, MF0(in.v, i - 1, j)))));
         if (i == nx - iu)
@@ -181,7 +202,7 @@ __global__ void k_mom_assemble(MomIn in, int iu, int iv, MomOp M, double* Dp, do
           rhs = add(rhs, mul(csn1, add(mul(diu, MF0(in.u, i, j - 1)), mul(dv, MF0(in.v, i, j - 1)))));
         if (j == ny - iv)
           rhs = add(rhs, mul(0.0, add(mul(diu, MF0(in.u, i, j + 1)), mul(dv, MF0(in.v, i, j + 1)))));
-        dinv = 1.0 / aP;
+        dinv = rcp_newton(aP);
       }
       M.P[g] = cP; M.W[g] = cW; M.E[g] = cE; M.S[g] = cS; M.N[g] = cN;
       M.b[g] = rhs;

@@ -14,6 +14,8 @@ profiler can restrict itself to that range (ncu --nvtx --nvtx-include
             the path
   unet      --reps forward passes of the learned preconditioner's network on
             the workload's operator and right-hand side (shipped weights)
+  momentum  --reps pairs of momentum-predictor solves (u then v) on the
+            workload's cells (seeded face fluxes), device-resident
 
     python -m simcoflow_gb300.profile_kernels --config c2 --kernel sweep --precision mixed
     python -m simcoflow_gb300.profile_kernels --config c3 --n 2048 --kernel projection
@@ -35,7 +37,8 @@ KERNELS = {"sweep": (0, {"fp64": 48, "mixed": 20}), "pupdate_spmv": (1, {"fp64":
            "resid_restrict": (3, {"fp64": 58, "mixed": 25}),
            "prolong": (4, {"fp64": 50, "mixed": 21}), "assemble": (5, {"fp64": 200, "mixed": 200}),
            "vcycle": (6, {"fp64": 0, "mixed": 0}), "setup": (7, {"fp64": 0, "mixed": 0}),
-           "projection": (None, {"fp64": 0, "mixed": 0}), "unet": (None, {"fp64": 0, "mixed": 0})}
+           "projection": (None, {"fp64": 0, "mixed": 0}), "unet": (None, {"fp64": 0, "mixed": 0}),
+           "momentum": (None, {"fp64": 0, "mixed": 0})}
 
 
 def main():
@@ -51,6 +54,28 @@ def main():
     c = synth.make_case(args.config, **({"n": args.n} if args.n else {}))
     t = {k: torch.from_numpy(np.ascontiguousarray(v.ravel(order="F"))).to(dev)
          for k, v in c.arrays.items() if isinstance(v, np.ndarray)}
+    if args.kernel == "momentum":
+        from . import momentum as M
+        T = lambda x: torch.from_numpy(np.ascontiguousarray(x.ravel(order="F"))).to(dev)
+        mis = {cp: synth.momentum_inputs(c, cp) for cp in ("u", "v")}
+        tin = {cp: {k: (T(v) if isinstance(v, np.ndarray) else v) for k, v in mi.items()}
+               for cp, mi in mis.items()}
+        work = {cp: (T(mi["pred"]), T(mi["Dp"])) for cp, mi in mis.items()}
+        ms = M.MomentumSolver(c.nx, c.ny, device_ptrs=True)
+        for cp in ("u", "v"):  # warm-up
+            ms.solve(cp, tin[cp], *work[cp])
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("kernels")
+        t0 = time.perf_counter()
+        for _ in range(args.reps):
+            sts = [ms.solve(cp, tin[cp], *work[cp]) for cp in ("u", "v")]
+        torch.cuda.synchronize()
+        dt_ms = (time.perf_counter() - t0) / args.reps * 1e3
+        torch.cuda.nvtx.range_pop()
+        ms.close()
+        print(json.dumps({"config": args.config, "kernel": "momentum", "nx": c.nx, "ny": c.ny,
+                          "ms_u_plus_v": dt_ms, "iters": [s.iters for s in sts]}))
+        return
     direct = args.kernel == "projection"
     s = P.ProjectionSolver(c.nx, c.ny, device_ptrs=True, precision=args.precision,
                            use_graph=not direct)
