@@ -212,6 +212,33 @@ int scf_proj_update_puv(scf_proj *h, const double *ustar, const double *vstar, d
                         double *Pp, double *p, double *u, double *v, double *mres,
                         scf_stats *st);
 
+/* The cut-cell geometry computed on the GPU, in place of
+ * scf_proj_set_geometry: what Grid_Preprocess derives every time step from
+ * the cells' solid level-set fields (src/Cutcell_Mod.f90:18-397: Cell_Geo_Cal
+ * with Edge_Geo_Cal for the pressure cells, the U/V clamps,
+ * DefineMomentumExchangeCell, NumberExternalCell), so that only those fields
+ * cross to the GPU.  Inputs (same memory kind as the handle's other arrays):
+ *   vof, phi        PCell%vof, %phi (nx,ny) from the free-surface step
+ *   vofS, phiS,     PCell%VofS, %PhiS, %nxS, %nyS (nx,ny) as Initial_Clsvof
+ *   nxS, nyS        leaves them for the body
+ *   vofS_u, vofS_v  UCell%VofS, VCell%VofS (nx,ny)
+ *   icorprob        the ICorProb corner rule of Cell_Geo_Cal (src/Main.f90:204)
+ * The handle keeps the result (apertures, WlLh, VofS after the solid and
+ * degenerate-cell rules, nxS/nyS after the corner rule, Posnu of the three
+ * families, MoExCell, clamped U/V solid fractions) on the GPU; it is
+ * bit-identical to the CPU restatement.  Needs scf_proj_set_grid first. */
+int scf_proj_set_solid(scf_proj *h, const double *vof, const double *phi, const double *vofS,
+                       const double *phiS, const double *nxS, const double *nyS,
+                       const double *vofS_u, const double *vofS_v, int icorprob);
+
+/* The geometry the handle holds (from scf_proj_set_geometry or
+ * scf_proj_set_solid) as host arrays in the layouts of scf_proj_set_geometry;
+ * nxS is available after scf_proj_set_solid only.  Any pointer may be NULL. */
+int scf_proj_get_geometry(scf_proj *h, double *vofS, double *nxS, double *nyS, double *WlLh,
+                          double *aE, double *aW, double *aN, double *aS, int32_t *posnu_p,
+                          int32_t *posnu_u, int32_t *posnu_v, int32_t *moex_u,
+                          int32_t *moex_v, double *vofS_u, double *vofS_v);
+
 /* Diagnostics: the assembled symmetric operator in Fortran (nx,ny) layout.
  * cE(i,j) = -A(row(i,j), row(i+1,j)), cN(i,j) = -A(row(i,j), row(i,j+1)),
  * diag(i,j) = A(row(i,j), row(i,j)) (-1 where Posnu = -1); rhs (nx,ny) is

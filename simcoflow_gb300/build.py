@@ -22,7 +22,7 @@ INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["scf_kernels.cu", "scf_mg.cu", "scf_line.cu", "scf_unet.cu", "scf_proj.cu",
-                "scf_noalloc.cu", "scf_mom.cu"]
+                "scf_noalloc.cu", "scf_mom.cu", "scf_geom.cu"]
 
 
 def nvcc() -> str:

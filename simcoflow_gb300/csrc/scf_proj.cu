@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../../include/scf_proj.h"
+#include "scf_geom_gpu.cuh"
 #include "scf_mg.cuh"
 #include "scf_unet.cuh"
 
@@ -97,6 +98,17 @@ struct scf_proj {
   int32_t *st_pp = nullptr, *st_pu = nullptr, *st_pv = nullptr, *st_mu = nullptr,
           *st_mv = nullptr;
   double *st_vsu = nullptr, *st_vsv = nullptr, *st_DpU = nullptr, *st_DpV = nullptr;
+  // GPU-computed geometry (scf_proj_set_solid): outputs, host-mode input
+  // staging, fixed-point and numbering scratch; allocated on first use
+  bool geo_alloc = false;
+  double *g_aE = nullptr, *g_aW = nullptr, *g_aN = nullptr, *g_aS = nullptr;
+  double *g_WlLh = nullptr, *g_vofS = nullptr, *g_nxS = nullptr, *g_nyS = nullptr,
+         *g_vsu = nullptr, *g_vsv = nullptr;
+  int32_t *g_pp = nullptr, *g_pu = nullptr, *g_pv = nullptr, *g_mu = nullptr, *g_mv = nullptr;
+  double* g_in[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  uint8_t *g_st0 = nullptr, *g_st1 = nullptr;
+  int *g_counts = nullptr, *g_flag = nullptr, *g_flag_host = nullptr;
+  int geo_sweeps = 0;
   double *st_us = nullptr, *st_vs = nullptr, *st_Pp = nullptr, *st_p = nullptr, *st_u = nullptr,
          *st_v = nullptr, *st_mres = nullptr;
 
@@ -1075,6 +1087,7 @@ int scf_proj_destroy(scf_proj* h) {
   delete h->net;
   for (void* p : h->allocs) cudaFree(p);
   if (h->sc_host) cudaFreeHost(h->sc_host);
+  if (h->g_flag_host) cudaFreeHost(h->g_flag_host);
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
@@ -1199,6 +1212,89 @@ int scf_proj_update_puv(scf_proj* h, const double* ustar, const double* vstar, d
                         double* Pp, double* p, double* u, double* v, double* mres,
                         scf_stats* st) {
   return solve_common(h, ustar, vstar, vb, Pp, p, u, v, mres, st, true);
+}
+
+int scf_proj_set_solid(scf_proj* h, const double* vof, const double* phi, const double* vofS,
+                       const double* phiS, const double* nxS, const double* nyS,
+                       const double* vofS_u, const double* vofS_v, int icorprob) {
+  if (!h || !vof || !phi || !vofS || !phiS || !nxS || !nyS || !vofS_u || !vofS_v)
+    return SCF_ERR_ARG;
+  if (!h->have_grid) return SCF_ERR_STATE;
+  CK(cudaSetDevice(h->device));
+  const int nx = h->nx, ny = h->ny;
+  const size_t n1 = (size_t)nx * ny, n0 = (size_t)(nx + 2) * (ny + 2);
+  int rc;
+  if (!h->geo_alloc) {
+    struct { void** p; size_t bytes; } a[] = {
+        {(void**)&h->g_aE, n0 * 8}, {(void**)&h->g_aW, n0 * 8}, {(void**)&h->g_aN, n0 * 8},
+        {(void**)&h->g_aS, n0 * 8}, {(void**)&h->g_WlLh, n1 * 8}, {(void**)&h->g_vofS, n1 * 8},
+        {(void**)&h->g_nxS, n1 * 8}, {(void**)&h->g_nyS, n1 * 8}, {(void**)&h->g_vsu, n1 * 8},
+        {(void**)&h->g_vsv, n1 * 8}, {(void**)&h->g_pp, n0 * 4}, {(void**)&h->g_pu, n0 * 4},
+        {(void**)&h->g_pv, n0 * 4}, {(void**)&h->g_mu, n1 * 4}, {(void**)&h->g_mv, n1 * 4},
+        {(void**)&h->g_st0, n0}, {(void**)&h->g_st1, n0},
+        {(void**)&h->g_counts, (size_t)3 * (nx + 1) * 4}, {(void**)&h->g_flag, 4}};
+    for (auto& e : a)
+      if ((rc = dev_alloc(h, e.p, e.bytes))) return rc;
+    if (!h->devptrs)
+      for (int k = 0; k < 6; ++k)
+        if ((rc = dev_alloc(h, (void**)&h->g_in[k], n1 * 8))) return rc;
+    if (cudaMallocHost((void**)&h->g_flag_host, sizeof(int)) != cudaSuccess) return SCF_ERR_NOMEM;
+    h->geo_alloc = true;
+  }
+  if ((rc = put(h, &h->st_vof, vof, n1)) || (rc = put(h, &h->st_phi, phi, n1))) return rc;
+  const double* src[6] = {vofS, phiS, nxS, nyS, vofS_u, vofS_v};
+  const double* dev[6];
+  for (int k = 0; k < 6; ++k) {
+    if (h->devptrs) {
+      dev[k] = src[k];
+    } else {
+      CK(cudaMemcpyAsync(h->g_in[k], src[k], n1 * 8, cudaMemcpyHostToDevice, h->stream));
+      dev[k] = h->g_in[k];
+    }
+  }
+  GeoIn gi{nx, ny, h->fin.dx, h->fin.dy, dev[0], dev[1], dev[2], dev[3], dev[4], dev[5]};
+  GeoOut go{h->fin.dx, h->fin.dy, h->g_aE, h->g_aW, h->g_aN, h->g_aS, h->g_WlLh, h->g_vofS,
+            h->g_nxS, h->g_nyS, h->g_vsu, h->g_vsv, h->g_pp, h->g_pu, h->g_pv, h->g_mu, h->g_mv};
+  const int sweeps = geometry_build(gi, go, h->g_st0, h->g_st1, h->g_counts, h->g_flag,
+                                    h->g_flag_host, icorprob ? 1 : 0, h->stream);
+  if (sweeps < 0) {
+    (void)cudaGetLastError();
+    return SCF_ERR_CUDA;
+  }
+  h->geo_sweeps = sweeps;
+  FortranIn& f = h->fin;
+  f.vof = h->st_vof; f.phi = h->st_phi; f.vofS = h->g_vofS; f.nyS = h->g_nyS;
+  f.WlLh = h->g_WlLh; f.aE = h->g_aE; f.aW = h->g_aW; f.aN = h->g_aN; f.aS = h->g_aS;
+  f.posnu_p = h->g_pp; f.posnu_u = h->g_pu; f.posnu_v = h->g_pv;
+  f.moex_u = h->g_mu; f.moex_v = h->g_mv; f.vofS_u = h->g_vsu; f.vofS_v = h->g_vsv;
+  CK(cudaStreamSynchronize(h->stream));
+  h->have_geom = true;
+  h->assembled = false;
+  return SCF_OK;
+}
+
+int scf_proj_get_geometry(scf_proj* h, double* vofS, double* nxS, double* nyS, double* WlLh,
+                          double* aE, double* aW, double* aN, double* aS, int32_t* posnu_p,
+                          int32_t* posnu_u, int32_t* posnu_v, int32_t* moex_u,
+                          int32_t* moex_v, double* vofS_u, double* vofS_v) {
+  if (!h) return SCF_ERR_ARG;
+  if (!h->have_geom) return SCF_ERR_STATE;
+  CK(cudaSetDevice(h->device));
+  const FortranIn& f = h->fin;
+  const size_t n1 = (size_t)h->nx * h->ny, n0 = (size_t)(h->nx + 2) * (h->ny + 2);
+  const bool own = f.vofS == h->g_vofS && h->geo_alloc;
+  if (nxS && !own) return SCF_ERR_STATE;
+  struct { void* dst; const void* src; size_t bytes; } c[] = {
+      {vofS, f.vofS, n1 * 8}, {nxS, own ? h->g_nxS : nullptr, n1 * 8}, {nyS, f.nyS, n1 * 8},
+      {WlLh, f.WlLh, n1 * 8}, {aE, f.aE, n0 * 8}, {aW, f.aW, n0 * 8}, {aN, f.aN, n0 * 8},
+      {aS, f.aS, n0 * 8}, {posnu_p, f.posnu_p, n0 * 4}, {posnu_u, f.posnu_u, n0 * 4},
+      {posnu_v, f.posnu_v, n0 * 4}, {moex_u, f.moex_u, n1 * 4}, {moex_v, f.moex_v, n1 * 4},
+      {vofS_u, f.vofS_u, n1 * 8}, {vofS_v, f.vofS_v, n1 * 8}};
+  for (auto& e : c)
+    if (e.dst && e.src)
+      CK(cudaMemcpyAsync(e.dst, e.src, e.bytes, cudaMemcpyDefault, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return SCF_OK;
 }
 
 int scf_proj_get_operator(scf_proj* h, double* cE, double* cN, double* diag, double* rhs) {

@@ -42,7 +42,8 @@ EXPORTS = ["scf_opts_default", "scf_proj_create", "scf_proj_destroy", "scf_proj_
            "scf_proj_poisson_solve", "scf_proj_update_puv", "scf_proj_get_operator",
            "scf_proj_vcycle", "scf_proj_time_kernel", "scf_rhs_norm_noalloc", "scf_strerror",
            "scf_proj_set_network", "scf_proj_solve_rhs", "scf_proj_set_opts",
-           "scf_batch_create", "scf_batch_set_io", "scf_batch_run", "scf_batch_destroy"]
+           "scf_batch_create", "scf_batch_set_io", "scf_batch_run", "scf_batch_destroy",
+           "scf_proj_set_solid", "scf_proj_get_geometry"]
 # every symbol declared in include/scf_unet.h
 UNET_EXPORTS = ["scf_unet_num_params", "scf_unet_create", "scf_unet_destroy",
                 "scf_unet_set_stream", "scf_unet_set_params", "scf_unet_get_params",
@@ -114,6 +115,8 @@ def load():
         L.scf_batch_set_io.argtypes = [vp, C.c_int, dp, dp, C.c_double, dp, dp, dp, dp, dp]
         L.scf_batch_run.argtypes = [vp, vp, C.POINTER(Stats)]
         L.scf_batch_destroy.argtypes = [vp]
+        L.scf_proj_set_solid.argtypes = [vp] + [dp] * 8 + [C.c_int]
+        L.scf_proj_get_geometry.argtypes = [vp] + [dp] * 8 + [ip] * 5 + [dp, dp]
         for name in EXPORTS:
             f = getattr(L, name)
             if f.restype is C.c_int or name.startswith("scf_proj"):
@@ -218,6 +221,41 @@ class ProjectionSolver:
             ptrs.append(self._ptr(g[k], shp, dt, k))
         self._keep["geom"] = [g[k] for k in GEOMETRY_ARGS]
         _check(load().scf_proj_set_geometry(self._h, *ptrs), "scf_proj_set_geometry")
+
+    def set_solid(self, vof, phi, vofS, phiS, nxS, nyS, vofS_u, vofS_v, icorprob=True):
+        """The cut-cell geometry computed on the GPU from the cells' solid
+        level-set fields (Grid_Preprocess), in place of set_geometry."""
+        args = (vof, phi, vofS, phiS, nxS, nyS, vofS_u, vofS_v)
+        names = ("vof", "phi", "vofS", "phiS", "nxS", "nyS", "vofS_u", "vofS_v")
+        ptrs = [self._ptr(a, self._n1(), np.float64, n) for a, n in zip(args, names)]
+        self._keep["geom"] = list(args)
+        _check(load().scf_proj_set_solid(self._h, *ptrs, int(bool(icorprob))),
+               "scf_proj_set_solid")
+
+    def get_geometry(self) -> dict:
+        """The geometry the handle holds, as host arrays (set_geometry's
+        keys plus nxS after set_solid)."""
+        n1, n0 = self._n1(), self._n0()
+        out = {k: np.zeros(n1, order="F") for k in ("vofS", "nxS", "nyS", "WlLh", "vofS_u",
+                                                       "vofS_v")}
+        out.update({k: np.zeros(n0, order="F") for k in ("aE", "aW", "aN", "aS")})
+        out.update({k: np.zeros(n0, dtype=np.int32, order="F")
+                    for k in ("posnu_p", "posnu_u", "posnu_v")})
+        out.update({k: np.zeros(n1, dtype=np.int32, order="F") for k in ("moex_u", "moex_v")})
+        order = ("vofS", "nxS", "nyS", "WlLh", "aE", "aW", "aN", "aS", "posnu_p", "posnu_u",
+                 "posnu_v", "moex_u", "moex_v", "vofS_u", "vofS_v")
+        rc = load().scf_proj_get_geometry(self._h, *[out[k].ctypes.data for k in order])
+        if rc == -7:  # nxS only exists for GPU-built geometry
+            del out["nxS"]
+            order = tuple(k for k in order if k != "nxS")
+            rc = load().scf_proj_get_geometry(self._h, *[out[k].ctypes.data if k in out else None
+                                                         for k in ("vofS", "nxS", "nyS", "WlLh",
+                                                                   "aE", "aW", "aN", "aS",
+                                                                   "posnu_p", "posnu_u",
+                                                                   "posnu_v", "moex_u", "moex_v",
+                                                                   "vofS_u", "vofS_v")])
+        _check(rc, "scf_proj_get_geometry")
+        return out
 
     def assemble(self, DpU, DpV, betaP: float, betaM: float, bc=(1, 1, 1, 0)):
         f = lambda a, n: self._ptr(a, self._n0(), np.float64, n)
