@@ -55,6 +55,9 @@ typedef struct scf_geom_out {
     int32_t *posnu_u, *posnu_v;/* UCell%Posnu, VCell%Posnu (0:nx+1,0:ny+1) */
     int32_t *moex_u, *moex_v;  /* UCell%MoExCell, VCell%MoExCell (1:nx,1:ny) */
     double *vofS_u, *vofS_v;   /* UCell%vofS, VCell%vofS (1:nx,1:ny) */
+    /* the solid fields before Grid_Preprocess, as Initial_Clsvof leaves them
+     * (the inputs of scf_proj_set_solid), (1:nx,1:ny) */
+    double *vofS_in, *nxS_in, *nyS_in, *vofS_u_in, *vofS_v_in;
 } scf_geom_out;
 
 /* Face coordinates of one axis: npts = cells+1 values from s0 to s1,

@@ -309,6 +309,11 @@ int scf_geom_build(int nx, int ny, const double* xf, const double* yf, int nsoli
                  vofSU.data(), nullptr, nullptr, nullptr);
   solid_fraction(nx, ny, vx.data(), vy.data(), vdx.data(), vdy.data(), nsolid, solids,
                  vofSV.data(), nullptr, nullptr, nullptr);
+  if (o->vofS_in) std::memcpy(o->vofS_in, vofS.data(), n1 * sizeof(double));
+  if (o->nxS_in) std::memcpy(o->nxS_in, nxS.data(), n1 * sizeof(double));
+  if (o->nyS_in) std::memcpy(o->nyS_in, nyS.data(), n1 * sizeof(double));
+  if (o->vofS_u_in) std::memcpy(o->vofS_u_in, vofSU.data(), n1 * sizeof(double));
+  if (o->vofS_v_in) std::memcpy(o->vofS_v_in, vofSV.data(), n1 * sizeof(double));
 
   // --- liquid fraction and level set of the P cells ---
   std::vector<double> vof(n1), phi(n1);

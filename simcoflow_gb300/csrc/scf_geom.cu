@@ -17,8 +17,8 @@
 // consecutive degenerate cells; the host stops when a sweep changes
 // nothing).  Arithmetic is IEEE FP64 in the reference's operation order, so
 // the results are bit-identical to a CPU restatement.  NumberExternalCell
-// numbers the kept cells with j fastest: per-column counts, a scan over the
-// columns, and per-column prefixes.
+// numbers the kept cells with j fastest: counts per (column, row-group)
+// strip, a scan over the strips, and a walk of each strip from its offset.
 #include <cstdint>
 
 #include "scf_internal.cuh"
@@ -28,6 +28,7 @@ namespace scf {
 namespace {
 
 constexpr double kEps = 1.0e-3, kEpsF = 1.0e-2, kRnd = 1.0e-24;
+constexpr int kRG = 32;  // row groups of the numbering
 
 __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
@@ -37,15 +38,47 @@ __device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, 
 #define G1(a, i, j) (a)[(size_t)((i)-1) + (size_t)((j)-1) * (size_t)nx]
 #define G0(a, i, j) (a)[(size_t)(i) + (size_t)(j) * (size_t)(nx + 2)]
 
+// l >= 1e-14 for a non-NaN double by its bit pattern (integer pipe; an FP64
+// compare issues on GB300's slow FP64 pipe); NaN compares false as in IEEE
+__device__ __forceinline__ bool ge_e14(double l) {
+  const long long b = __double_as_longlong(l);
+  return (b & 0x7fffffffffffffffll) <= 0x7ff0000000000000ll && b >= 0x3d06849b86a12b9bll;
+}
+
+// IEEE comparisons of a double with a constant c > 0 on the integer pipe:
+// for non-NaN x the signed 64-bit bit patterns order like the values when c
+// is positive (negative x, -0 included, have negative patterns); NaN compares
+// false.  gt_neg(x, c) is x > -c.
+__device__ __forceinline__ bool nan_b(long long b) {
+  return (b & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+}
+__device__ __forceinline__ bool gt(double x, double c) {
+  const long long b = __double_as_longlong(x);
+  return !nan_b(b) && b > __double_as_longlong(c);
+}
+__device__ __forceinline__ bool ge(double x, double c) {
+  const long long b = __double_as_longlong(x);
+  return !nan_b(b) && b >= __double_as_longlong(c);
+}
+__device__ __forceinline__ bool lt(double x, double c) {
+  const long long b = __double_as_longlong(x);
+  return !nan_b(b) && b < __double_as_longlong(c);
+}
+__device__ __forceinline__ bool gt_neg(double x, double c) {
+  const long long b = __double_as_longlong(x);
+  return !nan_b(b) && (b >= 0 || (b & 0x7fffffffffffffffll) < __double_as_longlong(c));
+}
+
 // Edge_Geo_Cal: solid fraction of the edge p1-p2 under the linear level set
 __device__ __forceinline__ double edge_solid(double p1x, double p1y, double p2x, double p2y,
                                              double a, double b, double p) {
   const double l1 = add(add(mul(a, p1x), mul(b, p1y)), p);
   const double l2 = add(add(mul(a, p2x), mul(b, p2y)), p);
-  const double e = 1.0e-14;
-  if (l1 >= e && l2 >= e) return 0.0;
-  if (l1 < e && l2 < e) return 1.0;
-  if (l1 >= e && l2 < e) return dvd(fabs(l2), add(fabs(l1), fabs(l2)));
+  const bool g1 = ge_e14(l1), g2 = ge_e14(l2);
+  const bool n1 = !isnan(l1), n2 = !isnan(l2);
+  if (g1 && g2) return 0.0;
+  if (!g1 && n1 && !g2 && n2) return 1.0;
+  if (g1 && !g2 && n2) return dvd(fabs(l2), add(fabs(l1), fabs(l2)));
   return dvd(fabs(l1), add(fabs(l1), fabs(l2)));
 }
 
@@ -59,8 +92,26 @@ __global__ void k_geo_faces(GeoIn in, GeoOut o) {
   for (int iy = blockIdx.y * 8 + threadIdx.y; iy < ny; iy += gridDim.y * 8) {
     const int i = ix + 1, j = iy + 1;
     const double dx = G1(in.dx, i, j), dy = G1(in.dy, i, j);
-    const double x0 = mul(-dx, 0.5), x1 = mul(dx, 0.5), y0 = mul(-dy, 0.5), y1 = mul(dy, 0.5);
     const double a = G1(in.nxS, i, j), b = G1(in.nyS, i, j), p = G1(in.phiS, i, j);
+    G1(o.vofS, i, j) = G1(in.vofS, i, j);
+    G1(o.nxS, i, j) = a;
+    G1(o.nyS, i, j) = b;
+    // Far from the body every corner's level-set value is >= 1e-14 (deep
+    // inside, < 1e-14): every edge gives exactly 0 (1), the wall length 0 and
+    // the open apertures exactly 1 (0).  The test runs in FP32 on values
+    // widened and narrowed by bit manipulation, with a margin far above FP32
+    // rounding, so it only ever takes cells whose FP64 result is certain.
+    const float pf = d2f_rn(p), af = fabsf(d2f_rn(a)), bf = fabsf(d2f_rn(b));
+    const float reach = 0.5f * (af * d2f_rn(dx) + bf * d2f_rn(dy));
+    const float margin = 1.0e-4f * (fabsf(pf) + reach) + 1.0e-12f;
+    const bool out = pf - reach > margin, in_ = pf + reach < -margin;
+    if (out || in_) {
+      const double ap = out ? 1.0 : 0.0;
+      G1(o.WlLh, i, j) = 0.0;
+      G0(o.aW, i, j) = ap; G0(o.aE, i, j) = ap; G0(o.aN, i, j) = ap; G0(o.aS, i, j) = ap;
+      continue;
+    }
+    const double x0 = mul(-dx, 0.5), x1 = mul(dx, 0.5), y0 = mul(-dy, 0.5), y1 = mul(dy, 0.5);
     const double w = edge_solid(x0, y0, x0, y1, a, b, p);
     const double n = edge_solid(x0, y1, x1, y1, a, b, p);
     const double e = edge_solid(x1, y1, x1, y0, a, b, p);
@@ -71,10 +122,15 @@ __global__ void k_geo_faces(GeoIn in, GeoOut o) {
     G0(o.aE, i, j) = sub(1.0, e);
     G0(o.aN, i, j) = sub(1.0, n);
     G0(o.aS, i, j) = sub(1.0, s);
-    G1(o.vofS, i, j) = G1(in.vofS, i, j);
-    G1(o.nxS, i, j) = a;
-    G1(o.nyS, i, j) = b;
   }
+}
+
+// 2 a b / (a + b + 1e-24); two fully open (1, 1) or closed (0, 0) faces give
+// exactly 1 or 0 (2 / (2 + 1e-24) rounds to 1), without the FP64 division
+__device__ __forceinline__ double hmean(double a, double b) {
+  const long long ba = __double_as_longlong(a), bb = __double_as_longlong(b);
+  if (ba == bb && (ba == 0x3ff0000000000000ll || ba == 0)) return a;
+  return dvd(mul(mul(2.0, a), b), add(add(a, b), kRnd));
 }
 
 // harmonic averaging of the interior shared faces (i in 2..nx-1, j in
@@ -86,12 +142,8 @@ __global__ void k_geo_average(int nx, int ny, GeoOut o) {
   if (i > nx - 1) return;
   for (int iy = blockIdx.y * 8 + threadIdx.y; iy + 2 <= ny - 1; iy += gridDim.y * 8) {
     const int j = iy + 2;
-    double av = dvd(mul(mul(2.0, G0(o.aN, i, j)), G0(o.aS, i, j + 1)),
-                    add(add(G0(o.aN, i, j), G0(o.aS, i, j + 1)), kRnd));
-    G0(o.aN, i, j) = av;
-    G0(o.aS, i, j + 1) = av;
-    av = dvd(mul(mul(2.0, G0(o.aE, i, j)), G0(o.aW, i + 1, j)),
-             add(add(G0(o.aE, i, j), G0(o.aW, i + 1, j)), kRnd));
+    G0(o.aN, i, j) = G0(o.aS, i, j + 1) = hmean(G0(o.aN, i, j), G0(o.aS, i, j + 1));
+    const double av = hmean(G0(o.aE, i, j), G0(o.aW, i + 1, j));
     G0(o.aE, i, j) = av;
     G0(o.aW, i + 1, j) = av;
   }
@@ -108,10 +160,10 @@ __global__ void k_geo_status(int nx, int ny, GeoOut o, const uint8_t* st, uint8_
     const int i = ix + 1, j = iy + 1;
     const double vs = G1(o.vofS, i, j);
     uint8_t s = G0(st, i, j);
-    if (!s && vs < 1.0 - kEps) {
+    if (!s && lt(vs, 1.0 - kEps)) {
       const double w = G0(st, i - 1, j) ? 0.0 : G0(o.aW, i, j);
       const double so = G0(st, i, j - 1) ? 0.0 : G0(o.aS, i, j);
-      if (add(w, G0(o.aE, i, j)) < kRnd || add(so, G0(o.aN, i, j)) < kRnd) {
+      if (lt(add(w, G0(o.aE, i, j)), kRnd) || lt(add(so, G0(o.aN, i, j)), kRnd)) {
         s = 1;
         *changed = 1;
       }
@@ -125,7 +177,7 @@ __global__ void k_geo_status_init(int nx, int ny, GeoOut o, uint8_t* st) {
   const int ix = blockIdx.x * 32 + threadIdx.x;
   if (ix >= nx) return;
   for (int iy = blockIdx.y * 8 + threadIdx.y; iy < ny; iy += gridDim.y * 8)
-    G0(st, ix + 1, iy + 1) = G1(o.vofS, ix + 1, iy + 1) > 1.0 - kEps ? 1 : 0;
+    G0(st, ix + 1, iy + 1) = gt(G1(o.vofS, ix + 1, iy + 1), 1.0 - kEps) ? 1 : 0;
 }
 
 // the rule's result: faces of a cell with status zero, and the faces its
@@ -147,7 +199,7 @@ __global__ void k_geo_apply(int nx, int ny, GeoOut o, const uint8_t* st) {
     double vs = G1(o.vofS, i, j);
     if (s) vs = 1.0;
     G1(o.vofS, i, j) = vs;
-    if (fabs(sub(vs, 1.0)) < kRnd) {
+    if (__double_as_longlong(vs) == 0x3ff0000000000000ll) {  // |vs - 1| < 1e-24
       const double dx = G1(o.dx, i, j), dy = G1(o.dy, i, j);
       if (w == 0.0 || e == 0.0) G1(o.WlLh, i, j) = dy;
       if (n == 0.0 || so == 0.0) G1(o.WlLh, i, j) = dx;
@@ -163,17 +215,17 @@ __global__ void k_geo_corner(int nx, int ny, GeoOut o) {
   for (int iy = blockIdx.y * 8 + threadIdx.y; iy + 1 <= ny - 4; iy += gridDim.y * 8) {
     const int i = ix + 1, j = iy + 1;
     const double v0 = G1(o.vofS, i, j);
-    if (!(v0 > -kEps && v0 < kEps)) continue;
+    if (!(gt_neg(v0, kEps) && lt(v0, kEps))) continue;
     const double v1 = G1(o.vofS, i, j + 1), v2 = G1(o.vofS, i, j + 2);
     const double dx = G1(o.dx, i, j);
-    if (v1 > 0.6 - kEps && v1 < 0.6 + kEps && v2 > 0.6 - kEps && v2 < 0.6 + kEps) {
+    if (gt(v1, 0.6 - kEps) && lt(v1, 0.6 + kEps) && gt(v2, 0.6 - kEps) && lt(v2, 0.6 + kEps)) {
       G0(o.aN, i, j) = 0.40;
       G0(o.aS, i, j + 1) = 0.4;
       G1(o.WlLh, i, j) = mul(0.6, dx);
       G1(o.nyS, i, j) = -1.0;
       G1(o.nxS, i, j) = 0.0;
     }
-    if (v1 > 1.0 - kEps && v1 < 1.0 + kEps) {
+    if (gt(v1, 1.0 - kEps) && lt(v1, 1.0 + kEps)) {
       G1(o.WlLh, i, j) = dx;
       G1(o.nyS, i, j) = -1.0;
       G1(o.nxS, i, j) = 0.0;
@@ -191,31 +243,31 @@ __global__ void k_geo_moex(GeoIn in, GeoOut o) {
   for (int iy = blockIdx.y * 8 + threadIdx.y; iy < ny; iy += gridDim.y * 8) {
     const int i = ix + 1, j = iy + 1;
     double vu = G1(in.vofS_u, i, j), vv = G1(in.vofS_v, i, j);
-    if (vu > 1.0 - kEps) vu = 1.0;
-    if (vv > 1.0 - kEps) vv = 1.0;
+    if (gt(vu, 1.0 - kEps)) vu = 1.0;
+    if (gt(vv, 1.0 - kEps)) vv = 1.0;
     G1(o.vofS_u, i, j) = vu;
     G1(o.vofS_v, i, j) = vv;
     int mu = 0, mv = 0;
     const double vs = G1(o.vofS, i, j);
-    if (vu >= kEps && vu < 1.0 - kEps) {
+    if (ge(vu, kEps) && lt(vu, 1.0 - kEps)) {
       if (i < nx) {
-        if (vs >= 1.0 - kEps || G1(o.vofS, i + 1, j) >= 1.0 - kEps || G0(o.aE, i, j) < kEpsF) {
+        if (ge(vs, 1.0 - kEps) || ge(G1(o.vofS, i + 1, j), 1.0 - kEps) || lt(G0(o.aE, i, j), kEpsF)) {
           mu = 1;
           G0(o.aE, i, j) = 0.0;
           G0(o.aW, i + 1, j) = 0.0;
         }
-      } else if (vs >= 1.0 - kEps) {
+      } else if (ge(vs, 1.0 - kEps)) {
         mu = 1;
       }
     }
-    if (vv >= kEps && vv < 1.0 - kEps) {
+    if (ge(vv, kEps) && lt(vv, 1.0 - kEps)) {
       if (j < ny) {
-        if (vs >= 1.0 - kEps || G1(o.vofS, i, j + 1) >= 1.0 - kEps || G0(o.aN, i, j) < kEpsF) {
+        if (ge(vs, 1.0 - kEps) || ge(G1(o.vofS, i, j + 1), 1.0 - kEps) || lt(G0(o.aN, i, j), kEpsF)) {
           mv = 1;
           G0(o.aN, i, j) = 0.0;
           G0(o.aS, i, j + 1) = 0.0;
         }
-      } else if (vs >= 1.0 - kEps) {
+      } else if (ge(vs, 1.0 - kEps)) {
         mv = 1;
       }
     }
@@ -227,67 +279,76 @@ __global__ void k_geo_moex(GeoIn in, GeoOut o) {
 // NumberExternalCell, three families at once.  keep(f,i,j): P: VofS < 1-eps
 // (i<=nx, j<=ny); U: i <= nx-1; V: j <= ny-1.
 __device__ __forceinline__ bool keep(const GeoOut& o, int nx, int ny, int f, int i, int j) {
-  if (f == 0) return G1(o.vofS, i, j) < 1.0 - kEps;
-  if (f == 1) return i <= nx - 1 && G1(o.vofS_u, i, j) < 1.0 - kEps;
-  return j <= ny - 1 && G1(o.vofS_v, i, j) < 1.0 - kEps;
+  if (f == 0) return lt(G1(o.vofS, i, j), 1.0 - kEps);
+  if (f == 1) return i <= nx - 1 && lt(G1(o.vofS_u, i, j), 1.0 - kEps);
+  return j <= ny - 1 && lt(G1(o.vofS_v, i, j), 1.0 - kEps);
 }
 
-// counts[f*(nx+1) + i-1]: kept cells of column i (one warp per column)
+// counts[f*(nx*kRG+1) + (i-1)*kRG + g]: kept cells of column i in row group
+// g (rows g*rl+1 .. (g+1)*rl); one thread per (column, group), consecutive
+// threads on consecutive columns (coalesced loads)
 __global__ void k_geo_count(int nx, int ny, GeoOut o, int* counts) {
   pdl_wait();
-  const int lane = threadIdx.x & 31;
-  const int col = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (col >= 3 * nx) return;
-  const int f = col / nx, i = col % nx + 1;
+  const int i = blockIdx.x * 32 + threadIdx.x + 1;
+  const int g = blockIdx.y * 8 + threadIdx.y, f = blockIdx.z;
+  if (i > nx || g >= kRG) return;
+  const int rl = (ny + kRG - 1) / kRG, j0 = g * rl + 1, j1 = min(ny, j0 + rl - 1);
   int c = 0;
-  for (int j = 1 + lane; j <= ny; j += 32) c += keep(o, nx, ny, f, i, j) ? 1 : 0;
-  for (int s = 16; s > 0; s >>= 1) c += __shfl_down_sync(0xffffffffu, c, s);
-  if (lane == 0) counts[f * (nx + 1) + i - 1] = c;
+  for (int j = j0; j <= j1; ++j) c += keep(o, nx, ny, f, i, j) ? 1 : 0;
+  counts[f * (nx * kRG + 1) + (i - 1) * kRG + g] = c;
 }
 
-// exclusive scan of each family's column counts (one block of 1024
-// threads per family, serial chunks per thread, then a block scan)
+// exclusive scan of each family's counts in (column, group) order: one block
+// of 1024 threads per family walks the counts in tiles of 1024 (coalesced),
+// scanning each tile by warp shuffles and carrying the running total
 __global__ void k_geo_scan(int nx, int* counts) {
   pdl_wait();
-  __shared__ int part[1024];
-  int* c = counts + blockIdx.x * (nx + 1);
-  const int t = threadIdx.x, nt = blockDim.x;
-  const int per = (nx + nt - 1) / nt, a = t * per, b = a + per < nx ? a + per : nx;
-  int sum = 0;
-  for (int k = a; k < b; ++k) sum += c[k];
-  part[t] = sum;
+  __shared__ int wsum[32];
+  __shared__ int carry;
+  const int n = nx * kRG;
+  int* c = counts + blockIdx.x * (n + 1);
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  if (t == 0) carry = 0;
   __syncthreads();
-  for (int s = 1; s < nt; s <<= 1) {  // inclusive Hillis-Steele scan of the chunk sums
-    const int v = t >= s ? part[t - s] : 0;
+  for (int base = 0; base < n; base += 1024) {
+    const int k = base + t;
+    const int v = k < n ? c[k] : 0;
+    int x = v;  // inclusive warp scan
+    for (int s = 1; s < 32; s <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, s);
+      if (lane >= s) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
     __syncthreads();
-    part[t] += v;
+    if (w == 0) {  // scan of the 32 warp sums
+      int z = wsum[lane];
+      for (int s = 1; s < 32; s <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, z, s);
+        if (lane >= s) z += y;
+      }
+      wsum[lane] = z;
+    }
+    __syncthreads();
+    const int before = carry + (w > 0 ? wsum[w - 1] : 0) + x - v;
+    if (k < n) c[k] = before;
+    __syncthreads();
+    if (t == 1023) carry = before + v;
     __syncthreads();
   }
-  int run = t > 0 ? part[t - 1] : 0;
-  for (int k = a; k < b; ++k) {
-    const int v = c[k];
-    c[k] = run;
-    run += v;
-  }
-  if (t == nt - 1) c[nx] = part[nt - 1];  // total
+  if (t == 0) c[n] = carry;  // total
 }
 
-// per-column numbering with j fastest (one warp per column)
+// numbering with j fastest: each (column, group) thread walks its rows from
+// its offset
 __global__ void k_geo_number(int nx, int ny, GeoOut o, const int* counts) {
   pdl_wait();
-  const int lane = threadIdx.x & 31;
-  const int col = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (col >= 3 * nx) return;
-  const int f = col / nx, i = col % nx + 1;
+  const int i = blockIdx.x * 32 + threadIdx.x + 1;
+  const int g = blockIdx.y * 8 + threadIdx.y, f = blockIdx.z;
+  if (i > nx || g >= kRG) return;
   int32_t* pn = f == 0 ? o.posnu_p : f == 1 ? o.posnu_u : o.posnu_v;
-  int base = counts[f * (nx + 1) + i - 1];
-  for (int j0 = 1; j0 <= ny; j0 += 32) {
-    const int j = j0 + lane;
-    const bool k = j <= ny && keep(o, nx, ny, f, i, j);
-    const unsigned m = __ballot_sync(0xffffffffu, k);
-    if (j <= ny) G0(pn, i, j) = k ? base + __popc(m & ((1u << lane) - 1u)) : -1;
-    base += __popc(m);
-  }
+  const int rl = (ny + kRG - 1) / kRG, j0 = g * rl + 1, j1 = min(ny, j0 + rl - 1);
+  int k = counts[f * (nx * kRG + 1) + (i - 1) * kRG + g];
+  for (int j = j0; j <= j1; ++j) G0(pn, i, j) = keep(o, nx, ny, f, i, j) ? k++ : -1;
 }
 
 #undef G1
@@ -301,10 +362,13 @@ dim3 cell_grid(int nx, int ny) {
 }  // namespace
 
 // The whole pipeline on stream s.  st0/st1: status buffers ((nx+2)(ny+2)
-// bytes), counts: 3*(nx+1) ints, flag: one device int, flag_host: pinned.
+// bytes), counts: geometry_count_ints(nx) ints, flag: one device int,
+// flag_host: pinned.
 // Returns the number of fixed-point sweeps, or -1 if they did not settle
 // within nx+ny+2 sweeps (not possible for a chain of finite length) or a
 // CUDA call failed.
+size_t geometry_count_ints(int nx) { return 3 * ((size_t)nx * kRG + 1); }
+
 int geometry_build(const GeoIn& in, const GeoOut& o, uint8_t* st0, uint8_t* st1, int* counts,
                    int* flag, int* flag_host, int icorprob, cudaStream_t s) {
   const int nx = in.nx, ny = in.ny;
@@ -338,10 +402,10 @@ int geometry_build(const GeoIn& in, const GeoOut& o, uint8_t* st0, uint8_t* st1,
   launch_k(k_geo_apply, g, b, 0, s, nx, ny, o, (const uint8_t*)cur);
   if (icorprob && ny >= 5) launch_k(k_geo_corner, g, b, 0, s, nx, ny, o);
   launch_k(k_geo_moex, g, b, 0, s, in, o);
-  const int warps = 3 * nx, blocks = (warps * 32 + 255) / 256;
-  launch_k(k_geo_count, dim3(blocks), dim3(256), 0, s, nx, ny, o, counts);
+  const dim3 ng((nx + 31) / 32, kRG / 8, 3);
+  launch_k(k_geo_count, ng, b, 0, s, nx, ny, o, counts);
   launch_k(k_geo_scan, dim3(3), dim3(1024), 0, s, nx, counts);
-  launch_k(k_geo_number, dim3(blocks), dim3(256), 0, s, nx, ny, o, (const int*)counts);
+  launch_k(k_geo_number, ng, b, 0, s, nx, ny, o, (const int*)counts);
   if (cudaGetLastError() != cudaSuccess) return -1;
   return sweeps;
 }

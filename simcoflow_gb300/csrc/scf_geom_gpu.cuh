@@ -22,6 +22,7 @@ struct GeoOut {
   int32_t *moex_u, *moex_v;              // (1:nx,1:ny)
 };
 
+size_t geometry_count_ints(int nx);  // size of the numbering scratch
 int geometry_build(const GeoIn& in, const GeoOut& o, uint8_t* st0, uint8_t* st1, int* counts,
                    int* flag, int* flag_host, int icorprob, cudaStream_t s);
 

@@ -1232,7 +1232,7 @@ int scf_proj_set_solid(scf_proj* h, const double* vof, const double* phi, const 
         {(void**)&h->g_vsv, n1 * 8}, {(void**)&h->g_pp, n0 * 4}, {(void**)&h->g_pu, n0 * 4},
         {(void**)&h->g_pv, n0 * 4}, {(void**)&h->g_mu, n1 * 4}, {(void**)&h->g_mv, n1 * 4},
         {(void**)&h->g_st0, n0}, {(void**)&h->g_st1, n0},
-        {(void**)&h->g_counts, (size_t)3 * (nx + 1) * 4}, {(void**)&h->g_flag, 4}};
+        {(void**)&h->g_counts, geometry_count_ints(nx) * 4}, {(void**)&h->g_flag, 4}};
     for (auto& e : a)
       if ((rc = dev_alloc(h, e.p, e.bytes))) return rc;
     if (!h->devptrs)

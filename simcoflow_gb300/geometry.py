@@ -39,7 +39,8 @@ class _Out(C.Structure):
     _fields_ = [(n, _P) for n in ("x", "y", "dx", "dy", "dxU", "dyV", "vof", "phi", "vofS",
                                   "phiS", "nxS", "nyS", "WlLh", "aE", "aW", "aN", "aS")] + \
                [(n, _I) for n in ("posnu_p", "posnu_u", "posnu_v", "moex_u", "moex_v")] + \
-               [(n, _P) for n in ("vofS_u", "vofS_v")]
+               [(n, _P) for n in ("vofS_u", "vofS_v", "vofS_in", "nxS_in", "nyS_in",
+                                  "vofS_u_in", "vofS_v_in")]
 
 
 def _load():
@@ -106,7 +107,8 @@ def build(xf: np.ndarray, yf: np.ndarray, solids: list[Solid], surface: Surface,
     f1 = lambda dt=np.float64: np.zeros((nx, ny), dtype=dt, order="F")
     f0 = lambda dt=np.float64: np.zeros((nx + 2, ny + 2), dtype=dt, order="F")
     g = {k: f1() for k in ("x", "y", "dx", "dy", "dxU", "dyV", "vof", "phi", "vofS", "phiS",
-                           "nxS", "nyS", "WlLh", "vofS_u", "vofS_v")}
+                           "nxS", "nyS", "WlLh", "vofS_u", "vofS_v", "vofS_in", "nxS_in",
+                           "nyS_in", "vofS_u_in", "vofS_v_in")}
     g.update({k: f0() for k in ("aE", "aW", "aN", "aS")})
     g.update({k: f0(np.int32) for k in ("posnu_p", "posnu_u", "posnu_v")})
     g.update({k: f1(np.int32) for k in ("moex_u", "moex_v")})

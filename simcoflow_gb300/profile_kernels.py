@@ -16,6 +16,8 @@ profiler can restrict itself to that range (ncu --nvtx --nvtx-include
             the workload's operator and right-hand side (shipped weights)
   momentum  --reps pairs of momentum-predictor solves (u then v) on the
             workload's cells (seeded face fluxes), device-resident
+  geometry  --reps GPU builds of the cut-cell geometry (scf_proj_set_solid)
+            from the workload's solid level-set fields, device-resident
 
     python -m simcoflow_gb300.profile_kernels --config c2 --kernel sweep --precision mixed
     python -m simcoflow_gb300.profile_kernels --config c3 --n 2048 --kernel projection
@@ -38,7 +40,7 @@ KERNELS = {"sweep": (0, {"fp64": 48, "mixed": 20}), "pupdate_spmv": (1, {"fp64":
            "prolong": (4, {"fp64": 50, "mixed": 21}), "assemble": (5, {"fp64": 200, "mixed": 200}),
            "vcycle": (6, {"fp64": 0, "mixed": 0}), "setup": (7, {"fp64": 0, "mixed": 0}),
            "projection": (None, {"fp64": 0, "mixed": 0}), "unet": (None, {"fp64": 0, "mixed": 0}),
-           "momentum": (None, {"fp64": 0, "mixed": 0})}
+           "momentum": (None, {"fp64": 0, "mixed": 0}), "geometry": (None, {"fp64": 0, "mixed": 0})}
 
 
 def main():
@@ -54,6 +56,23 @@ def main():
     c = synth.make_case(args.config, **({"n": args.n} if args.n else {}))
     t = {k: torch.from_numpy(np.ascontiguousarray(v.ravel(order="F"))).to(dev)
          for k, v in c.arrays.items() if isinstance(v, np.ndarray)}
+    if args.kernel == "geometry":
+        keys = ("vof", "phi", "vofS_in", "phiS", "nxS_in", "nyS_in", "vofS_u_in", "vofS_v_in")
+        gs = P.ProjectionSolver(c.nx, c.ny, device_ptrs=True)
+        gs.set_grid(t["dx"], t["dy"], t["dxU"], t["dyV"])
+        gs.set_solid(*[t[k] for k in keys])  # warm-up
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("kernels")
+        t0 = time.perf_counter()
+        for _ in range(args.reps):
+            gs.set_solid(*[t[k] for k in keys])
+        torch.cuda.synchronize()
+        dt_ms = (time.perf_counter() - t0) / args.reps * 1e3
+        torch.cuda.nvtx.range_pop()
+        gs.close()
+        print(json.dumps({"config": args.config, "kernel": "geometry", "nx": c.nx, "ny": c.ny,
+                          "ms_set_solid": dt_ms}))
+        return
     if args.kernel == "momentum":
         from . import momentum as M
         T = lambda x: torch.from_numpy(np.ascontiguousarray(x.ravel(order="F"))).to(dev)

@@ -114,7 +114,8 @@ def build_case(name, xf, yf, solids, surface, modes_u, modes_v, dt, ratio, vorte
     arrays = {k: g[k] for k in ("dx", "dy", "dxU", "dyV", "vof", "phi", "vofS", "nyS", "WlLh",
                                 "aE", "aW", "aN", "aS", "posnu_p", "posnu_u", "moex_u",
                                 "vofS_u", "posnu_v", "moex_v", "vofS_v", "x", "y", "phiS",
-                                "nxS")}
+                                "nxS", "vofS_in", "nxS_in", "nyS_in", "vofS_u_in",
+                                "vofS_v_in")}
     arrays["DpU"] = np.full((nx + 2, ny + 2), dt, order="F")
     arrays["DpV"] = np.full((nx + 2, ny + 2), dt, order="F")
     arrays["ustar"], arrays["vstar"] = us, vs
