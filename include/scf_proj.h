@@ -265,6 +265,14 @@ int scf_proj_vcycle(scf_proj *h, const double *b, double *x);
 #define SCF_K_SETUP 7          /* assembly + multigrid hierarchy setup (device work only) */
 int scf_proj_time_kernel(scf_proj *h, int kernel, int reps, double *ms_per_launch);
 
+/* Diagnostics: q[k] = a[k] / b[k] for k < n by the FP64 division that the
+ * assembly, the correction, the momentum and the geometry kernels use
+ * (integer-pipe arithmetic, correctly rounded to nearest even like IEEE
+ * division).  Host arrays; runs on the given device.  No counterpart in the
+ * reference; it exists so that tests can compare the division bit for bit
+ * with IEEE division on many operands. */
+int scf_diag_divide(const double *a, const double *b, double *q, int64_t n, int device);
+
 /* Allocation-free right-hand side.  Computes the right-hand side of the
  * pressure equation exactly as SetPoissonVectors does
  * (src/ProjectionP_Mod.f90:313-317) into rhs (nx,ny) (0 where Posnu = -1)

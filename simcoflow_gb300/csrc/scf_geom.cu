@@ -33,7 +33,8 @@ constexpr int kRG = 32;  // row groups of the numbering
 __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
+// IEEE division, correctly rounded, on the integer pipe
+__device__ __forceinline__ double dvd(double a, double b) { return div_rn(a, b); }
 
 #define G1(a, i, j) (a)[(size_t)((i)-1) + (size_t)((j)-1) * (size_t)nx]
 #define G0(a, i, j) (a)[(size_t)(i) + (size_t)(j) * (size_t)(nx + 2)]

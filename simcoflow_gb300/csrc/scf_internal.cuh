@@ -132,6 +132,53 @@ __device__ __forceinline__ double pos_part(double v) {
   return __double2hiint(v) < 0 ? 0.0 : v;
 }
 
+// Correctly rounded FP64 quotient a / b (IEEE round to nearest even), on the
+// integer pipe: an FP64 division costs about ten instructions on GB300's slow
+// FP64 pipe, this one a few dozen integer instructions and one FP32
+// reciprocal approximation.  Method: Newton-Raphson iteration
+// y <- y (2 - m y) for the reciprocal of b's significand m in [1, 2) in
+// 64-bit fixed point (2^63 = 1), seeded by the FP32 reciprocal approximation
+// of m truncated to 24 bits (relative error near 2^-22; the steps square it,
+// and every truncation keeps y at or below 1/m); the 53-bit quotient of the
+// significands from one high product; then the exact remainder corrects the
+// last digit and gives the round-to-nearest-even bit, the closing step of long
+// division (Knuth, TAOCP vol. 2, 4.3.1).  An exact midpoint cannot occur for
+// a quotient of two 53-bit significands.  Zero, subnormal, infinite or NaN
+// operands and results outside the normal range take the IEEE division.
+__device__ __forceinline__ double div_rn(double a, double b) {
+  using u64 = unsigned long long;
+  const u64 ua = (u64)__double_as_longlong(a), ub = (u64)__double_as_longlong(b);
+  const int ea = (int)((ua >> 52) & 0x7ff), eb = (int)((ub >> 52) & 0x7ff);
+  const u64 ma = (ua & 0xfffffffffffffull) | (1ull << 52);
+  const u64 mb = (ub & 0xfffffffffffffull) | (1ull << 52);
+  const bool ge = ma >= mb;                 // quotient of the significands in [1, 2)
+  const int E = ea - eb + 1022 + (int)ge;   // biased exponent of the result
+  if ((unsigned)(ea - 1) >= 2046u || (unsigned)(eb - 1) >= 2046u || (unsigned)(E - 1) >= 2045u)
+    return __ddiv_rn(a, b);
+  float y0;
+  asm("rcp.approx.ftz.f32 %0, %1;"
+      : "=f"(y0)
+      : "f"(__uint_as_float(0x3f800000u | (unsigned)((ub >> 29) & 0x7fffffu))));
+  const unsigned yb = __float_as_uint(y0);  // in [0.49, 1]: exponent field 125 .. 127
+  u64 Y = (u64)(0x800000u | (yb & 0x7fffffu)) << (39 + (int)(yb >> 23) - 126);
+  const u64 M = mb << 11;
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    const u64 P = __umul64hi(M, Y);       // m y 2^62
+    Y = __umul64hi(Y, (1ull << 63) - P) << 2;  // y (2 - m y) 2^63
+  }
+  u64 Q = __umul64hi(ma << 11, Y) >> (ge ? 10 : 9);  // the true digit string or one below
+  u64 R = (ma << (ge ? 52 : 53)) - Q * mb;           // exact remainder, modulo 2^64
+  if ((long long)R < 0) { Q -= 1; R += mb; }
+  if (R >= mb) { Q += 1; R -= mb; }
+  if (R >= mb) { Q += 1; R -= mb; }
+  const u64 R2 = R << 1;
+  Q += (u64)((R2 > mb) | ((R2 == mb) & (Q & 1ull)));
+  // Q in [2^52, 2^53]: adding it to the exponent field carries 2^53 into it
+  const u64 bits = ((ua ^ ub) & (1ull << 63)) | (((u64)(E - 1) << 52) + Q);
+  return __longlong_as_double((long long)bits);
+}
+
 // PDL is on unless SCF_NO_PDL is set in the environment.
 bool pdl_enabled();
 
@@ -189,6 +236,7 @@ inline dim3 grid_for(int nx, int ny, int cells_per_thread_x = 2) {
 
 // ---- kernel launchers (scf_kernels.cu) ----
 void launch_assemble(const FortranIn& in, LevelView L0, Scalars* sc, cudaStream_t s);
+void launch_divide(const double* a, const double* b, double* q, long long n, cudaStream_t s);
 void launch_excess(LevelView L, double* di, cudaStream_t s);
 void launch_coarsen(LevelView F, LevelView C, double* di, cudaStream_t s);
 void launch_coarse_setup(LevelView C, double* Ainv, int* cmap, int* nc, cudaStream_t s);

@@ -14,7 +14,8 @@ namespace {
 __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
+// IEEE division, correctly rounded, on the integer pipe
+__device__ __forceinline__ double dvd(double a, double b) { return div_rn(a, b); }
 
 __device__ __forceinline__ int tid2() { return threadIdx.y * blockDim.x + threadIdx.x; }
 __device__ __forceinline__ bool block00() {
@@ -597,15 +598,11 @@ __global__ void k_update_xr(LevelView L, double* __restrict__ x, const double* _
 
 // Pressure-gradient correction of one face between cells s (self) and n
 // (east or north neighbour): returns false when the reference leaves the
-// face alone.  G = (Pp_n - Pp_s)*BetaM*BetaP/BetaW*Dp/dist.
-// Faces inside one phase divide by BetaM or BetaP; they multiply by the
-// reciprocal (rM = 1/BetaM, rP = 1/BetaP, each a correctly rounded FP64
-// division made once per thread) instead, which moves G by at most an ulp
-// of an FP64 division on the slow FP64 pipe (the velocities are compared
-// with the oracle to a tolerance, the operator bit for bit).
+// face alone.  G = (Pp_n - Pp_s)*BetaM*BetaP/BetaW*Dp/dist, every operation
+// rounded as in the reference.
 __device__ __forceinline__ bool face_grad(int cs, int cn, double phis, double phin, double pps,
-                                          double ppn, double bP, double bM, double rP, double rM,
-                                          double Dp, double dist, double* G) {
+                                          double ppn, double bP, double bM, double Dp,
+                                          double dist, double* G) {
   const double tol = 1.0e-24;
   const double t = mul(mul(sub(ppn, pps), bM), bP);
   double q;
@@ -614,7 +611,7 @@ __device__ __forceinline__ bool face_grad(int cs, int cn, double phis, double ph
       double l = dvd(fabs(phis), add(add(fabs(phis), fabs(phin)), tol));
       q = dvd(t, add(mul(l, bM), mul(sub(1.0, l), bP)));
     } else if (cn == 1) {
-      q = mul(t, rM);
+      q = dvd(t, bM);
     } else {
       return false;
     }
@@ -623,7 +620,7 @@ __device__ __forceinline__ bool face_grad(int cs, int cn, double phis, double ph
       double l = dvd(fabs(phis), add(add(fabs(phis), fabs(phin)), tol));
       q = dvd(t, add(mul(l, bP), mul(sub(1.0, l), bM)));
     } else if (cn == 2) {
-      q = mul(t, rP);
+      q = dvd(t, bP);
     } else {
       return false;
     }
@@ -643,7 +640,6 @@ __global__ void k_final_solution(FortranIn in, LevelView L, const double* __rest
   const int ix = blockIdx.x * kBX + threadIdx.x;
   const int P = L.pitch;
   double acc = 0.0;
-  const double rP = dvd(1.0, in.betaP), rM = dvd(1.0, in.betaM);
   if (ix < nx) {
     for (int iy = blockIdx.y * kBY + threadIdx.y; iy < ny; iy += gridDim.y * kBY) {
       const int i = ix + 1, j = iy + 1;
@@ -677,7 +673,7 @@ __global__ void k_final_solution(FortranIn in, LevelView L, const double* __rest
         const double ppn = in.posnu_p[fo0(nx, i + 1, j)] != -1 ? x[kl + 1] : 0.0;
         double G;
         if (face_grad(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], ppc,
-                      ppn, bP, bM, rP, rM, in.DpU[k0], in.dxU[k1], &G))
+                      ppn, bP, bM, in.DpU[k0], in.dxU[k1], &G))
           u[k0] = sub(us[k0], G);
       }
       if (j <= ny - 1 && in.posnu_v[k0] != -1 && in.moex_v[k1] != 1) {
@@ -685,7 +681,7 @@ __global__ void k_final_solution(FortranIn in, LevelView L, const double* __rest
         const double ppn = in.posnu_p[fo0(nx, i, j + 1)] != -1 ? x[kl + P] : 0.0;
         double G;
         if (face_grad(cs, cell_class(in.vof[kn], in.phi[kn], in.vofS[kn]), phis, in.phi[kn], ppc,
-                      ppn, bP, bM, rP, rM, in.DpV[k0], in.dyV[k1], &G))
+                      ppn, bP, bM, in.DpV[k0], in.dyV[k1], &G))
           v[k0] = sub(vs[k0], G);
       }
       if (act) p[k0] = ppc;
@@ -741,6 +737,13 @@ __global__ void k_final_zero(FortranIn in, double* p, double* u, double* v) {
   }
 }
 
+// the assembly's division on arrays (diagnostics)
+__global__ void k_divide(const double* a, const double* b, double* q, long long n) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+       k += (long long)gridDim.x * blockDim.x)
+    q[k] = dvd(a[k], b[k]);
+}
+
 __global__ void k_to_fortran(LevelView L, const double* src, double* dst) {
   pdl_wait();
   const int ix = blockIdx.x * kBX + threadIdx.x;
@@ -779,6 +782,9 @@ static const dim3 kBlock(kBX, kBY);
 
 void launch_assemble(const FortranIn& in, LevelView L0, Scalars* sc, cudaStream_t s) {
   launch_k(k_assemble, grid_for(in.nx, in.ny, 1), kBlock, 0, s, in, L0, sc);
+}
+void launch_divide(const double* a, const double* b, double* q, long long n, cudaStream_t s) {
+  launch_k(k_divide, dim3(152 * 8), dim3(256), 0, s, a, b, q, n);
 }
 void launch_excess(LevelView L, double* di, cudaStream_t s) {
   launch_k(k_excess, grid_for(L.nx, L.ny, 1), kBlock, 0, s, L, di);

@@ -28,7 +28,8 @@ namespace {
 __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
+// IEEE division, correctly rounded, on the integer pipe
+__device__ __forceinline__ double dvd(double a, double b) { return div_rn(a, b); }
 
 constexpr int TX = 64, TY = 32, NTM = 256;  // Krylov tiles: 64 x 32 cells, 256 threads
 

@@ -887,6 +887,35 @@ void scf_opts_default(scf_opts* o) {
   o->smoother = SCF_SMOOTH_AUTO;
 }
 
+int scf_diag_divide(const double* a, const double* b, double* q, int64_t n, int device) {
+  if (n < 0 || (n > 0 && (!a || !b || !q))) return SCF_ERR_ARG;
+  if (n == 0) return SCF_OK;
+  CK(cudaSetDevice(device));
+  double* d = nullptr;
+  const size_t bytes = (size_t)n * 8;
+  CK(cudaMalloc(&d, 3 * bytes));
+  int rc = SCF_OK;
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaFree(d);
+    return SCF_ERR_CUDA;
+  }
+  if (cudaMemcpyAsync(d, a, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(d + n, b, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    rc = SCF_ERR_CUDA;
+  if (rc == SCF_OK) {
+    launch_divide(d, d + n, d + 2 * n, (long long)n, s);
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(q, d + 2 * n, bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      rc = SCF_ERR_CUDA;
+  }
+  cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  cudaFree(d);
+  return rc;
+}
+
 const char* scf_strerror(int code) {
   switch (code) {
     case SCF_OK: return "ok";

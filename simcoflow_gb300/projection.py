@@ -43,7 +43,7 @@ EXPORTS = ["scf_opts_default", "scf_proj_create", "scf_proj_destroy", "scf_proj_
            "scf_proj_vcycle", "scf_proj_time_kernel", "scf_rhs_norm_noalloc", "scf_strerror",
            "scf_proj_set_network", "scf_proj_solve_rhs", "scf_proj_set_opts",
            "scf_batch_create", "scf_batch_set_io", "scf_batch_run", "scf_batch_destroy",
-           "scf_proj_set_solid", "scf_proj_get_geometry"]
+           "scf_proj_set_solid", "scf_proj_get_geometry", "scf_diag_divide"]
 # every symbol declared in include/scf_unet.h
 UNET_EXPORTS = ["scf_unet_num_params", "scf_unet_create", "scf_unet_destroy",
                 "scf_unet_set_stream", "scf_unet_set_params", "scf_unet_get_params",
@@ -117,6 +117,8 @@ def load():
         L.scf_batch_destroy.argtypes = [vp]
         L.scf_proj_set_solid.argtypes = [vp] + [dp] * 8 + [C.c_int]
         L.scf_proj_get_geometry.argtypes = [vp] + [dp] * 8 + [ip] * 5 + [dp, dp]
+        L.scf_diag_divide.argtypes = [dp, dp, dp, C.c_int64, C.c_int]
+        L.scf_diag_divide.restype = C.c_int
         for name in EXPORTS:
             f = getattr(L, name)
             if f.restype is C.c_int or name.startswith("scf_proj"):
@@ -352,6 +354,19 @@ class ProjectionSolver:
         self.set_grid(a["dx"], a["dy"], a["dxU"], a["dyV"])
         self.set_geometry(**{k: a[k] for k in GEOMETRY_ARGS})
         self.assemble(a["DpU"], a["DpV"], case.betaP, case.betaM, case.bc)
+
+
+def divide(a, b, device: int = 0):
+    """a / b elementwise by the library's FP64 division (the one its
+    bit-exact kernels use), on the GPU; numpy float64 arrays in and out."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    if a.shape != b.shape:
+        raise ValueError("a and b need the same shape")
+    q = np.empty_like(a)
+    _check(load().scf_diag_divide(a.ctypes.data, b.ctypes.data, q.ctypes.data, a.size, device),
+           "scf_diag_divide")
+    return q
 
 
 def project_case(case, **opts):

@@ -1,0 +1,92 @@
+"""The library's FP64 division (integer-pipe Newton-Raphson reciprocal with
+a remainder-corrected last digit, used by the bit-exact assembly, correction,
+momentum and geometry kernels) against IEEE division, bit for bit, through
+the C-ABI diagnostic scf_diag_divide.
+
+numpy's float64 division is IEEE-754 division rounded to nearest even, the
+same operation the reference's Fortran `/` performs."""
+import numpy as np
+import pytest
+
+from simcoflow_gb300 import projection as P
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(x):
+    return np.asarray(x, dtype=np.float64).view(np.uint64)
+
+
+def check(a, b):
+    q = P.divide(a, b)
+    with np.errstate(all="ignore"):
+        e = a / b
+    same = (bits(q) == bits(e)) | (np.isnan(q) & np.isnan(e))
+    if not same.all():
+        k = np.flatnonzero(~same)[:5]
+        raise AssertionError(f"{(~same).sum()} mismatches, e.g. "
+                             + ", ".join(f"{a[i].hex()}/{b[i].hex()}: {q[i].hex()} vs {e[i].hex()}"
+                                         for i in k))
+
+
+def test_random_bit_patterns():
+    """Every exponent and mantissa pattern, NaN/Inf/zero/subnormal included."""
+    rng = np.random.default_rng(11)
+    n = 4_000_000
+    a = rng.integers(0, 2**64, n, dtype=np.uint64).view(np.float64)
+    b = rng.integers(0, 2**64, n, dtype=np.uint64).view(np.float64)
+    check(a, b)
+
+
+def test_moderate_exponents():
+    """The normal-range fast path: exponents within 2^+-60 of each other."""
+    rng = np.random.default_rng(12)
+    n = 4_000_000
+    a = rng.uniform(1.0, 2.0, n) * np.exp2(rng.integers(-60, 61, n)) * rng.choice([-1, 1], n)
+    b = rng.uniform(1.0, 2.0, n) * np.exp2(rng.integers(-60, 61, n)) * rng.choice([-1, 1], n)
+    check(a, b)
+
+
+def test_sparse_and_dense_mantissas():
+    """Significands with few bits set or cleared (powers of two, 1 - ulp,
+    all ones): the digit-correction and carry edges."""
+    rng = np.random.default_rng(13)
+    n = 1_000_000
+    def pattern():
+        m = np.zeros(n, dtype=np.uint64)
+        for _ in range(3):
+            on = rng.random(n) < 0.6
+            m |= np.where(on, np.uint64(1) << rng.integers(0, 52, n).astype(np.uint64),
+                          np.uint64(0))
+        flip = rng.random(n) < 0.5
+        m = np.where(flip, m ^ np.uint64(0xFFFFFFFFFFFFF), m)
+        e = rng.integers(1013, 1033, n).astype(np.uint64)
+        return ((e << np.uint64(52)) | m).view(np.float64)
+    check(pattern(), pattern())
+
+
+def test_near_exact_quotients():
+    """a within a few ulps of b*q for short q: quotients on or next to
+    representable values, where the remainder decides the last bit."""
+    rng = np.random.default_rng(14)
+    n = 1_000_000
+    b = rng.uniform(1.0, 2.0, n) * np.exp2(rng.integers(-20, 21, n))
+    q = rng.integers(1, 2**20, n) * np.exp2(rng.integers(-30, 10, n))
+    a = (b * q).view(np.uint64) + rng.integers(-2, 3, n).astype(np.int64).view(np.uint64)
+    check(a.view(np.float64), b)
+
+
+def test_range_edges():
+    """Results next to overflow and underflow, and the special operands."""
+    big, tiny = np.finfo(np.float64).max, np.finfo(np.float64).tiny
+    vals = np.array([0.0, -0.0, 1.0, -1.0, np.inf, -np.inf, np.nan, big, -big, tiny, -tiny,
+                     tiny / 3, 5e-324, 2.0, 0.5, 3.0, 1.0 + 2**-52, 2.0 - 2**-52,
+                     1.7976931348623157e308 / 2, 2.2250738585072014e-308 * 2])
+    a, b = np.meshgrid(vals, vals)
+    check(a.ravel(), b.ravel())
+    rng = np.random.default_rng(15)
+    n = 200_000
+    x = rng.uniform(1.0, 2.0, n)
+    check(x * 2.0**1000, rng.uniform(0.1, 1.0, n) * 2.0**-23)   # overflow side
+    check(x * 2.0**-1000, rng.uniform(1.0, 9.0, n) * 2.0**22)   # gradual underflow side
+    check(x * 2.0**-1021, rng.uniform(0.5, 2.0, n))             # around the smallest normal
