@@ -159,8 +159,9 @@ WORKLOADS = {
 KERNEL_BYTES = {
     "fp64": {"sweep": 48, "pupdate_spmv": 56, "update_xr": 48, "resid_restrict": 58,
              "prolong": 50},
-    # fine level of the mixed path: x, b (FP32 copy of r), di FP32; BF16 couplings
-    "mixed": {"sweep": 20, "pupdate_spmv": 52, "update_xr": 56, "resid_restrict": 25,
+    # fine level of the mixed path: x, b (FP32 copy of r), di FP32; BF16 couplings;
+    # FP32 search direction p of the outer PCG
+    "mixed": {"sweep": 20, "pupdate_spmv": 44, "update_xr": 52, "resid_restrict": 25,
               "prolong": 21},
 }
 KERNEL_IDS = (("sweep", 0), ("pupdate_spmv", 1), ("update_xr", 2), ("resid_restrict", 3),

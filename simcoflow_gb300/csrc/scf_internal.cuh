@@ -97,6 +97,13 @@ __device__ __forceinline__ void pdl_wait() {
 // IEEE-754 binary32/binary64 encodings; the rare operands outside the normal
 // range (zero excepted) take the hardware conversion.
 
+// The rare operands take the hardware conversion (or division) through an
+// out-of-line call: the compiler then branches around it instead of
+// predicating an FP64-pipe instruction into every use.
+static __device__ __noinline__ double f2d_rare(float f) { return (double)f; }
+static __device__ __noinline__ float d2f_rare(double d) { return (float)d; }
+static __device__ __noinline__ double div_rare(double a, double b) { return __ddiv_rn(a, b); }
+
 // exact widening float -> double
 __device__ __forceinline__ double f2d_exact(float f) {
   const unsigned u = __float_as_uint(f);
@@ -106,7 +113,7 @@ __device__ __forceinline__ double f2d_exact(float f) {
     return __hiloint2double((int)hi, (int)(u << 29));
   }
   if ((u << 1) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);  // +-0
-  return (double)f;  // subnormal, infinity, NaN
+  return f2d_rare(f);  // subnormal, infinity, NaN
 }
 
 // double -> float, round to nearest even
@@ -124,7 +131,7 @@ __device__ __forceinline__ float d2f_rn(double d) {
     return __uint_as_float(f);
   }
   if (((hi << 1) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);  // +-0
-  return (float)d;  // below or above the binary32 normal range, infinity, NaN
+  return d2f_rare(d);  // below or above the binary32 normal range, infinity, NaN
 }
 
 // max(v, 0) for a v that is not NaN, by the sign bit (-0 gives +0)
@@ -154,7 +161,7 @@ __device__ __forceinline__ double div_rn(double a, double b) {
   const bool ge = ma >= mb;                 // quotient of the significands in [1, 2)
   const int E = ea - eb + 1022 + (int)ge;   // biased exponent of the result
   if ((unsigned)(ea - 1) >= 2046u || (unsigned)(eb - 1) >= 2046u || (unsigned)(E - 1) >= 2045u)
-    return __ddiv_rn(a, b);
+    return div_rare(a, b);
   float y0;
   asm("rcp.approx.ftz.f32 %0, %1;"
       : "=f"(y0)
@@ -247,6 +254,9 @@ void launch_rhs_given(int nx, int ny, const double* bF, LevelView L0, double* bv
                       float* r32, double* x, Scalars* sc, double* part, double rtol, int maxit,
                       cudaStream_t s);
 void launch_update_xr(LevelView L0, double* x, const double* p, double* r, float* r32,
+                      const float* z32, const double* q, Scalars* sc, double* part,
+                      unsigned long long cond, cudaStream_t s);
+void launch_update_xr(LevelView L0, double* x, const float* p, double* r, float* r32,
                       const float* z32, const double* q, Scalars* sc, double* part,
                       unsigned long long cond, cudaStream_t s);
 void launch_final_solution(const FortranIn& in, LevelView L0, const double* x,

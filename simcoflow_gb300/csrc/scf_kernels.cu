@@ -6,6 +6,8 @@
 // explicitly rounded operations (__dmul_rn/__dadd_rn/...) in the reference's
 // operation order, so that no multiply-add is fused and results match a
 // CPU restatement bit for bit.  The PCG vector updates use FMA freely.
+#include <type_traits>
+
 #include "scf_internal.cuh"
 
 namespace scf {
@@ -517,7 +519,8 @@ __device__ void rhs_finish(double acc, bool bad, Scalars* sc, double* part, doub
 // iteration count, tests convergence and, inside a graph loop, clears the
 // loop condition.  Block (0,0) also counts body executions and stops the
 // loop after maxit+2 of them whatever else happens.
-__global__ void k_update_xr(LevelView L, double* __restrict__ x, const double* __restrict__ p,
+template <class PT>
+__global__ void k_update_xr(LevelView L, double* __restrict__ x, const PT* __restrict__ p,
                             double* __restrict__ r, float* __restrict__ r32,
                             const float* __restrict__ z32, const double* __restrict__ q,
                             Scalars* sc, double* part, unsigned long long cond) {
@@ -539,7 +542,13 @@ __global__ void k_update_xr(LevelView L, double* __restrict__ x, const double* _
       const size_t k = (size_t)iy * L.pitch + ix0;
       double2 xv = *reinterpret_cast<double2*>(x + k);
       double2 rv = *reinterpret_cast<double2*>(r + k);
-      const double2 pv = *reinterpret_cast<const double2*>(p + k);
+      double2 pv;
+      if constexpr (std::is_same<PT, float>::value) {
+        const float2 pf = *reinterpret_cast<const float2*>(p + k);
+        pv = make_double2(f2d_exact(pf.x), f2d_exact(pf.y));
+      } else {
+        pv = *reinterpret_cast<const double2*>(p + k);
+      }
       const double2 qv = *reinterpret_cast<const double2*>(q + k);
       xv.x = fma(alpha, pv.x, xv.x);
       rv.x = fma(-alpha, qv.x, rv.x);
@@ -810,8 +819,14 @@ void launch_rhs_given(int nx, int ny, const double* bF, LevelView L0, double* bv
 void launch_update_xr(LevelView L0, double* x, const double* p, double* r, float* r32,
                       const float* z32, const double* q, Scalars* sc, double* part,
                       unsigned long long cond, cudaStream_t s) {
-  launch_k(k_update_xr, grid_for(L0.nx, L0.ny), kBlock, 0, s, L0, x, p, r, r32, z32, q, sc, part,
-           cond);
+  launch_k(k_update_xr<double>, grid_for(L0.nx, L0.ny), kBlock, 0, s, L0, x, p, r, r32, z32, q, sc,
+           part, cond);
+}
+void launch_update_xr(LevelView L0, double* x, const float* p, double* r, float* r32,
+                      const float* z32, const double* q, Scalars* sc, double* part,
+                      unsigned long long cond, cudaStream_t s) {
+  launch_k(k_update_xr<float>, grid_for(L0.nx, L0.ny), kBlock, 0, s, L0, x, p, r, r32, z32, q, sc,
+           part, cond);
 }
 void launch_final_solution(const FortranIn& in, LevelView L0, const double* x,
                            const double* bvec, const double* ustar, const double* vstar,

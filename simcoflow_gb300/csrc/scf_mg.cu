@@ -440,53 +440,103 @@ __device__ __forceinline__ double conv_z(float z) { return f2d_exact(z); }
 __device__ __forceinline__ double conv_z(double z) { return z; }
 
 // p_new = z + beta p_old (= z on the first iteration), q = A p_new, p.q and
-// alpha = r.z / p.q.  A 64x32 tile of p_new with a one-cell halo is built in
-// shared memory, so each p_new is formed once per CTA.
+// alpha = r.z / p.q.  Register-blocked stencil: a warp covers 32 consecutive
+// columns, of which it updates the inner 30 (the first and last lane only
+// form p_new for their neighbours, so every lane runs the same code), and
+// each thread walks `rows` rows of its column, keeping p_new of the rows
+// above and below in registers, taking east/west values from the adjacent
+// lanes and loading the next row one step ahead.  No shared memory and no
+// block barrier before the arithmetic, so the FP64 pipe stays fed.  The
+// search direction has z's precision: FP64 for the FP64 preconditioner; FP32
+// for the FP32 one, whose z carries FP32 accuracy anyway.  With an FP32
+// direction the update and the products of p.q run in FP32, summed with
+// Kahan's compensated summation per thread and in FP64 across threads (p.q
+// only sets the step length alpha),
+// while q = A p and the x/r updates stay FP64 on the same rounded p, so r
+// keeps tracking b - A x in FP64.  That leaves five FP64 operations per cell
+// (the product with the diagonal and four FMAs), the kernel's bound on
+// GB300's FP64 pipe.
 template <class ZT>
 __global__ void __launch_bounds__(NT)
-k_pupdate_spmv_t(LevelView L, const ZT* __restrict__ z, const double* __restrict__ pold,
-                 double* __restrict__ pnew, double* __restrict__ q, Scalars* sc, double* part) {
+k_pupdate_spmv_t(LevelView L, const ZT* __restrict__ z, const ZT* __restrict__ pold,
+                 ZT* __restrict__ pnew, double* __restrict__ q, Scalars* sc, double* part,
+                 int rows) {
   pdl_wait();
   if (sc->done) return;
-  constexpr int WX = SX + 2, WY = SY + 2;
-  __shared__ double ps[WY][WX];
+  constexpr bool F32 = std::is_same<ZT, float>::value;
   const int nx = L.nx, ny = L.ny, P = L.pitch;
-  const int x0 = blockIdx.x * SX, y0 = blockIdx.y * SY;
-  const int t = tlin();
+  const int lane = threadIdx.x;  // blockDim (32, 8): a warp is 32 consecutive columns
+  const int cx = blockIdx.x * 30 - 1 + lane;
+  const bool col = cx >= 0 && cx < nx;          // a column of the grid
+  const bool upd = col && lane > 0 && lane < 31;  // updated by this lane
+  const int r0 = (blockIdx.y * 8 + threadIdx.y) * rows;
+  const int r1 = r0 + rows < ny ? r0 + rows : ny;
   const bool first = sc->iter == 0;
   const double beta = sc->beta;
-  for (int e = t; e < WX * WY; e += NT) {
-    const int ex = e % WX, ey = e / WX;
-    const int gx = x0 - 1 + ex, gy = y0 - 1 + ey;
-    double v = 0.0;
-    if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
-      const size_t g = (size_t)gy * P + gx;
-      const double zd = conv_z(z[g]);
-      v = first ? zd : fma(beta, pold[g], zd);
+  const float beta_f = (float)beta;
+  // raw inputs of p_new at row y of this column (zeros outside the grid)
+  struct Raw { ZT z, p; };
+  auto load = [&](int y) -> Raw {
+    Raw r{ZT(0), ZT(0)};
+    if (col && y >= 0 && y < ny) {
+      const size_t g = (size_t)y * P + cx;
+      r.z = z[g];
+      if (!first) r.p = pold[g];
     }
-    ps[ey][ex] = v;
-  }
-  __syncthreads();
+    return r;
+  };
+  auto form = [&](const Raw& r) -> ZT {
+    if constexpr (F32) return fmaf(beta_f, r.p, r.z);
+    else return fma(beta, r.p, r.z);
+  };
+  auto wide = [](ZT v) -> double {
+    if constexpr (F32) return f2d_exact(v);
+    else return v;
+  };
   double acc = 0.0;
-  for (int e = t; e < SX * SY; e += NT) {
-    const int ex = e % SX, ey = e / SX;
-    const int gx = x0 + ex, gy = y0 + ey;
-    if (gx < nx && gy < ny) {
-      const size_t g = (size_t)gy * P + gx;
-      const int lx = ex + 1, ly = ey + 1;
-      const double pc = ps[ly][lx];
-      double qv = pos_part(L.dg[g]) * pc;
-      qv = fma(-L.cE[g], ps[ly][lx + 1], qv);
-      qv = fma(-L.cE[g - 1], ps[ly][lx - 1], qv);
-      qv = fma(-L.cN[g], ps[ly + 1][lx], qv);
-      qv = fma(-L.cN[g - P], ps[ly - 1][lx], qv);
-      pnew[g] = pc;
-      q[g] = qv;
-      acc = fma(pc, qv, acc);
+  float accf = 0.0f, accc = 0.0f;
+  if (r0 < r1) {  // uniform across the warp (one threadIdx.y per warp)
+    double pm = wide(form(load(r0 - 1)));
+    ZT pcr = form(load(r0));
+    double pc = wide(pcr);
+    double cNd = col ? L.cN[(size_t)(r0 - 1) * P + cx] : 0.0;
+    Raw nxt = load(r0 + 1);
+    for (int iy = r0; iy < r1; ++iy) {
+      const size_t k = (size_t)iy * P + cx;
+      double dg = 0.0, cE = 0.0, cN = 0.0;
+      if (col) { dg = L.dg[k]; cE = L.cE[k]; cN = L.cN[k]; }
+      const ZT ppr = form(nxt);
+      nxt = load(iy + 2);  // one row ahead
+      const double pp = wide(ppr);
+      const double pl = __shfl_up_sync(0xffffffffu, pc, 1);
+      const double pr = __shfl_down_sync(0xffffffffu, pc, 1);
+      const double cEl = __shfl_up_sync(0xffffffffu, cE, 1);
+      double qv = pos_part(dg) * pc;
+      qv = fma(-cE, pr, qv);
+      qv = fma(-cEl, pl, qv);
+      qv = fma(-cN, pp, qv);
+      qv = fma(-cNd, pm, qv);
+      if (upd) {
+        q[k] = qv;
+        pnew[k] = pcr;
+        if constexpr (F32) {  // compensated FP32 sum of the FP32 products
+          const float y = fmaf(pcr, d2f_rn(qv), -accc);
+          const float t = accf + y;
+          accc = (t - accf) - y;
+          accf = t;
+        } else {
+          acc = fma(pc, qv, acc);
+        }
+      }
+      pm = pc;
+      pc = pp;
+      pcr = ppr;
+      cNd = cN;
     }
   }
+  if constexpr (F32) acc = f2d_exact(accf) - f2d_exact(accc);
   double tot, dummy;
-  if (grid_sum2(acc, 0.0, part, &sc->tickets[T_PQ], &tot, &dummy) && t == 0) {
+  if (grid_sum2(acc, 0.0, part, &sc->tickets[T_PQ], &tot, &dummy) && tlin() == 0) {
     sc->pq = tot;
     sc->alpha = sc->rz / tot;
   }
@@ -820,10 +870,38 @@ void launch_dot_rz_t(int nx, int ny, int pitch, const BT* r, const T* z, int fle
            flexible, sc, part);
 }
 
+// Grid of the direction update + SpMV: 30-column bands times strips of 8
+// warps, each warp `rows` rows long, with `rows` chosen so that the grid is at
+// most one wave of resident CTAs (a second, partly filled wave would double
+// the kernel's time for a fraction of the work).
 template <class ZT>
-void launch_pupdate_spmv_t(LevelView L0, const ZT* z, const double* pold, double* pnew,
+dim3 pupdate_grid(int nx, int ny, int* rows) {
+  static int cap[2][16];  // resident CTAs per device and precision (0 = unknown)
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int& c = cap[std::is_same<ZT, float>::value][dev & 15];
+  if (c == 0) {
+    int sms = 0, per = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pupdate_spmv_t<ZT>, 256, 0);
+    c = sms * per > 0 ? sms * per : 1;
+  }
+  const int bands = (nx + 29) / 30;
+  const int strips = c / bands > 1 ? c / bands : 1;
+  int r = (ny + 8 * strips - 1) / (8 * strips);
+  if (r < 4) r = 4;
+  *rows = r;
+  return dim3(bands, (ny + 8 * r - 1) / (8 * r));
+}
+template dim3 pupdate_grid<double>(int, int, int*);
+template dim3 pupdate_grid<float>(int, int, int*);
+
+template <class ZT>
+void launch_pupdate_spmv_t(LevelView L0, const ZT* z, const ZT* pold, ZT* pnew,
                            double* q, Scalars* sc, double* part, cudaStream_t s) {
-  launch_k(k_pupdate_spmv_t<ZT>, tiles(L0.nx, L0.ny), dim3(NT), 0, s, L0, z, pold, pnew, q, sc, part);
+  int rows = 0;
+  const dim3 g = pupdate_grid<ZT>(L0.nx, L0.ny, &rows);
+  launch_k(k_pupdate_spmv_t<ZT>, g, dim3(32, 8), 0, s, L0, z, pold, pnew, q, sc, part, rows);
 }
 
 void launch_inv_diag(const LevelView& L, double* di, cudaStream_t s) {
@@ -931,7 +1009,7 @@ template void launch_dot_rz_t<float, float>(int, int, int, const float*, const f
                                             Scalars*, double*, cudaStream_t);
 template void launch_pupdate_spmv_t<double>(LevelView, const double*, const double*, double*,
                                             double*, Scalars*, double*, cudaStream_t);
-template void launch_pupdate_spmv_t<float>(LevelView, const float*, const double*, double*,
+template void launch_pupdate_spmv_t<float>(LevelView, const float*, const float*, float*,
                                            double*, Scalars*, double*, cudaStream_t);
 
 }  // namespace scf

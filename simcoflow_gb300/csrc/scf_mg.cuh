@@ -88,8 +88,11 @@ template <class T, class BT>
 void launch_dot_rz_t(int nx, int ny, int pitch, const BT* r, const T* z, int flexible,
                      Scalars* sc, double* part, cudaStream_t s);
 
+// grid (and rows per thread) of the direction update + SpMV kernel
 template <class ZT>
-void launch_pupdate_spmv_t(LevelView L0, const ZT* z, const double* pold, double* pnew,
+dim3 pupdate_grid(int nx, int ny, int* rows);
+template <class ZT>
+void launch_pupdate_spmv_t(LevelView L0, const ZT* z, const ZT* pold, ZT* pnew,
                            double* q, Scalars* sc, double* part, cudaStream_t s);
 
 // Line relaxation (scf_line.cu).  Lines longer than kLineMaxLen cells are

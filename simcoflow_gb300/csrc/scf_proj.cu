@@ -510,9 +510,12 @@ void enqueue_iteration(scf_proj* h, const double* pold, double* pnew, unsigned l
     launch_pupdate_spmv_t<double>(L0, buf64(h, 0, zf), pold, pnew, h->q, h->sc, h->part, s);
     launch_update_xr(L0, h->xsol, pnew, L0.b, nullptr, nullptr, h->q, h->sc, h->part, cond, s);
   } else {
+    // the FP32 preconditioner's search direction is FP32 (in the same buffers)
     const float* z = buf32(h, 0, zf);
-    launch_pupdate_spmv_t<float>(L0, z, pold, pnew, h->q, h->sc, h->part, s);
-    launch_update_xr(L0, h->xsol, pnew, L0.b, h->r32, z, h->q, h->sc, h->part, cond, s);
+    const float* po = reinterpret_cast<const float*>(pold);
+    float* pn = reinterpret_cast<float*>(pnew);
+    launch_pupdate_spmv_t<float>(L0, z, po, pn, h->q, h->sc, h->part, s);
+    launch_update_xr(L0, h->xsol, (const float*)pn, L0.b, h->r32, z, h->q, h->sc, h->part, cond, s);
   }
 }
 
@@ -733,8 +736,10 @@ int run_learned(scf_proj* h, int* nn_iters, int* fell_back) {
     } else {
       enqueue_vcycle(h, h->sc, true, s);
     }
-    launch_pupdate_spmv_t<float>(L0, z, pold, pnew, h->q, h->sc, h->part, s);
-    launch_update_xr(L0, h->xsol, pnew, L0.b, h->r32, z, h->q, h->sc, h->part, 0ull, s);
+    float* pn = reinterpret_cast<float*>(pnew);
+    launch_pupdate_spmv_t<float>(L0, z, reinterpret_cast<const float*>(pold), pn, h->q, h->sc,
+                                 h->part, s);
+    launch_update_xr(L0, h->xsol, (const float*)pn, L0.b, h->r32, z, h->q, h->sc, h->part, 0ull, s);
     CK(cudaGetLastError());
     std::swap(pold, pnew);
     if ((rc = read_scalars(h))) return rc;
@@ -1079,6 +1084,10 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
     const size_t gy = (size_t)(ny + 7) / 8;
     size_t rb = (size_t)((nx + 31) / 32) * (gy < 1024 ? gy : 1024);
     if (rb > nblk) nblk = rb;
+    // direction update + SpMV
+    int rows = 0;
+    for (const dim3 g : {pupdate_grid<double>(nx, ny, &rows), pupdate_grid<float>(nx, ny, &rows)})
+      if ((size_t)g.x * g.y > nblk) nblk = (size_t)g.x * g.y;
     // r.z fused into the last line relaxation: one block per pair of rows
     const size_t lb = (size_t)(ny + 1) / 2;
     if (lb > nblk) nblk = lb;
@@ -1384,14 +1393,19 @@ int scf_proj_time_kernel(scf_proj* h, int kernel, int reps, double* ms) {
     }
     if (kernel == SCF_K_PUPDATE_SPMV) {
       if (h->mixed)
-        launch_pupdate_spmv_t<float>(L0, buf32(h, 0, 0), h->pA, h->pB, h->q, h->sc_diag, h->part, s);
+        launch_pupdate_spmv_t<float>(L0, buf32(h, 0, 0), reinterpret_cast<const float*>(h->pA),
+                                     reinterpret_cast<float*>(h->pB), h->q, h->sc_diag, h->part, s);
       else
         launch_pupdate_spmv_t<double>(L0, L0.x, h->pA, h->pB, h->q, h->sc_diag, h->part, s);
       return;
     }
     if (kernel == SCF_K_UPDATE_XR) {
-      launch_update_xr(L0, h->xsol, h->pB, L0.b, h->r32, h->mixed ? buf32(h, 0, 0) : nullptr, h->q,
-                       h->sc_diag, h->part, 0ull, s);
+      if (h->mixed)
+        launch_update_xr(L0, h->xsol, reinterpret_cast<const float*>(h->pB), L0.b, h->r32,
+                         buf32(h, 0, 0), h->q, h->sc_diag, h->part, 0ull, s);
+      else
+        launch_update_xr(L0, h->xsol, h->pB, L0.b, h->r32, nullptr, h->q, h->sc_diag, h->part,
+                         0ull, s);
       return;
     }
     if (kernel == SCF_K_ASSEMBLE) {

@@ -34,8 +34,8 @@ import numpy as np
 from . import projection as P
 from . import synth
 
-KERNELS = {"sweep": (0, {"fp64": 48, "mixed": 20}), "pupdate_spmv": (1, {"fp64": 56, "mixed": 52}),
-           "update_xr": (2, {"fp64": 48, "mixed": 56}),
+KERNELS = {"sweep": (0, {"fp64": 48, "mixed": 20}), "pupdate_spmv": (1, {"fp64": 56, "mixed": 44}),
+           "update_xr": (2, {"fp64": 48, "mixed": 52}),
            "resid_restrict": (3, {"fp64": 58, "mixed": 25}),
            "prolong": (4, {"fp64": 50, "mixed": 21}), "assemble": (5, {"fp64": 200, "mixed": 200}),
            "vcycle": (6, {"fp64": 0, "mixed": 0}), "setup": (7, {"fp64": 0, "mixed": 0}),
