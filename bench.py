@@ -325,6 +325,103 @@ def extra_momentum(case, local, args):
     return out
 
 
+def extra_tecplot(case, local, args):
+    """Print_Result_Tecplot_PCent's file of the headline workload (15 blocks
+    of nx*ny "(f24.14)" records) from device-resident fields: the formatting
+    kernel alone (CUDA events), the text into a host buffer, and the whole
+    file written to the box's temporary directory; against the C
+    restatement's formatting into a host buffer on all host cores."""
+    import ctypes
+    import tempfile
+    import torch
+    from simcoflow_gb300 import output as Out
+    nx, ny = case.nx, case.ny
+    rng = np.random.default_rng(17)
+    F = lambda a: np.asfortranarray(a)
+    A = case.arrays
+    f = {"x": A["x"], "y": A["y"], "p": F(rng.standard_normal((nx + 2, ny + 2))),
+         "u": A["u0"], "v": A["v0"], "phi": A["phi"], "vof": A["vof"],
+         "phiS": F(rng.standard_normal((nx, ny))), "vofS": A["vofS"],
+         "mres": F(rng.standard_normal((nx, ny)) * 1e-12),
+         "flux": F(rng.standard_normal((nx + 2, ny + 2, 2))),
+         "nxS": F(rng.uniform(-1, 1, (nx, ny))), "nyS": F(rng.uniform(-1, 1, (nx, ny)))}
+    f = {k: F(np.asarray(v, dtype=np.float64)) for k, v in f.items()}
+    dev = torch.device("cuda", local)
+    tf = {k: torch.from_numpy(np.ascontiguousarray(v.ravel(order="F"))).to(dev)
+          for k, v in f.items()}
+    L = Out.load()
+    size = L.scf_tecplot_size(Out.PCELL, nx, ny)
+    cells = nx * ny
+    out = {"workload": f"Tecplot P-cell file of the {nx}x{ny} headline workload "
+                       f"(15 variables, {size / 1e9:.2f} GB of text)"}
+    # formatting kernel alone
+    body = torch.empty(15 * cells * 25, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(3):
+        Out.format_device("p", nx, ny, tf, body, stream.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 10
+    e0.record(stream)
+    for _ in range(reps):
+        Out.format_device("p", nx, ny, tf, body, stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms_kernel = e0.elapsed_time(e1) / reps
+    # algorithmic bytes: 15 x 8 B read (neighbour values of the averages come
+    # from cache) and 15 x 25 B of text written per cell
+    alg = cells * 15 * (8 + 25)
+    peak, peak_kind = _peaks()
+    # the text into a host buffer (C-ABI call only; the buffer is made once)
+    st, keep = Out._fields(Out.PCELL, nx, ny, tf, True)
+    buf = ctypes.create_string_buffer(size)
+    n = ctypes.c_int64(0)
+
+    def text_once():
+        rc = L.scf_tecplot_text(Out.PCELL, nx, ny, ctypes.byref(st), Out.DEVICE_PTRS, buf, size,
+                                ctypes.byref(n), local)
+        if rc != 0:
+            raise RuntimeError(f"scf_tecplot_text {rc}")
+
+    for _ in range(2):
+        text_once()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        text_once()
+    ms_text = (time.perf_counter() - t0) / 3 * 1e3
+    with tempfile.TemporaryDirectory() as d:
+        os.makedirs(os.path.join(d, "Tecplot"))
+        ms_file = min(Out.write("p", nx, ny, tf, 1, d + "/", device_ptrs=True, device=local)
+                      for _ in range(3))
+    out["gpu"] = {
+        "ms_format_kernel": round(ms_kernel, 3),
+        "roofline": {"bound": "hbm", "achieved": round(alg / (ms_kernel * 1e-3) / 1e9, 1),
+                     "peak": peak, "unit": "GB/s",
+                     "frac": round(alg / (ms_kernel * 1e-3) / 1e9 / peak, 3),
+                     "peak_kind": peak_kind, "bytes_per_cell": 15 * (8 + 25)},
+        "ms_text_in_host_memory": round(ms_text, 2),
+        "ms_file_write": round(ms_file, 2),
+        "timing": "kernel: CUDA events; text: host clock around scf_tecplot_text "
+                  "(kernel, pinned 16 MiB chunks, 4 copy threads); file: host clock around "
+                  "scf_tecplot_write (one writer thread) into the temporary directory"}
+    if not args.no_cpu:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle as O
+        threads = os.cpu_count() or 1
+        O.lib().oracle_set_threads(threads)
+        cbuf = ctypes.create_string_buffer(size + 256)
+        args_ = [O._p(f[k]) for k in O.PCELL_FIELDS]
+        t0 = time.perf_counter()
+        m = O.lib().oracle_tecplot_pcell(nx, ny, *args_, cbuf)
+        cpu_ms = (time.perf_counter() - t0) * 1e3
+        out["cpu"] = {"ms_text_in_host_memory": round(cpu_ms, 1), "cores": threads,
+                      "kind": "port", "sample": "the whole file text (C restatement, "
+                      "snprintf %24.14f per record, OpenMP over rows) into a host buffer"}
+        out["identical_to_oracle"] = bool(m == n.value and
+                                          ctypes.string_at(cbuf, m) == ctypes.string_at(buf, m))
+        out["speedup_text_vs_cpu"] = round(cpu_ms / ms_text, 1)
+    return out
+
+
 def extra_batch(local):
     """64 uneven instances in one graph launch with autotuned schedules."""
     from simcoflow_gb300 import synth, batch as Bt
@@ -604,7 +701,8 @@ def run_ours(args):
         for name, fn in (("learned", lambda: extra_learned(case, tdev, dev, local, args)),
                          ("stretched_4096", lambda: extra_stretched(local, args)),
                          ("batch_64", lambda: extra_batch(local)),
-                         ("momentum_2048", lambda: extra_momentum(case, local, args))):
+                         ("momentum_2048", lambda: extra_momentum(case, local, args)),
+                         ("tecplot_2048", lambda: extra_tecplot(case, local, args))):
             try:
                 extras[name] = fn()
             except Exception as e:  # an extra must not hide the headline line

@@ -50,6 +50,7 @@ extern "C" {
 #define SCF_ERR_TIMEOUT (-6)       /* a bounded device-side wait ran out */
 #define SCF_ERR_STATE (-7)         /* call order: e.g. solve before assemble */
 #define SCF_ERR_NOMEM (-8)         /* device allocation failed */
+#define SCF_ERR_IO (-9)            /* a file could not be opened or written */
 
 #define SCF_PREC_FP64 0  /* FP64 MG preconditioner inside FP64 PCG */
 #define SCF_PREC_MIXED 1 /* FP32 MG with BF16 couplings inside FP64 flexible PCG */

@@ -1,7 +1,8 @@
 """Build recipe of the oracle (test infrastructure only).
 
-Compiles oracle/scf_oracle.c (projection) and oracle/mom_oracle.c (momentum
-predictor solves) into oracle/_build/liboracle.so with gcc.
+Compiles oracle/scf_oracle.c (projection), oracle/mom_oracle.c (momentum
+predictor solves) and oracle/out_oracle.c (Tecplot result files) into
+oracle/_build/liboracle.so with gcc.
 -ffp-contract=off keeps every multiply and add separately rounded, as in
 the reference's Fortran build (mpif77 without FMA flags), so that the
 restatement gives the same bits on x86-64 and aarch64.
@@ -16,7 +17,7 @@ OUT = HERE / "_build" / "liboracle.so"
 
 
 def build(force: bool = False) -> Path:
-    srcs = [HERE / "scf_oracle.c", HERE / "mom_oracle.c"]
+    srcs = [HERE / "scf_oracle.c", HERE / "mom_oracle.c", HERE / "out_oracle.c"]
     OUT.parent.mkdir(exist_ok=True)
     newest = max(p.stat().st_mtime for p in srcs)
     if force or not OUT.exists() or OUT.stat().st_mtime < newest:

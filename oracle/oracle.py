@@ -27,6 +27,10 @@ Pieces:
     mom_predict SetMatrix, SetVectors, solve, DeltaGetValues, gradient update,
                 Dp copies              src/PredictorUV_mod.f90:507-563, 622-885
                 (solve: SuperLU, or the C BiCGStab of the CPU baseline)
+  C restatement of the Tecplot result files (out_oracle.c)
+    tecplot_pcell / tecplot_vcell   Print_Result_Tecplot_PCent / _UCent /
+                _VCent                 src/PrintResult.f90:39-168
+    f24_14      the "(f24.14)" number format
 """
 from __future__ import annotations
 
@@ -82,6 +86,11 @@ def lib():
                                           C.POINTER(C.c_double)])
         L.oracle_num_threads.restype = C.c_int
         L.oracle_set_threads.argtypes = [C.c_int]
+        L.oracle_format_many.argtypes = [_P, C.c_int64, C.c_char_p]
+        L.oracle_tecplot_pcell.restype = C.c_int64
+        L.oracle_tecplot_pcell.argtypes = [C.c_int, C.c_int] + [_P] * 13 + [C.c_char_p]
+        L.oracle_tecplot_vcell.restype = C.c_int64
+        L.oracle_tecplot_vcell.argtypes = [C.c_int, C.c_int, C.c_int] + [_P] * 7 + [C.c_char_p]
         _lib = L
     return _lib
 
@@ -472,3 +481,37 @@ def mom_predict(mi, solver="direct", rtol=1e-14, maxit=500) -> dict:
                         _p(mi["dx"]), _p(mi["dy"]), mi["dt"], _p(pred), _p(Dp))
     return {"pred": pred, "Dp": Dp, "matr": op["matr"], "rhm": op["rhm"], "x": x,
             "A": A, "b": b, "iters": its, "bad": op["bad"]}
+
+
+# ---------------------------------------------------------------------------
+# Tecplot result files (out_oracle.c; src/PrintResult.f90:39-168)
+# ---------------------------------------------------------------------------
+PCELL_FIELDS = ["x", "y", "p", "u", "v", "phi", "vof", "phiS", "vofS", "mres", "flux", "nxS",
+                "nyS"]
+VCELL_FIELDS = ["x", "y", "vel", "phi", "vof", "phiS", "vofS"]
+
+
+def f24_14(values) -> bytes:
+    """F24.14 text of every value, 24 bytes each, no line ends."""
+    v = np.ascontiguousarray(values, dtype=np.float64).ravel()
+    out = C.create_string_buffer(24 * v.size + 1)
+    lib().oracle_format_many(v.ctypes.data_as(_P), v.size, out)
+    return out.raw[:24 * v.size]
+
+
+def tecplot_size(nvar, nx, ny) -> int:
+    return 200 + nvar * nx * ny * 25
+
+
+def tecplot_pcell(nx, ny, f) -> bytes:
+    """The text of Print_Result_Tecplot_PCent's file (without particles)."""
+    buf = C.create_string_buffer(tecplot_size(15, nx, ny))
+    n = lib().oracle_tecplot_pcell(nx, ny, *[_p(f[k]) for k in PCELL_FIELDS], buf)
+    return buf.raw[:n]
+
+
+def tecplot_vcell(comp, nx, ny, f) -> bytes:
+    """The text of Print_Result_Tecplot_UCent (comp 0) / _VCent (comp 1)."""
+    buf = C.create_string_buffer(tecplot_size(8, nx, ny))
+    n = lib().oracle_tecplot_vcell(comp, nx, ny, *[_p(f[k]) for k in VCELL_FIELDS], buf)
+    return buf.raw[:n]

@@ -22,7 +22,7 @@ INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["scf_kernels.cu", "scf_mg.cu", "scf_line.cu", "scf_unet.cu", "scf_proj.cu",
-                "scf_noalloc.cu", "scf_mom.cu", "scf_geom.cu"]
+                "scf_noalloc.cu", "scf_mom.cu", "scf_geom.cu", "scf_out.cu"]
 
 
 def nvcc() -> str:
@@ -48,7 +48,7 @@ def _stale(out: Path, deps: list[Path]) -> bool:
 def build_proj(force: bool = False, verbose: bool = False) -> Path:
     LIB.mkdir(exist_ok=True)
     out = LIB / "libscf_proj.so"
-    headers = list(CSRC.glob("*.cuh")) + [INCLUDE / "scf_proj.h"]
+    headers = list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
     objs, jobs = [], []
     for src in CUDA_SOURCES:
         s = CSRC / src

@@ -932,6 +932,7 @@ const char* scf_strerror(int code) {
     case SCF_ERR_TIMEOUT: return "bounded device wait ran out";
     case SCF_ERR_STATE: return "call order (grid, geometry and assemble must come first)";
     case SCF_ERR_NOMEM: return "device memory allocation failed";
+    case SCF_ERR_IO: return "file could not be opened or written";
     default: return "unknown status";
   }
 }

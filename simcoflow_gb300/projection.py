@@ -31,7 +31,8 @@ _lib = None
 SCF_OK = 0
 SCF_ERR_NOT_CONVERGED = -4
 ERRORS = {-1: "SCF_ERR_ARG", -2: "SCF_ERR_CUDA", -3: "SCF_ERR_NAN", -4: "SCF_ERR_NOT_CONVERGED",
-          -5: "SCF_ERR_STALL", -6: "SCF_ERR_TIMEOUT", -7: "SCF_ERR_STATE", -8: "SCF_ERR_NOMEM"}
+          -5: "SCF_ERR_STALL", -6: "SCF_ERR_TIMEOUT", -7: "SCF_ERR_STATE", -8: "SCF_ERR_NOMEM",
+          -9: "SCF_ERR_IO"}
 PREC = {"fp64": 0, "mixed": 1}
 FLAG_DEVICE_PTRS = 1
 FLAG_NO_GRAPH = 2

@@ -114,3 +114,49 @@ def test_momentum_input_struct_layout(tmp_path):
     assert int(out[0]) == ctypes.sizeof(M.MomIn)
     for n, off in zip(fields, out[1:]):
         assert int(off) == getattr(M.MomIn, n).offset, n
+
+
+def test_proj_library_exports_output_header_symbols(built):
+    from simcoflow_gb300 import build, output
+    lib = ctypes.CDLL(str(build.build_proj()))
+    names = _declared("scf_out.h")
+    for n in names:
+        assert hasattr(lib, n), n
+    assert sorted(output.EXPORTS) == names
+
+
+def test_output_field_struct_layouts(tmp_path):
+    """The ctypes mirrors of scf_tecplot_pcell / _vcell have the header's layout."""
+    import shutil
+    import subprocess
+    if not shutil.which("gcc"):
+        import pytest
+        pytest.skip("no C compiler")
+    from simcoflow_gb300 import output as O
+    for cname, S in (("scf_tecplot_pcell", O.PCellFields), ("scf_tecplot_vcell", O.VCellFields)):
+        src = tmp_path / f"{cname}.c"
+        fields = [n for n, _ in S._fields_]
+        src.write_text(
+            '#include <stdio.h>\n#include <stddef.h>\n#include "scf_out.h"\n'
+            "int main(void) {\n"
+            f'  printf("%zu\\n", sizeof({cname}));\n'
+            + "".join(f'  printf("%zu\\n", offsetof({cname}, {n}));\n' for n in fields)
+            + "  return 0;\n}\n")
+        exe = tmp_path / cname
+        subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+        out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+        assert int(out[0]) == ctypes.sizeof(S)
+        for n, off in zip(fields, out[1:]):
+            assert int(off) == getattr(S, n).offset, n
+
+
+def test_tecplot_size_host_only(built):
+    """scf_tecplot_size is host arithmetic: header plus 25 bytes per record."""
+    from simcoflow_gb300 import output as O
+    L = O.load()
+    hdr_p = len(' title = "flow"\n') + len(
+        ' variables ="x","y","p","u","v","phi","vof","phiS","vofS","vofA","Mres","FluxU",'
+        '"FluxV","nxS","nyS"\n') + len(" zone i=   37,k=   29,f=block\n")
+    assert L.scf_tecplot_size(O.PCELL, 37, 29) == hdr_p + 15 * 37 * 29 * 25
+    assert L.scf_tecplot_size(O.UCELL, 37, 29) > 8 * 37 * 29 * 25
+    assert L.scf_tecplot_size(7, 37, 29) == -1
