@@ -28,6 +28,8 @@ Pieces:
                 Dp copies              src/PredictorUV_mod.f90:507-563, 622-885
                 (solve: SuperLU, or the C BiCGStab of the CPU baseline)
   C restatement of the Tecplot result files (out_oracle.c)
+  cutcell_literal.grid_preprocess   pure-Python Grid_Preprocess + NewCellFace
+                for the P, U and V families (src/Cutcell_Mod.f90:18-725)
     tecplot_pcell / tecplot_vcell   Print_Result_Tecplot_PCent / _UCent /
                 _VCent                 src/PrintResult.f90:39-168
     f24_14      the "(f24.14)" number format
@@ -515,3 +517,10 @@ def tecplot_vcell(comp, nx, ny, f) -> bytes:
     buf = C.create_string_buffer(tecplot_size(8, nx, ny))
     n = lib().oracle_tecplot_vcell(comp, nx, ny, *[_p(f[k]) for k in VCELL_FIELDS], buf)
     return buf.raw[:n]
+
+
+def grid_preprocess_literal(nx, ny, grids, fams, icorprob=True, aln_old=None):
+    """Grid_Preprocess + NewCellFace for all three families (see
+    cutcell_literal)."""
+    import cutcell_literal
+    return cutcell_literal.grid_preprocess(nx, ny, grids, fams, icorprob, aln_old)

@@ -22,7 +22,10 @@ INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["scf_kernels.cu", "scf_mg.cu", "scf_line.cu", "scf_unet.cu", "scf_proj.cu",
-                "scf_noalloc.cu", "scf_mom.cu", "scf_geom.cu", "scf_out.cu"]
+                "scf_noalloc.cu", "scf_mom.cu", "scf_geom.cu", "scf_out.cu", "scf_cutcell.cu"]
+# per-file flags: the cut-cell geometry restates the reference's expressions
+# with every multiply and add rounded on its own (no FMA contraction)
+EXTRA_FLAGS = {"scf_cutcell.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:
@@ -56,7 +59,7 @@ def build_proj(force: bool = False, verbose: bool = False) -> Path:
         objs.append(o)
         if force or _stale(o, [s] + headers):
             cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                   "-I", str(INCLUDE), "-c", str(s), "-o", str(o)]
+                   *EXTRA_FLAGS.get(src, []), "-I", str(INCLUDE), "-c", str(s), "-o", str(o)]
             if verbose:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)

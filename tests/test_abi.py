@@ -160,3 +160,38 @@ def test_tecplot_size_host_only(built):
     assert L.scf_tecplot_size(O.PCELL, 37, 29) == hdr_p + 15 * 37 * 29 * 25
     assert L.scf_tecplot_size(O.UCELL, 37, 29) > 8 * 37 * 29 * 25
     assert L.scf_tecplot_size(7, 37, 29) == -1
+
+
+def test_proj_library_exports_cutcell_header_symbols(built):
+    from simcoflow_gb300 import build, cutcell
+    lib = ctypes.CDLL(str(build.build_proj()))
+    names = _declared("scf_cutcell.h")
+    for n in names:
+        assert hasattr(lib, n), n
+    assert sorted(cutcell.EXPORTS) == names
+
+
+def test_cutcell_struct_layouts(tmp_path):
+    """The ctypes mirrors of scf_cell_grid / _solid / _geom have the header's layout."""
+    import shutil
+    import subprocess
+    if not shutil.which("gcc"):
+        import pytest
+        pytest.skip("no C compiler")
+    from simcoflow_gb300 import cutcell as CU
+    for cname, S in (("scf_cell_grid", CU.CellGrid), ("scf_cell_solid", CU.CellSolid),
+                     ("scf_cell_geom", CU.CellGeom)):
+        src = tmp_path / f"{cname}.c"
+        fields = [n for n, _ in S._fields_]
+        src.write_text(
+            '#include <stdio.h>\n#include <stddef.h>\n#include "scf_cutcell.h"\n'
+            "int main(void) {\n"
+            f'  printf("%zu\\n", sizeof({cname}));\n'
+            + "".join(f'  printf("%zu\\n", offsetof({cname}, {n}));\n' for n in fields)
+            + "  return 0;\n}\n")
+        exe = tmp_path / cname
+        subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+        out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+        assert int(out[0]) == ctypes.sizeof(S)
+        for n, off in zip(fields, out[1:]):
+            assert int(off) == getattr(S, n).offset, n
