@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "../../include/scf_cutcell.h"
@@ -57,24 +58,46 @@ __device__ __forceinline__ double& C2(double* a, const Fam& f, int i, int j, int
   return a[I1(f, i, j) + k * N1(f)];
 }
 
-// Edge_Geo_Cal (:302-337): solid fraction of the edge p1-p2 and the centre of
-// its solid part
-__device__ void edge(double p1x, double p1y, double p2x, double p2y, double a, double b,
-                     double p, double* area, double* fx, double* fy) {
-  const double l1 = a * p1x + b * p1y + p, l2 = a * p2x + b * p2y + p;
-  const double eps = 1.0e-14;
-  *fx = 0.5 * (p1x + p2x);
-  *fy = 0.5 * (p1y + p2y);
-  if (l1 >= eps && l2 >= eps) {
+// IEEE division on the integer pipe (bit-identical; GB300's FP64 pipe is slow).
+// Halvings are written as products with 0.5, which round identically.
+__device__ __forceinline__ double dv(double a, double b) { return div_rn(a, b); }
+// sqrt(x) with the common x = 0 (open or closed cells) taken without the FP64 pipe
+__device__ __forceinline__ double sqrt0(double x) { return x == 0.0 ? x : sqrt(x); }
+
+// l >= 1e-14 and l < 1e-14 (both false for NaN) by the bit pattern, on the
+// integer pipe: for non-NaN doubles and a positive constant the signed
+// 64-bit patterns order like the values
+constexpr long long kE14 = 0x3d06849b86a12b9bll;  // 1.0e-14
+__device__ __forceinline__ bool nan_bits(long long u) {
+  return (u & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+}
+__device__ __forceinline__ bool ge14(double l) {
+  const long long u = __double_as_longlong(l);
+  return !nan_bits(u) && u >= kE14;
+}
+__device__ __forceinline__ bool lt14(double l) {
+  const long long u = __double_as_longlong(l);
+  return !nan_bits(u) && u < kE14;
+}
+
+// Edge_Geo_Cal (:302-337) from the level set at the edge's ends l1 (p1) and
+// l2 (p2): solid fraction of the edge and the centre of its solid part.
+// (mx, my) is the edge's midpoint 0.5*(p1+p2), given exactly by the caller.
+__device__ void edge(double p1x, double p1y, double p2x, double p2y, double l1, double l2,
+                     double mx, double my, double* area, double* fx, double* fy) {
+  *fx = mx;
+  *fy = my;
+  const bool g1 = ge14(l1), g2 = ge14(l2), s1 = lt14(l1), s2 = lt14(l2);
+  if (g1 && g2) {
     *area = 0.0;
-  } else if (l1 < eps && l2 < eps) {
+  } else if (s1 && s2) {
     *area = 1.0;
-  } else if (l1 >= eps && l2 < eps) {
-    *area = fabs(l2) / (fabs(l1) + fabs(l2));
+  } else if (g1 && s2) {
+    *area = dv(fabs(l2), fabs(l1) + fabs(l2));
     if (fabs(p1x - p2x) <= 1.0e-10) *fy = p2y - 0.5 * *area * (p2y - p1y);
     else *fx = p2x - 0.5 * *area * (p2x - p1x);
-  } else if (l1 < eps && l2 >= eps) {
-    *area = fabs(l1) / (fabs(l1) + fabs(l2));
+  } else if (s1 && g2) {
+    *area = dv(fabs(l1), fabs(l1) + fabs(l2));
     if (fabs(p1x - p2x) <= 1.0e-10) *fy = p1y - 0.5 * *area * (p1y - p2y);
     else *fx = p1x - 0.5 * *area * (p1x - p2x);
   } else {
@@ -87,26 +110,47 @@ __device__ void edge(double p1x, double p1y, double p2x, double p2y, double a, d
   const int j = blockIdx.y * 8 + threadIdx.y + 1;         \
   if (i > (f).nx || j > (f).ny) return;
 
+// bit-exact equality of two doubles on the integer pipe
+__device__ __forceinline__ bool same(double a, double b) {
+  return __double_as_longlong(a) == __double_as_longlong(b);
+}
+
 // Cell_Geo_Cal (:45-89): edge fractions, solid-part face centres, WlLh from
-// the solid fractions; Cell_Cent = 0
+// the solid fractions; Cell_Cent = 0.  Exact rewrites of the reference's
+// expressions: the corners are (-h, -k), (-h, k), (h, k), (h, -k) with
+// h = dx*0.5, k = dy*0.5 (the reference's -dx*(0.5-ii) for ii = 0, 1); a
+// product with -h is the negated product with h, so the level set at each
+// corner is +-(a h) +- (b k) + phiS, evaluated once per corner (the
+// reference evaluates it once per edge through the corner, the same
+// expression); the midpoints of the edges are the corners' shared
+// coordinate and 0 (-k + k = +0); WlLh is +0 when the opposite fractions are
+// equal.
 __global__ void k_cg_edges(Fam f) {
   CELL_LOOP(f)
   const double dx = f.dx[I1(f, i, j)], dy = f.dy[I1(f, i, j)];
   const double a = f.nxS[I1(f, i, j)], b = f.nyS[I1(f, i, j)], p = f.phiS[I1(f, i, j)];
-  const double x0 = -dx * (0.5 - 0.0), x1 = -dx * (0.5 - 1.0);
-  const double y0 = -dy * (0.5 - 0.0), y1 = -dy * (0.5 - 1.0);
+  const double h = dx * 0.5, k = dy * 0.5;
+  const double x0 = -h, x1 = h, y0 = -k, y1 = k;
+  const double ah = a * h, bk = b * k;
+  const double l00 = -ah + -bk + p, l01 = -ah + bk + p;
+  const double l11 = ah + bk + p, l10 = ah + -bk + p;
   double W, N, E, S, fx, fy;
-  edge(x0, y0, x0, y1, a, b, p, &W, &fx, &fy);
+  edge(x0, y0, x0, y1, l00, l01, x0, 0.0, &W, &fx, &fy);
   C2(f.FCW, f, i, j, 0) = fx; C2(f.FCW, f, i, j, 1) = fy;
-  edge(x0, y1, x1, y1, a, b, p, &N, &fx, &fy);
+  edge(x0, y1, x1, y1, l01, l11, 0.0, y1, &N, &fx, &fy);
   FC(f.FCN, f, i, j, 0) = fx; FC(f.FCN, f, i, j, 1) = fy;
-  edge(x1, y1, x1, y0, a, b, p, &E, &fx, &fy);
+  edge(x1, y1, x1, y0, l11, l10, x1, 0.0, &E, &fx, &fy);
   FC(f.FCE, f, i, j, 0) = fx; FC(f.FCE, f, i, j, 1) = fy;
-  edge(x1, y0, x0, y0, a, b, p, &S, &fx, &fy);
+  edge(x1, y0, x0, y0, l10, l00, 0.0, y0, &S, &fx, &fy);
   C2(f.FCS, f, i, j, 0) = fx; C2(f.FCS, f, i, j, 1) = fy;
   f.aW[I0(f, i, j)] = W; f.aN[I0(f, i, j)] = N; f.aE[I0(f, i, j)] = E; f.aS[I0(f, i, j)] = S;
-  const double ta = (E - W) * dx, tb = (N - S) * dy;
-  f.WlLh[I1(f, i, j)] = sqrt(ta * ta + tb * tb);
+  double wl = 0.0;
+  if (!same(E, W) || !same(N, S) || nan_bits(__double_as_longlong(E)) ||
+      nan_bits(__double_as_longlong(N))) {
+    const double ta = (E - W) * dx, tb = (N - S) * dy;
+    wl = sqrt0(ta * ta + tb * tb);
+  }
+  f.WlLh[I1(f, i, j)] = wl;
   C2(f.cent, f, i, j, 0) = 0.0;
   C2(f.cent, f, i, j, 1) = 0.0;
   if (f.delh) f.delh[I1(f, i, j)] = 0.0;
@@ -146,16 +190,28 @@ __global__ void k_cg_ghost_rows(Fam f) {
   FC(f.FCN, f, i, ny + 1, 1) = en1 + dyn;
 }
 
-// (:114-153) open fractions and the open parts' face centres
+// (:114-153) open fractions and the open parts' face centres.  |c| < epsi
+// and a < epsiF on the bit patterns (integer pipe; a is never NaN here, an
+// open fraction in [0, 1]); 1 - 0 and 1 - 1 without the FP64 pipe.
+constexpr long long kEpsiBits = 0x3f50624dd2f1a9fcll;   // 1.0e-3
+constexpr long long kEpsFBits = 0x3f847ae147ae147bll;   // 1.0e-2
 __device__ __forceinline__ double open_centre(double c, double a, double h) {
-  double r = fabs(c) < kEpsi ? 0.0 : (0.5 - a / 2.0) * copysign(1.0, -c) * h;
-  return a < kEpsF ? 0.0 : r;
+  if (__double_as_longlong(a) < kEpsFBits) return 0.0;  // a >= 0: a < epsiF
+  const long long cb = __double_as_longlong(c) & 0x7fffffffffffffffll;
+  if (cb < kEpsiBits) return 0.0;  // |c| < epsi (NaN c takes the formula, as in IEEE)
+  return (0.5 - a * 0.5) * copysign(1.0, -c) * h;
+}
+__device__ __forceinline__ double one_minus(double x) {
+  if (same(x, 0.0)) return 1.0;
+  if (same(x, 1.0)) return 0.0;
+  return 1.0 - x;
 }
 __global__ void k_cg_open(Fam f) {
   CELL_LOOP(f)
   const double dx = f.dx[I1(f, i, j)], dy = f.dy[I1(f, i, j)];
   const size_t k = I0(f, i, j);
-  const double W = 1.0 - f.aW[k], E = 1.0 - f.aE[k], N = 1.0 - f.aN[k], S = 1.0 - f.aS[k];
+  const double W = one_minus(f.aW[k]), E = one_minus(f.aE[k]), N = one_minus(f.aN[k]),
+               S = one_minus(f.aS[k]);
   f.aW[k] = W; f.aE[k] = E; f.aN[k] = N; f.aS[k] = S;
   FC(f.FCE, f, i, j, 1) = open_centre(FC(f.FCE, f, i, j, 1), E, dy);
   C2(f.FCW, f, i, j, 1) = open_centre(C2(f.FCW, f, i, j, 1), W, dy);
@@ -166,28 +222,37 @@ __global__ void k_cg_open(Fam f) {
 // (:155-203) faces shared by two inner cells: harmonic mean of the open
 // fractions, weighted face centres; each thread owns its cell's north and
 // east faces
+// (a*u + b*v) / (u + v + 1e-24) for the open fractions u, v of a shared
+// face: two fully open faces (u = v = 1) give (a + b) / 2 exactly (1e-24 is
+// far below an ulp of 2), without the division
+__device__ __forceinline__ double wmean(double a, double u, double b, double v) {
+  if (u == 1.0 && v == 1.0) return (a + b) * 0.5;
+  return dv(a * u + b * v, u + v + kRnd);
+}
+__device__ __forceinline__ double hmean(double u, double v) {
+  if (u == 1.0 && v == 1.0) return 1.0;  // 2 / (2 + 1e-24) rounds to 1
+  return dv(2.0 * u * v, u + v + kRnd);
+}
 __global__ void k_cg_average(Fam f) {
   CELL_LOOP(f)
   if (i < 2 || i > f.nx - 1 || j < 2 || j > f.ny - 1) return;
   const size_t k = I0(f, i, j), kn = I0(f, i, j + 1), ke = I0(f, i + 1, j);
   const double N = f.aN[k], Sn = f.aS[kn];
-  double av = 2.0 * N * Sn / (N + Sn + kRnd);
-  const double n0 = (FC(f.FCN, f, i, j, 0) * N + C2(f.FCS, f, i, j + 1, 0) * Sn) / (N + Sn + kRnd);
-  double n1 = (FC(f.FCN, f, i, j, 1) * N +
-               (C2(f.FCS, f, i, j + 1, 1) + (f.y[I1(f, i, j + 1)] - f.y[I1(f, i, j)])) * Sn) /
-              (N + Sn + kRnd);
-  if (N < kEpsF && Sn < kEpsF) n1 = f.dy[I1(f, i, j)] / 2.0;
+  double av = hmean(N, Sn);
+  const double n0 = wmean(FC(f.FCN, f, i, j, 0), N, C2(f.FCS, f, i, j + 1, 0), Sn);
+  double n1 = wmean(FC(f.FCN, f, i, j, 1), N,
+                    C2(f.FCS, f, i, j + 1, 1) + (f.y[I1(f, i, j + 1)] - f.y[I1(f, i, j)]), Sn);
+  if (N < kEpsF && Sn < kEpsF) n1 = f.dy[I1(f, i, j)] * 0.5;
   FC(f.FCN, f, i, j, 0) = n0;
   FC(f.FCN, f, i, j, 1) = n1;
   f.aN[k] = av;
   f.aS[kn] = av;
   const double E = f.aE[k], We = f.aW[ke];
-  av = 2.0 * E * We / (E + We + kRnd);
-  double e0 = (FC(f.FCE, f, i, j, 0) * E +
-               (C2(f.FCW, f, i + 1, j, 0) + (f.x[I1(f, i + 1, j)] - f.x[I1(f, i, j)])) * We) /
-              (E + We + kRnd);
-  const double e1 = (FC(f.FCE, f, i, j, 1) * E + C2(f.FCW, f, i + 1, j, 1) * We) / (E + We + kRnd);
-  if (E < kEpsF && We < kEpsF) e0 = f.dx[I1(f, i, j)] / 2.0;
+  av = hmean(E, We);
+  double e0 = wmean(FC(f.FCE, f, i, j, 0), E,
+                    C2(f.FCW, f, i + 1, j, 0) + (f.x[I1(f, i + 1, j)] - f.x[I1(f, i, j)]), We);
+  const double e1 = wmean(FC(f.FCE, f, i, j, 1), E, C2(f.FCW, f, i + 1, j, 1), We);
+  if (E < kEpsF && We < kEpsF) e0 = f.dx[I1(f, i, j)] * 0.5;
   FC(f.FCE, f, i, j, 0) = e0;
   FC(f.FCE, f, i, j, 1) = e1;
   f.aE[k] = av;
@@ -230,11 +295,11 @@ __global__ void k_ncf_cent(Fam t, Fam p, int u) {
   const int mo = t.moex[k];
   if (mo != 1 && t.vofS[k] > kEpsi) {
     if (u) {
-      C2(t.cent, t, i, j, 0) = FC(p.FCE, p, i, j, 0) - p.dx[k] / 2.0;
+      C2(t.cent, t, i, j, 0) = FC(p.FCE, p, i, j, 0) - p.dx[k] * 0.5;
       C2(t.cent, t, i, j, 1) = FC(p.FCE, p, i, j, 1);
     } else {
       C2(t.cent, t, i, j, 0) = FC(p.FCN, p, i, j, 0);
-      C2(t.cent, t, i, j, 1) = FC(p.FCN, p, i, j, 1) - p.dy[k] / 2.0;
+      C2(t.cent, t, i, j, 1) = FC(p.FCN, p, i, j, 1) - p.dy[k] * 0.5;
     }
   }
   if (mo != 1) return;
@@ -244,15 +309,15 @@ __global__ void k_ncf_cent(Fam t, Fam p, int u) {
     const double Ec = t.aE[I0(t, i, j)], Ew = t.aE[I0(t, i - 1, j)];
     double cx = C2(t.cent, t, i, j, 0), cy = C2(t.cent, t, i, j, 1);
     if (Nc * Ns == 0.0) {
-      cx = FC(t.FCN, t, i, j, 0) * Nc / (Nc + tol) + FC(t.FCN, t, i, j - 1, 0) * Ns / (Ns + tol);
+      cx = dv(FC(t.FCN, t, i, j, 0) * Nc, Nc + tol) + dv(FC(t.FCN, t, i, j - 1, 0) * Ns, Ns + tol);
     } else {
-      cy = FC(t.FCE, t, i, j, 1) * Ec / (Ec + tol) + FC(t.FCE, t, i - 1, j, 1) * Ew / (Ew + tol);
-      cx = -(nys * cy + phs) / (nxs + tol);
+      cy = dv(FC(t.FCE, t, i, j, 1) * Ec, Ec + tol) + dv(FC(t.FCE, t, i - 1, j, 1) * Ew, Ew + tol);
+      cx = dv(-(nys * cy + phs), nxs + tol);
     }
     if (Ec * Ew == 0.0) {
-      cy = FC(t.FCE, t, i, j, 1) * Ec / (Ec + tol) + FC(t.FCE, t, i - 1, j, 1) * Ew / (Ew + tol);
+      cy = dv(FC(t.FCE, t, i, j, 1) * Ec, Ec + tol) + dv(FC(t.FCE, t, i - 1, j, 1) * Ew, Ew + tol);
     } else {
-      cy = -(nxs * cx + phs) / (nys + tol);
+      cy = dv(-(nxs * cx + phs), nys + tol);
     }
     C2(t.cent, t, i, j, 0) = cx;
     C2(t.cent, t, i, j, 1) = cy;
@@ -284,7 +349,7 @@ __global__ void k_ncf_delh(Fam t) {
   t.delh[k] = d;
   const double a = (t.aE[I0(t, i, j)] - t.aW[I0(t, i, j)]) * t.dx[k];
   const double b = (t.aN[I0(t, i, j)] - t.aS[I0(t, i, j)]) * t.dy[k];
-  t.WlLh[k] = sqrt(a * a + b * b);
+  t.WlLh[k] = sqrt0(a * a + b * b);
 }
 
 // EastFaceInterpolationInf (:551-604) for i = 1..nx-1; bdx = BGrid%dx
@@ -298,7 +363,7 @@ __global__ void k_ncf_east(Fam t, const double* bdx, int iu) {
     const double e0 = C2(t.cent, t, i + 1, j, 0), e1 = C2(t.cent, t, i + 1, j, 1);
     const double sxe = e0 + B - c0;
     const double sy = e1 - c1;
-    double eta = fabs(FC(t.FCE, t, i, j, 0) - c0) / sxe;
+    double eta = dv(fabs(FC(t.FCE, t, i, j, 0) - c0), sxe);
     if (eta >= 1.0) eta = 0.5;
     const double xf = (1.0 - eta) * c0 + eta * (e0 + B);
     const double yf = (1.0 - eta) * c1 + eta * e1;
@@ -311,8 +376,8 @@ __global__ void k_ncf_east(Fam t, const double* bdx, int iu) {
       const double f0 = FC(t.FCE, t, i, j, 0), f1 = FC(t.FCE, t, i, j, 1);
       const double fcd = 0.5 * (fabs(f0 * t.nxS[a] + f1 * t.nyS[a] + t.phiS[a]) +
                                 fabs((f0 - B) * t.nxS[b] + f1 * t.nyS[b] + t.phiS[b]));
-      al = fabs(fcd) / fabs(ipd);
-      dal = sy * nyf / (sxe * fabs(ipd));
+      al = dv(fabs(fcd), fabs(ipd));
+      dal = dv(sy * nyf, sxe * fabs(ipd));
       if (fabs(ipd) < 1.0e-5) {
         dal = 0.0;
         al = 1.0;
@@ -351,7 +416,7 @@ __global__ void k_ncf_north(Fam t, const double* bdy, int iv) {
     const double n0 = C2(t.cent, t, i, j + 1, 0), n1 = C2(t.cent, t, i, j + 1, 1);
     const double syn = n1 + B - c1;
     const double sx = n0 - c0;
-    double eta = fabs(FC(t.FCN, t, i, j, 1) - c1) / syn;
+    double eta = dv(fabs(FC(t.FCN, t, i, j, 1) - c1), syn);
     if (eta >= 1.0) eta = 0.5;
     const double xf = (1.0 - eta) * c0 + eta * n0;
     const double yf = (1.0 - eta) * c1 + eta * (n1 + B);
@@ -364,8 +429,8 @@ __global__ void k_ncf_north(Fam t, const double* bdy, int iv) {
       const double f0 = FC(t.FCN, t, i, j, 0), f1 = FC(t.FCN, t, i, j, 1);
       const double fcd = 0.5 * (fabs(f0 * t.nxS[a] + f1 * t.nyS[a] + t.phiS[a]) +
                                 fabs(f0 * t.nxS[b] + (f1 - B) * t.nyS[b] + t.phiS[b]));
-      al = fabs(ipd) / fabs(fcd);
-      dal = sx * nxf / (syn * fabs(ipd));
+      al = dv(fabs(ipd), fabs(fcd));
+      dal = dv(sx * nxf, syn * fabs(ipd));
       if (fabs(ipd) < 1.0e-5) {
         dal = 0.0;
         al = 1.0;
@@ -405,6 +470,28 @@ __global__ void k_ncf_north_ghost(Fam t) {
 
 dim3 cells(int nx, int ny) { return dim3((nx + 31) / 32, (ny + 7) / 8); }
 
+// Device work arena kept between calls (allocating and mapping some GB of
+// device memory costs more than the whole computation), one per device,
+// grown on demand; calls are serialised by arena_lock.
+std::mutex arena_lock;
+bool arena_get(int device, size_t bytes, char** p) {
+  static char* buf[16] = {};
+  static size_t cap[16] = {};
+  const int d = device & 15;
+  if (cap[d] < bytes) {
+    if (buf[d]) cudaFree(buf[d]);
+    buf[d] = nullptr;
+    cap[d] = 0;
+    if (cudaMalloc(&buf[d], bytes) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return false;
+    }
+    cap[d] = bytes;
+  }
+  *p = buf[d];
+  return true;
+}
+
 }  // namespace
 }  // namespace scf
 
@@ -426,6 +513,7 @@ extern "C" int scf_grid_preprocess(int nx, int ny, const scf_cell_grid grid[3],
   const cudaMemcpyKind out_kind = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
   const size_t n1 = (size_t)nx * ny, n0 = (size_t)(nx + 2) * (ny + 2);
   int rc = SCF_OK;
+  bool locked = false;
   cudaStream_t s = nullptr;
   char* arena = nullptr;
   uint8_t *st0 = nullptr, *st1 = nullptr;
@@ -440,7 +528,10 @@ extern "C" int scf_grid_preprocess(int nx, int ny, const scf_cell_grid grid[3],
   const size_t per = dbl * 8 + ints * 4 + 256;
   if (cudaSetDevice(device) != cudaSuccess) return SCF_ERR_CUDA;
   if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return SCF_ERR_CUDA;
-  if (cudaMalloc(&arena, 3 * per) != cudaSuccess) {
+  // the work arena is kept for the next step (one per device, grown on demand)
+  arena_lock.lock();
+  locked = true;
+  if (!arena_get(device, 3 * per, &arena)) {
     rc = SCF_ERR_NOMEM;
     goto done;
   }
@@ -507,9 +598,9 @@ extern "C" int scf_grid_preprocess(int nx, int ny, const scf_cell_grid grid[3],
     CKC(cudaGetLastError());
     // the P family's apertures, WlLh, rules, corner rule, exchange cells and
     // the three numberings (scf_geom.cu); its face centres are the ones above
-    if (cudaMalloc(&st0, n0) != cudaSuccess || cudaMalloc(&st1, n0) != cudaSuccess ||
-        cudaMalloc(&counts, geometry_count_ints(nx) * 4) != cudaSuccess ||
-        cudaMalloc(&flag, 4) != cudaSuccess || cudaMallocHost(&flag_host, 4) != cudaSuccess) {
+    if (cudaMallocAsync(&st0, n0, s) != cudaSuccess || cudaMallocAsync(&st1, n0, s) != cudaSuccess ||
+        cudaMallocAsync(&counts, geometry_count_ints(nx) * 4, s) != cudaSuccess ||
+        cudaMallocAsync(&flag, 4, s) != cudaSuccess || cudaMallocHost(&flag_host, 4) != cudaSuccess) {
       rc = SCF_ERR_NOMEM;
       goto done;
     }
@@ -575,14 +666,14 @@ extern "C" int scf_grid_preprocess(int nx, int ny, const scf_cell_grid grid[3],
   }
   CKC(cudaStreamSynchronize(s));
 done:
+  if (st0) cudaFreeAsync(st0, s);
+  if (st1) cudaFreeAsync(st1, s);
+  if (counts) cudaFreeAsync(counts, s);
+  if (flag) cudaFreeAsync(flag, s);
   if (s) cudaStreamSynchronize(s);
-  if (arena) cudaFree(arena);
-  if (st0) cudaFree(st0);
-  if (st1) cudaFree(st1);
-  if (counts) cudaFree(counts);
-  if (flag) cudaFree(flag);
   if (flag_host) cudaFreeHost(flag_host);
   if (s) cudaStreamDestroy(s);
+  if (locked) arena_lock.unlock();
   if (ms)
     *ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return rc;

@@ -60,41 +60,66 @@ def _shape(kind, nx, ny):
     return {"1": (nx, ny), "0": (nx + 2, ny + 2), "c": (nx, ny, 2), "f": (nx + 2, ny + 2, 2)}[kind]
 
 
-def _host(a, shape, name):
+def _arr(a, shape, name, dev):
+    if dev:
+        import torch
+        if not (isinstance(a, torch.Tensor) and a.is_cuda and a.is_contiguous()
+                and a.dtype == torch.float64 and a.numel() == int(np.prod(shape))):
+            raise ValueError(f"{name}: expected a contiguous CUDA float64 tensor of "
+                             f"{int(np.prod(shape))} elements")
+        return a, a.data_ptr()
     a = np.asarray(a)
     if a.shape != shape or a.dtype != np.float64 or not a.flags["F_CONTIGUOUS"]:
         raise ValueError(f"{name}: expected a Fortran-ordered float64{shape}")
-    return a
+    return a, a.ctypes.data
 
 
 def grid_preprocess(grids: dict, fams: dict, icorprob: bool = True, state: dict | None = None,
-                    device: int = 0):
-    """Grid_Preprocess + NewCellFace on the GPU; returns ({f: outputs}, ms)."""
-    nx, ny = grids["p"]["dx"].shape
+                    device: int = 0, nx: int | None = None, ny: int | None = None):
+    """Grid_Preprocess + NewCellFace on the GPU; returns ({f: outputs}, ms).
+    With CUDA torch tensors as inputs (flat, Fortran element order; give nx
+    and ny) everything stays on the device and the outputs are CUDA tensors
+    with the same element counts as the Fortran arrays."""
+    import importlib
+    dev = not isinstance(grids["p"]["dx"], np.ndarray)
+    if not dev:
+        nx, ny = grids["p"]["dx"].shape
+    elif nx is None or ny is None:
+        raise ValueError("device inputs need nx and ny")
+    torch = importlib.import_module("torch") if dev else None
     G = (CellGrid * 3)()
     S = (CellSolid * 3)()
     O = (CellGeom * 3)()
     keep, out = [], {}
     for k, f in enumerate(FAMILIES):
         for n in GRID:
-            a = _host(grids[f][n], (nx, ny), f"{f}.{n}")
+            a, ptr = _arr(grids[f][n], (nx, ny), f"{f}.{n}", dev)
             keep.append(a)
-            setattr(G[k], n, a.ctypes.data)
+            setattr(G[k], n, ptr)
         for n in SOLID:
-            a = _host(fams[f][n], (nx, ny), f"{f}.{n}")
+            a, ptr = _arr(fams[f][n], (nx, ny), f"{f}.{n}", dev)
             keep.append(a)
-            setattr(S[k], n, a.ctypes.data)
+            setattr(S[k], n, ptr)
         out[f] = {}
         for n, kind, dt in GEOM:
             if f == "p" and n in UV_ONLY:
                 continue
             shape = _shape(kind, nx, ny)
-            a = np.zeros(shape, dtype=np.float64 if dt == "d" else np.int32, order="F")
-            if state and f in state and n in INOUT and n in state[f]:
-                a[...] = state[f][n]
+            if dev:
+                a = torch.zeros(int(np.prod(shape)),
+                                dtype=torch.float64 if dt == "d" else torch.int32,
+                                device=grids["p"]["dx"].device)
+                if state and f in state and n in INOUT and n in state[f]:
+                    a.copy_(state[f][n])
+                ptr = a.data_ptr()
+            else:
+                a = np.zeros(shape, dtype=np.float64 if dt == "d" else np.int32, order="F")
+                if state and f in state and n in INOUT and n in state[f]:
+                    a[...] = state[f][n]
+                ptr = a.ctypes.data
             out[f][n] = a
-            setattr(O[k], n, a.ctypes.data)
+            setattr(O[k], n, ptr)
     ms = C.c_double(0.0)
-    P._check(load().scf_grid_preprocess(nx, ny, G, S, O, 1 if icorprob else 0, 0, device,
-                                        C.byref(ms)), "scf_grid_preprocess")
+    P._check(load().scf_grid_preprocess(nx, ny, G, S, O, 1 if icorprob else 0, 1 if dev else 0,
+                                        device, C.byref(ms)), "scf_grid_preprocess")
     return out, ms.value

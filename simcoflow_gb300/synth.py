@@ -297,3 +297,80 @@ def momentum_inputs(case: Case, comp: str, rey: float = 1.0e5, seed: int = 0) ->
             "Dp": (A["DpU"] if comp == "u" else A["DpV"]).copy(order="F"),
             "dt": case.dt, "beta_vis": BETA_VIS, "nua": NU_A, "nuw": NU_W, "nuref": NU_W,
             "rey": rey, "fr": 1.0 / np.sqrt(9.81)}
+
+
+# ---------------------------------------------------------------------------
+# Inputs of the three cell families' cut-cell geometry (scf_grid_preprocess)
+# ---------------------------------------------------------------------------
+def frac_v(a, b, p, dx, dy):
+    """frac (src/Clsvof_Mod.f90:1371-1404) on arrays: the solid fraction of
+    a cell under the linear level set a x + b y + p."""
+    with np.errstate(all="ignore"):
+        tnx, tny = np.abs(a), np.abs(b)
+        h = 0.5 * (tnx * dx + tny * dy)
+        xx = (0.5 * tny * dy - p) / dx / tnx + 0.5
+        yy = (0.5 * tnx * dx - p) / dy / tny + 0.5
+        top = np.where(yy > 1.0, ((yy - 1.0) / yy) ** 2.0, 0.0)
+        right = np.where(xx > 1.0, ((xx - 1.0) / xx) ** 2.0, 0.0)
+        gen = 0.5 * xx * yy * (1.0 - top - right)
+        v = np.where(tny <= 1e-20, 0.5 - p / dx, gen)
+        v = np.where(tnx <= 1e-20, 0.5 - p / dy, v)
+        v = np.where(p - h >= 0.0, 0.0, v)
+        v = np.where(p + h <= 0.0, 1.0, v)
+    v = np.where(v < 1e-14, 0.0, v)
+    return np.where(v >= 1.0 - 1e-14, 1.0, v)
+
+
+def circles_levelset(circles, x, y):
+    """Distance to the nearest circle and its outward normal at (x, y)."""
+    best = np.full(x.shape, 1e30), np.zeros(x.shape), np.ones(x.shape)
+    for cx, cy, r in circles:
+        dx, dy = x - cx, y - cy
+        d = np.sqrt(dx * dx + dy * dy)
+        ph, a, b = d - r, dx / d, dy / d
+        m = ph < best[0]
+        best = tuple(np.where(m, c, o) for c, o in zip((ph, a, b), best))
+    return best
+
+
+def family_grids(xf, yf):
+    """P, U and V grids (x, y, dx, dy; (nx,ny), Fortran order) from the node
+    coordinates, by Mesh_Mod's formulas (src/Mesh_Mod.f90:120-175)."""
+    F = np.asfortranarray
+    xf, yf = np.asarray(xf, dtype=float), np.asarray(yf, dtype=float)
+    xc, yc = 0.5 * (xf[1:] + xf[:-1]), 0.5 * (yf[1:] + yf[:-1])
+    X, Y = np.meshgrid(xc, yc, indexing="ij")
+    DX, DY = np.meshgrid(xf[1:] - xf[:-1], yf[1:] - yf[:-1], indexing="ij")
+    p = {"x": F(X), "y": F(Y), "dx": F(DX), "dy": F(DY)}
+    dxu = DX.copy()
+    dxu[:-1, :] = X[1:, :] - X[:-1, :]
+    u = {"x": F(X + 0.5 * DX), "y": F(Y.copy()), "dx": F(dxu), "dy": F(DY.copy())}
+    dyv = DY.copy()
+    dyv[:, :-1] = Y[:, 1:] - Y[:, :-1]
+    v = {"x": F(X.copy()), "y": F(Y + 0.5 * DY), "dx": F(DX.copy()), "dy": F(dyv)}
+    return {"p": p, "u": u, "v": v}
+
+
+def family_fields(grids, circles):
+    """The solid level-set fields (vofS, phiS, nxS, nyS) of each family for
+    circular bodies: the level set linearised at the cell centre, the solid
+    fraction by frac."""
+    F = np.asfortranarray
+    out = {}
+    for f, g in grids.items():
+        ph, a, b = circles_levelset(circles, g["x"], g["y"])
+        out[f] = {"vofS": F(frac_v(a, b, ph, g["dx"], g["dy"])), "phiS": F(ph), "nxS": F(a),
+                  "nyS": F(b)}
+    return out
+
+
+def cutcell_inputs(case: Case):
+    """(grids, fields) of the three cell families for a case with circular
+    bodies (c1, c2, c4, c5 and random instances)."""
+    circles = []
+    for s in case.meta["solids"]:
+        if s.kind != G.SOLID_CIRCLE:
+            raise ValueError("cutcell_inputs: circular bodies only")
+        circles.append((s.cx, s.cy, s.r))
+    grids = family_grids(case.meta["xf"], case.meta["yf"])
+    return grids, family_fields(grids, circles)

@@ -97,3 +97,29 @@ def test_argument_errors(cuda):
     grids["u"]["dx"] = np.zeros((8, 9), order="F")
     with pytest.raises(ValueError):
         CU.grid_preprocess(grids, fams)
+
+
+def test_device_pointers_match_host(cuda):
+    import torch
+    nx, ny = 37, 33
+    grids, fams = CC.case(nx, ny, CC.CIRCLES, stretch=0.2, seed=8)
+    host, _ = CU.grid_preprocess(grids, fams)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a.ravel(order="F"))).cuda()
+    dev, _ = CU.grid_preprocess({f: {k: T(v) for k, v in g.items()} for f, g in grids.items()},
+                                {f: {k: T(v) for k, v in g.items()} for f, g in fams.items()},
+                                nx=nx, ny=ny)
+    for f in ("p", "u", "v"):
+        for k, a in host[f].items():
+            b = dev[f][k].cpu().numpy()
+            assert np.array_equal(np.asarray(a).ravel(order="F").view(np.uint8),
+                                  b.view(np.uint8)), (f, k)
+
+
+def test_headline_grid_family_inputs(cuda, oracle):
+    """synth.cutcell_inputs on a small circles case: GPU equals the literal."""
+    from simcoflow_gb300 import synth
+    c = synth.c2(n=48)
+    grids, fams = synth.cutcell_inputs(c)
+    got, _ = CU.grid_preprocess(grids, fams)
+    lit = oracle.grid_preprocess_literal(c.nx, c.ny, grids, fams)
+    compare(got, lit)
