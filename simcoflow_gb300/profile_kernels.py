@@ -14,6 +14,10 @@ profiler can restrict itself to that range (ncu --nvtx --nvtx-include
             the path
   unet      --reps forward passes of the learned preconditioner's network on
             the workload's operator and right-hand side (shipped weights)
+  cutcell   --reps GPU builds of the P, U and V cells' cut-cell geometry
+            (scf_grid_preprocess) from the workload's circles, device-resident
+  tecplot   --reps formattings of the P-cell Tecplot records into a device
+            buffer (scf_tecplot_format)
   momentum  --reps pairs of momentum-predictor solves (u then v) on the
             workload's cells (seeded face fluxes), device-resident
   geometry  --reps GPU builds of the cut-cell geometry (scf_proj_set_solid)
@@ -40,7 +44,8 @@ KERNELS = {"sweep": (0, {"fp64": 48, "mixed": 20}), "pupdate_spmv": (1, {"fp64":
            "prolong": (4, {"fp64": 50, "mixed": 21}), "assemble": (5, {"fp64": 200, "mixed": 200}),
            "vcycle": (6, {"fp64": 0, "mixed": 0}), "setup": (7, {"fp64": 0, "mixed": 0}),
            "projection": (None, {"fp64": 0, "mixed": 0}), "unet": (None, {"fp64": 0, "mixed": 0}),
-           "momentum": (None, {"fp64": 0, "mixed": 0}), "geometry": (None, {"fp64": 0, "mixed": 0})}
+           "momentum": (None, {"fp64": 0, "mixed": 0}), "geometry": (None, {"fp64": 0, "mixed": 0}),
+           "cutcell": (None, {"fp64": 0, "mixed": 0}), "tecplot": (None, {"fp64": 0, "mixed": 0})}
 
 
 def main():
@@ -72,6 +77,47 @@ def main():
         gs.close()
         print(json.dumps({"config": args.config, "kernel": "geometry", "nx": c.nx, "ny": c.ny,
                           "ms_set_solid": dt_ms}))
+        return
+    if args.kernel == "cutcell":
+        from . import cutcell as CU
+        grids, fams = synth.cutcell_inputs(c)
+        T = lambda x: torch.from_numpy(np.ascontiguousarray(x.ravel(order="F"))).to(dev)
+        tg = {f: {k: T(v) for k, v in g.items()} for f, g in grids.items()}
+        tf = {f: {k: T(v) for k, v in g.items()} for f, g in fams.items()}
+        CU.grid_preprocess(tg, tf, nx=c.nx, ny=c.ny)  # warm-up
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("kernels")
+        t0 = time.perf_counter()
+        for _ in range(args.reps):
+            CU.grid_preprocess(tg, tf, nx=c.nx, ny=c.ny)
+        torch.cuda.synchronize()
+        dt_ms = (time.perf_counter() - t0) / args.reps * 1e3
+        torch.cuda.nvtx.range_pop()
+        print(json.dumps({"config": args.config, "kernel": "cutcell", "nx": c.nx, "ny": c.ny,
+                          "ms_grid_preprocess": dt_ms}))
+        return
+    if args.kernel == "tecplot":
+        from . import output as Out
+        rng = np.random.default_rng(17)
+        f = {"x": t["x"], "y": t["y"], "p": t["ustar"], "u": t["u0"], "v": t["v0"],
+             "phi": t["phi"], "vof": t["vof"], "phiS": t["phiS"], "vofS": t["vofS"],
+             "mres": t["x"], "flux": torch.from_numpy(rng.standard_normal(
+                 2 * (c.nx + 2) * (c.ny + 2))).to(dev), "nxS": t["nxS"], "nyS": t["nyS"]}
+        body = torch.empty(15 * c.nx * c.ny * 25, dtype=torch.uint8, device=dev)
+        st = torch.cuda.current_stream()
+        Out.format_device("p", c.nx, c.ny, f, body, st.cuda_stream)  # warm-up
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("kernels")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(args.reps):
+            Out.format_device("p", c.nx, c.ny, f, body, st.cuda_stream)
+        e1.record(st)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        ms = e0.elapsed_time(e1) / args.reps
+        print(json.dumps({"config": args.config, "kernel": "tecplot", "nx": c.nx, "ny": c.ny,
+                          "ms_format": ms, "text_GBps": 15 * c.nx * c.ny * 25 / (ms * 1e-3) / 1e9}))
         return
     if args.kernel == "momentum":
         from . import momentum as M
