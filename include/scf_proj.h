@@ -149,7 +149,7 @@ int scf_batch_run(scf_batch *b, void *stream, struct scf_stats *stats);
 int scf_batch_destroy(scf_batch *b);
 
 /* Fill opts with defaults: FP64, host pointers, device 0, maxit 200,
- * rtol 1e-8, 2 pre / 2 post sweeps, omega 1.9, coarse_max 16. */
+ * rtol 1e-8, 2 pre / 2 post sweeps, omega 1.9, coarse_max 64. */
 void scf_opts_default(scf_opts *opts);
 
 /* Create a solver for an nx-by-ny pressure grid (Isize, Jsize).  Allocates

@@ -205,7 +205,7 @@ def symmetric_operator(case, matr):
 SMOOTHERS = {"point": 0, "line": 1}
 
 
-def mgpcg(case, matr, rhm, rtol=1e-13, maxit=500, npre=2, npost=2, omega=1.9, coarse_max=16,
+def mgpcg(case, matr, rhm, rtol=1e-13, maxit=500, npre=2, npost=2, omega=1.9, coarse_max=64,
           threads=0, smoother="point"):
     """CPU FP64 MG-PCG on the symmetric operator.  Returns (Pp-interior x as
     (nx,ny) Fortran array, iterations, true relres, levels).  smoother:
@@ -225,7 +225,7 @@ def mgpcg(case, matr, rhm, rtol=1e-13, maxit=500, npre=2, npost=2, omega=1.9, co
     return np.asfortranarray(x.reshape(ny, nx).T), it, rel.value, nlev.value
 
 
-def vcycle(case, matr, b_f, npre=2, npost=2, omega=1.9, coarse_max=16,
+def vcycle(case, matr, b_f, npre=2, npost=2, omega=1.9, coarse_max=64,
            smoother="point") -> np.ndarray:
     nx, ny = case.nx, case.ny
     cE, cN, dg = symmetric_operator(case, matr)

@@ -888,7 +888,7 @@ void scf_opts_default(scf_opts* o) {
   o->npre = 2;
   o->npost = 2;
   o->omega = 1.9;
-  o->coarse_max = 16;
+  o->coarse_max = 64;
   o->smoother = SCF_SMOOTH_AUTO;
 }
 

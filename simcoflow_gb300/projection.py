@@ -148,7 +148,7 @@ class ProjectionSolver:
     def __init__(self, nx: int, ny: int, precision: str = "fp64", device: int = 0,
                  device_ptrs: bool = False, use_graph: bool = True, maxit: int = 200,
                  rtol: float = 1e-8, npre: int = 2, npost: int = 2, omega: float = 1.9,
-                 coarse_max: int = 16, smoother: str = "auto", precond: str = "mg"):
+                 coarse_max: int = 64, smoother: str = "auto", precond: str = "mg"):
         L = load()
         o = Opts()
         L.scf_opts_default(C.byref(o))

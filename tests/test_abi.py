@@ -72,7 +72,7 @@ def test_host_only_entry_points(built):
     assert b"NaN" in L.scf_strerror(-3)
     o = projection.Opts()
     L.scf_opts_default(ctypes.byref(o))
-    assert o.maxit == 200 and o.rtol == 1e-8 and o.coarse_max == 16
+    assert o.maxit == 200 and o.rtol == 1e-8 and o.coarse_max == 64
     # argument checks happen before any CUDA call
     h = ctypes.c_void_p()
     assert L.scf_proj_create(ctypes.byref(h), 1, 5, ctypes.byref(o)) == -1
