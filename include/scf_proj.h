@@ -173,7 +173,11 @@ int scf_proj_set_grid(scf_proj *h, const double *dx, const double *dy, const dou
  *   posnu_p                           PCell%Posnu, (nx+2,ny+2)
  *   posnu_u, posnu_v                  UCell%Posnu, VCell%Posnu, (nx+2,ny+2)
  *   moex_u, moex_v                    UCell%MoExCell, VCell%MoExCell, (nx,ny)
- *   vofS_u, vofS_v                    UCell%vofS, VCell%vofS, (nx,ny) */
+ *   vofS_u, vofS_v                    UCell%vofS, VCell%vofS, (nx,ny)
+ * Host mode: the six U/V arrays are read only by the velocity correction, so
+ * their copies are made by the next scf_proj_poisson_solve / update_puv
+ * while its PCG runs; those six host arrays must stay unchanged until that
+ * call returns (the others may be reused once this call returns). */
 int scf_proj_set_geometry(scf_proj *h, const double *vof, const double *phi,
                           const double *vofS, const double *nyS, const double *WlLh,
                           const double *aE, const double *aW, const double *aN,

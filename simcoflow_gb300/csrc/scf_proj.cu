@@ -38,6 +38,15 @@ struct scf_proj {
   // operator setup still running on `stream`
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t copy_done = nullptr;
+  cudaEvent_t late_done = nullptr;  // the copies only the correction reads
+  // host mode: set_geometry's U/V arrays (read by the correction only), copied
+  // by the next solve on the copy stream while the PCG runs
+  struct Late {
+    void* dst;
+    const void* src;
+    size_t bytes;
+  } late[6] = {};
+  bool late_pending = false;
   bool devptrs = false;
   bool mixed = false;
 
@@ -795,23 +804,31 @@ int solve_common(scf_proj* h, const double* ustar, const double* vstar, double v
   CK(cudaEventRecord(h->ev[0], cs));
   const double *dus = ustar, *dvs = vstar;
   double *dPp = Pp, *dp = p, *du = u, *dv = v, *dm = mres;
+  bool late = false;  // copies that only the correction waits for
   if (!h->devptrs) {
     CK(cudaMemcpyAsync(h->st_us, ustar, n0 * 8, cudaMemcpyHostToDevice, cs));
     CK(cudaMemcpyAsync(h->st_vs, vstar, n0 * 8, cudaMemcpyHostToDevice, cs));
     dus = h->st_us; dvs = h->st_vs;
     dPp = Pp ? h->st_Pp : nullptr;
+    CK(cudaEventRecord(h->copy_done, cs));
+    CK(cudaStreamWaitEvent(s, h->copy_done, 0));
+    // the rest is read by the correction only: these copies run during the solve
     if (correct) {
       CK(cudaMemcpyAsync(h->st_p, p, n0 * 8, cudaMemcpyHostToDevice, cs));
       CK(cudaMemcpyAsync(h->st_u, u, n0 * 8, cudaMemcpyHostToDevice, cs));
       CK(cudaMemcpyAsync(h->st_v, v, n0 * 8, cudaMemcpyHostToDevice, cs));
       dp = h->st_p; du = h->st_u; dv = h->st_v; dm = h->st_mres;
+      late = true;
     }
+    if (h->late_pending) {
+      for (const auto& e : h->late)
+        CK(cudaMemcpyAsync(e.dst, e.src, e.bytes, cudaMemcpyHostToDevice, cs));
+      h->late_pending = false;
+      late = true;
+    }
+    if (late) CK(cudaEventRecord(h->late_done, cs));
   }
   CK(cudaEventRecord(h->ev[1], cs));
-  if (cs != s) {
-    CK(cudaEventRecord(h->copy_done, cs));
-    CK(cudaStreamWaitEvent(s, h->copy_done, 0));
-  }
   LevelView L0 = h->lev[0];
   // the NaN flag of a previous solve must not leak into this one
   CK(cudaMemsetAsync(&h->sc->nan, 0, sizeof(int), s));
@@ -822,6 +839,7 @@ int solve_common(scf_proj* h, const double* ustar, const double* vstar, double v
   int rc = learned(h) ? run_learned(h, &nn_iters, &fell_back) : run_pcg(h);
   if (rc) return rc;
   CK(cudaEventRecord(h->ev[2], s));
+  if (late) CK(cudaStreamWaitEvent(s, h->late_done, 0));
   launch_final_solution(h->fin, L0, h->xsol, h->bvec, dus, dvs, dPp, dp, du, dv, correct ? 1 : 0,
                         h->sc, h->part, s);
   if (correct) {
@@ -967,7 +985,8 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
     return fail(SCF_ERR_CUDA);
   h->own_stream = true;
   if (cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&h->copy_done, cudaEventDisableTiming) != cudaSuccess)
+      cudaEventCreateWithFlags(&h->copy_done, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->late_done, cudaEventDisableTiming) != cudaSuccess)
     return fail(SCF_ERR_CUDA);
   for (auto& e : h->ev)
     if (cudaEventCreate(&e) != cudaSuccess) return fail(SCF_ERR_CUDA);
@@ -1132,6 +1151,7 @@ int scf_proj_destroy(scf_proj* h) {
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   if (h->copy_done) cudaEventDestroy(h->copy_done);
+  if (h->late_done) cudaEventDestroy(h->late_done);
   delete h;
   return SCF_OK;
 }
@@ -1195,11 +1215,23 @@ int scf_proj_set_geometry(scf_proj* h, const double* vof, const double* phi, con
       (rc = put(h, &h->st_vofS, vofS, n1)) || (rc = put(h, &h->st_nyS, nyS, n1)) ||
       (rc = put(h, &h->st_WlLh, WlLh, n1)) || (rc = put(h, &h->st_aE, aE, n0)) ||
       (rc = put(h, &h->st_aW, aW, n0)) || (rc = put(h, &h->st_aN, aN, n0)) ||
-      (rc = put(h, &h->st_aS, aS, n0)) || (rc = put(h, &h->st_pp, posnu_p, n0)) ||
-      (rc = put(h, &h->st_pu, posnu_u, n0)) || (rc = put(h, &h->st_mu, moex_u, n1)) ||
-      (rc = put(h, &h->st_vsu, vofS_u, n1)) || (rc = put(h, &h->st_pv, posnu_v, n0)) ||
-      (rc = put(h, &h->st_mv, moex_v, n1)) || (rc = put(h, &h->st_vsv, vofS_v, n1)))
+      (rc = put(h, &h->st_aS, aS, n0)) || (rc = put(h, &h->st_pp, posnu_p, n0)))
     return rc;
+  if (!posnu_u || !moex_u || !vofS_u || !posnu_v || !moex_v || !vofS_v) return SCF_ERR_ARG;
+  if (h->devptrs) {
+    h->st_pu = const_cast<int32_t*>(posnu_u); h->st_mu = const_cast<int32_t*>(moex_u);
+    h->st_vsu = const_cast<double*>(vofS_u); h->st_pv = const_cast<int32_t*>(posnu_v);
+    h->st_mv = const_cast<int32_t*>(moex_v); h->st_vsv = const_cast<double*>(vofS_v);
+  } else {
+    // read by the correction only: copied by the next solve, during its PCG
+    h->late[0] = {h->st_pu, posnu_u, n0 * 4};
+    h->late[1] = {h->st_mu, moex_u, n1 * 4};
+    h->late[2] = {h->st_vsu, vofS_u, n1 * 8};
+    h->late[3] = {h->st_pv, posnu_v, n0 * 4};
+    h->late[4] = {h->st_mv, moex_v, n1 * 4};
+    h->late[5] = {h->st_vsv, vofS_v, n1 * 8};
+    h->late_pending = true;
+  }
   FortranIn& f = h->fin;
   f.vof = h->st_vof; f.phi = h->st_phi; f.vofS = h->st_vofS; f.nyS = h->st_nyS;
   f.WlLh = h->st_WlLh; f.aE = h->st_aE; f.aW = h->st_aW; f.aN = h->st_aN; f.aS = h->st_aS;
@@ -1307,6 +1339,7 @@ int scf_proj_set_solid(scf_proj* h, const double* vof, const double* phi, const 
   f.posnu_p = h->g_pp; f.posnu_u = h->g_pu; f.posnu_v = h->g_pv;
   f.moex_u = h->g_mu; f.moex_v = h->g_mv; f.vofS_u = h->g_vsu; f.vofS_v = h->g_vsv;
   CK(cudaStreamSynchronize(h->stream));
+  h->late_pending = false;  // the U/V arrays now come from the GPU geometry
   h->have_geom = true;
   h->assembled = false;
   return SCF_OK;
@@ -1319,6 +1352,11 @@ int scf_proj_get_geometry(scf_proj* h, double* vofS, double* nxS, double* nyS, d
   if (!h) return SCF_ERR_ARG;
   if (!h->have_geom) return SCF_ERR_STATE;
   CK(cudaSetDevice(h->device));
+  if (h->late_pending) {  // U/V arrays not copied yet: copy them now
+    for (const auto& e : h->late)
+      CK(cudaMemcpyAsync(e.dst, e.src, e.bytes, cudaMemcpyHostToDevice, h->stream));
+    h->late_pending = false;
+  }
   const FortranIn& f = h->fin;
   const size_t n1 = (size_t)h->nx * h->ny, n0 = (size_t)(h->nx + 2) * (h->ny + 2);
   const bool own = f.vofS == h->g_vofS && h->geo_alloc;
