@@ -152,8 +152,8 @@ WORKLOADS = {
     "c3": "4096x4096 y-stretched grid, rotated plate, density 1000:1.2 (plain FP64 MG-PCG)",
 }
 
-# compulsory bytes per fine cell of each measured kernel, per precision
-# (kernel table).  sweep = one red-black iteration (both colours)
+# compulsory bytes per fine cell of each measured kernel, per precision:
+# sweep = one red-black iteration (both colours)
 # in one pass; resid_restrict = sweep + residual + 2x2 restriction;
 # prolong = prolongation fused into a sweep.
 KERNEL_BYTES = {
