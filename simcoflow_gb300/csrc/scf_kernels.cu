@@ -816,17 +816,37 @@ void launch_rhs_given(int nx, int ny, const double* bF, LevelView L0, double* bv
   launch_k(k_rhs_given, grid_for(nx, ny, 1), kBlock, 0, s, nx, ny, bF, L0, bvec, r, r32, x, sc,
            part, rtol, maxit);
 }
+// Grid of the x/r update: one wave of resident CTAs (grid-stride rows), so
+// that every thread walks nearly the same number of rows and no partly
+// filled second wave follows.
+template <class PT>
+dim3 xr_grid(int nx, int ny) {
+  static int per[16];  // resident CTAs per SM, per device (0 = unknown)
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int& c = per[dev & 15];
+  if (c == 0) {
+    int sms = 0, n = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_update_xr<PT>, kThreads, 0);
+    c = sms * n > 0 ? sms * n : 1;
+  }
+  const dim3 g = grid_for(nx, ny);
+  const int gy = c / (int)g.x > 1 ? c / (int)g.x : 1;
+  return dim3(g.x, gy < (int)g.y ? gy : g.y);
+}
+
 void launch_update_xr(LevelView L0, double* x, const double* p, double* r, float* r32,
                       const float* z32, const double* q, Scalars* sc, double* part,
                       unsigned long long cond, cudaStream_t s) {
-  launch_k(k_update_xr<double>, grid_for(L0.nx, L0.ny), kBlock, 0, s, L0, x, p, r, r32, z32, q, sc,
-           part, cond);
+  launch_k(k_update_xr<double>, xr_grid<double>(L0.nx, L0.ny), kBlock, 0, s, L0, x, p, r, r32,
+           z32, q, sc, part, cond);
 }
 void launch_update_xr(LevelView L0, double* x, const float* p, double* r, float* r32,
                       const float* z32, const double* q, Scalars* sc, double* part,
                       unsigned long long cond, cudaStream_t s) {
-  launch_k(k_update_xr<float>, grid_for(L0.nx, L0.ny), kBlock, 0, s, L0, x, p, r, r32, z32, q, sc,
-           part, cond);
+  launch_k(k_update_xr<float>, xr_grid<float>(L0.nx, L0.ny), kBlock, 0, s, L0, x, p, r, r32,
+           z32, q, sc, part, cond);
 }
 void launch_final_solution(const FortranIn& in, LevelView L0, const double* x,
                            const double* bvec, const double* ustar, const double* vstar,
