@@ -211,7 +211,7 @@ __device__ __forceinline__ double shfl_up_d(double v, int lane_delta) {
 // instead of repeating the two IEEE FP64 divisions: the same function of the
 // same bits.  Away from the interface every face qualifies, which halves the
 // divisions on GB300's slow FP64 pipe.
-__global__ void k_assemble(FortranIn in, LevelView L, Scalars* sc) {
+__global__ void __launch_bounds__(kThreads, 4) k_assemble(FortranIn in, LevelView L, Scalars* sc) {
   pdl_wait();
   const int nx = in.nx, ny = in.ny;
   const int ix = blockIdx.x * kBX + threadIdx.x;
@@ -640,7 +640,8 @@ __device__ __forceinline__ bool face_grad(int cs, int cn, double phis, double ph
   return true;
 }
 
-__global__ void k_final_solution(FortranIn in, LevelView L, const double* __restrict__ x,
+__global__ void __launch_bounds__(kThreads, 4)
+k_final_solution(FortranIn in, LevelView L, const double* __restrict__ x,
                                  const double* __restrict__ bvec, const double* __restrict__ us,
                                  const double* __restrict__ vs, double* Pp, double* p, double* u,
                                  double* v, int correct, Scalars* sc, double* part) {

@@ -120,7 +120,8 @@ __device__ __forceinline__ double rcp_newton(double x) {
 // SetMatrix + SetVectors for one cell per thread; also the Krylov start
 // x = 0, r = r^ = b, p = v = 0 and ||b||^2.  Dp is the Fortran (0:nx+1,
 // 0:ny+1) array, written for the assembled cells only.
-__global__ void k_mom_assemble(MomIn in, int iu, int iv, MomOp M, double* Dp, double* x,
+__global__ void __launch_bounds__(256, 3)
+k_mom_assemble(MomIn in, int iu, int iv, MomOp M, double* Dp, double* x,
                                double* r, double* rh, double* p0, double* v0, MomScalars* sc,
                                double* part) {
   pdl_wait();
