@@ -422,6 +422,76 @@ def extra_tecplot(case, local, args):
     return out
 
 
+def extra_vtr(case, local, args):
+    """Print_Result_VTK_2D's ParaView file of the headline workload (X, Y, Z
+    coordinates, the 3-component velocity, its two components and five
+    scalars: 10 nx*ny REAL(4) values) from device-resident fields: the text
+    into a host buffer and the file written to the box's temporary directory;
+    against the C restatement's formatting into a host buffer on all host
+    cores."""
+    import ctypes
+    import tempfile
+    import torch
+    from simcoflow_gb300 import output as Out
+    nx, ny = case.nx, case.ny
+    rng = np.random.default_rng(23)
+    F = lambda a: np.asfortranarray(np.asarray(a, dtype=np.float64))
+    A = case.arrays
+    f = {"x": A["x"], "y": A["y"], "u": A["u0"], "v": A["v0"],
+         "p": rng.standard_normal((nx + 2, ny + 2)), "phi": A["phi"],
+         "phiS": rng.standard_normal((nx, ny)), "vof": A["vof"], "vofS": A["vofS"]}
+    f = {k: F(v) for k, v in f.items()}
+    dev = torch.device("cuda", local)
+    tf = {k: torch.from_numpy(np.ascontiguousarray(v.ravel(order="F"))).to(dev)
+          for k, v in f.items()}
+    L = Out.load()
+    size = L.scf_vtr_size(nx, ny)
+    out = {"workload": f"ParaView VTR file of the {nx}x{ny} headline workload "
+                       f"({10 * nx * ny / 1e6:.1f} M REAL(4) values, {size / 1e9:.2f} GB of text)"}
+    st, keep = Out._pack(Out.VTR_FIELDS, Out.VtrFields, nx, ny, tf, True)
+    buf = ctypes.create_string_buffer(size)
+    n = ctypes.c_int64(0)
+
+    def text_once():
+        rc = L.scf_vtr_text(nx, ny, ctypes.byref(st), Out.DEVICE_PTRS, buf, size, ctypes.byref(n),
+                            local)
+        if rc != 0:
+            raise RuntimeError(f"scf_vtr_text {rc}")
+
+    for _ in range(2):
+        text_once()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        text_once()
+    ms_text = (time.perf_counter() - t0) / 3 * 1e3
+    with tempfile.TemporaryDirectory() as d:
+        os.makedirs(os.path.join(d, "Paraview"))
+        ms_file = min(Out.vtr_write(nx, ny, tf, 1, d + "/", device_ptrs=True, device=local)
+                      for _ in range(3))
+    out["gpu"] = {"ms_text_in_host_memory": round(ms_text, 2), "ms_file_write": round(ms_file, 2),
+                  "timing": "text: host clock around scf_vtr_text (literal records, one "
+                            "formatting kernel, pinned 16 MiB chunks, 4 copy threads); file: host "
+                            "clock around scf_vtr_write (one writer thread) into the temporary "
+                            "directory"}
+    if not args.no_cpu:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle as O
+        threads = os.cpu_count() or 1
+        O.lib().oracle_set_threads(threads)
+        cbuf = ctypes.create_string_buffer(size + 2048)
+        args_ = [O._p(f[k]) for k in O.VTR_FIELDS]
+        t0 = time.perf_counter()
+        m = O.lib().oracle_vtr(nx, ny, *args_, cbuf)
+        cpu_ms = (time.perf_counter() - t0) * 1e3
+        out["cpu"] = {"ms_text_in_host_memory": round(cpu_ms, 1), "cores": threads,
+                      "kind": "port", "sample": "the whole file text (C restatement, snprintf "
+                      "%.8E per value, OpenMP over values) into a host buffer"}
+        out["identical_to_oracle"] = bool(m == n.value and
+                                          ctypes.string_at(cbuf, m) == ctypes.string_at(buf, m))
+        out["speedup_text_vs_cpu"] = round(cpu_ms / ms_text, 1)
+    return out
+
+
 def extra_cutcell(case, local, args):
     """The per-step cut-cell geometry of the P, U and V cells
     (Grid_Preprocess + NewCellFace, scf_grid_preprocess) on the headline
@@ -732,6 +802,7 @@ def run_ours(args):
                          ("batch_64", lambda: extra_batch(local)),
                          ("momentum_2048", lambda: extra_momentum(case, local, args)),
                          ("tecplot_2048", lambda: extra_tecplot(case, local, args)),
+                         ("vtr_2048", lambda: extra_vtr(case, local, args)),
                          ("cutcell_2048", lambda: extra_cutcell(case, local, args))):
             try:
                 extras[name] = fn()

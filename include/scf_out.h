@@ -1,4 +1,5 @@
-/* scf_out.h -- Tecplot result files of SIMCOFlow written from the GPU.
+/* scf_out.h -- result files of SIMCOFlow written from the GPU: the Tecplot
+ * files and the ParaView (VTR) file.
  *
  * Replaces Print_Result_Tecplot_PCent / _UCent / _VCent
  * (src/PrintResult.f90:39-168): the same files, byte for byte, with the text
@@ -82,6 +83,40 @@ int scf_tecplot_format(int kind, int nx, int ny, const void *fields, char *dev_t
 /* Diagnostics: format n doubles (host arrays) as F24.14 into out (24*n
  * bytes, no line ends). */
 int scf_format_f24_14(const double *v, int64_t n, char *out, int device);
+
+/* ---- ParaView file: Print_Result_VTK_2D (src/PrintResult.f90:165-190)
+ * through VTR_open_file / VTR_write_mesh / VTR_write_var / VTR_close_file
+ * (src/VTR_mod.f90:79-379).  The XML records are the module's, byte for
+ * byte.  The values are REAL(4) (real(x, kind=4), round to nearest) in
+ * list-directed output, whose text the Fortran standard leaves to the
+ * compiler; this library writes each value as a blank and 15 characters
+ * (the sign or a blank, then the correctly rounded "%.8E" of the exact
+ * REAL(4) value: 9 significant digits, which read back to the same REAL(4);
+ * "NaN", "Infinity", "-Infinity" right-justified), five values per record. */
+typedef struct scf_vtr_fields {
+  const double *x, *y;              /* TGrid%x, %y (nx,ny): x(:,1), y(1,:) are written */
+  const double *u, *v, *p;          /* TVar%u, %v, %p (nx+2,ny+2): (1:nx,1:ny) written */
+  const double *phi, *phiS;         /* TCell%phi, %phiS (nx,ny) */
+  const double *vof, *vofS;         /* TCell%vof, %vofS (nx,ny) */
+} scf_vtr_fields;
+
+/* Bytes of the file for an nx-by-ny grid. */
+int64_t scf_vtr_size(int nx, int ny);
+
+/* The whole file text into buf (host memory, capacity cap; *len receives
+ * the size). */
+int scf_vtr_text(int nx, int ny, const scf_vtr_fields *fields, int flags, char *buf, int64_t cap,
+                 int64_t *len, int device);
+
+/* Write dir/Paraview/FlowField_<iter as %08d>.vtr (the reference's name; the
+ * Paraview/ directory must exist).  ms, when not NULL, receives the elapsed
+ * wall time. */
+int scf_vtr_write(int nx, int ny, const scf_vtr_fields *fields, int flags, int64_t iter,
+                  const char *dir, int device, double *ms);
+
+/* Diagnostics: the 15 characters of real(v[k], kind=4) for n doubles (host
+ * arrays) into out (15*n bytes, no separators). */
+int scf_format_e15_8(const double *v, int64_t n, char *out, int device);
 
 #ifdef __cplusplus
 }

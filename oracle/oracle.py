@@ -33,6 +33,9 @@ Pieces:
     tecplot_pcell / tecplot_vcell   Print_Result_Tecplot_PCent / _UCent /
                 _VCent                 src/PrintResult.f90:39-168
     f24_14      the "(f24.14)" number format
+    vtr         Print_Result_VTK_2D's ParaView file   src/PrintResult.f90:165-190,
+                src/VTR_mod.f90:79-379
+    e15_8       its list-directed REAL(4) value text (15 characters)
 """
 from __future__ import annotations
 
@@ -93,6 +96,9 @@ def lib():
         L.oracle_tecplot_pcell.argtypes = [C.c_int, C.c_int] + [_P] * 13 + [C.c_char_p]
         L.oracle_tecplot_vcell.restype = C.c_int64
         L.oracle_tecplot_vcell.argtypes = [C.c_int, C.c_int, C.c_int] + [_P] * 7 + [C.c_char_p]
+        L.oracle_format_e15_8.argtypes = [_P, C.c_int64, C.c_char_p]
+        L.oracle_vtr.restype = C.c_int64
+        L.oracle_vtr.argtypes = [C.c_int, C.c_int] + [_P] * 9 + [C.c_char_p]
         _lib = L
     return _lib
 
@@ -516,6 +522,29 @@ def tecplot_vcell(comp, nx, ny, f) -> bytes:
     """The text of Print_Result_Tecplot_UCent (comp 0) / _VCent (comp 1)."""
     buf = C.create_string_buffer(tecplot_size(8, nx, ny))
     n = lib().oracle_tecplot_vcell(comp, nx, ny, *[_p(f[k]) for k in VCELL_FIELDS], buf)
+    return buf.raw[:n]
+
+
+VTR_FIELDS = ["x", "y", "u", "v", "p", "phi", "phiS", "vof", "vofS"]
+
+
+def e15_8(values) -> bytes:
+    """The 15-character REAL(4) text of every value, no separators."""
+    v = np.ascontiguousarray(values, dtype=np.float64).ravel()
+    out = C.create_string_buffer(15 * v.size + 1)
+    lib().oracle_format_e15_8(v.ctypes.data_as(_P), v.size, out)
+    return out.raw[:15 * v.size]
+
+
+def vtr_size(nx, ny) -> int:
+    n = 10 * nx * ny + nx + ny + 1
+    return 2000 + 16 * n + n // 5 + 10
+
+
+def vtr(nx, ny, f) -> bytes:
+    """The text of Print_Result_VTK_2D's FlowField_<iter>.vtr."""
+    buf = C.create_string_buffer(vtr_size(nx, ny))
+    n = lib().oracle_vtr(nx, ny, *[_p(f[k]) for k in VTR_FIELDS], buf)
     return buf.raw[:n]
 
 

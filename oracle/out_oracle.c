@@ -20,6 +20,17 @@
  * ',f=block').
  * Arrays: (nx,ny) = (1:nx,1:ny); (nx+2,ny+2) = (0:nx+1,0:ny+1); flux =
  * Flux_n1(0:nx+1,0:ny+1,2).
+ *
+ * Also the ParaView file of Print_Result_VTK_2D (src/PrintResult.f90:165-190)
+ * through the VTR module (src/VTR_mod.f90:79-379): XML records "(100A)"
+ * exactly as the module writes them, and the values as REAL(4)
+ * (real(x, kind=4): round to nearest) in list-directed output.  The text of
+ * a list-directed real is processor-dependent (the Fortran standard leaves
+ * its layout to the compiler), so this format is defined here, not taken
+ * from a compiler: every value is a blank and 15 characters, the sign ('-'
+ * or a blank) and the correctly rounded "%.8E" of the exact value (9
+ * significant digits, enough to give back the same REAL(4)); "NaN",
+ * "Infinity", "-Infinity" right-justified in the 15; five values per record.
  */
 #include <math.h>
 #include <stdint.h>
@@ -130,5 +141,135 @@ int64_t oracle_tecplot_vcell(int comp, int nx, int ny, const double *x, const do
   p = put_block(p, 0, phiS, NULL, nx, ny);
   p = put_block(p, 0, vofS, NULL, nx, ny);
   p = put_block(p, 4, vof, vofS, nx, ny);
+  return (int64_t)(p - buf);
+}
+
+/* ------------------------------------------------------------------------
+ * ParaView VTR file (src/PrintResult.f90:165-190, src/VTR_mod.f90)
+ * ------------------------------------------------------------------------ */
+
+/* the 15 characters of one REAL(4) value */
+void oracle_e15_8(double x, char *o) {
+  const float f = (float)x;
+  const char *word = NULL;
+  if (isnan(f)) word = "NaN";
+  else if (isinf(f)) word = f < 0 ? "-Infinity" : "Infinity";
+  if (word) {
+    const int n = (int)strlen(word);
+    memset(o, ' ', 15 - n);
+    memcpy(o + 15 - n, word, n);
+    return;
+  }
+  char b[32];
+  const int n = snprintf(b, sizeof b, "%.8E", (double)f);
+  memset(o, ' ', 15);
+  memcpy(o + 15 - n, b, n);
+}
+
+void oracle_format_e15_8(const double *v, int64_t n, char *out) {
+  for (int64_t k = 0; k < n; ++k) oracle_e15_8(v[k], out + 15 * k);
+}
+
+/* list-directed record(s) of n values: value k is a blank and its 15
+ * characters; a line end after every fifth value and after the last */
+static char *put_values(char *p, int64_t n, double (*get)(const void *, int64_t),
+                        const void *ctx) {
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < n; ++k) {
+    char *o = p + k * 16 + k / 5;  /* after k values and k / 5 line ends */
+    o[0] = ' ';
+    oracle_e15_8(get(ctx, k), o + 1);
+    if (k % 5 == 4 || k == n - 1) o[16] = '\n';
+  }
+  return p + n * 16 + (n + 4) / 5;
+}
+
+struct vtr_ctx {
+  int nx, ny;
+  const double *a, *b;
+};
+static double get_x(const void *c, int64_t k) {  /* x(i,1) */
+  const struct vtr_ctx *q = c;
+  return q->a[k];
+}
+static double get_y(const void *c, int64_t k) {  /* y(1,j) */
+  const struct vtr_ctx *q = c;
+  return q->a[(size_t)k * q->nx];
+}
+static double get_zero(const void *c, int64_t k) {
+  (void)c;
+  (void)k;
+  return 0.0;
+}
+static double get_11(const void *c, int64_t k) {  /* a(i,j) of (nx,ny) */
+  const struct vtr_ctx *q = c;
+  return q->a[k];
+}
+static double get_00(const void *c, int64_t k) {  /* a(i,j) of (0:nx+1,0:ny+1) */
+  const struct vtr_ctx *q = c;
+  const int64_t i = k % q->nx + 1, j = k / q->nx + 1;
+  return q->a[(size_t)i + (size_t)j * (q->nx + 2)];
+}
+static double get_vel3(const void *c, int64_t k) {  /* (u, v, 0) per point */
+  const struct vtr_ctx *q = c;
+  const int64_t cell = k / 3, comp = k % 3;
+  if (comp == 2) return 0.0;
+  const int64_t i = cell % q->nx + 1, j = cell / q->nx + 1;
+  return (comp == 0 ? q->a : q->b)[(size_t)i + (size_t)j * (q->nx + 2)];
+}
+
+/* integer of "(I6)" after trim(adjustl()) */
+static void i6(int v, char *b) {
+  if (v < -99999 || v > 999999) strcpy(b, "******");
+  else sprintf(b, "%d", v);
+}
+
+/* Print_Result_VTK_2D: x, y (nx,ny); u, v, pr (0:nx+1,0:ny+1); phi, phiS,
+ * vof, vofS (nx,ny).  Returns the bytes written into buf. */
+int64_t oracle_vtr(int nx, int ny, const double *x, const double *y, const double *u,
+                   const double *v, const double *pr, const double *phi, const double *phiS,
+                   const double *vof, const double *vofS, char *buf) {
+  char *p = buf, ni[16], nj[16];
+  i6(nx, ni);
+  i6(ny, nj);
+  struct vtr_ctx c = {nx, ny, NULL, NULL};
+  const int64_t n = (int64_t)nx * ny;
+  p += sprintf(p, "<VTKFile type=\"RectilinearGrid\" version=\"0.1\" format=\"ascii\">\n");
+  p += sprintf(p, " <RectilinearGrid WholeExtent=\"1 %s 1 %s 1 1 \">\n", ni, nj);
+  p += sprintf(p, "  <Piece Extent=\"1 %s 1 %s 1 1 \">\n", ni, nj);
+  p += sprintf(p, "   <Coordinates>\n");
+  const char *axes[3] = {"X", "Y", "Z"};
+  for (int a = 0; a < 3; ++a) {
+    p += sprintf(p, "    <DataArray type=\"Float32\" Name=\"%s_COORDINATES\" "
+                    "NumberOfComponents=\"1\" format=\"ascii\">\n", axes[a]);
+    c.a = a == 0 ? x : y;
+    p = a == 0 ? put_values(p, nx, get_x, &c)
+        : a == 1 ? put_values(p, ny, get_y, &c) : put_values(p, 1, get_zero, &c);
+    p += sprintf(p, "    </DataArray>\n");
+  }
+  p += sprintf(p, "   </Coordinates>\n");
+  p += sprintf(p, "   <PointData>\n");
+  /* VTR_write_vector_2d (src/VTR_mod.f90:212-262) */
+  const char *vnames[3] = {"Velocity", "X_Velocity", "Y_Velocity"};
+  for (int a = 0; a < 3; ++a) {
+    p += sprintf(p, "        <DataArray type=\"Float32\" Name=\"%s\" NumberOfComponents=\"%d\" "
+                    "format=\"ascii\">\n", vnames[a], a == 0 ? 3 : 1);
+    c.a = a == 2 ? v : u;
+    c.b = v;
+    p = a == 0 ? put_values(p, 3 * n, get_vel3, &c) : put_values(p, n, get_00, &c);
+    p += sprintf(p, "        </DataArray>\n");
+  }
+  /* VTR_write_scalar_2d (src/VTR_mod.f90:330-344) */
+  const char *snames[5] = {"Pressure", "Levelset", "SolidLvs", "Vof", "SolidVof"};
+  const double *sarr[5] = {pr, phi, phiS, vof, vofS};
+  for (int a = 0; a < 5; ++a) {
+    p += sprintf(p, "         <DataArray type=\"Float32\" Name=\"%s\" NumberOfComponents=\"1\" "
+                    "format=\"ascii\">\n", snames[a]);
+    c.a = sarr[a];
+    p = put_values(p, n, a == 0 ? get_00 : get_11, &c);
+    p += sprintf(p, "         </DataArray>\n");
+  }
+  /* VTR_close_file (src/VTR_mod.f90:363-379) */
+  p += sprintf(p, "     </PointData>\n   </Piece>\n  </RectilinearGrid>\n</VTKFile>\n");
   return (int64_t)(p - buf);
 }

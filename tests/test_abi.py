@@ -126,14 +126,16 @@ def test_proj_library_exports_output_header_symbols(built):
 
 
 def test_output_field_struct_layouts(tmp_path):
-    """The ctypes mirrors of scf_tecplot_pcell / _vcell have the header's layout."""
+    """The ctypes mirrors of scf_tecplot_pcell / _vcell and scf_vtr_fields
+    have the header's layout."""
     import shutil
     import subprocess
     if not shutil.which("gcc"):
         import pytest
         pytest.skip("no C compiler")
     from simcoflow_gb300 import output as O
-    for cname, S in (("scf_tecplot_pcell", O.PCellFields), ("scf_tecplot_vcell", O.VCellFields)):
+    for cname, S in (("scf_tecplot_pcell", O.PCellFields), ("scf_tecplot_vcell", O.VCellFields),
+                     ("scf_vtr_fields", O.VtrFields)):
         src = tmp_path / f"{cname}.c"
         fields = [n for n, _ in S._fields_]
         src.write_text(
@@ -195,3 +197,15 @@ def test_cutcell_struct_layouts(tmp_path):
         assert int(out[0]) == ctypes.sizeof(S)
         for n, off in zip(fields, out[1:]):
             assert int(off) == getattr(S, n).offset, n
+
+
+def test_vtr_size_host_only(built, oracle):
+    """scf_vtr_size is host arithmetic, equal to the oracle file's length."""
+    import numpy as np
+    from simcoflow_gb300 import output as O
+    from test_out_oracle import vtr_fields
+    L = O.load()
+    for nx, ny in ((1, 1), (5, 3), (64, 33)):
+        f = vtr_fields(np.random.default_rng(nx), nx, ny)
+        assert L.scf_vtr_size(nx, ny) == len(oracle.vtr(nx, ny, f))
+    assert L.scf_vtr_size(0, 4) == -1

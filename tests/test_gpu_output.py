@@ -1,12 +1,13 @@
-"""GPU Tecplot writers (include/scf_out.h) against the oracle's restatement of
-Print_Result_Tecplot_PCent / _UCent / _VCent (src/PrintResult.f90:39-168),
-byte for byte, through the C-ABI."""
+"""GPU result-file writers (include/scf_out.h) against the oracle's
+restatement of Print_Result_Tecplot_PCent / _UCent / _VCent
+(src/PrintResult.f90:39-168) and of Print_Result_VTK_2D's ParaView file
+(:165-190, src/VTR_mod.f90), byte for byte, through the C-ABI."""
 import numpy as np
 import pytest
 
 from simcoflow_gb300 import output as O
 
-from test_out_oracle import edge_values, fields
+from test_out_oracle import edge_values, fields, real4_edges, vtr_fields
 
 pytestmark = pytest.mark.gpu
 
@@ -79,3 +80,42 @@ def test_device_format_matches_records(cuda, oracle):
     txt = oracle.tecplot_vcell(1, nx, ny, f)
     body = txt[txt.index(b"f=block\n") + len(b"f=block\n"):]
     assert bytes(out.cpu().numpy()) == body
+
+
+def test_e15_8_matches_oracle(cuda, oracle):
+    rng = np.random.default_rng(31)
+    v = real4_edges(rng, 200000)
+    # doubles just either side of float rounding boundaries
+    f = rng.integers(0, 2**31, 100000, dtype=np.uint64).astype(np.uint32).view(np.float32)
+    f = f[np.isfinite(f)].astype(np.float64)
+    half = np.abs(f) * 2.0**-25
+    v = np.concatenate([v, f + half, f - half, f + half * (1 + 2.0**-20)])
+    assert O.e15_8(v) == oracle.e15_8(v)
+
+
+@pytest.mark.parametrize("nx,ny", [(1, 1), (7, 5), (37, 29), (301, 257)])
+def test_vtr_text_matches_oracle(cuda, oracle, nx, ny):
+    rng = np.random.default_rng(nx * 997 + ny)
+    f = vtr_fields(rng, nx, ny)
+    flat = f["phi"].ravel(order="F")  # a view of the Fortran-ordered array
+    edges = real4_edges(rng, 0)
+    n = min(flat.size, edges.size)
+    flat[:n] = edges[:n]
+    assert O.vtr_text(nx, ny, f) == oracle.vtr(nx, ny, f)
+
+
+def test_vtr_device_pointers_and_file(cuda, oracle, tmp_path):
+    """Device-resident fields, written to dir/Paraview/FlowField_<iter>.vtr in
+    several 16 MiB chunks (3.3 M values)."""
+    import torch
+    rng = np.random.default_rng(19)
+    nx, ny = 600, 550
+    f = vtr_fields(rng, nx, ny)
+    dev = {k: torch.from_numpy(np.ascontiguousarray(a.ravel(order="F"))).cuda()
+           for k, a in f.items()}
+    (tmp_path / "Paraview").mkdir()
+    ms = O.vtr_write(nx, ny, dev, 77, str(tmp_path) + "/", device_ptrs=True)
+    data = (tmp_path / "Paraview" / "FlowField_00000077.vtr").read_bytes()
+    assert data == oracle.vtr(nx, ny, f)
+    assert len(data) == O.load().scf_vtr_size(nx, ny)
+    assert ms > 0.0
