@@ -367,63 +367,105 @@ __global__ void k_coarsen(LevelView F, LevelView C, double* di) {
   }
 }
 
-// Dense inverse of the coarsest operator (at most kMaxCoarse unknowns) by
-// Gauss-Jordan elimination without pivoting (the matrix is SPD).
-__global__ void k_coarse_setup(LevelView C, double* Ainv, int* cmap, int* nc_out) {
+// Dense inverse of the coarsest operator (at most kMaxCoarse unknowns).  The
+// operator is SPD with lexicographic numbering, so its bandwidth is at most
+// the level's width: A = L D L^T is factored within the band (right-looking,
+// no pivoting; one reciprocal per step, taken by the thread that finishes the
+// next pivot), then each thread solves L D L^T x = e_c for one column c of
+// the inverse.  kCoarseCtas CTAs split the columns; each factors the small
+// matrix itself (n dependent steps), which is cheaper than a second launch
+// to share the factor.
+constexpr int kCoarseCtas = 8;
+__global__ void __launch_bounds__(kMaxCoarse) k_coarse_setup(LevelView C, double* Ainv, int* cmap,
+                                                             int* nc_out) {
   pdl_wait();
-  __shared__ double A[kMaxCoarse * kMaxCoarse];
-  __shared__ double rowp[kMaxCoarse], colp[kMaxCoarse];
-  __shared__ int map[kMaxCoarse];
-  __shared__ int n;
-  const int t = threadIdx.x, NT = blockDim.x;
+  constexpr int M = kMaxCoarse;
+  __shared__ double A[M * M];  // row-major, stride M; L below the diagonal, D on it
+  __shared__ double col[M], dinv[M];
+  __shared__ int map[M], wsum[M / 32], band;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const int ncell = C.nx * C.ny;
-  if (t == 0) {
-    int c = 0;
-    for (int k = 0; k < ncell; ++k) {
-      int ix = k % C.nx, iy = k / C.nx;
-      map[k] = C.dg[(size_t)iy * C.pitch + ix] >= 0.0 ? c++ : -1;
+  // numbering of the cells that take part (dg >= 0), in lexicographic order
+  const int ix = t % C.nx, iy = t / C.nx;
+  const size_t kk = (size_t)iy * C.pitch + ix;
+  const bool act = t < ncell && C.dg[kk] >= 0.0;
+  const unsigned bal = __ballot_sync(0xffffffffu, act);
+  if (lane == 0) wsum[w] = __popc(bal);
+  if (t == 0) band = 0;
+  for (int e = t; e < M * M; e += M) A[e] = 0.0;
+  __syncthreads();
+  int off = 0, n = 0;
+  for (int k = 0; k < M / 32; ++k) {
+    off += k < w ? wsum[k] : 0;
+    n += wsum[k];
+  }
+  const int r = act ? off + __popc(bal & ((1u << lane) - 1)) : -1;
+  map[t] = r;
+  __syncthreads();
+  if (act) {
+    A[r * M + r] = C.dg[kk];
+    int b = 0;
+    if (ix + 1 < C.nx && map[t + 1] >= 0) {
+      const int c = map[t + 1];
+      A[r * M + c] = -C.cE[kk];
+      A[c * M + r] = -C.cE[kk];
+      b = c - r;
     }
-    n = c;
+    if (iy + 1 < C.ny && map[t + C.nx] >= 0) {
+      const int c = map[t + C.nx];
+      A[r * M + c] = -C.cN[kk];
+      A[c * M + r] = -C.cN[kk];
+      b = max(b, c - r);
+    }
+    atomicMax(&band, b);
   }
   __syncthreads();
-  const int nn = n;
-  for (int e = t; e < nn * nn; e += NT) A[e] = 0.0;
+  const int bw = band;
+  if (t == 0 && n > 0) dinv[0] = 1.0 / A[0];
   __syncthreads();
-  if (t == 0) {
-    for (int k = 0; k < ncell; ++k) {
-      int r = map[k];
-      if (r < 0) continue;
-      int ix = k % C.nx, iy = k / C.nx;
-      size_t kk = (size_t)iy * C.pitch + ix;
-      A[r * nn + r] = C.dg[kk];
-      if (ix + 1 < C.nx && map[k + 1] >= 0) {
-        int c = map[k + 1];
-        A[r * nn + c] = -C.cE[kk]; A[c * nn + r] = -C.cE[kk];
-      }
-      if (iy + 1 < C.ny && map[k + C.nx] >= 0) {
-        int c = map[k + C.nx];
-        A[r * nn + c] = -C.cN[kk]; A[c * nn + r] = -C.cN[kk];
-      }
-    }
-  }
-  __syncthreads();
-  for (int p = 0; p < nn; ++p) {
-    const double piv = A[p * nn + p];
-    for (int j = t; j < nn; j += NT) {
-      rowp[j] = (j == p) ? 1.0 / piv : A[p * nn + j] / piv;
-      colp[j] = A[j * nn + p];
+  // step k: L[i][k] = A[i][k] / d_k, then A[i][j] -= L[i][k] A[j][k] for
+  // k < j <= i <= k + bw (the trailing band triangle)
+  for (int k = 0; k < n; ++k) {
+    const int last = min(n - 1, k + bw);
+    if (t > 0 && k + t <= last) {
+      const int i = k + t;
+      col[i] = A[i * M + k];
+      A[i * M + k] = col[i] * dinv[k];
     }
     __syncthreads();
-    for (int e = t; e < nn * nn; e += NT) {
-      int i = e / nn, j = e % nn;
-      if (i == p) A[e] = rowp[j];
-      else A[e] = ((j == p) ? 0.0 : A[e]) - colp[i] * rowp[j];
+    const int m = last - k;  // trailing rows
+    if (m == 0 && t == 0 && k + 1 < n) dinv[k + 1] = 1.0 / A[(k + 1) * M + k + 1];  // bw 0
+    for (int e = t; e < m * m; e += M) {
+      const int i = k + 1 + e / m, j = k + 1 + e % m;
+      if (j <= i) {
+        const double a = A[i * M + j] - A[i * M + k] * col[j];
+        A[i * M + j] = a;
+        if (e == 0) dinv[k + 1] = 1.0 / a;  // the next pivot is final
+      }
     }
     __syncthreads();
   }
-  for (int e = t; e < nn * nn; e += NT) Ainv[e] = A[e];
-  for (int k = t; k < ncell; k += NT) cmap[k] = map[k];
-  if (t == 0) *nc_out = nn;
+  // column c of the inverse: L y = e_c, z = D^-1 y, L^T x = z
+  const int c = blockIdx.x + t * (int)gridDim.x;
+  if (c < n) {
+    double xv[M];
+    for (int i = 0; i < n; ++i) {
+      double y = i == c ? 1.0 : 0.0;
+      if (i > c)
+        for (int j = max(c, i - bw); j < i; ++j) y -= A[i * M + j] * xv[j];
+      xv[i] = y;
+    }
+    for (int i = n - 1; i >= 0; --i) {
+      double x = xv[i] * dinv[i];
+      for (int j = i + 1; j <= min(n - 1, i + bw); ++j) x -= A[j * M + i] * xv[j];
+      xv[i] = x;
+      Ainv[(size_t)i * n + c] = x;
+    }
+  }
+  if (blockIdx.x == 0) {
+    for (int k = t; k < ncell; k += M) cmap[k] = map[k];
+    if (t == 0) *nc_out = n;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -803,7 +845,7 @@ void launch_coarsen(LevelView F, LevelView C, double* di, cudaStream_t s) {
   launch_k(k_coarsen, grid_for(C.nx, C.ny, 1), kBlock, 0, s, F, C, di);
 }
 void launch_coarse_setup(LevelView C, double* Ainv, int* cmap, int* nc, cudaStream_t s) {
-  launch_k(k_coarse_setup, dim3(1), dim3(1024), 0, s, C, Ainv, cmap, nc);
+  launch_k(k_coarse_setup, dim3(kCoarseCtas), dim3(kMaxCoarse), 0, s, C, Ainv, cmap, nc);
 }
 void launch_rhs(const FortranIn& in, const double* ustar, const double* vstar, double vb,
                 LevelView L0, double* bvec, double* r, float* r32, double* x, Scalars* sc,
