@@ -254,6 +254,24 @@ def extra_stretched(local, args):
                 return s.update_puv(t["ustar"], t["vstar"], u, v, p, case.vb, Pp=Pp,
                                     mres=m)[2]
 
+            # each arm at its fastest V-cycle schedule (the autotuner's candidates;
+            # the line smoother uses only the coarse-correction weight)
+            schedule = None
+            if not args.no_tune:
+                from simcoflow_gb300 import batch as Bt
+                best = None
+                for sch in sorted({(2, 2, sc[2]) for sc in Bt.SCHEDULES}):
+                    s.set_schedule(*sch)
+                    step()
+                    torch.cuda.synchronize(dev)
+                    t0 = time.perf_counter()
+                    stt = step()
+                    torch.cuda.synchronize(dev)
+                    ms_t = time.perf_counter() - t0
+                    if stt.status == 0 and (best is None or ms_t < best[0]):
+                        best = (ms_t, sch)
+                schedule = best[1]
+                s.set_schedule(*schedule)
             step()
             torch.cuda.synchronize(dev)
             e0, e1 = torch.cuda.Event(True), torch.cuda.Event(True)
@@ -264,7 +282,7 @@ def extra_stretched(local, args):
             e1.record()
             torch.cuda.synchronize(dev)
             out[prec] = {"ms": round(e0.elapsed_time(e1) / reps, 3), "iters": st.iters,
-                         "relres_true": st.relres_true,
+                         "relres_true": st.relres_true, "schedule": schedule,
                          "smoother": {1: "point", 2: "line"}.get(st.smoother)}
         finally:
             s.close()

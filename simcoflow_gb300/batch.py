@@ -24,7 +24,8 @@ import numpy as np
 from . import projection as P
 
 # candidate schedules: (npre, npost, omega)
-SCHEDULES = [(1, 1, 1.9), (2, 2, 1.9), (2, 2, 1.95), (2, 1, 1.9), (3, 3, 1.9), (1, 2, 1.9)]
+SCHEDULES = [(1, 1, 1.9), (2, 2, 1.9), (2, 2, 1.95), (2, 2, 1.97), (2, 1, 1.9), (3, 3, 1.9),
+             (1, 2, 1.9)]
 
 
 def size_class(nx: int, ny: int) -> int:
