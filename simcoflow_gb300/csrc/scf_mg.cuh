@@ -64,7 +64,7 @@ void launch_tail(const TailDesc<T, CT>& d, Scalars* sc, cudaStream_t s);
 // kSweepBoxY; cells outside the grid read as zero.
 constexpr int kSweepBoxX = 80, kSweepBoxY = 42;  // 64x32 tile + 8 / 5 cells around
 constexpr int kSweepMaps = 6;                    // x0, x1, b, di, cE, cN
-// encodes the six maps into host memory; false when the driver has no tensor
+// encodes the six maps into host memory; false when the CUDA driver has no tensor
 // maps or refuses one
 bool make_sweep_maps(const MgView<float, __nv_bfloat16, float>& L, float* const xbuf[2],
                      const float* b, CUtensorMap* maps);

@@ -1,6 +1,6 @@
 """GPU parity of the projection path against the oracle, through the C-ABI.
 
-Tolerances (spec bar): pressure rel-L2 <= 1e-8, corrected velocity
+Tolerances: pressure rel-L2 <= 1e-8, corrected velocity
 rel-L2 <= 1e-9, when both sides are driven to the FP64 floor; assembly and
 right-hand side bit for bit.
 """
