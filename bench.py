@@ -510,6 +510,42 @@ def extra_vtr(case, local, args):
     return out
 
 
+def extra_lsweep(case, local, args):
+    """The level-set part of one X_Sweep and one Y_Sweep on the headline grid
+    with device-resident fields, against the C restatement on one core."""
+    import torch
+    from simcoflow_gb300 import clsvof as CL
+    sys.path.insert(0, str(ROOT / "tests"))
+    from test_clsvof_oracle import ls_fields
+    nx, ny = case.nx, case.ny
+    f = ls_fields(np.random.default_rng(29), nx, ny)
+    t0 = np.asfortranarray(np.random.default_rng(30).standard_normal((nx, ny)))
+    dev = torch.device("cuda", local)
+    tf = {k: torch.from_numpy(np.ascontiguousarray(a.ravel(order="F"))).to(dev)
+          for k, a in f.items()}
+    tt = torch.from_numpy(np.ascontiguousarray(t0.ravel(order="F"))).to(dev)
+    for _ in range(3):
+        CL.sweep(CL.X, nx, ny, tf, 1e-4, tt, device_ptrs=True, device=local)
+    reps = 10
+    ms = 0.0
+    for _ in range(reps):
+        ms += CL.sweep(CL.X, nx, ny, tf, 1e-4, tt, device_ptrs=True, device=local)
+        ms += CL.sweep(CL.Y, nx, ny, tf, 1e-4, tt, device_ptrs=True, device=local)
+    out = {"workload": f"level-set update of one X_Sweep and one Y_Sweep, {nx}x{ny}",
+           "gpu": {"ms_x_plus_y": round(ms / reps, 3),
+                   "timing": "host clock around scf_ls_sweep (device pointers; each call "
+                             "creates a stream, launches one kernel and synchronises)"}}
+    if not args.no_cpu:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle as O
+        t1 = time.perf_counter()
+        O.ls_sweep(1, nx, ny, f, 1e-4, O.ls_sweep(0, nx, ny, f, 1e-4, t0))
+        cpu_ms = (time.perf_counter() - t1) * 1e3
+        out["cpu"] = {"ms_x_plus_y": round(cpu_ms, 1), "cores": 1, "kind": "port",
+                      "sample": "the literal sequential loops (C restatement)"}
+    return out
+
+
 def extra_cutcell(case, local, args):
     """The per-step cut-cell geometry of the P, U and V cells
     (Grid_Preprocess + NewCellFace, scf_grid_preprocess) on the headline
@@ -821,6 +857,7 @@ def run_ours(args):
                          ("momentum_2048", lambda: extra_momentum(case, local, args)),
                          ("tecplot_2048", lambda: extra_tecplot(case, local, args)),
                          ("vtr_2048", lambda: extra_vtr(case, local, args)),
+                         ("ls_sweep_2048", lambda: extra_lsweep(case, local, args)),
                          ("cutcell_2048", lambda: extra_cutcell(case, local, args))):
             try:
                 extras[name] = fn()

@@ -17,7 +17,8 @@ OUT = HERE / "_build" / "liboracle.so"
 
 
 def build(force: bool = False) -> Path:
-    srcs = [HERE / "scf_oracle.c", HERE / "mom_oracle.c", HERE / "out_oracle.c"]
+    srcs = [HERE / "scf_oracle.c", HERE / "mom_oracle.c", HERE / "out_oracle.c",
+            HERE / "clsvof_oracle.c"]
     OUT.parent.mkdir(exist_ok=True)
     newest = max(p.stat().st_mtime for p in srcs)
     if force or not OUT.exists() or OUT.stat().st_mtime < newest:

@@ -36,6 +36,9 @@ Pieces:
     vtr         Print_Result_VTK_2D's ParaView file   src/PrintResult.f90:165-190,
                 src/VTR_mod.f90:79-379
     e15_8       its list-directed REAL(4) value text (15 characters)
+  C restatement of the CLSVOF sweeps' level-set part (clsvof_oracle.c)
+    ls_sweep    X_Sweep / Y_Sweep temls update   src/Clsvof_Mod.f90:1074-1123,
+                1191-1244
 """
 from __future__ import annotations
 
@@ -99,6 +102,7 @@ def lib():
         L.oracle_format_e15_8.argtypes = [_P, C.c_int64, C.c_char_p]
         L.oracle_vtr.restype = C.c_int64
         L.oracle_vtr.argtypes = [C.c_int, C.c_int] + [_P] * 9 + [C.c_char_p]
+        L.oracle_ls_sweep.argtypes = [C.c_int] * 3 + [_P] * 12 + [C.c_double, _P]
         _lib = L
     return _lib
 
@@ -546,6 +550,17 @@ def vtr(nx, ny, f) -> bytes:
     buf = C.create_string_buffer(vtr_size(nx, ny))
     n = lib().oracle_vtr(nx, ny, *[_p(f[k]) for k in VTR_FIELDS], buf)
     return buf.raw[:n]
+
+
+LS_FIELDS = ["phi", "vofS", "dx", "dy", "x", "y", "aE", "aW", "aN", "aS", "ue", "ve"]
+
+
+def ls_sweep(dir, nx, ny, f, dtv, temls):
+    """X_Sweep (dir 0) / Y_Sweep (dir 1) level-set update of a copy of
+    temls (Fortran-ordered (nx,ny)); returns the new array."""
+    out = np.asfortranarray(np.array(temls, dtype=np.float64))
+    lib().oracle_ls_sweep(dir, nx, ny, *[_p(f[k]) for k in LS_FIELDS], dtv, _p(out))
+    return out
 
 
 def grid_preprocess_literal(nx, ny, grids, fams, icorprob=True, aln_old=None):

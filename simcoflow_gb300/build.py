@@ -22,10 +22,12 @@ INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["scf_kernels.cu", "scf_mg.cu", "scf_line.cu", "scf_unet.cu", "scf_proj.cu",
-                "scf_noalloc.cu", "scf_mom.cu", "scf_geom.cu", "scf_out.cu", "scf_cutcell.cu"]
-# per-file flags: the cut-cell geometry restates the reference's expressions
-# with every multiply and add rounded on its own (no FMA contraction)
-EXTRA_FLAGS = {"scf_cutcell.cu": ["-fmad=false"]}
+                "scf_noalloc.cu", "scf_mom.cu", "scf_geom.cu", "scf_out.cu", "scf_cutcell.cu",
+                "scf_clsvof.cu"]
+# per-file flags: the cut-cell geometry and the level-set sweeps restate the
+# reference's expressions with every multiply and add rounded on its own (no
+# FMA contraction)
+EXTRA_FLAGS = {"scf_cutcell.cu": ["-fmad=false"], "scf_clsvof.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:

@@ -1,0 +1,78 @@
+"""Python host API over the level-set sweeps of libscf_proj.so
+(include/scf_clsvof.h): the level-set part of X_Sweep / Y_Sweep
+(src/Clsvof_Mod.f90:1074-1123, 1191-1244) on the GPU.
+
+Fields are the reference's Fortran arrays (Fortran-ordered numpy float64):
+(nx,ny) phi, vofS, dx, dy, x, y; (nx+2,ny+2) aE, aW, aN, aS; ue (nx+1,ny)
+for ue(0:nx,1:ny); ve (nx,ny+1) for ve(1:nx,0:ny); with device_ptrs=True,
+contiguous CUDA float64 tensors with those element counts.  No CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import projection as P
+
+EXPORTS = ["scf_ls_sweep"]
+X, Y = 0, 1
+DEVICE_PTRS = 1
+FIELDS = [("phi", "1"), ("vofS", "1"), ("dx", "1"), ("dy", "1"), ("x", "1"), ("y", "1"),
+          ("aE", "0"), ("aW", "0"), ("aN", "0"), ("aS", "0"), ("ue", "u"), ("ve", "v")]
+
+
+class LsFields(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n, _ in FIELDS]
+
+
+def load():
+    L = P.load()
+    if not getattr(L, "_ls_bound", False):
+        L.scf_ls_sweep.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_void_p,
+                                   C.c_int, C.c_int, C.POINTER(C.c_double)]
+        L.scf_ls_sweep.restype = C.c_int
+        L._ls_bound = True
+    return L
+
+
+def _pack(nx, ny, f, device_ptrs):
+    st, keep = LsFields(), []
+    for name, sk in FIELDS:
+        a = f[name]
+        shape = {"1": (nx, ny), "0": (nx + 2, ny + 2), "u": (nx + 1, ny), "v": (nx, ny + 1)}[sk]
+        if device_ptrs:
+            import torch
+            if not (isinstance(a, torch.Tensor) and a.is_cuda and a.is_contiguous()
+                    and a.dtype == torch.float64 and a.numel() == int(np.prod(shape))):
+                raise ValueError(f"{name}: expected a contiguous CUDA float64 tensor of "
+                                 f"{int(np.prod(shape))} elements")
+            ptr = a.data_ptr()
+        else:
+            if (not isinstance(a, np.ndarray) or a.shape != shape or a.dtype != np.float64
+                    or not a.flags["F_CONTIGUOUS"]):
+                raise ValueError(f"{name}: expected a Fortran-ordered float64{shape}")
+            ptr = a.ctypes.data
+        keep.append(a)
+        setattr(st, name, ptr)
+    return st, keep
+
+
+def sweep(dir: int, nx: int, ny: int, fields: dict, dtv: float, temls, device_ptrs: bool = False,
+          device: int = 0) -> float:
+    """Apply one sweep's level-set update to temls in place (a Fortran-ordered
+    (nx,ny) float64 array, or a CUDA tensor with device_ptrs); returns the
+    call's elapsed milliseconds."""
+    st, keep = _pack(nx, ny, fields, device_ptrs)
+    if device_ptrs:
+        ptr = temls.data_ptr()
+    else:
+        if (not isinstance(temls, np.ndarray) or temls.shape != (nx, ny)
+                or temls.dtype != np.float64 or not temls.flags["F_CONTIGUOUS"]):
+            raise ValueError("temls: expected a Fortran-ordered float64 (nx,ny)")
+        ptr = temls.ctypes.data
+    ms = C.c_double(0.0)
+    P._check(load().scf_ls_sweep(dir, nx, ny, C.byref(st), float(dtv), ptr,
+                                 DEVICE_PTRS if device_ptrs else 0, device, C.byref(ms)),
+             "scf_ls_sweep")
+    return ms.value

@@ -209,3 +209,34 @@ def test_vtr_size_host_only(built, oracle):
         f = vtr_fields(np.random.default_rng(nx), nx, ny)
         assert L.scf_vtr_size(nx, ny) == len(oracle.vtr(nx, ny, f))
     assert L.scf_vtr_size(0, 4) == -1
+
+
+def test_proj_library_exports_clsvof_header_symbols(built):
+    from simcoflow_gb300 import build, clsvof
+    lib = ctypes.CDLL(str(build.build_proj()))
+    names = _declared("scf_clsvof.h")
+    for n in names:
+        assert hasattr(lib, n), n
+    assert sorted(clsvof.EXPORTS) == names
+
+
+def test_ls_fields_struct_layout(tmp_path):
+    """The ctypes mirror of scf_ls_fields has the header's layout."""
+    import shutil
+    import subprocess
+    if not shutil.which("gcc"):
+        import pytest
+        pytest.skip("no C compiler")
+    from simcoflow_gb300 import clsvof
+    fields = [n for n, _ in clsvof.LsFields._fields_]
+    src = tmp_path / "ls.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "scf_clsvof.h"\n'
+                   'int main(void) {\n  printf("%zu\\n", sizeof(scf_ls_fields));\n'
+                   + "".join(f'  printf("%zu\\n", offsetof(scf_ls_fields, {n}));\n'
+                             for n in fields) + "  return 0;\n}\n")
+    exe = tmp_path / "ls"
+    subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    assert int(out[0]) == ctypes.sizeof(clsvof.LsFields)
+    for n, off in zip(fields, out[1:]):
+        assert int(off) == getattr(clsvof.LsFields, n).offset, n
