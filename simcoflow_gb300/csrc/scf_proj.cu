@@ -39,6 +39,10 @@ struct scf_proj {
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t copy_done = nullptr;
   cudaEvent_t late_done = nullptr;  // the copies only the correction reads
+  // mixed setup: each level's conversion to FP32/BF16 runs on `aux` as soon
+  // as the level exists, beside the coarsening of the next levels
+  cudaStream_t aux = nullptr;
+  cudaEvent_t lev_ev[32] = {}, aux_done = nullptr;
   // host mode: set_geometry's U/V arrays (read by the correction only), copied
   // by the next solve on the copy stream while the PCG runs
   struct Late {
@@ -429,17 +433,29 @@ void enqueue_line_setup_t(const std::vector<MgView<T, CT, T>>& nat,
 
 // assembly of the fine operator and setup of the whole hierarchy
 void enqueue_setup(scf_proj* h, Scalars* sc, cudaStream_t s) {
+  const size_t nl = h->lev.size();
+  // mixed: level l's largest coupling and FP32/BF16 copy on `aux` once level
+  // l is built (an event per level), joined before the line setup
+  auto convert = [&](size_t l) {
+    cudaEventRecord(h->lev_ev[l], s);
+    cudaStreamWaitEvent(h->aux, h->lev_ev[l], 0);
+    launch_max_coupling(h->lev[l], h->maxbits + l, h->aux);
+    launch_to_mixed(h->lev[l], h->mix[l], h->maxbits + l, h->cscale + l, h->aux);
+  };
+  if (h->mixed) cudaMemsetAsync(h->maxbits, 0, sizeof(unsigned) * nl, s);
   launch_assemble(h->fin, h->lev[0], sc, s);
   // FP64 inverse diagonals serve the FP64 smoothers only
   launch_excess(h->lev[0], h->mixed ? nullptr : h->di64[0], s);
-  for (size_t l = 1; l < h->lev.size(); ++l)
+  if (h->mixed) convert(0);
+  for (size_t l = 1; l < nl; ++l) {
     launch_coarsen(h->lev[l - 1], h->lev[l], h->mixed ? nullptr : h->di64[l], s);
+    if (h->mixed) convert(l);
+  }
   launch_coarse_setup(h->lev.back(), h->Ainv, h->cmap, h->ncoarse, s);
-  if (h->mixed)
-    for (size_t l = 0; l < h->lev.size(); ++l) {
-      launch_max_coupling(h->lev[l], h->maxbits + l, s);
-      launch_to_mixed(h->lev[l], h->mix[l], h->maxbits + l, h->cscale + l, s);
-    }
+  if (h->mixed) {
+    cudaEventRecord(h->aux_done, h->aux);
+    cudaStreamWaitEvent(s, h->aux_done, 0);
+  }
   if (h->line) {
     if (h->mixed) {
       enqueue_line_setup_t(h->mix, h->t32, s);
@@ -988,6 +1004,14 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
       cudaEventCreateWithFlags(&h->copy_done, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&h->late_done, cudaEventDisableTiming) != cudaSuccess)
     return fail(SCF_ERR_CUDA);
+  if (h->mixed) {
+    if (cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->aux_done, cudaEventDisableTiming) != cudaSuccess)
+      return fail(SCF_ERR_CUDA);
+    for (auto& e : h->lev_ev)
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+        return fail(SCF_ERR_CUDA);
+  }
   for (auto& e : h->ev)
     if (cudaEventCreate(&e) != cudaSuccess) return fail(SCF_ERR_CUDA);
   // FP64 multigrid levels
@@ -1152,6 +1176,10 @@ int scf_proj_destroy(scf_proj* h) {
   if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   if (h->copy_done) cudaEventDestroy(h->copy_done);
   if (h->late_done) cudaEventDestroy(h->late_done);
+  if (h->aux) cudaStreamDestroy(h->aux);
+  if (h->aux_done) cudaEventDestroy(h->aux_done);
+  for (auto& e : h->lev_ev)
+    if (e) cudaEventDestroy(e);
   delete h;
   return SCF_OK;
 }
