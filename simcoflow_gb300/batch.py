@@ -24,8 +24,10 @@ import numpy as np
 from . import projection as P
 
 # candidate schedules: (npre, npost, omega)
-SCHEDULES = [(1, 1, 1.9), (2, 2, 1.9), (2, 2, 1.95), (2, 2, 1.97), (2, 1, 1.9), (3, 3, 1.9),
-             (1, 2, 1.9)]
+# candidates of the batch autotuner (one representative instance per size
+# class), and of a single large projection, which also tries omega 1.97
+BATCH_SCHEDULES = [(1, 1, 1.9), (2, 2, 1.9), (2, 2, 1.95), (2, 1, 1.9), (3, 3, 1.9), (1, 2, 1.9)]
+SCHEDULES = BATCH_SCHEDULES + [(2, 2, 1.97)]
 
 
 def size_class(nx: int, ny: int) -> int:
@@ -73,7 +75,7 @@ class _Instance:
         self.s.close()
 
 
-def autotune(insts, schedules=SCHEDULES, reps=3, log=None):
+def autotune(insts, schedules=BATCH_SCHEDULES, reps=3, log=None):
     """Fastest schedule per size class: {class: (npre, npost, omega)}."""
     import torch
     table = {}

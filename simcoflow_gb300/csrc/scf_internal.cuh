@@ -244,7 +244,7 @@ inline dim3 grid_for(int nx, int ny, int cells_per_thread_x = 2) {
 // ---- kernel launchers (scf_kernels.cu) ----
 void launch_assemble(const FortranIn& in, LevelView L0, Scalars* sc, cudaStream_t s);
 void launch_divide(const double* a, const double* b, double* q, long long n, cudaStream_t s);
-void launch_excess(LevelView L, double* di, cudaStream_t s);
+void launch_excess(LevelView L, double* di, unsigned* zero_bits, int nzero, cudaStream_t s);
 void launch_coarsen(LevelView F, LevelView C, double* di, cudaStream_t s);
 void launch_coarse_setup(LevelView C, double* Ainv, int* cmap, int* nc, cudaStream_t s);
 void launch_rhs(const FortranIn& in, const double* ustar, const double* vstar, double vb,

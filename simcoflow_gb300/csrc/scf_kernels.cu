@@ -306,8 +306,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_assemble(FortranIn in, LevelVie
 // diagonal excess dg - (cE + cW + cN + cS), clamped at zero, and the
 // inverse diagonal (0 where the cell has no unknown; skipped when di is null:
 // the mixed-precision hierarchy builds its own FP32 inverse diagonals)
-__global__ void k_excess(LevelView L, double* di) {
+// also clears the per-level largest-coupling words (zero_bits, nzero) that
+// the mixed setup's k_max_coupling raises after this kernel
+__global__ void k_excess(LevelView L, double* di, unsigned* zero_bits, int nzero) {
   pdl_wait();
+  if (zero_bits && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.y == 0 && threadIdx.x < nzero)
+    zero_bits[threadIdx.x] = 0u;
   const int ix = blockIdx.x * kBX + threadIdx.x;
   if (ix >= L.nx) return;
   for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY) {
@@ -838,8 +842,8 @@ void launch_assemble(const FortranIn& in, LevelView L0, Scalars* sc, cudaStream_
 void launch_divide(const double* a, const double* b, double* q, long long n, cudaStream_t s) {
   launch_k(k_divide, dim3(152 * 8), dim3(256), 0, s, a, b, q, n);
 }
-void launch_excess(LevelView L, double* di, cudaStream_t s) {
-  launch_k(k_excess, grid_for(L.nx, L.ny, 1), kBlock, 0, s, L, di);
+void launch_excess(LevelView L, double* di, unsigned* zero_bits, int nzero, cudaStream_t s) {
+  launch_k(k_excess, grid_for(L.nx, L.ny, 1), kBlock, 0, s, L, di, zero_bits, nzero);
 }
 void launch_coarsen(LevelView F, LevelView C, double* di, cudaStream_t s) {
   launch_k(k_coarsen, grid_for(C.nx, C.ny, 1), kBlock, 0, s, F, C, di);

@@ -432,27 +432,35 @@ void enqueue_line_setup_t(const std::vector<MgView<T, CT, T>>& nat,
 }
 
 // assembly of the fine operator and setup of the whole hierarchy
-void enqueue_setup(scf_proj* h, Scalars* sc, cudaStream_t s) {
+// fork: mixed levels are converted on `aux` (one projection on the GPU); a
+// batch branch keeps everything on `s`, since its branches already overlap.
+void enqueue_setup(scf_proj* h, Scalars* sc, cudaStream_t s, bool fork = true) {
   const size_t nl = h->lev.size();
   // mixed: level l's largest coupling and FP32/BF16 copy on `aux` once level
   // l is built (an event per level), joined before the line setup
+  cudaStream_t cs = fork ? h->aux : s;
   auto convert = [&](size_t l) {
-    cudaEventRecord(h->lev_ev[l], s);
-    cudaStreamWaitEvent(h->aux, h->lev_ev[l], 0);
-    launch_max_coupling(h->lev[l], h->maxbits + l, h->aux);
-    launch_to_mixed(h->lev[l], h->mix[l], h->maxbits + l, h->cscale + l, h->aux);
+    if (fork) {
+      cudaEventRecord(h->lev_ev[l], s);
+      cudaStreamWaitEvent(h->aux, h->lev_ev[l], 0);
+    }
+    launch_max_coupling(h->lev[l], h->maxbits + l, cs);
+    launch_to_mixed(h->lev[l], h->mix[l], h->maxbits + l, h->cscale + l, cs);
   };
-  if (h->mixed) cudaMemsetAsync(h->maxbits, 0, sizeof(unsigned) * nl, s);
   launch_assemble(h->fin, h->lev[0], sc, s);
-  // FP64 inverse diagonals serve the FP64 smoothers only
-  launch_excess(h->lev[0], h->mixed ? nullptr : h->di64[0], s);
-  if (h->mixed) convert(0);
+  // FP64 inverse diagonals serve the FP64 smoothers only; the mixed setup's
+  // largest couplings restart from zero
+  launch_excess(h->lev[0], h->mixed ? nullptr : h->di64[0], h->mixed ? h->maxbits : nullptr,
+                (int)nl, s);
+  if (h->mixed && fork) convert(0);
   for (size_t l = 1; l < nl; ++l) {
     launch_coarsen(h->lev[l - 1], h->lev[l], h->mixed ? nullptr : h->di64[l], s);
-    if (h->mixed) convert(l);
+    if (h->mixed && fork) convert(l);
   }
   launch_coarse_setup(h->lev.back(), h->Ainv, h->cmap, h->ncoarse, s);
-  if (h->mixed) {
+  if (h->mixed && !fork)
+    for (size_t l = 0; l < nl; ++l) convert(l);
+  if (h->mixed && fork) {
     cudaEventRecord(h->aux_done, h->aux);
     cudaStreamWaitEvent(s, h->aux_done, 0);
   }
@@ -635,7 +643,7 @@ int add_batch_branch(scf_proj* h, const BatchIO& io, cudaGraph_t g, cudaStream_t
   long long lb = 0;
   do {
     cudaMemsetAsync(h->sc, 0, sizeof(Scalars), cs);
-    enqueue_setup(h, h->sc, cs);
+    enqueue_setup(h, h->sc, cs, false);
     LevelView L0 = h->lev[0];
     launch_rhs(h->fin, io.ustar, io.vstar, io.vb, L0, h->bvec, L0.b, h->r32, h->xsol, h->sc,
                h->part, h->opts.rtol, h->opts.maxit, cs);
