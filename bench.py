@@ -141,7 +141,7 @@ def reduce_max(x: float, pg, device) -> float:
 
 
 def make_case(name: str, rank: int):
-    from simcoflow_gb300 import synth
+    from gen import synth
     return synth.make_case(name, instance=rank)
 
 
@@ -233,7 +233,8 @@ def extra_learned(case, tdev, dev, local, args):
 def extra_stretched(local, args):
     """The 4096^2 y-stretched configuration (line smoother), mixed and plain FP64."""
     import torch
-    from simcoflow_gb300 import synth, projection as P
+    from gen import synth
+    from simcoflow_gb300 import projection as P
     case = synth.c3()
     dev = torch.device("cuda", local)
     t = {k: torch.from_numpy(np.ascontiguousarray(v.ravel(order="F"))).to(dev)
@@ -296,7 +297,7 @@ def extra_momentum(case, local, args):
     (operator, right-hand side, BiCGStab, scatter) on all host cores."""
     import torch
     from simcoflow_gb300 import momentum as M
-    from simcoflow_gb300 import synth
+    from gen import synth
     dev = torch.device("cuda", local)
     out = {"workload": f"u and v implicit solves on the {case.nx}x{case.ny} cells of the "
                        "headline workload (seeded face fluxes, Re 1e5)"}
@@ -515,8 +516,7 @@ def extra_lsweep(case, local, args):
     with device-resident fields, against the C restatement on one core."""
     import torch
     from simcoflow_gb300 import clsvof as CL
-    sys.path.insert(0, str(ROOT / "tests"))
-    from test_clsvof_oracle import ls_fields
+    from gen.synth import ls_fields
     nx, ny = case.nx, case.ny
     f = ls_fields(np.random.default_rng(29), nx, ny)
     t0 = np.asfortranarray(np.random.default_rng(30).standard_normal((nx, ny)))
@@ -552,7 +552,7 @@ def extra_cutcell(case, local, args):
     workload's grid and bodies, device-resident."""
     import torch
     from simcoflow_gb300 import cutcell as CU
-    from simcoflow_gb300 import synth
+    from gen import synth
     grids, fams = synth.cutcell_inputs(case)
     dev = torch.device("cuda", local)
     T = lambda a: torch.from_numpy(np.ascontiguousarray(a.ravel(order="F"))).to(dev)
@@ -577,7 +577,8 @@ def extra_cutcell(case, local, args):
 
 def extra_batch(local):
     """64 uneven instances in one graph launch with autotuned schedules."""
-    from simcoflow_gb300 import synth, batch as Bt
+    from gen import synth
+    from simcoflow_gb300 import batch as Bt
     cases = [synth.c5(instance=i) for i in range(64)]
     bp = Bt.BatchProjector(cases, precision="mixed", rtol=1e-8, maxit=300, device=local)
     try:

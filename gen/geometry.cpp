@@ -20,7 +20,7 @@
 #include <cstring>
 #include <vector>
 
-#include "../../include/scf_geom.h"
+#include "scf_geom.h"
 
 namespace {
 

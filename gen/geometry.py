@@ -1,4 +1,4 @@
-"""ctypes binding of libscf_geom.so (include/scf_geom.h): builds the cut-cell
+"""ctypes binding of libscf_gen.so (gen/scf_geom.h): builds the cut-cell
 geometry of a synthetic projection case in the reference's Fortran layouts.
 
 Restates, for synthetic solids and free surfaces, Initial_Grid/InitialUVGrid
@@ -13,7 +13,7 @@ from pathlib import Path
 
 import numpy as np
 
-_LIB = Path(__file__).resolve().parent / "_lib" / "libscf_geom.so"
+_LIB = Path(__file__).resolve().parent / "_lib" / "libscf_gen.so"
 _lib = None
 
 SOLID_CIRCLE = 0
@@ -43,12 +43,21 @@ class _Out(C.Structure):
                                   "vofS_u_in", "vofS_v_in")]
 
 
+def use_library(path) -> None:
+    """Load the generator from another build of geometry.cpp (the CPU arm of
+    the benchmark uses the oracle's copy); call before the first case."""
+    global _LIB, _lib
+    if _lib is not None and Path(path) != _LIB:
+        raise RuntimeError("the generator library is already loaded")
+    _LIB = Path(path)
+
+
 def _load():
     global _lib
     if _lib is None:
         if not _LIB.exists():
             from . import build
-            build.build_geom()
+            build.build()
         lib = C.CDLL(str(_LIB))
         lib.scf_geom_axis.restype = C.c_int
         lib.scf_geom_axis.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, C.c_double,

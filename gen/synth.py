@@ -191,6 +191,26 @@ def random_instance(config: int, n: int, instance: int, nmodes: int = 16, dt: fl
                       meta={"ratio": ratio, "ncirc": ncirc})
 
 
+def walls(n: int = 128, instance: int = 0, seed=None, ny: int | None = None) -> Case:
+    """Parity workload whose solids cut the first and last rows and the
+    first and last columns: circles centred on or just inside the W, S, N
+    and E walls, a two-mode surface crossing many faces.  The reference
+    averages the two cells' apertures of a face only for i, j = 2..N-1
+    (src/Cutcell_Mod.f90:161-204), so on these rows and columns the W / S
+    entry of a row and the E / N entry of its neighbour differ (by a few
+    per cent here): the assembled matrix is not symmetric."""
+    rng = _rng(6, instance, seed)
+    ny = n if ny is None else ny
+    xf = G.axis(n + 1, 0.0, 1.0)
+    yf = G.axis(ny + 1, 0.0, 1.0)
+    solids = [G.Solid(G.SOLID_CIRCLE, 0.02, 0.3, r=0.08), G.Solid(G.SOLID_CIRCLE, 0.6, 0.01, r=0.06),
+              G.Solid(G.SOLID_CIRCLE, 0.3, 0.99, r=0.05), G.Solid(G.SOLID_CIRCLE, 0.985, 0.7, r=0.05)]
+    surf = G.Surface(0.5, [0.03, 0.01], [4 * np.pi, 10 * np.pi],
+                     [float(rng.uniform(0, 2 * np.pi)), float(rng.uniform(0, 2 * np.pi))])
+    mu, mv = _modes(rng, 16), _modes(rng, 16)
+    return build_case("walls", xf, yf, solids, surf, mu, mv, 1e-3, RHO_W / 1.2, vb=0.0)
+
+
 def c4(n: int = 512, instance: int = 0, seed=None) -> Case:
     return random_instance(4, n, instance, seed=seed)
 
@@ -206,7 +226,7 @@ def c5(instance: int = 0, n: int | None = None, seed=None) -> Case:
     return random_instance(5, side, instance, nmodes=16, dt=1e-3, seed=seed)
 
 
-CONFIGS = {"c1": c1, "c2": c2, "c3": c3, "c4": c4, "c5": c5}
+CONFIGS = {"c1": c1, "c2": c2, "c3": c3, "c4": c4, "c5": c5, "walls": walls}
 
 
 def make_case(name: str, **kw) -> Case:
@@ -374,3 +394,27 @@ def cutcell_inputs(case: Case):
         circles.append((s.cx, s.cy, s.r))
     grids = family_grids(case.meta["xf"], case.meta["yf"])
     return grids, family_fields(grids, circles)
+
+
+# ---------------------------------------------------------------------------
+# Inputs of the CLSVOF sweeps' level-set transport (scf_ls_sweep)
+# ---------------------------------------------------------------------------
+def ls_fields(rng, nx, ny):
+    """Random inputs of one CLSVOF level-set sweep (scf_ls_sweep) on an nx x ny
+    grid: level set, solid fractions, spacings and centres, face apertures
+    (some closed), face velocities ue (nx+1,ny) and ve (nx,ny+1)."""
+    F = np.asfortranarray
+    x = np.cumsum(rng.uniform(0.5, 1.5, nx))
+    y = np.cumsum(rng.uniform(0.5, 1.5, ny))
+    dx = F(np.broadcast_to(np.gradient(x)[:, None], (nx, ny)).copy())
+    dy = F(np.broadcast_to(np.gradient(y)[None, :], (nx, ny)).copy())
+    f = {"phi": F(rng.standard_normal((nx, ny))),
+         "vofS": F(rng.choice([0.0, 0.0, 0.3, 1.0], (nx, ny))),
+         "dx": dx, "dy": dy,
+         "x": F(np.broadcast_to(x[:, None], (nx, ny)).copy()),
+         "y": F(np.broadcast_to(y[None, :], (nx, ny)).copy())}
+    for k in ("aE", "aW", "aN", "aS"):
+        f[k] = F(rng.choice([0.0, 0.5, 1.0], (nx + 2, ny + 2)) * rng.uniform(0.5, 1, (nx + 2, ny + 2)))
+    f["ue"] = F(rng.standard_normal((nx + 1, ny)))
+    f["ve"] = F(rng.standard_normal((nx, ny + 1)))
+    return f

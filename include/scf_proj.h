@@ -105,7 +105,10 @@ typedef struct scf_stats {
     int learned_iters;  /* iterations preconditioned by the network (SCF_PRECOND_LEARNED) */
     int launches;       /* kernel launches of this call, graph nodes counted per
                            execution, including those of the assembly before it */
-    int reserved_i;
+    int asym_faces;     /* faces whose two rows carry different entries (the
+                           reference forms a row's W/S entries from the row's
+                           own cell, src/ProjectionP_Mod.f90:176-195); the
+                           solve applies those rows exactly */
 } scf_stats;
 
 typedef struct scf_proj scf_proj;
@@ -244,12 +247,41 @@ int scf_proj_get_geometry(scf_proj *h, double *vofS, double *nxS, double *nyS, d
                           int32_t *posnu_u, int32_t *posnu_v, int32_t *moex_u,
                           int32_t *moex_v, double *vofS_u, double *vofS_v);
 
-/* Diagnostics: the assembled symmetric operator in Fortran (nx,ny) layout.
+/* Diagnostics: the east / north entries and the diagonal of the assembled
+ * rows in Fortran (nx,ny) layout (the full rows: scf_proj_get_matrix).
  * cE(i,j) = -A(row(i,j), row(i+1,j)), cN(i,j) = -A(row(i,j), row(i,j+1)),
  * diag(i,j) = A(row(i,j), row(i,j)) (-1 where Posnu = -1); rhs (nx,ny) is
  * the last right-hand side (0 where Posnu = -1).  Any pointer may be NULL;
  * always host pointers. */
 int scf_proj_get_operator(scf_proj *h, double *cE, double *cN, double *diag, double *rhs);
+
+/* The assembled matrix as the reference's dense copy matr(Isize,Jsize,5)
+ * of SetPoissonMatrix (src/ProjectionP_Mod.f90:176-230, written at :183,
+ * :193, :228, :240, :250): per cell the S, W, diagonal, E and N entries of
+ * its row, off-diagonals negated, 0 where the row has no entry and on cells
+ * with Posnu = -1.  Each row's W and S entries are the row's own
+ * (PoCoef(i,j,2)*WEdge_Area(i,j), PoCoef(i,j,1)*SEdge_Area(i,j)), which may
+ * differ from the neighbouring row's E / N entry: in the last bits where an
+ * interface face's density weight is formed from either side
+ * (:415-418 against :493-498), and by more on the first and last rows and
+ * columns, whose face apertures the reference does not average
+ * (src/Cutcell_Mod.f90:161-204).  The solve applies every row as written.
+ * asym_faces (may be NULL) receives the number of faces whose two entries
+ * differ, asym_max (may be NULL) the largest relative difference.  matr may
+ * be NULL; host pointers always. */
+int scf_proj_get_matrix(scf_proj *h, double *matr, int *asym_faces, double *asym_max);
+
+/* Fault injection for tests of the bounded device waits (the reference's
+ * only failure mechanism is a pause, src/ProjectionP_Mod.f90:209-213; here
+ * a wait that runs out returns SCF_ERR_TIMEOUT).  On `device`, every later
+ * TMA-staged sweep (mixed precision, levels of at least 128 x 64 cells) that
+ * reduces nothing across the grid lets its CTA of linear index `cta` arm its
+ * shared-memory barrier without issuing the copies, so that CTA's wait runs
+ * out after `spins` polls of at most about a microsecond each: the solve
+ * returns SCF_ERR_TIMEOUT with no copy in flight.  cta = -1 and
+ * spins = 1048576 restore normal operation.  Re-assemble (or use a new
+ * handle) after an injected timeout.  Device-wide; not for production use. */
+int scf_diag_tma_timeout(int device, int cta, int spins);
 
 /* Diagnostics: apply one multigrid V-cycle (the preconditioner) to b and
  * return x, both host arrays in Fortran (nx,ny) layout. */
@@ -299,7 +331,8 @@ int scf_diag_divide(const double *a, const double *b, double *q, int64_t n, int 
  *    outputs are valid once the stream has passed this call.
  *  - The first call on each device looks up the scratch array's device
  *    address (cudaGetSymbolAddress); make that first call on a device before
- *    any stream capture.
+ *    any stream capture.  Only a lookup that succeeded is kept; after a
+ *    failed one (SCF_ERR_CUDA) the next call looks the address up again.
  *  - All calls share the one scratch array, which keeps the last call's
  *    contents: calls that overlap on the GPU (different streams or host
  *    threads) race, so the caller must serialise them. */

@@ -2,7 +2,10 @@
 
 Compiles oracle/scf_oracle.c (projection), oracle/mom_oracle.c (momentum
 predictor solves) and oracle/out_oracle.c (Tecplot result files) into
-oracle/_build/liboracle.so with gcc.
+oracle/_build/liboracle.so with gcc, and a copy of the synthetic-input
+generator (gen/geometry.cpp) into oracle/_build/libgeom.so, so that the
+CPU arm of the benchmark builds its inputs without loading anything of the
+product package.
 -ffp-contract=off keeps every multiply and add separately rounded, as in
 the reference's Fortran build (mpif77 without FMA flags), so that the
 restatement gives the same bits on x86-64 and aarch64.
@@ -14,6 +17,7 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_build" / "liboracle.so"
+GEOM = HERE / "_build" / "libgeom.so"
 
 
 def build(force: bool = False) -> Path:
@@ -30,5 +34,15 @@ def build(force: bool = False) -> Path:
     return OUT
 
 
+def geom_lib(force: bool = False) -> Path:
+    """The oracle's build of the synthetic-input generator."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_gen_build", HERE.parent / "gen" / "build.py")
+    gb = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gb)
+    return gb.compile_to(GEOM, force)
+
+
 if __name__ == "__main__":
     print(build(force=True))
+    print(geom_lib(force=True))

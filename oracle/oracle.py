@@ -77,7 +77,7 @@ def lib():
         L.oracle_row_residual.restype = C.c_double
         L.oracle_row_residual.argtypes = [C.c_int, C.c_int, _P, _P, _P, _I]
         L.oracle_mgpcg.restype = C.c_int
-        L.oracle_mgpcg.argtypes = [C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_double, C.c_int,
+        L.oracle_mgpcg.argtypes = [C.c_int, C.c_int, _P, _P, _P, _P, _P, _P, _P, C.c_double, C.c_int,
                                    C.c_int, C.c_int, C.c_double, C.c_int, _P, C.POINTER(C.c_int),
                                    C.c_int]
         L.oracle_vcycle.argtypes = [C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_int, C.c_int,
@@ -200,7 +200,7 @@ def solve_direct(A, b) -> np.ndarray:
 
 
 def symmetric_operator(case, matr):
-    """The symmetric 5-point storage of the CUDA path built from matr:
+    """The symmetric 5-point storage of the multigrid built from matr:
     cE = -matr(.,.,4), cN = -matr(.,.,5), dg = matr(.,.,3) (-1 without an
     unknown), in 0-based C order (ny, nx) flattened."""
     nx, ny = case.nx, case.ny
@@ -212,16 +212,31 @@ def symmetric_operator(case, matr):
     return f(cE), f(cN), f(dg)
 
 
+def own_west_south(case, matr):
+    """Each row's own west and south couplings, -matr(.,.,2) and
+    -matr(.,.,1) (src/ProjectionP_Mod.f90:183,193), in the same 0-based
+    order; the PCG applies the rows with them."""
+    nx, ny = case.nx, case.ny
+    act = case["posnu_p"][1:nx + 1, 1:ny + 1] != -1
+    cW = np.where(act, -matr[:, :, 1], 0.0) + 0.0
+    cS = np.where(act, -matr[:, :, 0], 0.0) + 0.0
+    f = lambda a: np.ascontiguousarray(a.T).ravel()
+    return f(cW), f(cS)
+
+
 SMOOTHERS = {"point": 0, "line": 1}
 
 
 def mgpcg(case, matr, rhm, rtol=1e-13, maxit=500, npre=2, npost=2, omega=1.9, coarse_max=64,
           threads=0, smoother="point"):
-    """CPU FP64 MG-PCG on the symmetric operator.  Returns (Pp-interior x as
-    (nx,ny) Fortran array, iterations, true relres, levels).  smoother:
-    'point' (red-black Gauss-Seidel) or 'line' (alternating zebra lines)."""
+    """CPU FP64 MG-PCG: the PCG applies the assembled rows as written (own
+    west / south entries), the V-cycle preconditioner the symmetric storage.
+    Returns (Pp-interior x as (nx,ny) Fortran array, iterations, true relres,
+    levels).  smoother: 'point' (red-black Gauss-Seidel) or 'line'
+    (alternating zebra lines)."""
     nx, ny = case.nx, case.ny
     cE, cN, dg = symmetric_operator(case, matr)
+    cW, cS = own_west_south(case, matr)
     b = np.ascontiguousarray(rhm.T).ravel()
     x = np.zeros(nx * ny)
     rel = C.c_double(0.0)
@@ -229,7 +244,8 @@ def mgpcg(case, matr, rhm, rtol=1e-13, maxit=500, npre=2, npost=2, omega=1.9, co
     if threads:
         lib().oracle_set_threads(threads)
     it = lib().oracle_mgpcg(nx, ny, cE.ctypes.data_as(_P), cN.ctypes.data_as(_P),
-                            dg.ctypes.data_as(_P), b.ctypes.data_as(_P), x.ctypes.data_as(_P),
+                            dg.ctypes.data_as(_P), cW.ctypes.data_as(_P), cS.ctypes.data_as(_P),
+                            b.ctypes.data_as(_P), x.ctypes.data_as(_P),
                             rtol, maxit, npre, npost, omega, coarse_max, C.byref(rel),
                             C.byref(nlev), SMOOTHERS[smoother])
     return np.asfortranarray(x.reshape(ny, nx).T), it, rel.value, nlev.value

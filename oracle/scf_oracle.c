@@ -446,6 +446,9 @@ double oracle_row_residual(int nx, int ny, const double *matr, const double *Pp,
  * as the timed CPU baseline.  Symmetric 5-point storage per level:
  *   cE(i,j): coupling of (i,j) and (i+1,j); cN(i,j): of (i,j) and (i,j+1);
  *   dg(i,j): diagonal; a cell without an unknown has dg = -1 and no couplings.
+ * The PCG's own operator applies the rows as assembled: the optional cW /
+ * cS of oracle_mgpcg are each row's own west / south couplings
+ * (-matr(.,.,2), -matr(.,.,1)), which may differ from the neighbour's cE / cN.
  * The fine level is taken from matr: cE = -matr(.,.,4), cN = -matr(.,.,5),
  * dg = matr(.,.,3).  Coarse levels are the Galerkin product P^T A P with
  * piecewise-constant 2x2 aggregation, computed as summed couplings plus the
@@ -461,6 +464,12 @@ typedef struct {
     int nx, ny;
     double *cE, *cN, *dg, *ex;
     double *x, *b, *r;
+    /* fine level of the PCG operator only (NULL elsewhere): each row's own
+       west / south couplings, -matr(.,.,2) and -matr(.,.,1).  The reference
+       forms them from the row's cell (src/ProjectionP_Mod.f90:183,193), so
+       they may differ from the neighbour's cE / cN; the V-cycle uses the
+       symmetric cE / cN. */
+    const double *cW, *cS;
 } olevel;
 
 typedef struct {
@@ -746,9 +755,9 @@ static void apply_A(const olevel *L, const double *p, double *q) {
             size_t k = (size_t)iy * nx + ix;
             double s = (L->dg[k] > 0.0 ? L->dg[k] : 0.0) * p[k];
             if (ix + 1 < nx) s = s - L->cE[k] * p[k + 1];
-            if (ix > 0) s = s - L->cE[k - 1] * p[k - 1];
+            if (ix > 0) s = s - (L->cW ? L->cW[k] : L->cE[k - 1]) * p[k - 1];
             if (iy + 1 < ny) s = s - L->cN[k] * p[k + nx];
-            if (iy > 0) s = s - L->cN[k - nx] * p[k - nx];
+            if (iy > 0) s = s - (L->cS ? L->cS[k] : L->cN[k - nx]) * p[k - nx];
             q[k] = s;
         }
 }
@@ -762,6 +771,7 @@ static void apply_A(const olevel *L, const double *p, double *q) {
  * iterations = (-maxit)%1000.
  */
 int oracle_mgpcg(int nx, int ny, const double *cE, const double *cN, const double *dg,
+                 const double *cW, const double *cS,
                  const double *b, double *x, double rtol, int maxit, int npre, int npost,
                  double omega, int coarse_max, double *relres, int *nlev_out, int smoother) {
     omg M;
@@ -783,6 +793,10 @@ int oracle_mgpcg(int nx, int ny, const double *cE, const double *cN, const doubl
     }
     coarse_factor(&M);
     if (nlev_out) *nlev_out = M.nlev;
+    /* the PCG applies the rows as assembled (the V-cycle never reads these) */
+    olevel Fx = M.lev[0];
+    Fx.cW = cW;
+    Fx.cS = cS;
     olevel *F = &M.lev[0];
     double *r = dalloc(n), *z = dalloc(n), *p = dalloc(n), *q = dalloc(n);
     for (size_t k = 0; k < n; ++k) { x[k] = 0.0; r[k] = b[k]; }
@@ -796,7 +810,7 @@ int oracle_mgpcg(int nx, int ny, const double *cE, const double *cN, const doubl
         vcycle(&M, 0);
         memcpy(z, F->x, n * sizeof(double));
         for (int c = 1; c < ncyc; ++c) {
-            apply_A(F, z, q);
+            apply_A(&Fx, z, q);
             for (size_t k = 0; k < n; ++k) F->b[k] = r[k] - q[k];
             vcycle(&M, 0);
             for (size_t k = 0; k < n; ++k) z[k] += F->x[k];
@@ -809,14 +823,14 @@ int oracle_mgpcg(int nx, int ny, const double *cE, const double *cN, const doubl
             for (size_t k = 0; k < n; ++k) p[k] = z[k] + beta * p[k];
         }
         rz = rz_new;
-        apply_A(F, p, q);
+        apply_A(&Fx, p, q);
         double alpha = rz / dot(p, q, n);
 #pragma omp parallel for schedule(static)
         for (size_t k = 0; k < n; ++k) { x[k] += alpha * p[k]; r[k] -= alpha * q[k]; }
         double rn = sqrt(dot(r, r, n));
         if (rn <= rtol * bnorm) { it++; break; }
     }
-    apply_A(F, x, q);
+    apply_A(&Fx, x, q);
     {
         double s = 0.0;
         for (size_t k = 0; k < n; ++k) { double d = b[k] - q[k]; s += d * d; }

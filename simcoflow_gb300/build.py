@@ -1,7 +1,6 @@
 """Build the native libraries of simcoflow_gb300 in-tree.
 
 libscf_proj.so  CUDA kernels + C-ABI (include/scf_proj.h), sm_103a only
-libscf_geom.so  host geometry builder (include/scf_geom.h)
 
 Objects and libraries go to simcoflow_gb300/_lib/ (git-ignored).  Each CUDA
 translation unit is compiled in its own nvcc process, in parallel.
@@ -72,22 +71,8 @@ def build_proj(force: bool = False, verbose: bool = False) -> Path:
     return out
 
 
-def build_geom(force: bool = False) -> Path:
-    LIB.mkdir(exist_ok=True)
-    out = LIB / "libscf_geom.so"
-    src = CSRC / "geometry.cpp"
-    if force or _stale(out, [src, INCLUDE / "scf_geom.h"]):
-        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-              "-I", str(INCLUDE), str(src), "-o", str(out)])
-    return out
-
-
 def build_all(force: bool = False) -> None:
-    with ThreadPoolExecutor(max_workers=2) as ex:
-        f1 = ex.submit(build_proj, force)
-        f2 = ex.submit(build_geom, force)
-        f1.result()
-        f2.result()
+    build_proj(force)
 
 
 if __name__ == "__main__":

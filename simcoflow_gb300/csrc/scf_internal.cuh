@@ -30,6 +30,20 @@ struct LevelView {
   double* ex;  // diagonal excess dg - sum of couplings, clamped at 0
   double* x;   // iterate / correction
   double* b;   // right-hand side
+  // Fine level only (null on coarser levels).  The reference writes each
+  // row's west and south entries from the row's own cell (PoCoef(i,j,2) *
+  // WEdge_Area(i,j), PoCoef(i,j,1) * SEdge_Area(i,j)), not from the
+  // neighbour's east / north entry; the two differ in rounding where the
+  // density weight of an interface face is formed from either side, and by
+  // more where the face apertures of the two cells were not averaged (the
+  // first and last rows and columns).  wW / wS hold the row's own entries
+  // (magnitudes, 0 where the row has none) and arow[iy] != 0 marks the rows
+  // where some cell's entry differs from its neighbour's cE / cN.  The FP64
+  // operator of the PCG (q = A p, the true residual) uses them; the
+  // multigrid preconditioner uses the symmetric cE / cN.
+  double* wW;
+  double* wS;
+  int* arow;
 };
 
 // Fortran-layout inputs of the assembly, right-hand side and correction.
@@ -54,6 +68,10 @@ struct Scalars {
   int pad[2];  // pad[0]: guard counter of the graph loop
   int anan;    // NaN or Inf met by the operator setup (kept until the next assembly)
   unsigned tickets[8];  // last-block counters, one per reduction site
+  // set by the assembly: faces whose two rows' entries differ, and the
+  // largest relative difference (float bits); kept until the next assembly
+  int asym_faces;
+  unsigned asym_max_bits;
 };
 
 enum Ticket { T_RHS = 0, T_RZ, T_PQ, T_RR, T_RES, T_MRES, T_DOT };
@@ -244,7 +262,9 @@ inline dim3 grid_for(int nx, int ny, int cells_per_thread_x = 2) {
 // ---- kernel launchers (scf_kernels.cu) ----
 void launch_assemble(const FortranIn& in, LevelView L0, Scalars* sc, cudaStream_t s);
 void launch_divide(const double* a, const double* b, double* q, long long n, cudaStream_t s);
-void launch_excess(LevelView L, double* di, unsigned* zero_bits, int nzero, cudaStream_t s);
+void launch_matr_out(const FortranIn& in, LevelView L0, double* matr, cudaStream_t s);
+void launch_excess(LevelView L, double* di, unsigned* zero_bits, int nzero, Scalars* sc,
+                   cudaStream_t s);
 void launch_coarsen(LevelView F, LevelView C, double* di, cudaStream_t s);
 void launch_coarse_setup(LevelView C, double* Ainv, int* cmap, int* nc, cudaStream_t s);
 void launch_rhs(const FortranIn& in, const double* ustar, const double* vstar, double vb,

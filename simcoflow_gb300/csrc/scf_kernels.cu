@@ -284,8 +284,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_assemble(FortranIn in, LevelVie
     prevN = f[3];
     prevNpc = pc[3];
     if (!in_x) continue;
+    if (ix == 0) L.arow[iy] = 0;  // raised by k_excess where the row's entries differ
     if (!act) {
       L.cE[kl] = 0.0; L.cN[kl] = 0.0; L.dg[kl] = -1.0;
+      L.wW[kl] = 0.0; L.wS[kl] = 0.0;
       continue;
     }
     const double aS = in.aS[k0], aW = in.aW[k0], aE = in.aE[k0], aN = in.aN[k0];
@@ -300,6 +302,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_assemble(FortranIn in, LevelVie
     L.dg[kl] = d;
     L.cE[kl] = (i < nx && in.posnu_p[fo0(nx, i + 1, j)] != -1) ? tE : 0.0;
     L.cN[kl] = (j < ny && in.posnu_p[fo0(nx, i, j + 1)] != -1) ? tN : 0.0;
+    // the row's own west / south entries (src/ProjectionP_Mod.f90:176-195)
+    L.wW[kl] = (i > 1 && in.posnu_p[fo0(nx, i - 1, j)] != -1) ? tW : 0.0;
+    L.wS[kl] = (j > 1 && in.posnu_p[fo0(nx, i, j - 1)] != -1) ? tS : 0.0;
   }
 }
 
@@ -308,20 +313,49 @@ __global__ void __launch_bounds__(kThreads, 4) k_assemble(FortranIn in, LevelVie
 // the mixed-precision hierarchy builds its own FP32 inverse diagonals)
 // also clears the per-level largest-coupling words (zero_bits, nzero) that
 // the mixed setup's k_max_coupling raises after this kernel
-__global__ void k_excess(LevelView L, double* di, unsigned* zero_bits, int nzero) {
+//
+// On the fine level (L.wW set) it also compares every row's own west / south
+// entries with the neighbours' east / north ones, raises arow for the rows
+// where one differs, and counts those faces and their largest relative
+// difference into the solve's scalars.
+__global__ void k_excess(LevelView L, double* di, unsigned* zero_bits, int nzero, Scalars* sc) {
   pdl_wait();
   if (zero_bits && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.y == 0 && threadIdx.x < nzero)
     zero_bits[threadIdx.x] = 0u;
   const int ix = blockIdx.x * kBX + threadIdx.x;
-  if (ix >= L.nx) return;
-  for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY) {
-    const size_t k = (size_t)iy * L.pitch + ix;
-    const double d = L.dg[k];
-    if (di) di[k] = d > 0.0 ? 1.0 / d : 0.0;
-    if (d < 0.0) { L.ex[k] = 0.0; continue; }
-    double s = add(add(add(L.cE[k], L.cE[k - 1]), L.cN[k]), L.cN[k - L.pitch]);
-    double e = sub(d, s);
-    L.ex[k] = e > 0.0 ? e : 0.0;
+  int nasym = 0;
+  float rmax = 0.0f;
+  if (ix < L.nx) {
+    for (int iy = blockIdx.y * kBY + threadIdx.y; iy < L.ny; iy += gridDim.y * kBY) {
+      const size_t k = (size_t)iy * L.pitch + ix;
+      const double d = L.dg[k];
+      if (di) di[k] = d > 0.0 ? 1.0 / d : 0.0;
+      if (d < 0.0) { L.ex[k] = 0.0; continue; }
+      const double cw = L.cE[k - 1], cs = L.cN[k - L.pitch];
+      double s = add(add(add(L.cE[k], cw), L.cN[k]), cs);
+      double e = sub(d, s);
+      L.ex[k] = e > 0.0 ? e : 0.0;
+      if (L.wW) {
+        const double ww = L.wW[k], ws = L.wS[k];
+        const bool dw = ww != cw, ds = ws != cs;
+        if (dw || ds) {
+          L.arow[iy] = 1;
+          nasym += (int)dw + (int)ds;
+          if (dw) rmax = fmaxf(rmax, (float)(fabs(ww - cw) / fmax(fabs(ww), fabs(cw))));
+          if (ds) rmax = fmaxf(rmax, (float)(fabs(ws - cs) / fmax(fabs(ws), fabs(cs))));
+        }
+      }
+    }
+  }
+  if (L.wW && sc) {
+    for (int o = 16; o > 0; o >>= 1) {
+      nasym += __shfl_down_sync(0xffffffffu, nasym, o);
+      rmax = fmaxf(rmax, __shfl_down_sync(0xffffffffu, rmax, o));
+    }
+    if (threadIdx.x == 0 && nasym > 0) {
+      atomicAdd(&sc->asym_faces, nasym);
+      atomicMax(&sc->asym_max_bits, __float_as_uint(rmax));
+    }
   }
 }
 
@@ -715,8 +749,10 @@ k_final_solution(FortranIn in, LevelView L, const double* __restrict__ x,
         }
       }
       if (act) {
-        double ax = pos_part(L.dg[kl]) * x[kl] - L.cE[kl] * x[kl + 1] - L.cE[kl - 1] * x[kl - 1] -
-                    L.cN[kl] * x[kl + P] - L.cN[kl - P] * x[kl - P];
+        const bool own = L.arow && L.arow[iy];  // the row's own west / south entries
+        const double cw = own ? L.wW[kl] : L.cE[kl - 1], cs = own ? L.wS[kl] : L.cN[kl - P];
+        double ax = pos_part(L.dg[kl]) * x[kl] - L.cE[kl] * x[kl + 1] - cw * x[kl - 1] -
+                    L.cN[kl] * x[kl + P] - cs * x[kl - P];
         double rr = bvec[kl] - ax;
         acc = fma(rr, rr, acc);
       }
@@ -793,6 +829,32 @@ __global__ void k_final_zero(FortranIn in, double* p, double* u, double* v) {
   }
 }
 
+// The reference's dense copy matr(Isize,Jsize,5) of the assembled rows
+// (src/ProjectionP_Mod.f90:176-230): S, W, diagonal, E, N entries of each
+// row, negated couplings off the diagonal, 0 where the row has no entry and
+// on cells without an unknown.
+__global__ void k_matr_out(FortranIn in, LevelView L, double* __restrict__ matr) {
+  pdl_wait();
+  const int nx = in.nx, ny = in.ny;
+  const int ix = blockIdx.x * kBX + threadIdx.x;
+  if (ix >= nx) return;
+  const size_t n1 = (size_t)nx * ny;
+  for (int iy = blockIdx.y * kBY + threadIdx.y; iy < ny; iy += gridDim.y * kBY) {
+    const int i = ix + 1, j = iy + 1;
+    const size_t k1 = fo1(nx, i, j), kl = (size_t)iy * L.pitch + ix;
+    double m[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    if (in.posnu_p[fo0(nx, i, j)] != -1) {
+      if (j > 1 && in.posnu_p[fo0(nx, i, j - 1)] != -1) m[0] = -L.wS[kl];
+      if (i > 1 && in.posnu_p[fo0(nx, i - 1, j)] != -1) m[1] = -L.wW[kl];
+      m[2] = L.dg[kl];
+      if (i < nx && in.posnu_p[fo0(nx, i + 1, j)] != -1) m[3] = -L.cE[kl];
+      if (j < ny && in.posnu_p[fo0(nx, i, j + 1)] != -1) m[4] = -L.cN[kl];
+    }
+#pragma unroll
+    for (int f = 0; f < 5; ++f) matr[k1 + f * n1] = m[f];
+  }
+}
+
 // the assembly's division on arrays (diagnostics)
 __global__ void k_divide(const double* a, const double* b, double* q, long long n) {
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
@@ -839,11 +901,15 @@ static const dim3 kBlock(kBX, kBY);
 void launch_assemble(const FortranIn& in, LevelView L0, Scalars* sc, cudaStream_t s) {
   launch_k(k_assemble, grid_for(in.nx, in.ny, 1), kBlock, 0, s, in, L0, sc);
 }
+void launch_matr_out(const FortranIn& in, LevelView L0, double* matr, cudaStream_t s) {
+  launch_k(k_matr_out, grid_for(in.nx, in.ny, 1), kBlock, 0, s, in, L0, matr);
+}
 void launch_divide(const double* a, const double* b, double* q, long long n, cudaStream_t s) {
   launch_k(k_divide, dim3(152 * 8), dim3(256), 0, s, a, b, q, n);
 }
-void launch_excess(LevelView L, double* di, unsigned* zero_bits, int nzero, cudaStream_t s) {
-  launch_k(k_excess, grid_for(L.nx, L.ny, 1), kBlock, 0, s, L, di, zero_bits, nzero);
+void launch_excess(LevelView L, double* di, unsigned* zero_bits, int nzero, Scalars* sc,
+                   cudaStream_t s) {
+  launch_k(k_excess, grid_for(L.nx, L.ny, 1), kBlock, 0, s, L, di, zero_bits, nzero, sc);
 }
 void launch_coarsen(LevelView F, LevelView C, double* di, cudaStream_t s) {
   launch_k(k_coarsen, grid_for(C.nx, C.ny, 1), kBlock, 0, s, F, C, di);

@@ -224,14 +224,18 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
                "r"(bytes)
                : "memory");
 }
+// One bounded poll: the thread may be suspended inside try_wait until the
+// phase completes, but for at most kPollNs nanoseconds (the suspend-time
+// hint), so kMbarSpins polls take at most about a second.
+constexpr unsigned kPollNs = 1024;
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   unsigned ok;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity)
+      : "r"(smem_addr(bar)), "r"(parity), "n"(kPollNs)
       : "memory");
   return ok != 0;
 }
@@ -253,6 +257,12 @@ constexpr int kOffB = r128(kBoxF32), kOffD = 2 * r128(kBoxF32), kOffE = 3 * r128
 constexpr int kOffN = kOffE + r128(kBoxBF16), kOffBar = kOffN + r128(kBoxBF16);
 constexpr int kTmaSmem = 128 + kOffBar + 16;  // + slack to align the base
 constexpr int kMbarSpins = 1 << 20;
+// Fault injection for tests (scf_diag_tma_timeout): the CTA with this linear
+// index, in launches that reduce nothing across the grid, arms its barrier
+// without issuing its copies -- nothing is in flight, so its bounded wait
+// runs out -- and every wait polls at most g_tma_spins times.
+__device__ int g_tma_skip_cta = -1;
+__device__ int g_tma_spins = kMbarSpins;
 
 template <int FIRST, bool ZERO, bool PROLONG, bool RESTRICT, bool RZ, int ITER>
 __global__ void __launch_bounds__(NT)
@@ -276,6 +286,8 @@ k_sweep_tma(MgView<float, __nv_bfloat16, float> L, MgView<float, __nv_bfloat16, 
   const int wx0 = x0 - OX, wy0 = y0 - OY;  // window origin (x: a multiple of 8)
   const int t = tlin();
   const float cs = L.csp ? __ldg(L.csp) : 1.0f;
+  const int spins = g_tma_spins;
+  const bool skip = !RZ && (int)(blockIdx.y * gridDim.x + blockIdx.x) == g_tma_skip_cta;
   if (t == 0) {
     mbar_init(bar, 1);
     mbar_init_fence();
@@ -283,11 +295,13 @@ k_sweep_tma(MgView<float, __nv_bfloat16, float> L, MgView<float, __nv_bfloat16, 
   __syncthreads();
   if (t == 0) {
     mbar_expect_tx(bar, (ZERO ? 0u : (unsigned)kBoxF32) + 2u * kBoxF32 + 2u * kBoxBF16);
-    if (!ZERO) tma_load_2d(xw, maps + xin, wx0, wy0, bar);
-    tma_load_2d(bw, maps + 2, wx0, wy0, bar);
-    tma_load_2d(dw, maps + 3, wx0, wy0, bar);
-    tma_load_2d(ew, maps + 4, wx0, wy0, bar);
-    tma_load_2d(nw, maps + 5, wx0, wy0, bar);
+    if (!skip) {
+      if (!ZERO) tma_load_2d(xw, maps + xin, wx0, wy0, bar);
+      tma_load_2d(bw, maps + 2, wx0, wy0, bar);
+      tma_load_2d(dw, maps + 3, wx0, wy0, bar);
+      tma_load_2d(ew, maps + 4, wx0, wy0, bar);
+      tma_load_2d(nw, maps + 5, wx0, wy0, bar);
+    }
   }
   if (ZERO)
     for (int e = t; e < kBoxCells; e += NT) xw[e] = 0.0f;
@@ -306,17 +320,18 @@ k_sweep_tma(MgView<float, __nv_bfloat16, float> L, MgView<float, __nv_bfloat16, 
     }
   }
   bool ok = false;
-  for (int it = 0; it < kMbarSpins && !ok; ++it) ok = mbar_try_wait(bar, 0);
-  if (!ok) {  // record, let the copies land (bounded), leave
+  for (int it = 0; it < spins && !ok; ++it) ok = mbar_try_wait(bar, 0);
+  // one decision for the whole block (the barrier also orders the window's
+  // shared-memory contents before the phases below)
+  if (!__syncthreads_and(ok)) {  // record, let the copies land (bounded), leave
     if (t == 0) {
       sc->status = kErrTimeout;
       sc->done = 1;
     }
-    for (int it = 0; it < kMbarSpins && !mbar_try_wait(bar, 0); ++it) {
+    for (int it = 0; it < spins && !mbar_try_wait(bar, 0); ++it) {
     }
     return;
   }
-  __syncthreads();
   auto W = [&](int gx, int gy) { return (gy - wy0) * kSweepBoxX + (gx - wx0); };
   if (PROLONG) {
 #pragma unroll
@@ -510,12 +525,19 @@ k_pupdate_spmv_t(LevelView L, const ZT* __restrict__ z, const ZT* __restrict__ p
       const double pp = wide(ppr);
       const double pl = __shfl_up_sync(0xffffffffu, pc, 1);
       const double pr = __shfl_down_sync(0xffffffffu, pc, 1);
-      const double cEl = __shfl_up_sync(0xffffffffu, cE, 1);
+      double cW = __shfl_up_sync(0xffffffffu, cE, 1), cS = cNd;
+      // rows whose own west / south entries differ from the neighbours'
+      // east / north ones take them from wW / wS (the row flag is the same
+      // for the whole warp)
+      if (L.arow && L.arow[iy] && col) {
+        cW = L.wW[k];
+        cS = L.wS[k];
+      }
       double qv = pos_part(dg) * pc;
       qv = fma(-cE, pr, qv);
-      qv = fma(-cEl, pl, qv);
+      qv = fma(-cW, pl, qv);
       qv = fma(-cN, pp, qv);
-      qv = fma(-cNd, pm, qv);
+      qv = fma(-cS, pm, qv);
       if (upd) {
         q[k] = qv;
         pnew[k] = pcr;
@@ -916,6 +938,13 @@ void launch_max_coupling(const LevelView& L, unsigned* out_bits, cudaStream_t s)
 void launch_to_mixed(const LevelView& F, const MgView<float, __nv_bfloat16, float>& M,
                      const unsigned* max_bits, float* cscale_out, cudaStream_t s) {
   launch_k(k_to_mixed, small_grid(F.nx, F.ny), dim3(32, 8), 0, s, F, M, max_bits, cscale_out);
+}
+
+int set_tma_fault(int cta, int spins) {
+  if (cudaMemcpyToSymbol(g_tma_skip_cta, &cta, sizeof(int)) != cudaSuccess ||
+      cudaMemcpyToSymbol(g_tma_spins, &spins, sizeof(int)) != cudaSuccess)
+    return -1;
+  return 0;
 }
 
 void launch_sweep_tma(const MgView<float, __nv_bfloat16, float>& L,

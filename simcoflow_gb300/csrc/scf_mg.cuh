@@ -68,6 +68,11 @@ constexpr int kSweepMaps = 6;                    // x0, x1, b, di, cE, cN
 // maps or refuses one
 bool make_sweep_maps(const MgView<float, __nv_bfloat16, float>& L, float* const xbuf[2],
                      const float* b, CUtensorMap* maps);
+// Fault injection for tests: in the TMA sweeps that reduce nothing across
+// the grid, the CTA of linear index `cta` (-1: none) arms its barrier without
+// issuing its copies, and every barrier wait polls at most `spins` times
+// (default 1 << 20).  Device-wide; returns 0 or -1 (CUDA error).
+int set_tma_fault(int cta, int spins);
 void launch_sweep_tma(const MgView<float, __nv_bfloat16, float>& L,
                       const MgView<float, __nv_bfloat16, float>& C, const CUtensorMap* maps,
                       int xin, int first, bool zero, bool prolong, bool restrict_, bool rz,

@@ -16,6 +16,7 @@
 // that loads the library holds it (about 33 KB) until the process exits.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <mutex>
@@ -105,11 +106,12 @@ __global__ void k_rhs_norm_noalloc(int nx, int ny, const double* __restrict__ us
   }
 }
 
-// Device address of g_rhs_scratch, looked up once per device.
+// Device address of g_rhs_scratch per device.  Only a successful lookup is
+// kept: a failed one (for example a first call made while its stream was
+// being captured) leaves the slot empty and the next call tries again.
 constexpr int kMaxDevices = 64;
-double* g_scratch_ptr[kMaxDevices];
-std::once_flag g_scratch_once[kMaxDevices];
-cudaError_t g_scratch_err[kMaxDevices];
+std::atomic<double*> g_scratch_ptr[kMaxDevices];
+std::mutex g_scratch_mu;
 
 }  // namespace
 
@@ -127,15 +129,19 @@ extern "C" int scf_rhs_norm_noalloc(int nx, int ny, const double* ustar, const d
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return SCF_ERR_CUDA;
   if (dev < 0 || dev >= kMaxDevices) return SCF_ERR_ARG;
-  // once per device, with that device current: the host-side name of the
-  // array is only a stand-in, the kernel needs its device address
-  std::call_once(g_scratch_once[dev], [dev]() {
-    void* p = nullptr;
-    g_scratch_err[dev] = cudaGetSymbolAddress(&p, g_rhs_scratch);
-    g_scratch_ptr[dev] = static_cast<double*>(p);
-  });
-  if (g_scratch_err[dev] != cudaSuccess || !g_scratch_ptr[dev]) return SCF_ERR_CUDA;
-  double* scratch = g_scratch_ptr[dev];
+  // with the device current, until one lookup succeeds: the host-side name
+  // of the array is only a stand-in, the kernel needs its device address
+  double* scratch = g_scratch_ptr[dev].load(std::memory_order_acquire);
+  if (!scratch) {
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    scratch = g_scratch_ptr[dev].load(std::memory_order_relaxed);
+    if (!scratch) {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_rhs_scratch) != cudaSuccess || !p) return SCF_ERR_CUDA;
+      scratch = static_cast<double*>(p);
+      g_scratch_ptr[dev].store(scratch, std::memory_order_release);
+    }
+  }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // the ticket must start at zero (a previous call that was cut short could
   // have left it set); memset does not allocate

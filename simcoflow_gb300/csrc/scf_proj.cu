@@ -451,7 +451,7 @@ void enqueue_setup(scf_proj* h, Scalars* sc, cudaStream_t s, bool fork = true) {
   // FP64 inverse diagonals serve the FP64 smoothers only; the mixed setup's
   // largest couplings restart from zero
   launch_excess(h->lev[0], h->mixed ? nullptr : h->di64[0], h->mixed ? h->maxbits : nullptr,
-                (int)nl, s);
+                (int)nl, sc, s);
   if (h->mixed && fork) convert(0);
   for (size_t l = 1; l < nl; ++l) {
     launch_coarsen(h->lev[l - 1], h->lev[l], h->mixed ? nullptr : h->di64[l], s);
@@ -910,6 +910,7 @@ int solve_common(scf_proj* h, const double* ustar, const double* vstar, double v
     if (h->graph_cond && h->gexec && !learned(h)) n += (long long)(S.pad[0] / 2) * h->body_launches;
     n += h->body_runs * h->body_launches;
     st->launches = (int)n;
+    st->asym_faces = S.asym_faces;
   }
   h->pending_launches = 0;
   return status == kOk ? SCF_OK : status;
@@ -1034,6 +1035,11 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
     if ((rc = level_array(h, ly, L.pitch, &di))) return fail(rc);
     double* x2 = nullptr;
     if ((rc = level_array(h, ly, L.pitch, &x2))) return fail(rc);
+    if (h->lev.empty()) {  // the fine level: the rows' own west / south entries
+      if ((rc = level_array(h, ly, L.pitch, &L.wW)) || (rc = level_array(h, ly, L.pitch, &L.wS)) ||
+          (rc = dev_alloc(h, (void**)&L.arow, sizeof(int) * (size_t)ly)))
+        return fail(rc);
+    }
     h->lev.push_back(L);
     h->di64.push_back(di);
     h->x2_64.push_back(x2);
@@ -1431,6 +1437,43 @@ int scf_proj_get_operator(scf_proj* h, double* cE, double* cN, double* diag, dou
   return rc;
 }
 
+int scf_diag_tma_timeout(int device, int cta, int spins) {
+  if (cta < -1 || spins < 1) return SCF_ERR_ARG;
+  CK(cudaSetDevice(device));
+  CK(cudaDeviceSynchronize());  // no sweep of an earlier call sees a half-set pair
+  return set_tma_fault(cta, spins) == 0 ? SCF_OK : SCF_ERR_CUDA;
+}
+
+int scf_proj_get_matrix(scf_proj* h, double* matr, int* asym_faces, double* asym_max) {
+  if (!h) return SCF_ERR_ARG;
+  if (!h->assembled) return SCF_ERR_STATE;
+  CK(cudaSetDevice(h->device));
+  const size_t n1 = (size_t)h->nx * h->ny;
+  int rc = SCF_OK;
+  if (matr) {
+    double* tmp = nullptr;
+    CK(cudaMallocAsync((void**)&tmp, 5 * n1 * 8, h->stream));
+    launch_matr_out(h->fin, h->lev[0], tmp, h->stream);
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(matr, tmp, 5 * n1 * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
+      rc = SCF_ERR_CUDA;
+    cudaFreeAsync(tmp, h->stream);
+  }
+  if (rc == SCF_OK)
+    CK(cudaMemcpyAsync(h->sc_host, h->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (rc == SCF_OK) {
+    if (asym_faces) *asym_faces = h->sc_host->asym_faces;
+    if (asym_max) {
+      unsigned b = h->sc_host->asym_max_bits;
+      float f;
+      memcpy(&f, &b, sizeof(f));
+      *asym_max = (double)f;
+    }
+  }
+  return rc;
+}
+
 int scf_proj_time_kernel(scf_proj* h, int kernel, int reps, double* ms) {
   if (!h || !ms || reps < 1 || kernel < 0 || kernel > SCF_K_SETUP) return SCF_ERR_ARG;
   if (!h->assembled) return SCF_ERR_STATE;
@@ -1515,6 +1558,10 @@ int scf_proj_time_kernel(scf_proj* h, int kernel, int reps, double* ms) {
   CK(cudaEventRecord(h->ev[5], s));
   for (int r = 0; r < reps; ++r) launch();
   CK(cudaEventRecord(h->ev[6], s));
+  // the assembly alone clears the row flags of the exact west / south
+  // entries; the excess pass raises them again (same operator, same bits)
+  if (kernel == SCF_K_ASSEMBLE)
+    launch_excess(L0, h->mixed ? nullptr : h->di64[0], nullptr, 0, h->sc_diag, s);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(s));
   if (vexec) cudaGraphExecDestroy(vexec);
@@ -1748,6 +1795,7 @@ int scf_proj_solve_rhs(scf_proj* h, const double* b, double* x, double* r, int m
       n += (long long)(S.pad[0] / 2) * h->body_launches;
     n += h->body_runs * h->body_launches;
     st->launches = (int)n;
+    st->asym_faces = S.asym_faces;
   }
   h->pending_launches = 0;
   return status == kOk ? SCF_OK : status;

@@ -189,7 +189,7 @@ def generate_pairs(n_inst=250, n_iter=16, size=512, config=4, seed=None, device=
     Returns dict of CUDA tensors: ops [n_inst][3][nx*ny] (cE, cN, dg), r, e
     [n_inst*n_iter][nx*ny], inst index per pair."""
     import torch
-    from . import synth
+    from gen import synth
     dev = torch.device("cuda", device)
     nn = size * size
     ops = torch.zeros((n_inst, 3, nn), dtype=torch.float64, device=dev)

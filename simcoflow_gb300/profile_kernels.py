@@ -36,7 +36,7 @@ import time
 import numpy as np
 
 from . import projection as P
-from . import synth
+from gen import synth
 
 KERNELS = {"sweep": (0, {"fp64": 48, "mixed": 20}), "pupdate_spmv": (1, {"fp64": 56, "mixed": 44}),
            "update_xr": (2, {"fp64": 48, "mixed": 52}),

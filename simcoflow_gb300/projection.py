@@ -44,7 +44,8 @@ EXPORTS = ["scf_opts_default", "scf_proj_create", "scf_proj_destroy", "scf_proj_
            "scf_proj_vcycle", "scf_proj_time_kernel", "scf_rhs_norm_noalloc", "scf_strerror",
            "scf_proj_set_network", "scf_proj_solve_rhs", "scf_proj_set_opts",
            "scf_batch_create", "scf_batch_set_io", "scf_batch_run", "scf_batch_destroy",
-           "scf_proj_set_solid", "scf_proj_get_geometry", "scf_diag_divide"]
+           "scf_proj_set_solid", "scf_proj_get_geometry", "scf_diag_divide",
+           "scf_proj_get_matrix", "scf_diag_tma_timeout"]
 # every symbol declared in include/scf_unet.h
 UNET_EXPORTS = ["scf_unet_num_params", "scf_unet_create", "scf_unet_destroy",
                 "scf_unet_set_stream", "scf_unet_set_params", "scf_unet_get_params",
@@ -67,7 +68,7 @@ class Stats(C.Structure):
                 ("ms_assemble", C.c_double), ("ms_solve", C.c_double),
                 ("ms_correct", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double),
                 ("smoother", C.c_int), ("learned_iters", C.c_int), ("launches", C.c_int),
-                ("reserved_i", C.c_int)]
+                ("asym_faces", C.c_int)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -104,6 +105,7 @@ def load():
         L.scf_proj_update_puv.argtypes = [vp, dp, dp, C.c_double, dp, dp, dp, dp, dp,
                                           C.POINTER(Stats)]
         L.scf_proj_get_operator.argtypes = [vp, dp, dp, dp, dp]
+        L.scf_proj_get_matrix.argtypes = [vp, dp, C.POINTER(C.c_int), C.POINTER(C.c_double)]
         L.scf_proj_vcycle.argtypes = [vp, dp, dp]
         L.scf_proj_time_kernel.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]
         L.scf_rhs_norm_noalloc.argtypes = [C.c_int, C.c_int] + [dp] * 10 + [ip, C.c_double, dp,
@@ -120,6 +122,8 @@ def load():
         L.scf_proj_get_geometry.argtypes = [vp] + [dp] * 8 + [ip] * 5 + [dp, dp]
         L.scf_diag_divide.argtypes = [dp, dp, dp, C.c_int64, C.c_int]
         L.scf_diag_divide.restype = C.c_int
+        L.scf_diag_tma_timeout.argtypes = [C.c_int, C.c_int, C.c_int]
+        L.scf_diag_tma_timeout.restype = C.c_int
         for name in EXPORTS:
             f = getattr(L, name)
             if f.restype is C.c_int or name.startswith("scf_proj"):
@@ -308,6 +312,16 @@ class ProjectionSolver:
                "scf_proj_get_operator")
         return dict(zip(("cE", "cN", "diag", "rhs"), out))
 
+    def get_matrix(self):
+        """The assembled rows as the reference's matr(Isize,Jsize,5) (S, W,
+        diagonal, E, N; Fortran order), the number of faces whose two rows
+        carry different entries and their largest relative difference."""
+        m = np.zeros((self.nx, self.ny, 5), order="F")
+        na, mx = C.c_int(0), C.c_double(0.0)
+        _check(load().scf_proj_get_matrix(self._h, m.ctypes.data, C.byref(na), C.byref(mx)),
+               "scf_proj_get_matrix")
+        return m, na.value, mx.value
+
     def set_schedule(self, npre: int, npost: int, omega: float):
         """V-cycle schedule of this handle (rebuilds its graph)."""
         _check(load().scf_proj_set_opts(self._h, npre, npost, omega), "scf_proj_set_opts")
@@ -357,6 +371,16 @@ class ProjectionSolver:
         self.assemble(a["DpU"], a["DpV"], case.betaP, case.betaM, case.bc)
 
 
+TMA_SPINS_DEFAULT = 1 << 20
+
+
+def inject_tma_timeout(cta: int, spins: int, device: int = 0):
+    """Test-only fault injection (scf_diag_tma_timeout): CTA `cta` of the
+    TMA-staged sweeps arms its barrier without issuing copies and waits at
+    most `spins` polls; cta=-1 with the default spins turns it off."""
+    _check(load().scf_diag_tma_timeout(device, cta, spins), "scf_diag_tma_timeout")
+
+
 def divide(a, b, device: int = 0):
     """a / b elementwise by the library's FP64 division (the one its
     bit-exact kernels use), on the GPU; numpy float64 arrays in and out."""
@@ -379,7 +403,8 @@ def project_case(case, **opts):
         a = case.arrays
         u, v, p = a["u0"].copy(order="F"), a["v0"].copy(order="F"), a["p0"].copy(order="F")
         Pp, mres, st = s.update_puv(a["ustar"], a["vstar"], u, v, p, case.vb)
+        m, na, mx = s.get_matrix()
         return {"Pp": Pp, "u": u, "v": v, "p": p, "mres": mres, "stats": st.as_dict(),
-                "operator": s.get_operator()}
+                "operator": s.get_operator(), "matr": m, "asym_faces": na, "asym_max": mx}
     finally:
         s.close()

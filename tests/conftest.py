@@ -25,8 +25,9 @@ def oracle():
 @pytest.fixture(scope="session")
 def built():
     """Native libraries of the package (built in-tree if missing)."""
+    from gen import build as gen_build
     from simcoflow_gb300 import build
-    build.build_geom()
+    gen_build.build()
     if not (ROOT / "simcoflow_gb300" / "_lib" / "libscf_proj.so").exists():
         build.build_proj()
     return True

@@ -1,9 +1,9 @@
 """Seeded cut-cell inputs for the geometry tests: the three cell families'
-grids and solid level-set fields (simcoflow_gb300.synth's builders) on
+grids and solid level-set fields (gen.synth's builders) on
 optionally stretched grids with circular bodies."""
 import numpy as np
 
-from simcoflow_gb300.synth import circles_levelset, family_fields, family_grids, frac_v  # noqa: F401
+from gen.synth import circles_levelset, family_fields, family_grids, frac_v  # noqa: F401
 
 
 def case(nx, ny, circles, stretch=0.0, seed=0):

@@ -19,8 +19,8 @@ sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "oracle"))
 
 import oracle as O  # noqa: E402
-from simcoflow_gb300 import geometry as G  # noqa: E402
-from simcoflow_gb300 import synth  # noqa: E402
+from gen import geometry as G  # noqa: E402
+from gen import synth  # noqa: E402
 
 INPUTS = ("dx", "dy", "dxU", "dyV", "vof", "phi", "vofS", "nyS", "WlLh", "aE", "aW", "aN", "aS",
           "posnu_p", "posnu_u", "moex_u", "vofS_u", "posnu_v", "moex_v", "vofS_v", "DpU", "DpV",

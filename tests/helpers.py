@@ -3,7 +3,7 @@ from pathlib import Path
 
 import numpy as np
 
-from simcoflow_gb300 import synth
+from gen import synth
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 GOLDEN_CASES = ("c1_n16", "box25x19")

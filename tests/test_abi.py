@@ -7,8 +7,8 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent.parent
 
 
-def _declared(header):
-    text = (ROOT / "include" / header).read_text()
+def _declared(header, folder="include"):
+    text = (ROOT / folder / header).read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(scf_[a-z_0-9]+)\s*\(", text)))
 
@@ -33,11 +33,15 @@ def test_proj_library_exports_unet_header_symbols(built):
     assert sorted(projection.UNET_EXPORTS) == names
 
 
-def test_geom_library_exports_header_symbols(built):
-    from simcoflow_gb300 import build
-    lib = ctypes.CDLL(str(build.build_geom()))
-    for n in _declared("scf_geom.h"):
-        assert hasattr(lib, n), n
+def test_generator_library_exports_header_symbols(built):
+    """The synthetic-input generator (gen/, not part of the product) and the
+    oracle's copy of it, which the benchmark's CPU arm loads."""
+    from gen import build as gen_build
+    import build as oracle_build  # oracle/build.py
+    for path in (gen_build.build(), oracle_build.geom_lib()):
+        lib = ctypes.CDLL(str(path))
+        for n in _declared("scf_geom.h", "gen"):
+            assert hasattr(lib, n), n
 
 
 def test_struct_layouts_match_header(tmp_path):

@@ -5,23 +5,7 @@ same Fortran loops: X_Sweep (src/Clsvof_Mod.f90:1074-1123) and Y_Sweep
 import numpy as np
 import pytest
 
-
-def ls_fields(rng, nx, ny):
-    F = np.asfortranarray
-    x = np.cumsum(rng.uniform(0.5, 1.5, nx))
-    y = np.cumsum(rng.uniform(0.5, 1.5, ny))
-    dx = F(np.broadcast_to(np.gradient(x)[:, None], (nx, ny)).copy())
-    dy = F(np.broadcast_to(np.gradient(y)[None, :], (nx, ny)).copy())
-    f = {"phi": F(rng.standard_normal((nx, ny))),
-         "vofS": F(rng.choice([0.0, 0.0, 0.3, 1.0], (nx, ny))),
-         "dx": dx, "dy": dy,
-         "x": F(np.broadcast_to(x[:, None], (nx, ny)).copy()),
-         "y": F(np.broadcast_to(y[None, :], (nx, ny)).copy())}
-    for k in ("aE", "aW", "aN", "aS"):
-        f[k] = F(rng.choice([0.0, 0.5, 1.0], (nx + 2, ny + 2)) * rng.uniform(0.5, 1, (nx + 2, ny + 2)))
-    f["ue"] = F(rng.standard_normal((nx + 1, ny)))
-    f["ve"] = F(rng.standard_normal((nx, ny + 1)))
-    return f
+from gen.synth import ls_fields
 
 
 def py_sweep(dir, nx, ny, f, dtv, t):

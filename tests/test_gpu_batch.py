@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 from helpers import rel_l2
-from simcoflow_gb300 import synth
+from gen import synth
 
 pytestmark = pytest.mark.gpu
 

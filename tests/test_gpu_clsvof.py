@@ -6,7 +6,7 @@ import pytest
 
 from simcoflow_gb300 import clsvof as CL
 
-from test_clsvof_oracle import ls_fields
+from gen.synth import ls_fields
 
 pytestmark = pytest.mark.gpu
 

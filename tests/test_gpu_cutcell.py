@@ -117,7 +117,7 @@ def test_device_pointers_match_host(cuda):
 
 def test_headline_grid_family_inputs(cuda, oracle):
     """synth.cutcell_inputs on a small circles case: GPU equals the literal."""
-    from simcoflow_gb300 import synth
+    from gen import synth
     c = synth.c2(n=48)
     grids, fams = synth.cutcell_inputs(c)
     got, _ = CU.grid_preprocess(grids, fams)

@@ -4,9 +4,9 @@ the CPU builder, bit for bit, and a projection on GPU-built geometry."""
 import numpy as np
 import pytest
 
-from simcoflow_gb300 import geometry as G
+from gen import geometry as G
 from simcoflow_gb300 import projection as P
-from simcoflow_gb300 import synth
+from gen import synth
 
 pytestmark = pytest.mark.gpu
 

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from helpers import rel_l2
-from simcoflow_gb300 import synth
+from gen import synth
 from simcoflow_gb300 import projection as P
 
 pytestmark = pytest.mark.gpu

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from helpers import rel_l2
-from simcoflow_gb300 import synth
+from gen import synth
 from simcoflow_gb300 import projection as P
 
 pytestmark = pytest.mark.gpu
@@ -19,7 +19,7 @@ def _active(c):
 
 
 def _odd_stretched():
-    from simcoflow_gb300 import geometry as G
+    from gen import geometry as G
     rng = np.random.Generator(np.random.PCG64(23))
     xf = G.axis(38, 0.0, 1.0)
     yf = G.axis(30, 0.0, 1.0, True, 0.45, 0.55, 12)

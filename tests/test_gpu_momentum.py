@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from simcoflow_gb300 import momentum as M
-from simcoflow_gb300 import synth
+from gen import synth
 
 pytestmark = pytest.mark.gpu
 

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from helpers import GOLDEN_CASES, load_golden, rel_l2
-from simcoflow_gb300 import synth
+from gen import synth
 from simcoflow_gb300 import projection as P
 
 pytestmark = pytest.mark.gpu
@@ -27,7 +27,19 @@ def _gpu_project(c, **kw):
     return P.project_case(c, **kw)
 
 
-def _check_operator(c, op, matr, rhm):
+def _asym_faces(matr):
+    """Faces whose two rows carry different entries: a row's own W (S) entry
+    against its west (south) neighbour's E (N) entry."""
+    W, El = -matr[1:, :, 1], -matr[:-1, :, 3]
+    S, Nl = -matr[:, 1:, 0], -matr[:, :-1, 4]
+    return int((W != El).sum() + (S != Nl).sum())
+
+
+def _check_operator(c, g, matr, rhm):
+    """All five columns of the assembled rows bit for bit (S, W, diagonal,
+    E, N of src/ProjectionP_Mod.f90:176-230), the right-hand side, and the
+    count of faces whose two rows differ."""
+    op = g["operator"]
     act = _active(c)
     cE = np.where(act, -matr[:, :, 3], 0.0) + 0.0
     cN = np.where(act, -matr[:, :, 4], 0.0) + 0.0
@@ -36,6 +48,10 @@ def _check_operator(c, op, matr, rhm):
     assert np.array_equal(op["cN"], cN)
     assert np.array_equal(op["diag"], dg)
     assert np.array_equal(op["rhs"], rhm)
+    for f in range(5):
+        assert np.array_equal(g["matr"][:, :, f], matr[:, :, f]), f"matr(:,:,{f + 1})"
+    assert g["asym_faces"] == _asym_faces(matr)
+    assert g["stats"]["asym_faces"] == g["asym_faces"]
 
 
 def _check_solution(c, g, exp):
@@ -53,7 +69,7 @@ def _check_solution(c, g, exp):
 def test_golden_fixture(cuda, name, precision):
     c, exp = load_golden(name)
     g = _gpu_project(c, precision=precision)
-    _check_operator(c, g["operator"], exp["matr"], exp["rhm"])
+    _check_operator(c, g, exp["matr"], exp["rhm"])
     _check_solution(c, g, exp)
     assert g["stats"]["relres_true"] < 1e-11
 
@@ -64,18 +80,21 @@ def test_golden_fixture(cuda, name, precision):
     lambda: synth.c4(n=40, instance=7),
     lambda: synth.random_instance(5, 9, 3),
     lambda: synth.c5(instance=1, n=96),
-], ids=["c1_128", "c1_33", "c4_40", "r9", "c5_96"])
+    lambda: synth.walls(64),
+    lambda: synth.walls(128),
+    lambda: synth.walls(97, ny=61),
+], ids=["c1_128", "c1_33", "c4_40", "r9", "c5_96", "walls_64", "walls_128", "walls_97x61"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_parity_vs_oracle(cuda, oracle, maker, precision):
     c = maker()
     exp = oracle.project(c)
     g = _gpu_project(c, precision=precision)
-    _check_operator(c, g["operator"], exp["matr"], exp["rhm"])
+    _check_operator(c, g, exp["matr"], exp["rhm"])
     _check_solution(c, g, exp)
 
 
 def test_odd_rectangular_grid(cuda, oracle):
-    from simcoflow_gb300 import geometry as G
+    from gen import geometry as G
     rng = np.random.Generator(np.random.PCG64(11))
     xf = G.axis(34, 0.0, 1.7)
     yf = G.axis(18, 0.0, 0.9)
@@ -85,7 +104,7 @@ def test_odd_rectangular_grid(cuda, oracle):
                          1e-3, 50.0, vb=-0.02)
     exp = oracle.project(c)
     g = _gpu_project(c)
-    _check_operator(c, g["operator"], exp["matr"], exp["rhm"])
+    _check_operator(c, g, exp["matr"], exp["rhm"])
     _check_solution(c, g, exp)
 
 
@@ -125,7 +144,8 @@ def test_deterministic_and_graph_free_path_agree(cuda, precision):
 _PDL_PROBE = r'''
 import sys, numpy as np
 sys.path.insert(0, sys.argv[1])
-from simcoflow_gb300 import synth, projection as P
+from gen import synth
+from simcoflow_gb300 import projection as P
 c = synth.c4(n=320, instance=3)
 for prec in ("fp64", "mixed"):
     g = P.project_case(c, precision=prec, rtol=1e-10, maxit=300)
@@ -271,7 +291,8 @@ def test_full_size_c2(cuda, oracle):
 _TMA_PROBE = r'''
 import sys, numpy as np
 sys.path.insert(0, sys.argv[1])
-from simcoflow_gb300 import synth, projection as P
+from gen import synth
+from simcoflow_gb300 import projection as P
 c = synth.c4(n=330, instance=5)
 g = P.project_case(c, precision="mixed", rtol=1e-10, maxit=300)
 np.save(sys.argv[2] + "_Pp.npy", g["Pp"])
@@ -296,3 +317,15 @@ def test_tma_staged_sweep_matches_plain_sweep(cuda, tmp_path):
         assert r.returncode == 0, r.stderr[-2000:]
     assert np.array_equal(np.load(tmp_path / "tma_Pp.npy"), np.load(tmp_path / "plain_Pp.npy"))
     assert np.load(tmp_path / "tma_it.npy")[0] == np.load(tmp_path / "plain_it.npy")[0]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_wall_case_with_line_smoother(cuda, oracle, precision):
+    """The rows that differ from their neighbours' (solids on the walls) with
+    the line-smoothed preconditioner: same operator, same solution."""
+    c = synth.walls(96, instance=2)
+    exp = oracle.project(c)
+    g = _gpu_project(c, precision=precision, smoother="line")
+    assert g["stats"]["smoother"] == P.SMOOTHERS["line"]
+    _check_operator(c, g, exp["matr"], exp["rhm"])
+    _check_solution(c, g, exp)

@@ -3,7 +3,7 @@ restated SetMatrix / SetVectors system, its solves, and a closed-form case."""
 import numpy as np
 import pytest
 
-from simcoflow_gb300 import synth
+from gen import synth
 
 CASES = [lambda: synth.c1(n=48), lambda: synth.c4(n=64, instance=2),
          lambda: synth.random_instance(5, 40, 3)]

@@ -6,8 +6,8 @@ import math
 import numpy as np
 import pytest
 
-from simcoflow_gb300 import geometry as G
-from simcoflow_gb300 import synth
+from gen import geometry as G
+from gen import synth
 
 
 def _nosolid_case(n, ratio=1000.0 / 1.2, amp=0.0, dt=1e-3):
@@ -145,6 +145,50 @@ def test_oracle_mgpcg_matches_direct(oracle, built):
     x = oracle.x_from_interior(c, xi)
     assert rel < 1e-12
     assert np.linalg.norm(x - r["x"]) / np.linalg.norm(r["x"]) < 1e-10
+
+
+def _row_entries(matr):
+    """(own W, west neighbour's E, own S, south neighbour's N) magnitudes."""
+    return -matr[1:, :, 1], -matr[:-1, :, 3], -matr[:, 1:, 0], -matr[:, :-1, 4]
+
+
+def test_wall_solids_make_rows_differ_and_mgpcg_solves_them(oracle, built):
+    """Solids on the first / last rows and columns: the reference leaves those
+    faces' apertures unaveraged (src/Cutcell_Mod.f90:161-204), so a row's own
+    W / S entry (src/ProjectionP_Mod.f90:183,193) differs by per cent from
+    the neighbour's E / N entry.  The MG-PCG, which applies the rows as
+    written, agrees with the direct solve of the reference's CSR; solving the
+    symmetrised rows instead misses it by far more than the tolerances."""
+    c = synth.walls(64)
+    r = oracle.project(c)
+    W, El, S, Nl = _row_entries(r["matr"])
+    worst = max(np.abs(W - El).max() / np.abs(W).max(), np.abs(S - Nl).max() / np.abs(S).max())
+    assert worst > 1e-2
+    xi, it, rel, _ = oracle.mgpcg(c, r["matr"], r["rhm"], rtol=1e-13)
+    x = oracle.x_from_interior(c, xi)
+    assert rel < 1e-12
+    assert np.linalg.norm(x - r["x"]) / np.linalg.norm(r["x"]) < 1e-10
+    # the symmetrised rows (W / S taken from the neighbours) give another solution
+    m = r["matr"].copy(order="F")
+    m[1:, :, 1] = m[:-1, :, 3]
+    m[:, 1:, 0] = m[:, :-1, 4]
+    act = c["posnu_p"][1:c.nx + 1, 1:c.ny + 1] != -1
+    m[:, :, 0] *= act
+    m[:, :, 1] *= act
+    xs, _, _, _ = oracle.mgpcg(c, m, r["rhm"], rtol=1e-13)
+    xs = oracle.x_from_interior(c, xs)
+    assert np.linalg.norm(xs - r["x"]) / np.linalg.norm(r["x"]) > 1e-4
+
+
+def test_interface_faces_differ_in_the_last_bits(oracle, built):
+    """Away from walls the rows differ only where the interface's density
+    weight is formed from either side (src/ProjectionP_Mod.f90:415-418
+    against :493-498): a few faces, relative differences near rounding."""
+    c = synth.c1(n=64)
+    W, El, S, Nl = _row_entries(oracle.matrix(c)[0])
+    n = int((W != El).sum() + (S != Nl).sum())
+    assert n > 0
+    assert max(np.abs(W - El).max() / np.abs(W).max(), np.abs(S - Nl).max() / np.abs(S).max()) < 1e-13
 
 
 # ---- geometry: package builder vs the literal restatement ----

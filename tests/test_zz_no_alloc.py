@@ -17,7 +17,7 @@ import numpy as np
 import pytest
 
 from simcoflow_gb300 import projection as P
-from simcoflow_gb300 import synth
+from gen import synth
 
 pytestmark = pytest.mark.gpu
 
