@@ -80,6 +80,12 @@ def lib():
         L.oracle_mgpcg.argtypes = [C.c_int, C.c_int, _P, _P, _P, _P, _P, _P, _P, C.c_double, C.c_int,
                                    C.c_int, C.c_int, C.c_double, C.c_int, _P, C.POINTER(C.c_int),
                                    C.c_int]
+        L.oracle_mgpcg_matr.restype = C.c_int
+        L.oracle_mgpcg_matr.argtypes = [C.c_int, C.c_int, _P, _P, _I, _P, C.c_double, C.c_int,
+                                        C.c_int, C.c_int, C.c_double, C.c_int, _P,
+                                        C.POINTER(C.c_int), C.c_int]
+        L.oracle_scatter_interior.argtypes = [C.c_int, C.c_int, _I, _P, C.c_int, C.c_int,
+                                              C.c_int, C.c_int, _P]
         L.oracle_vcycle.argtypes = [C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_int, C.c_int,
                                     C.c_double, C.c_int, C.c_int]
         L.oracle_mom_matrix.restype = C.c_int
@@ -123,15 +129,21 @@ def pocoef(case, literal=False) -> np.ndarray:
     return pc
 
 
-def matrix(case, pc=None):
-    """Returns (matr (nx,ny,5), scipy CSR in Posnu numbering)."""
-    import scipy.sparse as sp
+def matrix(case, pc=None, csr=True):
+    """Returns (matr (nx,ny,5), scipy CSR in Posnu numbering); with
+    csr=False only the dense copy matr is built (and None returned for A)."""
     a = case.arrays
     if pc is None:
         pc = pocoef(case)
     nx, ny = case.nx, case.ny
     nmax = nx * ny
     matr = np.zeros((nx, ny, 5), order="F")
+    if not csr:
+        wb, eb, sb, nb = case.bc
+        lib().oracle_matrix(nx, ny, _p(pc), _p(a["aE"]), _p(a["aW"]), _p(a["aN"]), _p(a["aS"]),
+                            _p(a["posnu_p"]), wb, eb, sb, nb, _p(matr), None, None, None)
+        return matr, None
+    import scipy.sparse as sp
     rowptr = np.zeros(nmax + 1, dtype=np.int32)
     cols = np.zeros(5 * nmax, dtype=np.int32)
     vals = np.zeros(5 * nmax)
@@ -261,6 +273,43 @@ def vcycle(case, matr, b_f, npre=2, npost=2, omega=1.9, coarse_max=64,
                         dg.ctypes.data_as(_P), b.ctypes.data_as(_P), x.ctypes.data_as(_P), npre,
                         npost, omega, coarse_max, SMOOTHERS[smoother])
     return np.asfortranarray(x.reshape(ny, nx).T)
+
+
+def line_smoother_wanted(case) -> bool:
+    """The library's automatic smoother choice: lines when some cell's aspect
+    ratio exceeds 2."""
+    dx, dy = case["dx"], case["dy"]
+    return bool(max((dx / dy).max(), (dy / dx).max()) > 2.0)
+
+
+def project_mg(case, rtol=1e-8, maxit=500, npre=2, npost=2, omega=1.9, coarse_max=64,
+               smoother=None, threads=0) -> dict:
+    """The whole projection in C on all host threads, as the timed CPU
+    baseline runs it: pocoef, the dense rows, the right-hand side, the FP64
+    MG-PCG to rtol (the PCG on the rows as written, the V-cycle on their
+    symmetric part; maxit < 0 encodes cycles per application, see
+    oracle_mgpcg), scatter and correction.  smoother None picks lines where
+    the library would."""
+    if threads:
+        lib().oracle_set_threads(threads)
+    if smoother is None:
+        smoother = "line" if line_smoother_wanted(case) else "point"
+    nx, ny = case.nx, case.ny
+    pc = pocoef(case)
+    matr, _ = matrix(case, pc, csr=False)
+    rhm, _ = rhs(case)
+    xint = np.zeros((nx, ny), order="F")
+    rel = C.c_double(0.0)
+    nlev = C.c_int(0)
+    it = lib().oracle_mgpcg_matr(nx, ny, _p(matr), _p(rhm), _p(case["posnu_p"]), _p(xint), rtol,
+                                 maxit, npre, npost, omega, coarse_max, C.byref(rel),
+                                 C.byref(nlev), SMOOTHERS[smoother])
+    Pp = np.zeros((nx + 2, ny + 2), order="F")
+    wb, eb, sb, nb = case.bc
+    lib().oracle_scatter_interior(nx, ny, _p(case["posnu_p"]), _p(xint), wb, eb, sb, nb, _p(Pp))
+    u, v, p, mres = correct(case, Pp)
+    return {"Pp": Pp, "u": u, "v": v, "p": p, "mres": mres, "matr": matr, "rhm": rhm,
+            "iters": it, "relres": rel.value, "levels": nlev.value, "smoother": smoother}
 
 
 def x_from_interior(case, xint):

@@ -53,140 +53,169 @@ static inline int is_dry(double vof, double phi, double vofS) {
  * but divides by the BetaD left over from the previous cell; literal=0
  * uses the intended rule (BetaD = BetaP in that branch).
  */
+/* One cell of ComputePossionMatrixCoefficient; *pBetaW / *pBetaD carry the
+ * loop's BetaW / BetaD from the previously visited cell (literal mode reads
+ * them, see below). */
+static void pocoef_cell(int nx, int ny, int i, int j, int literal, const double *vof,
+                        const double *phi, const double *vofS, const double *dxP,
+                        const double *dyP, const double *dxU, const double *dyV,
+                        const double *DpU, const double *DpV, double betaP, double betaM,
+                        double *pocoef, double *pBetaW, double *pBetaD) {
+    const double tol = 1.0e-24;
+    double BetaW = *pBetaW, BetaD = *pBetaD, Lamda;
+#define WET(ii, jj) is_wet(F1(vof, ii, jj), F1(phi, ii, jj), F1(vofS, ii, jj))
+#define DRY(ii, jj) is_dry(F1(vof, ii, jj), F1(phi, ii, jj), F1(vofS, ii, jj))
+#define LAM(ii, jj) (fabs(F1(phi, i, j)) / ((fabs(F1(phi, i, j)) + fabs(F1(phi, ii, jj))) + tol))
+    if (WET(i, j)) {
+        /* south */
+        if (j > 1) {
+            if (DRY(i, j - 1)) {
+                Lamda = LAM(i, j - 1);
+                BetaW = Lamda * betaM + (1.0 - Lamda) * betaP;
+                PC(1, i, j) = F0(DpV, i, j - 1) * F1(dxP, i, j) / F1(dyV, i, j - 1) * betaP * betaM / BetaW;
+            } else if (WET(i, j - 1)) {
+                BetaW = betaM;
+                PC(1, i, j) = F0(DpV, i, j - 1) * F1(dxP, i, j) / F1(dyV, i, j - 1) * betaP * betaM / BetaW;
+            }
+        } else {
+            BetaW = betaM;
+            PC(1, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaW;
+        }
+        /* west */
+        if (i > 1) {
+            if (DRY(i - 1, j)) {
+                Lamda = LAM(i - 1, j);
+                BetaW = Lamda * betaM + (1.0 - Lamda) * betaP;
+                PC(2, i, j) = F0(DpU, i - 1, j) * F1(dyP, i, j) / F1(dxU, i - 1, j) * betaP * betaM / BetaW;
+            } else if (WET(i - 1, j)) {
+                BetaW = betaM;
+                PC(2, i, j) = F0(DpU, i - 1, j) * F1(dyP, i, j) / F1(dxU, i - 1, j) * betaP * betaM / BetaW;
+            }
+        } else {
+            BetaW = betaM;
+            PC(2, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaW;
+        }
+        /* east */
+        if (i < nx) {
+            if (DRY(i + 1, j)) {
+                Lamda = LAM(i + 1, j);
+                BetaW = Lamda * betaM + (1.0 - Lamda) * betaP;
+                PC(3, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaW;
+            } else if (WET(i + 1, j)) {
+                BetaW = betaM;
+                PC(3, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaW;
+            }
+        } else {
+            BetaW = betaM;
+            PC(3, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaW;
+        }
+        /* north */
+        if (j < ny) {
+            if (DRY(i, j + 1)) {
+                Lamda = LAM(i, j + 1);
+                BetaW = Lamda * betaM + (1.0 - Lamda) * betaP;
+                PC(4, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaW;
+            } else if (WET(i, j + 1)) {
+                BetaW = betaM;
+                PC(4, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaW;
+            }
+        } else {
+            BetaW = betaM;
+            PC(4, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaW;
+        }
+    } else if (DRY(i, j)) {
+        /* south */
+        if (j > 1) {
+            if (WET(i, j - 1)) {
+                Lamda = LAM(i, j - 1);
+                BetaD = Lamda * betaP + (1.0 - Lamda) * betaM;
+                PC(1, i, j) = F0(DpV, i, j - 1) * F1(dxP, i, j) / F1(dyV, i, j - 1) * betaP * betaM / BetaD;
+            } else if (DRY(i, j - 1)) {
+                if (literal) BetaW = betaP; /* :506 assigns BetaW, :507 divides by BetaD */
+                else BetaD = betaP;
+                PC(1, i, j) = F0(DpV, i, j - 1) * F1(dxP, i, j) / F1(dyV, i, j - 1) * betaP * betaM / BetaD;
+            }
+        } else {
+            BetaD = betaP;
+            PC(1, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaD;
+        }
+        /* west */
+        if (i > 1) {
+            if (WET(i - 1, j)) {
+                Lamda = LAM(i - 1, j);
+                BetaD = Lamda * betaP + (1.0 - Lamda) * betaM;
+                PC(2, i, j) = F0(DpU, i - 1, j) * F1(dyP, i, j) / F1(dxU, i - 1, j) * betaP * betaM / BetaD;
+            } else if (DRY(i - 1, j)) {
+                BetaD = betaP;
+                PC(2, i, j) = F0(DpU, i - 1, j) * F1(dyP, i, j) / F1(dxU, i - 1, j) * betaP * betaM / BetaD;
+            }
+        } else {
+            BetaD = betaP;
+            PC(2, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaD;
+        }
+        /* east */
+        if (i < nx) {
+            if (WET(i + 1, j)) {
+                Lamda = LAM(i + 1, j);
+                BetaD = Lamda * betaP + (1.0 - Lamda) * betaM;
+                PC(3, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaD;
+            } else if (DRY(i + 1, j)) {
+                BetaD = betaP;
+                PC(3, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaD;
+            }
+        } else {
+            BetaD = betaP;
+            PC(3, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaD;
+        }
+        /* north */
+        if (j < ny) {
+            if (WET(i, j + 1)) {
+                Lamda = LAM(i, j + 1);
+                BetaD = Lamda * betaP + (1.0 - Lamda) * betaM;
+                PC(4, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaD;
+            } else if (DRY(i, j + 1)) {
+                BetaD = betaP;
+                PC(4, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaD;
+            }
+        } else {
+            BetaD = betaP;
+            PC(4, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaD;
+        }
+    }
+#undef WET
+#undef DRY
+#undef LAM
+    *pBetaW = BetaW;
+    *pBetaD = BetaD;
+    (void)ny;
+}
+
 void oracle_pocoef(int nx, int ny, int literal, const double *vof, const double *phi,
                    const double *vofS, const double *dxP, const double *dyP,
                    const double *dxU, const double *dyV, const double *DpU,
                    const double *DpV, double betaP, double betaM, double *pocoef) {
-    const double tol = 1.0e-24;
-    double BetaW = NAN, BetaD = NAN, Lamda;
-    for (size_t k = 0; k < (size_t)nx * ny * 4; ++k) pocoef[k] = 0.0;
-    for (int i = 1; i <= nx; ++i) {
-        for (int j = 1; j <= ny; ++j) {
-#define WET(ii, jj) is_wet(F1(vof, ii, jj), F1(phi, ii, jj), F1(vofS, ii, jj))
-#define DRY(ii, jj) is_dry(F1(vof, ii, jj), F1(phi, ii, jj), F1(vofS, ii, jj))
-#define LAM(ii, jj) (fabs(F1(phi, i, j)) / ((fabs(F1(phi, i, j)) + fabs(F1(phi, ii, jj))) + tol))
-            if (WET(i, j)) {
-                /* south */
-                if (j > 1) {
-                    if (DRY(i, j - 1)) {
-                        Lamda = LAM(i, j - 1);
-                        BetaW = Lamda * betaM + (1.0 - Lamda) * betaP;
-                        PC(1, i, j) = F0(DpV, i, j - 1) * F1(dxP, i, j) / F1(dyV, i, j - 1) * betaP * betaM / BetaW;
-                    } else if (WET(i, j - 1)) {
-                        BetaW = betaM;
-                        PC(1, i, j) = F0(DpV, i, j - 1) * F1(dxP, i, j) / F1(dyV, i, j - 1) * betaP * betaM / BetaW;
-                    }
-                } else {
-                    BetaW = betaM;
-                    PC(1, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaW;
-                }
-                /* west */
-                if (i > 1) {
-                    if (DRY(i - 1, j)) {
-                        Lamda = LAM(i - 1, j);
-                        BetaW = Lamda * betaM + (1.0 - Lamda) * betaP;
-                        PC(2, i, j) = F0(DpU, i - 1, j) * F1(dyP, i, j) / F1(dxU, i - 1, j) * betaP * betaM / BetaW;
-                    } else if (WET(i - 1, j)) {
-                        BetaW = betaM;
-                        PC(2, i, j) = F0(DpU, i - 1, j) * F1(dyP, i, j) / F1(dxU, i - 1, j) * betaP * betaM / BetaW;
-                    }
-                } else {
-                    BetaW = betaM;
-                    PC(2, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaW;
-                }
-                /* east */
-                if (i < nx) {
-                    if (DRY(i + 1, j)) {
-                        Lamda = LAM(i + 1, j);
-                        BetaW = Lamda * betaM + (1.0 - Lamda) * betaP;
-                        PC(3, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaW;
-                    } else if (WET(i + 1, j)) {
-                        BetaW = betaM;
-                        PC(3, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaW;
-                    }
-                } else {
-                    BetaW = betaM;
-                    PC(3, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaW;
-                }
-                /* north */
-                if (j < ny) {
-                    if (DRY(i, j + 1)) {
-                        Lamda = LAM(i, j + 1);
-                        BetaW = Lamda * betaM + (1.0 - Lamda) * betaP;
-                        PC(4, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaW;
-                    } else if (WET(i, j + 1)) {
-                        BetaW = betaM;
-                        PC(4, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaW;
-                    }
-                } else {
-                    BetaW = betaM;
-                    PC(4, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaW;
-                }
-            } else if (DRY(i, j)) {
-                /* south */
-                if (j > 1) {
-                    if (WET(i, j - 1)) {
-                        Lamda = LAM(i, j - 1);
-                        BetaD = Lamda * betaP + (1.0 - Lamda) * betaM;
-                        PC(1, i, j) = F0(DpV, i, j - 1) * F1(dxP, i, j) / F1(dyV, i, j - 1) * betaP * betaM / BetaD;
-                    } else if (DRY(i, j - 1)) {
-                        if (literal) BetaW = betaP; /* :506 assigns BetaW, :507 divides by BetaD */
-                        else BetaD = betaP;
-                        PC(1, i, j) = F0(DpV, i, j - 1) * F1(dxP, i, j) / F1(dyV, i, j - 1) * betaP * betaM / BetaD;
-                    }
-                } else {
-                    BetaD = betaP;
-                    PC(1, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaD;
-                }
-                /* west */
-                if (i > 1) {
-                    if (WET(i - 1, j)) {
-                        Lamda = LAM(i - 1, j);
-                        BetaD = Lamda * betaP + (1.0 - Lamda) * betaM;
-                        PC(2, i, j) = F0(DpU, i - 1, j) * F1(dyP, i, j) / F1(dxU, i - 1, j) * betaP * betaM / BetaD;
-                    } else if (DRY(i - 1, j)) {
-                        BetaD = betaP;
-                        PC(2, i, j) = F0(DpU, i - 1, j) * F1(dyP, i, j) / F1(dxU, i - 1, j) * betaP * betaM / BetaD;
-                    }
-                } else {
-                    BetaD = betaP;
-                    PC(2, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaD;
-                }
-                /* east */
-                if (i < nx) {
-                    if (WET(i + 1, j)) {
-                        Lamda = LAM(i + 1, j);
-                        BetaD = Lamda * betaP + (1.0 - Lamda) * betaM;
-                        PC(3, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaD;
-                    } else if (DRY(i + 1, j)) {
-                        BetaD = betaP;
-                        PC(3, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaD;
-                    }
-                } else {
-                    BetaD = betaP;
-                    PC(3, i, j) = F0(DpU, i, j) * F1(dyP, i, j) / F1(dxU, i, j) * betaP * betaM / BetaD;
-                }
-                /* north */
-                if (j < ny) {
-                    if (WET(i, j + 1)) {
-                        Lamda = LAM(i, j + 1);
-                        BetaD = Lamda * betaP + (1.0 - Lamda) * betaM;
-                        PC(4, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaD;
-                    } else if (DRY(i, j + 1)) {
-                        BetaD = betaP;
-                        PC(4, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaD;
-                    }
-                } else {
-                    BetaD = betaP;
-                    PC(4, i, j) = F0(DpV, i, j) * F1(dxP, i, j) / F1(dyV, i, j) * betaP * betaM / BetaD;
-                }
-            }
-#undef WET
-#undef DRY
-#undef LAM
-        }
+    const size_t n4 = (size_t)nx * ny * 4;
+#pragma omp parallel for schedule(static)
+    for (size_t k = 0; k < n4; ++k) pocoef[k] = 0.0;
+    if (literal) {
+        /* the reference's loop order (j innermost): the stale BetaD read by
+           the dry/dry south face is the one cell (i,j-1) left behind */
+        double BetaW = NAN, BetaD = NAN;
+        for (int i = 1; i <= nx; ++i)
+            for (int j = 1; j <= ny; ++j)
+                pocoef_cell(nx, ny, i, j, 1, vof, phi, vofS, dxP, dyP, dxU, dyV, DpU, DpV,
+                            betaP, betaM, pocoef, &BetaW, &BetaD);
+        return;
     }
-    (void)BetaW;
+    /* the intended rule reads nothing left over from another cell, so the
+       cells are independent: memory order (i innermost), all threads */
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= ny; ++j) {
+        double BetaW = NAN, BetaD = NAN;
+        for (int i = 1; i <= nx; ++i)
+            pocoef_cell(nx, ny, i, j, 0, vof, phi, vofS, dxP, dyP, dxU, dyV, DpU, DpV, betaP,
+                        betaM, pocoef, &BetaW, &BetaD);
+    }
 }
 
 /*
@@ -197,18 +226,77 @@ void oracle_pocoef(int nx, int ny, int literal, const double *vof, const double 
  * rowptr has n_rows+1 entries, cols/vals room for 5*n_rows.
  * Returns the number of rows (ExtCell+1).
  */
+/* One row of SetPoissonMatrix into matr (and vals/cols when given). */
+static int matrix_row(int nx, int ny, int i, int j, const double *pocoef, const double *aE,
+                      const double *aW, const double *aN, const double *aS,
+                      const int32_t *posnu, int wb, int eb, int sb, int nbc, double *matr,
+                      double *values, int *cc) {
+    const double tol = 1.0e-24;
+    int nnz = 0;
+    if (j > 1 && F0(posnu, i, j - 1) != -1) {
+        cc[nnz] = F0(posnu, i, j - 1);
+        values[nnz] = -PC(1, i, j) * F0(aS, i, j);
+        MT(1, i, j) = values[nnz];
+        nnz++;
+    }
+    if (i > 1 && F0(posnu, i - 1, j) != -1) {
+        cc[nnz] = F0(posnu, i - 1, j);
+        values[nnz] = -PC(2, i, j) * F0(aW, i, j);
+        MT(2, i, j) = values[nnz];
+        nnz++;
+    }
+    cc[nnz] = F0(posnu, i, j);
+    double d = PC(1, i, j) * F0(aS, i, j) + PC(2, i, j) * F0(aW, i, j) +
+               PC(3, i, j) * F0(aE, i, j) + PC(4, i, j) * F0(aN, i, j);
+    if (sb == 1 && j == 1) d = d - PC(1, i, j) * F0(aS, i, j);
+    if (wb == 1 && i == 1) d = d - PC(2, i, j) * F0(aW, i, j);
+    if (eb == 1 && i == nx) d = d - PC(3, i, j) * F0(aE, i, j);
+    if (nbc == 1 && j == ny) d = d - PC(4, i, j) * F0(aN, i, j);
+    d = d + copysign(1.0, d) * tol;
+    values[nnz] = d;
+    MT(3, i, j) = d;
+    nnz++;
+    if (i < nx && F0(posnu, i + 1, j) != -1) {
+        cc[nnz] = F0(posnu, i + 1, j);
+        values[nnz] = -PC(3, i, j) * F0(aE, i, j);
+        MT(4, i, j) = values[nnz];
+        nnz++;
+    }
+    if (j < ny && F0(posnu, i, j + 1) != -1) {
+        cc[nnz] = F0(posnu, i, j + 1);
+        values[nnz] = -PC(4, i, j) * F0(aN, i, j);
+        MT(5, i, j) = values[nnz];
+        nnz++;
+    }
+    return nnz;
+}
+
 int oracle_matrix(int nx, int ny, const double *pocoef, const double *aE, const double *aW,
                   const double *aN, const double *aS, const int32_t *posnu, int wb, int eb,
                   int sb, int nbc, double *matr, int32_t *rowptr, int32_t *cols, double *vals) {
-    const double tol = 1.0e-24;
-    int nrows = 0;
-    for (int i = 1; i <= nx; ++i)
+    const size_t n5 = (size_t)nx * ny * 5;
+#pragma omp parallel for schedule(static)
+    for (size_t k = 0; k < n5; ++k) matr[k] = 0.0;
+    if (!rowptr) {
+        /* the dense copy only: rows are independent */
+#pragma omp parallel for schedule(static)
         for (int j = 1; j <= ny; ++j)
-            if (F0(posnu, i, j) != -1) nrows++;
-    for (size_t k = 0; k < (size_t)nx * ny * 5; ++k) matr[k] = 0.0;
+            for (int i = 1; i <= nx; ++i) {
+                double values[5];
+                int cc[5];
+                if (F0(posnu, i, j) != -1)
+                    matrix_row(nx, ny, i, j, pocoef, aE, aW, aN, aS, posnu, wb, eb, sb, nbc,
+                               matr, values, cc);
+            }
+        int nrows = 0;
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i)
+                if (F0(posnu, i, j) != -1) nrows++;
+        return nrows;
+    }
     /* rows are numbered with j fastest (src/Cutcell_Mod.f90:347-351), which is
        also the visiting order here, so CSR rows are written in order */
-    int nnz_total = 0;
+    int nnz_total = 0, nrows = 0;
     rowptr[0] = 0;
     for (int i = 1; i <= nx; ++i) {
         for (int j = 1; j <= ny; ++j) {
@@ -216,48 +304,15 @@ int oracle_matrix(int nx, int ny, const double *pocoef, const double *aE, const 
             if (row == -1) continue;
             double values[5];
             int cc[5];
-            int nnz = 0;
-            if (j > 1 && F0(posnu, i, j - 1) != -1) {
-                cc[nnz] = F0(posnu, i, j - 1);
-                values[nnz] = -PC(1, i, j) * F0(aS, i, j);
-                MT(1, i, j) = values[nnz];
-                nnz++;
-            }
-            if (i > 1 && F0(posnu, i - 1, j) != -1) {
-                cc[nnz] = F0(posnu, i - 1, j);
-                values[nnz] = -PC(2, i, j) * F0(aW, i, j);
-                MT(2, i, j) = values[nnz];
-                nnz++;
-            }
-            cc[nnz] = row;
-            double d = PC(1, i, j) * F0(aS, i, j) + PC(2, i, j) * F0(aW, i, j) +
-                       PC(3, i, j) * F0(aE, i, j) + PC(4, i, j) * F0(aN, i, j);
-            if (sb == 1 && j == 1) d = d - PC(1, i, j) * F0(aS, i, j);
-            if (wb == 1 && i == 1) d = d - PC(2, i, j) * F0(aW, i, j);
-            if (eb == 1 && i == nx) d = d - PC(3, i, j) * F0(aE, i, j);
-            if (nbc == 1 && j == ny) d = d - PC(4, i, j) * F0(aN, i, j);
-            d = d + copysign(1.0, d) * tol;
-            values[nnz] = d;
-            MT(3, i, j) = d;
-            nnz++;
-            if (i < nx && F0(posnu, i + 1, j) != -1) {
-                cc[nnz] = F0(posnu, i + 1, j);
-                values[nnz] = -PC(3, i, j) * F0(aE, i, j);
-                MT(4, i, j) = values[nnz];
-                nnz++;
-            }
-            if (j < ny && F0(posnu, i, j + 1) != -1) {
-                cc[nnz] = F0(posnu, i, j + 1);
-                values[nnz] = -PC(4, i, j) * F0(aN, i, j);
-                MT(5, i, j) = values[nnz];
-                nnz++;
-            }
+            int nnz = matrix_row(nx, ny, i, j, pocoef, aE, aW, aN, aS, posnu, wb, eb, sb, nbc,
+                                 matr, values, cc);
             for (int k = 0; k < nnz; ++k) {
                 cols[nnz_total + k] = cc[k];
                 vals[nnz_total + k] = values[k];
             }
             nnz_total += nnz;
             rowptr[row + 1] = nnz_total;
+            nrows++;
         }
     }
     return nrows;
@@ -272,8 +327,10 @@ void oracle_rhs(int nx, int ny, const double *u, const double *v, const double *
                 const double *aW, const double *aN, const double *aS, const double *dxP,
                 const double *dyP, const double *nyS, const double *WlLh, const int32_t *posnu,
                 double vb, double *rhm, double *rhs) {
-    for (int i = 1; i <= nx; ++i) {
-        for (int j = 1; j <= ny; ++j) {
+    /* cells are independent: memory order, all threads */
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= ny; ++j) {
+        for (int i = 1; i <= nx; ++i) {
             int ictr = F0(posnu, i, j);
             F1(rhm, i, j) = 0.0;
             if (ictr == -1) continue;
@@ -295,9 +352,12 @@ void oracle_rhs(int nx, int ny, const double *u, const double *v, const double *
  */
 void oracle_scatter(int nx, int ny, const int32_t *posnu, const double *x, int wb, int eb,
                     int sb, int nbc, double *Pp) {
-    for (size_t k = 0; k < (size_t)(nx + 2) * (ny + 2); ++k) Pp[k] = 0.0;
-    for (int i = 1; i <= nx; ++i)
-        for (int j = 1; j <= ny; ++j) {
+    const size_t n0 = (size_t)(nx + 2) * (ny + 2);
+#pragma omp parallel for schedule(static)
+    for (size_t k = 0; k < n0; ++k) Pp[k] = 0.0;
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
             int c = F0(posnu, i, j);
             F0(Pp, i, j) = (c != -1) ? x[c] : 0.0;
         }
@@ -331,8 +391,12 @@ void oracle_correct(int nx, int ny, const double *Pp, const double *ustar, const
     const double tol = 1.0e-24;
 #define WET(ii, jj) is_wet(F1(vof, ii, jj), F1(phi, ii, jj), F1(vofS, ii, jj))
 #define DRY(ii, jj) is_dry(F1(vof, ii, jj), F1(phi, ii, jj), F1(vofS, ii, jj))
-    for (int i = 1; i <= nx - 1; ++i) {
-        for (int j = 1; j <= ny; ++j) {
+    /* every stage below writes each element from its own loop iteration only
+       (reading what earlier stages wrote), so a stage's iterations run in
+       memory order on all threads without changing a result */
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= ny; ++j) {
+        for (int i = 1; i <= nx - 1; ++i) {
             if (F0(posnu_u, i, j) != -1 && F1(moex_u, i, j) != 1) {
                 double BetaW, Lamda, G;
                 int set = 0;
@@ -362,8 +426,9 @@ void oracle_correct(int nx, int ny, const double *Pp, const double *ustar, const
             }
         }
     }
-    for (int i = 1; i <= nx; ++i) {
-        for (int j = 1; j <= ny - 1; ++j) {
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= ny - 1; ++j) {
+        for (int i = 1; i <= nx; ++i) {
             if (F0(posnu_v, i, j) != -1 && F1(moex_v, i, j) != 1) {
                 double BetaW, Lamda, G;
                 int set = 0;
@@ -395,8 +460,9 @@ void oracle_correct(int nx, int ny, const double *Pp, const double *ustar, const
     }
 #undef WET
 #undef DRY
-    for (int i = 1; i <= nx; ++i)
-        for (int j = 1; j <= ny; ++j)
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i)
             if (F0(posnu_p, i, j) != -1) F0(p, i, j) = F0(Pp, i, j);
     for (int i = 1; i <= nx; ++i) {
         int j = ny;
@@ -404,16 +470,18 @@ void oracle_correct(int nx, int ny, const double *Pp, const double *ustar, const
                        F0(v, i, j - 1) * F0(aS, i, j) * F1(dxP, i, j)) /
                       F1(dxP, i, j) / F0(aN, i, j);
     }
-    for (int i = 1; i <= nx; ++i) {
-        for (int j = 1; j <= ny; ++j) {
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= ny; ++j) {
+        for (int i = 1; i <= nx; ++i) {
             F1(mres, i, j) = (F0(u, i, j) * F0(aE, i, j) - F0(u, i - 1, j) * F0(aW, i, j)) * F1(dyP, i, j) +
                              (F0(v, i, j) * F0(aN, i, j) - F0(v, i, j - 1) * F0(aS, i, j)) * F1(dxP, i, j) -
                              vb * F1(nyS, i, j) * F1(WlLh, i, j);
             if (F1(vofS, i, j) > 1.0 - EPSI) F1(mres, i, j) = 0.0;
         }
     }
-    for (int i = 1; i <= nx; ++i) {
-        for (int j = 1; j <= ny; ++j) {
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= ny; ++j) {
+        for (int i = 1; i <= nx; ++i) {
             if (F1(vofS, i, j) > 1.0 - EPSI) F0(p, i, j) = 0.0;
             if (F1(vofS_u, i, j) >= 1.0 - EPSI) F0(u, i, j) = 0.0;
             if (F1(vofS_v, i, j) >= 1.0 - EPSI) F0(v, i, j) = 0.0;
@@ -484,6 +552,15 @@ typedef struct {
 } omg;
 
 static double *dalloc(size_t n) { return (double *)calloc(n ? n : 1, sizeof(double)); }
+static void pzero(double *a, size_t n) {
+#pragma omp parallel for schedule(static)
+    for (size_t k = 0; k < n; ++k) a[k] = 0.0;
+}
+static void pcopy(double *dst, const double *src, size_t n) {
+#pragma omp parallel for schedule(static)
+    for (size_t k = 0; k < n; ++k) dst[k] = src[k];
+}
+
 
 static void level_alloc(olevel *L, int nx, int ny) {
     size_t n = (size_t)nx * ny;
@@ -629,41 +706,59 @@ static void line_half(olevel *L, int dir, int color) {
     const double *cE = L->cE, *cN = L->cN, *dg = L->dg, *b = L->b;
     double *x = L->x;
     int nlines = dir == 0 ? ny : nx, len = dir == 0 ? nx : ny;
+    /* lines along y are solved LB at a time (LB lines of one parity, two
+       columns apart), interleaved cell by cell, so that a row's cache lines
+       serve all of them; each line's arithmetic is that of a lone solve */
+    enum { LB = 8 };
+    const int per = dir == 0 ? 1 : LB;
+    const int nblk = ((nlines - color + 1) / 2 + per - 1) / per;
 #pragma omp parallel
     {
-        double *cp = dalloc((size_t)len), *dp = dalloc((size_t)len);
+        double *cp = dalloc((size_t)len * per), *dp = dalloc((size_t)len * per);
 #pragma omp for schedule(static)
-        for (int q = color; q < nlines; q += 2) {
+        for (int blk = 0; blk < nblk; ++blk) {
+            int q0 = color + 2 * per * blk, nq = 0;
+            int qs[LB];
+            for (int t = 0; t < per && q0 + 2 * t < nlines; ++t) qs[nq++] = q0 + 2 * t;
             /* cell k of line q: index and its in-line / cross couplings */
             for (int k = 0; k < len; ++k) {
-                int ix = dir == 0 ? k : q, iy = dir == 0 ? q : k;
-                size_t c = (size_t)iy * nx + ix;
-                double a = 0.0, up = 0.0, d = 1.0, r = 0.0;
-                if (dg[c] > 0.0) {
-                    d = dg[c];
-                    r = b[c];
-                    if (dir == 0) {
-                        a = ix > 0 ? -cE[c - 1] : 0.0;
-                        up = ix + 1 < nx ? -cE[c] : 0.0;
-                        if (iy + 1 < ny) r = r + cN[c] * x[c + nx];
-                        if (iy > 0) r = r + cN[c - nx] * x[c - nx];
-                    } else {
-                        a = iy > 0 ? -cN[c - nx] : 0.0;
-                        up = iy + 1 < ny ? -cN[c] : 0.0;
-                        if (ix + 1 < nx) r = r + cE[c] * x[c + 1];
-                        if (ix > 0) r = r + cE[c - 1] * x[c - 1];
+                for (int t = 0; t < nq; ++t) {
+                    int q = qs[t];
+                    int ix = dir == 0 ? k : q, iy = dir == 0 ? q : k;
+                    size_t c = (size_t)iy * nx + ix;
+                    double a = 0.0, up = 0.0, d = 1.0, r = 0.0;
+                    if (dg[c] > 0.0) {
+                        d = dg[c];
+                        r = b[c];
+                        if (dir == 0) {
+                            a = ix > 0 ? -cE[c - 1] : 0.0;
+                            up = ix + 1 < nx ? -cE[c] : 0.0;
+                            if (iy + 1 < ny) r = r + cN[c] * x[c + nx];
+                            if (iy > 0) r = r + cN[c - nx] * x[c - nx];
+                        } else {
+                            a = iy > 0 ? -cN[c - nx] : 0.0;
+                            up = iy + 1 < ny ? -cN[c] : 0.0;
+                            if (ix + 1 < nx) r = r + cE[c] * x[c + 1];
+                            if (ix > 0) r = r + cE[c - 1] * x[c - 1];
+                        }
                     }
+                    double *cpt = cp + (size_t)t * len, *dpt = dp + (size_t)t * len;
+                    double den = k > 0 ? d - a * cpt[k - 1] : d;
+                    cpt[k] = up / den;
+                    dpt[k] = (k > 0 ? r - a * dpt[k - 1] : r) / den;
                 }
-                double den = k > 0 ? d - a * cp[k - 1] : d;
-                cp[k] = up / den;
-                dp[k] = (k > 0 ? r - a * dp[k - 1] : r) / den;
             }
-            double xn = 0.0;
+            double xn[LB];
+            for (int t = 0; t < nq; ++t) xn[t] = 0.0;
             for (int k = len - 1; k >= 0; --k) {
-                int ix = dir == 0 ? k : q, iy = dir == 0 ? q : k;
-                size_t c = (size_t)iy * nx + ix;
-                xn = dp[k] - (k + 1 < len ? cp[k] * xn : 0.0);
-                x[c] = dg[c] > 0.0 ? xn : 0.0;
+                for (int t = 0; t < nq; ++t) {
+                    int q = qs[t];
+                    int ix = dir == 0 ? k : q, iy = dir == 0 ? q : k;
+                    size_t c = (size_t)iy * nx + ix;
+                    const double *cpt = cp + (size_t)t * len, *dpt = dp + (size_t)t * len;
+                    xn[t] = dpt[k] - (k + 1 < len ? cpt[k] * xn[t] : 0.0);
+                    x[c] = dg[c] > 0.0 ? xn[t] : 0.0;
+                }
             }
         }
         free(cp); free(dp);
@@ -722,7 +817,7 @@ static void vcycle(omg *M, int l) {
     olevel *L = &M->lev[l];
     size_t n = (size_t)L->nx * L->ny;
     if (l == M->nlev - 1) { coarse_solve(M); return; }
-    memset(L->x, 0, n * sizeof(double));
+    pzero(L->x, n);
     if (M->line) {
         /* a line step (x-lines and y-lines) counts as two sweeps */
         for (int s = 0; s < (M->npre + 1) / 2; ++s) line_step(L, 0);
@@ -781,9 +876,9 @@ int oracle_mgpcg(int nx, int ny, const double *cE, const double *cN, const doubl
     if (maxit < 0) { ncyc = (-maxit) / 1000; maxit = (-maxit) % 1000; if (ncyc < 1) ncyc = 1; }
     size_t n = (size_t)nx * ny;
     level_alloc(&M.lev[0], nx, ny);
-    memcpy(M.lev[0].cE, cE, n * sizeof(double));
-    memcpy(M.lev[0].cN, cN, n * sizeof(double));
-    memcpy(M.lev[0].dg, dg, n * sizeof(double));
+    pcopy(M.lev[0].cE, cE, n);
+    pcopy(M.lev[0].cN, cN, n);
+    pcopy(M.lev[0].dg, dg, n);
     compute_excess(&M.lev[0]);
     M.nlev = 1;
     while (M.lev[M.nlev - 1].nx * M.lev[M.nlev - 1].ny > coarse_max && M.nlev < 32 &&
@@ -799,24 +894,27 @@ int oracle_mgpcg(int nx, int ny, const double *cE, const double *cN, const doubl
     Fx.cS = cS;
     olevel *F = &M.lev[0];
     double *r = dalloc(n), *z = dalloc(n), *p = dalloc(n), *q = dalloc(n);
-    for (size_t k = 0; k < n; ++k) { x[k] = 0.0; r[k] = b[k]; }
+    pzero(x, n);
+    pcopy(r, b, n);
     double bnorm = sqrt(dot(b, b, n));
     int it = 0;
     if (bnorm == 0.0) { *relres = 0.0; goto done; }
     double rz = 0.0;
     for (it = 0; it < maxit; ++it) {
         /* z = M^{-1} r (ncyc V-cycles, each on the current residual) */
-        memcpy(F->b, r, n * sizeof(double));
+        pcopy(F->b, r, n);
         vcycle(&M, 0);
-        memcpy(z, F->x, n * sizeof(double));
+        pcopy(z, F->x, n);
         for (int c = 1; c < ncyc; ++c) {
             apply_A(&Fx, z, q);
+#pragma omp parallel for schedule(static)
             for (size_t k = 0; k < n; ++k) F->b[k] = r[k] - q[k];
             vcycle(&M, 0);
+#pragma omp parallel for schedule(static)
             for (size_t k = 0; k < n; ++k) z[k] += F->x[k];
         }
         double rz_new = dot(r, z, n);
-        if (it == 0) memcpy(p, z, n * sizeof(double));
+        if (it == 0) pcopy(p, z, n);
         else {
             double beta = rz_new / rz;
 #pragma omp parallel for schedule(static)
@@ -833,6 +931,7 @@ int oracle_mgpcg(int nx, int ny, const double *cE, const double *cN, const doubl
     apply_A(&Fx, x, q);
     {
         double s = 0.0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
         for (size_t k = 0; k < n; ++k) { double d = b[k] - q[k]; s += d * d; }
         *relres = sqrt(s) / bnorm;
     }
@@ -841,6 +940,63 @@ done:
     for (int l = 0; l < M.nlev; ++l) level_free(&M.lev[l]);
     free(M.chol); free(M.cmap);
     return it;
+}
+
+/*
+ * The same MG-PCG taking the reference's matr(nx,ny,5) and rhm(nx,ny)
+ * directly (Fortran layouts) and returning x in the (nx,ny) interior layout
+ * (0 on cells with Posnu = -1); the storage conversions run on all threads.
+ * This is the timed CPU baseline's solve: no Python work between assembly
+ * and correction.
+ */
+int oracle_mgpcg_matr(int nx, int ny, const double *matr, const double *rhm,
+                      const int32_t *posnu, double *xint, double rtol, int maxit, int npre,
+                      int npost, double omega, int coarse_max, double *relres, int *nlev_out,
+                      int smoother) {
+    const size_t n = (size_t)nx * ny;
+    double *cE = dalloc(n), *cN = dalloc(n), *dg = dalloc(n), *cW = dalloc(n), *cS = dalloc(n);
+    double *b = dalloc(n), *x = dalloc(n);
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+            const size_t k = (size_t)(j - 1) * nx + (i - 1);
+            const int act = F0(posnu, i, j) != -1;
+            cE[k] = act ? -MT(4, i, j) + 0.0 : 0.0;
+            cN[k] = act ? -MT(5, i, j) + 0.0 : 0.0;
+            cW[k] = act ? -MT(2, i, j) + 0.0 : 0.0;
+            cS[k] = act ? -MT(1, i, j) + 0.0 : 0.0;
+            dg[k] = act ? MT(3, i, j) : -1.0;
+            b[k] = F1(rhm, i, j);
+        }
+    int it = oracle_mgpcg(nx, ny, cE, cN, dg, cW, cS, b, x, rtol, maxit, npre, npost, omega,
+                          coarse_max, relres, nlev_out, smoother);
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i)
+            F1(xint, i, j) = F0(posnu, i, j) != -1 ? x[(size_t)(j - 1) * nx + (i - 1)] : 0.0;
+    free(cE); free(cN); free(dg); free(cW); free(cS); free(b); free(x);
+    return it;
+}
+
+/* DeltaPressureGetValues + DeltaPressureBoundaryCondition from an (nx,ny)
+ * interior solution (0 where Posnu = -1) instead of a Posnu-ordered vector */
+void oracle_scatter_interior(int nx, int ny, const int32_t *posnu, const double *xint, int wb,
+                             int eb, int sb, int nbc, double *Pp) {
+    const size_t n0 = (size_t)(nx + 2) * (ny + 2);
+#pragma omp parallel for schedule(static)
+    for (size_t k = 0; k < n0; ++k) Pp[k] = 0.0;
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i)
+            F0(Pp, i, j) = F0(posnu, i, j) != -1 ? F1(xint, i, j) : 0.0;
+    for (int i = 1; i <= nx; ++i) {
+        F0(Pp, i, 0) = (double)sb * F0(Pp, i, 1);
+        F0(Pp, i, ny + 1) = (double)nbc * F0(Pp, i, ny);
+    }
+    for (int j = 1; j <= ny; ++j) {
+        F0(Pp, 0, j) = (double)wb * F0(Pp, 1, j);
+        F0(Pp, nx + 1, j) = (double)eb * F0(Pp, nx, j);
+    }
 }
 
 /* one V-cycle on b (0-based), output x; exposed for bitwise tests */
