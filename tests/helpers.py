@@ -22,3 +22,15 @@ def rel_l2(a, b):
     d = np.linalg.norm(np.asarray(a) - np.asarray(b))
     n = np.linalg.norm(np.asarray(b))
     return d / n if n > 0 else d
+
+
+def rel_l2_finite(a, b):
+    """rel_l2 over the finite entries, after checking that both arrays have
+    their non-finite entries in the same places.  The reference's top-row
+    continuity divides by the north aperture of every top-row cell
+    (src/ComputePUV_Mod.f90:177-182), which is 0 / 0 on a solid cell whose V
+    cell is not solid enough to be zeroed afterwards (:227-245)."""
+    a, b = np.asarray(a), np.asarray(b)
+    fa, fb = np.isfinite(a), np.isfinite(b)
+    assert np.array_equal(fa, fb), "non-finite entries differ"
+    return rel_l2(a[fa], b[fb])

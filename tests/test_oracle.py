@@ -296,3 +296,32 @@ def test_oracle_line_smoother_on_stretched_grid(oracle, built):
         its[n] = (itp, itl)
     assert all(itl < 30 for _, itl in its.values())
     assert all(itp > 3 * itl for itp, itl in its.values())
+
+
+def test_whole_projection_in_c_matches_direct_solve(oracle, built):
+    """The timed CPU baseline's path (every stage in C, the dense rows only,
+    the MG-PCG on them) gives the direct solve's projection, with the
+    literal loops' rows."""
+    for c in (synth.c1(n=64), synth.walls(64), synth.c3(n=64)):
+        d = oracle.project(c)
+        m = oracle.project_mg(c, rtol=1e-13, maxit=300)
+        assert np.array_equal(m["matr"], d["matr"])
+        assert np.array_equal(m["rhm"], d["rhm"])
+        assert m["relres"] < 1e-12
+        for k, tol in (("Pp", 1e-10), ("u", 1e-11), ("v", 1e-11)):
+            assert np.linalg.norm(m[k] - d[k]) / np.linalg.norm(d[k]) < tol, k
+    assert oracle.project_mg(synth.c3(n=64))["smoother"] == "line"
+
+
+def test_top_row_continuity_divides_by_a_closed_face(oracle, built):
+    """A solid cell of the top row whose V cell is not solid enough to be
+    zeroed: the reference's top-row continuity (src/ComputePUV_Mod.f90:177-182)
+    divides by its closed north face, 0 / 0, and nothing clears the result
+    (:227-245).  The restatement keeps that (one NaN in v here)."""
+    c = synth.walls(48)
+    d = oracle.project(c)
+    bad = np.argwhere(~np.isfinite(d["v"]))
+    assert bad.tolist() == [[13, 48]]
+    i, j = bad[0]
+    assert c["aN"][i, j] == 0.0 and c["posnu_p"][i, j] == -1
+    assert np.isfinite(d["u"]).all() and np.isfinite(d["mres"]).all()
