@@ -1,19 +1,26 @@
 #!/usr/bin/env python
 """Benchmark: milliseconds per pressure projection solved to FP64 relative
-residual 1e-8, on the 2048x2048 two-phase cut-cell workload (three seeded
-circles, density ratio 1000:1.2), one GB300.
+residual 1e-8 on one GB300, on the 4096x4096 configuration the metric is
+quoted on: a y-stretched grid (geometric ratio 1.01 outside the band
+y in [0.45, 0.55]) with a thin rotated plate, a two-mode free surface and
+density ratio 1000:1.2.
 
 One step = one full projection of SIMCOFlow's UpdatePUV projection part:
 operator assembly + multigrid setup, right-hand side, PCG solve to
 ||b - A x||_2 <= 1e-8 ||b||_2, velocity correction, mass residual.
 
   value  device-resident: every input already in HBM (device pointers
-         through the C-ABI), CUDA events on the solver's stream
+         through the C-ABI), CUDA events on the solver's stream; the
+         mixed-precision path (FP64 flexible PCG, FP32/BF16 multigrid), each
+         arm at its autotuned V-cycle schedule.  The same line carries the
+         plain FP64 MG-PCG arm and the learned + mixed arm on the same
+         workload, each with its error against an FP64 oracle solve
   e2e    the same projection through the C-ABI with pinned host buffers:
          host->device copies of all inputs and device->host copies of all
          outputs inside the timed region
   --impl reference  the CPU restatement of the reference path (the oracle,
-         C + OpenMP on all host cores), same workload and metric
+         C + OpenMP on all host cores), same workload, config and metric;
+         it loads nothing of the product package
 
 Prints one JSON line (rank 0).  Under torchrun each rank solves its own
 seeded instance (replicas, no collective on the data path).
@@ -140,155 +147,379 @@ def reduce_max(x: float, pg, device) -> float:
     return float(t.item())
 
 
-def make_case(name: str, rank: int):
+def make_case(name: str, rank: int, **kw):
     from gen import synth
-    return synth.make_case(name, instance=rank)
+    return synth.make_case(name, instance=rank, **kw)
 
 
 WORKLOADS = {
-    "c2": "2048x2048 cut-cell two-phase projection, 3 seeded circles, density 1000:1.2, "
-          "32-mode u*, dt 5e-4 (plain FP64 MG-PCG)",
-    "c1": "128x128 cut-cell two-phase projection, circle r=0.1, density 1000:1.2",
-    "c3": "4096x4096 y-stretched grid, rotated plate, density 1000:1.2 (plain FP64 MG-PCG)",
+    "c3": "4096x4096 y-stretched grid (geometric ratio 1.01 outside the band y in "
+          "[0.45,0.55]), 0.3x0.02 plate rotated 10 degrees at (0.5,0.35), two-mode free "
+          "surface (0.02, 0.01), density 1000:1.2, 64 seeded u* modes + Gaussian vortex 0.5, "
+          "dt 2.5e-4",
+    "c2": "2048x2048 uniform grid, three seeded circles r U(0.04,0.1), surface "
+          "0.5+0.03 sin(4 pi x + theta), density 1000:1.2, 32 seeded u* modes, dt 5e-4",
+    "c1": "128x128 uniform grid, circle r=0.1 at (0.5,0.35), surface 0.5+0.02 sin(2 pi x), "
+          "density 1000:1.2, 8 seeded u* modes, dt 1e-3",
 }
 
-# compulsory bytes per fine cell of each measured kernel, per precision:
-# sweep = one red-black iteration (both colours)
-# in one pass; resid_restrict = sweep + residual + 2x2 restriction;
-# prolong = prolongation fused into a sweep.
+# Compulsory DRAM bytes per fine cell of each timed kernel (each array element
+# the launch touches counted once), per precision.
+#   pupdate_spmv  p = z + beta p, q = A p, p.q: z, p_old, p_new, dg, cE, cN, q
+#   update_xr     x += alpha p, r -= alpha q, FP32 copy of r, r.r, r.z
+#   line          one parity of x-lines: relaxed rows dg, b, cE, cN, x written
+#                 (16 B), the other rows' x and cN (6 B); 22 B per two cells
+#   fine_pre      first pre-smoothing launch: zero start, fused iterations,
+#                 residual + restriction: b, inverse diagonal, cE, cN, x
+#                 written, a quarter of the coarse b written
+#   fine_post     last post-smoothing launch: x, b, inverse diagonal, cE, cN,
+#                 a quarter of the coarse x read, x written
+#   assemble      14 FP64 / int32 input fields read, cE, cN, dg, own W and S
+#                 entries written (Fortran inputs with their ghost rings)
 KERNEL_BYTES = {
-    "fp64": {"sweep": 48, "pupdate_spmv": 56, "update_xr": 48, "resid_restrict": 58,
-             "prolong": 50},
-    # fine level of the mixed path: x, b (FP32 copy of r), di FP32; BF16 couplings;
-    # FP32 search direction p of the outer PCG
-    "mixed": {"sweep": 20, "pupdate_spmv": 44, "update_xr": 52, "resid_restrict": 25,
-              "prolong": 21},
+    "fp64": {"pupdate_spmv": 56, "update_xr": 48, "fine_pre": 40, "fine_post": 48,
+             "assemble": 152},
+    "mixed": {"pupdate_spmv": 44, "update_xr": 52, "line": 11, "fine_pre": 17, "fine_post": 21,
+              "assemble": 152},
 }
-KERNEL_IDS = (("sweep", 0), ("pupdate_spmv", 1), ("update_xr", 2), ("resid_restrict", 3),
-              ("prolong", 4), ("vcycle", 6), ("setup", 7))
-
-
-def cpu_projection_ms(case, threads: int, rtol: float = 1e-8):
-    """One projection through the oracle's C restatement (assembly, RHS,
-    FP64 MG-PCG to rtol, correction) on `threads` host threads.  Returns
-    (ms, info, solution)."""
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle as O
-    O.lib().oracle_set_threads(threads)
-    t0 = time.perf_counter()
-    pc = O.pocoef(case)
-    matr, A = O.matrix(case, pc)
-    rhm, b = O.rhs(case)
-    xi, it, rel, nlev = O.mgpcg(case, matr, rhm, rtol=rtol, maxit=500, npre=2, npost=2,
-                                omega=1.9, threads=threads)
-    x = O.x_from_interior(case, xi)
-    Pp = O.scatter(case, x)
-    u, v, p, mres = O.correct(case, Pp)
-    ms = (time.perf_counter() - t0) * 1e3
-    return ms, {"iters": it, "relres": rel, "levels": nlev}, {"Pp": Pp, "u": u, "v": v}
+KERNEL_IDS = {"pupdate_spmv": 1, "update_xr": 2, "assemble": 5, "vcycle": 6, "setup": 7,
+              "line": 8, "fine_pre": 9, "fine_post": 10}
+# the dominant kernel of each smoother's path by share of the launch list
+# (profiles/launches_c3_4096_mixed.md, profiles/launches_c2_mixed.md): its
+# name as ncu lists it and the scf_proj_time_kernel id that launches it
+DOMINANT = {
+    "line": ("line", "k_line<float, __nv_bfloat16, 8, 0, 0>",
+             "one parity of the fine level's x-lines (zebra line relaxation, FP32 iterate, "
+             "BF16 couplings)"),
+    "point": ("fine_pre", "k_sweep_tma<0, 1, 0, 1, 0, 2>",
+              "the fine level's pre-smoothing launch (two red-black iterations from zero, "
+              "residual and 2x2 restriction, TMA-staged)"),
+}
 
 
 def _rel(a, b):
-    d = np.linalg.norm(np.asarray(a) - np.asarray(b))
-    n = np.linalg.norm(np.asarray(b))
+    a, b = np.asarray(a), np.asarray(b)
+    m = np.isfinite(a) & np.isfinite(b)
+    d = np.linalg.norm(a[m] - b[m])
+    n = np.linalg.norm(b[m])
     return float(d / n) if n > 0 else float(d)
 
 
-def extra_learned(case, tdev, dev, local, args):
-    """The headline case with the learned preconditioner (shipped weights)."""
+def _oracle():
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    return O
+
+
+def cpu_projection(case, threads: int, rtol: float = 1e-8, maxit: int = 500):
+    """One projection through the oracle's C restatement (PoCoef, the dense
+    rows, RHS, FP64 MG-PCG to rtol, scatter, correction) on `threads` host
+    threads.  Returns (ms, result)."""
+    O = _oracle()
+    O.lib().oracle_set_threads(threads)
+    t0 = time.perf_counter()
+    r = O.project_mg(case, rtol=rtol, maxit=maxit)
+    return (time.perf_counter() - t0) * 1e3, r
+
+
+def errors_vs(out, ref):
+    """Relative L2 errors of a projection's outputs against the FP64 oracle."""
+    return {"p_rel_l2": _rel(out["Pp"], ref["Pp"]),
+            "u_rel_l2": _rel(out["u"], ref["u"]), "v_rel_l2": _rel(out["v"], ref["v"])}
+
+
+def _tdev(case, dev):
     import torch
-    from simcoflow_gb300 import learned as Lr, projection as P
-    params, meta = Lr.load_weights()
+    return {k: torch.from_numpy(np.ascontiguousarray(v.ravel(order="F"))).to(dev)
+            for k, v in case.arrays.items() if isinstance(v, np.ndarray)}
+
+
+def _host(t, shape):
+    return t.cpu().numpy().reshape(shape, order="F")
+
+
+def device_arm(case, tdev, local, precision, *, steps, warmup, precond="mg", schedule=None,
+               tune=True, sample_clocks=False, stream=None, use_graph=True, pg=None,
+               kernels=True):
+    """Device-resident projections (inputs in HBM, device pointers through
+    the C-ABI), timed with CUDA events on the solver's stream.  Returns the
+    per-step time, statistics, the autotuned schedule, live per-kernel
+    times and the last step's outputs (host copies)."""
+    import ctypes
+    import torch
+    from simcoflow_gb300 import projection as P
+    dev = torch.device("cuda", local)
+    stream = stream or torch.cuda.Stream(device=dev)
     nx, ny = case.nx, case.ny
-    s = P.ProjectionSolver(nx, ny, precision="mixed", precond="learned", device=local,
-                           device_ptrs=True, rtol=1e-8, maxit=200)
+    s = P.ProjectionSolver(nx, ny, precision=precision, device=local, device_ptrs=True,
+                           rtol=1e-8, maxit=300, use_graph=use_graph, precond=precond)
     try:
-        s.set_network(params)
+        if precond == "learned":
+            from simcoflow_gb300 import learned as Lr
+            params, _ = Lr.load_weights()
+            s.set_network(params)
+        s.set_stream(stream.cuda_stream)
         s.set_grid(tdev["dx"], tdev["dy"], tdev["dxU"], tdev["dyV"])
         s.set_geometry(**{k: tdev[k] for k in P.GEOMETRY_ARGS})
         u, v, p = tdev["u0"].clone(), tdev["v0"].clone(), tdev["p0"].clone()
         Pp = torch.zeros_like(tdev["p0"])
-        m = torch.zeros(nx * ny, dtype=torch.float64, device=dev)
+        mres = torch.zeros(nx * ny, dtype=torch.float64, device=dev)
 
+        # u, v, p are corrected in place; the faces a projection corrects
+        # do not read their old value and the others keep it, so every step
+        # gives the first step's result
         def step():
             s.assemble(tdev["DpU"], tdev["DpV"], case.betaP, case.betaM, case.bc)
-            return s.update_puv(tdev["ustar"], tdev["vstar"], u, v, p, case.vb, Pp=Pp, mres=m)[2]
+            return s.update_puv(tdev["ustar"], tdev["vstar"], u, v, p, case.vb, Pp=Pp,
+                                mres=mres)[2]
 
-        step()
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        reps = max(1, min(args.steps, 3))
-        for _ in range(reps):
+        st = step()
+        smoother = {1: "point", 2: "line"}.get(st.smoother)
+        # V-cycle schedule from the project's autotuner, by time to the
+        # tolerance on this workload (the line smoother varies only omega)
+        if schedule is None and tune:
+            from simcoflow_gb300 import batch as Bt
+            cands = Bt.SCHEDULES if smoother == "point" else sorted(
+                {(2, 2, sc[2]) for sc in Bt.SCHEDULES})
+            best = None
+            for sch in cands:
+                s.set_schedule(*sch)
+                step()
+                torch.cuda.synchronize(dev)
+                t0 = time.perf_counter()
+                for _ in range(2):
+                    stt = step()
+                torch.cuda.synchronize(dev)
+                ms_t = (time.perf_counter() - t0) / 2
+                if stt.status == 0 and (best is None or ms_t < best[0]):
+                    best = (ms_t, sch)
+            schedule = best[1] if best else None
+        if schedule is not None:
+            s.set_schedule(*schedule)
+        for _ in range(warmup):
             st = step()
+        if pg:
+            pg.barrier()
         torch.cuda.synchronize(dev)
-        ms = (time.perf_counter() - t0) / reps * 1e3
-        return {"ms": round(ms, 3), "iters": st.iters, "learned_iters": st.learned_iters,
-                "fallback_to_vcycle": bool(st.fallbacks), "relres_true": st.relres_true,
-                "training": {k: meta.get(k) for k in ("instances", "iters", "size", "steps",
-                                                      "batch", "loss_first", "loss_last")}}
+        clk = ClockSampler(local) if sample_clocks else None
+        if clk:
+            clk.__enter__()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        iters, relres, nlaunch, lit = [], [], [], []
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize(dev)
+        h0 = time.monotonic()
+        e0.record(stream)
+        for _ in range(steps):
+            st = step()
+            iters.append(st.iters)
+            relres.append(st.relres_true)
+            nlaunch.append(st.launches)
+            lit.append(st.learned_iters)
+        e1.record(stream)
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize(dev)
+        if clk:
+            clk.mark(h0, time.monotonic())
+            clk.__exit__()
+        ms = e0.elapsed_time(e1) / steps
+        if pg:
+            ms = reduce_max(ms, pg, dev)
+        out = {"Pp": _host(Pp, (nx + 2, ny + 2)), "u": _host(u, (nx + 2, ny + 2)),
+               "v": _host(v, (nx + 2, ny + 2)), "mres": _host(mres, (nx, ny))}
+        kt = {}
+        if kernels:
+            for name, kid in KERNEL_IDS.items():  # live per-kernel timing on the same data
+                if name == "line" and smoother != "line":
+                    continue
+                if name in ("fine_pre", "fine_post") and smoother != "point":
+                    continue
+                o = ctypes.c_double(0.0)
+                if P.load().scf_proj_time_kernel(s._h, kid, 50, ctypes.byref(o)) == 0:
+                    kt[name] = o.value
+        return {"ms": ms, "iters": iters, "relres": relres, "levels": st.levels,
+                "launches": nlaunch, "learned_iters": lit, "fallbacks": st.fallbacks,
+                "asym_faces": st.asym_faces, "smoother": smoother, "schedule": schedule,
+                "kt": kt, "clk": clk.summary() if clk else None, "out": out}
     finally:
         s.close()
 
 
-def extra_stretched(local, args):
-    """The 4096^2 y-stretched configuration (line smoother), mixed and plain FP64."""
+def kernel_table(arm, prec, cells, peak):
+    out = {}
+    for k, v in arm["kt"].items():
+        out[k] = {"ms": round(v, 5)}
+        if k in KERNEL_BYTES[prec]:
+            gbs = KERNEL_BYTES[prec][k] * cells / (v * 1e-3) / 1e9
+            out[k]["GBps"] = round(gbs, 1)
+            out[k]["frac"] = round(gbs / peak, 3)
+    return out
+
+
+def e2e_arm(case, local, stream, *, steps, warmup, schedule, pg=None, solid=False):
+    """The mixed projection through the C-ABI with pinned host buffers: every
+    input copied host->device and every output device->host inside the timed
+    region (the grid, fixed for a run, is set once)."""
+    import torch
+    from simcoflow_gb300 import projection as P
+    dev = torch.device("cuda", local)
+    A = case.arrays
+    nx, ny = case.nx, case.ny
+
+    def pinned(a):
+        t = torch.empty(a.size, dtype=torch.float64 if a.dtype == np.float64 else torch.int32)
+        t = t.pin_memory()
+        arr = t.numpy().reshape(a.shape, order="F")
+        arr[...] = a
+        return arr
+
+    solid_keys = ["vof", "phi", "vofS_in", "phiS", "nxS_in", "nyS_in", "vofS_u_in", "vofS_v_in"]
+    geo_keys = solid_keys if solid else list(P.GEOMETRY_ARGS)
+    H = {k: pinned(A[k]) for k in set(geo_keys) | {"dx", "dy", "dxU", "dyV", "DpU", "DpV",
+                                                    "ustar", "vstar"}}
+    hu, hv, hpp = pinned(A["u0"]), pinned(A["v0"]), pinned(A["p0"])
+    hPp = pinned(np.zeros((nx + 2, ny + 2), order="F"))
+    hm = pinned(np.zeros((nx, ny), order="F"))
+    hs = P.ProjectionSolver(nx, ny, precision="mixed", device=local, rtol=1e-8, maxit=300)
+    try:
+        hs.set_stream(stream.cuda_stream)
+        if schedule:
+            hs.set_schedule(*schedule)
+        hs.set_grid(H["dx"], H["dy"], H["dxU"], H["dyV"])
+        h2d = (sum(H[k].nbytes for k in geo_keys + ["DpU", "DpV", "ustar", "vstar"]) +
+               hu.nbytes + hv.nbytes + hpp.nbytes)
+        d2h = hPp.nbytes + hu.nbytes + hv.nbytes + hpp.nbytes + hm.nbytes
+
+        def step():
+            if solid:
+                hs.set_solid(*[H[k] for k in solid_keys])
+            else:
+                hs.set_geometry(**{k: H[k] for k in P.GEOMETRY_ARGS})
+            hs.assemble(H["DpU"], H["DpV"], case.betaP, case.betaM, case.bc)
+            _, _, st = hs.update_puv(H["ustar"], H["vstar"], hu, hv, hpp, case.vb, Pp=hPp,
+                                     mres=hm)
+            return st.mres_max  # the step's result (max |mres|), read on the host
+
+        for _ in range(warmup):
+            step()
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize(dev)
+        # host clock: every call returns once its outputs are in host memory
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            step()
+        tot = time.perf_counter() - t0
+        ms = tot / steps * 1e3
+        if pg:
+            ms = reduce_max(ms, pg, dev)
+        return {"value": round(ms, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h),
+                "out": {"Pp": hPp.copy(order="F"), "u": hu.copy(order="F"),
+                        "v": hv.copy(order="F")}}
+    finally:
+        hs.close()
+
+
+def extra_c4_eval(local, args, threads):
+    """The learned preconditioner's evaluation on unseen instances of the
+    fourth configuration (1024^2 and 4096^2, uniform grids, density ratio
+    log-uniform in [10,1000]): learned + mixed against the mixed V-cycle and
+    the plain FP64 arm, each with its error against the FP64 oracle."""
     import torch
     from gen import synth
-    from simcoflow_gb300 import projection as P
-    case = synth.c3()
+    out = {"workload": "unseen c4 instances (0-4 circles r U(0.03,0.12), surface amplitude "
+                       "U(0,0.05) wavenumber 1-6, density ratio log-U[10,1000], 16 u* modes), "
+                       "FP64 relres 1e-8"}
     dev = torch.device("cuda", local)
-    t = {k: torch.from_numpy(np.ascontiguousarray(v.ravel(order="F"))).to(dev)
-         for k, v in case.arrays.items() if isinstance(v, np.ndarray)}
-    out = {"workload": WORKLOADS["c3"], "nx": case.nx, "ny": case.ny}
-    for prec in ("mixed", "fp64"):
-        s = P.ProjectionSolver(case.nx, case.ny, precision=prec, device=local, device_ptrs=True,
-                               rtol=1e-8, maxit=300)
-        try:
-            s.set_grid(t["dx"], t["dy"], t["dxU"], t["dyV"])
-            s.set_geometry(**{k: t[k] for k in P.GEOMETRY_ARGS})
-            u, v, p = t["u0"].clone(), t["v0"].clone(), t["p0"].clone()
-            Pp = torch.zeros_like(t["p0"])
-            m = torch.zeros(case.nx * case.ny, dtype=torch.float64, device=dev)
-
-            def step():
-                s.assemble(t["DpU"], t["DpV"], case.betaP, case.betaM, case.bc)
-                return s.update_puv(t["ustar"], t["vstar"], u, v, p, case.vb, Pp=Pp,
-                                    mres=m)[2]
-
-            # each arm at its fastest V-cycle schedule (the autotuner's candidates;
-            # the line smoother uses only the coarse-correction weight)
-            schedule = None
-            if not args.no_tune:
-                from simcoflow_gb300 import batch as Bt
-                best = None
-                for sch in sorted({(2, 2, sc[2]) for sc in Bt.SCHEDULES}):
-                    s.set_schedule(*sch)
-                    step()
-                    torch.cuda.synchronize(dev)
-                    t0 = time.perf_counter()
-                    stt = step()
-                    torch.cuda.synchronize(dev)
-                    ms_t = time.perf_counter() - t0
-                    if stt.status == 0 and (best is None or ms_t < best[0]):
-                        best = (ms_t, sch)
-                schedule = best[1]
-                s.set_schedule(*schedule)
-            step()
-            torch.cuda.synchronize(dev)
-            e0, e1 = torch.cuda.Event(True), torch.cuda.Event(True)
-            e0.record()
-            reps = 2
-            for _ in range(reps):
-                st = step()
-            e1.record()
-            torch.cuda.synchronize(dev)
-            out[prec] = {"ms": round(e0.elapsed_time(e1) / reps, 3), "iters": st.iters,
-                         "relres_true": st.relres_true, "schedule": schedule,
-                         "smoother": {1: "point", 2: "line"}.get(st.smoother)}
-        finally:
-            s.close()
-    out["speedup_mixed_vs_plain"] = round(out["fp64"]["ms"] / out["mixed"]["ms"], 3)
+    for n, inst in ((1024, 1001), (4096, 1002)):
+        case = synth.c4(n=n, instance=inst)
+        t = _tdev(case, dev)
+        row = {"ratio": round(case.meta["ratio"], 2), "circles": case.meta["ncirc"]}
+        ref = None
+        if not args.no_cpu:
+            _, ref = cpu_projection(case, threads, rtol=1e-12)
+            row["oracle_relres"] = ref["relres"]
+        for name, prec, pre in (("mixed", "mixed", "mg"), ("learned_mixed", "mixed", "learned"),
+                                ("plain_fp64", "fp64", "mg")):
+            a = device_arm(case, t, local, prec, steps=3, warmup=1, precond=pre, tune=False,
+                           kernels=False)
+            r = {"ms": round(a["ms"], 3), "iters": a["iters"][-1],
+                 "relres_true": a["relres"][-1]}
+            if pre == "learned":
+                r["learned_iters"] = a["learned_iters"][-1]
+                r["fallback_to_vcycle"] = bool(a["fallbacks"])
+            if ref is not None:
+                r["err_vs_fp64_oracle"] = errors_vs(a["out"], ref)
+            row[name] = r
+        out[f"{n}x{n}"] = row
+        del t
+        torch.cuda.empty_cache()
     return out
+
+
+def extra_batch(local, args, threads):
+    """64 uneven instances in one graph launch with autotuned schedules and
+    sweep tiles, with every instance's error against the FP64 oracle."""
+    from gen import synth
+    from simcoflow_gb300 import batch as Bt
+    cases = [synth.c5(instance=i) for i in range(64)]
+    bp = Bt.BatchProjector(cases, precision="mixed", rtol=1e-8, maxit=300, device=local)
+    try:
+        bp.run()
+        times = []
+        for _ in range(3):
+            st, ms = bp.run()
+            times.append(ms)
+        ms = min(times)
+        res = {"workload": "64 instances, sides 256..1024 (log-uniform, multiples of 32), "
+                           "density ratio log-U[10,1000], 0-4 circles, 16-mode u*, dt 1e-3",
+               "cells": int(sum(c.nx * c.ny for c in cases)), "ms_per_batch": round(ms, 3),
+               "solves_per_s": round(64 / (ms * 1e-3), 1),
+               "iters_min_max": [min(x["iters"] for x in st), max(x["iters"] for x in st)],
+               "max_relres_true": max(x["relres_true"] for x in st),
+               "launch": "one CUDA graph (64 branches, conditional-while PCG per branch)",
+               "autotune": json.loads(bp.table_json())}
+        if not args.no_cpu:
+            O = _oracle()
+            O.lib().oracle_set_threads(threads)
+            errs = []
+            for i, c in enumerate(cases):
+                ref = O.project_mg(c, rtol=1e-12, maxit=500)
+                e = errors_vs(bp.result(i), ref)
+                errs.append({"side": c.nx, "ratio": round(c.meta["ratio"], 1),
+                             "iters": st[i]["iters"], "p": float(f"{e['p_rel_l2']:.3e}"),
+                             "uv": float(f"{max(e['u_rel_l2'], e['v_rel_l2']):.3e}")})
+            res["per_instance_err_vs_fp64_oracle"] = errs
+            res["max_err_p"] = max(x["p"] for x in errs)
+            res["max_err_uv"] = max(x["uv"] for x in errs)
+        return res
+    finally:
+        bp.close()
+
+
+def extra_c2(local, args, threads, peak):
+    """The 2048^2 configuration (uniform grid, point smoother): mixed and
+    plain FP64, device-resident, with errors against the FP64 oracle."""
+    import torch
+    case = make_case("c2", 0)
+    dev = torch.device("cuda", local)
+    t = _tdev(case, dev)
+    out = {"workload": WORKLOADS["c2"]}
+    ref = None
+    if not args.no_cpu:
+        _, ref = cpu_projection(case, threads, rtol=1e-12)
+    for name, prec in (("mixed", "mixed"), ("plain_fp64", "fp64")):
+        a = device_arm(case, t, local, prec, steps=max(3, min(args.steps, 10)), warmup=3)
+        r = {"ms": round(a["ms"], 4), "iters": a["iters"][-1], "relres_true": a["relres"][-1],
+             "schedule": a["schedule"], "kernels": kernel_table(a, prec, case.nx * case.ny, peak)}
+        if ref is not None:
+            r["err_vs_fp64_oracle"] = errors_vs(a["out"], ref)
+        out[name] = r
+    out["speedup_mixed_vs_plain"] = round(out["plain_fp64"]["ms"] / out["mixed"]["ms"], 3)
+    return out, case
 
 
 def extra_momentum(case, local, args):
@@ -575,62 +806,77 @@ def extra_cutcell(case, local, args):
                               "inputs (includes its device allocation and output copies)"}}
 
 
-def extra_batch(local):
-    """64 uneven instances in one graph launch with autotuned schedules."""
-    from gen import synth
-    from simcoflow_gb300 import batch as Bt
-    cases = [synth.c5(instance=i) for i in range(64)]
-    bp = Bt.BatchProjector(cases, precision="mixed", rtol=1e-8, maxit=300, device=local)
-    try:
-        bp.run()
-        times = []
-        for _ in range(3):
-            st, ms = bp.run()
-            times.append(ms)
-        ms = min(times)
-        return {"workload": "64 instances, sides 256..1024 (log-uniform, multiples of 32), "
-                            "density ratio log-U[10,1000], 0-4 circles, 16-mode u*, dt 1e-3",
-                "cells": int(sum(c.nx * c.ny for c in cases)), "ms_per_batch": round(ms, 3),
-                "solves_per_s": round(64 / (ms * 1e-3), 1),
-                "iters_min_max": [min(x["iters"] for x in st), max(x["iters"] for x in st)],
-                "max_relres_true": max(x["relres_true"] for x in st),
-                "launch": "one CUDA graph (64 branches, conditional-while PCG per branch)",
-                "autotune": json.loads(bp.table_json())}
-    finally:
-        bp.close()
+def _config(case, name):
+    """The line's config: identical in both arms (workload and sizes only)."""
+    return {"workload": WORKLOADS.get(name, name), "name": name, "nx": case.nx, "ny": case.ny,
+            "l2": "inputs larger than L2 (no flush needed)"}
+
+
+def cpu_reference_settings(case, threads):
+    """Bounded sample of the reference's own solver settings on the CPU
+    restatement: PCG with 10 V-cycles per preconditioner application
+    (BoomerAMG MaxIter 10, src/ProjectionP_Mod.f90:130) and, with rtol 1e-20
+    (:111), 50 iterations (:108).  After an untimed warm-up, one and three
+    iterations are timed; the 50-iteration projection is projected from their
+    difference."""
+    O = _oracle()
+    O.lib().oracle_set_threads(threads)
+    O.project_mg(case, rtol=1e-20, maxit=-(10 * 1000 + 1))  # warm-up (untimed)
+    t = []
+    for its in (1, 3):
+        t0 = time.perf_counter()
+        r = O.project_mg(case, rtol=1e-20, maxit=-(10 * 1000 + its))
+        t.append((time.perf_counter() - t0) * 1e3)
+    per_it = (t[1] - t[0]) / 2
+    return {"ms_1_iteration": round(t[0], 1), "ms_3_iterations": round(t[1], 1),
+            "ms_per_iteration": round(per_it, 1),
+            "ms_50_iterations_projected": round(t[0] + 49 * per_it, 1),
+            "relres_after_3": r["relres"], "cores": threads,
+            "settings": "PCG maxit 50, rtol 1e-20, 10 V-cycles per application "
+                        "(src/ProjectionP_Mod.f90:106-133); sample: 1 and 3 iterations"}
 
 
 def run_reference(args):
     world, rank, local = _dist()
     if rank != 0:
         return 0
+    # the generator built by the oracle's recipe: nothing of the product loads
+    O = _oracle()
+    import build as oracle_build  # oracle/build.py
+    from gen import geometry
+    geometry.use_library(oracle_build.geom_lib())
     case = make_case(args.config, 0)
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
-        cpu_projection_ms(case, threads)
-    times, info = [], {}
+        cpu_projection(case, threads)
+    times, r = [], None
     for _ in range(args.steps):
-        ms, info, _ = cpu_projection_ms(case, threads)
+        ms, r = cpu_projection(case, threads)
         times.append(ms)
     ms = float(np.mean(times))
-    line = {"impl": "reference", "metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded, shapes and distributions of the named config)",
-            "config": {"workload": WORKLOADS.get(args.config, args.config), "name": args.config,
-                       "nx": case.nx, "ny": case.ny},
-            "cpu_baseline": {"value": ms, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"one full {case.nx}x{case.ny} projection per step "
-                                       f"(C restatement + OpenMP; Fortran+HYPRE reference "
-                                       f"unbuildable: no Fortran compiler, MPI or HYPRE)",
-                             "iters": info.get("iters")},
-            "e2e": {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line = {"impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded; shapes and distributions of the named config)",
+            "config": _config(case, args.config),
+            "cpu_baseline": {"value": round(ms, 3), "unit": UNIT, "cores": threads,
+                             "kind": "port",
+                             "sample": f"one full {case.nx}x{case.ny} projection per step: the "
+                                       f"oracle's C restatement (PoCoef, rows, RHS, FP64 "
+                                       f"MG-PCG to relres 1e-8 with the {r['smoother']} "
+                                       f"smoother, correction), OpenMP; the Fortran+HYPRE "
+                                       f"reference is unbuildable (no Fortran compiler, MPI "
+                                       f"or HYPRE)",
+                             "iters": r["iters"], "relres": r["relres"]},
+            "e2e": {"value": round(ms, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+    del O
     return 0
 
 
 def run_ours(args):
-    import ctypes
     import torch
     world, rank, local = _dist()
     from simcoflow_gb300 import build as B
@@ -643,260 +889,141 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
         pg = dist
+    P.load()
     case = make_case(args.config, rank)
-    A = case.arrays
     nx, ny = case.nx, case.ny
     cells = nx * ny
     stream = torch.cuda.Stream(device=dev)
+    tdev = _tdev(case, dev)
+    peak, peak_kind = _peaks()
+    use_graph = not args.no_graph
 
-    def barrier():
-        if pg:
-            pg.barrier()
-        torch.cuda.synchronize(dev)
-
-    def max_over_ranks(x):
-        return reduce_max(x, pg, dev)
-
-    tdev = {k: torch.from_numpy(np.ascontiguousarray(v.ravel(order="F"))).to(dev)
-            for k, v in A.items() if isinstance(v, np.ndarray)}
-
-    def device_arm(precision, sample_clocks):
-        """Device-resident projections: inputs in HBM, device pointers."""
-        s = P.ProjectionSolver(nx, ny, precision=precision, device=local, device_ptrs=True,
-                               rtol=1e-8, maxit=200, use_graph=not args.no_graph)
-        s.set_stream(stream.cuda_stream)
-        s.set_grid(tdev["dx"], tdev["dy"], tdev["dxU"], tdev["dyV"])
-        s.set_geometry(**{k: tdev[k] for k in P.GEOMETRY_ARGS})
-        u, v, p = tdev["u0"].clone(), tdev["v0"].clone(), tdev["p0"].clone()
-        Pp = torch.zeros_like(tdev["p0"])
-        mres = torch.zeros(cells, dtype=torch.float64, device=dev)
-
-        def step():
-            s.assemble(tdev["DpU"], tdev["DpV"], case.betaP, case.betaM, case.bc)
-            _, _, st = s.update_puv(tdev["ustar"], tdev["vstar"], u, v, p, case.vb, Pp=Pp,
-                                    mres=mres)
-            return st
-
-        # V-cycle schedule from the project's autotuner (same candidates as the
-        # batch path), chosen by time to the tolerance on this workload
-        schedule = None
-        if not args.no_tune:
-            from simcoflow_gb300 import batch as Bt
-            best = None
-            for sch in Bt.SCHEDULES:
-                s.set_schedule(*sch)
-                step()
-                torch.cuda.synchronize(dev)
-                t0 = time.perf_counter()
-                for _ in range(2):
-                    stt = step()
-                torch.cuda.synchronize(dev)
-                ms_t = (time.perf_counter() - t0) / 2
-                if stt.status == 0 and (best is None or ms_t < best[0]):
-                    best = (ms_t, sch)
-            schedule = best[1]
-            s.set_schedule(*schedule)
-        for _ in range(args.warmup):
-            st = step()
-        barrier()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        iters, relres, nlaunch = [], [], []
-        clk = ClockSampler(local) if sample_clocks else None
-        if clk:
-            clk.__enter__()
-        barrier()
-        h0 = time.monotonic()
-        e0.record(stream)
-        for _ in range(args.steps):
-            st = step()
-            iters.append(st.iters)
-            relres.append(st.relres_true)
-            nlaunch.append(st.launches)
-        e1.record(stream)
-        barrier()
-        if clk:
-            clk.mark(h0, time.monotonic())
-            clk.__exit__()
-        ms = max_over_ranks(e0.elapsed_time(e1)) / args.steps
-        kt = {}
-        for name, kid in KERNEL_IDS:  # live per-kernel timing on the same data
-            out = ctypes.c_double(0.0)
-            if P.load().scf_proj_time_kernel(s._h, kid, 50, ctypes.byref(out)) == 0:
-                kt[name] = out.value
-        s.close()
-        return {"ms": ms, "iters": iters, "relres": relres, "levels": st.levels, "kt": kt,
-                "launches": nlaunch,
-                "clk": clk.summary() if clk else None, "schedule": schedule}
-
-    plain = device_arm("fp64", False)
-    mixed = device_arm("mixed", True)
-
-    # ---- end-to-end: the headline (mixed) path through host (pinned) buffers ----
-    def pinned(a):
-        t = torch.empty(a.size, dtype=torch.float64 if a.dtype == np.float64 else torch.int32)
-        t = t.pin_memory()
-        arr = t.numpy().reshape(a.shape, order="F")
-        arr[...] = a
-        return arr, t
-
-    hp = {k: pinned(v) for k, v in A.items() if isinstance(v, np.ndarray)}
-    H = {k: v[0] for k, v in hp.items()}
-    hs = P.ProjectionSolver(nx, ny, precision="mixed", device=local, rtol=1e-8, maxit=200,
-                            use_graph=not args.no_graph)
-    hs.set_stream(stream.cuda_stream)
-    hu, hv, hpp = pinned(A["u0"])[0], pinned(A["v0"])[0], pinned(A["p0"])[0]
-    hPp = pinned(np.zeros((nx + 2, ny + 2), order="F"))[0]
-    hm = pinned(np.zeros((nx, ny), order="F"))[0]
-    # the grid is fixed for a whole run (Initial_Grid, src/Mesh_Mod.f90:54-175): set once;
-    # everything the time step changes is copied in and out every step
-    in_keys = [*P.GEOMETRY_ARGS, "DpU", "DpV", "ustar", "vstar"]
-    h2d = sum(H[k].nbytes for k in in_keys) + hu.nbytes + hv.nbytes + hpp.nbytes
-    d2h = hPp.nbytes + hu.nbytes + hv.nbytes + hpp.nbytes + hm.nbytes
-    hs.set_grid(H["dx"], H["dy"], H["dxU"], H["dyV"])
-
-    def e2e_step():
-        hs.set_geometry(**{k: H[k] for k in P.GEOMETRY_ARGS})
-        hs.assemble(H["DpU"], H["DpV"], case.betaP, case.betaM, case.bc)
-        _, _, st_ = hs.update_puv(H["ustar"], H["vstar"], hu, hv, hpp, case.vb, Pp=hPp, mres=hm)
-        return st_.mres_max  # the step's result (max |mres|), read on the host
-
-    for _ in range(args.warmup):
-        e2e_step()
-    barrier()
-    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    f0.record(stream)
-    for _ in range(args.steps):
-        e2e_step()
-    f1.record(stream)
-    barrier()
-    e2e_ms = max_over_ranks(f0.elapsed_time(f1)) / args.steps
-
-    # the same step with the cut-cell geometry derived on the GPU
-    # (scf_proj_set_solid): only the solid level-set fields cross
-    solid_keys = ["vof", "phi", "vofS_in", "phiS", "nxS_in", "nyS_in", "vofS_u_in", "vofS_v_in"]
-    h2d_solid = (sum(H[k].nbytes for k in solid_keys + ["DpU", "DpV", "ustar", "vstar"]) +
-                 hu.nbytes + hv.nbytes + hpp.nbytes)
-
-    def e2e_solid_step():
-        hs.set_solid(*[H[k] for k in solid_keys])
-        hs.assemble(H["DpU"], H["DpV"], case.betaP, case.betaM, case.bc)
-        _, _, st_ = hs.update_puv(H["ustar"], H["vstar"], hu, hv, hpp, case.vb, Pp=hPp, mres=hm)
-        return st_.mres_max
-
-    for _ in range(args.warmup):
-        e2e_solid_step()
-    barrier()
-    f0.record(stream)
-    for _ in range(args.steps):
-        e2e_solid_step()
-    f1.record(stream)
-    barrier()
-    e2e_solid_ms = max_over_ranks(f0.elapsed_time(f1)) / args.steps
-    hs.close()
-
+    mixed = device_arm(case, tdev, local, "mixed", steps=args.steps, warmup=args.warmup,
+                       tune=not args.no_tune, sample_clocks=True, stream=stream,
+                       use_graph=use_graph, pg=pg)
+    plain = device_arm(case, tdev, local, "fp64", steps=args.steps, warmup=args.warmup,
+                       tune=not args.no_tune, stream=stream, use_graph=use_graph, pg=pg)
+    learned = None
+    if not args.no_learned:
+        learned = device_arm(case, tdev, local, "mixed", precond="learned",
+                             steps=max(1, min(args.steps, 5)), warmup=1,
+                             schedule=mixed["schedule"], stream=stream, use_graph=use_graph,
+                             pg=pg, kernels=False)
+    del tdev
+    torch.cuda.empty_cache()
+    e2e = e2e_arm(case, local, stream, steps=args.steps, warmup=args.warmup,
+                  schedule=mixed["schedule"], pg=pg)
+    e2e_solid = e2e_arm(case, local, stream, steps=args.steps, warmup=args.warmup,
+                        schedule=mixed["schedule"], pg=pg, solid=True)
     if rank != 0:
         if pg:
             pg.destroy_process_group()
         return 0
 
-    peak, peak_kind = _peaks()
-
-    def kernel_table(arm, prec):
-        out = {}
-        for k, v in arm["kt"].items():
-            out[k] = {"ms": round(v, 5)}
-            if k in KERNEL_BYTES[prec]:
-                out[k]["GBps"] = round(KERNEL_BYTES[prec][k] * cells / (v * 1e-3) / 1e9, 1)
-        return out
-
-    # dominant kernel of the headline path: the fine-level sweep (4 of them per
-    # V-cycle on the fine grid, plus the fused restrict / prolong variants)
-    dom = "sweep"
+    # roofline: the dominant kernel of the headline path, timed live (CUDA
+    # events around 50 back-to-back launches on the solver's stream, same
+    # data) right after the timed region
+    dkey, dname, ddesc = DOMINANT[mixed["smoother"]]
     roof = None
-    if dom in mixed["kt"] and mixed["kt"][dom] > 0:
-        bytes_launch = KERNEL_BYTES["mixed"][dom] * cells
-        achieved = bytes_launch / (mixed["kt"][dom] * 1e-3) / 1e9
-        traffic = None
-        tf = ROOT / "profiles" / "traffic.json"
-        if tf.exists():
-            try:
-                traffic = json.loads(tf.read_text()).get(f"mixed_{dom}_{args.config}")
-            except Exception:
-                traffic = None
-        roof = {"bound": "hbm",
-                "kernel": "k_sweep_tma<FIRST=1,ZERO=0,PROLONG=0,RESTRICT=0,RZ=0,ITER=1> "
-                          "(TMA-staged FP32/BF16 red-black iteration, fine grid)",
+    if dkey in mixed["kt"] and mixed["kt"][dkey] > 0:
+        bytes_launch = KERNEL_BYTES["mixed"][dkey] * cells
+        achieved = bytes_launch / (mixed["kt"][dkey] * 1e-3) / 1e9
+        roof = {"bound": "hbm", "kernel": dname, "what": ddesc,
                 "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                "bytes_per_launch": bytes_launch, "ms_per_launch": mixed["kt"][dom],
-                "traffic": traffic,
+                "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} (hbm_gbs)",
+                "bytes_per_launch": bytes_launch,
+                "bytes_model": f"{KERNEL_BYTES['mixed'][dkey]} B per fine cell "
+                               "(compulsory: each element the launch touches once)",
+                "ms_per_launch": round(mixed["kt"][dkey], 5),
+                "traffic": None,
+                "traffic_note": "dram bytes of this kernel are in the committed ncu summary "
+                                "of the same workload (profiles/); bench.py runs no profiler",
                 "kernel_timing": "CUDA events around 50 back-to-back launches on the solver "
-                                 "stream, right after the timed region, same data"}
-    # kernel launches of the timed steps as the library counts them (direct
-    # launches plus the kernel nodes of each executed graph loop body)
-    launches = sum(mixed["launches"])
-    cpu = None
-    err = None
+                                 "stream after the timed region, same data"}
+    threads = os.cpu_count() or 1
+    cpu = err = ref_settings = None
     if world == 1 and not args.no_cpu:
-        threads = os.cpu_count() or 1
-        ms_cpu, info, _ = cpu_projection_ms(case, threads)
-        cpu = {"value": round(ms_cpu, 2), "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"one full {nx}x{ny} projection (C restatement of the reference path, "
-                         f"OpenMP, {info['iters']} MG-PCG iterations)"}
-        # error statement of the headline result against the FP64 oracle driven
-        # to its floor (checker only; not timed)
-        _, info13, ref = cpu_projection_ms(case, threads, rtol=1e-13)
-        err = {"p_rel_l2": _rel(hPp, ref["Pp"]),
-               "uv_rel_l2": _rel(np.concatenate([hu.ravel(), hv.ravel()]),
-                                 np.concatenate([ref["u"].ravel(), ref["v"].ravel()])),
-               "oracle": f"C restatement, FP64 MG-PCG to relres {info13['relres']:.1e}"}
+        ms_cpu, rc = cpu_projection(case, threads)
+        cpu = {"value": round(ms_cpu, 1), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"one full {nx}x{ny} projection (the oracle's C restatement: PoCoef, "
+                         f"rows, RHS, FP64 MG-PCG to relres 1e-8 with the {rc['smoother']} "
+                         f"smoother ({rc['iters']} iterations), correction; OpenMP)"}
+        # the FP64 oracle solve every result's error is stated against
+        # (checker only; outside every timed region)
+        _, ref = cpu_projection(case, threads, rtol=1e-12)
+        err = {"oracle": f"C restatement, FP64 MG-PCG to relres {ref['relres']:.1e} "
+                         f"({ref['iters']} iterations)",
+               "mixed": errors_vs(mixed["out"], ref), "plain_fp64": errors_vs(plain["out"], ref),
+               "e2e": errors_vs(e2e["out"], ref), "e2e_gpu_geometry": errors_vs(e2e_solid["out"],
+                                                                                 ref)}
+        if learned:
+            err["learned_mixed"] = errors_vs(learned["out"], ref)
+        if not args.no_ref_settings:
+            ref_settings = cpu_reference_settings(case, threads)
     extras = {}
     if world == 1 and not args.no_extras:
-        for name, fn in (("learned", lambda: extra_learned(case, tdev, dev, local, args)),
-                         ("stretched_4096", lambda: extra_stretched(local, args)),
-                         ("batch_64", lambda: extra_batch(local)),
-                         ("momentum_2048", lambda: extra_momentum(case, local, args)),
-                         ("tecplot_2048", lambda: extra_tecplot(case, local, args)),
-                         ("vtr_2048", lambda: extra_vtr(case, local, args)),
-                         ("ls_sweep_2048", lambda: extra_lsweep(case, local, args)),
-                         ("cutcell_2048", lambda: extra_cutcell(case, local, args))):
+        c2line = None
+
+        def c2():
+            nonlocal c2line
+            r, c2line = extra_c2(local, args, threads, peak)
+            return r
+        steps = [("c2_2048", c2),
+                 ("c4_eval", lambda: extra_c4_eval(local, args, threads)),
+                 ("batch_64", lambda: extra_batch(local, args, threads)),
+                 ("momentum_2048", lambda: extra_momentum(c2line, local, args)),
+                 ("tecplot_2048", lambda: extra_tecplot(c2line, local, args)),
+                 ("vtr_2048", lambda: extra_vtr(c2line, local, args)),
+                 ("ls_sweep_2048", lambda: extra_lsweep(c2line, local, args)),
+                 ("cutcell_2048", lambda: extra_cutcell(c2line, local, args))]
+        for name, fn in steps:
             try:
                 extras[name] = fn()
             except Exception as e:  # an extra must not hide the headline line
                 extras[name] = {"error": f"{type(e).__name__}: {e}"}
+            torch.cuda.empty_cache()
     ms_step = mixed["ms"]
+
+    def arm_line(a, prec):
+        return {"ms": round(a["ms"], 4), "iters": a["iters"][-1], "relres_true": a["relres"][-1],
+                "schedule": a["schedule"], "smoother": a["smoother"],
+                "kernels": kernel_table(a, prec, cells, peak)}
     line = {
         "metric": METRIC, "value": round(ms_step, 4), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
-        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64+f32/bf16",
+        "precision": "FP64 outer PCG (operator, residuals, dot products, alpha/beta, true "
+                     "residual, correction); FP32 multigrid iterate with BF16 couplings "
+                     "rescaled per level; FP64 coarsest solve",
         "data": "synthetic (seeded; shapes and distributions of the named config)",
-        "config": {"workload": WORKLOADS.get(args.config, args.config), "name": args.config,
-                   "nx": nx, "ny": ny,
-                   "path": "FP64 flexible PCG + FP32/BF16 multigrid (mixed)",
-                   "parallelism": f"replicas x{world}",
-                   "launch": "direct launches" if args.no_graph else "CUDA graph (conditional while)",
-                   "l2": "inputs larger than L2 (about 1.3 GB of arrays per projection)"},
+        "config": _config(case, args.config),
+        "path": "mixed: FP64 flexible PCG + FP32/BF16 multigrid V-cycle "
+                f"({mixed['smoother']} smoother), one CUDA graph with a conditional while "
+                "node" if use_graph else "direct launches",
+        "parallelism": f"replicas x{world}",
         "solves_per_s": round(1e3 * world / ms_step, 2),
         "iters": mixed["iters"][-1], "relres_true": mixed["relres"][-1],
-        "levels": mixed["levels"],
+        "levels": mixed["levels"], "asym_faces": mixed["asym_faces"],
         "schedule": {"npre_npost_omega": mixed["schedule"],
                      "source": "autotuner (simcoflow_gb300.batch.SCHEDULES), per arm"},
-        "plain_fp64_mg_pcg": {"ms": round(plain["ms"], 4), "iters": plain["iters"][-1],
-                              "relres_true": plain["relres"][-1],
-                              "schedule": plain["schedule"],
-                              "kernels": kernel_table(plain, "fp64")},
-        "speedup_vs_plain": round(plain["ms"] / ms_step, 3),
-        "e2e": {"value": round(e2e_ms, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
-        "e2e_gpu_geometry": {"value": round(e2e_solid_ms, 4), "unit": UNIT,
-                             "h2d_bytes_per_step": int(h2d_solid),
-                             "d2h_bytes_per_step": int(d2h),
+        "plain_fp64_mg_pcg": arm_line(plain, "fp64"),
+        "speedup_vs_plain_fp64": round(plain["ms"] / ms_step, 3),
+        "e2e": {k: v for k, v in e2e.items() if k != "out"},
+        "e2e_gpu_geometry": {**{k: v for k, v in e2e_solid.items() if k != "out"},
                              "path": "scf_proj_set_solid: Grid_Preprocess's derived geometry "
                                      "computed on the GPU from the solid level-set fields"},
-        "roofline": roof, "kernels": kernel_table(mixed, "mixed"),
-        "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": mixed["clk"],
+        "roofline": roof, "kernels": kernel_table(mixed, "mixed", cells, peak),
+        "gpu_launches": int(sum(mixed["launches"])), "cpu_baseline": cpu,
+        "cpu_reference_settings": ref_settings, "clocks": mixed["clk"],
         "err_vs_fp64_oracle": err, **extras,
     }
+    if learned:
+        line["learned_mixed"] = {"ms": round(learned["ms"], 4), "iters": learned["iters"][-1],
+                                 "learned_iters": learned["learned_iters"][-1],
+                                 "fallback_to_vcycle": bool(learned["fallbacks"]),
+                                 "relres_true": learned["relres"][-1],
+                                 "speedup_vs_plain_fp64": round(plain["ms"] / learned["ms"], 3)}
     print(json.dumps(line), flush=True)
     if pg:
         pg.destroy_process_group()
@@ -906,15 +1033,19 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", default="c2")
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--config", default="c3")
+    ap.add_argument("--no-cpu", action="store_true",
+                    help="skip the CPU baseline and the oracle error statements")
+    ap.add_argument("--no-ref-settings", action="store_true",
+                    help="skip the CPU sample of the reference's 10-cycle solver settings")
     ap.add_argument("--no-tune", action="store_true",
                     help="default V-cycle schedule instead of the autotuned one")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned + mixed arm")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the learned, 4096^2 stretched and 64-instance batch lines")
+                    help="skip the 2048^2, c4 evaluation, batch and file-format lines")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch the same kernels one by one instead of through the CUDA graph "
                          "(profilers cannot see kernel nodes of graphs with conditional nodes)")

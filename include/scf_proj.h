@@ -300,6 +300,12 @@ int scf_proj_vcycle(scf_proj *h, const double *b, double *x);
 #define SCF_K_ASSEMBLE 5       /* operator assembly from the Fortran arrays */
 #define SCF_K_VCYCLE 6         /* one whole V-cycle, captured as a CUDA graph */
 #define SCF_K_SETUP 7          /* assembly + multigrid hierarchy setup (device work only) */
+#define SCF_K_LINE 8           /* one fine-level pass of the line smoother (one parity of the
+                                  lines along x, iterate not zero), as the V-cycle runs it */
+#define SCF_K_FINE_PRE 9       /* the fine level's first pre-smoothing launch of the point
+                                  smoother (zero start, fused iterations, restriction) */
+#define SCF_K_FINE_POST 10     /* its last post-smoothing launch (prolongation, fused
+                                  iterations, r.z of the PCG) */
 int scf_proj_time_kernel(scf_proj *h, int kernel, int reps, double *ms_per_launch);
 
 /* Diagnostics: q[k] = a[k] / b[k] for k < n by the FP64 division that the

@@ -1475,7 +1475,7 @@ int scf_proj_get_matrix(scf_proj* h, double* matr, int* asym_faces, double* asym
 }
 
 int scf_proj_time_kernel(scf_proj* h, int kernel, int reps, double* ms) {
-  if (!h || !ms || reps < 1 || kernel < 0 || kernel > SCF_K_SETUP) return SCF_ERR_ARG;
+  if (!h || !ms || reps < 1 || kernel < 0 || kernel > SCF_K_FINE_POST) return SCF_ERR_ARG;
   if (!h->assembled) return SCF_ERR_STATE;
   CK(cudaSetDevice(h->device));
   cudaStream_t s = h->stream;
@@ -1530,7 +1530,47 @@ int scf_proj_time_kernel(scf_proj* h, int kernel, int reps, double* ms) {
       launch_assemble(h->fin, L0, h->sc_diag, s);
       return;
     }
+    if (kernel == SCF_K_LINE) {  // one fine-level pass along x, as the V-cycle runs it
+      if (h->mixed) {
+        MgF V = h->mix[0];
+        V.b = h->r32;
+        launch_line(V, 1, false, h->sc_diag, s);
+      } else if (!h->lf64n.empty()) {
+        launch_line_solve<double, double>(view64(h, 0), h->lf64n[0], 1, false, h->sc_diag, s);
+      } else {
+        launch_line(view64(h, 0), 1, false, h->sc_diag, s);
+      }
+      return;
+    }
     if (!two) return;
+    if (kernel == SCF_K_FINE_PRE || kernel == SCF_K_FINE_POST) {
+      // the fine level's first pre-smoothing and last post-smoothing launches
+      // of the point-smoothed V-cycle, with the handle's fused iteration count
+      const bool pre = kernel == SCF_K_FINE_PRE;
+      const std::vector<int> it = sweep_launches(pre ? h->opts.npre : h->opts.npost, h->mixed);
+      const int iters = pre ? it.front() : it.back();
+      const bool one = it.size() == 1;  // that launch is also the last (pre) / first (post)
+      const bool zero = pre, restr = pre && one, prol = !pre && one, rz = !pre;
+      if (h->mixed) {
+        MgF V = h->mix[0];
+        V.b = h->r32;
+        V.xin = pre ? nullptr : buf32(h, 0, 0);
+        V.x = buf32(h, 0, 1);
+        if (tma_level(h, 0))
+          launch_sweep_tma(V, h->mix[1], h->dmaps[0], 0, pre ? 0 : 1, zero, prol, restr, rz, om,
+                           1, h->sc_diag, h->part, s, iters);
+        else
+          launch_sweep(V, h->mix[1], pre ? 0 : 1, zero, prol, restr, rz, om, 1, h->sc_diag,
+                       h->part, s, iters);
+      } else {
+        MgD V = view64(h, 0);
+        V.xin = pre ? nullptr : buf64(h, 0, 0);
+        V.x = buf64(h, 0, 1);
+        launch_sweep(V, view64(h, 1), pre ? 0 : 1, zero, prol, restr, rz, om, 0, h->sc_diag,
+                     h->part, s, iters);
+      }
+      return;
+    }
     const bool smooth = kernel == SCF_K_SMOOTH, restr = kernel == SCF_K_RESID_RESTRICT,
                prol = kernel == SCF_K_PROLONG;
     const int first = restr ? 0 : 1;

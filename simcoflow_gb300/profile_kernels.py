@@ -7,8 +7,11 @@ profiler can restrict itself to that range (ncu --nvtx --nvtx-include
 "kernels/").  Work items:
 
   sweep, pupdate_spmv, update_xr, resid_restrict, prolong, assemble, vcycle,
-  setup     one kernel (or the captured V-cycle / setup) launched back to
-            back through scf_proj_time_kernel
+  setup, line, fine_pre, fine_post
+            one kernel (or the captured V-cycle / setup) launched back to
+            back through scf_proj_time_kernel (line: one fine-level pass of
+            the line smoother; fine_pre / fine_post: the point smoother's
+            first and last fine-level launches of a V-cycle)
   projection  --reps whole projections (assembly, right-hand side, PCG,
             correction) with direct launches, no graph: the launch list of
             the path
@@ -45,7 +48,9 @@ KERNELS = {"sweep": (0, {"fp64": 48, "mixed": 20}), "pupdate_spmv": (1, {"fp64":
            "vcycle": (6, {"fp64": 0, "mixed": 0}), "setup": (7, {"fp64": 0, "mixed": 0}),
            "projection": (None, {"fp64": 0, "mixed": 0}), "unet": (None, {"fp64": 0, "mixed": 0}),
            "momentum": (None, {"fp64": 0, "mixed": 0}), "geometry": (None, {"fp64": 0, "mixed": 0}),
-           "cutcell": (None, {"fp64": 0, "mixed": 0}), "tecplot": (None, {"fp64": 0, "mixed": 0})}
+           "cutcell": (None, {"fp64": 0, "mixed": 0}), "tecplot": (None, {"fp64": 0, "mixed": 0}),
+           "line": (8, {"fp64": 0, "mixed": 11}), "fine_pre": (9, {"fp64": 40, "mixed": 17}),
+           "fine_post": (10, {"fp64": 48, "mixed": 21})}
 
 
 def main():
