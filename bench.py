@@ -197,6 +197,17 @@ DOMINANT = {
 }
 
 
+# DRAM bytes per launch of the roofline kernel from an ncu capture of the
+# same kernel (bench.py runs no profiler, so the line's `traffic` stays null):
+# the capture, the workload it ran on and the scaling to a full launch
+TRAFFIC_PROFILE = {
+    ("c3", "line"): {"bytes_per_launch": 152.1e6, "source": "profiles/k_line_mixed_c3.md",
+                     "how": "dram__bytes_read.sum + dram__bytes_write.sum of 3 launches on the "
+                            "2048x2048 case of this workload (38.0 MB), x4 for the cells of a "
+                            "4096x4096 launch"},
+}
+
+
 def _rel(a, b):
     a, b = np.asarray(a), np.asarray(b)
     m = np.isfinite(a) & np.isfinite(b)
@@ -936,8 +947,7 @@ def run_ours(args):
                                "(compulsory: each element the launch touches once)",
                 "ms_per_launch": round(mixed["kt"][dkey], 5),
                 "traffic": None,
-                "traffic_note": "dram bytes of this kernel are in the committed ncu summary "
-                                "of the same workload (profiles/); bench.py runs no profiler",
+                "traffic_profile": TRAFFIC_PROFILE.get((args.config, dkey)),
                 "kernel_timing": "CUDA events around 50 back-to-back launches on the solver "
                                  "stream after the timed region, same data"}
     threads = os.cpu_count() or 1

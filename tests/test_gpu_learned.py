@@ -58,10 +58,15 @@ def test_learned_needs_network_and_mixed_precision(cuda):
 
 
 def test_training_gain_and_preconditioner_comparison(cuda):
-    """Trained against untrained network on held-out pairs of the plain
-    MG-PCG (the network's objective), and the FPCG iteration counts of the
-    V-cycle alone, the trained network and the untrained one (the fallback
-    bounds the loss against the V-cycle)."""
+    """What the trained network gains, measured: on held-out pairs of the
+    plain MG-PCG (the network's objective) it leaves a clearly smaller share
+    of the error energy than the untrained network.  As a preconditioner of
+    the flexible PCG it does not beat the V-cycle it was meant to replace:
+    its first iteration reduces the residual less than the 0.6 the switch
+    asks for, the V-cycle takes over, and the solve needs at least as many
+    iterations and more time than the V-cycle alone.  Both facts are
+    asserted, so a change in either direction shows up here."""
+    import time
     import torch
     from simcoflow_gb300 import learned as Lr
     pairs = Lr.generate_pairs(n_inst=3, n_iter=4, size=256, config=4, seed=12345)
@@ -85,12 +90,21 @@ def test_training_gain_and_preconditioner_comparison(cuda):
         net.close()
     # the trained network explains part of the error of every pair class;
     # the untrained one explains none of it (normalised loss near or above 1)
-    assert losses["trained"] < 0.9
-    assert losses["trained"] < 0.8 * losses["untrained"]
+    assert losses["trained"] < 0.75
+    assert losses["trained"] < 0.7 * losses["untrained"]
     c = synth.random_instance(4, 256, 9002)
-    its = {k: _project(c, rtol=1e-8, **kw)["stats"]
-           for k, kw in (("mg", {}), ("learned", {"precond": "learned"}))}
-    print("held-out loss", losses, "iterations",
-          {k: (v["iters"], v["learned_iters"], v["fallbacks"]) for k, v in its.items()})
-    assert its["learned"]["relres_true"] < 1e-8
-    assert its["learned"]["iters"] <= its["mg"]["iters"] + 4
+    res = {}
+    for k, kw in (("mg", {}), ("learned", {"precond": "learned"})):
+        _project(c, rtol=1e-8, **kw)  # warm-up
+        t0 = time.perf_counter()
+        st = _project(c, rtol=1e-8, **kw)["stats"]
+        res[k] = (st, time.perf_counter() - t0)
+    print("held-out loss", losses, "iterations / s",
+          {k: (v[0]["iters"], v[0]["learned_iters"], v[0]["fallbacks"], round(v[1], 4))
+           for k, v in res.items()})
+    mg, lr = res["mg"][0], res["learned"][0]
+    assert lr["relres_true"] < 1e-8 and mg["relres_true"] < 1e-8
+    # the measured negative: one learned iteration, then the V-cycle, and no
+    # fewer iterations than the V-cycle alone
+    assert lr["learned_iters"] >= 1 and lr["fallbacks"] == 1
+    assert mg["iters"] <= lr["iters"] <= mg["iters"] + 4
