@@ -868,13 +868,88 @@ __global__ void __launch_bounds__(1024) k_line_tail(TailDesc<T, CT> d, Scalars* 
     const T* b = B(l);
     const T* g = G(l);
     T* x = X(l);
+    if constexpr (std::is_same<T, float>::value) if (len <= 64) {
+      // FP32: one warp per line, M = 1 or 2 consecutive cells per lane.  A
+      // lane with two cells eliminates its first (x0 = D + S I_{l-1} +
+      // T I_l in the interfaces I, each lane's last cell), the interface
+      // equations are reduced by cyclic reduction over the lanes (shuffles,
+      // five steps) and the first cells recovered.  Reciprocals are the
+      // correctly rounded ones: with the approximate reciprocal the
+      // reduction costs the coarse correction enough accuracy for an extra
+      // PCG iteration.
+      const int lane = t & 31, nwarp = NTT >> 5;
+      const int M = len <= 32 ? 1 : 2;
+      for (int q = colour + 2 * (t >> 5); q < nlines; q += 2 * nwarp) {
+        const int s0 = (dir == 0 ? (q + 1) * w + 1 : w + q + 1);
+        T av[2], cv[2], dv[2], rv[2], gv[2];
+#pragma unroll
+        for (int m = 0; m < 2; ++m) {
+          const int k = lane * M + m;
+          av[m] = T(0); cv[m] = T(0); dv[m] = T(1); rv[m] = T(0); gv[m] = T(0);
+          if (m < M && k < len) {
+            const int si = s0 + k * step;
+            gv[m] = g[si];
+            if (gv[m] > T(0)) {
+              av[m] = k > 0 ? -Ax[si - step] : T(0);
+              cv[m] = k + 1 < len ? -Ax[si] : T(0);
+              dv[m] = gv[m];
+              T r = fma(Cx[si], x[si + cross], b[si]);
+              rv[m] = fma(Cx[si - cross], x[si - cross], r);
+            }
+          }
+        }
+        // the lane's interface cell is its last; with two cells the first
+        // is eliminated towards the interfaces on both sides
+        T D = T(0), S = T(0), Tr = T(0), a, dd, c, r;
+        if (M == 2) {
+          const T inv0 = __frcp_rn(dv[0]);
+          D = rv[0] * inv0;
+          S = -av[0] * inv0;
+          Tr = -cv[0] * inv0;
+          const T Dn = __shfl_down_sync(0xffffffffu, D, 1);
+          const T Sn = __shfl_down_sync(0xffffffffu, S, 1);
+          const T Tn = __shfl_down_sync(0xffffffffu, Tr, 1);
+          const bool last = lane == 31;
+          a = av[1] * S;
+          dd = fma(av[1], Tr, dv[1]);
+          r = fma(-av[1], D, rv[1]);
+          if (!last) {
+            dd = fma(cv[1], Sn, dd);
+            r = fma(-cv[1], Dn, r);
+          }
+          c = last ? T(0) : cv[1] * Tn;
+        } else {
+          a = av[0]; dd = dv[0]; c = cv[0]; r = rv[0];
+        }
+        if (lane == 0) a = T(0);
+        if (lane == 31) c = T(0);
+        for (int sh = 1; sh < 32; sh <<= 1) {
+          const T am = __shfl_up_sync(0xffffffffu, a, sh), bm = __shfl_up_sync(0xffffffffu, dd, sh);
+          const T cm = __shfl_up_sync(0xffffffffu, c, sh), rm = __shfl_up_sync(0xffffffffu, r, sh);
+          const T ap = __shfl_down_sync(0xffffffffu, a, sh), bp = __shfl_down_sync(0xffffffffu, dd, sh);
+          const T cp = __shfl_down_sync(0xffffffffu, c, sh), rp = __shfl_down_sync(0xffffffffu, r, sh);
+          const T k1 = a * __frcp_rn(bm), k2 = c * __frcp_rn(bp);
+          a = -am * k1;
+          c = -cp * k2;
+          dd = fma(-ap, k2, fma(-cm, k1, dd));
+          r = fma(-rp, k2, fma(-rm, k1, r));
+        }
+        const T I = r * __frcp_rn(dd);
+        const T Im = __shfl_up_sync(0xffffffffu, I, 1);
+        const int kl = lane * M + M - 1;  // the interface cell
+        if (kl < len) x[s0 + kl * step] = gv[M - 1] > T(0) ? I : T(0);
+        if (M == 2 && lane * 2 < len) {
+          const T x0 = fma(S, lane > 0 ? Im : T(0), fma(Tr, I, D));
+          x[s0 + lane * 2 * step] = gv[0] > T(0) ? x0 : T(0);
+        }
+      }
+      __syncthreads();
+      return;
+    }
     if (std::is_same<T, double>::value && len <= 32) {
       // FP64: one warp per line, one cell per lane, cyclic reduction by
       // shuffles -- log2 len steps instead of 2 len dependent elimination
-      // steps, which the FP64 pipe's latency makes long.  (FP32 keeps the
-      // serial elimination: with the approximate reciprocal the reduction
-      // costs the coarse correction enough accuracy for an extra PCG
-      // iteration.)
+      // steps, which the FP64 pipe's latency makes long.
       const int lane = t & 31, nwarp = NTT >> 5;
       for (int q = colour + 2 * (t >> 5); q < nlines; q += 2 * nwarp) {
         const int si = (dir == 0 ? (q + 1) * w + 1 : w + q + 1) + lane * step;

@@ -1094,9 +1094,12 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
   if ((rc = dev_alloc(h, (void**)&h->ncoarse, sizeof(int)))) return fail(rc);
   // the single-CTA tail: the first level >= 1 with at most tail_cells() cells
   // whose levels fit one CTA's shared memory (ragged grids may need a later one)
+  // (FP32 tails stage their operators in shared memory and reach 64 x 64
+  // levels; FP64 tails read them through L1 and stop at tail_cells())
   if (!getenv("SCF_NO_TAIL")) {
+    const long pcells = h->mixed && !getenv("SCF_TAIL_CELLS") ? kTailMaxCells32 : tail_cells();
     for (int l = 1; l < nlev; ++l) {
-      if ((long)h->lev[l].nx * h->lev[l].ny > tail_cells() || nlev - l > kTailMaxLevels) continue;
+      if ((long)h->lev[l].nx * h->lev[l].ny > pcells || nlev - l > kTailMaxLevels) continue;
       auto fill = [&](auto& d, auto view) {
         d.n = nlev - l;
         for (int k = 0; k < d.n; ++k) d.lv[k] = view(l + k);
@@ -1105,15 +1108,19 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
         d.Ainv = h->Ainv; d.cmap = h->cmap; d.nc = h->ncoarse;
         return tail_prepare(d);
       };
-      int bad = fill(h->tail64, [h](int k) { return view64(h, k); });
-      if (h->mixed) bad |= fill(h->tail32, [h](int k) { return h->mix[k]; });
+      const int bad = h->mixed ? fill(h->tail32, [h](int k) { return h->mix[k]; })
+                               : fill(h->tail64, [h](int k) { return view64(h, k); });
       if (!bad) { h->tail0 = l; break; }
     }
   }
-  // the single-CTA tail of the line smoother, chosen the same way
+  // the single-CTA tail of the line smoother, chosen the same way; its FP32
+  // lines are solved by a warp each (up to 64 cells), so FP32 tails reach
+  // 64 x 64 levels
   if (o.smoother != SCF_SMOOTH_POINT && !getenv("SCF_NO_TAIL")) {
+    const long lcells = h->mixed && !getenv("SCF_TAIL_CELLS") ? kLineTailMaxCells32 : tail_cells();
     for (int l = 1; l < nlev; ++l) {
-      if ((long)h->lev[l].nx * h->lev[l].ny > tail_cells() || nlev - l + 1 > kTailMaxLevels)
+      if ((long)h->lev[l].nx * h->lev[l].ny > lcells || h->lev[l].nx > 64 || h->lev[l].ny > 64 ||
+          nlev - l + 1 > kTailMaxLevels)
         continue;
       auto fill = [&](auto& d, auto view) {
         d.n = nlev - l;
