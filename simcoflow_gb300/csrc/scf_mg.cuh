@@ -33,7 +33,6 @@ struct MgView {
 // The coarse end of a V-cycle in one CTA (levels of at most kTailMaxCells
 // cells, the last of them the coarsest).
 constexpr int kTailMaxCells = 1024;
-constexpr int kTailMaxCells32 = 4096;      // FP32 point tails (operators staged)
 constexpr int kLineTailMaxCells32 = 4096;  // FP32 line tails (lines of at most 64 cells)
 constexpr int kTailMaxLevels = 12;
 template <class T, class CT>

