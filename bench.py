@@ -290,11 +290,14 @@ def device_arm(case, tdev, local, precision, *, steps, warmup, precond="mg", sch
         # tolerance on this workload (the line smoother varies only omega)
         if schedule is None and tune:
             from simcoflow_gb300 import batch as Bt
-            cands = Bt.SCHEDULES if smoother == "point" else sorted(
-                {(2, 2, sc[2]) for sc in Bt.SCHEDULES})
+            # point smoother: every schedule with every sweep tile
+            cands = ([(*sc, tn) for tn in Bt.TILES for sc in Bt.SCHEDULES]
+                     if smoother == "point" else sorted({(2, 2, sc[2]) for sc in Bt.SCHEDULES}))
             best = None
             for sch in cands:
-                s.set_schedule(*sch)
+                s.set_schedule(*sch[:3])
+                if len(sch) > 3:
+                    s.set_tile(Bt.TILES[sch[3]])
                 step()
                 torch.cuda.synchronize(dev)
                 t0 = time.perf_counter()
@@ -306,7 +309,10 @@ def device_arm(case, tdev, local, precision, *, steps, warmup, precond="mg", sch
                     best = (ms_t, sch)
             schedule = best[1] if best else None
         if schedule is not None:
-            s.set_schedule(*schedule)
+            s.set_schedule(*schedule[:3])
+            if len(schedule) > 3:
+                from simcoflow_gb300 import batch as Bt
+                s.set_tile(Bt.TILES[schedule[3]])
         for _ in range(warmup):
             st = step()
         if pg:
@@ -397,7 +403,10 @@ def e2e_arm(case, local, stream, *, steps, warmup, schedule, pg=None, solid=Fals
     try:
         hs.set_stream(stream.cuda_stream)
         if schedule:
-            hs.set_schedule(*schedule)
+            hs.set_schedule(*schedule[:3])
+            if len(schedule) > 3:
+                from simcoflow_gb300 import batch as Bt
+                hs.set_tile(Bt.TILES[schedule[3]])
         hs.set_grid(H["dx"], H["dy"], H["dxU"], H["dyV"])
         h2d = (sum(H[k].nbytes for k in geo_keys + ["DpU", "DpV", "ustar", "vstar"]) +
                hu.nbytes + hv.nbytes + hpp.nbytes)
@@ -1016,7 +1025,8 @@ def run_ours(args):
         "iters": mixed["iters"][-1], "relres_true": mixed["relres"][-1],
         "levels": mixed["levels"], "asym_faces": mixed["asym_faces"],
         "schedule": {"npre_npost_omega": mixed["schedule"],
-                     "source": "autotuner (simcoflow_gb300.batch.SCHEDULES), per arm"},
+                     "source": "autotuner (simcoflow_gb300.batch.SCHEDULES, and TILES for the "
+                               "point smoother), per arm"},
         "plain_fp64_mg_pcg": arm_line(plain, "fp64"),
         "speedup_vs_plain_fp64": round(plain["ms"] / ms_step, 3),
         "e2e": {k: v for k, v in e2e.items() if k != "out"},

@@ -135,6 +135,16 @@ int scf_proj_solve_rhs(struct scf_proj *h, const double *b, double *x, double *r
  * autotuner. */
 int scf_proj_set_opts(struct scf_proj *h, int npre, int npost, double omega);
 
+/* Sweep tile of the red-black (point) smoother on an existing handle;
+ * rebuilds its graph.  SCF_TILE_64X32 (default): 64 x 32 cells per CTA, the
+ * larger FP32 levels staged by TMA; SCF_TILE_32X32: 32 x 32 cells per CTA,
+ * plain loads on every level (twice the CTAs, for small grids).  Both give
+ * the same iterates bit for bit; the autotuner picks by time.  No effect on
+ * the line smoother.  No counterpart in the reference. */
+#define SCF_TILE_64X32 0
+#define SCF_TILE_32X32 1
+int scf_proj_set_tile(struct scf_proj *h, int tile);
+
 /* Batched projections: many independent, assembled handles (device-pointer
  * mode, one device, MG preconditioner, graphs on) solved by ONE graph
  * launch.  Each instance is an independent branch of the graph: operator

@@ -9,8 +9,9 @@ Every instance is a handle of the C-ABI in device-pointer mode; the batch
 graph (scf_batch_* in include/scf_proj.h) holds one independent branch per
 instance: operator setup, right-hand side, the PCG loop as a conditional
 WHILE node, the correction.  The autotuner times each candidate schedule
-(pre/post sweeps, coarse-correction scale) on one representative instance of
-every size class and keeps the fastest time to the tolerance.
+(pre/post sweeps, coarse-correction scale) with each sweep tile shape on one
+representative instance of every size class and keeps the fastest time to
+the tolerance.
 """
 from __future__ import annotations
 
@@ -28,6 +29,9 @@ from . import projection as P
 # class), and of a single large projection, which also tries omega 1.97
 BATCH_SCHEDULES = [(1, 1, 1.9), (2, 2, 1.9), (2, 2, 1.95), (2, 1, 1.9), (3, 3, 1.9), (1, 2, 1.9)]
 SCHEDULES = BATCH_SCHEDULES + [(2, 2, 1.97)]
+# sweep tiles of the point smoother (scf_proj_set_tile): 64 x 32 cells per
+# CTA (TMA-staged on the larger FP32 levels) and 32 x 32 (plain loads)
+TILES = {"64x32": 0, "32x32": 1}
 
 
 def size_class(nx: int, ny: int) -> int:
@@ -75,8 +79,10 @@ class _Instance:
         self.s.close()
 
 
-def autotune(insts, schedules=BATCH_SCHEDULES, reps=3, log=None):
-    """Fastest schedule per size class: {class: (npre, npost, omega)}."""
+def autotune(insts, schedules=BATCH_SCHEDULES, tiles=TILES, reps=3, log=None):
+    """Fastest schedule and sweep tile per size class:
+    {class: (npre, npost, omega, tile name)}.  Every schedule is timed with
+    every tile on one representative instance of the class."""
     import torch
     table = {}
     reps_by_class = {}
@@ -84,17 +90,19 @@ def autotune(insts, schedules=BATCH_SCHEDULES, reps=3, log=None):
         reps_by_class.setdefault(size_class(inst.case.nx, inst.case.ny), inst)
     for cls, inst in sorted(reps_by_class.items()):
         best = None
-        for sch in schedules:
-            inst.s.set_schedule(*sch)
-            inst.solve_once()  # warm (graph build)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            for _ in range(reps):
-                st = inst.solve_once()
-            torch.cuda.synchronize()
-            ms = (time.perf_counter() - t0) / reps * 1e3
-            if st.status == 0 and (best is None or ms < best[0]):
-                best = (ms, sch, st.iters)
+        for tname, tile in tiles.items():
+            inst.s.set_tile(tile)
+            for sch in schedules:
+                inst.s.set_schedule(*sch)
+                inst.solve_once()  # warm (graph build)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                for _ in range(reps):
+                    st = inst.solve_once()
+                torch.cuda.synchronize()
+                ms = (time.perf_counter() - t0) / reps * 1e3
+                if st.status == 0 and (best is None or ms < best[0]):
+                    best = (ms, (*sch, tname), st.iters)
         table[cls] = best[1]
         if log:
             log(f"autotune class 2^{cls}: {best[1]} {best[0]:.2f} ms, {best[2]} iterations")
@@ -113,7 +121,8 @@ class BatchProjector:
         for inst in self.insts:
             sch = self.table.get(size_class(inst.case.nx, inst.case.ny))
             if sch is not None:
-                inst.s.set_schedule(*sch)
+                inst.s.set_schedule(*sch[:3])
+                inst.s.set_tile(TILES[sch[3]] if len(sch) > 3 else 0)
         L = P.load()
         handles = (C.c_void_p * len(self.insts))(*[i.s._h.value for i in self.insts])
         b = C.c_void_p()

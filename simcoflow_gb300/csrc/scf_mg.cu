@@ -27,6 +27,9 @@ namespace scf {
 namespace {
 
 constexpr int SX = 64, SY = 32, NT = 256;
+// the second tile shape of the plain-load sweep (an autotuner candidate):
+// twice the CTAs of the default tile on a level, for small grids
+constexpr int SX2 = 32, SY2 = 32;
 
 template <class CT, class T>
 __device__ __forceinline__ T cload(const CT* p, size_t k, float cs);
@@ -90,7 +93,7 @@ __device__ bool grid_sum2(double a, double b, double* part, unsigned* ticket, do
 
 
 template <class T, class CT, class BT, int FIRST, bool ZERO, bool PROLONG, bool RESTRICT, bool RZ,
-          int ITER>
+          int ITER, int TX, int TY>
 __global__ void __launch_bounds__(NT)
 k_sweep(MgView<T, CT, BT> L, MgView<T, CT, T> C, T omega, int flexible, Scalars* sc,
         double* part) {
@@ -99,10 +102,10 @@ k_sweep(MgView<T, CT, BT> L, MgView<T, CT, T> C, T omega, int flexible, Scalars*
   // x halo: one ring per colour phase (ITER red-black iterations), plus one
   // for the residual of the restriction
   constexpr int H = 2 * ITER + (RESTRICT ? 1 : 0);
-  constexpr int WX = SX + 2 * H, WY = SY + 2 * H;
+  constexpr int WX = TX + 2 * H, WY = TY + 2 * H;
   __shared__ T xs[WY][WX];
   const int nx = L.nx, ny = L.ny, P = L.pitch;
-  const int x0 = blockIdx.x * SX, y0 = blockIdx.y * SY;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   const int t = tlin();
   const float cs = L.csp ? __ldg(L.csp) : 1.0f;
 
@@ -140,7 +143,7 @@ k_sweep(MgView<T, CT, BT> L, MgView<T, CT, T> C, T omega, int flexible, Scalars*
   for (int q = 0; q < 2 * ITER; ++q) {
     const int colour = (q & 1) ? 1 - FIRST : FIRST;
     const int R = H - 1 - q;
-    const int CW = (SX + 2 * R) / 2, RH = SY + 2 * R;
+    const int CW = (TX + 2 * R) / 2, RH = TY + 2 * R;
     for (int e = t; e < CW * RH; e += NT) {
       const int k = e % CW, ey = e / CW;
       const int gy = y0 - R + ey;
@@ -153,8 +156,8 @@ k_sweep(MgView<T, CT, BT> L, MgView<T, CT, T> C, T omega, int flexible, Scalars*
   // phase 3: write the tile; optional r.z (accumulated in T per thread, then
   // combined in FP64)
   T a1 = T(0);
-  for (int e = t; e < SX * SY; e += NT) {
-    const int ex = e % SX, ey = e / SX;
+  for (int e = t; e < TX * TY; e += NT) {
+    const int ex = e % TX, ey = e / TX;
     const int gx = x0 + ex, gy = y0 + ey;
     if (gx < nx && gy < ny) {
       const size_t g = (size_t)gy * P + gx;
@@ -167,8 +170,8 @@ k_sweep(MgView<T, CT, BT> L, MgView<T, CT, T> C, T omega, int flexible, Scalars*
   if (RESTRICT) {
     // residual of each tile cell, summed 2x2 onto the coarse level
     const int I0 = x0 >> 1, J0 = y0 >> 1;
-    for (int e = t; e < (SX / 2) * (SY / 2); e += NT) {
-      const int ci = e % (SX / 2), cj = e / (SX / 2);
+    for (int e = t; e < (TX / 2) * (TY / 2); e += NT) {
+      const int ci = e % (TX / 2), cj = e / (TX / 2);
       const int I = I0 + ci, J = J0 + cj;
       if (I >= C.nx || J >= C.ny) continue;
       T s = T(0);
@@ -839,7 +842,9 @@ bool pdl_enabled() {
 
 thread_local long long g_launches = 0;
 
-static dim3 tiles(int nx, int ny) { return dim3((nx + SX - 1) / SX, (ny + SY - 1) / SY); }
+static dim3 tiles(int nx, int ny, int tx = SX, int ty = SY) {
+  return dim3((nx + tx - 1) / tx, (ny + ty - 1) / ty);
+}
 static dim3 small_grid(int nx, int ny) {
   int gy = (ny + 7) / 8;
   return dim3((nx + 31) / 32, gy < 1024 ? gy : 1024);
@@ -855,17 +860,27 @@ static dim3 reduce_grid(int nx, int ny) {
 template <class T, class CT, class BT>
 void launch_sweep(const MgView<T, CT, BT>& L, const MgView<T, CT, T>& C, int first, bool zero,
                   bool prolong, bool restrict_, bool rz, double omega, int flexible, Scalars* sc,
-                  double* part, cudaStream_t s, int iters) {
-  const dim3 g = tiles(L.nx, L.ny);
+                  double* part, cudaStream_t s, int iters, int tile) {
   const T om = (T)omega;
 #define SCF_SWEEP(F, Z, PR, RS, R)                                                              \
   do {                                                                                          \
-    if (iters == 2)                                                                             \
-      launch_k(k_sweep<T, CT, BT, F, Z, PR, RS, R, 2>, g, dim3(NT), 0, s, L, C, om, flexible,  \
-               sc, part);                                                                       \
-    else                                                                                        \
-      launch_k(k_sweep<T, CT, BT, F, Z, PR, RS, R, 1>, g, dim3(NT), 0, s, L, C, om, flexible,  \
-               sc, part);                                                                       \
+    if (tile == 1) {                                                                            \
+      const dim3 g = tiles(L.nx, L.ny, SX2, SY2);                                               \
+      if (iters == 2)                                                                           \
+        launch_k(k_sweep<T, CT, BT, F, Z, PR, RS, R, 2, SX2, SY2>, g, dim3(NT), 0, s, L, C, om, \
+                 flexible, sc, part);                                                           \
+      else                                                                                      \
+        launch_k(k_sweep<T, CT, BT, F, Z, PR, RS, R, 1, SX2, SY2>, g, dim3(NT), 0, s, L, C, om, \
+                 flexible, sc, part);                                                           \
+    } else {                                                                                    \
+      const dim3 g = tiles(L.nx, L.ny);                                                         \
+      if (iters == 2)                                                                           \
+        launch_k(k_sweep<T, CT, BT, F, Z, PR, RS, R, 2, SX, SY>, g, dim3(NT), 0, s, L, C, om,   \
+                 flexible, sc, part);                                                           \
+      else                                                                                      \
+        launch_k(k_sweep<T, CT, BT, F, Z, PR, RS, R, 1, SX, SY>, g, dim3(NT), 0, s, L, C, om,   \
+                 flexible, sc, part);                                                           \
+    }                                                                                           \
   } while (0)
   // the combinations the V-cycle uses (pre: red first; post: black first)
   if (first == 0 && zero && !prolong && !restrict_ && !rz) SCF_SWEEP(0, true, false, false, false);
@@ -1026,7 +1041,7 @@ bool make_sweep_maps(const MgView<float, __nv_bfloat16, float>& L, float* const 
 #define SCF_INST(T, CT, BT)                                                                   \
   template void launch_sweep<T, CT, BT>(const MgView<T, CT, BT>&, const MgView<T, CT, T>&, int, \
                                         bool, bool, bool, bool, double, int, Scalars*, double*, \
-                                        cudaStream_t, int);                                     \
+                                        cudaStream_t, int, int);                                \
   template void launch_coarse_solve_t<T, CT, BT>(const MgView<T, CT, BT>&, const double*,      \
                                                  const int*, const int*, Scalars*, cudaStream_t);
 SCF_INST(double, double, double)

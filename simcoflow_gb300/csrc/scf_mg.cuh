@@ -81,10 +81,11 @@ void launch_sweep_tma(const MgView<float, __nv_bfloat16, float>& L,
                       int iters);
 
 // One fused launch of `iters` (1 or 2) red-black iterations on level L.
+// tile 0: 64 x 32 cells per CTA; 1: 32 x 32 (see SCF_TILE_* in scf_proj.h).
 template <class T, class CT, class BT>
 void launch_sweep(const MgView<T, CT, BT>& L, const MgView<T, CT, T>& C, int first, bool zero,
                   bool prolong, bool restrict_, bool rz, double omega, int flexible, Scalars* sc,
-                  double* part, cudaStream_t s, int iters = 1);
+                  double* part, cudaStream_t s, int iters = 1, int tile = 0);
 
 template <class T, class CT, class BT>
 void launch_coarse_solve_t(const MgView<T, CT, BT>& C, const double* Ainv, const int* cmap,

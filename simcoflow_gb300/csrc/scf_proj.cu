@@ -53,6 +53,7 @@ struct scf_proj {
   bool late_pending = false;
   bool devptrs = false;
   bool mixed = false;
+  int tile = SCF_TILE_64X32;  // point-smoother sweep tile (scf_proj_set_tile)
 
   // FP64 multigrid levels (setup hierarchy; level 0 is the fine operator of
   // the PCG, its b is the PCG residual r and its x the FP64 z)
@@ -197,7 +198,7 @@ float* buf32(scf_proj* h, int l, int i) { return i == 0 ? h->mix[l].x : h->x2_32
 // tensor maps were accepted (SCF_NO_TMA turns it off)
 bool tma_level(const scf_proj* h, int l) {
   static const bool off = getenv("SCF_NO_TMA") != nullptr;
-  return !off && l < (int)h->tma.size() && h->tma[l];
+  return !off && h->tile == SCF_TILE_64X32 && l < (int)h->tma.size() && h->tma[l];
 }
 
 // Largest level handled by the single-CTA tails (SCF_TAIL_CELLS overrides
@@ -278,7 +279,7 @@ void enqueue_vcycle_t(scf_proj* h, ViewFn view, BufFn buf, const TailDesc<T, CT>
         }
       }
       launch_sweep(f, c, 0, it == 0, false, it == npre - 1, false, om, flexible, sc, h->part, s,
-                   pre[it]);
+                   pre[it], h->tile);
     }
   }
   if (h->tail0 > 0) {
@@ -302,7 +303,8 @@ void enqueue_vcycle_t(scf_proj* h, ViewFn view, BufFn buf, const TailDesc<T, CT>
           continue;
         }
       }
-      launch_sweep(f, c, 1, false, it == 0, false, rz, om, flexible, sc, h->part, s, post[it]);
+      launch_sweep(f, c, 1, false, it == 0, false, rz, om, flexible, sc, h->part, s, post[it],
+                   h->tile);
     }
   }
 }
@@ -1567,13 +1569,13 @@ int scf_proj_time_kernel(scf_proj* h, int kernel, int reps, double* ms) {
                            1, h->sc_diag, h->part, s, iters);
         else
           launch_sweep(V, h->mix[1], pre ? 0 : 1, zero, prol, restr, rz, om, 1, h->sc_diag,
-                       h->part, s, iters);
+                       h->part, s, iters, h->tile);
       } else {
         MgD V = view64(h, 0);
         V.xin = pre ? nullptr : buf64(h, 0, 0);
         V.x = buf64(h, 0, 1);
         launch_sweep(V, view64(h, 1), pre ? 0 : 1, zero, prol, restr, rz, om, 0, h->sc_diag,
-                     h->part, s, iters);
+                     h->part, s, iters, h->tile);
       }
       return;
     }
@@ -1749,6 +1751,17 @@ int scf_proj_set_opts(scf_proj* h, int npre, int npost, double omega) {
   h->tail32.omega = (float)omega;
   h->ltail64.omega = omega;
   h->ltail32.omega = (float)omega;
+  destroy_graph(h);
+  if (h->assembled && !(h->opts.flags & SCF_FLAG_NO_GRAPH)) return build_graph(h);
+  return SCF_OK;
+}
+
+int scf_proj_set_tile(scf_proj* h, int tile) {
+  if (!h || (tile != SCF_TILE_64X32 && tile != SCF_TILE_32X32)) return SCF_ERR_ARG;
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  if (tile == h->tile) return SCF_OK;
+  h->tile = tile;
   destroy_graph(h);
   if (h->assembled && !(h->opts.flags & SCF_FLAG_NO_GRAPH)) return build_graph(h);
   return SCF_OK;

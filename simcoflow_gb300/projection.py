@@ -45,7 +45,7 @@ EXPORTS = ["scf_opts_default", "scf_proj_create", "scf_proj_destroy", "scf_proj_
            "scf_proj_set_network", "scf_proj_solve_rhs", "scf_proj_set_opts",
            "scf_batch_create", "scf_batch_set_io", "scf_batch_run", "scf_batch_destroy",
            "scf_proj_set_solid", "scf_proj_get_geometry", "scf_diag_divide",
-           "scf_proj_get_matrix", "scf_diag_tma_timeout"]
+           "scf_proj_get_matrix", "scf_diag_tma_timeout", "scf_proj_set_tile"]
 # every symbol declared in include/scf_unet.h
 UNET_EXPORTS = ["scf_unet_num_params", "scf_unet_create", "scf_unet_destroy",
                 "scf_unet_set_stream", "scf_unet_set_params", "scf_unet_get_params",
@@ -114,6 +114,7 @@ def load():
         L.scf_proj_set_network.argtypes = [vp, vp, C.c_int]
         L.scf_proj_solve_rhs.argtypes = [vp, dp, dp, dp, C.c_int, C.POINTER(Stats)]
         L.scf_proj_set_opts.argtypes = [vp, C.c_int, C.c_int, C.c_double]
+        L.scf_proj_set_tile.argtypes = [vp, C.c_int]
         L.scf_batch_create.argtypes = [C.POINTER(vp), C.POINTER(vp), C.c_int]
         L.scf_batch_set_io.argtypes = [vp, C.c_int, dp, dp, C.c_double, dp, dp, dp, dp, dp]
         L.scf_batch_run.argtypes = [vp, vp, C.POINTER(Stats)]
@@ -327,6 +328,12 @@ class ProjectionSolver:
         _check(load().scf_proj_set_opts(self._h, npre, npost, omega), "scf_proj_set_opts")
         self.opts.npre, self.opts.npost, self.opts.omega = npre, npost, omega
 
+    def set_tile(self, tile: int):
+        """Sweep tile of the point smoother: 0 = 64x32 (TMA-staged on large
+        FP32 levels), 1 = 32x32 (plain loads); rebuilds the handle's graph."""
+        _check(load().scf_proj_set_tile(self._h, int(tile)), "scf_proj_set_tile")
+        self.tile = int(tile)
+
     def set_network(self, params):
         """Weights of the learned preconditioner (float32 array of
         scf_unet_num_params() values, order of include/scf_unet.h)."""
@@ -394,11 +401,14 @@ def divide(a, b, device: int = 0):
     return q
 
 
-def project_case(case, **opts):
+def project_case(case, tile=None, **opts):
     """Full projection of a synth.Case through the C-ABI with host arrays:
-    returns dict(Pp, u, v, p, mres, stats)."""
+    returns dict(Pp, u, v, p, mres, stats).  tile: sweep tile of the point
+    smoother (None: the default)."""
     s = ProjectionSolver(case.nx, case.ny, **opts)
     try:
+        if tile is not None:
+            s.set_tile(tile)
         s.setup_case(case)
         a = case.arrays
         u, v, p = a["u0"].copy(order="F"), a["v0"].copy(order="F"), a["p0"].copy(order="F")

@@ -38,6 +38,9 @@ def test_batch_equals_single_instance_and_oracle(cuda, oracle):
         # a second launch of the same graph gives the same answers
         stats2, _ = bp.run()
         assert [s["iters"] for s in stats2] == [s["iters"] for s in stats]
+        # the autotuner chose a schedule and a sweep tile for every size class
+        for cls, entry in bp.table.items():
+            assert len(entry) == 4 and entry[3] in B.TILES, (cls, entry)
     finally:
         bp.close()
 
