@@ -139,7 +139,8 @@ int scf_proj_set_opts(struct scf_proj *h, int npre, int npost, double omega);
  * rebuilds its graph.  SCF_TILE_64X32 (default): 64 x 32 cells per CTA, the
  * larger FP32 levels staged by TMA; SCF_TILE_32X32: 32 x 32 cells per CTA,
  * plain loads on every level (twice the CTAs, for small grids).  Both give
- * the same iterates bit for bit; the autotuner picks by time.  No effect on
+ * the same V-cycle bit for bit (the PCG's r.z, summed per tile, differs in
+ * the last bits); the autotuner picks by time.  No effect on
  * the line smoother.  No counterpart in the reference. */
 #define SCF_TILE_64X32 0
 #define SCF_TILE_32X32 1

@@ -334,15 +334,27 @@ def test_wall_case_with_line_smoother(cuda, oracle, precision):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_sweep_tiles_give_the_same_iterates(cuda, oracle, precision):
+def test_sweep_tiles_give_the_same_vcycle(cuda, oracle, precision):
     """The point smoother's two sweep tiles (64x32 with TMA staging on the
     larger FP32 levels, 32x32 with plain loads) recompute their halo rings
-    exactly, so both give global red-black half-sweeps: the same projection
-    bit for bit."""
+    exactly, so both give global red-black half-sweeps: the same V-cycle bit
+    for bit.  The PCG's r.z is summed per tile, so beta and the iterates then
+    differ in the last bits only: both projections meet the parity bar."""
     c = synth.c5(instance=3, n=288)
-    a = _gpu_project(c, precision=precision, tile=0)
-    b = _gpu_project(c, precision=precision, tile=1)
-    assert a["stats"]["smoother"] == P.SMOOTHERS["point"]
-    assert a["stats"]["iters"] == b["stats"]["iters"]
-    for k in ("Pp", "u", "v", "p", "mres"):
-        assert np.array_equal(a[k], b[k]), k
+    rng = np.random.Generator(np.random.PCG64(3))
+    b = np.asfortranarray(rng.normal(size=(c.nx, c.ny)) * _active(c))
+    xs = []
+    for tile in (0, 1):
+        s = P.ProjectionSolver(c.nx, c.ny, precision=precision)
+        try:
+            s.set_tile(tile)
+            s.setup_case(c)
+            xs.append(s.vcycle(b))
+        finally:
+            s.close()
+    assert np.array_equal(xs[0], xs[1])
+    exp = oracle.project(c)
+    for tile in (0, 1):
+        g = _gpu_project(c, precision=precision, tile=tile)
+        assert g["stats"]["smoother"] == P.SMOOTHERS["point"]
+        _check_solution(c, g, exp)
