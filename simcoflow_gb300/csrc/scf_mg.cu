@@ -519,10 +519,24 @@ k_pupdate_spmv_t(LevelView L, const ZT* __restrict__ z, const ZT* __restrict__ p
     double pc = wide(pcr);
     double cNd = col ? L.cN[(size_t)(r0 - 1) * P + cx] : 0.0;
     Raw nxt = load(r0 + 1);
+    // FP32 direction: the operator of a row is loaded one row ahead, like p
+    // (measured faster there; the FP64 form, with more registers live, is not)
+    double dgn = 0.0, cEn = 0.0, cNn = 0.0;
+    if (F32 && col) {
+      const size_t k0 = (size_t)r0 * P + cx;
+      dgn = L.dg[k0]; cEn = L.cE[k0]; cNn = L.cN[k0];
+    }
     for (int iy = r0; iy < r1; ++iy) {
       const size_t k = (size_t)iy * P + cx;
-      double dg = 0.0, cE = 0.0, cN = 0.0;
-      if (col) { dg = L.dg[k]; cE = L.cE[k]; cN = L.cN[k]; }
+      double dg = dgn, cE = cEn, cN = cNn;
+      if constexpr (F32) {
+        if (col && iy + 1 < r1) {
+          const size_t k1 = k + P;
+          dgn = L.dg[k1]; cEn = L.cE[k1]; cNn = L.cN[k1];
+        }
+      } else {
+        if (col) { dg = L.dg[k]; cE = L.cE[k]; cN = L.cN[k]; }
+      }
       const ZT ppr = form(nxt);
       nxt = load(iy + 2);  // one row ahead
       const double pp = wide(ppr);
