@@ -763,37 +763,55 @@ def extra_vtr(case, local, args):
 
 
 def extra_lsweep(case, local, args):
-    """The level-set part of one X_Sweep and one Y_Sweep on the headline grid
-    with device-resident fields, against the C restatement on one core."""
+    """One X_Sweep and one Y_Sweep of the CLSVOF step on the headline grid
+    with device-resident fields: the level-set part alone, and the whole
+    sweep (VOF PLIC fluxes + level set in one kernel), against the C
+    restatement on one core."""
     import torch
     from simcoflow_gb300 import clsvof as CL
-    from gen.synth import ls_fields
+    from gen.synth import ls_fields, vof_fields, wave_inlet
     nx, ny = case.nx, case.ny
     f = ls_fields(np.random.default_rng(29), nx, ny)
+    v = vof_fields(np.random.default_rng(31), nx, ny, f)
+    wave = wave_inlet(f)
     t0 = np.asfortranarray(np.random.default_rng(30).standard_normal((nx, ny)))
     dev = torch.device("cuda", local)
-    tf = {k: torch.from_numpy(np.ascontiguousarray(a.ravel(order="F"))).to(dev)
-          for k, a in f.items()}
-    tt = torch.from_numpy(np.ascontiguousarray(t0.ravel(order="F"))).to(dev)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a.ravel(order="F"))).to(dev)
+    tf, tv = {k: T(a) for k, a in f.items()}, {k: T(a) for k, a in v.items()}
+    tt, tvf = T(t0), T(v["vof"])
     for _ in range(3):
         CL.sweep(CL.X, nx, ny, tf, 1e-4, tt, device_ptrs=True, device=local)
+        CL.clsvof_sweep(CL.X, nx, ny, tf, tv, 1e-4, tvf, temls=tt, wave=wave, device_ptrs=True,
+                        device=local)
     reps = 10
-    ms = 0.0
+    ms = msv = 0.0
     for _ in range(reps):
         ms += CL.sweep(CL.X, nx, ny, tf, 1e-4, tt, device_ptrs=True, device=local)
         ms += CL.sweep(CL.Y, nx, ny, tf, 1e-4, tt, device_ptrs=True, device=local)
-    out = {"workload": f"level-set update of one X_Sweep and one Y_Sweep, {nx}x{ny}",
-           "gpu": {"ms_x_plus_y": round(ms / reps, 3),
-                   "timing": "host clock around scf_ls_sweep (device pointers; each call "
-                             "creates a stream, launches one kernel and synchronises)"}}
+    for _ in range(reps):
+        msv += CL.clsvof_sweep(CL.X, nx, ny, tf, tv, 1e-4, tvf, temls=tt, wave=wave,
+                               device_ptrs=True, device=local)
+        msv += CL.clsvof_sweep(CL.Y, nx, ny, tf, tv, 1e-4, tvf, temls=tt, device_ptrs=True,
+                               device=local)
+    out = {"workload": f"one X_Sweep and one Y_Sweep after Interface_Reconstruct, {nx}x{ny} "
+                       "(random interface, solid and aperture fields)",
+           "gpu": {"ms_levelset_x_plus_y": round(ms / reps, 3),
+                   "ms_vof_and_levelset_x_plus_y": round(msv / reps, 3),
+                   "timing": "host clock around scf_ls_sweep / scf_clsvof_sweep (device "
+                             "pointers; each call creates a stream, launches one kernel and "
+                             "synchronises)"}}
     if not args.no_cpu:
         sys.path.insert(0, str(ROOT / "oracle"))
         import oracle as O
         t1 = time.perf_counter()
         O.ls_sweep(1, nx, ny, f, 1e-4, O.ls_sweep(0, nx, ny, f, 1e-4, t0))
         cpu_ms = (time.perf_counter() - t1) * 1e3
-        out["cpu"] = {"ms_x_plus_y": round(cpu_ms, 1), "cores": 1, "kind": "port",
-                      "sample": "the literal sequential loops (C restatement)"}
+        t1 = time.perf_counter()
+        O.vof_sweep(1, nx, ny, f, v, 1e-4, O.vof_sweep(0, nx, ny, f, v, 1e-4, v["vof"], wave))
+        cpu_vof = (time.perf_counter() - t1) * 1e3
+        out["cpu"] = {"ms_levelset_x_plus_y": round(cpu_ms, 1),
+                      "ms_vof_and_levelset_x_plus_y": round(cpu_ms + cpu_vof, 1), "cores": 1,
+                      "kind": "port", "sample": "the literal sequential loops (C restatement)"}
     return out
 
 
@@ -993,7 +1011,7 @@ def run_ours(args):
                  ("momentum_2048", lambda: extra_momentum(c2line, local, args)),
                  ("tecplot_2048", lambda: extra_tecplot(c2line, local, args)),
                  ("vtr_2048", lambda: extra_vtr(c2line, local, args)),
-                 ("ls_sweep_2048", lambda: extra_lsweep(c2line, local, args)),
+                 ("clsvof_sweeps_2048", lambda: extra_lsweep(c2line, local, args)),
                  ("cutcell_2048", lambda: extra_cutcell(c2line, local, args))]
         for name, fn in steps:
             try:

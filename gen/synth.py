@@ -406,8 +406,10 @@ def ls_fields(rng, nx, ny):
     F = np.asfortranarray
     x = np.cumsum(rng.uniform(0.5, 1.5, nx))
     y = np.cumsum(rng.uniform(0.5, 1.5, ny))
-    dx = F(np.broadcast_to(np.gradient(x)[:, None], (nx, ny)).copy())
-    dy = F(np.broadcast_to(np.gradient(y)[None, :], (nx, ny)).copy())
+    gx = np.gradient(x) if nx > 1 else np.diff(x, prepend=0.0)
+    gy = np.gradient(y) if ny > 1 else np.diff(y, prepend=0.0)
+    dx = F(np.broadcast_to(gx[:, None], (nx, ny)).copy())
+    dy = F(np.broadcast_to(gy[None, :], (nx, ny)).copy())
     f = {"phi": F(rng.standard_normal((nx, ny))),
          "vofS": F(rng.choice([0.0, 0.0, 0.3, 1.0], (nx, ny))),
          "dx": dx, "dy": dy,
@@ -418,3 +420,49 @@ def ls_fields(rng, nx, ny):
     f["ue"] = F(rng.standard_normal((nx + 1, ny)))
     f["ve"] = F(rng.standard_normal((nx, ny + 1)))
     return f
+
+
+# ---------------------------------------------------------------------------
+# Inputs of the CLSVOF sweeps' VOF transport (scf_clsvof_sweep)
+# ---------------------------------------------------------------------------
+def vof_fields(rng, nx, ny, f):
+    """Random VOF inputs of one CLSVOF sweep on the grid of ls_fields' f:
+    liquid fractions (empty, full, slightly outside [0,1] and interface
+    cells), the interface normal and distance that Interface_Reconstruct
+    leaves, the solid normal and distance, and solid fractions spread over
+    every branch of the face-flux routines (none, below 1e-3, cut, nearly
+    and fully solid).  Some apertures are set to exactly 1 and some face
+    velocities to 0.  Updates f's vofS, apertures and velocities in place
+    and returns the VOF fields."""
+    F = np.asfortranarray
+    shape = (nx, ny)
+    kind = rng.integers(0, 8, shape)
+    vof = rng.uniform(0.02, 0.98, shape)
+    vof[kind == 0] = 0.0
+    vof[kind == 1] = 1.0
+    vof[kind == 2] = rng.choice([5e-15, -1e-16, 1.0 - 5e-15, 1.0 + 1e-15], int((kind == 2).sum()))
+    f["vofS"][:] = F(rng.choice([0.0, 0.0, 0.0, 5e-4, 0.25, 0.6, 0.9995, 1.0], shape))
+    th = rng.uniform(0.0, 2.0 * np.pi, shape)
+    nxv, nyv = np.cos(th), np.sin(th)
+    axis = rng.integers(0, 6, shape)
+    nxv[axis == 0], nyv[axis == 0] = 0.0, 1.0
+    nxv[axis == 1], nyv[axis == 1] = -1.0, 0.0
+    h = np.hypot(f["dx"], f["dy"])
+    ths = rng.uniform(0.0, 2.0 * np.pi, shape)
+    for k in ("aE", "aW", "aN", "aS"):
+        a = f[k]
+        a[rng.random(a.shape) < 0.3] = 1.0
+    f["ue"][rng.random(f["ue"].shape) < 0.1] = 0.0
+    f["ve"][rng.random(f["ve"].shape) < 0.1] = 0.0
+    return {"vof": F(vof), "nxv": F(nxv), "nyv": F(nyv),
+            "dis": F(rng.uniform(-0.6, 0.6, shape) * h),
+            "nxs": F(np.cos(ths)), "nys": F(np.sin(ths)),
+            "phiS": F(rng.uniform(-0.5, 0.5, shape) * h)}
+
+
+def wave_inlet(f):
+    """X_Sweep's wave-inlet constants {Amp0, kw, omew, Depthw, NondiT, k}
+    with the still-water level inside the grid's first column."""
+    y = f["y"][0]
+    span = max(y[-1] - y[0], float(f["dy"][0, 0]))
+    return np.array([0.05 * span, 2.0 * np.pi / span, 0.7, 0.5 * (y[0] + y[-1]), 1.25, 3.0])

@@ -1,22 +1,30 @@
-/* scf_clsvof.h -- level-set transport of SIMCOFlow's CLSVOF sweeps on the GPU.
+/* scf_clsvof.h -- SIMCOFlow's CLSVOF sweeps on the GPU.
  *
- * Replaces the level-set part of X_Sweep (src/Clsvof_Mod.f90:1074-1123) and
- * of Y_Sweep (:1191-1244): the face fluxes of the level set phi (central
- * averages inside, the one-sided slope formulas on the first and last
- * faces) and their update of temls, which the reference applies in one
- * sequential loop over faces.  Each cell's result here is the value that
- * loop leaves, with the same operations in the same order (IEEE FP64, no
- * FMA contraction), so the output is bit-identical to a literal restatement
- * of those loops.  The VOF part of the sweeps (PLIC face fluxes after
- * Interface_Reconstruct) and Redistance are not part of this library.
+ * Replaces X_Sweep (src/Clsvof_Mod.f90:989-1124) and Y_Sweep (:1126-1245)
+ * after their call of Interface_Reconstruct:
+ *  - the level-set part (:1074-1123, :1191-1244): face fluxes of phi
+ *    (central averages inside, one-sided slope formulas on the first and
+ *    last faces) and their update of temls;
+ *  - the VOF part (:1004-1069, :1141-1189): the PLIC face fluxes of the
+ *    upwind cell (frac for cells without solid, CellGeoCal for cut cells,
+ *    the full/empty and solid shortcuts of topflux .. leftflux, :1416-1522),
+ *    their update of temvf after its division by (1 - vofS), and the
+ *    inflow through the first face (X: the wave inlet, Y: vof ve(0) dtv).
+ * The reference applies each in one sequential loop over faces.  Each
+ * cell's result here is the value that loop leaves, with the same
+ * operations in the same order (IEEE FP64, no FMA contraction), so the
+ * output is bit-identical to a literal restatement of those loops.
+ * Interface_Reconstruct, Redistance and the updates of Coupled_LS_VOF
+ * between the sweeps are not part of this library.
  *
  * Arrays are the reference's Fortran arrays (column-major):
  *   (nx,ny)      phi, vofS, dx, dy, x, y, temls   (1:Isize,1:Jsize)
  *   (nx+2,ny+2)  aE, aW, aN, aS                   E/W/N/SEdge_Area (0:Isize+1,0:Jsize+1)
  *   (nx+1,ny)    ue                               ue(0:Isize,1:Jsize)
  *   (nx,ny+1)    ve                               ve(1:Isize,0:Jsize)
- * Host pointers, or device pointers with SCF_LS_DEVICE_PTRS.  nx, ny >= 3
- * (the boundary formulas read three cells).
+ *   (nx,ny)      vof, nx, ny, dis, nxs, nys, phiS, temvf
+ * Host pointers, or device pointers with SCF_LS_DEVICE_PTRS.  The level-set
+ * update needs nx, ny >= 3 (its boundary formulas read three cells).
  */
 #ifndef SCF_CLSVOF_H
 #define SCF_CLSVOF_H
@@ -42,6 +50,32 @@ typedef struct scf_ls_fields {
  * dtv.  ms, when not NULL, receives the elapsed wall time of the call. */
 int scf_ls_sweep(int dir, int nx, int ny, const scf_ls_fields *f, double dtv, double *temls,
                  int flags, int device, double *ms);
+
+typedef struct scf_vof_fields {
+  const double *vof;            /* vfl = PCell%vof */
+  const double *nx, *ny, *dis;  /* interface normal and distance of Interface_Reconstruct */
+  const double *nxs, *nys;      /* PCell%nxs, PCell%nys */
+  const double *phiS;           /* PCell%phiS */
+} scf_vof_fields;
+
+/* X_Sweep's wave inlet (src/Clsvof_Mod.f90:1057-1068): cells of column 1
+ * whose bottom lies below Depthw + Amp0 sin(kw xwu - omew (NondiT + k dtv)),
+ * xwu = x(1,1) - dx(1,1)/2, take in vof(1,j) ue(0,j) dtv through face 0.
+ * The sine is evaluated on the host (libm), as by the reference. */
+typedef struct scf_vof_wave {
+  double amp0, kw, omew, depthw; /* Amp0, kw, omew, Depthw (src/Main.f90:156-166) */
+  double nondit;                 /* NondiT */
+  int k;                         /* the sub-step k of Coupled_LS_VOF */
+} scf_vof_wave;
+
+/* One whole sweep (X_Sweep or Y_Sweep after Interface_Reconstruct): the VOF
+ * update of temvf (in/out, (nx,ny)) and, when temls is not NULL, the
+ * level-set update of temls, in one kernel.  f->phi is read only with
+ * temls.  wave is read by the X sweep only; NULL: no inflow through face 0
+ * of X.  nx, ny >= 1 (>= 3 with temls). */
+int scf_clsvof_sweep(int dir, int nx, int ny, const scf_ls_fields *f, const scf_vof_fields *v,
+                     const scf_vof_wave *wave, double dtv, double *temvf, double *temls,
+                     int flags, int device, double *ms);
 
 #ifdef __cplusplus
 }

@@ -36,9 +36,13 @@ Pieces:
     vtr         Print_Result_VTK_2D's ParaView file   src/PrintResult.f90:165-190,
                 src/VTR_mod.f90:79-379
     e15_8       its list-directed REAL(4) value text (15 characters)
-  C restatement of the CLSVOF sweeps' level-set part (clsvof_oracle.c)
+  C restatement of the CLSVOF sweeps after Interface_Reconstruct (clsvof_oracle.c)
     ls_sweep    X_Sweep / Y_Sweep temls update   src/Clsvof_Mod.f90:1074-1123,
                 1191-1244
+    vof_sweep   X_Sweep / Y_Sweep temvf update   src/Clsvof_Mod.f90:1004-1069,
+                1141-1189, with topflux .. leftflux (:1416-1522)
+    frac, cellgeocal                             src/Clsvof_Mod.f90:1371-1404,
+                2159-2253
 """
 from __future__ import annotations
 
@@ -109,6 +113,10 @@ def lib():
         L.oracle_vtr.restype = C.c_int64
         L.oracle_vtr.argtypes = [C.c_int, C.c_int] + [_P] * 9 + [C.c_char_p]
         L.oracle_ls_sweep.argtypes = [C.c_int] * 3 + [_P] * 12 + [C.c_double, _P]
+        L.oracle_frac.restype = C.c_double
+        L.oracle_frac.argtypes = [C.c_double] * 5
+        L.oracle_cellgeocal.argtypes = [C.c_double] * 8 + [_P, _P]
+        L.oracle_vof_sweep.argtypes = [C.c_int] * 3 + [_P] * 11 + [_P] * 7 + [_P, C.c_double, _P]
         _lib = L
     return _lib
 
@@ -626,6 +634,33 @@ def ls_sweep(dir, nx, ny, f, dtv, temls):
     out = np.asfortranarray(np.array(temls, dtype=np.float64))
     lib().oracle_ls_sweep(dir, nx, ny, *[_p(f[k]) for k in LS_FIELDS], dtv, _p(out))
     return out
+
+
+VOF_LS_FIELDS = ["vofS", "dx", "dy", "x", "y", "aE", "aW", "aN", "aS", "ue", "ve"]
+VOF_FIELDS = ["vof", "nxv", "nyv", "dis", "nxs", "nys", "phiS"]
+
+
+def vof_sweep(dir, nx, ny, f, v, dtv, temvf, wave=None):
+    """X_Sweep (dir 0) / Y_Sweep (dir 1) VOF update of a copy of temvf
+    (Fortran-ordered (nx,ny)) after Interface_Reconstruct; v holds vof,
+    nxv, nyv, dis, nxs, nys, phiS; wave the X inlet's {Amp0, kw, omew,
+    Depthw, NondiT, k} (None: no inlet flux).  Returns the new array."""
+    out = np.asfortranarray(np.array(temvf, dtype=np.float64))
+    w = None if wave is None else np.ascontiguousarray(wave, dtype=np.float64)
+    lib().oracle_vof_sweep(dir, nx, ny, *[_p(f[k]) for k in VOF_LS_FIELDS],
+                           *[_p(v[k]) for k in VOF_FIELDS], _p(w), dtv, _p(out))
+    return out
+
+
+def frac(nx, ny, diss, dx, dy) -> float:
+    return lib().oracle_frac(nx, ny, diss, dx, dy)
+
+
+def cellgeocal(nxs, nys, phis, nxl, nyl, phil, dx, dy):
+    """(vols, volf) of CellGeoCal."""
+    a, b = C.c_double(), C.c_double()
+    lib().oracle_cellgeocal(nxs, nys, phis, nxl, nyl, phil, dx, dy, C.byref(a), C.byref(b))
+    return a.value, b.value
 
 
 def grid_preprocess_literal(nx, ny, grids, fams, icorprob=True, aln_old=None):

@@ -1,6 +1,8 @@
-"""Python host API over the level-set sweeps of libscf_proj.so
-(include/scf_clsvof.h): the level-set part of X_Sweep / Y_Sweep
-(src/Clsvof_Mod.f90:1074-1123, 1191-1244) on the GPU.
+"""Python host API over the CLSVOF sweeps of libscf_proj.so
+(include/scf_clsvof.h): X_Sweep / Y_Sweep after Interface_Reconstruct
+(src/Clsvof_Mod.f90:989-1124, 1126-1245) on the GPU -- the level-set part
+alone (sweep) or the VOF part with, optionally, the level-set part in the
+same kernel (clsvof_sweep).
 
 Fields are the reference's Fortran arrays (Fortran-ordered numpy float64):
 (nx,ny) phi, vofS, dx, dy, x, y; (nx+2,ny+2) aE, aW, aN, aS; ue (nx+1,ny)
@@ -15,15 +17,27 @@ import numpy as np
 
 from . import projection as P
 
-EXPORTS = ["scf_ls_sweep"]
+EXPORTS = ["scf_ls_sweep", "scf_clsvof_sweep"]
 X, Y = 0, 1
 DEVICE_PTRS = 1
 FIELDS = [("phi", "1"), ("vofS", "1"), ("dx", "1"), ("dy", "1"), ("x", "1"), ("y", "1"),
           ("aE", "0"), ("aW", "0"), ("aN", "0"), ("aS", "0"), ("ue", "u"), ("ve", "v")]
 
 
+VOF_FIELDS = ["vof", "nxv", "nyv", "dis", "nxs", "nys", "phiS"]
+
+
 class LsFields(C.Structure):
     _fields_ = [(n, C.c_void_p) for n, _ in FIELDS]
+
+
+class VofFields(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in VOF_FIELDS]
+
+
+class VofWave(C.Structure):
+    _fields_ = [("amp0", C.c_double), ("kw", C.c_double), ("omew", C.c_double),
+                ("depthw", C.c_double), ("nondit", C.c_double), ("k", C.c_int)]
 
 
 def load():
@@ -32,14 +46,20 @@ def load():
         L.scf_ls_sweep.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_void_p,
                                    C.c_int, C.c_int, C.POINTER(C.c_double)]
         L.scf_ls_sweep.restype = C.c_int
+        L.scf_clsvof_sweep.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_int,
+                                       C.c_int, C.POINTER(C.c_double)]
+        L.scf_clsvof_sweep.restype = C.c_int
         L._ls_bound = True
     return L
 
 
-def _pack(nx, ny, f, device_ptrs):
-    st, keep = LsFields(), []
-    for name, sk in FIELDS:
-        a = f[name]
+def _pack(nx, ny, f, device_ptrs, fields=FIELDS, cls=LsFields, optional=()):
+    st, keep = cls(), []
+    for name, sk in fields:
+        a = f.get(name)
+        if a is None and name in optional:
+            continue
         shape = {"1": (nx, ny), "0": (nx + 2, ny + 2), "u": (nx + 1, ny), "v": (nx, ny + 1)}[sk]
         if device_ptrs:
             import torch
@@ -75,4 +95,43 @@ def sweep(dir: int, nx: int, ny: int, fields: dict, dtv: float, temls, device_pt
     P._check(load().scf_ls_sweep(dir, nx, ny, C.byref(st), float(dtv), ptr,
                                  DEVICE_PTRS if device_ptrs else 0, device, C.byref(ms)),
              "scf_ls_sweep")
+    return ms.value
+
+
+def _target(a, nx, ny, device_ptrs, name):
+    if device_ptrs:
+        import torch
+        if not (isinstance(a, torch.Tensor) and a.is_cuda and a.is_contiguous()
+                and a.dtype == torch.float64 and a.numel() == nx * ny):
+            raise ValueError(f"{name}: expected a contiguous CUDA float64 tensor of {nx * ny} "
+                             "elements")
+        return a.data_ptr()
+    if (not isinstance(a, np.ndarray) or a.shape != (nx, ny) or a.dtype != np.float64
+            or not a.flags["F_CONTIGUOUS"]):
+        raise ValueError(f"{name}: expected a Fortran-ordered float64 (nx,ny)")
+    return a.ctypes.data
+
+
+def clsvof_sweep(dir: int, nx: int, ny: int, fields: dict, vof: dict, dtv: float, temvf,
+                 temls=None, wave=None, device_ptrs: bool = False, device: int = 0) -> float:
+    """One whole X_Sweep (dir X) or Y_Sweep (dir Y) after Interface_Reconstruct:
+    the VOF update of temvf and, when temls is given, the level-set update
+    of temls, in place.  fields as for sweep() (phi only needed with temls);
+    vof holds (nx,ny) vof, nxv, nyv, dis (Interface_Reconstruct's normal and
+    distance), nxs, nys, phiS; wave the X inlet's (Amp0, kw, omew, Depthw,
+    NondiT, k) or None (no inflow through face 0 of X).  Returns the call's
+    elapsed milliseconds."""
+    st, keep = _pack(nx, ny, fields, device_ptrs, optional=("phi",) if temls is None else ())
+    vs, keep2 = _pack(nx, ny, vof, device_ptrs, [(n, "1") for n in VOF_FIELDS], VofFields)
+    pv = _target(temvf, nx, ny, device_ptrs, "temvf")
+    pl = None if temls is None else _target(temls, nx, ny, device_ptrs, "temls")
+    w = None
+    if wave is not None:
+        a, k, o, d, t, kk = wave
+        w = VofWave(float(a), float(k), float(o), float(d), float(t), int(kk))
+    ms = C.c_double(0.0)
+    P._check(load().scf_clsvof_sweep(dir, nx, ny, C.byref(st), C.byref(vs),
+                                     None if w is None else C.byref(w), float(dtv), pv, pl,
+                                     DEVICE_PTRS if device_ptrs else 0, device, C.byref(ms)),
+             "scf_clsvof_sweep")
     return ms.value

@@ -4,6 +4,8 @@ import ctypes
 import re
 from pathlib import Path
 
+import pytest
+
 ROOT = Path(__file__).resolve().parent.parent
 
 
@@ -224,23 +226,28 @@ def test_proj_library_exports_clsvof_header_symbols(built):
     assert sorted(clsvof.EXPORTS) == names
 
 
-def test_ls_fields_struct_layout(tmp_path):
-    """The ctypes mirror of scf_ls_fields has the header's layout."""
+@pytest.mark.parametrize("cname,pyname,rename", [
+    ("scf_ls_fields", "LsFields", {}),
+    ("scf_vof_fields", "VofFields", {"nxv": "nx", "nyv": "ny"}),
+    ("scf_vof_wave", "VofWave", {})])
+def test_clsvof_struct_layouts(tmp_path, cname, pyname, rename):
+    """The ctypes mirrors of scf_ls_fields, scf_vof_fields and scf_vof_wave
+    have the header's layouts."""
     import shutil
     import subprocess
     if not shutil.which("gcc"):
-        import pytest
         pytest.skip("no C compiler")
     from simcoflow_gb300 import clsvof
-    fields = [n for n, _ in clsvof.LsFields._fields_]
+    cls = getattr(clsvof, pyname)
+    fields = [n for n, _ in cls._fields_]
     src = tmp_path / "ls.c"
     src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "scf_clsvof.h"\n'
-                   'int main(void) {\n  printf("%zu\\n", sizeof(scf_ls_fields));\n'
-                   + "".join(f'  printf("%zu\\n", offsetof(scf_ls_fields, {n}));\n'
+                   f'int main(void) {{\n  printf("%zu\\n", sizeof({cname}));\n'
+                   + "".join(f'  printf("%zu\\n", offsetof({cname}, {rename.get(n, n)}));\n'
                              for n in fields) + "  return 0;\n}\n")
     exe = tmp_path / "ls"
     subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
-    assert int(out[0]) == ctypes.sizeof(clsvof.LsFields)
+    assert int(out[0]) == ctypes.sizeof(cls)
     for n, off in zip(fields, out[1:]):
-        assert int(off) == getattr(clsvof.LsFields, n).offset, n
+        assert int(off) == getattr(cls, n).offset, n

@@ -1,6 +1,7 @@
-"""GPU level-set sweeps (include/scf_clsvof.h) against the oracle's literal
-restatement of X_Sweep / Y_Sweep's level-set loops (src/Clsvof_Mod.f90:
-1074-1123, 1191-1244), bit for bit, through the C-ABI."""
+"""GPU CLSVOF sweeps (include/scf_clsvof.h) against the oracle's literal
+restatement of X_Sweep / Y_Sweep after Interface_Reconstruct
+(src/Clsvof_Mod.f90:989-1124, 1126-1245): the level-set loops and the VOF
+loops with their PLIC face fluxes, bit for bit, through the C-ABI."""
 import numpy as np
 import pytest
 
@@ -47,3 +48,96 @@ def test_ls_sweep_rejects_small_grids(cuda):
     t = np.asfortranarray(np.zeros((2, 5)))
     with pytest.raises(P.ProjectionError):
         CL.sweep(CL.X, 2, 5, f, 1e-3, t)
+
+
+# ---------------------------------------------------------------------------
+# Whole sweeps: the VOF part (src/Clsvof_Mod.f90:1004-1069, 1141-1189) with
+# the PLIC face fluxes, and the fused VOF + level-set kernel
+# ---------------------------------------------------------------------------
+def _vof_case(seed, nx, ny):
+    from gen.synth import vof_fields, wave_inlet
+    rng = np.random.default_rng(seed)
+    f = ls_fields(rng, nx, ny)
+    v = vof_fields(rng, nx, ny, f)
+    t = np.asfortranarray(v["vof"] + 0.1 * rng.standard_normal((nx, ny)))
+    return f, v, t, wave_inlet(f)
+
+
+def _same(a, b):
+    return np.array_equal(a, b, equal_nan=True)
+
+
+@pytest.mark.parametrize("dir", [CL.X, CL.Y])
+@pytest.mark.parametrize("nx,ny", [(1, 1), (2, 5), (3, 3), (37, 29), (300, 257)])
+def test_vof_sweep_bit_exact(cuda, oracle, dir, nx, ny):
+    f, v, t, wave = _vof_case(11 * nx + ny + dir, nx, ny)
+    for w in (wave, None):
+        want = oracle.vof_sweep(dir, nx, ny, f, v, 0.3, t, w)
+        got = t.copy(order="F")
+        CL.clsvof_sweep(dir, nx, ny, f, v, 0.3, got, wave=w)
+        assert _same(got, want)
+
+
+@pytest.mark.parametrize("dir", [CL.X, CL.Y])
+def test_clsvof_sweep_fused_levelset_bit_exact(cuda, oracle, dir):
+    """temvf and temls in one kernel: each equals its own literal loops."""
+    nx, ny = 129, 67
+    f, v, t, wave = _vof_case(40 + dir, nx, ny)
+    tl = np.asfortranarray(np.random.default_rng(41).standard_normal((nx, ny)))
+    want_v = oracle.vof_sweep(dir, nx, ny, f, v, 0.2, t, wave)
+    want_l = oracle.ls_sweep(dir, nx, ny, f, 0.2, tl)
+    got_v, got_l = t.copy(order="F"), tl.copy(order="F")
+    CL.clsvof_sweep(dir, nx, ny, f, v, 0.2, got_v, temls=got_l, wave=wave)
+    assert _same(got_v, want_v)
+    assert np.array_equal(got_l, want_l)
+
+
+def test_clsvof_sweeps_device_pointers_1024(cuda, oracle):
+    """Device-resident fields at 1024x1024: an X sweep then a Y sweep on the
+    same temvf / temls, as Coupled_LS_VOF's odd sub-steps order them."""
+    import torch
+    nx = ny = 1024
+    f, v, t, wave = _vof_case(77, nx, ny)
+    tl = np.asfortranarray(np.random.default_rng(78).standard_normal((nx, ny)))
+    want_v = oracle.vof_sweep(1, nx, ny, f, v, 0.1, oracle.vof_sweep(0, nx, ny, f, v, 0.1, t, wave))
+    want_l = oracle.ls_sweep(1, nx, ny, f, 0.1, oracle.ls_sweep(0, nx, ny, f, 0.1, tl))
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a.ravel(order="F"))).cuda()
+    df, dv = {k: T(a) for k, a in f.items()}, {k: T(a) for k, a in v.items()}
+    tv, tt = T(t), T(tl)
+    CL.clsvof_sweep(CL.X, nx, ny, df, dv, 0.1, tv, temls=tt, wave=wave, device_ptrs=True)
+    CL.clsvof_sweep(CL.Y, nx, ny, df, dv, 0.1, tv, temls=tt, device_ptrs=True)
+    back = lambda x: x.cpu().numpy().reshape((nx, ny), order="F")
+    assert _same(back(tv), want_v)
+    assert np.array_equal(back(tt), want_l)
+
+
+def test_vof_sweep_conserves_each_line_2048(cuda):
+    """Full size, no solid, open apertures, closed line ends: every row (X)
+    and column (Y) keeps its liquid volume to rounding."""
+    import torch
+    nx = ny = 2048
+    f, v, _, _ = _vof_case(9, nx, ny)
+    f["vofS"][:] = 0.0
+    for k in ("aE", "aW", "aN", "aS"):
+        f[k][:] = 1.0
+    f["ue"][0, :] = f["ue"][nx, :] = 0.0
+    f["ve"][:, 0] = f["ve"][:, ny] = 0.0
+    t = np.asfortranarray(v["vof"].copy())
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a.ravel(order="F"))).cuda()
+    df, dv = {k: T(a) for k, a in f.items() if k != "phi"}, {k: T(a) for k, a in v.items()}
+    for d in (CL.X, CL.Y):
+        tv = T(t)
+        CL.clsvof_sweep(d, nx, ny, df, dv, 0.05, tv, device_ptrs=True)
+        out = tv.cpu().numpy().reshape((nx, ny), order="F")
+        h = f["dx"] if d == CL.X else f["dy"]
+        assert np.allclose((out * h).sum(axis=d), (t * h).sum(axis=d), rtol=0, atol=1e-9)
+        assert (np.abs(out - t) > 1e-6).mean() > 0.25
+
+
+def test_clsvof_sweep_rejects_bad_arguments(cuda):
+    from simcoflow_gb300 import projection as P
+    f, v, t, _ = _vof_case(2, 2, 5)
+    with pytest.raises(P.ProjectionError):  # the level-set part needs 3 cells a line
+        CL.clsvof_sweep(CL.X, 2, 5, f, v, 1e-3, t.copy(order="F"), temls=t.copy(order="F"))
+    with pytest.raises(P.ProjectionError):
+        CL.clsvof_sweep(2, 2, 5, f, v, 1e-3, t.copy(order="F"))
