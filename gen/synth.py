@@ -466,3 +466,43 @@ def wave_inlet(f):
     y = f["y"][0]
     span = max(y[-1] - y[0], float(f["dy"][0, 0]))
     return np.array([0.05 * span, 2.0 * np.pi / span, 0.7, 0.5 * (y[0] + y[-1]), 1.25, 3.0])
+
+
+def reconstruct_fields(rng, nx, ny, band=3.0):
+    """Random inputs of Interface_Reconstruct on an nx x ny stretched grid:
+    a liquid circle's level set (a signed distance, with noise on a third
+    of the cells so that both branches of the normal's one-sided tests
+    occur), liquid fractions (empty, full, interface values, the edge
+    values around 1e-14; interface values within band cells of the circle),
+    and a solid half-plane through its centre with its normal, distance and
+    solid fractions (the half-plane's, and 5e-4 on a few cells)."""
+    F = np.asfortranarray
+    xs = np.cumsum(rng.uniform(0.5, 1.5, nx))
+    ys = np.cumsum(rng.uniform(0.5, 1.5, ny))
+    x = F(np.broadcast_to(xs[:, None], (nx, ny)).copy())
+    y = F(np.broadcast_to(ys[None, :], (nx, ny)).copy())
+    gx = np.gradient(xs) if nx > 1 else np.ones(1)
+    gy = np.gradient(ys) if ny > 1 else np.ones(1)
+    dx = F(np.broadcast_to(gx[:, None], (nx, ny)).copy())
+    dy = F(np.broadcast_to(gy[None, :], (nx, ny)).copy())
+    cx, cy = rng.uniform(0.3, 0.7) * xs[-1], rng.uniform(0.3, 0.7) * ys[-1]
+    r = 0.3 * min(xs[-1], ys[-1])
+    phi = np.hypot(x - cx, y - cy) - r
+    noisy = rng.random((nx, ny)) < 0.33
+    phi = np.where(noisy, phi * rng.uniform(0.5, 1.5, (nx, ny)), phi)
+    h = np.maximum(dx, dy)
+    th = rng.uniform(0.0, 2.0 * np.pi)
+    nxs, nys = np.cos(th), np.sin(th)
+    c = -(nxs * cx + nys * cy)
+    phis = nxs * x + nys * y + c
+    vofs = frac_v(nxs, nys, phis, dx, dy)  # the solid part, nxs x + nys y + phis < 0
+    vofs[rng.random((nx, ny)) < 0.02] = 5e-4
+    fluid = 1.0 - vofs
+    vof = np.where(phi < -band * h, fluid,
+                   np.where(phi > band * h, 0.0, rng.uniform(0.02, 0.98, (nx, ny)) * fluid))
+    edge = rng.random((nx, ny)) < 0.05
+    vof[edge] = rng.choice([0.0, 1e-14, 2e-14, 1.0 - 2e-14, 1.0], int(edge.sum()))
+    vof = np.minimum(vof, fluid)
+    return {"x": x, "y": y, "dx": dx, "dy": dy, "phi": F(phi), "vof": F(vof), "vofS": F(vofs),
+            "nxs": F(np.full((nx, ny), nxs)), "nys": F(np.full((nx, ny), nys)),
+            "phiS": F(phis)}

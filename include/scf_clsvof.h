@@ -14,8 +14,9 @@
  * cell's result here is the value that loop leaves, with the same
  * operations in the same order (IEEE FP64, no FMA contraction), so the
  * output is bit-identical to a literal restatement of those loops.
- * Interface_Reconstruct, Redistance and the updates of Coupled_LS_VOF
- * between the sweeps are not part of this library.
+ * Interface_Reconstruct, which each sweep calls first, is
+ * scf_interface_reconstruct below.  Redistance and the updates of
+ * Coupled_LS_VOF between the sweeps are not part of this library.
  *
  * Arrays are the reference's Fortran arrays (column-major):
  *   (nx,ny)      phi, vofS, dx, dy, x, y, temls   (1:Isize,1:Jsize)
@@ -76,6 +77,31 @@ typedef struct scf_vof_wave {
 int scf_clsvof_sweep(int dir, int nx, int ny, const scf_ls_fields *f, const scf_vof_fields *v,
                      const scf_vof_wave *wave, double dtv, double *temvf, double *temls,
                      int flags, int device, double *ms);
+
+/* Interface_Reconstruct (src/Clsvof_Mod.f90:1250-1321, UpdateNorVec = 1):
+ * the PLIC interface of every cell from the liquid fraction vof, the level
+ * set phi and the solid's vofS, nxs, nys, phiS -- the unit normal (nxv,
+ * nyv) from Normal_Vector_Irre (:1710-1919) or the one-sided boundary
+ * differences, and the line distance dis from distance (:1323-1369) for
+ * two-phase cells or DistanceFluidCalculate's Ridders root (:1957-2155) for
+ * cells cut by the solid; (0, 1) and the flat-interface distance elsewhere.
+ * Bit-identical to the reference's sequential loop, including the values
+ * its locals carry from one cell to the next (a boundary cell's missing
+ * normal component, a failed bracket's distance).
+ * Where the reference pauses for the operator, the library goes on as after
+ * the operator's "go"; where it reads outside an array or a value never set
+ * it takes a defined one (Vset(1,:) for a direction search whose cosines
+ * are all NaN, 0 for a distance carried from before the first cell, an
+ * empty liquid polygon when the non-solid polygon has no vertex).  Each such
+ * event is counted in *events (may be NULL).  nx, ny >= 3. */
+typedef struct scf_ir_fields {
+  const double *vof, *vofS, *phi; /* PCell%vof, vofS, phi */
+  const double *nxs, *nys, *phiS; /* PCell%nxs, nys, phiS */
+  const double *x, *y, *dx, *dy;  /* PGrid */
+} scf_ir_fields;
+
+int scf_interface_reconstruct(int nx, int ny, const scf_ir_fields *f, double *nxv, double *nyv,
+                              double *dis, int *events, int flags, int device, double *ms);
 
 #ifdef __cplusplus
 }

@@ -364,3 +364,372 @@ void oracle_vof_sweep(int dir, int nx, int ny, const double *vofS, const double 
 #undef V
 #undef TV
 }
+
+/* ------------------------------------------------------------------------
+ * Interface_Reconstruct (src/Clsvof_Mod.f90:1250-1321) with
+ * Normal_Vector_Irre (:1710-1919), distance (:1323-1369),
+ * DistanceFluidCalculate (:1957-2042), zriddr (:2044-2105) and LiqFuncVol
+ * (:2107-2155), as the reference's loop over cells (i outer, j inner).
+ *
+ * The loop's locals nxx, nyy and diss keep their values from one cell to
+ * the next: a flagged cell of column 1 or nx (rows 2..ny-1) takes nyy from
+ * the cell before it, one of row 1 or ny (columns 2..nx-1) takes nxx, and a
+ * three-phase cell whose Ridders bracket fails keeps diss.  Restated as
+ * written, with 0 for their values before the first cell.
+ * Where the reference pauses for the operator ('pause'), reads outside an
+ * array or uses a value never set, this restatement goes on as after the
+ * operator's "go" (or with the documented value) and counts the event in
+ * *events.
+ * Vset is the direction table as Coupled_LS_VOF leaves it (:746-753): its
+ * line 747 sets Vset(1,2) = 1 again instead of Vset(2,2), so Vset(1,:) =
+ * (0, 1) and Vset(2,:) = (0, 0) (module storage, zero at start).
+ * ---------------------------------------------------------------------- */
+static const double VSET[8][2] = {{0, 1}, {0, 0}, {-1, 0}, {-1, -1}, {-1, 1}, {1, 0}, {1, -1}, {1, 1}};
+
+typedef struct {
+  int nx, ny;
+  const double *vfl, *vfls, *phi, *x, *y;
+  int *events;
+} IrCtx;
+
+#define IRC1(a, i, j) (a)[(size_t)((i) - 1) + (size_t)((j) - 1) * (size_t)c->nx]
+
+/* The direction of Vset most parallel to (vx, vy), then the one-sided pair
+ * whose gradient is closer to unit length (:1768-1832 and :1860-1912). */
+static void most_parallel(const IrCtx *c, int i, int j, int imv0, double *nxo, double *nyo) {
+  const double *phi = c->phi, *x = c->x, *y = c->y;
+  const double nuy = 0.075 / 8.0;
+  double vx = (IRC1(phi, i + 1, j) - IRC1(phi, i - 1, j)) / (IRC1(x, i + 1, j) - IRC1(x, i - 1, j));
+  double vy = (IRC1(phi, i, j + 1) - IRC1(phi, i, j - 1)) / (IRC1(y, i, j + 1) - IRC1(y, i, j - 1));
+  double maxv = 0.0, vx1, vx2, vy1, vy2, qv1, qv2;
+  int imv = imv0;
+  for (int ii = 1; ii <= 8; ++ii) {
+    const double a = VSET[ii - 1][0], b = VSET[ii - 1][1];
+    const double cp = fabs(a * vx + b * vy) / (sqrt(a * a + b * b) * sqrt(vx * vx + vy * vy));
+    if (cp >= maxv) {
+      maxv = cp;
+      imv = ii;
+    }
+  }
+  if (imv == 0) { /* the reference reads Vset(0,:) outside the table */
+    ++*c->events;
+    imv = 1;
+  }
+  const double v11 = -VSET[imv - 1][1], v12 = VSET[imv - 1][0];
+  if (v11 == -1) {
+    vx1 = (IRC1(phi, i, j) - IRC1(phi, i - 1, j)) / (IRC1(x, i, j) - IRC1(x, i - 1, j));
+    vx2 = (IRC1(phi, i + 1, j) - IRC1(phi, i, j)) / (IRC1(x, i + 1, j) - IRC1(x, i, j));
+  } else if (v11 == 0) {
+    vx1 = (IRC1(phi, i + 1, j) - IRC1(phi, i - 1, j)) / (IRC1(x, i + 1, j) - IRC1(x, i - 1, j));
+    vx2 = vx1;
+  } else {
+    vx1 = (IRC1(phi, i + 1, j) - IRC1(phi, i, j)) / (IRC1(x, i + 1, j) - IRC1(x, i, j));
+    vx2 = (IRC1(phi, i, j) - IRC1(phi, i - 1, j)) / (IRC1(x, i, j) - IRC1(x, i - 1, j));
+  }
+  if (v12 == -1) {
+    vy1 = (IRC1(phi, i, j) - IRC1(phi, i, j - 1)) / (IRC1(y, i, j) - IRC1(y, i, j - 1));
+    vy2 = (IRC1(phi, i, j + 1) - IRC1(phi, i, j)) / (IRC1(y, i, j + 1) - IRC1(y, i, j));
+  } else if (v12 == 0) {
+    vy1 = (IRC1(phi, i, j + 1) - IRC1(phi, i, j - 1)) / (IRC1(y, i, j + 1) - IRC1(y, i, j - 1));
+    vy2 = vy1;
+  } else {
+    vy1 = (IRC1(phi, i, j + 1) - IRC1(phi, i, j)) / (IRC1(y, i, j + 1) - IRC1(y, i, j));
+    vy2 = (IRC1(phi, i, j) - IRC1(phi, i, j - 1)) / (IRC1(y, i, j) - IRC1(y, i, j - 1));
+  }
+  qv1 = fabs(1.0 - sqrt(vx1 * vx1 + vy1 * vy1));
+  qv2 = fabs(1.0 - sqrt(vx2 * vx2 + vy2 * vy2));
+  if (qv1 < qv2 + nuy) {
+    *nxo = vx1;
+    *nyo = vy1;
+  } else {
+    *nxo = vx2;
+    *nyo = vy2;
+  }
+}
+
+/* Normal_Vector_Irre (:1710-1919) for 1 < i < nx, 1 < j < ny. */
+static void normal_irre(const IrCtx *c, int i, int j, double *nxo, double *nyo) {
+  const double *phi = c->phi, *x = c->x, *y = c->y, *vfls = c->vfls;
+  const double eta = 0.075;
+  const int nx = c->nx, ny = c->ny;
+  double vx, vy, q[3];
+  int dx, dy;
+  if (IRC1(vfls, i, j) >= EPSI) {
+    if (IRC1(vfls, i + 1, j) < 1.0 - EPSI && IRC1(vfls, i - 1, j) < 1.0 - EPSI)
+      *nxo = (IRC1(phi, i + 1, j) - IRC1(phi, i - 1, j)) / (IRC1(x, i + 1, j) - IRC1(x, i - 1, j));
+    else if (IRC1(vfls, i + 1, j) >= 1.0 - EPSI)
+      *nxo = (IRC1(phi, i, j) - IRC1(phi, i - 1, j)) / (IRC1(x, i, j) - IRC1(x, i - 1, j));
+    else
+      *nxo = (IRC1(phi, i + 1, j) - IRC1(phi, i, j)) / (IRC1(x, i + 1, j) - IRC1(x, i, j));
+    if (IRC1(vfls, i, j + 1) < 1.0 - EPSI && IRC1(vfls, i, j - 1) < 1.0 - EPSI)
+      *nyo = (IRC1(phi, i, j + 1) - IRC1(phi, i, j - 1)) / (IRC1(y, i, j + 1) - IRC1(y, i, j - 1));
+    else if (IRC1(vfls, i, j + 1) > 1.0 - EPSI)
+      *nyo = (IRC1(phi, i, j) - IRC1(phi, i, j - 1)) / (IRC1(y, i, j) - IRC1(y, i, j - 1));
+    else
+      *nyo = (IRC1(phi, i, j + 1) - IRC1(phi, i, j)) / (IRC1(y, i, j + 1) - IRC1(y, i, j));
+    return;
+  }
+  if (i >= 3) vx = (IRC1(phi, i, j) - IRC1(phi, i - 2, j)) / (IRC1(x, i, j) - IRC1(x, i - 2, j));
+  else vx = (IRC1(phi, i, j) - IRC1(phi, i - 1, j)) / (IRC1(x, i, j) - IRC1(x, i - 1, j));
+  vy = (IRC1(phi, i - 1, j + 1) - IRC1(phi, i - 1, j - 1)) /
+       (IRC1(y, i - 1, j + 1) - IRC1(y, i - 1, j - 1));
+  q[0] = fabs(1.0 - sqrt(vx * vx + vy * vy));
+  vx = (IRC1(phi, i + 1, j) - IRC1(phi, i - 1, j)) / (IRC1(x, i + 1, j) - IRC1(x, i - 1, j));
+  vy = (IRC1(phi, i, j + 1) - IRC1(phi, i, j - 1)) / (IRC1(y, i, j + 1) - IRC1(y, i, j - 1));
+  q[1] = fabs(1.0 - sqrt(vx * vx + vy * vy));
+  if (i <= nx - 2) vx = (IRC1(phi, i + 2, j) - IRC1(phi, i, j)) / (IRC1(x, i + 2, j) - IRC1(x, i, j));
+  else vx = (IRC1(phi, i + 1, j) - IRC1(phi, i, j)) / (IRC1(x, i + 1, j) - IRC1(x, i, j));
+  vy = (IRC1(phi, i + 1, j + 1) - IRC1(phi, i + 1, j - 1)) /
+       (IRC1(y, i + 1, j + 1) - IRC1(y, i + 1, j - 1));
+  q[2] = fabs(1.0 - sqrt(vx * vx + vy * vy));
+  if (q[0] < eta && q[2] >= eta) dx = -1;
+  else if (q[0] >= eta && q[2] < eta) dx = 1;
+  else if (q[0] < eta && q[1] < eta && q[2] < eta) dx = 0;
+  else if (q[0] >= eta && q[1] >= eta && q[2] >= eta) dx = 0;
+  else {
+    most_parallel(c, i, j, 0, nxo, nyo);
+    return;
+  }
+  if (j >= 3) vy = (IRC1(phi, i, j) - IRC1(phi, i, j - 2)) / (IRC1(y, i, j) - IRC1(y, i, j - 2));
+  else vy = (IRC1(phi, i, j) - IRC1(phi, i, j - 1)) / (IRC1(y, i, j) - IRC1(y, i, j - 1));
+  vx = (IRC1(phi, i + 1, j - 1) - IRC1(phi, i - 1, j - 1)) /
+       (IRC1(x, i + 1, j - 1) - IRC1(x, i - 1, j - 1));
+  q[0] = fabs(1.0 - sqrt(vx * vx + vy * vy));
+  vx = (IRC1(phi, i + 1, j) - IRC1(phi, i - 1, j)) / (IRC1(x, i + 1, j) - IRC1(x, i - 1, j));
+  vy = (IRC1(phi, i, j + 1) - IRC1(phi, i, j - 1)) / (IRC1(y, i, j + 1) - IRC1(y, i, j - 1));
+  q[1] = fabs(1.0 - sqrt(vx * vx + vy * vy));
+  vx = (IRC1(phi, i + 1, j + 1) - IRC1(phi, i - 1, j + 1)) /
+       (IRC1(x, i + 1, j + 1) - IRC1(x, i - 1, j + 1));
+  if (j <= ny - 2) vy = (IRC1(phi, i, j + 2) - IRC1(phi, i, j)) / (IRC1(y, i, j + 2) - IRC1(y, i, j));
+  else vy = (IRC1(phi, i, j + 1) - IRC1(phi, i, j)) / (IRC1(y, i, j + 1) - IRC1(y, i, j));
+  q[2] = fabs(1.0 - sqrt(vx * vx + vy * vy));
+  if (q[0] < eta && q[2] >= eta) dy = -1;
+  else if (q[0] >= eta && q[2] < eta) dy = 1;
+  else if (q[0] < eta && q[1] < eta && q[2] < eta) dy = 0;
+  else if (q[0] >= eta && q[1] >= eta && q[2] >= eta) dy = 0;
+  else {
+    most_parallel(c, i, j, 1, nxo, nyo);
+    return;
+  }
+  if (dx == -1) *nxo = (IRC1(phi, i, j) - IRC1(phi, i - 1, j)) / (IRC1(x, i, j) - IRC1(x, i - 1, j));
+  if (dx == 1) *nxo = (IRC1(phi, i + 1, j) - IRC1(phi, i, j)) / (IRC1(x, i + 1, j) - IRC1(x, i, j));
+  if (dx == 0)
+    *nxo = (IRC1(phi, i + 1, j) - IRC1(phi, i - 1, j)) / (IRC1(x, i + 1, j) - IRC1(x, i - 1, j));
+  if (dy == -1) *nyo = (IRC1(phi, i, j) - IRC1(phi, i, j - 1)) / (IRC1(y, i, j) - IRC1(y, i, j - 1));
+  if (dy == 1) *nyo = (IRC1(phi, i, j + 1) - IRC1(phi, i, j)) / (IRC1(y, i, j + 1) - IRC1(y, i, j));
+  if (dy == 0)
+    *nyo = (IRC1(phi, i, j + 1) - IRC1(phi, i, j - 1)) / (IRC1(y, i, j + 1) - IRC1(y, i, j - 1));
+}
+
+/* distance (:1323-1369): the PLIC line distance of a two-phase cell. */
+double oracle_plic_distance(double v, double dx, double dy, double nxx, double nyy) {
+  const double slop_eps = 1e-20, equal_eps = 1e-20;
+  double nx = fabs(nxx), ny = fabs(nyy), dll, dul, dlr, dur, vful, vflr, t;
+  if (nx < slop_eps) return (0.5 - v) * dy;
+  if (ny < slop_eps) return (0.5 - v) * dx;
+  dll = 0.5 * (nx * dx + ny * dy);
+  dul = 0.5 * (nx * dx - ny * dy);
+  dlr = -dul;
+  dur = -dll;
+  vful = oracle_frac(nx, ny, dul, dx, dy);
+  vflr = oracle_frac(nx, ny, dlr, dx, dy);
+  if (v <= vful && v <= vflr) {
+    if (vful > vflr) {
+      t = vful; vful = vflr; vflr = t;
+      t = dul; dul = dlr; dlr = t;
+    }
+    return dll - sqrt(((dul - dll) * (dul - dll)) * v / vful);
+  } else if (v >= vful && v >= vflr) {
+    if (vflr < vful) {
+      t = vful; vful = vflr; vflr = t;
+      t = dul; dul = dlr; dlr = t;
+    }
+    return dur + sqrt((dlr - dur) * (dlr - dur) * (1.0 - v) / (1.0 - vflr));
+  }
+  if (fabs(vflr - vful) < equal_eps) return 0.5 * (dul + dlr);
+  t = (v - vful) / (vflr - vful);
+  return dlr * t + dul * (1.0 - t);
+}
+
+/* LiqFuncVol (:2107-2155): volf minus the liquid part of the polygon node
+ * (closed, zero-padded to 6 entries) below the line through xf. */
+static double liq_func_vol(const double node[9][2], double nxf, double nyf, double volf,
+                           double dx, double dy, const double *xf, int *events) {
+  double pdt[9], nodel[20][2], vol;
+  const double phil = -(nxf * xf[0] + nyf * xf[1]);
+  int temp = 0, templ = 0;
+  for (int k = 1; k <= 6; ++k)
+    if (fabs(node[k - 1][0]) > 1e-14 || fabs(node[k - 1][1]) > 1e-14) temp = k;
+  for (int k = 1; k <= temp - 1; ++k) pdt[k - 1] = node[k - 1][0] * nxf + node[k - 1][1] * nyf + phil;
+  if (temp == 0) { /* the reference pauses and then reads pdt(0) */
+    ++*events;
+    return volf - 0.0;
+  }
+  pdt[temp - 1] = pdt[0];
+  for (int k = 1; k <= temp - 1; ++k) {
+    if (pdt[k - 1] <= 0.0) {
+      nodel[templ][0] = node[k - 1][0];
+      nodel[templ][1] = node[k - 1][1];
+      ++templ;
+    }
+    if (pdt[k - 1] * pdt[k] < 0.0) {
+      nodel[templ][0] = node[k - 1][0] + (node[k][0] - node[k - 1][0]) * fabs(pdt[k - 1]) /
+                                             (fabs(pdt[k - 1]) + fabs(pdt[k]));
+      nodel[templ][1] = node[k - 1][1] + (node[k][1] - node[k - 1][1]) * fabs(pdt[k - 1]) /
+                                             (fabs(pdt[k - 1]) + fabs(pdt[k]));
+      ++templ;
+    }
+  }
+  nodel[templ][0] = templ ? nodel[0][0] : 0.0;
+  nodel[templ][1] = templ ? nodel[0][1] : 0.0;
+  vol = 0.0;
+  for (int k = 0; k < templ; ++k)
+    vol = vol + 0.5 * (nodel[k][0] * nodel[k + 1][1] - nodel[k + 1][0] * nodel[k][1]);
+  return volf - fabs(vol / (dx * dy));
+}
+
+/* DistanceFluidCalculate + zriddr (:1957-2105).  Returns 1 and sets *phif
+ * when the reference assigns phif, 0 when it leaves it unchanged. */
+int oracle_dfc(double nxss, double nyss, double phiss, double nxf, double nyf, double volf,
+               double dx, double dy, double *phif, int *events) {
+  double node[9][2] = {{0.0}}, dpt[4], maxv[2] = {0.0, 0.0}, minv[2] = {0.0, 0.0};
+  const double dx2 = dx / 2.0, dy2 = dy / 2.0, tol = 1e-14, unused = -1.11e-30;
+  int temp = 0;
+  dpt[0] = dx2 * nxss - dy2 * nyss + phiss;
+  dpt[1] = -(dx2 * nxss) - dy2 * nyss + phiss;
+  dpt[2] = -(dx2 * nxss) + dy2 * nyss + phiss;
+  dpt[3] = dx2 * nxss + dy2 * nyss + phiss;
+  if (dpt[0] >= 0.0) { node[temp][0] = dx2; node[temp][1] = -dy2; ++temp; }
+  if (dpt[0] * dpt[1] < 0.0) { node[temp][0] = (dy2 * nyss - phiss) / nxss; node[temp][1] = -dy2; ++temp; }
+  if (dpt[1] >= 0.0) { node[temp][0] = -dx2; node[temp][1] = -dy2; ++temp; }
+  if (dpt[1] * dpt[2] < 0.0) { node[temp][0] = -dx2; node[temp][1] = (dx2 * nxss - phiss) / nyss; ++temp; }
+  if (dpt[2] >= 0.0) { node[temp][0] = -dx2; node[temp][1] = dy2; ++temp; }
+  if (dpt[2] * dpt[3] < 0.0) { node[temp][0] = (-(dy2 * nyss) - phiss) / nxss; node[temp][1] = dy2; ++temp; }
+  if (dpt[3] >= 0.0) { node[temp][0] = dx2; node[temp][1] = dy2; ++temp; }
+  if (dpt[3] * dpt[0] < 0.0) { node[temp][0] = dx2; node[temp][1] = (-(dx2 * nxss) - phiss) / nyss; ++temp; }
+  node[temp][0] = node[0][0];
+  node[temp][1] = node[0][1];
+  {
+    double maxdis = -2.0 * sqrt(dx * dx + dy * dy), mindis = 2.0 * sqrt(dx * dx + dy * dy);
+    for (int k = 0; k < temp; ++k) {
+      const double d23 = nxf * node[k][0] + nyf * node[k][1];
+      if (d23 > maxdis) { maxdis = d23; maxv[0] = node[k][0]; maxv[1] = node[k][1]; }
+      if (d23 < mindis) { mindis = d23; minv[0] = node[k][0]; minv[1] = node[k][1]; }
+    }
+  }
+  maxv[0] = maxv[0] + maxv[0] * nxf * EPSI;
+  maxv[1] = maxv[1] + maxv[1] * nyf * EPSI;
+  minv[0] = minv[0] - minv[0] * nxf * EPSI;
+  minv[1] = minv[1] - minv[1] * nyf * EPSI;
+  if (temp == 0 || (fabs(node[0][0]) < 1e-14 && fabs(node[0][1]) < 1e-14)) ++*events; /* pause */
+  /* zriddr(x1 = minv, x2 = maxv) */
+  double fl = liq_func_vol(node, nxf, nyf, volf, dx, dy, minv, events);
+  double fh = liq_func_vol(node, nxf, nyf, volf, dx, dy, maxv, events);
+  if ((fl > tol && fh < -tol) || (fl < -tol && fh > tol)) {
+    double xl[2] = {minv[0], minv[1]}, xh[2] = {maxv[0], maxv[1]}, ans[2] = {unused, unused};
+    double xm[2], xnew[2], fm, fnew, s;
+    for (int iter = 1; iter <= 1000; ++iter) {
+      xm[0] = 0.5 * (xl[0] + xh[0]);
+      xm[1] = 0.5 * (xl[1] + xh[1]);
+      fm = liq_func_vol(node, nxf, nyf, volf, dx, dy, xm, events);
+      s = sqrt(fm * fm - fl * fh);
+      if (s == 0.0) ++*events; /* pause */
+      const double sg = copysign(1.0, fl - fh);
+      xnew[0] = xm[0] + (xm[0] - xl[0]) * sg * fm / s;
+      xnew[1] = xm[1] + (xm[1] - xl[1]) * sg * fm / s;
+      if (sqrt((xnew[0] - ans[0]) * (xnew[0] - ans[0]) + (xnew[1] - ans[1]) * (xnew[1] - ans[1])) <=
+          tol) {
+        *phif = -(nxf * ans[0] + nyf * ans[1]);
+        return 1;
+      }
+      ans[0] = xnew[0];
+      ans[1] = xnew[1];
+      fnew = liq_func_vol(node, nxf, nyf, volf, dx, dy, ans, events);
+      if (fabs(fnew) <= tol) {
+        *phif = -(nxf * ans[0] + nyf * ans[1]);
+        return 1;
+      }
+      if (copysign(fm, fnew) != fm) {
+        xl[0] = xm[0]; xl[1] = xm[1]; fl = fm;
+        xh[0] = ans[0]; xh[1] = ans[1]; fh = fnew;
+      } else if (copysign(fl, fnew) != fl) {
+        xh[0] = ans[0]; xh[1] = ans[1]; fh = fnew;
+      } else if (copysign(fh, fnew) != fh) {
+        xl[0] = ans[0]; xl[1] = ans[1]; fl = fnew;
+      } else {
+        ++*events; /* pause */
+      }
+      if (sqrt((xh[0] - xl[0]) * (xh[0] - xl[0]) + (xh[1] - xl[1]) * (xh[1] - xl[1])) <= tol) {
+        *phif = -(nxf * ans[0] + nyf * ans[1]);
+        return 1;
+      }
+    }
+    *phif = -(nxf * ans[0] + nyf * ans[1]);
+    return 1;
+  }
+  if (fl < tol && fl > -tol) {
+    *phif = -(nxf * minv[0] + nyf * minv[1]);
+    return 1;
+  }
+  if (fh < tol && fh > -tol) {
+    *phif = -(nxf * maxv[0] + nyf * maxv[1]);
+    return 1;
+  }
+  return 0;
+}
+
+/* Interface_Reconstruct (:1250-1321) with UpdateNorVec = 1; nx, ny >= 3.
+ * Outputs (nx,ny) nxv, nyv, dis.  Returns the number of events. */
+int oracle_interface_reconstruct(int nx, int ny, const double *vfl, const double *vfls,
+                                 const double *phi, const double *nxs, const double *nys,
+                                 const double *phis, const double *x, const double *y,
+                                 const double *dx, const double *dy, double *nxv, double *nyv,
+                                 double *dis) {
+  int events = 0;
+  IrCtx ctx = {nx, ny, vfl, vfls, phi, x, y, &events};
+  const IrCtx *c = &ctx;
+  double nxx = 0.0, nyy = 0.0, diss = 0.0, temp;
+  for (int i = 1; i <= nx; ++i)
+    for (int j = 1; j <= ny; ++j) {
+      const double v = C1(vfl, i, j), s = C1(vfls, i, j);
+      int flag = 0;
+      if (v >= VOFEPS && v < (1.0 - VOFEPS - s) && s < EPSI) flag = 1;
+      if (v >= VOFEPS && v < (1.0 - VOFEPS - s) && s >= EPSI && s < 1.0 - EPSI) flag = 2;
+      if (flag) {
+        if (i > 1 && i < nx && j > 1 && j < ny) {
+          normal_irre(c, i, j, &nxx, &nyy);
+        } else {
+          if (i == 1)
+            nxx = (IRC1(phi, i + 1, j) - IRC1(phi, i, j)) / (IRC1(x, i + 1, j) - IRC1(x, i, j));
+          else if (i == nx)
+            nxx = (IRC1(phi, i, j) - IRC1(phi, i - 1, j)) / (IRC1(x, i, j) - IRC1(x, i - 1, j));
+          if (j == 1)
+            nyy = (IRC1(phi, i, j + 1) - IRC1(phi, i, j)) / (IRC1(y, i, j + 1) - IRC1(y, i, j));
+          else if (j == ny)
+            nyy = (IRC1(phi, i, j) - IRC1(phi, i, j - 1)) / (IRC1(y, i, j) - IRC1(y, i, j - 1));
+        }
+        temp = sqrt(nxx * nxx + nyy * nyy);
+        if (temp < 1e-14) {
+          nxx = 0.0;
+          nyy = 1.0;
+        } else {
+          nxx = nxx / temp;
+          nyy = nyy / temp;
+        }
+        if (flag == 1)
+          diss = oracle_plic_distance(v, C1(dx, i, j), C1(dy, i, j), nxx, nyy);
+        else
+          oracle_dfc(C1(nxs, i, j), C1(nys, i, j), C1(phis, i, j), nxx, nyy, v, C1(dx, i, j),
+                     C1(dy, i, j), &diss, &events);
+      } else {
+        nxx = 0.0;
+        nyy = 1.0;
+        if (1.0 - s > VOFEPS) diss = (0.5 - v / (1.0 - s)) * C1(dy, i, j);
+        else diss = (0.0 - v) * C1(dy, i, j);
+      }
+      C1(nxv, i, j) = nxx;
+      C1(nyv, i, j) = nyy;
+      C1(dis, i, j) = diss;
+    }
+  return events;
+}

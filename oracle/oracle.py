@@ -43,6 +43,10 @@ Pieces:
                 1141-1189, with topflux .. leftflux (:1416-1522)
     frac, cellgeocal                             src/Clsvof_Mod.f90:1371-1404,
                 2159-2253
+    interface_reconstruct  Interface_Reconstruct with Normal_Vector_Irre,
+                distance, DistanceFluidCalculate, zriddr, LiqFuncVol
+                                                 src/Clsvof_Mod.f90:1250-1369,
+                1710-1919, 1957-2155
 """
 from __future__ import annotations
 
@@ -117,6 +121,12 @@ def lib():
         L.oracle_frac.argtypes = [C.c_double] * 5
         L.oracle_cellgeocal.argtypes = [C.c_double] * 8 + [_P, _P]
         L.oracle_vof_sweep.argtypes = [C.c_int] * 3 + [_P] * 11 + [_P] * 7 + [_P, C.c_double, _P]
+        L.oracle_interface_reconstruct.restype = C.c_int
+        L.oracle_interface_reconstruct.argtypes = [C.c_int, C.c_int] + [_P] * 10 + [_P] * 3
+        L.oracle_plic_distance.restype = C.c_double
+        L.oracle_plic_distance.argtypes = [C.c_double] * 5
+        L.oracle_dfc.restype = C.c_int
+        L.oracle_dfc.argtypes = [C.c_double] * 8 + [_P, C.POINTER(C.c_int)]
         _lib = L
     return _lib
 
@@ -661,6 +671,31 @@ def cellgeocal(nxs, nys, phis, nxl, nyl, phil, dx, dy):
     a, b = C.c_double(), C.c_double()
     lib().oracle_cellgeocal(nxs, nys, phis, nxl, nyl, phil, dx, dy, C.byref(a), C.byref(b))
     return a.value, b.value
+
+
+IR_FIELDS = ["vof", "vofS", "phi", "nxs", "nys", "phiS", "x", "y", "dx", "dy"]
+
+
+def interface_reconstruct(nx, ny, f):
+    """Interface_Reconstruct (UpdateNorVec = 1) on the (nx,ny) fields of f
+    (vof, vofS, phi, nxs, nys, phiS, x, y, dx, dy); returns
+    ({"nxv", "nyv", "dis"}, events)."""
+    out = {k: np.zeros((nx, ny), order="F") for k in ("nxv", "nyv", "dis")}
+    ev = lib().oracle_interface_reconstruct(nx, ny, *[_p(f[k]) for k in IR_FIELDS],
+                                            _p(out["nxv"]), _p(out["nyv"]), _p(out["dis"]))
+    return out, ev
+
+
+def plic_distance(v, dx, dy, nxx, nyy) -> float:
+    return lib().oracle_plic_distance(v, dx, dy, nxx, nyy)
+
+
+def dfc(nxss, nyss, phiss, nxf, nyf, volf, dx, dy, phif=0.0):
+    """DistanceFluidCalculate: (phif or the given one when unassigned,
+    assigned, events)."""
+    p, e = C.c_double(phif), C.c_int(0)
+    a = lib().oracle_dfc(nxss, nyss, phiss, nxf, nyf, volf, dx, dy, C.byref(p), C.byref(e))
+    return p.value, bool(a), e.value
 
 
 def grid_preprocess_literal(nx, ny, grids, fams, icorprob=True, aln_old=None):

@@ -2,7 +2,8 @@
 (include/scf_clsvof.h): X_Sweep / Y_Sweep after Interface_Reconstruct
 (src/Clsvof_Mod.f90:989-1124, 1126-1245) on the GPU -- the level-set part
 alone (sweep) or the VOF part with, optionally, the level-set part in the
-same kernel (clsvof_sweep).
+same kernel (clsvof_sweep); and Interface_Reconstruct (src/Clsvof_Mod.f90:
+1250-1321), which each sweep calls first (interface_reconstruct).
 
 Fields are the reference's Fortran arrays (Fortran-ordered numpy float64):
 (nx,ny) phi, vofS, dx, dy, x, y; (nx+2,ny+2) aE, aW, aN, aS; ue (nx+1,ny)
@@ -17,7 +18,7 @@ import numpy as np
 
 from . import projection as P
 
-EXPORTS = ["scf_ls_sweep", "scf_clsvof_sweep"]
+EXPORTS = ["scf_ls_sweep", "scf_clsvof_sweep", "scf_interface_reconstruct"]
 X, Y = 0, 1
 DEVICE_PTRS = 1
 FIELDS = [("phi", "1"), ("vofS", "1"), ("dx", "1"), ("dy", "1"), ("x", "1"), ("y", "1"),
@@ -35,6 +36,13 @@ class VofFields(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in VOF_FIELDS]
 
 
+IR_FIELDS = ["vof", "vofS", "phi", "nxs", "nys", "phiS", "x", "y", "dx", "dy"]
+
+
+class IrFields(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in IR_FIELDS]
+
+
 class VofWave(C.Structure):
     _fields_ = [("amp0", C.c_double), ("kw", C.c_double), ("omew", C.c_double),
                 ("depthw", C.c_double), ("nondit", C.c_double), ("k", C.c_int)]
@@ -50,6 +58,10 @@ def load():
                                        C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_int,
                                        C.c_int, C.POINTER(C.c_double)]
         L.scf_clsvof_sweep.restype = C.c_int
+        L.scf_interface_reconstruct.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                                C.c_void_p, C.c_void_p, C.POINTER(C.c_int),
+                                                C.c_int, C.c_int, C.POINTER(C.c_double)]
+        L.scf_interface_reconstruct.restype = C.c_int
         L._ls_bound = True
     return L
 
@@ -135,3 +147,23 @@ def clsvof_sweep(dir: int, nx: int, ny: int, fields: dict, vof: dict, dtv: float
                                      DEVICE_PTRS if device_ptrs else 0, device, C.byref(ms)),
              "scf_clsvof_sweep")
     return ms.value
+
+
+def interface_reconstruct(nx: int, ny: int, fields: dict, out: dict | None = None,
+                          device_ptrs: bool = False, device: int = 0):
+    """Interface_Reconstruct (UpdateNorVec = 1) on the GPU: fields holds the
+    (nx,ny) arrays vof, vofS, phi, nxs, nys, phiS, x, y, dx, dy.  Returns
+    ({"nxv", "nyv", "dis"}, events, elapsed ms); out, when given, supplies
+    the three output arrays (required with device_ptrs)."""
+    st, keep = _pack(nx, ny, fields, device_ptrs, [(n, "1") for n in IR_FIELDS], IrFields)
+    if out is None:
+        if device_ptrs:
+            raise ValueError("out: the three output tensors are required with device_ptrs")
+        out = {k: np.zeros((nx, ny), order="F") for k in ("nxv", "nyv", "dis")}
+    ptrs = [_target(out[k], nx, ny, device_ptrs, k) for k in ("nxv", "nyv", "dis")]
+    ev, ms = C.c_int(0), C.c_double(0.0)
+    P._check(load().scf_interface_reconstruct(nx, ny, C.byref(st), *ptrs, C.byref(ev),
+                                              DEVICE_PTRS if device_ptrs else 0, device,
+                                              C.byref(ms)),
+             "scf_interface_reconstruct")
+    return out, ev.value, ms.value

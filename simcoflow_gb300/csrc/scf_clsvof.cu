@@ -369,6 +369,431 @@ __global__ void k_ls_sweep(LsIn in, double* temls) {
     temls[idx] = ls_cell<DIR>(in, idx, (int)(idx % nx), (int)(idx / nx), temls[idx]);
 }
 
+// ---------------------------------------------------------------------------
+// Interface_Reconstruct (src/Clsvof_Mod.f90:1250-1321) with
+// Normal_Vector_Irre (:1710-1919), distance (:1323-1369),
+// DistanceFluidCalculate (:1957-2042), zriddr (:2044-2105) and LiqFuncVol
+// (:2107-2155).
+//
+// The reference loops over cells (i outer, j inner) and its locals nxx,
+// nyy, diss carry from one cell to the next.  Only three cases read a
+// carried value: a flagged cell of column 1 or nx (rows 2..ny-1) takes nyy
+// from the cell before it (j-1), one of row 1 or ny (columns 2..nx-1) takes
+// nxx from the cell before it (row ny: (i, ny-1); row 1: (i-1, ny)), and a
+// three-phase cell whose Ridders bracket fails keeps diss.  Each of those
+// values is the carrying cell's output, so the kernels run in passes:
+//   1. every cell that reads no carried normal (interior, corners, and
+//      unflagged boundary cells);
+//   2. row ny, then 3. row 1 (reading the outputs of passes 1 and 2);
+//   4. columns 1 and nx: a flagged cell walks back to the nearest unflagged
+//      cell (or row 1) and replays the short chain of nyy;
+//   5. cells whose bracket failed copy dis from the nearest earlier cell
+//      (loop order) whose dis was assigned.
+// Each pass writes only its own cells.  Where the reference pauses for the
+// operator, reads outside an array or uses a value never set, the kernels go
+// on as after the operator's "go" (or with the documented value) and count
+// the event.
+// ---------------------------------------------------------------------------
+// Vset as Coupled_LS_VOF leaves it (:746-753: its line 747 sets Vset(1,2)
+// again instead of Vset(2,2)).
+__constant__ double kVset[8][2] = {{0, 1}, {0, 0}, {-1, 0}, {-1, -1},
+                                   {-1, 1}, {1, 0}, {1, -1}, {1, 1}};
+
+struct IrIn {
+  int nx, ny;
+  const double *vof, *vofS, *phi, *nxs, *nys, *phiS, *x, *y, *dx, *dy;
+  double *nxv, *nyv, *dis;
+  unsigned char* failed;
+  int* events;
+  __device__ long long at(int i, int j) const { return (long long)(i - 1) + (long long)(j - 1) * nx; }
+  __device__ double P(int i, int j) const { return phi[at(i, j)]; }
+  __device__ double S(int i, int j) const { return vofS[at(i, j)]; }
+  __device__ double gx(int a, int b, int j) const {
+    return (phi[at(a, j)] - phi[at(b, j)]) / (x[at(a, j)] - x[at(b, j)]);
+  }
+  __device__ double gy(int i, int a, int b) const {
+    return (phi[at(i, a)] - phi[at(i, b)]) / (y[at(i, a)] - y[at(i, b)]);
+  }
+  __device__ int flag(int i, int j) const {
+    const double v = vof[at(i, j)], s = vofS[at(i, j)];
+    int f = 0;
+    if (v >= kVofEps && v < (1.0 - kVofEps - s) && s < kEpsi) f = 1;
+    if (v >= kVofEps && v < (1.0 - kVofEps - s) && s >= kEpsi && s < 1.0 - kEpsi) f = 2;
+    return f;
+  }
+};
+
+__device__ double unit_dev(double vx, double vy) { return fabs(1.0 - sqrt(vx * vx + vy * vy)); }
+
+// The direction of Vset most parallel to the central gradient, then the
+// one-sided pair closer to unit length (:1768-1832, :1860-1912).
+__device__ void most_parallel(const IrIn& c, int i, int j, int imv, double& nxo, double& nyo) {
+  const double vx = c.gx(i + 1, i - 1, j), vy = c.gy(i, j + 1, j - 1);
+  double maxv = 0.0;
+  for (int ii = 1; ii <= 8; ++ii) {
+    const double a = kVset[ii - 1][0], b = kVset[ii - 1][1];
+    const double cp = fabs(a * vx + b * vy) / (sqrt(a * a + b * b) * sqrt(vx * vx + vy * vy));
+    if (cp >= maxv) {
+      maxv = cp;
+      imv = ii;
+    }
+  }
+  if (imv == 0) {  // the reference reads Vset(0,:), outside the table
+    atomicAdd(c.events, 1);
+    imv = 1;
+  }
+  const double v11 = -kVset[imv - 1][1], v12 = kVset[imv - 1][0];
+  double vx1, vx2, vy1, vy2;
+  if (v11 == -1) {
+    vx1 = c.gx(i, i - 1, j);
+    vx2 = c.gx(i + 1, i, j);
+  } else if (v11 == 0) {
+    vx1 = vx2 = c.gx(i + 1, i - 1, j);
+  } else {
+    vx1 = c.gx(i + 1, i, j);
+    vx2 = c.gx(i, i - 1, j);
+  }
+  if (v12 == -1) {
+    vy1 = c.gy(i, j, j - 1);
+    vy2 = c.gy(i, j + 1, j);
+  } else if (v12 == 0) {
+    vy1 = vy2 = c.gy(i, j + 1, j - 1);
+  } else {
+    vy1 = c.gy(i, j + 1, j);
+    vy2 = c.gy(i, j, j - 1);
+  }
+  if (unit_dev(vx1, vy1) < unit_dev(vx2, vy2) + 0.075 / 8.0) {
+    nxo = vx1;
+    nyo = vy1;
+  } else {
+    nxo = vx2;
+    nyo = vy2;
+  }
+}
+
+__device__ int one_sided(double qm, double q0, double qp) {
+  const double eta = 0.075;
+  if (qm < eta && qp >= eta) return -1;
+  if (qm >= eta && qp < eta) return 1;
+  if (qm < eta && q0 < eta && qp < eta) return 0;
+  if (qm >= eta && q0 >= eta && qp >= eta) return 0;
+  return 2;  // none: the most-parallel rule
+}
+
+// Normal_Vector_Irre for 1 < i < nx, 1 < j < ny.
+__device__ void normal_irre(const IrIn& c, int i, int j, double& nxo, double& nyo) {
+  const int nx = c.nx, ny = c.ny;
+  if (c.S(i, j) >= kEpsi) {
+    if (c.S(i + 1, j) < 1.0 - kEpsi && c.S(i - 1, j) < 1.0 - kEpsi) nxo = c.gx(i + 1, i - 1, j);
+    else if (c.S(i + 1, j) >= 1.0 - kEpsi) nxo = c.gx(i, i - 1, j);
+    else nxo = c.gx(i + 1, i, j);
+    if (c.S(i, j + 1) < 1.0 - kEpsi && c.S(i, j - 1) < 1.0 - kEpsi) nyo = c.gy(i, j + 1, j - 1);
+    else if (c.S(i, j + 1) > 1.0 - kEpsi) nyo = c.gy(i, j, j - 1);
+    else nyo = c.gy(i, j + 1, j);
+    return;
+  }
+  double qm = unit_dev(i >= 3 ? c.gx(i, i - 2, j) : c.gx(i, i - 1, j), c.gy(i - 1, j + 1, j - 1));
+  const double q0 = unit_dev(c.gx(i + 1, i - 1, j), c.gy(i, j + 1, j - 1));
+  double qp = unit_dev(i <= nx - 2 ? c.gx(i + 2, i, j) : c.gx(i + 1, i, j),
+                       c.gy(i + 1, j + 1, j - 1));
+  const int dx = one_sided(qm, q0, qp);
+  if (dx == 2) {
+    most_parallel(c, i, j, 0, nxo, nyo);
+    return;
+  }
+  qm = unit_dev(c.gx(i + 1, i - 1, j - 1), j >= 3 ? c.gy(i, j, j - 2) : c.gy(i, j, j - 1));
+  qp = unit_dev(c.gx(i + 1, i - 1, j + 1), j <= ny - 2 ? c.gy(i, j + 2, j) : c.gy(i, j + 1, j));
+  const int dy = one_sided(qm, q0, qp);
+  if (dy == 2) {
+    most_parallel(c, i, j, 1, nxo, nyo);
+    return;
+  }
+  nxo = dx == -1 ? c.gx(i, i - 1, j) : dx == 1 ? c.gx(i + 1, i, j) : c.gx(i + 1, i - 1, j);
+  nyo = dy == -1 ? c.gy(i, j, j - 1) : dy == 1 ? c.gy(i, j + 1, j) : c.gy(i, j + 1, j - 1);
+}
+
+// distance: the PLIC line distance of a two-phase cell.
+__device__ double plic_distance(double v, double dx, double dy, double nxx, double nyy) {
+  const double nx = fabs(nxx), ny = fabs(nyy);
+  if (nx < 1e-20) return (0.5 - v) * dy;
+  if (ny < 1e-20) return (0.5 - v) * dx;
+  const double dll = 0.5 * (nx * dx + ny * dy), dur = -dll;
+  double dul = 0.5 * (nx * dx - ny * dy), dlr = -dul;
+  double vful = frac_part(nx, ny, dul, dx, dy), vflr = frac_part(nx, ny, dlr, dx, dy);
+  if (v <= vful && v <= vflr) {
+    if (vful > vflr) {
+      double t = vful; vful = vflr; vflr = t;
+      t = dul; dul = dlr; dlr = t;
+    }
+    return dll - sqrt(((dul - dll) * (dul - dll)) * v / vful);
+  }
+  if (v >= vful && v >= vflr) {
+    if (vflr < vful) {
+      double t = vful; vful = vflr; vflr = t;
+      t = dul; dul = dlr; dlr = t;
+    }
+    return dur + sqrt((dlr - dur) * (dlr - dur) * (1.0 - v) / (1.0 - vflr));
+  }
+  if (fabs(vflr - vful) < 1e-20) return 0.5 * (dul + dlr);
+  const double t = (v - vful) / (vflr - vful);
+  return dlr * t + dul * (1.0 - t);
+}
+
+// LiqFuncVol: volf minus the liquid part (below the line through xf) of
+// the closed polygon node, zero-padded; its vertex count is found as the
+// reference finds it, from the last non-zero entry of the first six.
+__device__ double liq_func_vol(const double (&node)[9][2], double nxf, double nyf, double volf,
+                               double dx, double dy, double xf0, double xf1, int* events) {
+  const double phil = -(nxf * xf0 + nyf * xf1);
+  int temp = 0;
+  for (int k = 1; k <= 6; ++k)
+    if (fabs(node[k - 1][0]) > 1e-14 || fabs(node[k - 1][1]) > 1e-14) temp = k;
+  if (temp == 0) {  // the reference pauses and then reads pdt(0)
+    atomicAdd(events, 1);
+    return volf - 0.0;
+  }
+  const int m = temp - 1;  // vertices; node[m] closes the polygon
+  double fx = 0.0, fy = 0.0, lx = 0.0, ly = 0.0, vol = 0.0;
+  int ml = 0;
+  auto add = [&](double a, double b) {
+    if (ml == 0) {
+      fx = a;
+      fy = b;
+    } else {
+      vol = vol + 0.5 * (lx * b - a * ly);
+    }
+    lx = a;
+    ly = b;
+    ++ml;
+  };
+  double pk = m > 0 ? node[0][0] * nxf + node[0][1] * nyf + phil : 0.0;
+  const double p0 = pk;
+  for (int k = 0; k < m; ++k) {
+    const double pn = k + 1 < m ? node[k + 1][0] * nxf + node[k + 1][1] * nyf + phil : p0;
+    if (pk <= 0.0) add(node[k][0], node[k][1]);
+    if (pk * pn < 0.0) {
+      const double w = fabs(pk), ws = fabs(pk) + fabs(pn);
+      add(node[k][0] + (node[k + 1][0] - node[k][0]) * w / ws,
+          node[k][1] + (node[k + 1][1] - node[k][1]) * w / ws);
+    }
+    pk = pn;
+  }
+  if (ml > 0) vol = vol + 0.5 * (lx * fy - fx * ly);
+  return volf - fabs(vol / (dx * dy));
+}
+
+// DistanceFluidCalculate + zriddr: true when the reference assigns phif.
+__device__ bool fluid_distance(double nxss, double nyss, double phiss, double nxf, double nyf,
+                               double volf, double dx, double dy, double& phif, int* events) {
+  double node[9][2];
+  for (int k = 0; k < 9; ++k) node[k][0] = node[k][1] = 0.0;
+  const double dx2 = dx / 2.0, dy2 = dy / 2.0, tol = 1e-14, unused = -1.11e-30;
+  const double d0 = dx2 * nxss - dy2 * nyss + phiss, d1 = -(dx2 * nxss) - dy2 * nyss + phiss;
+  const double d2 = -(dx2 * nxss) + dy2 * nyss + phiss, d3 = dx2 * nxss + dy2 * nyss + phiss;
+  int m = 0;
+  auto put = [&](double a, double b) {
+    node[m][0] = a;
+    node[m][1] = b;
+    ++m;
+  };
+  if (d0 >= 0.0) put(dx2, -dy2);
+  if (d0 * d1 < 0.0) put((dy2 * nyss - phiss) / nxss, -dy2);
+  if (d1 >= 0.0) put(-dx2, -dy2);
+  if (d1 * d2 < 0.0) put(-dx2, (dx2 * nxss - phiss) / nyss);
+  if (d2 >= 0.0) put(-dx2, dy2);
+  if (d2 * d3 < 0.0) put((-(dy2 * nyss) - phiss) / nxss, dy2);
+  if (d3 >= 0.0) put(dx2, dy2);
+  if (d3 * d0 < 0.0) put(dx2, (-(dx2 * nxss) - phiss) / nyss);
+  node[m][0] = node[0][0];  // m <= 8 above, so node[m] is in bounds
+  node[m][1] = node[0][1];
+  double mx0 = 0.0, mx1 = 0.0, mn0 = 0.0, mn1 = 0.0;
+  {
+    double maxd = -2.0 * sqrt(dx * dx + dy * dy), mind = 2.0 * sqrt(dx * dx + dy * dy);
+    for (int k = 0; k < m; ++k) {
+      const double t = nxf * node[k][0] + nyf * node[k][1];
+      if (t > maxd) {
+        maxd = t;
+        mx0 = node[k][0];
+        mx1 = node[k][1];
+      }
+      if (t < mind) {
+        mind = t;
+        mn0 = node[k][0];
+        mn1 = node[k][1];
+      }
+    }
+  }
+  mx0 = mx0 + mx0 * nxf * kEpsi;
+  mx1 = mx1 + mx1 * nyf * kEpsi;
+  mn0 = mn0 - mn0 * nxf * kEpsi;
+  mn1 = mn1 - mn1 * nyf * kEpsi;
+  if (m == 0 || (fabs(node[0][0]) < 1e-14 && fabs(node[0][1]) < 1e-14)) atomicAdd(events, 1);
+  double fl = liq_func_vol(node, nxf, nyf, volf, dx, dy, mn0, mn1, events);
+  double fh = liq_func_vol(node, nxf, nyf, volf, dx, dy, mx0, mx1, events);
+  if ((fl > tol && fh < -tol) || (fl < -tol && fh > tol)) {
+    double xl0 = mn0, xl1 = mn1, xh0 = mx0, xh1 = mx1, a0 = unused, a1 = unused;
+    for (int iter = 1; iter <= 1000; ++iter) {
+      const double xm0 = 0.5 * (xl0 + xh0), xm1 = 0.5 * (xl1 + xh1);
+      const double fm = liq_func_vol(node, nxf, nyf, volf, dx, dy, xm0, xm1, events);
+      const double s = sqrt(fm * fm - fl * fh);
+      if (s == 0.0) atomicAdd(events, 1);
+      const double sg = copysign(1.0, fl - fh);
+      const double xn0 = xm0 + (xm0 - xl0) * sg * fm / s, xn1 = xm1 + (xm1 - xl1) * sg * fm / s;
+      if (sqrt((xn0 - a0) * (xn0 - a0) + (xn1 - a1) * (xn1 - a1)) <= tol) {
+        phif = -(nxf * a0 + nyf * a1);
+        return true;
+      }
+      a0 = xn0;
+      a1 = xn1;
+      const double fnew = liq_func_vol(node, nxf, nyf, volf, dx, dy, a0, a1, events);
+      if (fabs(fnew) <= tol) {
+        phif = -(nxf * a0 + nyf * a1);
+        return true;
+      }
+      if (copysign(fm, fnew) != fm) {
+        xl0 = xm0; xl1 = xm1; fl = fm;
+        xh0 = a0; xh1 = a1; fh = fnew;
+      } else if (copysign(fl, fnew) != fl) {
+        xh0 = a0; xh1 = a1; fh = fnew;
+      } else if (copysign(fh, fnew) != fh) {
+        xl0 = a0; xl1 = a1; fl = fnew;
+      } else {
+        atomicAdd(events, 1);
+      }
+      if (sqrt((xh0 - xl0) * (xh0 - xl0) + (xh1 - xl1) * (xh1 - xl1)) <= tol) {
+        phif = -(nxf * a0 + nyf * a1);
+        return true;
+      }
+    }
+    phif = -(nxf * a0 + nyf * a1);
+    return true;
+  }
+  if (fl < tol && fl > -tol) {
+    phif = -(nxf * mn0 + nyf * mn1);
+    return true;
+  }
+  if (fh < tol && fh > -tol) {
+    phif = -(nxf * mx0 + nyf * mx1);
+    return true;
+  }
+  return false;
+}
+
+// The reference's body for cell (i, j) with the carried values nxx, nyy
+// (read only where the body reads them); writes nxv, nyv, dis and the
+// failed flag.
+__device__ void ir_cell(const IrIn& c, int i, int j, double nxx, double nyy) {
+  const long long a = c.at(i, j);
+  const int nx = c.nx, ny = c.ny, flag = c.flag(i, j);
+  const double v = c.vof[a], s = c.vofS[a];
+  double diss = 0.0;
+  bool assigned = true;
+  if (flag) {
+    if (i > 1 && i < nx && j > 1 && j < ny) {
+      normal_irre(c, i, j, nxx, nyy);
+    } else {
+      if (i == 1) nxx = c.gx(i + 1, i, j);
+      else if (i == nx) nxx = c.gx(i, i - 1, j);
+      if (j == 1) nyy = c.gy(i, j + 1, j);
+      else if (j == ny) nyy = c.gy(i, j, j - 1);
+    }
+    const double t = sqrt(nxx * nxx + nyy * nyy);
+    if (t < 1e-14) {
+      nxx = 0.0;
+      nyy = 1.0;
+    } else {
+      nxx = nxx / t;
+      nyy = nyy / t;
+    }
+    if (flag == 1)
+      diss = plic_distance(v, c.dx[a], c.dy[a], nxx, nyy);
+    else
+      assigned = fluid_distance(c.nxs[a], c.nys[a], c.phiS[a], nxx, nyy, v, c.dx[a], c.dy[a],
+                                diss, c.events);
+  } else {
+    nxx = 0.0;
+    nyy = 1.0;
+    if (1.0 - s > kVofEps) diss = (0.5 - v / (1.0 - s)) * c.dy[a];
+    else diss = (0.0 - v) * c.dy[a];
+  }
+  c.nxv[a] = nxx;
+  c.nyv[a] = nyy;
+  c.dis[a] = diss;
+  c.failed[a] = assigned ? 0 : 1;
+}
+
+// Pass 1: every cell whose body reads no carried normal component.
+__global__ void k_ir_main(IrIn c) {
+  const long long total = (long long)c.nx * c.ny;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(idx % c.nx) + 1, j = (int)(idx / c.nx) + 1;
+    const bool edge_i = i == 1 || i == c.nx, edge_j = j == 1 || j == c.ny;
+    if (edge_i != edge_j && c.flag(i, j)) continue;  // carried value: later passes
+    ir_cell(c, i, j, 0.0, 0.0);
+  }
+}
+
+// Passes 2 and 3: flagged cells of row ny (ROW 0) or row 1 (ROW 1),
+// columns 2..nx-1, with nxx carried from the cell before.
+template <int ROW>
+__global__ void k_ir_row(IrIn c) {
+  for (int i = 2 + blockIdx.x * blockDim.x + threadIdx.x; i <= c.nx - 1;
+       i += gridDim.x * blockDim.x) {
+    const int j = ROW == 0 ? c.ny : 1;
+    if (!c.flag(i, j)) continue;
+    const double nxx = ROW == 0 ? c.nxv[c.at(i, c.ny - 1)] : c.nxv[c.at(i - 1, c.ny)];
+    ir_cell(c, i, j, nxx, 0.0);
+  }
+}
+
+// Pass 4: flagged cells of columns 1 and nx, rows 2..ny-1: nyy carried down
+// the column from the nearest unflagged cell (or row 1).
+__global__ void k_ir_sides(IrIn c) {
+  const int rows = c.ny - 2;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 2 * rows; t += gridDim.x * blockDim.x) {
+    const int i = t < rows ? 1 : c.nx, j = 2 + (t < rows ? t : t - rows);
+    if (!c.flag(i, j)) continue;
+    int j0 = j - 1;
+    while (j0 > 1 && c.flag(i, j0)) --j0;
+    double nyy = c.nyv[c.at(i, j0)];
+    for (int jj = j0 + 1; jj < j; ++jj) {  // flagged cells between: their normalised nyy
+      const double nxx = i == 1 ? c.gx(i + 1, i, jj) : c.gx(i, i - 1, jj);
+      const double tt = sqrt(nxx * nxx + nyy * nyy);
+      nyy = tt < 1e-14 ? 1.0 : nyy / tt;
+    }
+    ir_cell(c, i, j, 0.0, nyy);
+  }
+}
+
+// Pass 5: a cell whose Ridders bracket failed keeps diss from the cell
+// before it in the loop order (i outer, j inner): copy the nearest earlier
+// assigned dis (0 before the first cell).
+__global__ void k_ir_carry_dis(IrIn c) {
+  const long long total = (long long)c.nx * c.ny;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    if (!c.failed[idx]) continue;
+    int i = (int)(idx % c.nx) + 1, j = (int)(idx / c.nx) + 1;
+    double d = 0.0;
+    for (;;) {
+      if (j > 1) --j;
+      else if (i > 1) {
+        --i;
+        j = c.ny;
+      } else {
+        atomicAdd(c.events, 1);  // the reference's diss before any cell: never set
+        break;
+      }
+      if (!c.failed[c.at(i, j)]) {
+        d = c.dis[c.at(i, j)];
+        break;
+      }
+    }
+    c.dis[idx] = d;
+  }
+}
+
 }  // namespace
 }  // namespace scf
 
@@ -514,4 +939,91 @@ extern "C" int scf_clsvof_sweep(int dir, int nx, int ny, const scf_ls_fields* f,
                        else k_clsvof_sweep<SCF_LS_Y, false><<<g, 256, 0, s>>>(vin, lin, o[0], o[1]);
                      }
                    });
+}
+
+extern "C" int scf_interface_reconstruct(int nx, int ny, const scf_ir_fields* f, double* nxv,
+                                         double* nyv, double* dis, int* events, int flags,
+                                         int device, double* ms) {
+  if (nx < 3 || ny < 3 || !f || !nxv || !nyv || !dis) return SCF_ERR_ARG;
+  const double* arr[10] = {f->vof, f->vofS, f->phi, f->nxs, f->nys,
+                           f->phiS, f->x, f->y, f->dx, f->dy};
+  for (auto a : arr)
+    if (!a) return SCF_ERR_ARG;
+  const auto t0 = std::chrono::steady_clock::now();
+  if (cudaSetDevice(device) != cudaSuccess) return SCF_ERR_CUDA;
+  const bool dev = (flags & SCF_LS_DEVICE_PTRS) != 0;
+  const size_t n1 = (size_t)nx * ny;
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return SCF_ERR_CUDA;
+  void* mem = nullptr;
+  int rc = SCF_OK;
+  // scratch: the event counter (16 B), the failed flags (n1 B); host mode
+  // adds the 10 inputs and 3 outputs
+  const size_t scratch = 16 + ((n1 + 15) / 16) * 16;
+  const size_t bytes = scratch + (dev ? 0 : 13 * n1 * 8);
+  int h_events = 0;
+  do {
+    if (cudaMalloc(&mem, bytes) != cudaSuccess) {
+      rc = SCF_ERR_NOMEM;
+      break;
+    }
+    char* base = static_cast<char*>(mem);
+    int* d_events = reinterpret_cast<int*>(base);
+    unsigned char* failed = reinterpret_cast<unsigned char*>(base + 16);
+    const double* d[10];
+    double* o[3] = {nxv, nyv, dis};
+    if (cudaMemsetAsync(d_events, 0, 16, s) != cudaSuccess) {
+      rc = SCF_ERR_CUDA;
+      break;
+    }
+    if (!dev) {
+      double* p = reinterpret_cast<double*>(base + scratch);
+      for (int a = 0; a < 10 && rc == SCF_OK; ++a) {
+        if (cudaMemcpyAsync(p, arr[a], n1 * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
+          rc = SCF_ERR_CUDA;
+        d[a] = p;
+        p += n1;
+      }
+      for (int b = 0; b < 3; ++b) {
+        o[b] = p;
+        p += n1;
+      }
+      if (rc) break;
+    } else {
+      for (int a = 0; a < 10; ++a) d[a] = arr[a];
+    }
+    const IrIn in{nx,   ny,   d[0], d[1], d[2], d[3], d[4], d[5], d[6],   d[7],
+                  d[8], d[9], o[0], o[1], o[2], failed, d_events};
+    const unsigned g = grid_for(n1);
+    k_ir_main<<<g, 256, 0, s>>>(in);
+    note_launch();
+    const unsigned gr = (unsigned)((nx + 127) / 128), gs = (unsigned)((2 * ny + 127) / 128);
+    k_ir_row<0><<<gr, 128, 0, s>>>(in);
+    note_launch();
+    k_ir_row<1><<<gr, 128, 0, s>>>(in);
+    note_launch();
+    k_ir_sides<<<gs, 128, 0, s>>>(in);
+    note_launch();
+    k_ir_carry_dis<<<g, 256, 0, s>>>(in);
+    note_launch();
+    if (cudaGetLastError() != cudaSuccess) {
+      rc = SCF_ERR_CUDA;
+      break;
+    }
+    if (cudaMemcpyAsync(&h_events, d_events, sizeof(int), cudaMemcpyDeviceToHost, s) !=
+        cudaSuccess)
+      rc = SCF_ERR_CUDA;
+    for (int b = 0; b < 3 && !dev && rc == SCF_OK; ++b) {
+      double* hb = b == 0 ? nxv : b == 1 ? nyv : dis;
+      if (cudaMemcpyAsync(hb, o[b], n1 * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        rc = SCF_ERR_CUDA;
+    }
+  } while (false);
+  if (cudaStreamSynchronize(s) != cudaSuccess && rc == SCF_OK) rc = SCF_ERR_CUDA;
+  if (mem) cudaFree(mem);
+  cudaStreamDestroy(s);
+  if (events) *events = h_events;
+  if (ms)
+    *ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return rc;
 }

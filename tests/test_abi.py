@@ -229,7 +229,8 @@ def test_proj_library_exports_clsvof_header_symbols(built):
 @pytest.mark.parametrize("cname,pyname,rename", [
     ("scf_ls_fields", "LsFields", {}),
     ("scf_vof_fields", "VofFields", {"nxv": "nx", "nyv": "ny"}),
-    ("scf_vof_wave", "VofWave", {})])
+    ("scf_vof_wave", "VofWave", {}),
+    ("scf_ir_fields", "IrFields", {})])
 def test_clsvof_struct_layouts(tmp_path, cname, pyname, rename):
     """The ctypes mirrors of scf_ls_fields, scf_vof_fields and scf_vof_wave
     have the header's layouts."""

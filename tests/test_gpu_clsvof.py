@@ -141,3 +141,66 @@ def test_clsvof_sweep_rejects_bad_arguments(cuda):
         CL.clsvof_sweep(CL.X, 2, 5, f, v, 1e-3, t.copy(order="F"), temls=t.copy(order="F"))
     with pytest.raises(P.ProjectionError):
         CL.clsvof_sweep(2, 2, 5, f, v, 1e-3, t.copy(order="F"))
+
+
+# ---------------------------------------------------------------------------
+# Interface_Reconstruct (src/Clsvof_Mod.f90:1250-1321)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("nx,ny,band", [(3, 3, 3.0), (4, 9, 3.0), (17, 12, 1e9), (64, 61, 3.0),
+                                        (300, 257, 1e9)])
+def test_interface_reconstruct_bit_exact(cuda, oracle, nx, ny, band):
+    from gen.synth import reconstruct_fields
+    f = reconstruct_fields(np.random.default_rng(nx * 7 + ny), nx, ny, band)
+    want, ev = oracle.interface_reconstruct(nx, ny, f)
+    got, ev2, _ = CL.interface_reconstruct(nx, ny, f)
+    for k in ("nxv", "nyv", "dis"):
+        assert _same(got[k], want[k]), k
+    assert ev2 == ev
+
+
+def test_interface_reconstruct_carried_values(cuda, oracle):
+    """Every interface cell flagged (no solid, vof 0.4 everywhere): the
+    boundary rows and columns read the normal component the previous cell
+    left, and a column-1 chain runs the whole column."""
+    from gen.synth import reconstruct_fields
+    nx, ny = 40, 33
+    f = reconstruct_fields(np.random.default_rng(8), nx, ny, band=1e9)
+    f["vofS"][:] = 0.0
+    f["vof"][:] = 0.4
+    want, ev = oracle.interface_reconstruct(nx, ny, f)
+    got, ev2, _ = CL.interface_reconstruct(nx, ny, f)
+    for k in ("nxv", "nyv", "dis"):
+        assert _same(got[k], want[k]), k
+
+
+def test_interface_reconstruct_failed_brackets_carry_the_distance(cuda, oracle):
+    """Three-phase cells whose liquid fraction exceeds the non-solid part have
+    no Ridders bracket: the reference keeps diss from the cell before (loop
+    order), possibly through a run of such cells."""
+    from gen.synth import reconstruct_fields
+    nx, ny = 48, 40
+    f = reconstruct_fields(np.random.default_rng(21), nx, ny, band=1e9)
+    cut = (f["vofS"] >= 0.05) & (f["vofS"] < 1 - 1e-3)
+    f["vofS"][cut] = 2e-3  # the flag sees a small solid part, the polygon a larger one
+    f["vof"][cut] = 0.99
+    want, ev = oracle.interface_reconstruct(nx, ny, f)
+    assert cut.sum() > 20
+    got, ev2, _ = CL.interface_reconstruct(nx, ny, f)
+    for k in ("nxv", "nyv", "dis"):
+        assert _same(got[k], want[k]), k
+    assert ev2 == ev
+
+
+def test_interface_reconstruct_device_pointers_1024(cuda, oracle):
+    import torch
+    from gen.synth import reconstruct_fields
+    nx = ny = 1024
+    f = reconstruct_fields(np.random.default_rng(5), nx, ny, band=6.0)
+    want, ev = oracle.interface_reconstruct(nx, ny, f)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a.ravel(order="F"))).cuda()
+    df = {k: T(a) for k, a in f.items()}
+    out = {k: torch.zeros(nx * ny, dtype=torch.float64, device="cuda")
+           for k in ("nxv", "nyv", "dis")}
+    CL.interface_reconstruct(nx, ny, df, out=out, device_ptrs=True)
+    for k in ("nxv", "nyv", "dis"):
+        assert _same(out[k].cpu().numpy().reshape((nx, ny), order="F"), want[k]), k
