@@ -506,3 +506,62 @@ def reconstruct_fields(rng, nx, ny, band=3.0):
     return {"x": x, "y": y, "dx": dx, "dy": dy, "phi": F(phi), "vof": F(vof), "vofS": F(vofs),
             "nxs": F(np.full((nx, ny), nxs)), "nys": F(np.full((nx, ny), nys)),
             "phiS": F(phis)}
+
+
+def clsvof_step_fields(rng, nx, ny, cfl=0.2):
+    """Inputs of one Coupled_LS_VOF step on an nx x ny stretched grid: a
+    liquid drop (level set = distance to a circle, liquid fractions from its
+    local tangent line) beside a solid half-plane (its fractions, normal and
+    distance; face apertures the open part of each face), in a solid-body
+    rotation about the drop's centre with the faces inside the solid closed;
+    dt gives the sub-steps (dt/6) a Courant number cfl.  Returns
+    (fields, vof, phi, dt, wave)."""
+    F = np.asfortranarray
+    xs = np.cumsum(rng.uniform(0.8, 1.2, nx))
+    ys = np.cumsum(rng.uniform(0.8, 1.2, ny))
+    gx, gy = np.gradient(xs), np.gradient(ys)
+    x = F(np.broadcast_to(xs[:, None], (nx, ny)).copy())
+    y = F(np.broadcast_to(ys[None, :], (nx, ny)).copy())
+    dx = F(np.broadcast_to(gx[:, None], (nx, ny)).copy())
+    dy = F(np.broadcast_to(gy[None, :], (nx, ny)).copy())
+    cx, cy = 0.45 * xs[-1], 0.5 * ys[-1]
+    r = 0.25 * min(xs[-1], ys[-1])
+    phi = np.hypot(x - cx, y - cy) - r
+    with np.errstate(all="ignore"):
+        nrm = np.hypot(x - cx, y - cy)
+        gnx, gny = (x - cx) / nrm, (y - cy) / nrm
+    th = rng.uniform(-0.3, 0.3) + np.pi  # solid on the right
+    nxs, nys = np.cos(th), np.sin(th)
+    c = -(nxs * (cx + 1.1 * r) + nys * cy)
+    phis = nxs * x + nys * y + c
+    vofs = frac_v(nxs, nys, phis, dx, dy)
+    vof = np.minimum(frac_v(gnx, gny, phi, dx, dy), 1.0 - vofs)
+    # face apertures: the part of each face with nxs x + nys y + c >= 0
+    def open_part(x0, y0, x1, y1):
+        f0, f1 = nxs * x0 + nys * y0 + c, nxs * x1 + nys * y1 + c
+        with np.errstate(all="ignore"):
+            t = np.where(f0 == f1, 0.5, f0 / (f0 - f1))
+        return np.where((f0 >= 0) & (f1 >= 0), 1.0, np.where((f0 < 0) & (f1 < 0), 0.0,
+                        np.where(f0 >= 0, t, 1.0 - t)))
+    aE = np.ones((nx + 2, ny + 2)); aW = np.ones((nx + 2, ny + 2))
+    aN = np.ones((nx + 2, ny + 2)); aS = np.ones((nx + 2, ny + 2))
+    aE[1:-1, 1:-1] = open_part(x + dx / 2, y - dy / 2, x + dx / 2, y + dy / 2)
+    aW[1:-1, 1:-1] = open_part(x - dx / 2, y - dy / 2, x - dx / 2, y + dy / 2)
+    aN[1:-1, 1:-1] = open_part(x - dx / 2, y + dy / 2, x + dx / 2, y + dy / 2)
+    aS[1:-1, 1:-1] = open_part(x - dx / 2, y - dy / 2, x + dx / 2, y - dy / 2)
+    # rotation about the drop's centre, closed faces inside the solid
+    xe = np.concatenate([[xs[0] - gx[0] / 2], xs + gx / 2])
+    yn = np.concatenate([[ys[0] - gy[0] / 2], ys + gy / 2])
+    om = 1.0
+    ue = -(ys[None, :] - cy) * om * np.ones((nx + 1, 1))
+    ve = (xs[:, None] - cx) * om * np.ones((1, ny + 1))
+    ue[1:, :] *= (aE[1:-1, 1:-1] > 0)
+    ve[:, 1:] *= (aN[1:-1, 1:-1] > 0)
+    umax = max(np.abs(ue).max(), np.abs(ve).max())
+    dt = 6.0 * cfl * min(gx.min(), gy.min()) / umax
+    fields = {"vofS": F(vofs), "nxs": F(np.full((nx, ny), nxs)), "nys": F(np.full((nx, ny), nys)),
+              "phiS": F(phis), "x": x, "y": y, "dx": dx, "dy": dy, "aE": F(aE), "aW": F(aW),
+              "aN": F(aN), "aS": F(aS), "ue": F(ue), "ve": F(ve)}
+    wave = np.array([0.05 * ys[-1], 2.0 * np.pi / xs[-1], 0.5, 0.3 * ys[-1], 0.0])
+    del xe, yn
+    return fields, F(vof), F(phi), dt, wave

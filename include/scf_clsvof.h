@@ -15,8 +15,8 @@
  * operations in the same order (IEEE FP64, no FMA contraction), so the
  * output is bit-identical to a literal restatement of those loops.
  * Interface_Reconstruct, which each sweep calls first, is
- * scf_interface_reconstruct below.  Redistance and the updates of
- * Coupled_LS_VOF between the sweeps are not part of this library.
+ * scf_interface_reconstruct below, Redistance scf_redistance, and the
+ * whole Coupled_LS_VOF step with a fixed solid scf_clsvof_step.
  *
  * Arrays are the reference's Fortran arrays (column-major):
  *   (nx,ny)      phi, vofS, dx, dy, x, y, temls   (1:Isize,1:Jsize)
@@ -102,6 +102,45 @@ typedef struct scf_ir_fields {
 
 int scf_interface_reconstruct(int nx, int ny, const scf_ir_fields *f, double *nxv, double *nyv,
                               double *dis, int *events, int flags, int device, double *ms);
+
+/* Redistance (src/Clsvof_Mod.f90:1525-1708): phi (in/out, (nx,ny)) rebuilt
+ * as the signed distance to the PLIC interface (nx, ny, dis of
+ * Interface_Reconstruct) within 4 cells of every interface cell, and
+ * +-5 sqrt(dx^2 + dy^2) outside that band.  Bit-identical to the
+ * reference's scatter over interface cells: each full or empty cell applies
+ * its sources' updates in the reference's order.  *events (may be NULL)
+ * counts the reference's two 'pause' checks that fire.  nx, ny >= 1. */
+typedef struct scf_rd_fields {
+  const double *vof, *vofS, *nxs, *nys, *phiS; /* PCell */
+  const double *x, *y, *dx, *dy;              /* PGrid */
+  const double *nx, *ny, *dis;                /* Interface_Reconstruct's output */
+} scf_rd_fields;
+
+int scf_redistance(int nx, int ny, const scf_rd_fields *f, double *phi, int *events, int flags,
+                   int device, double *ms);
+
+/* Coupled_LS_VOF (src/Clsvof_Mod.f90:730-959) with a fixed solid: six
+ * sub-steps of dt/6, each an X_Sweep then a Y_Sweep (odd sub-steps) or the
+ * reverse (even), every sweep after its Interface_Reconstruct, with the
+ * reference's updates of vof and phi after each sweep and Boundary_Condition
+ * between them; then Boundary_Condition, Interface_Reconstruct (nx, ny, dis
+ * out: PCell%nx, PCell%ny and the distance) and Redistance of phi.
+ * ObjectMovement and SolidVolumeFraction, which move the solid between
+ * sub-steps, stay with the caller: the solid fields are held as given.
+ * vof and phi are in/out.  wave: the X inlet (its k is ignored: each
+ * sub-step uses its own), or NULL.  Bit-identical to the reference's loops.
+ * *events (may be NULL) counts the reconstructions' and Redistance's
+ * events (see above).  nx, ny >= 3. */
+typedef struct scf_clsvof_fields {
+  const double *vofS, *nxs, *nys, *phiS; /* PCell: the solid */
+  const double *x, *y, *dx, *dy;         /* PGrid */
+  const double *aE, *aW, *aN, *aS;       /* (nx+2,ny+2) apertures */
+  const double *ue, *ve;                 /* the sweeps' face velocities */
+} scf_clsvof_fields;
+
+int scf_clsvof_step(int nx, int ny, const scf_clsvof_fields *f, const scf_vof_wave *wave,
+                    double dt, double *vof, double *phi, double *nx_out, double *ny_out,
+                    double *dis, int *events, int flags, int device, double *ms);
 
 #ifdef __cplusplus
 }

@@ -733,3 +733,293 @@ int oracle_interface_reconstruct(int nx, int ny, const double *vfl, const double
     }
   return events;
 }
+
+/* ------------------------------------------------------------------------
+ * Redistance (src/Clsvof_Mod.f90:1525-1708) with isinsiderect (:1921-1955):
+ * phi rebuilt as the distance to the PLIC interface within band_width = 4
+ * cells of every interface cell (module parameter, :9), the rest of phi
+ * set to +-5 sqrt(dx^2 + dy^2) outside the band.  The reference's scatter
+ * from each interface cell (i outer, j inner) is restated as written.
+ * dmin1 / dmax1 are fmin / fmax; the 'pause' checks count events.
+ * ---------------------------------------------------------------------- */
+static int inside_rect(double xp, double yp, double dx, double dy) {
+  const double x1 = -0.5 * dx, y1 = 0.5 * dy, x2 = 0.5 * dx, y2 = 0.5 * dy;
+  const double x3 = 0.5 * dx, y3 = -0.5 * dy, x4 = -0.5 * dx, y4 = -0.5 * dy;
+  const double b1 = sqrt((x1 - xp) * (x1 - xp) + (y1 - yp) * (y1 - yp));
+  const double b2 = sqrt((x2 - xp) * (x2 - xp) + (y2 - yp) * (y2 - yp));
+  const double b3 = sqrt((x3 - xp) * (x3 - xp) + (y3 - yp) * (y3 - yp));
+  const double b4 = sqrt((x4 - xp) * (x4 - xp) + (y4 - yp) * (y4 - yp));
+  const double u1 = 0.5 * (dx + b1 + b2), u2 = 0.5 * (dy + b2 + b3);
+  const double u3 = 0.5 * (dx + b3 + b4), u4 = 0.5 * (dy + b4 + b1);
+  const double area = dx * dy;
+  const double a1 = sqrt(u1 * (u1 - dx) * (u1 - b1) * (u1 - b2));
+  const double a2 = sqrt(u2 * (u2 - dy) * (u2 - b2) * (u2 - b3));
+  const double a3 = sqrt(u3 * (u3 - dx) * (u3 - b3) * (u3 - b4));
+  const double a4 = sqrt(u4 * (u4 - dy) * (u4 - b4) * (u4 - b1));
+  const double sum = a1 + a2 + a3 + a4;
+  return fabs(sum - area) < 1e-10;
+}
+
+int oracle_redistance(int nx, int ny, const double *vfl, const double *vfls, const double *nxs,
+                      const double *nys, const double *phis, const double *x, const double *y,
+                      const double *dx, const double *dy, const double *nxx1,
+                      const double *nyy1, const double *diss1, double *phi, double *phiaux,
+                      int *fix) {
+  const int band = 4;
+  const double tol = 1e-24;
+  int events = 0;
+  for (size_t k = 0; k < (size_t)nx * ny; ++k) {
+    fix[k] = 0;
+    phiaux[k] = 1e4;
+  }
+#define RA(a, i, j) C1(a, i, j)
+  for (int i = 1; i <= nx; ++i)
+    for (int j = 1; j <= ny; ++j) {
+      if (!((0.0 + VOFEPS) < RA(vfl, i, j) && RA(vfl, i, j) < (1.0 - VOFEPS - RA(vfls, i, j))))
+        continue;
+      RA(phiaux, i, j) = RA(diss1, i, j);
+      RA(fix, i, j) = 1;
+      const double dxs = RA(dx, i, j), dys = RA(dy, i, j);
+      const double nxs_ = RA(nxs, i, j), nys_ = RA(nys, i, j), phs = RA(phis, i, j);
+      const double n1 = RA(nxx1, i, j), n2 = RA(nyy1, i, j), d1 = RA(diss1, i, j);
+      for (int ii = -band; ii <= band; ++ii)
+        for (int jj = -band; jj <= band; ++jj) {
+          const int p = i + ii, q = j + jj;
+          if (!(p >= 1 && p <= nx && q >= 1 && q <= ny)) continue;
+          const double vT = RA(vfl, p, q), sT = RA(vfls, p, q);
+          if (!(vT < 0.0 + VOFEPS || vT >= 1.0 - VOFEPS - sT)) continue;
+          double *pa = &RA(phiaux, p, q);
+          RA(fix, p, q) = 1;
+          const int l = ii < -1 ? -1 : (ii > 1 ? 1 : ii), m = jj < -1 ? -1 : (jj > 1 ? 1 : jj);
+          double xv = dxs * (double)l / 2.0, yv = dys * (double)m / 2.0;
+          double dvs = nxs_ * xv + nys_ * yv + phs;
+          if (dvs < 0.0) {
+            if (fabs(yv) < VOFEPS) {
+              yv = dys / 2.0;
+              dvs = nxs_ * xv + nys_ * yv + phs;
+              if (dvs < 0.0) {
+                yv = -dys / 2.0;
+                dvs = nxs_ * xv + nys_ * yv + phs;
+                if (dvs < 0.0) {
+                  xv = dxs * (0.0 - (double)l) / 2.0;
+                  dvs = nxs_ * xv + nys_ * yv + phs;
+                  if (dvs < 0.0) yv = dys / 2.0;
+                }
+              }
+            } else if (fabs(xv) < VOFEPS) {
+              xv = dxs / 2.0;
+              dvs = nxs_ * xv + nys_ * yv + phs;
+              if (dvs < 0.0) {
+                xv = -dxs / 2.0;
+                dvs = nxs_ * xv + nys_ * yv + phs;
+                if (dvs < 0.0) {
+                  yv = dys * (0.0 - (double)m) / 2.0;
+                  dvs = nxs_ * xv + nys_ * yv + phs;
+                  if (dvs < 0.0) xv = dxs / 2.0;
+                }
+              }
+            } else {
+              yv = dys * (0.0 - (double)m) / 2.0;
+              dvs = nxs_ * xv + nys_ * yv + phs;
+              if (dvs < 0.0) {
+                xv = dxs * (0.0 - (double)l) / 2.0;
+                yv = dys * (double)m / 2.0;
+                dvs = nxs_ * xv + nys_ * yv + phs;
+                if (dvs < 0.0) yv = dys * (0.0 - (double)m) / 2.0;
+              }
+            }
+          }
+          const double rx = RA(x, p, q) - RA(x, i, j), ry = RA(y, p, q) - RA(y, i, j);
+          const double dv = n1 * xv + n2 * yv + d1;
+          double deuc;
+          if (dv * copysign(1.0, RA(phi, p, q)) <= 0.0) {
+            deuc = sqrt((rx - xv) * (rx - xv) + (ry - yv) * (ry - yv));
+            if (sT < EPSI) {
+              *pa = copysign(1.0, 0.5 - vT) * fmin(deuc, fabs(*pa));
+            } else {
+              if (fabs(deuc) < fabs(*pa) && vT >= 1.0 - VOFEPS - sT) *pa = -fabs(deuc);
+              if (fabs(deuc) < fabs(*pa) && vT < VOFEPS) *pa = fabs(deuc);
+            }
+          } else {
+            const double dij1 = n1 * rx + n2 * ry + d1;
+            const double xp = rx - dij1 * n1, yp = ry - dij1 * n2;
+            const int pointp = inside_rect(xp, yp, dxs, dys);
+            if (pointp && sT < EPSI) {
+              deuc = sqrt((rx - xp) * (rx - xp) + (ry - yp) * (ry - yp));
+              *pa = copysign(1.0, 0.5 - vT) * fmin(deuc, fabs(*pa));
+            } else if (pointp && sT >= EPSI && sT < 1.0 - EPSI) {
+              deuc = sqrt((rx - xp) * (rx - xp) + (ry - yp) * (ry - yp));
+              if (fabs(deuc) < fabs(*pa) && vT >= 1.0 - VOFEPS - sT) *pa = -fabs(deuc);
+              if (fabs(deuc) < fabs(*pa) && vT < VOFEPS) *pa = fabs(deuc);
+            } else if (sT >= 1.0 - EPSI) {
+              if (RA(vfls, i, j) < EPSI) {
+                deuc = sqrt((rx - xp) * (rx - xp) + (ry - yp) * (ry - yp));
+                if (fabs(deuc) < fabs(*pa)) *pa = copysign(1.0, dij1) * deuc;
+              }
+            } else {
+              const double xoff = fmax(fabs(xp) - 0.5 * dxs, 0.0);
+              const double yoff = fmax(fabs(yp) - 0.5 * dys, 0.0);
+              const double xfc = copysign(1.0, xp) * 0.5 * dxs, yfc = copysign(1.0, yp) * 0.5 * dys;
+              double xs, ys;
+              if (xoff * fabs(n1 + tol) >= yoff * fabs(n2 + tol)) {
+                xs = xfc;
+                ys = (d1 + n1 * xs) / (-n2 + tol);
+              } else {
+                ys = yfc;
+                xs = (d1 + n2 * ys) / (-n1 + tol);
+              }
+              deuc = sqrt((rx - xs) * (rx - xs) + (ry - ys) * (ry - ys));
+              const double dvs2 = nxs_ * xs + nys_ * ys + phs;
+              if (dvs2 >= 0.0) {
+                if (sT < EPSI) {
+                  *pa = copysign(1.0, 0.5 - vT) * fmin(deuc, fabs(*pa));
+                } else {
+                  if (fabs(deuc) < fabs(*pa) && vT >= 1.0 - VOFEPS - sT) *pa = -fabs(deuc);
+                  if (fabs(deuc) < fabs(*pa) && vT < VOFEPS) *pa = fabs(deuc);
+                }
+              }
+            }
+          }
+          if (*pa > 9.999e3) RA(fix, p, q) = 0;
+        }
+    }
+  for (int i = 1; i <= nx; ++i)
+    for (int j = 1; j <= ny; ++j) {
+      const double v = RA(vfl, i, j), s = RA(vfls, i, j);
+      const double h = sqrt(RA(dx, i, j) * RA(dx, i, j) + RA(dy, i, j) * RA(dy, i, j));
+      if (RA(fix, i, j) == 1) {
+        if (RA(phiaux, i, j) > 1e3) ++events; /* pause */
+        RA(phi, i, j) = RA(phiaux, i, j);
+      } else {
+        if (v <= VOFEPS) RA(phi, i, j) = (double)(band + 1) * h;
+        else if (v >= (1.0 - VOFEPS - s)) RA(phi, i, j) = -(double)(band + 1) * h;
+      }
+      if (v < VOFEPS && RA(phi, i, j) < -VOFEPS && s < 1.0 - EPSI) ++events; /* pause */
+    }
+#undef RA
+  return events;
+}
+
+/* ------------------------------------------------------------------------
+ * Coupled_LS_VOF (src/Clsvof_Mod.f90:730-959) with a fixed solid: nv = 6
+ * sub-steps of dtv = dt/6, each an X_Sweep then a Y_Sweep (odd k) or the
+ * reverse (even k) with Coupled_LS_VOF's updates after each sweep and
+ * Boundary_Condition (:961-973) between them, then Boundary_Condition,
+ * Interface_Reconstruct and Redistance.  ObjectMovement and
+ * SolidVolumeFraction, which move the solid body between sub-steps, are
+ * the caller's: here the solid fields stay as given.
+ * wave = {Amp0, kw, omew, Depthw, NondiT} (the X inlet; NULL: no inflow);
+ * vfl, phi in/out; nxv, nyv, dis out (the last reconstruction: PCell%nx,
+ * PCell%ny and the distance Redistance used).  Returns the events of the
+ * reconstructions and of Redistance.
+ * ---------------------------------------------------------------------- */
+static void boundary_condition(int nx, int ny, double *v) {
+  for (int i = 1; i <= nx; ++i) {
+    C1(v, i, 1) = C1(v, i, 2);
+    C1(v, i, ny) = C1(v, i, ny - 1);
+  }
+  for (int j = 1; j <= ny; ++j) {
+    C1(v, 1, j) = C1(v, 2, j);
+    C1(v, nx, j) = C1(v, nx - 1, j);
+  }
+}
+
+int oracle_clsvof_step(int nx, int ny, const double *vofS, const double *nxs, const double *nys,
+                       const double *phiS, const double *dx, const double *dy, const double *x,
+                       const double *y, const double *aE, const double *aW, const double *aN,
+                       const double *aS, const double *ue, const double *ve, const double *wave,
+                       double dt, double *vfl, double *phi, double *nxv, double *nyv,
+                       double *dis, double *work) {
+  const int nv = 6;
+  const size_t n1 = (size_t)nx * ny;
+  double *tvx = work, *tvy = work + n1, *tlx = work + 2 * n1, *tly = work + 3 * n1;
+  double *aux = work + 4 * n1;
+  int *fix = (int *)(work + 5 * n1);
+  const double dtv = dt / (double)nv;
+  int events = 0;
+  double w[6];
+#define REC() events += oracle_interface_reconstruct(nx, ny, vfl, vofS, phi, nxs, nys, phiS, x, y, \
+                                                     dx, dy, nxv, nyv, dis)
+#define XSWEEP(k)                                                                          \
+  do {                                                                                     \
+    REC();                                                                                 \
+    if (wave) {                                                                            \
+      for (int q = 0; q < 5; ++q) w[q] = wave[q];                                          \
+      w[5] = (double)(k);                                                                  \
+    }                                                                                      \
+    oracle_vof_sweep(0, nx, ny, vofS, dx, dy, x, y, aE, aW, aN, aS, ue, ve, vfl, nxv, nyv, \
+                     dis, nxs, nys, phiS, wave ? w : NULL, dtv, tvx);                      \
+    oracle_ls_sweep(0, nx, ny, phi, vofS, dx, dy, x, y, aE, aW, aN, aS, ue, ve, dtv, tlx);  \
+  } while (0)
+#define YSWEEP()                                                                           \
+  do {                                                                                     \
+    REC();                                                                                 \
+    oracle_vof_sweep(1, nx, ny, vofS, dx, dy, x, y, aE, aW, aN, aS, ue, ve, vfl, nxv, nyv, \
+                     dis, nxs, nys, phiS, NULL, dtv, tvy);                                 \
+    oracle_ls_sweep(1, nx, ny, phi, vofS, dx, dy, x, y, aE, aW, aN, aS, ue, ve, dtv, tly);  \
+  } while (0)
+  for (int k = 1; k <= nv; ++k) {
+    if (k % 2 == 1) {
+      for (size_t c = 0; c < n1; ++c) { tvx[c] = vfl[c]; tlx[c] = phi[c]; }
+      XSWEEP(k);
+      for (int i = 1; i <= nx; ++i)
+        for (int j = 1; j <= ny; ++j) {
+          const double den = (1.0 - C1(vofS, i, j) + TOLDENO) -
+                             dtv / C1(dx, i, j) * (UE(i, j) * E0(aE, i, j) - UE(i - 1, j) * E0(aW, i, j));
+          C1(tvx, i, j) = C1(tvx, i, j) / den;
+          C1(tlx, i, j) = C1(tlx, i, j) / den;
+          C1(vfl, i, j) = C1(tvx, i, j) * (1.0 - C1(vofS, i, j));
+          C1(phi, i, j) = C1(tlx, i, j);
+          if (C1(vfl, i, j) >= 1.0 - VOFEPS - C1(vofS, i, j)) C1(vfl, i, j) = 1.0 - C1(vofS, i, j);
+          if (C1(vfl, i, j) < VOFEPS) C1(vfl, i, j) = 0.0;
+        }
+      boundary_condition(nx, ny, vfl);
+      boundary_condition(nx, ny, phi);
+      for (size_t c = 0; c < n1; ++c) { tvy[c] = vfl[c]; tly[c] = phi[c]; }
+      YSWEEP();
+      for (int i = 1; i <= nx; ++i)
+        for (int j = 1; j <= ny; ++j) {
+          const double dd = VE(i, j) * E0(aN, i, j) - VE(i, j - 1) * E0(aS, i, j);
+          C1(tvy, i, j) = C1(tvy, i, j) + dtv / C1(dy, i, j) * C1(tvx, i, j) * dd;
+          C1(tly, i, j) = C1(tly, i, j) + dtv / C1(dy, i, j) * C1(tlx, i, j) * dd;
+          C1(vfl, i, j) = C1(tvy, i, j);
+          if (C1(vofS, i, j) < 1.0 - EPSI) C1(phi, i, j) = C1(tly, i, j) / (1.0 - C1(vofS, i, j));
+        }
+    } else {
+      for (size_t c = 0; c < n1; ++c) { tvy[c] = vfl[c]; tly[c] = phi[c]; }
+      YSWEEP();
+      for (int i = 1; i <= nx; ++i)
+        for (int j = 1; j <= ny; ++j) {
+          const double den = (1.0 - C1(vofS, i, j) + TOLDENO) -
+                             dtv / C1(dy, i, j) * (VE(i, j) * E0(aN, i, j) - VE(i, j - 1) * E0(aS, i, j));
+          C1(tvy, i, j) = C1(tvy, i, j) / den;
+          C1(tly, i, j) = C1(tly, i, j) / den;
+          C1(vfl, i, j) = C1(tvy, i, j) * (1.0 - C1(vofS, i, j));
+          C1(phi, i, j) = C1(tly, i, j);
+          if (C1(vfl, i, j) >= 1.0 - VOFEPS - C1(vofS, i, j)) C1(vfl, i, j) = 1.0 - C1(vofS, i, j);
+          if (C1(vfl, i, j) < VOFEPS) C1(vfl, i, j) = 0.0;
+        }
+      boundary_condition(nx, ny, vfl);
+      boundary_condition(nx, ny, phi);
+      for (size_t c = 0; c < n1; ++c) { tvx[c] = vfl[c]; tlx[c] = phi[c]; }
+      XSWEEP(k);
+      for (int i = 1; i <= nx; ++i)
+        for (int j = 1; j <= ny; ++j) {
+          const double dd = UE(i, j) * E0(aE, i, j) - UE(i - 1, j) * E0(aW, i, j);
+          C1(tvx, i, j) = C1(tvx, i, j) + dtv / C1(dx, i, j) * C1(tvy, i, j) * dd;
+          C1(tlx, i, j) = C1(tlx, i, j) + dtv / C1(dx, i, j) * C1(tly, i, j) * dd;
+          C1(vfl, i, j) = C1(tvx, i, j);
+          if (C1(vofS, i, j) < 1.0 - EPSI) C1(phi, i, j) = C1(tlx, i, j) / (1.0 - C1(vofS, i, j));
+        }
+    }
+    boundary_condition(nx, ny, vfl);
+    boundary_condition(nx, ny, phi);
+    REC();
+    events += oracle_redistance(nx, ny, vfl, vofS, nxs, nys, phiS, x, y, dx, dy, nxv, nyv, dis,
+                                phi, aux, fix);
+  }
+#undef REC
+#undef XSWEEP
+#undef YSWEEP
+  return events;
+}

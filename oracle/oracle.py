@@ -47,6 +47,9 @@ Pieces:
                 distance, DistanceFluidCalculate, zriddr, LiqFuncVol
                                                  src/Clsvof_Mod.f90:1250-1369,
                 1710-1919, 1957-2155
+    redistance  Redistance with isinsiderect     src/Clsvof_Mod.f90:1525-1708,
+                1921-1955
+    clsvof_step Coupled_LS_VOF with a fixed solid  src/Clsvof_Mod.f90:730-973
 """
 from __future__ import annotations
 
@@ -123,6 +126,10 @@ def lib():
         L.oracle_vof_sweep.argtypes = [C.c_int] * 3 + [_P] * 11 + [_P] * 7 + [_P, C.c_double, _P]
         L.oracle_interface_reconstruct.restype = C.c_int
         L.oracle_interface_reconstruct.argtypes = [C.c_int, C.c_int] + [_P] * 10 + [_P] * 3
+        L.oracle_redistance.restype = C.c_int
+        L.oracle_redistance.argtypes = [C.c_int, C.c_int] + [_P] * 12 + [_P, _P, _I]
+        L.oracle_clsvof_step.restype = C.c_int
+        L.oracle_clsvof_step.argtypes = [C.c_int, C.c_int] + [_P] * 14 + [_P, C.c_double] + [_P] * 6
         L.oracle_plic_distance.restype = C.c_double
         L.oracle_plic_distance.argtypes = [C.c_double] * 5
         L.oracle_dfc.restype = C.c_int
@@ -683,6 +690,41 @@ def interface_reconstruct(nx, ny, f):
     out = {k: np.zeros((nx, ny), order="F") for k in ("nxv", "nyv", "dis")}
     ev = lib().oracle_interface_reconstruct(nx, ny, *[_p(f[k]) for k in IR_FIELDS],
                                             _p(out["nxv"]), _p(out["nyv"]), _p(out["dis"]))
+    return out, ev
+
+
+RD_FIELDS = ["vof", "vofS", "nxs", "nys", "phiS", "x", "y", "dx", "dy", "nxv", "nyv", "dis"]
+
+
+def redistance(nx, ny, f, phi):
+    """Redistance of a copy of phi (Fortran-ordered (nx,ny)) from the
+    interface (nxv, nyv, dis) of Interface_Reconstruct; returns (phi,
+    events)."""
+    out = np.asfortranarray(np.array(phi, dtype=np.float64))
+    aux = np.zeros((nx, ny), order="F")
+    fix = np.zeros((nx, ny), dtype=np.int32, order="F")
+    ev = lib().oracle_redistance(nx, ny, *[_p(f[k]) for k in RD_FIELDS], _p(out), _p(aux),
+                                 fix.ctypes.data_as(_I))
+    return out, ev
+
+
+STEP_FIELDS = ["vofS", "nxs", "nys", "phiS", "dx", "dy", "x", "y", "aE", "aW", "aN", "aS", "ue",
+               "ve"]
+
+
+def clsvof_step(nx, ny, f, dt, vof, phi, wave=None):
+    """Coupled_LS_VOF with a fixed solid on copies of vof and phi; wave the X
+    inlet's {Amp0, kw, omew, Depthw, NondiT} or None.  Returns ({"vof",
+    "phi", "nxv", "nyv", "dis"}, events)."""
+    out = {"vof": np.asfortranarray(np.array(vof, dtype=np.float64)),
+           "phi": np.asfortranarray(np.array(phi, dtype=np.float64))}
+    for k in ("nxv", "nyv", "dis"):
+        out[k] = np.zeros((nx, ny), order="F")
+    work = np.zeros(6 * nx * ny)
+    w = None if wave is None else np.ascontiguousarray(wave[:5], dtype=np.float64)
+    ev = lib().oracle_clsvof_step(nx, ny, *[_p(f[k]) for k in STEP_FIELDS], _p(w), dt,
+                                  _p(out["vof"]), _p(out["phi"]), _p(out["nxv"]), _p(out["nyv"]),
+                                  _p(out["dis"]), _p(work))
     return out, ev
 
 

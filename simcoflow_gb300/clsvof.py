@@ -3,7 +3,10 @@
 (src/Clsvof_Mod.f90:989-1124, 1126-1245) on the GPU -- the level-set part
 alone (sweep) or the VOF part with, optionally, the level-set part in the
 same kernel (clsvof_sweep); and Interface_Reconstruct (src/Clsvof_Mod.f90:
-1250-1321), which each sweep calls first (interface_reconstruct).
+1250-1321), which each sweep calls first (interface_reconstruct), and
+Redistance (src/Clsvof_Mod.f90:1525-1708, redistance); and the whole
+Coupled_LS_VOF step with a fixed solid (src/Clsvof_Mod.f90:730-973,
+clsvof_step).
 
 Fields are the reference's Fortran arrays (Fortran-ordered numpy float64):
 (nx,ny) phi, vofS, dx, dy, x, y; (nx+2,ny+2) aE, aW, aN, aS; ue (nx+1,ny)
@@ -18,7 +21,8 @@ import numpy as np
 
 from . import projection as P
 
-EXPORTS = ["scf_ls_sweep", "scf_clsvof_sweep", "scf_interface_reconstruct"]
+EXPORTS = ["scf_ls_sweep", "scf_clsvof_sweep", "scf_interface_reconstruct", "scf_redistance",
+           "scf_clsvof_step"]
 X, Y = 0, 1
 DEVICE_PTRS = 1
 FIELDS = [("phi", "1"), ("vofS", "1"), ("dx", "1"), ("dy", "1"), ("x", "1"), ("y", "1"),
@@ -43,6 +47,22 @@ class IrFields(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in IR_FIELDS]
 
 
+RD_FIELDS = ["vof", "vofS", "nxs", "nys", "phiS", "x", "y", "dx", "dy", "nxv", "nyv", "dis"]
+
+
+class RdFields(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in RD_FIELDS]
+
+
+STEP_FIELDS = [("vofS", "1"), ("nxs", "1"), ("nys", "1"), ("phiS", "1"), ("x", "1"), ("y", "1"),
+               ("dx", "1"), ("dy", "1"), ("aE", "0"), ("aW", "0"), ("aN", "0"), ("aS", "0"),
+               ("ue", "u"), ("ve", "v")]
+
+
+class StepFields(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n, _ in STEP_FIELDS]
+
+
 class VofWave(C.Structure):
     _fields_ = [("amp0", C.c_double), ("kw", C.c_double), ("omew", C.c_double),
                 ("depthw", C.c_double), ("nondit", C.c_double), ("k", C.c_int)]
@@ -62,6 +82,15 @@ def load():
                                                 C.c_void_p, C.c_void_p, C.POINTER(C.c_int),
                                                 C.c_int, C.c_int, C.POINTER(C.c_double)]
         L.scf_interface_reconstruct.restype = C.c_int
+        L.scf_redistance.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                     C.POINTER(C.c_int), C.c_int, C.c_int,
+                                     C.POINTER(C.c_double)]
+        L.scf_redistance.restype = C.c_int
+        L.scf_clsvof_step.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_double,
+                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.POINTER(C.c_int), C.c_int, C.c_int,
+                                      C.POINTER(C.c_double)]
+        L.scf_clsvof_step.restype = C.c_int
         L._ls_bound = True
     return L
 
@@ -166,4 +195,47 @@ def interface_reconstruct(nx: int, ny: int, fields: dict, out: dict | None = Non
                                               DEVICE_PTRS if device_ptrs else 0, device,
                                               C.byref(ms)),
              "scf_interface_reconstruct")
+    return out, ev.value, ms.value
+
+
+def redistance(nx: int, ny: int, fields: dict, phi, device_ptrs: bool = False,
+               device: int = 0):
+    """Redistance on the GPU: phi (in place) rebuilt from the interface
+    (nxv, nyv, dis) of interface_reconstruct; fields holds the (nx,ny)
+    arrays vof, vofS, nxs, nys, phiS, x, y, dx, dy, nxv, nyv, dis.  Returns
+    (events, elapsed ms)."""
+    st, keep = _pack(nx, ny, fields, device_ptrs, [(n, "1") for n in RD_FIELDS], RdFields)
+    ptr = _target(phi, nx, ny, device_ptrs, "phi")
+    ev, ms = C.c_int(0), C.c_double(0.0)
+    P._check(load().scf_redistance(nx, ny, C.byref(st), ptr, C.byref(ev),
+                                   DEVICE_PTRS if device_ptrs else 0, device, C.byref(ms)),
+             "scf_redistance")
+    return ev.value, ms.value
+
+
+def clsvof_step(nx: int, ny: int, fields: dict, dt: float, vof, phi, wave=None,
+                out: dict | None = None, device_ptrs: bool = False, device: int = 0):
+    """One Coupled_LS_VOF step (six sub-steps of dt/6) with the solid held
+    fixed, on the GPU: vof and phi in place.  fields holds vofS, nxs, nys,
+    phiS, x, y, dx, dy ((nx,ny)), aE, aW, aN, aS ((nx+2,ny+2)), ue
+    ((nx+1,ny)), ve ((nx,ny+1)); wave the X inlet's (Amp0, kw, omew, Depthw,
+    NondiT) or None.  Returns ({"nxv", "nyv", "dis"} of the last
+    reconstruction, events, elapsed ms); out supplies those three arrays
+    (required with device_ptrs)."""
+    st, keep = _pack(nx, ny, fields, device_ptrs, STEP_FIELDS, StepFields)
+    if out is None:
+        if device_ptrs:
+            raise ValueError("out: the three output tensors are required with device_ptrs")
+        out = {k: np.zeros((nx, ny), order="F") for k in ("nxv", "nyv", "dis")}
+    pv, pp = _target(vof, nx, ny, device_ptrs, "vof"), _target(phi, nx, ny, device_ptrs, "phi")
+    ptrs = [_target(out[k], nx, ny, device_ptrs, k) for k in ("nxv", "nyv", "dis")]
+    w = None
+    if wave is not None:
+        w = VofWave(float(wave[0]), float(wave[1]), float(wave[2]), float(wave[3]),
+                    float(wave[4]), 0)
+    ev, ms = C.c_int(0), C.c_double(0.0)
+    P._check(load().scf_clsvof_step(nx, ny, C.byref(st), None if w is None else C.byref(w),
+                                    float(dt), pv, pp, *ptrs, C.byref(ev),
+                                    DEVICE_PTRS if device_ptrs else 0, device, C.byref(ms)),
+             "scf_clsvof_step")
     return out, ev.value, ms.value

@@ -9,7 +9,7 @@
 // subtracts its flux from cell f and scales cell f+1 by (1 - vofS) before
 // adding the flux to it, and a second loop applies the first and last
 // faces.  So every cell ends as a fixed expression of at most two face
-// fluxes, which each thread evaluates for its own cell:
+// fluxes, which the kernels evaluate for each cell:
 //   cell 1:          (t - f1 E1/d1) + phi1 u0 dtv W1/d1
 //   cell 2:          (t - f2 E2/d2) + f1 E1/d2
 //   cells 3..n-1:    (t (1 - s) + f(i-1) Wi/di) - fi Ei/di
@@ -17,8 +17,8 @@
 // The VOF update has the same shape (every face applied to both of its
 // cells), after the division of temvf by (1 - vofS); its cell 1 gets the
 // inflow through face 0 (X: the wave inlet, Y: vof ve(0) dtv) last.  Face
-// fluxes read only the sweep's inputs, never temvf, so each thread
-// computes the two fluxes of its cell itself.
+// fluxes read only the sweep's inputs, never temvf, so they can be
+// evaluated in any order.
 // Compiled with -fmad=false: the operations and their order are the
 // reference's, so results are bit-identical to the sequential loops.
 #include <chrono>
@@ -303,19 +303,26 @@ __device__ double vof_face(const VLine& L, int f, double dtv) {
   return flux;
 }
 
+constexpr int kSwTx = 32, kSwTy = 8;
+
+// One thread per cell of a 32 x 8 tile.  Each thread evaluates the VOF flux
+// of its cell's high face; the low face's comes from the neighbouring
+// thread through shared memory (the tile's first column (X) or row (Y)
+// evaluates it itself), so a face is evaluated about once.
 template <int DIR, bool LS>
-__global__ void k_clsvof_sweep(VofIn vin, LsIn lin, double* __restrict__ temvf,
-                               double* __restrict__ temls) {
+__global__ void __launch_bounds__(kSwTx* kSwTy)
+    k_clsvof_sweep(VofIn vin, LsIn lin, double* __restrict__ temvf, double* __restrict__ temls) {
+  __shared__ double face[kSwTy][kSwTx];
   const int nx = vin.nx, ny = vin.ny;
-  const long long total = (long long)nx * ny;
   const double dtv = vin.dtv;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const int i0 = (int)(idx % nx), j0 = (int)(idx / nx);
-    VLine L;
+  const int i0 = blockIdx.x * kSwTx + threadIdx.x, j0 = blockIdx.y * kSwTy + threadIdx.y;
+  const bool live = i0 < nx && j0 < ny;
+  VLine L;
+  int k = 0;
+  double fhi = 0.0;
+  if (live) {
     L.in = &vin;
     const long long e0 = (long long)(i0 + 1) + (long long)(j0 + 1) * (nx + 2);
-    int k;
     if (DIR == SCF_LS_X) {
       L.c0 = (long long)j0 * nx;
       L.st = 1;
@@ -339,25 +346,35 @@ __global__ void k_clsvof_sweep(VofIn vin, LsIn lin, double* __restrict__ temvf,
       L.DIR_X = false;
       k = j0 + 1;
     }
-    double t = temvf[idx];
-    const double s = L.S(k);
-    if (s < 1.0 - kVofEps) t = t / (1.0 - s);
-    if (k == 1) {
-      t = t - vof_face<DIR>(L, 1, dtv) * L.Hi(1) / L.D(1);
-      if (DIR == SCF_LS_X) {
-        double fin = 0.0;
-        if (vin.y[idx] - vin.dy[idx] / 2.0 < vin.level) fin = L.F(1) * L.V(0) * dtv;
-        t = t + fin * L.Lo(1) / L.D(1);
-      } else {
-        t = t + L.F(1) * L.V(0) * dtv * L.Lo(1) / L.D(1);
-      }
-    } else {
-      t = t * (1.0 - s) + vof_face<DIR>(L, k - 1, dtv) * L.Lo(k) / L.D(k);
-      t = t - vof_face<DIR>(L, k, dtv) * L.Hi(k) / L.D(k);
-    }
-    temvf[idx] = t;
-    if (LS) temls[idx] = ls_cell<DIR>(lin, idx, i0, j0, temls[idx]);
+    fhi = vof_face<DIR>(L, k, dtv);
   }
+  face[threadIdx.y][threadIdx.x] = fhi;
+  __syncthreads();
+  if (!live) return;
+  const long long idx = (long long)i0 + (long long)j0 * nx;
+  double t = temvf[idx];
+  const double s = L.S(k);
+  if (s < 1.0 - kVofEps) t = t / (1.0 - s);
+  if (k == 1) {
+    t = t - fhi * L.Hi(1) / L.D(1);
+    if (DIR == SCF_LS_X) {
+      double fin = 0.0;
+      if (vin.y[idx] - vin.dy[idx] / 2.0 < vin.level) fin = L.F(1) * L.V(0) * dtv;
+      t = t + fin * L.Lo(1) / L.D(1);
+    } else {
+      t = t + L.F(1) * L.V(0) * dtv * L.Lo(1) / L.D(1);
+    }
+  } else {
+    double flo;
+    if (DIR == SCF_LS_X ? threadIdx.x > 0 : threadIdx.y > 0)
+      flo = DIR == SCF_LS_X ? face[threadIdx.y][threadIdx.x - 1] : face[threadIdx.y - 1][threadIdx.x];
+    else
+      flo = vof_face<DIR>(L, k - 1, dtv);
+    t = t * (1.0 - s) + flo * L.Lo(k) / L.D(k);
+    t = t - fhi * L.Hi(k) / L.D(k);
+  }
+  temvf[idx] = t;
+  if (LS) temls[idx] = ls_cell<DIR>(lin, idx, i0, j0, temls[idx]);
 }
 
 template <int DIR>
@@ -794,6 +811,261 @@ __global__ void k_ir_carry_dis(IrIn c) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Redistance (src/Clsvof_Mod.f90:1525-1708) with isinsiderect (:1921-1955).
+// The reference scatters from every interface cell S (i outer, j inner) to
+// the full or empty cells T within band_width = 4 cells, each update reading
+// the value T holds so far.  Interface cells are never targets, so every
+// target here gathers its sources itself, in the reference's order, and
+// applies the same updates to the same running value: the result is the
+// scatter's, bit for bit.  dmin1 / dmax1 are fmin / fmax.
+// ---------------------------------------------------------------------------
+constexpr int kBand = 4;
+
+struct RdIn {
+  int nx, ny;
+  const double *vof, *vofS, *nxs, *nys, *phiS, *x, *y, *dx, *dy, *nxv, *nyv, *dis;
+  double* phi;
+  int* events;
+  __device__ long long at(int i, int j) const { return (long long)(i - 1) + (long long)(j - 1) * nx; }
+  __device__ bool source(int i, int j) const {
+    const double v = vof[at(i, j)];
+    return (0.0 + kVofEps) < v && v < (1.0 - kVofEps - vofS[at(i, j)]);
+  }
+};
+
+__device__ bool inside_rect(double xp, double yp, double dx, double dy) {
+  const double x1 = -0.5 * dx, y1 = 0.5 * dy, x2 = 0.5 * dx, y2 = 0.5 * dy;
+  const double x3 = 0.5 * dx, y3 = -0.5 * dy, x4 = -0.5 * dx, y4 = -0.5 * dy;
+  const double b1 = sqrt((x1 - xp) * (x1 - xp) + (y1 - yp) * (y1 - yp));
+  const double b2 = sqrt((x2 - xp) * (x2 - xp) + (y2 - yp) * (y2 - yp));
+  const double b3 = sqrt((x3 - xp) * (x3 - xp) + (y3 - yp) * (y3 - yp));
+  const double b4 = sqrt((x4 - xp) * (x4 - xp) + (y4 - yp) * (y4 - yp));
+  const double u1 = 0.5 * (dx + b1 + b2), u2 = 0.5 * (dy + b2 + b3);
+  const double u3 = 0.5 * (dx + b3 + b4), u4 = 0.5 * (dy + b4 + b1);
+  const double a1 = sqrt(u1 * (u1 - dx) * (u1 - b1) * (u1 - b2));
+  const double a2 = sqrt(u2 * (u2 - dy) * (u2 - b2) * (u2 - b3));
+  const double a3 = sqrt(u3 * (u3 - dx) * (u3 - b3) * (u3 - b4));
+  const double a4 = sqrt(u4 * (u4 - dy) * (u4 - b4) * (u4 - b1));
+  return fabs(a1 + a2 + a3 + a4 - dx * dy) < 1e-10;
+}
+
+// The reference's two guarded assignments for a target inside a cut cell.
+__device__ double closer(double pa, double deuc, double vT, double sT) {
+  if (fabs(deuc) < fabs(pa) && vT >= 1.0 - kVofEps - sT) pa = -fabs(deuc);
+  if (fabs(deuc) < fabs(pa) && vT < kVofEps) pa = fabs(deuc);
+  return pa;
+}
+
+// One update of target T's running value pa from source S = (i, j), T at
+// offset (ii, jj) (:1551-1676).
+__device__ double rd_update(const RdIn& c, int i, int j, int ii, int jj, double pa, double vT,
+                            double sT, double phiT, double xT, double yT) {
+  const double tol = 1e-24;
+  const long long a = c.at(i, j);
+  const double dxs = c.dx[a], dys = c.dy[a], nxs = c.nxs[a], nys = c.nys[a], phs = c.phiS[a];
+  const double n1 = c.nxv[a], n2 = c.nyv[a], d1 = c.dis[a];
+  auto solid = [&](double px, double py) { return nxs * px + nys * py + phs; };
+  const int l = ii < -1 ? -1 : (ii > 1 ? 1 : ii), m = jj < -1 ? -1 : (jj > 1 ? 1 : jj);
+  double xv = dxs * (double)l / 2.0, yv = dys * (double)m / 2.0;
+  if (solid(xv, yv) < 0.0) {
+    if (fabs(yv) < kVofEps) {
+      yv = dys / 2.0;
+      if (solid(xv, yv) < 0.0) {
+        yv = -dys / 2.0;
+        if (solid(xv, yv) < 0.0) {
+          xv = dxs * (0.0 - (double)l) / 2.0;
+          if (solid(xv, yv) < 0.0) yv = dys / 2.0;
+        }
+      }
+    } else if (fabs(xv) < kVofEps) {
+      xv = dxs / 2.0;
+      if (solid(xv, yv) < 0.0) {
+        xv = -dxs / 2.0;
+        if (solid(xv, yv) < 0.0) {
+          yv = dys * (0.0 - (double)m) / 2.0;
+          if (solid(xv, yv) < 0.0) xv = dxs / 2.0;
+        }
+      }
+    } else {
+      yv = dys * (0.0 - (double)m) / 2.0;
+      if (solid(xv, yv) < 0.0) {
+        xv = dxs * (0.0 - (double)l) / 2.0;
+        yv = dys * (double)m / 2.0;
+        if (solid(xv, yv) < 0.0) yv = dys * (0.0 - (double)m) / 2.0;
+      }
+    }
+  }
+  const double rx = xT - c.x[a], ry = yT - c.y[a];
+  const double dv = n1 * xv + n2 * yv + d1;
+  if (dv * copysign(1.0, phiT) <= 0.0) {
+    const double deuc = sqrt((rx - xv) * (rx - xv) + (ry - yv) * (ry - yv));
+    if (sT < kEpsi) return copysign(1.0, 0.5 - vT) * fmin(deuc, fabs(pa));
+    return closer(pa, deuc, vT, sT);
+  }
+  const double dij1 = n1 * rx + n2 * ry + d1;
+  const double xp = rx - dij1 * n1, yp = ry - dij1 * n2;
+  const bool in = inside_rect(xp, yp, dxs, dys);
+  if (in && sT < kEpsi) {
+    const double deuc = sqrt((rx - xp) * (rx - xp) + (ry - yp) * (ry - yp));
+    return copysign(1.0, 0.5 - vT) * fmin(deuc, fabs(pa));
+  }
+  if (in && sT >= kEpsi && sT < 1.0 - kEpsi)
+    return closer(pa, sqrt((rx - xp) * (rx - xp) + (ry - yp) * (ry - yp)), vT, sT);
+  if (sT >= 1.0 - kEpsi) {
+    if (c.vofS[a] < kEpsi) {
+      const double deuc = sqrt((rx - xp) * (rx - xp) + (ry - yp) * (ry - yp));
+      if (fabs(deuc) < fabs(pa)) pa = copysign(1.0, dij1) * deuc;
+    }
+    return pa;
+  }
+  const double xoff = fmax(fabs(xp) - 0.5 * dxs, 0.0), yoff = fmax(fabs(yp) - 0.5 * dys, 0.0);
+  const double xfc = copysign(1.0, xp) * 0.5 * dxs, yfc = copysign(1.0, yp) * 0.5 * dys;
+  double xs, ys;
+  if (xoff * fabs(n1 + tol) >= yoff * fabs(n2 + tol)) {
+    xs = xfc;
+    ys = (d1 + n1 * xs) / (-n2 + tol);
+  } else {
+    ys = yfc;
+    xs = (d1 + n2 * ys) / (-n1 + tol);
+  }
+  const double deuc = sqrt((rx - xs) * (rx - xs) + (ry - ys) * (ry - ys));
+  if (solid(xs, ys) >= 0.0) {
+    if (sT < kEpsi) return copysign(1.0, 0.5 - vT) * fmin(deuc, fabs(pa));
+    return closer(pa, deuc, vT, sT);
+  }
+  return pa;
+}
+
+constexpr int kRdTx = 32, kRdTy = 8;
+
+// One thread per cell (i fastest within a 32 x 8 tile); the source flags of
+// the tile and its 4-cell halo are staged in shared memory.
+__global__ void __launch_bounds__(kRdTx* kRdTy) k_redistance(RdIn c) {
+  __shared__ unsigned char src[kRdTy + 2 * kBand][kRdTx + 2 * kBand];
+  const int i0 = blockIdx.x * kRdTx, j0 = blockIdx.y * kRdTy;
+  const int tid = threadIdx.y * kRdTx + threadIdx.x;
+  for (int k = tid; k < (kRdTx + 2 * kBand) * (kRdTy + 2 * kBand); k += kRdTx * kRdTy) {
+    const int ti = k % (kRdTx + 2 * kBand), tj = k / (kRdTx + 2 * kBand);
+    const int i = i0 + ti - kBand + 1, j = j0 + tj - kBand + 1;  // 1-based
+    src[tj][ti] = (i >= 1 && i <= c.nx && j >= 1 && j <= c.ny && c.source(i, j)) ? 1 : 0;
+  }
+  __syncthreads();
+  const int p = i0 + threadIdx.x + 1, q = j0 + threadIdx.y + 1;
+  if (p > c.nx || q > c.ny) return;
+  const long long t = c.at(p, q);
+  const double vT = c.vof[t], sT = c.vofS[t];
+  const double h = sqrt(c.dx[t] * c.dx[t] + c.dy[t] * c.dy[t]);
+  double out = c.phi[t];
+  bool fix = false;
+  double pa = 1e4;
+  if (src[threadIdx.y + kBand][threadIdx.x + kBand]) {
+    pa = c.dis[t];
+    fix = true;
+  } else if (vT < 0.0 + kVofEps || vT >= 1.0 - kVofEps - sT) {
+    const double phiT = out, xT = c.x[t], yT = c.y[t];
+    for (int di = -kBand; di <= kBand; ++di)  // sources in the reference's order
+      for (int dj = -kBand; dj <= kBand; ++dj) {
+        if (!src[threadIdx.y + kBand + dj][threadIdx.x + kBand + di]) continue;
+        fix = true;
+        pa = rd_update(c, p + di, q + dj, -di, -dj, pa, vT, sT, phiT, xT, yT);
+        if (pa > 9.999e3) fix = false;
+      }
+  }
+  if (fix) {
+    if (pa > 1e3) atomicAdd(c.events, 1);  // the reference pauses here
+    out = pa;
+  } else {
+    if (vT <= kVofEps) out = (double)(kBand + 1) * h;
+    else if (vT >= (1.0 - kVofEps - sT)) out = -(double)(kBand + 1) * h;
+  }
+  if (vT < kVofEps && out < -kVofEps && sT < 1.0 - kEpsi) atomicAdd(c.events, 1);
+  c.phi[t] = out;
+}
+
+// ---------------------------------------------------------------------------
+// Coupled_LS_VOF (src/Clsvof_Mod.f90:730-959) between the sweeps: the
+// updates after the first and the second sweep of a sub-step and
+// Boundary_Condition (:961-973).
+// ---------------------------------------------------------------------------
+struct StepIn {
+  int nx, ny;
+  double dtv;
+  const double *vofS, *dx, *dy, *aE, *aW, *aN, *aS, *ue, *ve;
+  __device__ double vel(int dir, int i, int j) const {  // ue(i,j) / ve(i,j), 1-based cells
+    return dir == SCF_LS_X ? ue[(long long)i + (long long)(j - 1) * (nx + 1)]
+                           : ve[(long long)(i - 1) + (long long)j * nx];
+  }
+  __device__ double edge(const double* a, int i, int j) const {
+    return a[(long long)i + (long long)j * (nx + 2)];
+  }
+  // ue(i,j) E - ue(i-1,j) W  (X),  ve(i,j) N - ve(i,j-1) S  (Y)
+  __device__ double div(int dir, int i, int j) const {
+    return dir == SCF_LS_X ? vel(dir, i, j) * edge(aE, i, j) - vel(dir, i - 1, j) * edge(aW, i, j)
+                           : vel(dir, i, j) * edge(aN, i, j) - vel(dir, i, j - 1) * edge(aS, i, j);
+  }
+};
+
+// After the first sweep of a sub-step (direction DIR): temvf and temls
+// divided by the cell's net outflow factor; vof (clipped) and phi from them.
+template <int DIR>
+__global__ void k_after_first(StepIn c, double* tv, double* tl, double* vof, double* phi) {
+  const long long total = (long long)c.nx * c.ny;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(idx % c.nx) + 1, j = (int)(idx / c.nx) + 1;
+    const double s = c.vofS[idx], h = DIR == SCF_LS_X ? c.dx[idx] : c.dy[idx];
+    const double den = (1.0 - s + kTolDeno) - c.dtv / h * c.div(DIR, i, j);
+    const double a = tv[idx] / den, b = tl[idx] / den;
+    tv[idx] = a;
+    tl[idx] = b;
+    double v = a * (1.0 - s);
+    if (v >= 1.0 - kVofEps - s) v = 1.0 - s;
+    if (v < kVofEps) v = 0.0;
+    vof[idx] = v;
+    phi[idx] = b;
+  }
+}
+
+// After the second sweep (direction DIR): the first sweep's values (t1v,
+// t1l) times this direction's net outflow added; vof and phi from them.
+template <int DIR>
+__global__ void k_after_second(StepIn c, const double* t1v, const double* t1l, double* tv,
+                               double* tl, double* vof, double* phi) {
+  const long long total = (long long)c.nx * c.ny;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(idx % c.nx) + 1, j = (int)(idx / c.nx) + 1;
+    const double s = c.vofS[idx], h = DIR == SCF_LS_X ? c.dx[idx] : c.dy[idx];
+    const double d = c.div(DIR, i, j);
+    const double a = tv[idx] + c.dtv / h * t1v[idx] * d;
+    const double b = tl[idx] + c.dtv / h * t1l[idx] * d;
+    tv[idx] = a;
+    tl[idx] = b;
+    vof[idx] = a;
+    if (s < 1.0 - kEpsi) phi[idx] = b / (1.0 - s);
+  }
+}
+
+// Boundary_Condition on two fields: rows 1 and ny copy rows 2 and ny-1,
+// then columns 1 and nx copy columns 2 and nx-1 (the corners so take the
+// diagonal interior cell).  Reads interior cells only.
+__global__ void k_boundary(int nx, int ny, double* a, double* b) {
+  const int per = 2 * nx + 2 * (ny - 2);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 2 * per; t += gridDim.x * blockDim.x) {
+    double* v = t < per ? a : b;
+    const int e = t < per ? t : t - per;
+    int i, j;
+    if (e < nx) { i = e + 1; j = 1; }
+    else if (e < 2 * nx) { i = e - nx + 1; j = ny; }
+    else if (e < 2 * nx + ny - 2) { i = 1; j = e - 2 * nx + 2; }
+    else { i = nx; j = e - (2 * nx + ny - 2) + 2; }
+    const int si = i == 1 ? 2 : (i == nx ? nx - 1 : i);
+    const int sj = j == 1 ? 2 : (j == ny ? ny - 1 : j);
+    v[(long long)(i - 1) + (long long)(j - 1) * nx] = v[(long long)(si - 1) + (long long)(sj - 1) * nx];
+  }
+}
+
 }  // namespace
 }  // namespace scf
 
@@ -891,6 +1163,7 @@ extern "C" int scf_clsvof_sweep(int dir, int nx, int ny, const scf_ls_fields* f,
     return SCF_ERR_ARG;
   const bool ls = temls != nullptr;
   if (ls && (nx < 3 || ny < 3)) return SCF_ERR_ARG;
+  if ((ny + kSwTy - 1) / kSwTy > 65535) return SCF_ERR_ARG;  // grid rows
   // inputs: the level-set fields (phi only with temls), then the VOF fields
   const double* arr[19] = {f->phi, f->vofS, f->dx, f->dy, f->x, f->y, f->aE, f->aW, f->aN,
                            f->aS,  f->ue,   f->ve, v->vof, v->nx, v->ny, v->dis, v->nxs,
@@ -930,13 +1203,15 @@ extern "C" int scf_clsvof_sweep(int dir, int nx, int ny, const scf_ls_fields* f,
                      const VofIn vin{nx,    ny,    dtv,   level, d[1],  d[2],  d[3],
                                      d[5],  d[6],  d[7],  d[8],  d[9],  d[10], d[11],
                                      d[12], d[13], d[14], d[15], d[16], d[17], d[18]};
-                     const unsigned g = grid_for(n1);
+                     const dim3 g((unsigned)((nx + kSwTx - 1) / kSwTx),
+                                  (unsigned)((ny + kSwTy - 1) / kSwTy)),
+                         b(kSwTx, kSwTy);
                      if (dir == SCF_LS_X) {
-                       if (ls) k_clsvof_sweep<SCF_LS_X, true><<<g, 256, 0, s>>>(vin, lin, o[0], o[1]);
-                       else k_clsvof_sweep<SCF_LS_X, false><<<g, 256, 0, s>>>(vin, lin, o[0], o[1]);
+                       if (ls) k_clsvof_sweep<SCF_LS_X, true><<<g, b, 0, s>>>(vin, lin, o[0], o[1]);
+                       else k_clsvof_sweep<SCF_LS_X, false><<<g, b, 0, s>>>(vin, lin, o[0], o[1]);
                      } else {
-                       if (ls) k_clsvof_sweep<SCF_LS_Y, true><<<g, 256, 0, s>>>(vin, lin, o[0], o[1]);
-                       else k_clsvof_sweep<SCF_LS_Y, false><<<g, 256, 0, s>>>(vin, lin, o[0], o[1]);
+                       if (ls) k_clsvof_sweep<SCF_LS_Y, true><<<g, b, 0, s>>>(vin, lin, o[0], o[1]);
+                       else k_clsvof_sweep<SCF_LS_Y, false><<<g, b, 0, s>>>(vin, lin, o[0], o[1]);
                      }
                    });
 }
@@ -1018,6 +1293,250 @@ extern "C" int scf_interface_reconstruct(int nx, int ny, const scf_ir_fields* f,
       if (cudaMemcpyAsync(hb, o[b], n1 * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess)
         rc = SCF_ERR_CUDA;
     }
+  } while (false);
+  if (cudaStreamSynchronize(s) != cudaSuccess && rc == SCF_OK) rc = SCF_ERR_CUDA;
+  if (mem) cudaFree(mem);
+  cudaStreamDestroy(s);
+  if (events) *events = h_events;
+  if (ms)
+    *ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return rc;
+}
+
+extern "C" int scf_redistance(int nx, int ny, const scf_rd_fields* f, double* phi, int* events,
+                              int flags, int device, double* ms) {
+  if (nx < 1 || ny < 1 || !f || !phi) return SCF_ERR_ARG;
+  if ((ny + kRdTy - 1) / kRdTy > 65535) return SCF_ERR_ARG;  // grid rows
+  const double* arr[12] = {f->vof, f->vofS, f->nxs, f->nys, f->phiS, f->x,
+                           f->y,   f->dx,   f->dy,  f->nx,  f->ny,   f->dis};
+  for (auto a : arr)
+    if (!a) return SCF_ERR_ARG;
+  const auto t0 = std::chrono::steady_clock::now();
+  if (cudaSetDevice(device) != cudaSuccess) return SCF_ERR_CUDA;
+  const bool dev = (flags & SCF_LS_DEVICE_PTRS) != 0;
+  const size_t n1 = (size_t)nx * ny;
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return SCF_ERR_CUDA;
+  void* mem = nullptr;
+  int rc = SCF_OK, h_events = 0;
+  const size_t bytes = 16 + (dev ? 0 : 13 * n1 * 8);
+  do {
+    if (cudaMalloc(&mem, bytes) != cudaSuccess) {
+      rc = SCF_ERR_NOMEM;
+      break;
+    }
+    int* d_events = static_cast<int*>(mem);
+    if (cudaMemsetAsync(d_events, 0, 16, s) != cudaSuccess) {
+      rc = SCF_ERR_CUDA;
+      break;
+    }
+    const double* d[12];
+    double* dphi = phi;
+    if (!dev) {
+      double* p = reinterpret_cast<double*>(static_cast<char*>(mem) + 16);
+      for (int a = 0; a < 12 && rc == SCF_OK; ++a) {
+        if (cudaMemcpyAsync(p, arr[a], n1 * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
+          rc = SCF_ERR_CUDA;
+        d[a] = p;
+        p += n1;
+      }
+      dphi = p;
+      if (rc == SCF_OK &&
+          cudaMemcpyAsync(dphi, phi, n1 * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
+        rc = SCF_ERR_CUDA;
+      if (rc) break;
+    } else {
+      for (int a = 0; a < 12; ++a) d[a] = arr[a];
+    }
+    const RdIn in{nx,   ny,   d[0], d[1], d[2],  d[3],  d[4], d[5],
+                  d[6], d[7], d[8], d[9], d[10], d[11], dphi, d_events};
+    const dim3 grid((unsigned)((nx + kRdTx - 1) / kRdTx), (unsigned)((ny + kRdTy - 1) / kRdTy));
+    k_redistance<<<grid, dim3(kRdTx, kRdTy), 0, s>>>(in);
+    note_launch();
+    if (cudaGetLastError() != cudaSuccess) {
+      rc = SCF_ERR_CUDA;
+      break;
+    }
+    if (cudaMemcpyAsync(&h_events, d_events, sizeof(int), cudaMemcpyDeviceToHost, s) !=
+        cudaSuccess)
+      rc = SCF_ERR_CUDA;
+    if (rc == SCF_OK && !dev &&
+        cudaMemcpyAsync(phi, dphi, n1 * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+      rc = SCF_ERR_CUDA;
+  } while (false);
+  if (cudaStreamSynchronize(s) != cudaSuccess && rc == SCF_OK) rc = SCF_ERR_CUDA;
+  if (mem) cudaFree(mem);
+  cudaStreamDestroy(s);
+  if (events) *events = h_events;
+  if (ms)
+    *ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return rc;
+}
+
+namespace {
+
+void launch_reconstruct(const IrIn& in, size_t n1, cudaStream_t s) {
+  const unsigned g = grid_for(n1);
+  const unsigned gr = (unsigned)((in.nx + 127) / 128), gs = (unsigned)((2 * in.ny + 127) / 128);
+  k_ir_main<<<g, 256, 0, s>>>(in);
+  k_ir_row<0><<<gr, 128, 0, s>>>(in);
+  k_ir_row<1><<<gr, 128, 0, s>>>(in);
+  k_ir_sides<<<gs, 128, 0, s>>>(in);
+  k_ir_carry_dis<<<g, 256, 0, s>>>(in);
+  for (int q = 0; q < 5; ++q) note_launch();
+}
+
+}  // namespace
+
+extern "C" int scf_clsvof_step(int nx, int ny, const scf_clsvof_fields* f,
+                               const scf_vof_wave* wave, double dt, double* vof, double* phi,
+                               double* nxv, double* nyv, double* dis, int* events, int flags,
+                               int device, double* ms) {
+  if (nx < 3 || ny < 3 || !f || !vof || !phi || !nxv || !nyv || !dis) return SCF_ERR_ARG;
+  if ((ny + kSwTy - 1) / kSwTy > 65535) return SCF_ERR_ARG;
+  const double* arr[14] = {f->vofS, f->nxs, f->nys, f->phiS, f->x,  f->y,  f->dx,
+                           f->dy,   f->aE,  f->aW,  f->aN,   f->aS, f->ue, f->ve};
+  for (auto a : arr)
+    if (!a) return SCF_ERR_ARG;
+  const auto t0 = std::chrono::steady_clock::now();
+  if (cudaSetDevice(device) != cudaSuccess) return SCF_ERR_CUDA;
+  const bool dev = (flags & SCF_LS_DEVICE_PTRS) != 0;
+  const size_t n1 = (size_t)nx * ny, n0 = (size_t)(nx + 2) * (ny + 2);
+  const size_t cnt[14] = {n1, n1, n1, n1, n1, n1, n1, n1, n0, n0, n0, n0,
+                          (size_t)(nx + 1) * ny, (size_t)nx * (ny + 1)};
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return SCF_ERR_CUDA;
+  void* mem = nullptr;
+  int rc = SCF_OK, h_events = 0;
+  // scratch: events (16 B), failed flags, 4 sweep fields; host mode adds the
+  // 14 inputs and the 5 in/out fields
+  const size_t flags_b = ((n1 + 15) / 16) * 16;
+  size_t in_n = 0;
+  for (size_t c : cnt) in_n += c;
+  const size_t bytes = 16 + flags_b + 4 * n1 * 8 + (dev ? 0 : (in_n + 5 * n1) * 8);
+  do {
+    if (cudaMalloc(&mem, bytes) != cudaSuccess) {
+      rc = SCF_ERR_NOMEM;
+      break;
+    }
+    char* base = static_cast<char*>(mem);
+    int* d_events = reinterpret_cast<int*>(base);
+    unsigned char* failed = reinterpret_cast<unsigned char*>(base + 16);
+    double* w = reinterpret_cast<double*>(base + 16 + flags_b);
+    double *tvx = w, *tvy = w + n1, *tlx = w + 2 * n1, *tly = w + 3 * n1;
+    double* p = w + 4 * n1;
+    const double* d[14];
+    double* io[5] = {vof, phi, nxv, nyv, dis};
+    if (cudaMemsetAsync(d_events, 0, 16, s) != cudaSuccess) {
+      rc = SCF_ERR_CUDA;
+      break;
+    }
+    if (!dev) {
+      for (int a = 0; a < 14 && rc == SCF_OK; ++a) {
+        if (cudaMemcpyAsync(p, arr[a], cnt[a] * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
+          rc = SCF_ERR_CUDA;
+        d[a] = p;
+        p += cnt[a];
+      }
+      for (int b = 0; b < 5 && rc == SCF_OK; ++b) {
+        if (b < 2 && cudaMemcpyAsync(p, io[b], n1 * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
+          rc = SCF_ERR_CUDA;
+        io[b] = p;
+        p += n1;
+      }
+      if (rc) break;
+    } else {
+      for (int a = 0; a < 14; ++a) d[a] = arr[a];
+    }
+    double* dv = io[0];
+    double* dp = io[1];
+    // the X inlet's level per sub-step, on the host as in X_Sweep
+    double x11 = 0.0, dx11 = 0.0;
+    if (wave) {
+      if (dev) {
+        if (cudaMemcpy(&x11, f->x, 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(&dx11, f->dx, 8, cudaMemcpyDeviceToHost) != cudaSuccess) {
+          rc = SCF_ERR_CUDA;
+          break;
+        }
+      } else {
+        x11 = f->x[0];
+        dx11 = f->dx[0];
+      }
+    }
+    const int nv = 6;
+    const double dtv = dt / (double)nv;
+    const IrIn irc{nx,   ny,   dv,   d[0],  dp,    d[1],  d[2],   d[3],    d[4],
+                   d[5], d[6], d[7], io[2], io[3], io[4], failed, d_events};
+    const LsIn lin{nx,   ny,   dtv,  dp,   d[0],  d[6],  d[7],  d[4],
+                   d[5], d[8], d[9], d[10], d[11], d[12], d[13]};
+    const StepIn st{nx, ny, dtv, d[0], d[6], d[7], d[8], d[9], d[10], d[11], d[12], d[13]};
+    const dim3 gsw((unsigned)((nx + kSwTx - 1) / kSwTx), (unsigned)((ny + kSwTy - 1) / kSwTy)),
+        bsw(kSwTx, kSwTy);
+    const unsigned g = grid_for(n1);
+    const unsigned gb = (unsigned)((2 * (2 * nx + 2 * (ny - 2)) + 255) / 256);
+    auto sweep = [&](int dir, int k, double* tv, double* tl) {
+      launch_reconstruct(irc, n1, s);
+      double level = -INFINITY;
+      if (dir == SCF_LS_X && wave) {
+        const double xwu = x11 - dx11 / 2.0;
+        level = wave->depthw +
+                wave->amp0 * std::sin(wave->kw * xwu - wave->omew * (wave->nondit + (double)k * dtv));
+      }
+      const VofIn vin{nx,    ny,    dtv,   level, d[0],  d[6],  d[7],  d[5],  d[8],  d[9], d[10],
+                      d[11], d[12], d[13], dv,    io[2], io[3], io[4], d[1],  d[2],  d[3]};
+      if (dir == SCF_LS_X) k_clsvof_sweep<SCF_LS_X, true><<<gsw, bsw, 0, s>>>(vin, lin, tv, tl);
+      else k_clsvof_sweep<SCF_LS_Y, true><<<gsw, bsw, 0, s>>>(vin, lin, tv, tl);
+      note_launch();
+    };
+    for (int k = 1; k <= nv && rc == SCF_OK; ++k) {
+      const int first = k % 2 == 1 ? SCF_LS_X : SCF_LS_Y;
+      double *tv1 = first == SCF_LS_X ? tvx : tvy, *tl1 = first == SCF_LS_X ? tlx : tly;
+      double *tv2 = first == SCF_LS_X ? tvy : tvx, *tl2 = first == SCF_LS_X ? tly : tlx;
+      if (cudaMemcpyAsync(tv1, dv, n1 * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+          cudaMemcpyAsync(tl1, dp, n1 * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+        rc = SCF_ERR_CUDA;
+        break;
+      }
+      sweep(first, k, tv1, tl1);
+      if (first == SCF_LS_X) k_after_first<SCF_LS_X><<<g, 256, 0, s>>>(st, tv1, tl1, dv, dp);
+      else k_after_first<SCF_LS_Y><<<g, 256, 0, s>>>(st, tv1, tl1, dv, dp);
+      k_boundary<<<gb, 256, 0, s>>>(nx, ny, dv, dp);
+      note_launch();
+      note_launch();
+      if (cudaMemcpyAsync(tv2, dv, n1 * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+          cudaMemcpyAsync(tl2, dp, n1 * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+        rc = SCF_ERR_CUDA;
+        break;
+      }
+      const int second = first == SCF_LS_X ? SCF_LS_Y : SCF_LS_X;
+      sweep(second, k, tv2, tl2);
+      if (second == SCF_LS_Y)
+        k_after_second<SCF_LS_Y><<<g, 256, 0, s>>>(st, tv1, tl1, tv2, tl2, dv, dp);
+      else
+        k_after_second<SCF_LS_X><<<g, 256, 0, s>>>(st, tv1, tl1, tv2, tl2, dv, dp);
+      k_boundary<<<gb, 256, 0, s>>>(nx, ny, dv, dp);
+      note_launch();
+      note_launch();
+      launch_reconstruct(irc, n1, s);
+      const RdIn rd{nx,   ny,   dv,   d[0], d[1],  d[2],  d[3],  d[4],
+                    d[5], d[6], d[7], io[2], io[3], io[4], dp,    d_events};
+      const dim3 grd((unsigned)((nx + kRdTx - 1) / kRdTx), (unsigned)((ny + kRdTy - 1) / kRdTy));
+      k_redistance<<<grd, dim3(kRdTx, kRdTy), 0, s>>>(rd);
+      note_launch();
+    }
+    if (rc) break;
+    if (cudaGetLastError() != cudaSuccess) {
+      rc = SCF_ERR_CUDA;
+      break;
+    }
+    if (cudaMemcpyAsync(&h_events, d_events, sizeof(int), cudaMemcpyDeviceToHost, s) !=
+        cudaSuccess)
+      rc = SCF_ERR_CUDA;
+    double* host_out[5] = {vof, phi, nxv, nyv, dis};
+    for (int b = 0; b < 5 && !dev && rc == SCF_OK; ++b)
+      if (cudaMemcpyAsync(host_out[b], io[b], n1 * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        rc = SCF_ERR_CUDA;
   } while (false);
   if (cudaStreamSynchronize(s) != cudaSuccess && rc == SCF_OK) rc = SCF_ERR_CUDA;
   if (mem) cudaFree(mem);

@@ -230,7 +230,9 @@ def test_proj_library_exports_clsvof_header_symbols(built):
     ("scf_ls_fields", "LsFields", {}),
     ("scf_vof_fields", "VofFields", {"nxv": "nx", "nyv": "ny"}),
     ("scf_vof_wave", "VofWave", {}),
-    ("scf_ir_fields", "IrFields", {})])
+    ("scf_ir_fields", "IrFields", {}),
+    ("scf_rd_fields", "RdFields", {"nxv": "nx", "nyv": "ny"}),
+    ("scf_clsvof_fields", "StepFields", {})])
 def test_clsvof_struct_layouts(tmp_path, cname, pyname, rename):
     """The ctypes mirrors of scf_ls_fields, scf_vof_fields and scf_vof_wave
     have the header's layouts."""

@@ -204,3 +204,80 @@ def test_interface_reconstruct_device_pointers_1024(cuda, oracle):
     CL.interface_reconstruct(nx, ny, df, out=out, device_ptrs=True)
     for k in ("nxv", "nyv", "dis"):
         assert _same(out[k].cpu().numpy().reshape((nx, ny), order="F"), want[k]), k
+
+
+# ---------------------------------------------------------------------------
+# Redistance (src/Clsvof_Mod.f90:1525-1708)
+# ---------------------------------------------------------------------------
+def _rd_case(seed, nx, ny, band):
+    from gen.synth import reconstruct_fields
+    import oracle as O
+    f = reconstruct_fields(np.random.default_rng(seed), nx, ny, band)
+    rec, _ = O.interface_reconstruct(nx, ny, f)
+    g = dict(f)
+    g.update(rec)
+    return g
+
+
+@pytest.mark.parametrize("nx,ny,band", [(1, 1, 3.0), (3, 3, 3.0), (9, 7, 1e9), (40, 37, 3.0),
+                                        (300, 257, 3.0), (129, 65, 1e9)])
+def test_redistance_bit_exact(cuda, oracle, nx, ny, band):
+    g = _rd_case(nx * 5 + ny, nx, ny, band) if nx > 2 else None
+    if g is None:  # a single cell: no neighbours
+        g = _rd_case(3, 3, 3, band)
+        g = {k: np.asfortranarray(a[:1, :1]) for k, a in g.items()}
+    want, ev = oracle.redistance(nx, ny, g, g["phi"])
+    got = g["phi"].copy(order="F")
+    ev2, _ = CL.redistance(nx, ny, g, got)
+    assert np.array_equal(got, want, equal_nan=True)
+    assert ev2 == ev
+
+
+def test_redistance_device_pointers_1024(cuda, oracle):
+    import torch
+    nx = ny = 1024
+    g = _rd_case(6, nx, ny, 3.0)
+    want, ev = oracle.redistance(nx, ny, g, g["phi"])
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a.ravel(order="F"))).cuda()
+    dg = {k: T(a) for k, a in g.items()}
+    tp = T(g["phi"])
+    CL.redistance(nx, ny, dg, tp, device_ptrs=True)
+    assert np.array_equal(tp.cpu().numpy().reshape((nx, ny), order="F"), want, equal_nan=True)
+
+
+# ---------------------------------------------------------------------------
+# Coupled_LS_VOF with a fixed solid (src/Clsvof_Mod.f90:730-973)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("nx,ny,wave", [(3, 3, True), (9, 8, True), (64, 61, False),
+                                        (300, 257, True)])
+def test_clsvof_step_bit_exact(cuda, oracle, nx, ny, wave):
+    from gen.synth import clsvof_step_fields
+    f, vof, phi, dt, w = clsvof_step_fields(np.random.default_rng(nx + 2 * ny), nx, ny)
+    w = w if wave else None
+    want, ev = oracle.clsvof_step(nx, ny, f, dt, vof, phi, w)
+    gv, gp = vof.copy(order="F"), phi.copy(order="F")
+    out, ev2, _ = CL.clsvof_step(nx, ny, f, dt, gv, gp, wave=w)
+    assert _same(gv, want["vof"])
+    assert _same(gp, want["phi"])
+    for k in ("nxv", "nyv", "dis"):
+        assert _same(out[k], want[k]), k
+    assert ev2 == ev
+
+
+def test_clsvof_step_device_pointers_1024(cuda, oracle):
+    import torch
+    from gen.synth import clsvof_step_fields
+    nx = ny = 1024
+    f, vof, phi, dt, w = clsvof_step_fields(np.random.default_rng(17), nx, ny)
+    want, ev = oracle.clsvof_step(nx, ny, f, dt, vof, phi, w)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a.ravel(order="F"))).cuda()
+    df = {k: T(a) for k, a in f.items()}
+    tv, tp = T(vof), T(phi)
+    out = {k: torch.zeros(nx * ny, dtype=torch.float64, device="cuda")
+           for k in ("nxv", "nyv", "dis")}
+    CL.clsvof_step(nx, ny, df, dt, tv, tp, wave=w, out=out, device_ptrs=True)
+    back = lambda a: a.cpu().numpy().reshape((nx, ny), order="F")
+    assert _same(back(tv), want["vof"])
+    assert _same(back(tp), want["phi"])
+    for k in ("nxv", "nyv", "dis"):
+        assert _same(back(out[k]), want[k]), k
