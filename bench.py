@@ -801,8 +801,8 @@ def extra_lsweep(case, local, args):
     tv, tl = T(vof), T(phi)
     ms_sw = []
     for _ in range(reps):
-        a = CL.clsvof_sweep(CL.X, nx, ny, sf, vf, dt / 6, tv, temls=tl, wave=wave,
-                            device_ptrs=True, device=local)
+        a = CL.clsvof_sweep(CL.X, nx, ny, sf, vf, dt / 6, tv, temls=tl,
+                            wave=list(wave) + [1], device_ptrs=True, device=local)
         b = CL.clsvof_sweep(CL.Y, nx, ny, sf, vf, dt / 6, tv, temls=tl, device_ptrs=True,
                             device=local)
         ms_sw.append(a + b)

@@ -327,6 +327,13 @@ int scf_proj_time_kernel(scf_proj *h, int kernel, int reps, double *ms_per_launc
  * with IEEE division on many operands. */
 int scf_diag_divide(const double *a, const double *b, double *q, int64_t n, int device);
 
+/* Diagnostics: q[k] = sqrt(a[k]) by the FP64 square root that the CLSVOF
+ * kernels use (integer-pipe arithmetic, correctly rounded to nearest even
+ * like the IEEE square root).  Host arrays.  No counterpart in the
+ * reference; it exists so that tests can compare it bit for bit with the
+ * IEEE square root. */
+int scf_diag_sqrt(const double *a, double *q, int64_t n, int device);
+
 /* Allocation-free right-hand side.  Computes the right-hand side of the
  * pressure equation exactly as SetPoissonVectors does
  * (src/ProjectionP_Mod.f90:313-317) into rhs (nx,ny) (0 where Posnu = -1)

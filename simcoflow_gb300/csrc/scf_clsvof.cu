@@ -33,6 +33,15 @@
 namespace scf {
 namespace {
 
+// The kernels' FP64 division and square root: the correctly rounded
+// integer-pipe forms of the library (identical results to IEEE '/' and
+// sqrt; GB300's FP64 pipe is what bounds these kernels).
+__device__ __forceinline__ double dv(double a, double b) { return div_rn(a, b); }
+__device__ __forceinline__ double sq(double x) { return sqrt_rn(x); }
+// The FP64 pipe's division, for the geometric flux routines: their chains of
+// dependent divisions run faster there than on the longer integer-pipe form.
+__device__ __forceinline__ double dvh(double a, double b) { return __ddiv_rn(a, b); }
+
 struct LsIn {
   int nx, ny;
   double dtv;
@@ -64,25 +73,29 @@ __device__ double face_flux(const Line& L, int f, double dtv) {
   double l;
   if (f == 1) {
     if (u >= 0.0)
-      l = L.P(1) + L.D(1) / 2.0 * (1.0 - u * dtv / L.D(1)) * (L.P(2) - L.P(1)) / (L.C(2) - L.C(1));
+      l = L.P(1) + dv(L.D(1) * 0.5 * (1.0 - dv(u * dtv, L.D(1))) * (L.P(2) - L.P(1)),
+                      L.C(2) - L.C(1));
     else if (DIR == SCF_LS_X)
-      l = L.P(2) - L.D(2) / 2.0 * (1.0 + u * dtv / L.D(2)) * (L.P(3) - L.P(1)) / (2.0 * L.D(2));
+      l = L.P(2) - dv(L.D(2) * 0.5 * (1.0 + dv(u * dtv, L.D(2))) * (L.P(3) - L.P(1)),
+                      2.0 * L.D(2));
     else
-      l = L.P(2) - L.D(2) / 2.0 * (1.0 + u * dtv / L.D(2)) * (L.P(3) - L.P(1)) / (L.C(3) - L.C(1));
+      l = L.P(2) - dv(L.D(2) * 0.5 * (1.0 + dv(u * dtv, L.D(2))) * (L.P(3) - L.P(1)),
+                      L.C(3) - L.C(1));
     return l * u * dtv;
   }
   if (f == n) {
     if (u > 0.0)
-      l = L.P(n) + L.D(n) / 2.0 * (1.0 - u * dtv / L.D(n)) * (L.P(n) - L.P(n - 1)) /
-                       (L.C(n) - L.C(n - 1));
+      l = L.P(n) + dv(L.D(n) * 0.5 * (1.0 - dv(u * dtv, L.D(n))) * (L.P(n) - L.P(n - 1)),
+                      L.C(n) - L.C(n - 1));
     else
-      l = L.P(n) - L.D(n - 1) / 2.0 * (1.0 + u * dtv / L.D(n - 1)) * (L.P(n) - L.P(n - 1)) /
-                       (L.C(n) - L.C(n - 1));
+      l = L.P(n) - dv(L.D(n - 1) * 0.5 * (1.0 + dv(u * dtv, L.D(n - 1))) *
+                          (L.P(n) - L.P(n - 1)),
+                      L.C(n) - L.C(n - 1));
     return l * u * dtv;
   }
-  if (u >= 0.0) l = (L.P(f + 1) + L.P(f - 1)) / 2.0;
-  else if (f <= n - 2) l = (L.P(f + 2) + L.P(f)) / 2.0;
-  else l = (L.P(f + 1) + L.P(f - 1)) / 2.0;
+  if (u >= 0.0) l = (L.P(f + 1) + L.P(f - 1)) * 0.5;
+  else if (f <= n - 2) l = (L.P(f + 2) + L.P(f)) * 0.5;
+  else l = (L.P(f + 1) + L.P(f - 1)) * 0.5;
   return DIR == SCF_LS_X ? u * l * dtv : l * u * dtv;
 }
 
@@ -108,15 +121,15 @@ __device__ double ls_cell(const LsIn& in, long long idx, int i0, int j0, double 
   const int n = L.n;
   const double dtv = in.dtv;
   if (k == 1) {
-    t = t - face_flux<DIR>(L, 1, dtv) * L.Hi(1) / L.D(1);
-    t = t + L.P(1) * L.V(0) * dtv * L.Lo(1) / L.D(1);
+    t = t - dv(face_flux<DIR>(L, 1, dtv) * L.Hi(1), L.D(1));
+    t = t + dv(L.P(1) * L.V(0) * dtv * L.Lo(1), L.D(1));
   } else if (k == 2) {
-    t = t - face_flux<DIR>(L, 2, dtv) * L.Hi(2) / L.D(2);
-    t = t + face_flux<DIR>(L, 1, dtv) * L.Hi(1) / L.D(2);
+    t = t - dv(face_flux<DIR>(L, 2, dtv) * L.Hi(2), L.D(2));
+    t = t + dv(face_flux<DIR>(L, 1, dtv) * L.Hi(1), L.D(2));
   } else {
-    t = t * (1.0 - L.S(k)) + face_flux<DIR>(L, k - 1, dtv) * L.Lo(k) / L.D(k);
-    if (k < n || DIR == SCF_LS_X) t = t - face_flux<DIR>(L, k, dtv) * L.Hi(k) / L.D(k);
-    else t = t - face_flux<DIR>(L, k, dtv) / L.D(k);
+    t = t * (1.0 - L.S(k)) + dv(face_flux<DIR>(L, k - 1, dtv) * L.Lo(k), L.D(k));
+    if (k < n || DIR == SCF_LS_X) t = t - dv(face_flux<DIR>(L, k, dtv) * L.Hi(k), L.D(k));
+    else t = t - dv(face_flux<DIR>(L, k, dtv), L.D(k));
   }
   return t;
 }
@@ -132,18 +145,18 @@ __device__ double frac_part(double nx, double ny, double diss, double dx, double
   const double tnx = fabs(nx), tny = fabs(ny);
   if (diss + 0.5 * (tnx * dx + tny * dy) <= 0.0) return 1.0;
   if (diss - 0.5 * (tnx * dx + tny * dy) >= 0.0) return 0.0;
-  if (tnx <= 1e-20) return 0.5 - diss / dy;
-  if (tny <= 1e-20) return 0.5 - diss / dx;
-  const double xx = (0.5 * tny * dy - diss) / dx / tnx + 0.5;
-  const double yy = (0.5 * tnx * dx - diss) / dy / tny + 0.5;
+  if (tnx <= 1e-20) return 0.5 - dvh(diss, dy);
+  if (tny <= 1e-20) return 0.5 - dvh(diss, dx);
+  const double xx = dvh(dvh(0.5 * tny * dy - diss, dx), tnx) + 0.5;
+  const double yy = dvh(dvh(0.5 * tnx * dx - diss, dy), tny) + 0.5;
   const double total = 0.5 * xx * yy;
   double top = 0.0, right = 0.0;
   if (yy > 1.0) {
-    const double r = (yy - 1.0) / yy;
+    const double r = dvh(yy - 1.0, yy);
     top = r * r;
   }
   if (xx > 1.0) {
-    const double r = (xx - 1.0) / xx;
+    const double r = dvh(xx - 1.0, xx);
     right = r * r;
   }
   return total * (1.0 - top - right);
@@ -157,7 +170,7 @@ __device__ double frac_part(double nx, double ny, double diss, double dx, double
 __device__ void cell_geo(double nxs, double nys, double phis, double nxl, double nyl, double phil,
                          double dx, double dy, double& vols, double& volf) {
   double px[8], py[8], pd[8];  // at most 8 puts below (5 in exact arithmetic)
-  const double dx2 = dx / 2.0, dy2 = dy / 2.0;
+  const double dx2 = dx * 0.5, dy2 = dy * 0.5;
   const double d0 = dx2 * nxs - dy2 * nys + phis, d1 = -(dx2 * nxs) - dy2 * nys + phis;
   const double d2 = -(dx2 * nxs) + dy2 * nys + phis, d3 = dx2 * nxs + dy2 * nys + phis;
   int m = 0;
@@ -167,20 +180,20 @@ __device__ void cell_geo(double nxs, double nys, double phis, double nxl, double
     ++m;
   };
   if (d0 >= 0.0) put(dx2, -dy2);
-  if (d0 * d1 < 0.0) put((dy2 * nys - phis) / nxs, -dy2);
+  if (d0 * d1 < 0.0) put(dvh(dy2 * nys - phis, nxs), -dy2);
   if (d1 >= 0.0) put(-dx2, -dy2);
-  if (d1 * d2 < 0.0) put(-dx2, (dx2 * nxs - phis) / nys);
+  if (d1 * d2 < 0.0) put(-dx2, dvh(dx2 * nxs - phis, nys));
   if (d2 >= 0.0) put(-dx2, dy2);
-  if (d2 * d3 < 0.0) put((-(dy2 * nys) - phis) / nxs, dy2);
+  if (d2 * d3 < 0.0) put(dvh(-(dy2 * nys) - phis, nxs), dy2);
   if (d3 >= 0.0) put(dx2, dy2);
-  if (d3 * d0 < 0.0) put(dx2, (-(dx2 * nxs) - phis) / nys);
+  if (d3 * d0 < 0.0) put(dx2, dvh(-(dx2 * nxs) - phis, nys));
   double vol = 0.0;
   for (int k = 0; k < m; ++k) {
     const int k1 = k + 1 < m ? k + 1 : 0;
     vol = vol + 0.5 * (px[k] * py[k1] - px[k1] * py[k]);
     pd[k] = px[k] * nxl + py[k] * nyl + phil;
   }
-  vols = 1.0 - fabs(vol / (dx * dy));
+  vols = 1.0 - fabs(dvh(vol, dx * dy));
   // liquid polygon, streamed: keep its first vertex and the previous one
   double fx = 0.0, fy = 0.0, lx = 0.0, ly = 0.0;
   int ml = 0;
@@ -201,11 +214,11 @@ __device__ void cell_geo(double nxs, double nys, double phis, double nxl, double
     if (pd[k] <= 0.0) add(px[k], py[k]);
     if (pd[k] * pd[k1] < 0.0) {
       const double w = fabs(pd[k]), ws = fabs(pd[k]) + fabs(pd[k1]);
-      add(px[k] + (px[k1] - px[k]) * w / ws, py[k] + (py[k1] - py[k]) * w / ws);
+      add(px[k] + dvh((px[k1] - px[k]) * w, ws), py[k] + dvh((py[k1] - py[k]) * w, ws));
     }
   }
   if (ml > 0) vol = vol + 0.5 * (lx * fy - fx * ly);
-  volf = fabs(vol / (dx * dy));
+  volf = fabs(dvh(vol, dx * dy));
 }
 
 // The inputs of one cell's upwind flux.
@@ -233,8 +246,8 @@ __device__ double face_geo(const VofCell& c, double vdt) {
     const double ds = SIDE < 0 ? c.phiS - sh * ns : c.phiS + sh * ns;
     double volss;
     cell_geo(c.nxs, c.nys, ds, c.nxv, c.nyv, dl, sx, sy, volss, flux);
-    if (c.vof / (1.0 - c.vofS) >= 1.0 - kVofEps) flux = 1.0 - volss;
-    flux = flux / (1.0 - volss + kTolDeno);
+    if (dvh(c.vof, 1.0 - c.vofS) >= 1.0 - kVofEps) flux = 1.0 - volss;
+    flux = dvh(flux, 1.0 - volss + kTolDeno);
     if (c.vof + c.vofS > 1.0 - 1e-14) flux = 1.0;
   }
   return flux * vdt;
@@ -354,15 +367,15 @@ __global__ void __launch_bounds__(kSwTx* kSwTy)
   const long long idx = (long long)i0 + (long long)j0 * nx;
   double t = temvf[idx];
   const double s = L.S(k);
-  if (s < 1.0 - kVofEps) t = t / (1.0 - s);
+  if (s < 1.0 - kVofEps) t = dv(t, 1.0 - s);
   if (k == 1) {
-    t = t - fhi * L.Hi(1) / L.D(1);
+    t = t - dv(fhi * L.Hi(1), L.D(1));
     if (DIR == SCF_LS_X) {
       double fin = 0.0;
-      if (vin.y[idx] - vin.dy[idx] / 2.0 < vin.level) fin = L.F(1) * L.V(0) * dtv;
-      t = t + fin * L.Lo(1) / L.D(1);
+      if (vin.y[idx] - vin.dy[idx] * 0.5 < vin.level) fin = L.F(1) * L.V(0) * dtv;
+      t = t + dv(fin * L.Lo(1), L.D(1));
     } else {
-      t = t + L.F(1) * L.V(0) * dtv * L.Lo(1) / L.D(1);
+      t = t + dv(L.F(1) * L.V(0) * dtv * L.Lo(1), L.D(1));
     }
   } else {
     double flo;
@@ -370,8 +383,8 @@ __global__ void __launch_bounds__(kSwTx* kSwTy)
       flo = DIR == SCF_LS_X ? face[threadIdx.y][threadIdx.x - 1] : face[threadIdx.y - 1][threadIdx.x];
     else
       flo = vof_face<DIR>(L, k - 1, dtv);
-    t = t * (1.0 - s) + flo * L.Lo(k) / L.D(k);
-    t = t - fhi * L.Hi(k) / L.D(k);
+    t = t * (1.0 - s) + dv(flo * L.Lo(k), L.D(k));
+    t = t - dv(fhi * L.Hi(k), L.D(k));
   }
   temvf[idx] = t;
   if (LS) temls[idx] = ls_cell<DIR>(lin, idx, i0, j0, temls[idx]);
@@ -426,10 +439,10 @@ struct IrIn {
   __device__ double P(int i, int j) const { return phi[at(i, j)]; }
   __device__ double S(int i, int j) const { return vofS[at(i, j)]; }
   __device__ double gx(int a, int b, int j) const {
-    return (phi[at(a, j)] - phi[at(b, j)]) / (x[at(a, j)] - x[at(b, j)]);
+    return dv(phi[at(a, j)] - phi[at(b, j)], x[at(a, j)] - x[at(b, j)]);
   }
   __device__ double gy(int i, int a, int b) const {
-    return (phi[at(i, a)] - phi[at(i, b)]) / (y[at(i, a)] - y[at(i, b)]);
+    return dv(phi[at(i, a)] - phi[at(i, b)], y[at(i, a)] - y[at(i, b)]);
   }
   __device__ int flag(int i, int j) const {
     const double v = vof[at(i, j)], s = vofS[at(i, j)];
@@ -440,7 +453,7 @@ struct IrIn {
   }
 };
 
-__device__ double unit_dev(double vx, double vy) { return fabs(1.0 - sqrt(vx * vx + vy * vy)); }
+__device__ double unit_dev(double vx, double vy) { return fabs(1.0 - sq(vx * vx + vy * vy)); }
 
 // The direction of Vset most parallel to the central gradient, then the
 // one-sided pair closer to unit length (:1768-1832, :1860-1912).
@@ -449,7 +462,7 @@ __device__ void most_parallel(const IrIn& c, int i, int j, int imv, double& nxo,
   double maxv = 0.0;
   for (int ii = 1; ii <= 8; ++ii) {
     const double a = kVset[ii - 1][0], b = kVset[ii - 1][1];
-    const double cp = fabs(a * vx + b * vy) / (sqrt(a * a + b * b) * sqrt(vx * vx + vy * vy));
+    const double cp = dv(fabs(a * vx + b * vy), sq(a * a + b * b) * sq(vx * vx + vy * vy));
     if (cp >= maxv) {
       maxv = cp;
       imv = ii;
@@ -542,17 +555,17 @@ __device__ double plic_distance(double v, double dx, double dy, double nxx, doub
       double t = vful; vful = vflr; vflr = t;
       t = dul; dul = dlr; dlr = t;
     }
-    return dll - sqrt(((dul - dll) * (dul - dll)) * v / vful);
+    return dll - sq(dv(((dul - dll) * (dul - dll)) * v, vful));
   }
   if (v >= vful && v >= vflr) {
     if (vflr < vful) {
       double t = vful; vful = vflr; vflr = t;
       t = dul; dul = dlr; dlr = t;
     }
-    return dur + sqrt((dlr - dur) * (dlr - dur) * (1.0 - v) / (1.0 - vflr));
+    return dur + sq(dv((dlr - dur) * (dlr - dur) * (1.0 - v), 1.0 - vflr));
   }
   if (fabs(vflr - vful) < 1e-20) return 0.5 * (dul + dlr);
-  const double t = (v - vful) / (vflr - vful);
+  const double t = dv(v - vful, vflr - vful);
   return dlr * t + dul * (1.0 - t);
 }
 
@@ -590,13 +603,13 @@ __device__ double liq_func_vol(const double (&node)[9][2], double nxf, double ny
     if (pk <= 0.0) add(node[k][0], node[k][1]);
     if (pk * pn < 0.0) {
       const double w = fabs(pk), ws = fabs(pk) + fabs(pn);
-      add(node[k][0] + (node[k + 1][0] - node[k][0]) * w / ws,
-          node[k][1] + (node[k + 1][1] - node[k][1]) * w / ws);
+      add(node[k][0] + dv((node[k + 1][0] - node[k][0]) * w, ws),
+          node[k][1] + dv((node[k + 1][1] - node[k][1]) * w, ws));
     }
     pk = pn;
   }
   if (ml > 0) vol = vol + 0.5 * (lx * fy - fx * ly);
-  return volf - fabs(vol / (dx * dy));
+  return volf - fabs(dv(vol, dx * dy));
 }
 
 // DistanceFluidCalculate + zriddr: true when the reference assigns phif.
@@ -604,7 +617,7 @@ __device__ bool fluid_distance(double nxss, double nyss, double phiss, double nx
                                double volf, double dx, double dy, double& phif, int* events) {
   double node[9][2];
   for (int k = 0; k < 9; ++k) node[k][0] = node[k][1] = 0.0;
-  const double dx2 = dx / 2.0, dy2 = dy / 2.0, tol = 1e-14, unused = -1.11e-30;
+  const double dx2 = dx * 0.5, dy2 = dy * 0.5, tol = 1e-14, unused = -1.11e-30;
   const double d0 = dx2 * nxss - dy2 * nyss + phiss, d1 = -(dx2 * nxss) - dy2 * nyss + phiss;
   const double d2 = -(dx2 * nxss) + dy2 * nyss + phiss, d3 = dx2 * nxss + dy2 * nyss + phiss;
   int m = 0;
@@ -614,18 +627,18 @@ __device__ bool fluid_distance(double nxss, double nyss, double phiss, double nx
     ++m;
   };
   if (d0 >= 0.0) put(dx2, -dy2);
-  if (d0 * d1 < 0.0) put((dy2 * nyss - phiss) / nxss, -dy2);
+  if (d0 * d1 < 0.0) put(dv(dy2 * nyss - phiss, nxss), -dy2);
   if (d1 >= 0.0) put(-dx2, -dy2);
-  if (d1 * d2 < 0.0) put(-dx2, (dx2 * nxss - phiss) / nyss);
+  if (d1 * d2 < 0.0) put(-dx2, dv(dx2 * nxss - phiss, nyss));
   if (d2 >= 0.0) put(-dx2, dy2);
-  if (d2 * d3 < 0.0) put((-(dy2 * nyss) - phiss) / nxss, dy2);
+  if (d2 * d3 < 0.0) put(dv(-(dy2 * nyss) - phiss, nxss), dy2);
   if (d3 >= 0.0) put(dx2, dy2);
-  if (d3 * d0 < 0.0) put(dx2, (-(dx2 * nxss) - phiss) / nyss);
+  if (d3 * d0 < 0.0) put(dx2, dv(-(dx2 * nxss) - phiss, nyss));
   node[m][0] = node[0][0];  // m <= 8 above, so node[m] is in bounds
   node[m][1] = node[0][1];
   double mx0 = 0.0, mx1 = 0.0, mn0 = 0.0, mn1 = 0.0;
   {
-    double maxd = -2.0 * sqrt(dx * dx + dy * dy), mind = 2.0 * sqrt(dx * dx + dy * dy);
+    double maxd = -2.0 * sq(dx * dx + dy * dy), mind = 2.0 * sq(dx * dx + dy * dy);
     for (int k = 0; k < m; ++k) {
       const double t = nxf * node[k][0] + nyf * node[k][1];
       if (t > maxd) {
@@ -652,11 +665,12 @@ __device__ bool fluid_distance(double nxss, double nyss, double phiss, double nx
     for (int iter = 1; iter <= 1000; ++iter) {
       const double xm0 = 0.5 * (xl0 + xh0), xm1 = 0.5 * (xl1 + xh1);
       const double fm = liq_func_vol(node, nxf, nyf, volf, dx, dy, xm0, xm1, events);
-      const double s = sqrt(fm * fm - fl * fh);
+      const double s = sq(fm * fm - fl * fh);
       if (s == 0.0) atomicAdd(events, 1);
       const double sg = copysign(1.0, fl - fh);
-      const double xn0 = xm0 + (xm0 - xl0) * sg * fm / s, xn1 = xm1 + (xm1 - xl1) * sg * fm / s;
-      if (sqrt((xn0 - a0) * (xn0 - a0) + (xn1 - a1) * (xn1 - a1)) <= tol) {
+      const double xn0 = xm0 + dv((xm0 - xl0) * sg * fm, s);
+      const double xn1 = xm1 + dv((xm1 - xl1) * sg * fm, s);
+      if (sq((xn0 - a0) * (xn0 - a0) + (xn1 - a1) * (xn1 - a1)) <= tol) {
         phif = -(nxf * a0 + nyf * a1);
         return true;
       }
@@ -677,7 +691,7 @@ __device__ bool fluid_distance(double nxss, double nyss, double phiss, double nx
       } else {
         atomicAdd(events, 1);
       }
-      if (sqrt((xh0 - xl0) * (xh0 - xl0) + (xh1 - xl1) * (xh1 - xl1)) <= tol) {
+      if (sq((xh0 - xl0) * (xh0 - xl0) + (xh1 - xl1) * (xh1 - xl1)) <= tol) {
         phif = -(nxf * a0 + nyf * a1);
         return true;
       }
@@ -714,13 +728,13 @@ __device__ void ir_cell(const IrIn& c, int i, int j, double nxx, double nyy) {
       if (j == 1) nyy = c.gy(i, j + 1, j);
       else if (j == ny) nyy = c.gy(i, j, j - 1);
     }
-    const double t = sqrt(nxx * nxx + nyy * nyy);
+    const double t = sq(nxx * nxx + nyy * nyy);
     if (t < 1e-14) {
       nxx = 0.0;
       nyy = 1.0;
     } else {
-      nxx = nxx / t;
-      nyy = nyy / t;
+      nxx = dv(nxx, t);
+      nyy = dv(nyy, t);
     }
     if (flag == 1)
       diss = plic_distance(v, c.dx[a], c.dy[a], nxx, nyy);
@@ -730,7 +744,7 @@ __device__ void ir_cell(const IrIn& c, int i, int j, double nxx, double nyy) {
   } else {
     nxx = 0.0;
     nyy = 1.0;
-    if (1.0 - s > kVofEps) diss = (0.5 - v / (1.0 - s)) * c.dy[a];
+    if (1.0 - s > kVofEps) diss = (0.5 - dv(v, 1.0 - s)) * c.dy[a];
     else diss = (0.0 - v) * c.dy[a];
   }
   c.nxv[a] = nxx;
@@ -776,8 +790,8 @@ __global__ void k_ir_sides(IrIn c) {
     double nyy = c.nyv[c.at(i, j0)];
     for (int jj = j0 + 1; jj < j; ++jj) {  // flagged cells between: their normalised nyy
       const double nxx = i == 1 ? c.gx(i + 1, i, jj) : c.gx(i, i - 1, jj);
-      const double tt = sqrt(nxx * nxx + nyy * nyy);
-      nyy = tt < 1e-14 ? 1.0 : nyy / tt;
+      const double tt = sq(nxx * nxx + nyy * nyy);
+      nyy = tt < 1e-14 ? 1.0 : dv(nyy, tt);
     }
     ir_cell(c, i, j, 0.0, nyy);
   }
@@ -837,16 +851,16 @@ struct RdIn {
 __device__ bool inside_rect(double xp, double yp, double dx, double dy) {
   const double x1 = -0.5 * dx, y1 = 0.5 * dy, x2 = 0.5 * dx, y2 = 0.5 * dy;
   const double x3 = 0.5 * dx, y3 = -0.5 * dy, x4 = -0.5 * dx, y4 = -0.5 * dy;
-  const double b1 = sqrt((x1 - xp) * (x1 - xp) + (y1 - yp) * (y1 - yp));
-  const double b2 = sqrt((x2 - xp) * (x2 - xp) + (y2 - yp) * (y2 - yp));
-  const double b3 = sqrt((x3 - xp) * (x3 - xp) + (y3 - yp) * (y3 - yp));
-  const double b4 = sqrt((x4 - xp) * (x4 - xp) + (y4 - yp) * (y4 - yp));
+  const double b1 = sq((x1 - xp) * (x1 - xp) + (y1 - yp) * (y1 - yp));
+  const double b2 = sq((x2 - xp) * (x2 - xp) + (y2 - yp) * (y2 - yp));
+  const double b3 = sq((x3 - xp) * (x3 - xp) + (y3 - yp) * (y3 - yp));
+  const double b4 = sq((x4 - xp) * (x4 - xp) + (y4 - yp) * (y4 - yp));
   const double u1 = 0.5 * (dx + b1 + b2), u2 = 0.5 * (dy + b2 + b3);
   const double u3 = 0.5 * (dx + b3 + b4), u4 = 0.5 * (dy + b4 + b1);
-  const double a1 = sqrt(u1 * (u1 - dx) * (u1 - b1) * (u1 - b2));
-  const double a2 = sqrt(u2 * (u2 - dy) * (u2 - b2) * (u2 - b3));
-  const double a3 = sqrt(u3 * (u3 - dx) * (u3 - b3) * (u3 - b4));
-  const double a4 = sqrt(u4 * (u4 - dy) * (u4 - b4) * (u4 - b1));
+  const double a1 = sq(u1 * (u1 - dx) * (u1 - b1) * (u1 - b2));
+  const double a2 = sq(u2 * (u2 - dy) * (u2 - b2) * (u2 - b3));
+  const double a3 = sq(u3 * (u3 - dx) * (u3 - b3) * (u3 - b4));
+  const double a4 = sq(u4 * (u4 - dy) * (u4 - b4) * (u4 - b1));
   return fabs(a1 + a2 + a3 + a4 - dx * dy) < 1e-10;
 }
 
@@ -867,39 +881,39 @@ __device__ double rd_update(const RdIn& c, int i, int j, int ii, int jj, double 
   const double n1 = c.nxv[a], n2 = c.nyv[a], d1 = c.dis[a];
   auto solid = [&](double px, double py) { return nxs * px + nys * py + phs; };
   const int l = ii < -1 ? -1 : (ii > 1 ? 1 : ii), m = jj < -1 ? -1 : (jj > 1 ? 1 : jj);
-  double xv = dxs * (double)l / 2.0, yv = dys * (double)m / 2.0;
+  double xv = dxs * (double)l * 0.5, yv = dys * (double)m * 0.5;
   if (solid(xv, yv) < 0.0) {
     if (fabs(yv) < kVofEps) {
-      yv = dys / 2.0;
+      yv = dys * 0.5;
       if (solid(xv, yv) < 0.0) {
-        yv = -dys / 2.0;
+        yv = -dys * 0.5;
         if (solid(xv, yv) < 0.0) {
-          xv = dxs * (0.0 - (double)l) / 2.0;
-          if (solid(xv, yv) < 0.0) yv = dys / 2.0;
+          xv = dxs * (0.0 - (double)l) * 0.5;
+          if (solid(xv, yv) < 0.0) yv = dys * 0.5;
         }
       }
     } else if (fabs(xv) < kVofEps) {
-      xv = dxs / 2.0;
+      xv = dxs * 0.5;
       if (solid(xv, yv) < 0.0) {
-        xv = -dxs / 2.0;
+        xv = -dxs * 0.5;
         if (solid(xv, yv) < 0.0) {
-          yv = dys * (0.0 - (double)m) / 2.0;
-          if (solid(xv, yv) < 0.0) xv = dxs / 2.0;
+          yv = dys * (0.0 - (double)m) * 0.5;
+          if (solid(xv, yv) < 0.0) xv = dxs * 0.5;
         }
       }
     } else {
-      yv = dys * (0.0 - (double)m) / 2.0;
+      yv = dys * (0.0 - (double)m) * 0.5;
       if (solid(xv, yv) < 0.0) {
-        xv = dxs * (0.0 - (double)l) / 2.0;
-        yv = dys * (double)m / 2.0;
-        if (solid(xv, yv) < 0.0) yv = dys * (0.0 - (double)m) / 2.0;
+        xv = dxs * (0.0 - (double)l) * 0.5;
+        yv = dys * (double)m * 0.5;
+        if (solid(xv, yv) < 0.0) yv = dys * (0.0 - (double)m) * 0.5;
       }
     }
   }
   const double rx = xT - c.x[a], ry = yT - c.y[a];
-  const double dv = n1 * xv + n2 * yv + d1;
-  if (dv * copysign(1.0, phiT) <= 0.0) {
-    const double deuc = sqrt((rx - xv) * (rx - xv) + (ry - yv) * (ry - yv));
+  const double dvl = n1 * xv + n2 * yv + d1;
+  if (dvl * copysign(1.0, phiT) <= 0.0) {
+    const double deuc = sq((rx - xv) * (rx - xv) + (ry - yv) * (ry - yv));
     if (sT < kEpsi) return copysign(1.0, 0.5 - vT) * fmin(deuc, fabs(pa));
     return closer(pa, deuc, vT, sT);
   }
@@ -907,14 +921,14 @@ __device__ double rd_update(const RdIn& c, int i, int j, int ii, int jj, double 
   const double xp = rx - dij1 * n1, yp = ry - dij1 * n2;
   const bool in = inside_rect(xp, yp, dxs, dys);
   if (in && sT < kEpsi) {
-    const double deuc = sqrt((rx - xp) * (rx - xp) + (ry - yp) * (ry - yp));
+    const double deuc = sq((rx - xp) * (rx - xp) + (ry - yp) * (ry - yp));
     return copysign(1.0, 0.5 - vT) * fmin(deuc, fabs(pa));
   }
   if (in && sT >= kEpsi && sT < 1.0 - kEpsi)
-    return closer(pa, sqrt((rx - xp) * (rx - xp) + (ry - yp) * (ry - yp)), vT, sT);
+    return closer(pa, sq((rx - xp) * (rx - xp) + (ry - yp) * (ry - yp)), vT, sT);
   if (sT >= 1.0 - kEpsi) {
     if (c.vofS[a] < kEpsi) {
-      const double deuc = sqrt((rx - xp) * (rx - xp) + (ry - yp) * (ry - yp));
+      const double deuc = sq((rx - xp) * (rx - xp) + (ry - yp) * (ry - yp));
       if (fabs(deuc) < fabs(pa)) pa = copysign(1.0, dij1) * deuc;
     }
     return pa;
@@ -924,12 +938,12 @@ __device__ double rd_update(const RdIn& c, int i, int j, int ii, int jj, double 
   double xs, ys;
   if (xoff * fabs(n1 + tol) >= yoff * fabs(n2 + tol)) {
     xs = xfc;
-    ys = (d1 + n1 * xs) / (-n2 + tol);
+    ys = dv(d1 + n1 * xs, -n2 + tol);
   } else {
     ys = yfc;
-    xs = (d1 + n2 * ys) / (-n1 + tol);
+    xs = dv(d1 + n2 * ys, -n1 + tol);
   }
-  const double deuc = sqrt((rx - xs) * (rx - xs) + (ry - ys) * (ry - ys));
+  const double deuc = sq((rx - xs) * (rx - xs) + (ry - ys) * (ry - ys));
   if (solid(xs, ys) >= 0.0) {
     if (sT < kEpsi) return copysign(1.0, 0.5 - vT) * fmin(deuc, fabs(pa));
     return closer(pa, deuc, vT, sT);
@@ -955,7 +969,7 @@ __global__ void __launch_bounds__(kRdTx* kRdTy) k_redistance(RdIn c) {
   if (p > c.nx || q > c.ny) return;
   const long long t = c.at(p, q);
   const double vT = c.vof[t], sT = c.vofS[t];
-  const double h = sqrt(c.dx[t] * c.dx[t] + c.dy[t] * c.dy[t]);
+  const double h = sq(c.dx[t] * c.dx[t] + c.dy[t] * c.dy[t]);
   double out = c.phi[t];
   bool fix = false;
   double pa = 1e4;
@@ -1015,8 +1029,8 @@ __global__ void k_after_first(StepIn c, double* tv, double* tl, double* vof, dou
        idx += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(idx % c.nx) + 1, j = (int)(idx / c.nx) + 1;
     const double s = c.vofS[idx], h = DIR == SCF_LS_X ? c.dx[idx] : c.dy[idx];
-    const double den = (1.0 - s + kTolDeno) - c.dtv / h * c.div(DIR, i, j);
-    const double a = tv[idx] / den, b = tl[idx] / den;
+    const double den = (1.0 - s + kTolDeno) - dv(c.dtv, h) * c.div(DIR, i, j);
+    const double a = dv(tv[idx], den), b = dv(tl[idx], den);
     tv[idx] = a;
     tl[idx] = b;
     double v = a * (1.0 - s);
@@ -1038,12 +1052,12 @@ __global__ void k_after_second(StepIn c, const double* t1v, const double* t1l, d
     const int i = (int)(idx % c.nx) + 1, j = (int)(idx / c.nx) + 1;
     const double s = c.vofS[idx], h = DIR == SCF_LS_X ? c.dx[idx] : c.dy[idx];
     const double d = c.div(DIR, i, j);
-    const double a = tv[idx] + c.dtv / h * t1v[idx] * d;
-    const double b = tl[idx] + c.dtv / h * t1l[idx] * d;
+    const double a = tv[idx] + dv(c.dtv, h) * t1v[idx] * d;
+    const double b = tl[idx] + dv(c.dtv, h) * t1l[idx] * d;
     tv[idx] = a;
     tl[idx] = b;
     vof[idx] = a;
-    if (s < 1.0 - kEpsi) phi[idx] = b / (1.0 - s);
+    if (s < 1.0 - kEpsi) phi[idx] = dv(b, 1.0 - s);
   }
 }
 
@@ -1448,7 +1462,7 @@ extern "C" int scf_clsvof_step(int nx, int ny, const scf_clsvof_fields* f,
     } else {
       for (int a = 0; a < 14; ++a) d[a] = arr[a];
     }
-    double* dv = io[0];
+    double* dvof = io[0];
     double* dp = io[1];
     // the X inlet's level per sub-step, on the host as in X_Sweep
     double x11 = 0.0, dx11 = 0.0;
@@ -1466,7 +1480,7 @@ extern "C" int scf_clsvof_step(int nx, int ny, const scf_clsvof_fields* f,
     }
     const int nv = 6;
     const double dtv = dt / (double)nv;
-    const IrIn irc{nx,   ny,   dv,   d[0],  dp,    d[1],  d[2],   d[3],    d[4],
+    const IrIn irc{nx,   ny,   dvof,   d[0],  dp,    d[1],  d[2],   d[3],    d[4],
                    d[5], d[6], d[7], io[2], io[3], io[4], failed, d_events};
     const LsIn lin{nx,   ny,   dtv,  dp,   d[0],  d[6],  d[7],  d[4],
                    d[5], d[8], d[9], d[10], d[11], d[12], d[13]};
@@ -1484,7 +1498,7 @@ extern "C" int scf_clsvof_step(int nx, int ny, const scf_clsvof_fields* f,
                 wave->amp0 * std::sin(wave->kw * xwu - wave->omew * (wave->nondit + (double)k * dtv));
       }
       const VofIn vin{nx,    ny,    dtv,   level, d[0],  d[6],  d[7],  d[5],  d[8],  d[9], d[10],
-                      d[11], d[12], d[13], dv,    io[2], io[3], io[4], d[1],  d[2],  d[3]};
+                      d[11], d[12], d[13], dvof,    io[2], io[3], io[4], d[1],  d[2],  d[3]};
       if (dir == SCF_LS_X) k_clsvof_sweep<SCF_LS_X, true><<<gsw, bsw, 0, s>>>(vin, lin, tv, tl);
       else k_clsvof_sweep<SCF_LS_Y, true><<<gsw, bsw, 0, s>>>(vin, lin, tv, tl);
       note_launch();
@@ -1493,18 +1507,18 @@ extern "C" int scf_clsvof_step(int nx, int ny, const scf_clsvof_fields* f,
       const int first = k % 2 == 1 ? SCF_LS_X : SCF_LS_Y;
       double *tv1 = first == SCF_LS_X ? tvx : tvy, *tl1 = first == SCF_LS_X ? tlx : tly;
       double *tv2 = first == SCF_LS_X ? tvy : tvx, *tl2 = first == SCF_LS_X ? tly : tlx;
-      if (cudaMemcpyAsync(tv1, dv, n1 * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+      if (cudaMemcpyAsync(tv1, dvof, n1 * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
           cudaMemcpyAsync(tl1, dp, n1 * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
         rc = SCF_ERR_CUDA;
         break;
       }
       sweep(first, k, tv1, tl1);
-      if (first == SCF_LS_X) k_after_first<SCF_LS_X><<<g, 256, 0, s>>>(st, tv1, tl1, dv, dp);
-      else k_after_first<SCF_LS_Y><<<g, 256, 0, s>>>(st, tv1, tl1, dv, dp);
-      k_boundary<<<gb, 256, 0, s>>>(nx, ny, dv, dp);
+      if (first == SCF_LS_X) k_after_first<SCF_LS_X><<<g, 256, 0, s>>>(st, tv1, tl1, dvof, dp);
+      else k_after_first<SCF_LS_Y><<<g, 256, 0, s>>>(st, tv1, tl1, dvof, dp);
+      k_boundary<<<gb, 256, 0, s>>>(nx, ny, dvof, dp);
       note_launch();
       note_launch();
-      if (cudaMemcpyAsync(tv2, dv, n1 * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+      if (cudaMemcpyAsync(tv2, dvof, n1 * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
           cudaMemcpyAsync(tl2, dp, n1 * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
         rc = SCF_ERR_CUDA;
         break;
@@ -1512,14 +1526,14 @@ extern "C" int scf_clsvof_step(int nx, int ny, const scf_clsvof_fields* f,
       const int second = first == SCF_LS_X ? SCF_LS_Y : SCF_LS_X;
       sweep(second, k, tv2, tl2);
       if (second == SCF_LS_Y)
-        k_after_second<SCF_LS_Y><<<g, 256, 0, s>>>(st, tv1, tl1, tv2, tl2, dv, dp);
+        k_after_second<SCF_LS_Y><<<g, 256, 0, s>>>(st, tv1, tl1, tv2, tl2, dvof, dp);
       else
-        k_after_second<SCF_LS_X><<<g, 256, 0, s>>>(st, tv1, tl1, tv2, tl2, dv, dp);
-      k_boundary<<<gb, 256, 0, s>>>(nx, ny, dv, dp);
+        k_after_second<SCF_LS_X><<<g, 256, 0, s>>>(st, tv1, tl1, tv2, tl2, dvof, dp);
+      k_boundary<<<gb, 256, 0, s>>>(nx, ny, dvof, dp);
       note_launch();
       note_launch();
       launch_reconstruct(irc, n1, s);
-      const RdIn rd{nx,   ny,   dv,   d[0], d[1],  d[2],  d[3],  d[4],
+      const RdIn rd{nx,   ny,   dvof,   d[0], d[1],  d[2],  d[3],  d[4],
                     d[5], d[6], d[7], io[2], io[3], io[4], dp,    d_events};
       const dim3 grd((unsigned)((nx + kRdTx - 1) / kRdTx), (unsigned)((ny + kRdTy - 1) / kRdTy));
       k_redistance<<<grd, dim3(kRdTx, kRdTy), 0, s>>>(rd);

@@ -204,6 +204,50 @@ __device__ __forceinline__ double div_rn(double a, double b) {
   return __longlong_as_double((long long)bits);
 }
 
+static __device__ __noinline__ double sqrt_rare(double x) { return __dsqrt_rn(x); }
+
+// Correctly rounded FP64 square root (IEEE round to nearest even) on the
+// integer pipe, for the same reason as div_rn.  Method: x = M 2^(2k) with M
+// in [1, 4); Newton-Raphson iteration y <- y (3 - M y^2) / 2 for 1/sqrt(M)
+// in 64-bit fixed point (2^63 = 1), seeded by the FP32 reciprocal square
+// root approximation; the 53-bit root q ~ M y 2^52 of N = M 2^104 from one
+// high product; then the exact remainder r = N - q^2 moves q to the floor of
+// sqrt(N) and gives the rounding bit (round up when r > q: a square root is
+// never exactly halfway between two doubles), the integer square root's
+// closing step (Knuth, TAOCP vol. 2, 4.6.4; Muller et al., Handbook of
+// Floating-Point Arithmetic, ch. 9).  Zero, negative, subnormal, infinite or
+// NaN operands take the IEEE square root.
+__device__ __forceinline__ double sqrt_rn(double x) {
+  using u64 = unsigned long long;
+  const u64 ux = (u64)__double_as_longlong(x);
+  const int e = (int)(ux >> 52);  // the sign bit included: positive normal is 1 .. 2046
+  if ((unsigned)(e - 1) >= 2046u) return sqrt_rare(x);
+  const int E = e - 1023, odd = E & 1;
+  const u64 m = (ux & 0xfffffffffffffull) | (1ull << 52);
+  const u64 Mf = m << (10 + odd);  // M 2^62
+  float y0;
+  asm("rsqrt.approx.ftz.f32 %0, %1;"
+      : "=f"(y0)
+      : "f"(__uint_as_float((0x3f800000u + ((unsigned)odd << 23)) |
+                            (unsigned)((ux >> 29) & 0x7fffffu))));
+  const unsigned yb = __float_as_uint(y0);  // in (0.5, 1]: exponent field 126 or 127
+  u64 Y = (u64)(0x800000u | (yb & 0x7fffffu)) << (39 + (int)(yb >> 23) - 126);  // y 2^63
+#pragma unroll
+  for (int it = 0; it < 3; ++it) {
+    const u64 Z = __umul64hi(Mf, __umul64hi(Y, Y));  // M y^2 2^60
+    Y = __umul64hi(Y, (3ull << 60) - Z) << 3;        // y (3 - M y^2) / 2 2^63
+  }
+  u64 q = __umul64hi(Mf, Y) >> 9;  // M y 2^52: the root, to a unit or two
+  long long r = (long long)((m << (52 + odd)) - q * q);  // N - q^2 (small: low words suffice)
+  if (r < 0) { q -= 1; r += (long long)(2 * q + 1); }
+  if (r < 0) { q -= 1; r += (long long)(2 * q + 1); }
+  if (r > (long long)(2 * q)) { r -= (long long)(2 * q + 1); q += 1; }
+  if (r > (long long)(2 * q)) { r -= (long long)(2 * q + 1); q += 1; }
+  q += (u64)(r > (long long)q);
+  const int Er = (E >> 1) + 1023;  // floor(E / 2), biased
+  return __longlong_as_double((long long)(((u64)(Er - 1) << 52) + q));
+}
+
 // PDL is on unless SCF_NO_PDL is set in the environment.
 bool pdl_enabled();
 
@@ -262,6 +306,7 @@ inline dim3 grid_for(int nx, int ny, int cells_per_thread_x = 2) {
 // ---- kernel launchers (scf_kernels.cu) ----
 void launch_assemble(const FortranIn& in, LevelView L0, Scalars* sc, cudaStream_t s);
 void launch_divide(const double* a, const double* b, double* q, long long n, cudaStream_t s);
+void launch_sqrt(const double* a, double* q, long long n, cudaStream_t s);
 void launch_matr_out(const FortranIn& in, LevelView L0, double* matr, cudaStream_t s);
 void launch_excess(LevelView L, double* di, unsigned* zero_bits, int nzero, Scalars* sc,
                    cudaStream_t s);

@@ -862,6 +862,13 @@ __global__ void k_divide(const double* a, const double* b, double* q, long long 
     q[k] = dvd(a[k], b[k]);
 }
 
+// the library's integer-pipe square root on an array (diagnostics)
+__global__ void k_sqrt(const double* a, double* q, long long n) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+       k += (long long)gridDim.x * blockDim.x)
+    q[k] = sqrt_rn(a[k]);
+}
+
 __global__ void k_to_fortran(LevelView L, const double* src, double* dst) {
   pdl_wait();
   const int ix = blockIdx.x * kBX + threadIdx.x;
@@ -906,6 +913,9 @@ void launch_matr_out(const FortranIn& in, LevelView L0, double* matr, cudaStream
 }
 void launch_divide(const double* a, const double* b, double* q, long long n, cudaStream_t s) {
   launch_k(k_divide, dim3(152 * 8), dim3(256), 0, s, a, b, q, n);
+}
+void launch_sqrt(const double* a, double* q, long long n, cudaStream_t s) {
+  launch_k(k_sqrt, dim3(152 * 8), dim3(256), 0, s, a, q, n);
 }
 void launch_excess(LevelView L, double* di, unsigned* zero_bits, int nzero, Scalars* sc,
                    cudaStream_t s) {

@@ -966,6 +966,33 @@ int scf_diag_divide(const double* a, const double* b, double* q, int64_t n, int 
   return rc;
 }
 
+int scf_diag_sqrt(const double* a, double* q, int64_t n, int device) {
+  if (n < 0 || (n > 0 && (!a || !q))) return SCF_ERR_ARG;
+  if (n == 0) return SCF_OK;
+  CK(cudaSetDevice(device));
+  double* d = nullptr;
+  const size_t bytes = (size_t)n * 8;
+  CK(cudaMalloc(&d, 2 * bytes));
+  int rc = SCF_OK;
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaFree(d);
+    return SCF_ERR_CUDA;
+  }
+  if (cudaMemcpyAsync(d, a, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) rc = SCF_ERR_CUDA;
+  if (rc == SCF_OK) {
+    launch_sqrt(d, d + n, (long long)n, s);
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(q, d + n, bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      rc = SCF_ERR_CUDA;
+  }
+  cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  cudaFree(d);
+  return rc;
+}
+
 const char* scf_strerror(int code) {
   switch (code) {
     case SCF_OK: return "ok";

@@ -25,6 +25,9 @@ profiler can restrict itself to that range (ncu --nvtx --nvtx-include
             workload's cells (seeded face fluxes), device-resident
   geometry  --reps GPU builds of the cut-cell geometry (scf_proj_set_solid)
             from the workload's solid level-set fields, device-resident
+  clsvof    --reps Coupled_LS_VOF steps (scf_clsvof_step: six sub-steps of
+            reconstruction, sweeps, updates and Redistance) on a drop beside a
+            solid wall, --n cells a side (default 2048), device-resident
 
     python -m simcoflow_gb300.profile_kernels --config c2 --kernel sweep --precision mixed
     python -m simcoflow_gb300.profile_kernels --config c3 --n 2048 --kernel projection
@@ -49,6 +52,7 @@ KERNELS = {"sweep": (0, {"fp64": 48, "mixed": 20}), "pupdate_spmv": (1, {"fp64":
            "projection": (None, {"fp64": 0, "mixed": 0}), "unet": (None, {"fp64": 0, "mixed": 0}),
            "momentum": (None, {"fp64": 0, "mixed": 0}), "geometry": (None, {"fp64": 0, "mixed": 0}),
            "cutcell": (None, {"fp64": 0, "mixed": 0}), "tecplot": (None, {"fp64": 0, "mixed": 0}),
+           "clsvof": (None, {"fp64": 0, "mixed": 0}),
            "line": (8, {"fp64": 0, "mixed": 11}), "fine_pre": (9, {"fp64": 40, "mixed": 17}),
            "fine_post": (10, {"fp64": 48, "mixed": 21})}
 
@@ -63,6 +67,26 @@ def main():
     args = ap.parse_args()
     import torch
     dev = torch.device("cuda", 0)
+    if args.kernel == "clsvof":
+        from . import clsvof as CL
+        n = args.n or 2048
+        f, vof, phi, dt, wave = synth.clsvof_step_fields(np.random.default_rng(33), n, n)
+        T = lambda x: torch.from_numpy(np.ascontiguousarray(x.ravel(order="F"))).to(dev)
+        tf = {k: T(v) for k, v in f.items()}
+        out = {k: torch.zeros(n * n, dtype=torch.float64, device=dev)
+               for k in ("nxv", "nyv", "dis")}
+        tv, tp = T(vof), T(phi)
+        CL.clsvof_step(n, n, tf, dt, tv, tp, wave=wave, out=out, device_ptrs=True)  # warm-up
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("kernels")
+        t0 = time.perf_counter()
+        for _ in range(args.reps):
+            CL.clsvof_step(n, n, tf, dt, tv, tp, wave=wave, out=out, device_ptrs=True)
+        torch.cuda.synchronize()
+        dt_ms = (time.perf_counter() - t0) / args.reps * 1e3
+        torch.cuda.nvtx.range_pop()
+        print(json.dumps({"kernel": "clsvof", "nx": n, "ny": n, "ms_step": dt_ms}))
+        return
     c = synth.make_case(args.config, **({"n": args.n} if args.n else {}))
     t = {k: torch.from_numpy(np.ascontiguousarray(v.ravel(order="F"))).to(dev)
          for k, v in c.arrays.items() if isinstance(v, np.ndarray)}

@@ -44,7 +44,7 @@ EXPORTS = ["scf_opts_default", "scf_proj_create", "scf_proj_destroy", "scf_proj_
            "scf_proj_vcycle", "scf_proj_time_kernel", "scf_rhs_norm_noalloc", "scf_strerror",
            "scf_proj_set_network", "scf_proj_solve_rhs", "scf_proj_set_opts",
            "scf_batch_create", "scf_batch_set_io", "scf_batch_run", "scf_batch_destroy",
-           "scf_proj_set_solid", "scf_proj_get_geometry", "scf_diag_divide",
+           "scf_proj_set_solid", "scf_proj_get_geometry", "scf_diag_divide", "scf_diag_sqrt",
            "scf_proj_get_matrix", "scf_diag_tma_timeout", "scf_proj_set_tile"]
 # every symbol declared in include/scf_unet.h
 UNET_EXPORTS = ["scf_unet_num_params", "scf_unet_create", "scf_unet_destroy",
@@ -123,6 +123,8 @@ def load():
         L.scf_proj_get_geometry.argtypes = [vp] + [dp] * 8 + [ip] * 5 + [dp, dp]
         L.scf_diag_divide.argtypes = [dp, dp, dp, C.c_int64, C.c_int]
         L.scf_diag_divide.restype = C.c_int
+        L.scf_diag_sqrt.argtypes = [dp, dp, C.c_int64, C.c_int]
+        L.scf_diag_sqrt.restype = C.c_int
         L.scf_diag_tma_timeout.argtypes = [C.c_int, C.c_int, C.c_int]
         L.scf_diag_tma_timeout.restype = C.c_int
         for name in EXPORTS:
@@ -398,6 +400,15 @@ def divide(a, b, device: int = 0):
     q = np.empty_like(a)
     _check(load().scf_diag_divide(a.ctypes.data, b.ctypes.data, q.ctypes.data, a.size, device),
            "scf_diag_divide")
+    return q
+
+
+def sqrt(a, device: int = 0):
+    """sqrt(a) elementwise by the library's FP64 square root (the one its
+    CLSVOF kernels use), on the GPU; numpy float64 arrays in and out."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    q = np.empty_like(a)
+    _check(load().scf_diag_sqrt(a.ctypes.data, q.ctypes.data, a.size, device), "scf_diag_sqrt")
     return q
 
 

@@ -90,3 +90,57 @@ def test_range_edges():
     check(x * 2.0**1000, rng.uniform(0.1, 1.0, n) * 2.0**-23)   # overflow side
     check(x * 2.0**-1000, rng.uniform(1.0, 9.0, n) * 2.0**22)   # gradual underflow side
     check(x * 2.0**-1021, rng.uniform(0.5, 2.0, n))             # around the smallest normal
+
+
+# ---------------------------------------------------------------------------
+# The library's square root (integer-pipe Newton-Raphson reciprocal square
+# root with a remainder-corrected last digit, used by the CLSVOF kernels)
+# against numpy's float64 square root (IEEE, rounded to nearest even),
+# through scf_diag_sqrt.
+# ---------------------------------------------------------------------------
+def check_sqrt(a):
+    q = P.sqrt(a)
+    with np.errstate(all="ignore"):
+        e = np.sqrt(a)
+    same = (bits(q) == bits(e)) | (np.isnan(q) & np.isnan(e))
+    if not same.all():
+        k = np.flatnonzero(~same)[:5]
+        raise AssertionError(f"{(~same).sum()} mismatches, e.g. "
+                             + ", ".join(f"sqrt({a[i].hex()}): {q[i].hex()} vs {e[i].hex()}"
+                                         for i in k))
+
+
+def test_sqrt_random_bit_patterns():
+    rng = np.random.default_rng(21)
+    check_sqrt(rng.integers(0, 2**64, 8_000_000, dtype=np.uint64).view(np.float64))
+
+
+def test_sqrt_every_exponent_and_dense_mantissas():
+    """All 2046 normal exponents (odd and even), significands near 1, 2 and
+    4 (the root's carry into the exponent) and random."""
+    rng = np.random.default_rng(22)
+    e = np.repeat(np.arange(1, 2047, dtype=np.uint64), 2000)
+    m = rng.integers(0, 2**52, e.size, dtype=np.uint64)
+    edge = rng.random(e.size) < 0.3
+    m = np.where(edge, rng.choice(np.array([0, 1, 2, 2**52 - 1, 2**52 - 2, 2**51, 2**51 - 1],
+                                           dtype=np.uint64), e.size), m)
+    check_sqrt(((e << np.uint64(52)) | m).view(np.float64))
+
+
+def test_sqrt_near_squares():
+    """x within a few ulps of q^2 for short and long q: roots on or next to
+    representable values, where the remainder decides the last bit."""
+    rng = np.random.default_rng(23)
+    n = 2_000_000
+    q = rng.uniform(1.0, 2.0, n) * np.exp2(rng.integers(-500, 500, n))
+    q2 = np.floor(rng.uniform(1, 2**26, n)) * np.exp2(rng.integers(-200, 200, n))
+    for r in (q, q2):
+        a = (r * r).view(np.uint64) + rng.integers(-3, 4, n).astype(np.int64).view(np.uint64)
+        check_sqrt(a.view(np.float64))
+
+
+def test_sqrt_special_operands():
+    big, tiny = np.finfo(np.float64).max, np.finfo(np.float64).tiny
+    check_sqrt(np.array([0.0, -0.0, 1.0, -1.0, np.inf, -np.inf, np.nan, big, tiny, tiny / 3,
+                         5e-324, 2.0, 4.0, 0.25, 3.0, 1.0 + 2**-52, 4.0 - 2**-50, 2.0 - 2**-52,
+                         -tiny, -5e-324]))
