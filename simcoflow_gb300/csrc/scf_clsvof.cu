@@ -871,10 +871,17 @@ __device__ double closer(double pa, double deuc, double vT, double sT) {
   return pa;
 }
 
-// One update of target T's running value pa from source S = (i, j), T at
-// offset (ii, jj) (:1551-1676).
-__device__ double rd_update(const RdIn& c, int i, int j, int ii, int jj, double pa, double vT,
-                            double sT, double phiT, double xT, double yT) {
+// The reference's work for target T from source S = (i, j), T at offset
+// (ii, jj) (:1551-1676): the distance candidate deuc and which of its three
+// update rules applies, handed to emit(rule, deuc, dij1):
+//   1  T outside the solid (vofS < epsi): pa = sign(0.5 - vof(T)) min(deuc, |pa|)
+//   2  T cut by the solid, or any T when the segment test passes: the two
+//      guarded assignments of closer()
+//   3  T inside the solid, from a source without solid: pa = sign(dij1) deuc
+//      when deuc < |pa|.
+template <typename Emit>
+__device__ void rd_pair(const RdIn& c, int i, int j, int ii, int jj, double vT, double sT,
+                        double phiT, double xT, double yT, Emit&& emit) {
   const double tol = 1e-24;
   const long long a = c.at(i, j);
   const double dxs = c.dx[a], dys = c.dy[a], nxs = c.nxs[a], nys = c.nys[a], phs = c.phiS[a];
@@ -913,25 +920,23 @@ __device__ double rd_update(const RdIn& c, int i, int j, int ii, int jj, double 
   const double rx = xT - c.x[a], ry = yT - c.y[a];
   const double dvl = n1 * xv + n2 * yv + d1;
   if (dvl * copysign(1.0, phiT) <= 0.0) {
-    const double deuc = sq((rx - xv) * (rx - xv) + (ry - yv) * (ry - yv));
-    if (sT < kEpsi) return copysign(1.0, 0.5 - vT) * fmin(deuc, fabs(pa));
-    return closer(pa, deuc, vT, sT);
+    emit(sT < kEpsi ? 1 : 2, sq((rx - xv) * (rx - xv) + (ry - yv) * (ry - yv)), 0.0);
+    return;
   }
   const double dij1 = n1 * rx + n2 * ry + d1;
   const double xp = rx - dij1 * n1, yp = ry - dij1 * n2;
   const bool in = inside_rect(xp, yp, dxs, dys);
   if (in && sT < kEpsi) {
-    const double deuc = sq((rx - xp) * (rx - xp) + (ry - yp) * (ry - yp));
-    return copysign(1.0, 0.5 - vT) * fmin(deuc, fabs(pa));
+    emit(1, sq((rx - xp) * (rx - xp) + (ry - yp) * (ry - yp)), 0.0);
+    return;
   }
-  if (in && sT >= kEpsi && sT < 1.0 - kEpsi)
-    return closer(pa, sq((rx - xp) * (rx - xp) + (ry - yp) * (ry - yp)), vT, sT);
+  if (in && sT >= kEpsi && sT < 1.0 - kEpsi) {
+    emit(2, sq((rx - xp) * (rx - xp) + (ry - yp) * (ry - yp)), 0.0);
+    return;
+  }
   if (sT >= 1.0 - kEpsi) {
-    if (c.vofS[a] < kEpsi) {
-      const double deuc = sq((rx - xp) * (rx - xp) + (ry - yp) * (ry - yp));
-      if (fabs(deuc) < fabs(pa)) pa = copysign(1.0, dij1) * deuc;
-    }
-    return pa;
+    if (c.vofS[a] < kEpsi) emit(3, sq((rx - xp) * (rx - xp) + (ry - yp) * (ry - yp)), dij1);
+    return;
   }
   const double xoff = fmax(fabs(xp) - 0.5 * dxs, 0.0), yoff = fmax(fabs(yp) - 0.5 * dys, 0.0);
   const double xfc = copysign(1.0, xp) * 0.5 * dxs, yfc = copysign(1.0, yp) * 0.5 * dys;
@@ -944,18 +949,67 @@ __device__ double rd_update(const RdIn& c, int i, int j, int ii, int jj, double 
     xs = dv(d1 + n2 * ys, -n1 + tol);
   }
   const double deuc = sq((rx - xs) * (rx - xs) + (ry - ys) * (ry - ys));
-  if (solid(xs, ys) >= 0.0) {
-    if (sT < kEpsi) return copysign(1.0, 0.5 - vT) * fmin(deuc, fabs(pa));
-    return closer(pa, deuc, vT, sT);
+  if (solid(xs, ys) >= 0.0) emit(sT < kEpsi ? 1 : 2, deuc, 0.0);
+}
+
+// T is a target (full or empty), S a source (interface cell): disjoint sets.
+__device__ bool rd_target(double vT, double sT) {
+  return vT < 0.0 + kVofEps || vT >= 1.0 - kVofEps - sT;
+}
+
+// Rules 1 and 2 reduce to a minimum of deuc with a sign fixed by T, so a
+// target's result does not depend on the order of its sources; rule 3 takes
+// the sign of the first source (in the reference's order) reaching the
+// minimum, and targets inside the solid (the only ones it applies to) keep
+// the sequential order.  The pair pass: one thread per (source, offset)
+// pair, the minimum by an atomic on the distance's bits (non-negative
+// doubles order like their bit patterns).  key = ~0: no candidate.
+// flags bit 0: a source within the band; bit 1: a rule-1 update ran.
+__global__ void k_rd_sources(RdIn c, int* list, int* count) {
+  const long long total = (long long)c.nx * c.ny;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(idx % c.nx) + 1, j = (int)(idx / c.nx) + 1;
+    if (c.source(i, j)) list[atomicAdd(count, 1)] = (int)idx;
   }
-  return pa;
+}
+
+__global__ void k_rd_pairs(RdIn c, const int* list, const int* count, unsigned long long* key,
+                           unsigned* flags) {
+  const long long work = (long long)(*count) * 81;
+  for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < work;
+       w += (long long)gridDim.x * blockDim.x) {
+    const int sidx = list[w / 81], o = (int)(w % 81);
+    const int i = sidx % c.nx + 1, j = sidx / c.nx + 1;
+    const int ii = o / 9 - kBand, jj = o % 9 - kBand;
+    const int p = i + ii, q = j + jj;
+    if (p < 1 || p > c.nx || q < 1 || q > c.ny) continue;
+    const long long t = c.at(p, q);
+    const double vT = c.vof[t], sT = c.vofS[t];
+    if (!rd_target(vT, sT)) continue;
+    atomicOr(&flags[t], 1u);
+    if (sT >= 1.0 - kEpsi) continue;  // inside the solid: the sequential path
+    rd_pair(c, i, j, ii, jj, vT, sT, c.phi[t], c.x[t], c.y[t],
+            [&](int rule, double deuc, double) {
+              if (rule == 1) {
+                atomicOr(&flags[t], 2u);
+                if (deuc == deuc)
+                  atomicMin(&key[t], (unsigned long long)__double_as_longlong(deuc));
+              } else if (deuc < 1e4) {  // rule 2: an update needs deuc < |pa| <= 1e4
+                atomicMin(&key[t], (unsigned long long)__double_as_longlong(deuc));
+              }
+            });
+  }
 }
 
 constexpr int kRdTx = 32, kRdTy = 8;
 
-// One thread per cell (i fastest within a 32 x 8 tile); the source flags of
-// the tile and its 4-cell halo are staged in shared memory.
-__global__ void __launch_bounds__(kRdTx* kRdTy) k_redistance(RdIn c) {
+// One thread per cell (i fastest within a 32 x 8 tile).  Sources take their
+// PLIC distance; targets outside the solid read the pair pass's minimum;
+// targets inside the solid run their sources in the reference's order (the
+// source flags of the tile and its 4-cell halo staged in shared memory).
+__global__ void __launch_bounds__(kRdTx* kRdTy)
+    k_redistance(RdIn c, const unsigned long long* key, const unsigned* flags) {
   __shared__ unsigned char src[kRdTy + 2 * kBand][kRdTx + 2 * kBand];
   const int i0 = blockIdx.x * kRdTx, j0 = blockIdx.y * kRdTy;
   const int tid = threadIdx.y * kRdTx + threadIdx.x;
@@ -976,15 +1030,29 @@ __global__ void __launch_bounds__(kRdTx* kRdTy) k_redistance(RdIn c) {
   if (src[threadIdx.y + kBand][threadIdx.x + kBand]) {
     pa = c.dis[t];
     fix = true;
-  } else if (vT < 0.0 + kVofEps || vT >= 1.0 - kVofEps - sT) {
-    const double phiT = out, xT = c.x[t], yT = c.y[t];
-    for (int di = -kBand; di <= kBand; ++di)  // sources in the reference's order
-      for (int dj = -kBand; dj <= kBand; ++dj) {
-        if (!src[threadIdx.y + kBand + dj][threadIdx.x + kBand + di]) continue;
-        fix = true;
-        pa = rd_update(c, p + di, q + dj, -di, -dj, pa, vT, sT, phiT, xT, yT);
-        if (pa > 9.999e3) fix = false;
+  } else if (rd_target(vT, sT) && (flags[t] & 1u)) {
+    if (sT >= 1.0 - kEpsi) {
+      const double phiT = out, xT = c.x[t], yT = c.y[t];
+      for (int di = -kBand; di <= kBand; ++di)  // sources in the reference's order
+        for (int dj = -kBand; dj <= kBand; ++dj) {
+          if (!src[threadIdx.y + kBand + dj][threadIdx.x + kBand + di]) continue;
+          rd_pair(c, p + di, q + dj, -di, -dj, vT, sT, phiT, xT, yT,
+                  [&](int rule, double deuc, double dij1) {
+                    if (rule == 1) pa = copysign(1.0, 0.5 - vT) * fmin(deuc, fabs(pa));
+                    else if (rule == 2) pa = closer(pa, deuc, vT, sT);
+                    else if (fabs(deuc) < fabs(pa)) pa = copysign(1.0, dij1) * deuc;
+                  });
+        }
+    } else {
+      const unsigned long long k = key[t];
+      const double mn = k == ~0ull ? 1e4 : __longlong_as_double((long long)k);
+      if (sT < kEpsi) {  // rule 1
+        if (flags[t] & 2u) pa = copysign(1.0, 0.5 - vT) * fmin(mn, 1e4);
+      } else if (k != ~0ull) {  // rule 2: the smallest deuc below 1e4, signed by T
+        pa = vT >= 1.0 - kVofEps - sT ? -mn : mn;
       }
+    }
+    fix = !(pa > 9.999e3);
   }
   if (fix) {
     if (pa > 1e3) atomicAdd(c.events, 1);  // the reference pauses here
@@ -1317,6 +1385,32 @@ extern "C" int scf_interface_reconstruct(int nx, int ny, const scf_ir_fields* f,
   return rc;
 }
 
+namespace {
+
+// Redistance's scratch: the per-cell minimum key (8 B), flags (4 B) and
+// source list (4 B), and the source count.
+size_t rd_scratch_bytes(size_t n1) { return 16 + n1 * 16; }
+
+cudaError_t launch_redistance(const RdIn& in, void* scratch, size_t n1, cudaStream_t s) {
+  char* b = static_cast<char*>(scratch);
+  int* count = reinterpret_cast<int*>(b);
+  unsigned long long* key = reinterpret_cast<unsigned long long*>(b + 16);
+  unsigned* flags = reinterpret_cast<unsigned*>(b + 16 + n1 * 8);
+  int* list = reinterpret_cast<int*>(b + 16 + n1 * 12);
+  cudaError_t e = cudaMemsetAsync(count, 0, 16, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(key, 0xff, n1 * 8, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(flags, 0, n1 * 4, s);
+  if (e != cudaSuccess) return e;
+  k_rd_sources<<<grid_for(n1), 256, 0, s>>>(in, list, count);
+  k_rd_pairs<<<152 * 8, 256, 0, s>>>(in, list, count, key, flags);
+  const dim3 grid((unsigned)((in.nx + kRdTx - 1) / kRdTx), (unsigned)((in.ny + kRdTy - 1) / kRdTy));
+  k_redistance<<<grid, dim3(kRdTx, kRdTy), 0, s>>>(in, key, flags);
+  for (int q = 0; q < 3; ++q) note_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace
+
 extern "C" int scf_redistance(int nx, int ny, const scf_rd_fields* f, double* phi, int* events,
                               int flags, int device, double* ms) {
   if (nx < 1 || ny < 1 || !f || !phi) return SCF_ERR_ARG;
@@ -1333,7 +1427,7 @@ extern "C" int scf_redistance(int nx, int ny, const scf_rd_fields* f, double* ph
   if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return SCF_ERR_CUDA;
   void* mem = nullptr;
   int rc = SCF_OK, h_events = 0;
-  const size_t bytes = 16 + (dev ? 0 : 13 * n1 * 8);
+  const size_t bytes = 16 + rd_scratch_bytes(n1) + (dev ? 0 : 13 * n1 * 8);
   do {
     if (cudaMalloc(&mem, bytes) != cudaSuccess) {
       rc = SCF_ERR_NOMEM;
@@ -1344,10 +1438,11 @@ extern "C" int scf_redistance(int nx, int ny, const scf_rd_fields* f, double* ph
       rc = SCF_ERR_CUDA;
       break;
     }
+    void* rd_scratch = static_cast<char*>(mem) + 16;
     const double* d[12];
     double* dphi = phi;
     if (!dev) {
-      double* p = reinterpret_cast<double*>(static_cast<char*>(mem) + 16);
+      double* p = reinterpret_cast<double*>(static_cast<char*>(mem) + 16 + rd_scratch_bytes(n1));
       for (int a = 0; a < 12 && rc == SCF_OK; ++a) {
         if (cudaMemcpyAsync(p, arr[a], n1 * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
           rc = SCF_ERR_CUDA;
@@ -1364,9 +1459,10 @@ extern "C" int scf_redistance(int nx, int ny, const scf_rd_fields* f, double* ph
     }
     const RdIn in{nx,   ny,   d[0], d[1], d[2],  d[3],  d[4], d[5],
                   d[6], d[7], d[8], d[9], d[10], d[11], dphi, d_events};
-    const dim3 grid((unsigned)((nx + kRdTx - 1) / kRdTx), (unsigned)((ny + kRdTy - 1) / kRdTy));
-    k_redistance<<<grid, dim3(kRdTx, kRdTy), 0, s>>>(in);
-    note_launch();
+    if (launch_redistance(in, rd_scratch, n1, s) != cudaSuccess) {
+      rc = SCF_ERR_CUDA;
+      break;
+    }
     if (cudaGetLastError() != cudaSuccess) {
       rc = SCF_ERR_CUDA;
       break;
@@ -1427,7 +1523,8 @@ extern "C" int scf_clsvof_step(int nx, int ny, const scf_clsvof_fields* f,
   const size_t flags_b = ((n1 + 15) / 16) * 16;
   size_t in_n = 0;
   for (size_t c : cnt) in_n += c;
-  const size_t bytes = 16 + flags_b + 4 * n1 * 8 + (dev ? 0 : (in_n + 5 * n1) * 8);
+  const size_t bytes =
+      16 + flags_b + rd_scratch_bytes(n1) + 4 * n1 * 8 + (dev ? 0 : (in_n + 5 * n1) * 8);
   do {
     if (cudaMalloc(&mem, bytes) != cudaSuccess) {
       rc = SCF_ERR_NOMEM;
@@ -1436,7 +1533,8 @@ extern "C" int scf_clsvof_step(int nx, int ny, const scf_clsvof_fields* f,
     char* base = static_cast<char*>(mem);
     int* d_events = reinterpret_cast<int*>(base);
     unsigned char* failed = reinterpret_cast<unsigned char*>(base + 16);
-    double* w = reinterpret_cast<double*>(base + 16 + flags_b);
+    void* rd_scratch = base + 16 + flags_b;
+    double* w = reinterpret_cast<double*>(base + 16 + flags_b + rd_scratch_bytes(n1));
     double *tvx = w, *tvy = w + n1, *tlx = w + 2 * n1, *tly = w + 3 * n1;
     double* p = w + 4 * n1;
     const double* d[14];
@@ -1535,9 +1633,10 @@ extern "C" int scf_clsvof_step(int nx, int ny, const scf_clsvof_fields* f,
       launch_reconstruct(irc, n1, s);
       const RdIn rd{nx,   ny,   dvof,   d[0], d[1],  d[2],  d[3],  d[4],
                     d[5], d[6], d[7], io[2], io[3], io[4], dp,    d_events};
-      const dim3 grd((unsigned)((nx + kRdTx - 1) / kRdTx), (unsigned)((ny + kRdTy - 1) / kRdTy));
-      k_redistance<<<grd, dim3(kRdTx, kRdTy), 0, s>>>(rd);
-      note_launch();
+      if (launch_redistance(rd, rd_scratch, n1, s) != cudaSuccess) {
+        rc = SCF_ERR_CUDA;
+        break;
+      }
     }
     if (rc) break;
     if (cudaGetLastError() != cudaSuccess) {
