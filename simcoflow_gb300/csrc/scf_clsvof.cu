@@ -435,6 +435,7 @@ struct IrIn {
   double *nxv, *nyv, *dis;
   unsigned char* failed;
   int* events;
+  int *list, *count;  // the interface cells of pass 1 (scratch)
   __device__ long long at(int i, int j) const { return (long long)(i - 1) + (long long)(j - 1) * nx; }
   __device__ double P(int i, int j) const { return phi[at(i, j)]; }
   __device__ double S(int i, int j) const { return vofS[at(i, j)]; }
@@ -754,14 +755,33 @@ __device__ void ir_cell(const IrIn& c, int i, int j, double nxx, double nyy) {
 }
 
 // Pass 1: every cell whose body reads no carried normal component.
+// Unflagged cells take (0, 1) and the flat-interface distance here; the
+// flagged cells of pass 1 go to a list for k_ir_flagged, so that this
+// pass over every cell stays light (few registers, full occupancy).
 __global__ void k_ir_main(IrIn c) {
   const long long total = (long long)c.nx * c.ny;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
        idx += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(idx % c.nx) + 1, j = (int)(idx / c.nx) + 1;
-    const bool edge_i = i == 1 || i == c.nx, edge_j = j == 1 || j == c.ny;
-    if (edge_i != edge_j && c.flag(i, j)) continue;  // carried value: later passes
-    ir_cell(c, i, j, 0.0, 0.0);
+    if (c.flag(i, j)) {
+      const bool edge_i = i == 1 || i == c.nx, edge_j = j == 1 || j == c.ny;
+      if (edge_i == edge_j) c.list[atomicAdd(c.count, 1)] = (int)idx;  // else: a later pass
+      continue;
+    }
+    const double v = c.vof[idx], s = c.vofS[idx];
+    c.nxv[idx] = 0.0;
+    c.nyv[idx] = 1.0;
+    c.dis[idx] = 1.0 - s > kVofEps ? (0.5 - dv(v, 1.0 - s)) * c.dy[idx] : (0.0 - v) * c.dy[idx];
+    c.failed[idx] = 0;
+  }
+}
+
+// Pass 1's interface cells (interior cells and corners).
+__global__ void k_ir_flagged(IrIn c) {
+  const int n = *c.count;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int idx = c.list[k];
+    ir_cell(c, idx % c.nx + 1, idx / c.nx + 1, 0.0, 0.0);
   }
 }
 
@@ -1316,7 +1336,10 @@ extern "C" int scf_interface_reconstruct(int nx, int ny, const scf_ir_fields* f,
   int rc = SCF_OK;
   // scratch: the event counter (16 B), the failed flags (n1 B); host mode
   // adds the 10 inputs and 3 outputs
-  const size_t scratch = 16 + ((n1 + 15) / 16) * 16;
+  // scratch: the event counter and the list count (16 B), the failed flags
+  // (n1 B), the list (n1 ints); host mode adds the 10 inputs and 3 outputs
+  const size_t flags_b = ((n1 + 15) / 16) * 16;
+  const size_t scratch = 16 + flags_b + ((n1 * 4 + 15) / 16) * 16;
   const size_t bytes = scratch + (dev ? 0 : 13 * n1 * 8);
   int h_events = 0;
   do {
@@ -1327,6 +1350,7 @@ extern "C" int scf_interface_reconstruct(int nx, int ny, const scf_ir_fields* f,
     char* base = static_cast<char*>(mem);
     int* d_events = reinterpret_cast<int*>(base);
     unsigned char* failed = reinterpret_cast<unsigned char*>(base + 16);
+    int* list = reinterpret_cast<int*>(base + 16 + flags_b);
     const double* d[10];
     double* o[3] = {nxv, nyv, dis};
     if (cudaMemsetAsync(d_events, 0, 16, s) != cudaSuccess) {
@@ -1350,9 +1374,11 @@ extern "C" int scf_interface_reconstruct(int nx, int ny, const scf_ir_fields* f,
       for (int a = 0; a < 10; ++a) d[a] = arr[a];
     }
     const IrIn in{nx,   ny,   d[0], d[1], d[2], d[3], d[4], d[5], d[6],   d[7],
-                  d[8], d[9], o[0], o[1], o[2], failed, d_events};
+                  d[8], d[9], o[0], o[1], o[2], failed, d_events, list, d_events + 2};
     const unsigned g = grid_for(n1);
     k_ir_main<<<g, 256, 0, s>>>(in);
+    k_ir_flagged<<<152 * 2, 128, 0, s>>>(in);
+    note_launch();
     note_launch();
     const unsigned gr = (unsigned)((nx + 127) / 128), gs = (unsigned)((2 * ny + 127) / 128);
     k_ir_row<0><<<gr, 128, 0, s>>>(in);
@@ -1488,12 +1514,14 @@ namespace {
 void launch_reconstruct(const IrIn& in, size_t n1, cudaStream_t s) {
   const unsigned g = grid_for(n1);
   const unsigned gr = (unsigned)((in.nx + 127) / 128), gs = (unsigned)((2 * in.ny + 127) / 128);
+  cudaMemsetAsync(in.count, 0, sizeof(int), s);
   k_ir_main<<<g, 256, 0, s>>>(in);
+  k_ir_flagged<<<152 * 2, 128, 0, s>>>(in);
   k_ir_row<0><<<gr, 128, 0, s>>>(in);
   k_ir_row<1><<<gr, 128, 0, s>>>(in);
   k_ir_sides<<<gs, 128, 0, s>>>(in);
   k_ir_carry_dis<<<g, 256, 0, s>>>(in);
-  for (int q = 0; q < 5; ++q) note_launch();
+  for (int q = 0; q < 6; ++q) note_launch();
 }
 
 }  // namespace
@@ -1578,8 +1606,10 @@ extern "C" int scf_clsvof_step(int nx, int ny, const scf_clsvof_fields* f,
     }
     const int nv = 6;
     const double dtv = dt / (double)nv;
-    const IrIn irc{nx,   ny,   dvof,   d[0],  dp,    d[1],  d[2],   d[3],    d[4],
-                   d[5], d[6], d[7], io[2], io[3], io[4], failed, d_events};
+    // the reconstruction's list shares Redistance's source list (never in use together)
+    int* ir_list = reinterpret_cast<int*>(static_cast<char*>(rd_scratch) + 16 + n1 * 12);
+    const IrIn irc{nx,   ny,   dvof,  d[0],  dp,    d[1],   d[2],     d[3],    d[4],        d[5],
+                   d[6], d[7], io[2], io[3], io[4], failed, d_events, ir_list, d_events + 2};
     const LsIn lin{nx,   ny,   dtv,  dp,   d[0],  d[6],  d[7],  d[4],
                    d[5], d[8], d[9], d[10], d[11], d[12], d[13]};
     const StepIn st{nx, ny, dtv, d[0], d[6], d[7], d[8], d[9], d[10], d[11], d[12], d[13]};
