@@ -7,7 +7,9 @@
  * the multigrid V-cycle as the fallback (scf_proj_set_network in scf_proj.h).
  *
  * Network (about 0.26 M parameters), NHWC BF16 activations, FP32
- * accumulation on the tensor cores (mma.sync m16n8k16 BF16):
+ * accumulation on the tensor cores: the forward convolutions and the input
+ * gradients on tcgen05.mma with the accumulators in tensor memory, the
+ * weight gradients on mma.sync m16n8k16:
  *   level 0 (H x W, 16 ch):  e0a = relu(conv(in)),  e0 = relu(conv(e0a))
  *   level 1 (H/2, 32 ch):    e1a = relu(conv(pool(e0))), e1 = relu(conv(e1a))
  *   level 2 (H/4, 64 ch):    e2a = relu(conv(pool(e1))), e2 = relu(conv(e2a))
@@ -65,8 +67,27 @@ int scf_unet_target(scf_unet *u, int i, int nx, int ny, const double *e, const d
 /* Raw input (host, n*h*w*5 floats, NHWC with 5 channels), for tests. */
 int scf_unet_set_input(scf_unet *u, const float *x);
 
-/* Forward pass; z: n*h*w floats (device pointer when device != 0). */
+/* Convolution engine of the forward pass and the input gradients:
+ * 1 = tcgen05 (default), 0 = the mma.sync kernels (comparison only). */
+int scf_unet_set_engine(scf_unet *u, int engine);
+
+/* Forward pass; z: n*h*w floats (device pointer when device != 0).
+ * Returns -3 if a tcgen05 convolution's bounded wait ran out. */
 int scf_unet_forward(scf_unet *u, float *z, int device);
+
+/* One 3x3 convolution of the network on device arrays, for tests and
+ * measurements: NHWC BF16 in [n][H][W][cin] (half resolution with ups),
+ * wt BF16 [cout][9][cin], bias FP32 [cout], out BF16 [n][H][W][cout].
+ * Variants as the network uses them: forward with ReLU (ups = bwd = mask =
+ * 0), forward with nearest upsampling of `in` and the skip tensor `add`
+ * [n][H][W][cout] added (ups = 1, no ReLU), input gradient (bwd = 1, bias
+ * and add null) with `in` masked by maskp > 0 (mask = 1) or not.  Engine as
+ * scf_unet_set_engine; stream: a cudaStream_t or null.  Returns 0, -1 for
+ * arguments outside these variants, -2 for a CUDA error, -3 for a bounded
+ * wait that ran out. */
+int scf_unet_conv(int engine, int cin, int cout, int ups, int bwd, int mask, const void *in,
+                  const void *maskp, const void *wt, const float *bias, const void *add,
+                  void *out, int n, int H, int W, void *stream);
 
 /* Loss of the last forward pass against the target t (device, n*h*w
  * floats) on the cells where mask (device, n*h*w bytes) is nonzero:

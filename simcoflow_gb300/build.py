@@ -20,7 +20,8 @@ LIB = PKG / "_lib"
 INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["scf_kernels.cu", "scf_mg.cu", "scf_line.cu", "scf_unet.cu", "scf_proj.cu",
+CUDA_SOURCES = ["scf_kernels.cu", "scf_mg.cu", "scf_line.cu", "scf_unet.cu", "scf_unet_tc.cu",
+                "scf_proj.cu",
                 "scf_noalloc.cu", "scf_mom.cu", "scf_geom.cu", "scf_out.cu", "scf_cutcell.cu",
                 "scf_clsvof.cu"]
 # per-file flags: the cut-cell geometry and the level-set sweeps restate the

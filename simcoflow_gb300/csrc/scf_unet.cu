@@ -79,15 +79,7 @@ __device__ __forceinline__ uint4 mask8(uint4 v, uint4 m) {
   return v;
 }
 
-struct ConvP {
-  const bf16* in;     // [n][Hi][Wi][CIN]; Hi = H/2, Wi = W/2 with UPS
-  const bf16* mask;   // MASK: [n][H][W][CIN]; input used where mask > 0
-  const bf16* wt;     // [COUT][9][CIN]
-  const float* bias;  // [COUT] or null
-  const bf16* add;    // ADD: [n][H][W][COUT]
-  bf16* out;          // [n][H][W][COUT]
-  int n, H, W;
-};
+using ConvP = ConvArgs;
 
 template <int CIN, int COUT>
 constexpr int conv_smem() {
@@ -658,8 +650,8 @@ void conv_bwd(const ConvP& p, bool mask, int sms, cudaStream_t s) {
   if constexpr (up_pair<COUT, CIN>()) conv_t<CIN, COUT, false, false, false, false>(p, sms, s);
 }
 
-void conv_dispatch(int cin, int cout, const ConvP& p, bool ups, bool bwd, bool mask, int sms,
-                   cudaStream_t s) {
+void conv_mma(int cin, int cout, const ConvP& p, bool ups, bool bwd, bool mask, int sms,
+              cudaStream_t s) {
 #define SCF_CONV(CI, CO)                           \
   if (cin == CI && cout == CO) {                   \
     if (bwd) conv_bwd<CI, CO>(p, mask, sms, s);    \
@@ -670,6 +662,18 @@ void conv_dispatch(int cin, int cout, const ConvP& p, bool ups, bool bwd, bool m
   SCF_CONV(64, 32) SCF_CONV(64, 64)
 #undef SCF_CONV
 }
+
+}  // namespace
+
+// a layer's convolution on the selected engine (tcgen05 unless a test or a
+// measurement asks for the mma.sync kernel)
+void conv_dispatch(int engine, int cin, int cout, const ConvP& p, bool ups, bool bwd, bool mask,
+                   int sms, int* err, cudaStream_t s) {
+  if (engine == 1) conv_tc(cin, cout, p, ups, bwd, mask, sms, err, s);
+  else conv_mma(cin, cout, p, ups, bwd, mask, sms, s);
+}
+
+namespace {
 
 template <int CIN, int COUT, bool UPS, bool RELU>
 void wgrad_t(const WgP& p, int sms, cudaStream_t s) {
@@ -731,7 +735,7 @@ int UNet::create(int n, int h, int w, bool train, int device) {
   const size_t p0 = (size_t)n * h * w;
   auto px = [&](int level) { return p0 >> (2 * level); };
   if (alloc((void**)&in_, p0 * 16 * 2) || alloc((void**)&z_, p0 * 4) ||
-      alloc((void**)&red_, 4096 * 4))
+      alloc((void**)&red_, 4096 * 4) || alloc((void**)&tc_err_, 4))
     return -1;
   act_.assign(L.size(), nullptr);
   for (size_t i = 0; i < L.size(); ++i)
@@ -758,6 +762,7 @@ void UNet::destroy() {
   allocs_.clear();
   act_.clear(); pool_.clear(); g_.clear();
   params_ = grads_ = m_ = v_ = z_ = dz_ = red_ = nullptr;
+  tc_err_ = nullptr;
   wb_ = wt_ = in_ = nullptr;
 }
 
@@ -824,7 +829,7 @@ void UNet::forward(cudaStream_t s) {
     size_t off = 0;
     for (size_t j = 0; j < i; ++j) off += (size_t)L[j].cout * 9 * L[j].cin;
     p.wt = wb_ + off;
-    conv_dispatch(l.cin, l.cout, p, l.ups, false, false, sms_, s);
+    conv_dispatch(engine_, l.cin, l.cout, p, l.ups, false, false, sms_, tc_err_, s);
   }
   k_head<<<grid_for((size_t)n_ * h_ * w_, sms_), 256, 0, s>>>(
       act_.back(), params_ + num_params() - 17, (size_t)n_ * h_ * w_, z_);
@@ -942,7 +947,7 @@ void UNet::backward(cudaStream_t s) {
     p.bias = nullptr;
     p.out = g_[b];
     p.n = n_; p.H = H; p.W = W;
-    conv_dispatch(l.cout, l.cin, p, false, true, l.relu, sms_, s);
+    conv_dispatch(engine_, l.cout, l.cin, p, false, true, l.relu, sms_, tc_err_, s);
     int cur = b;
     if (l.ups) {  // gradient of nearest upsampling: 2x2 sums onto the coarse input
       const int c = other(a, b);
@@ -1063,6 +1068,27 @@ int scf_unet_set_input(scf_unet* u, const float* x) {
              : -2;
 }
 
+// -3 when a tcgen05 convolution's bounded wait ran out since the last check
+// (the flag is cleared); -2 for a CUDA error
+static int tc_status(scf_unet* u) {
+  int e = 0;
+  if (cudaMemcpyAsync(&e, u->net.tc_err_, 4, cudaMemcpyDeviceToHost, u->stream) != cudaSuccess ||
+      cudaStreamSynchronize(u->stream) != cudaSuccess)
+    return -2;
+  if (e) {
+    cudaMemsetAsync(u->net.tc_err_, 0, 4, u->stream);
+    cudaStreamSynchronize(u->stream);
+    return -3;
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+int scf_unet_set_engine(scf_unet* u, int engine) {
+  if (!u || (engine != 0 && engine != 1)) return -1;
+  u->net.engine_ = engine;
+  return 0;
+}
+
 int scf_unet_forward(scf_unet* u, float* z, int device) {
   if (!u) return -1;
   cudaSetDevice(u->device);
@@ -1075,7 +1101,40 @@ int scf_unet_forward(scf_unet* u, float* z, int device) {
       return -2;
   }
   if (cudaStreamSynchronize(u->stream) != cudaSuccess) return -2;
-  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+  return tc_status(u);
+}
+
+int scf_unet_conv(int engine, int cin, int cout, int ups, int bwd, int mask, const void* in,
+                  const void* maskp, const void* wt, const float* bias, const void* add,
+                  void* out, int n, int H, int W, void* stream) {
+  if ((engine != 0 && engine != 1) || n < 1 || H < 1 || W < 1 || !in || !wt || !out ||
+      (ups && (bwd || H % 2 || W % 2 || !add)) || (mask && (!bwd || !maskp)) ||
+      (!bwd && !ups && !bias))
+    return -1;
+  scf::ConvArgs a{};
+  a.in = (const __nv_bfloat16*)in;
+  a.mask = (const __nv_bfloat16*)maskp;
+  a.wt = (const __nv_bfloat16*)wt;
+  a.bias = bias;
+  a.add = (const __nv_bfloat16*)add;
+  a.out = (__nv_bfloat16*)out;
+  a.n = n; a.H = H; a.W = W;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaStream_t s = (cudaStream_t)stream;
+  int* err = nullptr;
+  if (cudaMalloc((void**)&err, 4) != cudaSuccess) return -2;
+  cudaMemsetAsync(err, 0, 4, s);
+  scf::conv_dispatch(engine, cin, cout, a, ups != 0, bwd != 0, mask != 0, sms, err, s);
+  int e = 0;
+  int rc = (cudaMemcpyAsync(&e, err, 4, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+            cudaStreamSynchronize(s) == cudaSuccess && cudaGetLastError() == cudaSuccess)
+               ? 0
+               : -2;
+  cudaFree(err);
+  if (rc == 0 && e) rc = -3;
+  return rc;
 }
 
 int scf_unet_loss(scf_unet* u, const float* t, const unsigned char* mask, float* loss_out) {
@@ -1101,7 +1160,7 @@ int scf_unet_backward(scf_unet* u) {
   cudaSetDevice(u->device);
   u->net.backward(u->stream);
   if (cudaStreamSynchronize(u->stream) != cudaSuccess) return -2;
-  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+  return tc_status(u);
 }
 
 int scf_unet_get_grads(scf_unet* u, float* g) {

@@ -9,6 +9,26 @@
 
 namespace scf {
 
+// One 3x3 convolution (zero padding, bias) of NHWC BF16 tensors.
+struct ConvArgs {
+  const __nv_bfloat16* in;    // [n][Hi][Wi][CIN]; Hi = H/2, Wi = W/2 when upsampling
+  const __nv_bfloat16* mask;  // backward of a ReLU layer: [n][H][W][CIN], input used where > 0
+  const __nv_bfloat16* wt;    // [COUT][9][CIN]
+  const float* bias;          // [COUT] or null
+  const __nv_bfloat16* add;   // skip tensor [n][H][W][COUT] added to the output, or null
+  __nv_bfloat16* out;         // [n][H][W][COUT]
+  int n, H, W;
+};
+
+// The convolution on the tcgen05 tensor cores (scf_unet_tc.cu).  Forward
+// (bwd = false): ups -> nearest-upsampled input plus skip add, else ReLU
+// output.  Input gradient (bwd = true, cin/cout the layer's cout/cin): mask ->
+// input masked by the ReLU output.  *err (device int) is set when a bounded
+// wait runs out.  Returns 0, or -1 for a channel pair or variant that the
+// network does not have or a failed launch.
+int conv_tc(int cin, int cout, const ConvArgs& a, bool ups, bool bwd, bool mask, int sms,
+            int* err, cudaStream_t s);
+
 struct UNetLayer {
   int cin, cout;  // channels in / out
   int level;      // resolution level of the output (0 = full)
@@ -50,6 +70,11 @@ class UNet {
 
   int n_ = 0, h_ = 0, w_ = 0;
   bool train_ = false;
+  // convolution engine: 1 = tcgen05 (TMEM accumulators), 0 = mma.sync (kept
+  // as the comparison for tests and measurements); weight gradients use
+  // mma.sync either way
+  int engine_ = 1;
+  int* tc_err_ = nullptr;  // device flag: a tcgen05 convolution's bounded wait ran out
   int sms_ = 152;
   float *params_ = nullptr, *grads_ = nullptr, *m_ = nullptr, *v_ = nullptr;
   __nv_bfloat16 *wb_ = nullptr, *wt_ = nullptr;  // BF16 weights and flipped transposes

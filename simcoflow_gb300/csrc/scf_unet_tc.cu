@@ -1,0 +1,426 @@
+// scf_unet_tc.cu -- 3x3 convolutions of the learned preconditioner on the
+// fifth-generation tensor cores (tcgen05.mma, accumulators in tensor memory).
+//
+// Implicit GEMM per tile: D[128 pixels][COUT] = sum over the 9 taps of
+// A_tap[128 pixels][CIN] x B_tap[CIN][COUT], BF16 operands from shared
+// memory, FP32 accumulation in TMEM (128 lanes = pixels, COUT columns).
+//
+// Tiles are 128 consecutive pixels of one image row.  A CTA owns a strip of
+// rows of one 128-pixel column segment and walks down it, so each tile stages
+// only ONE new input row: a ring of four staged rows holds the rows y-1, y,
+// y+1 of the current tile and the row y+2 that is loaded while the tensor
+// core works on the current tile.  A staged row keeps the 130 pixels
+// x0-1 .. x0+128 in the no-swizzle K-major canonical layout (8-pixel x 16-byte
+// core matrices, pixels 16 bytes apart inside a channel group, the 8-channel
+// groups LBO bytes apart), so the operand of tap (dy, dx) is the staged row
+// of y+dy-1 with its start address moved by dx pixels (16 bytes): the
+// one-pixel shifts of the 3x3 stencil cost no copies.  The weights of all
+// nine taps stay in shared memory in the same layout (8 output channels x
+// 16 bytes per core matrix).  Zero padding, nearest upsampling of a
+// half-resolution input and the ReLU mask of the backward pass are applied
+// while a row is staged.
+//
+// One thread issues the MMAs of a tile (9 taps x CIN/16 K-steps of
+// M=128, N=COUT, K=16) and commits them to an mbarrier; all 128 threads stage
+// the next row meanwhile, then wait (bounded) for the commit, read their
+// pixel's accumulator row from TMEM (thread t = lane t), add bias / skip,
+// apply ReLU and store BF16.  A wait that runs out sets *err, waits once
+// more (bounded) for the MMAs in flight, frees the tensor memory and returns.
+#include <cuda_bf16.h>
+
+#include <cstdint>
+
+#include "scf_unet.cuh"
+
+namespace scf {
+extern thread_local long long g_launches;  // defined with the multigrid launchers
+}  // namespace scf
+
+namespace scf {
+namespace {
+
+using bf16 = __nv_bfloat16;
+using bf162 = __nv_bfloat162;
+
+constexpr int kTile = 128;      // output pixels per tile = MMA M = threads per CTA
+constexpr int kRing = 4;        // staged rows
+constexpr int kSpins = 1 << 20; // bounded mbarrier polls (each suspends at most ~1 us)
+constexpr unsigned kPollNs = 1024;
+
+__device__ __forceinline__ unsigned saddr(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+// --- tcgen05 / mbarrier primitives -----------------------------------------
+__device__ __forceinline__ void bar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ bool bar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(saddr(bar)), "r"(parity), "n"(kPollNs)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool bar_wait_bounded(uint64_t* bar, unsigned parity) {
+  for (int i = 0; i < kSpins; ++i)
+    if (bar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, unsigned ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   saddr(slot)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, unsigned ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+// shared-memory matrix descriptor, no swizzle, K-major:
+// start address, leading byte offset (between 8-element K groups), stride
+// byte offset (between 8-row groups), all in 16-byte units; version 1
+__device__ __forceinline__ uint64_t sdesc(unsigned addr, unsigned lbo, unsigned sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+// instruction descriptor of kind::f16: D F32, A and B BF16, both K-major,
+// N >> 3 at bit 17, M >> 4 at bit 24
+template <int N>
+__host__ __device__ constexpr uint32_t idesc_bf16_m128() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(kTile >> 4) << 24);
+}
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          saddr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// 8 BF16 values of v where the matching value of m is positive, else 0
+__device__ __forceinline__ uint4 mask8(uint4 v, uint4 m) {
+  unsigned* pv = &v.x;
+  const unsigned* pm = &m.x;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const bf162 mm = *reinterpret_cast<const bf162*>(&pm[i]);
+    unsigned keep = 0;
+    if (__low2float(mm) > 0.0f) keep |= 0x0000ffffu;
+    if (__high2float(mm) > 0.0f) keep |= 0xffff0000u;
+    pv[i] &= keep;
+  }
+  return v;
+}
+
+// pixel slots per staged row (130 used).  Threads store consecutive 16-byte
+// groups of a pixel's channels, KC groups per pixel, into rows LBO_A bytes
+// apart; the slot count makes the eight stores of a quarter warp hit eight
+// different 16-byte bank groups: LBO_A = 64 (KC = 2), 32 (KC = 4) or
+// 16 (KC = 8) bytes modulo 128.
+template <int KC>
+constexpr int slots() {
+  return KC == 2 ? 132 : KC == 4 ? 130 : 137;
+}
+
+template <int CIN, int COUT>
+struct TcShape {
+  static constexpr int KC = CIN / 8;               // 16-byte channel groups
+  static constexpr int LBO_A = slots<KC>() * 16;   // between channel groups of a staged row
+  static constexpr int ROWB = KC * LBO_A;          // bytes per staged row
+  static constexpr int LBO_B = COUT * 16;          // between channel groups of a tap's weights
+  static constexpr int TAPB = CIN * COUT * 2;      // bytes per tap of weights
+  static constexpr int WB = 9 * TAPB;
+  static constexpr int OFF_RING = (WB + 127) / 128 * 128;
+  static constexpr int OFF_BIAS = OFF_RING + kRing * ROWB;
+  static constexpr int OFF_BAR = OFF_BIAS + COUT * 4;
+  static constexpr int SMEM = 128 + OFF_BAR + 16;  // + slack to align the base to 128 bytes
+  static constexpr unsigned TCOLS = COUT <= 32 ? 32u : 64u;  // TMEM columns (power of 2 >= 32)
+  static constexpr int NE = 130 * KC;                        // 16-byte groups of a staged row
+  static constexpr int NIT = (NE + kTile - 1) / kTile;       // per thread
+};
+
+template <int CIN, int COUT, bool UPS, bool MASK, bool ADD, bool RELU>
+__global__ void __launch_bounds__(kTile) k_conv_tc(ConvArgs p, int rows, int* err) {
+  using S = TcShape<CIN, COUT>;
+  constexpr int KC = S::KC, NE = S::NE, NIT = S::NIT;
+  extern __shared__ __align__(128) unsigned char tc_raw[];
+  unsigned char* sm = tc_raw + ((128u - (saddr(tc_raw) & 127u)) & 127u);
+  unsigned char* ring = sm + S::OFF_RING;
+  float* bias = reinterpret_cast<float*>(sm + S::OFF_BIAS);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + S::OFF_BAR);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + S::OFF_BAR + 8);
+  const int t = threadIdx.x, warp = t >> 5;
+
+  // weights [co][tap][ci] -> [tap][ci/8][co][8 ci] (output channel fastest:
+  // consecutive threads store consecutive 16-byte groups)
+  for (int i = t; i < COUT * 9 * KC; i += kTile) {
+    const int co = i % COUT, c = (i / COUT) % KC, tap = i / (COUT * KC);
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(p.wt) + (co * 9 + tap) * KC + c);
+    *reinterpret_cast<uint4*>(sm + tap * S::TAPB + c * S::LBO_B + co * 16) = v;
+  }
+  if (t < COUT) bias[t] = p.bias ? p.bias[t] : 0.0f;
+  if (warp == 0) tmem_alloc(tslot, S::TCOLS);
+  if (t == 0) bar_init(bar, 1);
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+
+  const int H = p.H, W = p.W;
+  const int Hi = UPS ? H / 2 : H, Wi = UPS ? W / 2 : W;
+  const int nseg = (W + kTile - 1) / kTile, chunks = (H + rows - 1) / rows;
+  const int items = p.n * nseg * chunks;
+  const unsigned abase = saddr(ring), wbase = saddr(sm);
+  constexpr uint32_t IDESC = idesc_bf16_m128<COUT>();
+  unsigned phase = 0;
+  bool ok = true;
+
+  // Staging of input row yy (full-resolution coordinate, -1..H) of image img
+  // for the segment at x0, in two halves: load() issues the global loads into
+  // registers, put() stores them into the row's ring slot.  Rows outside the
+  // image, pixels outside the row and the ReLU-masked entries are zeros.
+  uint4 v[NIT];
+  auto load = [&](int img, int x0, int yy) {
+#pragma unroll
+    for (int k = 0; k < NIT; ++k) {
+      const int e = t + k * kTile;
+      const int s = e / KC, c = e % KC, x = x0 - 1 + s;
+      v[k] = make_uint4(0u, 0u, 0u, 0u);
+      if (e < NE && yy >= 0 && yy < H && x >= 0 && x < W) {
+        const int yi = UPS ? (yy >> 1) : yy, xi = UPS ? (x >> 1) : x;
+        const size_t off = (((size_t)img * Hi + yi) * Wi + xi) * CIN + c * 8;
+        v[k] = __ldg(reinterpret_cast<const uint4*>(p.in + off));
+        if (MASK) v[k] = mask8(v[k], __ldg(reinterpret_cast<const uint4*>(p.mask + off)));
+      }
+    }
+  };
+  auto put = [&](int yy) {
+    unsigned char* dst = ring + ((yy + 1) & (kRing - 1)) * S::ROWB;
+#pragma unroll
+    for (int k = 0; k < NIT; ++k) {
+      const int e = t + k * kTile;
+      if (e < NE) *reinterpret_cast<uint4*>(dst + (e % KC) * S::LBO_A + (e / KC) * 16) = v[k];
+    }
+  };
+
+  for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
+    const int ch = item % chunks, seg = (item / chunks) % nseg, img = item / (chunks * nseg);
+    const int x0 = seg * kTile, ya = ch * rows, yb = min(H, ya + rows);
+    for (int yy = ya - 1; yy <= ya + 1; ++yy) {
+      load(img, x0, yy);
+      put(yy);
+    }
+    fence_async_smem();
+    __syncthreads();
+    for (int y = ya; y < yb; ++y) {
+      if (t == 0) {
+        tc_fence_after();
+#pragma unroll
+        for (int tap = 0; tap < 9; ++tap) {
+          const int dy = tap / 3, dx = tap % 3;
+          const unsigned arow = abase + ((y + dy) & (kRing - 1)) * S::ROWB + dx * 16;
+          const unsigned btap = wbase + tap * S::TAPB;
+#pragma unroll
+          for (int ks = 0; ks < CIN / 16; ++ks) {
+            const uint64_t a = sdesc(arow + 2 * ks * S::LBO_A, S::LBO_A, 128);
+            const uint64_t b = sdesc(btap + 2 * ks * S::LBO_B, S::LBO_B, 128);
+            mma_bf16(tmem, a, b, IDESC, (tap | ks) != 0);
+          }
+        }
+        mma_commit(bar);
+      }
+      // the next tile's new row: loads in flight during this tile's MMAs and
+      // epilogue, stored afterwards into the slot of row y-2 (read by no MMA
+      // in flight)
+      const bool more = y + 1 < yb;
+      if (more) load(img, x0, y + 2);
+      const bool got = bar_wait_bounded(bar, phase);
+      if (!__syncthreads_and(got)) {
+        ok = false;
+        break;
+      }
+      phase ^= 1u;
+      tc_fence_after();
+      uint32_t r[COUT];
+#pragma unroll
+      for (int j = 0; j < COUT / 16; ++j)
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + j * 16,
+                  *reinterpret_cast<uint32_t(*)[16]>(&r[j * 16]));
+      tmem_wait_ld();
+      const int x = x0 + t;
+      if (x < W) {
+        const size_t off = (((size_t)img * H + y) * W + x) * COUT;
+#pragma unroll
+        for (int g = 0; g < COUT / 8; ++g) {
+          float f[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k) f[k] = __uint_as_float(r[g * 8 + k]) + bias[g * 8 + k];
+          if (ADD) {
+            const uint4 a = __ldg(reinterpret_cast<const uint4*>(p.add + off) + g);
+            const bf162* ab = reinterpret_cast<const bf162*>(&a);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              f[2 * k] += __low2float(ab[k]);
+              f[2 * k + 1] += __high2float(ab[k]);
+            }
+          }
+          if (RELU) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) f[k] = fmaxf(f[k], 0.0f);
+          }
+          uint4 o;
+          bf162* ob = reinterpret_cast<bf162*>(&o);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) ob[k] = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+          *(reinterpret_cast<uint4*>(p.out + off) + g) = o;
+        }
+      }
+      if (more) put(y + 2);
+      fence_async_smem();
+      tc_fence_before();
+      __syncthreads();  // row y+2 staged; this tile's TMEM reads done before the next MMAs
+    }
+  }
+  if (!ok) {
+    if (t == 0) atomicExch(err, 1);
+    bar_wait_bounded(bar, phase);  // let the MMAs in flight finish (bounded)
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, S::TCOLS);
+}
+
+// resident CTAs per SM from the kernel's registers and shared memory (the
+// occupancy query does not count these kernels correctly) and the tensor
+// memory: 512 columns per SM
+template <class K>
+int resident_ctas(K k, int smem, unsigned tcols) {
+  cudaFuncAttributes fa{};
+  int dev = 0, smem_sm = 0, resv = 0, regs_sm = 0, thr_sm = 0;
+  if (cudaFuncGetAttributes(&fa, k) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) !=
+          cudaSuccess ||
+      cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev) !=
+          cudaSuccess ||
+      cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev) !=
+          cudaSuccess ||
+      cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev) != cudaSuccess)
+    return 0;
+  const int per_smem = smem_sm / (smem + fa.sharedSizeBytes + resv);
+  const int warp_regs = (fa.numRegs * 32 + 255) / 256 * 256;  // allocation unit: 256 per warp
+  const int per_regs = regs_sm / (warp_regs * (kTile / 32));
+  const int per_thr = thr_sm / kTile;
+  const int per_tmem = 512 / (int)tcols;
+  int o = per_smem;
+  if (per_regs < o) o = per_regs;
+  if (per_thr < o) o = per_thr;
+  if (per_tmem < o) o = per_tmem;
+  return o;
+}
+
+template <int CIN, int COUT, bool UPS, bool MASK, bool ADD, bool RELU>
+int launch_tc(const ConvArgs& a, int sms, int* err, cudaStream_t s) {
+  using S = TcShape<CIN, COUT>;
+  auto k = k_conv_tc<CIN, COUT, UPS, MASK, ADD, RELU>;
+  static const int occ = [k] {
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM) !=
+        cudaSuccess)
+      return 0;
+    return resident_ctas(k, S::SMEM, S::TCOLS);
+  }();
+  if (occ <= 0) return -1;
+  const long long nseg = (a.W + kTile - 1) / kTile;
+  const long long slots = (long long)sms * occ;
+  const long long total_rows = (long long)a.n * nseg * a.H;
+  int rows = (int)((total_rows + slots - 1) / slots);
+  if (rows < 1) rows = 1;
+  const long long items = (long long)a.n * nseg * ((a.H + rows - 1) / rows);
+  const int grid = (int)(items < slots ? items : slots);
+  k<<<grid, kTile, S::SMEM, s>>>(a, rows, err);
+  ++g_launches;
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int CI, int CO>
+constexpr bool up_pair() {
+  return (CI == 64 && CO == 64) || (CI == 64 && CO == 32) || (CI == 32 && CO == 16);
+}
+template <int CI, int CO>
+constexpr bool relu_pair() {
+  return (CI == 16 && CO == 16) || (CI == 16 && CO == 32) || (CI == 32 && CO == 32) ||
+         (CI == 32 && CO == 64) || (CI == 64 && CO == 64);
+}
+
+// forward: upsampling decoder layer (+ skip add) or conv + ReLU;
+// backward (input gradient): CIN/COUT are the layer's COUT/CIN, the output
+// gradient masked by the ReLU output for ReLU layers
+template <int CI, int CO>
+int dispatch_pair(const ConvArgs& a, bool ups, bool bwd, bool mask, int sms, int* err,
+                  cudaStream_t s) {
+  if (!bwd) {
+    if constexpr (up_pair<CI, CO>())
+      if (ups) return launch_tc<CI, CO, true, false, true, false>(a, sms, err, s);
+    if constexpr (relu_pair<CI, CO>())
+      if (!ups) return launch_tc<CI, CO, false, false, false, true>(a, sms, err, s);
+    return -1;
+  }
+  if constexpr (relu_pair<CO, CI>())
+    if (mask) return launch_tc<CI, CO, false, true, false, false>(a, sms, err, s);
+  if constexpr (up_pair<CO, CI>())
+    if (!mask) return launch_tc<CI, CO, false, false, false, false>(a, sms, err, s);
+  return -1;
+}
+
+}  // namespace
+
+int conv_tc(int cin, int cout, const ConvArgs& a, bool ups, bool bwd, bool mask, int sms,
+            int* err, cudaStream_t s) {
+#define SCF_TC(CI, CO) \
+  if (cin == CI && cout == CO) return dispatch_pair<CI, CO>(a, ups, bwd, mask, sms, err, s);
+  SCF_TC(16, 16) SCF_TC(16, 32) SCF_TC(32, 16) SCF_TC(32, 32) SCF_TC(32, 64) SCF_TC(64, 32)
+  SCF_TC(64, 64)
+#undef SCF_TC
+  return -1;
+}
+
+}  // namespace scf

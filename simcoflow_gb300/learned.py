@@ -57,6 +57,9 @@ def lib():
         L.scf_unet_backward.argtypes = [vp]
         L.scf_unet_get_grads.argtypes = [vp, vp]
         L.scf_unet_adam.argtypes = [vp, fp, fp, fp, fp, ip]
+        L.scf_unet_set_engine.argtypes = [vp, ip]
+        L.scf_unet_conv.argtypes = [ip, ip, ip, ip, ip, ip, vp, vp, vp, vp, vp, vp, ip, ip, ip,
+                                    vp]
         for name in P.UNET_EXPORTS:
             getattr(L, name).restype = C.c_int
         _bound = True
@@ -88,6 +91,10 @@ class UNet:
 
     def __del__(self):
         self.close()
+
+    def set_engine(self, engine: int):
+        """Convolution engine: 1 = tcgen05 (default), 0 = mma.sync (comparison)."""
+        _ck(lib().scf_unet_set_engine(self._h, engine), "scf_unet_set_engine")
 
     def set_stream(self, ptr: int):
         _ck(lib().scf_unet_set_stream(self._h, C.c_void_p(ptr)), "scf_unet_set_stream")

@@ -64,6 +64,8 @@ def main():
     ap.add_argument("--kernel", default="sweep", choices=sorted(KERNELS))
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--engine", type=int, default=1, choices=[0, 1],
+                    help="unet: convolutions on tcgen05 (1) or mma.sync (0)")
     args = ap.parse_args()
     import torch
     dev = torch.device("cuda", 0)
@@ -205,6 +207,7 @@ def main():
         h, w = (c.ny + 7) // 8 * 8, (c.nx + 7) // 8 * 8
         net = Lr.UNet(1, h, w)
         net.set_params(params)
+        net.set_engine(args.engine)
         f = lambda a: torch.from_numpy(np.ascontiguousarray(a.ravel(order="F"))).to(dev)
         sig = torch.zeros(1, dtype=torch.float32, device=dev)
         net.features(0, c.nx, c.ny, f(op["rhs"]), f(op["cE"]), f(op["cN"]), f(op["diag"]), sig)

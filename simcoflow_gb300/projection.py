@@ -51,7 +51,7 @@ UNET_EXPORTS = ["scf_unet_num_params", "scf_unet_create", "scf_unet_destroy",
                 "scf_unet_set_stream", "scf_unet_set_params", "scf_unet_get_params",
                 "scf_unet_features", "scf_unet_target", "scf_unet_set_input", "scf_unet_forward",
                 "scf_unet_loss", "scf_unet_set_dz", "scf_unet_backward", "scf_unet_get_grads",
-                "scf_unet_adam"]
+                "scf_unet_adam", "scf_unet_set_engine", "scf_unet_conv"]
 
 
 class Opts(C.Structure):
