@@ -44,6 +44,13 @@ struct LevelView {
   double* wW;
   double* wS;
   int* arow;
+  // Fine level of a mixed-precision handle only (null otherwise): cE, cN and
+  // max(dg, 0) each split into two floats, (hi, lo) with hi = fl32(c) and
+  // lo = fl32(c - hi), so hi + lo carries c to a relative 2^-48.  The PCG's
+  // q = A p with an FP32 direction p is summed from them on the FP32 pipe.
+  float2* fE;
+  float2* fN;
+  float2* fD;
 };
 
 // Fortran-layout inputs of the assembly, right-hand side and correction.
@@ -150,6 +157,30 @@ __device__ __forceinline__ float d2f_rn(double d) {
   }
   if (((hi << 1) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);  // +-0
   return d2f_rare(d);  // below or above the binary32 normal range, infinity, NaN
+}
+
+// c as hi + lo: hi = fl32(c), lo = fl32(c - hi) (the difference is exact in
+// FP64), together within a relative 2^-48 of c (for lo in the binary32
+// normal range)
+__device__ __forceinline__ float2 split_ff(double c) {
+  const float hi = d2f_rn(c);
+  return make_float2(hi, d2f_rn(c - f2d_exact(hi)));
+}
+
+// (sh, sl) += -(a.x + a.y) * x in float-float arithmetic on the FP32 pipe:
+// the product a.x * x exactly as s + e (an FMA gives the rounding error), s
+// added to sh by Knuth's TwoSum (the rounding error of the sum recovered
+// exactly), the errors and the small product a.y * x collected in sl.  Every
+// operation is an explicit round-to-nearest intrinsic, so the compiler
+// neither fuses nor reorders the error terms away.
+__device__ __forceinline__ void ff_sub_prod(float2 a, float x, float& sh, float& sl) {
+  const float s = __fmul_rn(-a.x, x);
+  const float e = __fmaf_rn(-a.x, x, -s);
+  const float t = __fadd_rn(sh, s);
+  const float bv = __fsub_rn(t, sh);
+  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bv)), __fsub_rn(s, bv));
+  sh = t;
+  sl = __fmaf_rn(-a.y, x, __fadd_rn(sl, __fadd_rn(err, e)));
 }
 
 // max(v, 0) for a v that is not NaN, by the sign bit (-0 gives +0)

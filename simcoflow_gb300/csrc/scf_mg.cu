@@ -458,30 +458,22 @@ __device__ __forceinline__ double conv_z(float z) { return f2d_exact(z); }
 __device__ __forceinline__ double conv_z(double z) { return z; }
 
 // p_new = z + beta p_old (= z on the first iteration), q = A p_new, p.q and
-// alpha = r.z / p.q.  Register-blocked stencil: a warp covers 32 consecutive
-// columns, of which it updates the inner 30 (the first and last lane only
-// form p_new for their neighbours, so every lane runs the same code), and
-// each thread walks `rows` rows of its column, keeping p_new of the rows
-// above and below in registers, taking east/west values from the adjacent
-// lanes and loading the next row one step ahead.  No shared memory and no
-// block barrier before the arithmetic, so the FP64 pipe stays fed.  The
-// search direction has z's precision: FP64 for the FP64 preconditioner; FP32
-// for the FP32 one, whose z carries FP32 accuracy anyway.  With an FP32
-// direction the update and the products of p.q run in FP32, summed with
-// Kahan's compensated summation per thread and in FP64 across threads (p.q
-// only sets the step length alpha),
-// while q = A p and the x/r updates stay FP64 on the same rounded p, so r
-// keeps tracking b - A x in FP64.  That leaves five FP64 operations per cell
-// (the product with the diagonal and four FMAs), the kernel's bound on
-// GB300's FP64 pipe.
-template <class ZT>
+// alpha = r.z / p.q, with an FP64 direction (the FP64 preconditioner).
+// Register-blocked stencil: a warp covers 32 consecutive columns, of which
+// it updates the inner 30 (the first and last lane only form p_new for their
+// neighbours, so every lane runs the same code), and each thread walks
+// `rows` rows of its column, keeping p_new of the rows above and below in
+// registers, taking east/west values from the adjacent lanes and loading the
+// next row one step ahead.  No shared memory and no block barrier before the
+// arithmetic, so the FP64 pipe stays fed: five FP64 operations per cell (the
+// product with the diagonal and four FMAs) are the kernel's bound on GB300's
+// FP64 pipe.
 __global__ void __launch_bounds__(NT)
-k_pupdate_spmv_t(LevelView L, const ZT* __restrict__ z, const ZT* __restrict__ pold,
-                 ZT* __restrict__ pnew, double* __restrict__ q, Scalars* sc, double* part,
+k_pupdate_spmv_t(LevelView L, const double* __restrict__ z, const double* __restrict__ pold,
+                 double* __restrict__ pnew, double* __restrict__ q, Scalars* sc, double* part,
                  int rows) {
   pdl_wait();
   if (sc->done) return;
-  constexpr bool F32 = std::is_same<ZT, float>::value;
   const int nx = L.nx, ny = L.ny, P = L.pitch;
   const int lane = threadIdx.x;  // blockDim (32, 8): a warp is 32 consecutive columns
   const int cx = blockIdx.x * 30 - 1 + lane;
@@ -491,11 +483,10 @@ k_pupdate_spmv_t(LevelView L, const ZT* __restrict__ z, const ZT* __restrict__ p
   const int r1 = r0 + rows < ny ? r0 + rows : ny;
   const bool first = sc->iter == 0;
   const double beta = sc->beta;
-  const float beta_f = (float)beta;
   // raw inputs of p_new at row y of this column (zeros outside the grid)
-  struct Raw { ZT z, p; };
+  struct Raw { double z, p; };
   auto load = [&](int y) -> Raw {
-    Raw r{ZT(0), ZT(0)};
+    Raw r{0.0, 0.0};
     if (col && y >= 0 && y < ny) {
       const size_t g = (size_t)y * P + cx;
       r.z = z[g];
@@ -503,43 +494,19 @@ k_pupdate_spmv_t(LevelView L, const ZT* __restrict__ z, const ZT* __restrict__ p
     }
     return r;
   };
-  auto form = [&](const Raw& r) -> ZT {
-    if constexpr (F32) return fmaf(beta_f, r.p, r.z);
-    else return fma(beta, r.p, r.z);
-  };
-  auto wide = [](ZT v) -> double {
-    if constexpr (F32) return f2d_exact(v);
-    else return v;
-  };
+  auto form = [&](const Raw& r) -> double { return fma(beta, r.p, r.z); };
   double acc = 0.0;
-  float accf = 0.0f, accc = 0.0f;
   if (r0 < r1) {  // uniform across the warp (one threadIdx.y per warp)
-    double pm = wide(form(load(r0 - 1)));
-    ZT pcr = form(load(r0));
-    double pc = wide(pcr);
+    double pm = form(load(r0 - 1));
+    double pc = form(load(r0));
     double cNd = col ? L.cN[(size_t)(r0 - 1) * P + cx] : 0.0;
     Raw nxt = load(r0 + 1);
-    // FP32 direction: the operator of a row is loaded one row ahead, like p
-    // (measured faster there; the FP64 form, with more registers live, is not)
-    double dgn = 0.0, cEn = 0.0, cNn = 0.0;
-    if (F32 && col) {
-      const size_t k0 = (size_t)r0 * P + cx;
-      dgn = L.dg[k0]; cEn = L.cE[k0]; cNn = L.cN[k0];
-    }
     for (int iy = r0; iy < r1; ++iy) {
       const size_t k = (size_t)iy * P + cx;
-      double dg = dgn, cE = cEn, cN = cNn;
-      if constexpr (F32) {
-        if (col && iy + 1 < r1) {
-          const size_t k1 = k + P;
-          dgn = L.dg[k1]; cEn = L.cE[k1]; cNn = L.cN[k1];
-        }
-      } else {
-        if (col) { dg = L.dg[k]; cE = L.cE[k]; cN = L.cN[k]; }
-      }
-      const ZT ppr = form(nxt);
+      double dg = 0.0, cE = 0.0, cN = 0.0;
+      if (col) { dg = L.dg[k]; cE = L.cE[k]; cN = L.cN[k]; }
+      const double pp = form(nxt);
       nxt = load(iy + 2);  // one row ahead
-      const double pp = wide(ppr);
       const double pl = __shfl_up_sync(0xffffffffu, pc, 1);
       const double pr = __shfl_down_sync(0xffffffffu, pc, 1);
       double cW = __shfl_up_sync(0xffffffffu, cE, 1), cS = cNd;
@@ -557,23 +524,112 @@ k_pupdate_spmv_t(LevelView L, const ZT* __restrict__ z, const ZT* __restrict__ p
       qv = fma(-cS, pm, qv);
       if (upd) {
         q[k] = qv;
-        pnew[k] = pcr;
-        if constexpr (F32) {  // compensated FP32 sum of the FP32 products
-          const float y = fmaf(pcr, d2f_rn(qv), -accc);
-          const float t = accf + y;
-          accc = (t - accf) - y;
-          accf = t;
-        } else {
-          acc = fma(pc, qv, acc);
-        }
+        pnew[k] = pc;
+        acc = fma(pc, qv, acc);
       }
       pm = pc;
       pc = pp;
-      pcr = ppr;
       cNd = cN;
     }
   }
-  if constexpr (F32) acc = f2d_exact(accf) - f2d_exact(accc);
+  double tot, dummy;
+  if (grid_sum2(acc, 0.0, part, &sc->tickets[T_PQ], &tot, &dummy) && tlin() == 0) {
+    sc->pq = tot;
+    sc->alpha = sc->rz / tot;
+  }
+}
+
+// The same with an FP32 direction (the FP32 preconditioner, whose z carries
+// FP32 accuracy anyway): p_new = z + beta p_old and the products of p.q in
+// FP32 (Kahan's compensated sum per thread, FP64 across threads; p.q only
+// sets the step length alpha).  q = A p keeps FP64 accuracy without the
+// FP64 pipe: the operator comes as float pairs (hi + lo within 2^-48 of the
+// FP64 entries, split once per setup) and the five products with the FP32
+// direction are summed in float-float arithmetic (exact products by FMA,
+// Knuth's TwoSum), so q = hi + lo is within about 2^-46 of the sum of the
+// magnitudes of its terms -- against 2^-53 for the FP64 sum, far below what
+// the recursive residual r -= alpha q notices at the solver's tolerances --
+// for one FP64 addition per cell.  Free of the FP64 bound, the kernel is
+// bound by memory latency, so it is one thread per cell over a grid-stride
+// row loop: each thread has all its loads (the direction of the cell and its
+// four neighbours, which mostly hit L1 / L2, and the operator) in flight at
+// once.  Cells outside the grid count as zeros.
+__global__ void __launch_bounds__(NT)
+k_pupdate_spmv_ff(LevelView L, const float* __restrict__ z, const float* __restrict__ pold,
+                  float* __restrict__ pnew, double* __restrict__ q, Scalars* sc, double* part) {
+  pdl_wait();
+  if (sc->done) return;
+  const int nx = L.nx, ny = L.ny, P = L.pitch;
+  const bool first = sc->iter == 0;
+  const float beta = first ? 0.0f : (float)sc->beta;
+  const float* __restrict__ po = first ? z : pold;  // beta = 0: any finite array
+  const float2* __restrict__ fD = L.fD;
+  const float2* __restrict__ fE = L.fE;
+  const float2* __restrict__ fN = L.fN;
+  const int* __restrict__ arow = L.arow;
+  const int ix = blockIdx.x * 32 + threadIdx.x;
+  const int S = gridDim.y * 8;
+  const float2 f0 = make_float2(0.0f, 0.0f);
+  // everything a cell reads, fetched one row step ahead of its use
+  struct In {
+    float z[5], p[5];  // centre, west, east, south, north
+    float2 d, e, w, n, s;
+    int flag;
+  };
+  auto fetch = [&](int iy, In& v) {
+    const size_t k = (size_t)iy * P + ix;
+    const bool in[5] = {true, ix > 0, ix + 1 < nx, iy > 0, iy + 1 < ny};
+    const ptrdiff_t off[5] = {0, -1, 1, -(ptrdiff_t)P, (ptrdiff_t)P};
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      v.z[j] = in[j] ? z[k + off[j]] : 0.0f;
+      v.p[j] = in[j] ? po[k + off[j]] : 0.0f;
+    }
+    v.d = fD[k];
+    v.e = fE[k];
+    v.n = fN[k];
+    v.w = in[1] ? fE[k - 1] : f0;
+    v.s = in[3] ? fN[k - P] : f0;
+    v.flag = arow[iy];
+  };
+  float accf = 0.0f, accc = 0.0f;
+  int iy = blockIdx.y * 8 + threadIdx.y;
+  if (ix < nx && iy < ny) {
+    In cur;
+    fetch(iy, cur);
+    for (; iy < ny; iy += S) {
+      In nxt;
+      const bool more = iy + S < ny;
+      if (more) fetch(iy + S, nxt);
+      const size_t k = (size_t)iy * P + ix;
+      float pv[5];
+#pragma unroll
+      for (int j = 0; j < 5; ++j) pv[j] = fmaf(beta, cur.p[j], cur.z[j]);
+      float2 cW = cur.w, cS = cur.s;
+      // rows whose own west / south entries differ from the neighbours'
+      // east / north ones take them from wW / wS
+      if (cur.flag) {
+        cW = split_ff(L.wW[k]);
+        cS = split_ff(L.wS[k]);
+      }
+      const float pc = pv[0];
+      float sh = __fmul_rn(cur.d.x, pc);
+      float sl = __fmaf_rn(cur.d.y, pc, __fmaf_rn(cur.d.x, pc, -sh));
+      ff_sub_prod(cur.e, pv[2], sh, sl);
+      ff_sub_prod(cW, pv[1], sh, sl);
+      ff_sub_prod(cur.n, pv[4], sh, sl);
+      ff_sub_prod(cS, pv[3], sh, sl);
+      q[k] = f2d_exact(sh) + f2d_exact(sl);
+      pnew[k] = pc;
+      // compensated FP32 sum of the FP32 products
+      const float y = fmaf(pc, __fadd_rn(sh, sl), -accc);
+      const float t = accf + y;
+      accc = (t - accf) - y;
+      accf = t;
+      if (more) cur = nxt;
+    }
+  }
+  const double acc = f2d_exact(accf) - f2d_exact(accc);
   double tot, dummy;
   if (grid_sum2(acc, 0.0, part, &sc->tickets[T_PQ], &tot, &dummy) && tlin() == 0) {
     sc->pq = tot;
@@ -648,6 +704,11 @@ __global__ void k_to_mixed(LevelView F, MgView<float, __nv_bfloat16, float> M,
     }
     const_cast<float*>(M.dg)[k] = d;
     const_cast<float*>(M.di)[k] = di;
+    if (F.fD) {  // the fine level's float pairs
+      F.fE[k] = split_ff(F.cE[k]);
+      F.fN[k] = split_ff(F.cN[k]);
+      F.fD[k] = split_ff(pos_part(F.dg[k]));
+    }
   }
 }
 
@@ -921,20 +982,19 @@ void launch_dot_rz_t(int nx, int ny, int pitch, const BT* r, const T* z, int fle
            flexible, sc, part);
 }
 
-// Grid of the direction update + SpMV: 30-column bands times strips of 8
-// warps, each warp `rows` rows long, with `rows` chosen so that the grid is at
-// most one wave of resident CTAs (a second, partly filled wave would double
-// the kernel's time for a fraction of the work).
-template <class ZT>
+// Grid of the FP64-direction update + SpMV: 30-column bands times strips of
+// 8 warps, each warp `rows` rows long, with `rows` chosen so that the grid is
+// at most one wave of resident CTAs (a second, partly filled wave would
+// double the kernel's time for a fraction of the work).
 dim3 pupdate_grid(int nx, int ny, int* rows) {
-  static int cap[2][16];  // resident CTAs per device and precision (0 = unknown)
+  static int cap[16];  // resident CTAs per device (0 = unknown)
   int dev = 0;
   cudaGetDevice(&dev);
-  int& c = cap[std::is_same<ZT, float>::value][dev & 15];
+  int& c = cap[dev & 15];
   if (c == 0) {
     int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pupdate_spmv_t<ZT>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pupdate_spmv_t, 256, 0);
     c = sms * per > 0 ? sms * per : 1;
   }
   const int bands = (nx + 29) / 30;
@@ -944,15 +1004,37 @@ dim3 pupdate_grid(int nx, int ny, int* rows) {
   *rows = r;
   return dim3(bands, (ny + 8 * r - 1) / (8 * r));
 }
-template dim3 pupdate_grid<double>(int, int, int*);
-template dim3 pupdate_grid<float>(int, int, int*);
 
-template <class ZT>
-void launch_pupdate_spmv_t(LevelView L0, const ZT* z, const ZT* pold, ZT* pnew,
-                           double* q, Scalars* sc, double* part, cudaStream_t s) {
+template <>
+void launch_pupdate_spmv_t<double>(LevelView L0, const double* z, const double* pold,
+                                   double* pnew, double* q, Scalars* sc, double* part,
+                                   cudaStream_t s) {
   int rows = 0;
-  const dim3 g = pupdate_grid<ZT>(L0.nx, L0.ny, &rows);
-  launch_k(k_pupdate_spmv_t<ZT>, g, dim3(32, 8), 0, s, L0, z, pold, pnew, q, sc, part, rows);
+  const dim3 g = pupdate_grid(L0.nx, L0.ny, &rows);
+  launch_k(k_pupdate_spmv_t, g, dim3(32, 8), 0, s, L0, z, pold, pnew, q, sc, part, rows);
+}
+// FP32-direction grid: 32-column bands times row strips, about eight CTAs
+// per SM in all (measured best on the 2048^2 and 4096^2 levels: fewer leave
+// memory latency exposed, more make the last-block reduction longer)
+dim3 pupdate_ff_grid(int nx, int ny) {
+  static int sms[16];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int& n = sms[dev & 15];
+  if (n == 0) {
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  const int gx = (nx + 31) / 32;
+  int gy = 8 * n / gx > 1 ? 8 * n / gx : 1;
+  if (gy > (ny + 7) / 8) gy = (ny + 7) / 8;
+  return dim3(gx, gy);
+}
+template <>
+void launch_pupdate_spmv_t<float>(LevelView L0, const float* z, const float* pold, float* pnew,
+                                  double* q, Scalars* sc, double* part, cudaStream_t s) {
+  launch_k(k_pupdate_spmv_ff, pupdate_ff_grid(L0.nx, L0.ny), dim3(32, 8), 0, s, L0, z, pold,
+           pnew, q, sc, part);
 }
 
 void launch_inv_diag(const LevelView& L, double* di, cudaStream_t s) {
@@ -1065,9 +1147,5 @@ template void launch_dot_rz_t<double, double>(int, int, int, const double*, cons
                                               Scalars*, double*, cudaStream_t);
 template void launch_dot_rz_t<float, float>(int, int, int, const float*, const float*, int,
                                             Scalars*, double*, cudaStream_t);
-template void launch_pupdate_spmv_t<double>(LevelView, const double*, const double*, double*,
-                                            double*, Scalars*, double*, cudaStream_t);
-template void launch_pupdate_spmv_t<float>(LevelView, const float*, const float*, float*,
-                                           double*, Scalars*, double*, cudaStream_t);
 
 }  // namespace scf

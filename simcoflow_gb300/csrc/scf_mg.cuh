@@ -95,9 +95,10 @@ template <class T, class BT>
 void launch_dot_rz_t(int nx, int ny, int pitch, const BT* r, const T* z, int flexible,
                      Scalars* sc, double* part, cudaStream_t s);
 
-// grid (and rows per thread) of the direction update + SpMV kernel
-template <class ZT>
+// grids of the direction update + SpMV kernels: FP64 direction (and rows
+// per thread), FP32 direction
 dim3 pupdate_grid(int nx, int ny, int* rows);
+dim3 pupdate_ff_grid(int nx, int ny);
 template <class ZT>
 void launch_pupdate_spmv_t(LevelView L0, const ZT* z, const ZT* pold, ZT* pnew,
                            double* q, Scalars* sc, double* part, cudaStream_t s);

@@ -1068,6 +1068,11 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
       if ((rc = level_array(h, ly, L.pitch, &L.wW)) || (rc = level_array(h, ly, L.pitch, &L.wS)) ||
           (rc = dev_alloc(h, (void**)&L.arow, sizeof(int) * (size_t)ly)))
         return fail(rc);
+      // mixed: the float pairs of the operator for the FP32-direction SpMV
+      if (h->mixed &&
+          ((rc = level_array(h, ly, L.pitch, &L.fE)) || (rc = level_array(h, ly, L.pitch, &L.fN)) ||
+           (rc = level_array(h, ly, L.pitch, &L.fD))))
+        return fail(rc);
     }
     h->lev.push_back(L);
     h->di64.push_back(di);
@@ -1179,7 +1184,7 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
     if (rb > nblk) nblk = rb;
     // direction update + SpMV
     int rows = 0;
-    for (const dim3 g : {pupdate_grid<double>(nx, ny, &rows), pupdate_grid<float>(nx, ny, &rows)})
+    for (const dim3 g : {pupdate_grid(nx, ny, &rows), pupdate_ff_grid(nx, ny)})
       if ((size_t)g.x * g.y > nblk) nblk = (size_t)g.x * g.y;
     // r.z fused into the last line relaxation: one block per pair of rows
     const size_t lb = (size_t)(ny + 1) / 2;
