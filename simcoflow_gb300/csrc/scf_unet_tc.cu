@@ -219,35 +219,42 @@ __global__ void __launch_bounds__(kTile) k_conv_tc(ConvArgs p, int rows, int* er
   // registers, put() stores them into the row's ring slot.  Rows outside the
   // image, pixels outside the row and the ReLU-masked entries are zeros.
   uint4 v[NIT];
-  auto load = [&](int img, int x0, int yy) {
+  auto load_to = [&](uint4 (&u)[NIT], int img, int x0, int yy) {
 #pragma unroll
     for (int k = 0; k < NIT; ++k) {
       const int e = t + k * kTile;
       const int s = e / KC, c = e % KC, x = x0 - 1 + s;
-      v[k] = make_uint4(0u, 0u, 0u, 0u);
+      u[k] = make_uint4(0u, 0u, 0u, 0u);
       if (e < NE && yy >= 0 && yy < H && x >= 0 && x < W) {
         const int yi = UPS ? (yy >> 1) : yy, xi = UPS ? (x >> 1) : x;
         const size_t off = (((size_t)img * Hi + yi) * Wi + xi) * CIN + c * 8;
-        v[k] = __ldg(reinterpret_cast<const uint4*>(p.in + off));
-        if (MASK) v[k] = mask8(v[k], __ldg(reinterpret_cast<const uint4*>(p.mask + off)));
+        u[k] = __ldg(reinterpret_cast<const uint4*>(p.in + off));
+        if (MASK) u[k] = mask8(u[k], __ldg(reinterpret_cast<const uint4*>(p.mask + off)));
       }
     }
   };
-  auto put = [&](int yy) {
+  auto put_from = [&](const uint4 (&u)[NIT], int yy) {
     unsigned char* dst = ring + ((yy + 1) & (kRing - 1)) * S::ROWB;
 #pragma unroll
     for (int k = 0; k < NIT; ++k) {
       const int e = t + k * kTile;
-      if (e < NE) *reinterpret_cast<uint4*>(dst + (e % KC) * S::LBO_A + (e / KC) * 16) = v[k];
+      if (e < NE) *reinterpret_cast<uint4*>(dst + (e % KC) * S::LBO_A + (e / KC) * 16) = u[k];
     }
   };
+  auto load = [&](int img, int x0, int yy) { load_to(v, img, x0, yy); };
+  auto put = [&](int yy) { put_from(v, yy); };
 
   for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
     const int ch = item % chunks, seg = (item / chunks) % nseg, img = item / (chunks * nseg);
     const int x0 = seg * kTile, ya = ch * rows, yb = min(H, ya + rows);
-    for (int yy = ya - 1; yy <= ya + 1; ++yy) {
-      load(img, x0, yy);
-      put(yy);
+    {  // the first tile's three rows: all loads in flight before any store
+      uint4 u0[NIT], u1[NIT];
+      load_to(u0, img, x0, ya - 1);
+      load_to(u1, img, x0, ya);
+      load(img, x0, ya + 1);
+      put_from(u0, ya - 1);
+      put_from(u1, ya);
+      put(ya + 1);
     }
     fence_async_smem();
     __syncthreads();
