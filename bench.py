@@ -45,6 +45,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "ms/projection to FP64 rel. residual 1e-8: learned+mixed FPCG vs plain MG-PCG"
 UNIT = "ms/projection"
 FALLBACK_HBM_GBS = 6800.0
+FALLBACK_BF16_TFLOPS = 1900.0
 
 
 def _peaks():
@@ -56,6 +57,64 @@ def _peaks():
         except Exception:
             pass
     return FALLBACK_HBM_GBS, "fallback"
+
+
+def _bf16_peak():
+    """Dense BF16 tensor peak (TFLOP/s, burst) and where it comes from."""
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["bf16_tflops"]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_BF16_TFLOPS, "fallback"
+
+
+def unet_forward_times(sizes=((1024, 1024), (4096, 4096)), reps=10):
+    """The learned preconditioner's network on its own: one forward pass
+    (14 3x3 convolutions, pooling, head) of one image, shipped weights and
+    seeded inputs, CUDA events around `reps` back-to-back passes after two
+    warm-ups, on both convolution engines (tcgen05 with TMEM accumulators,
+    the default; the mma.sync kernels, for comparison).  FLOPs: 2 x 9 x
+    cin x cout per pixel of each convolution at its level."""
+    import torch
+    from simcoflow_gb300 import learned as Lr
+    peak, kind = _bf16_peak()
+    params, _ = Lr.load_weights()
+    rng = np.random.Generator(np.random.PCG64(5))
+    out = {}
+    for (h, w) in sizes:
+        flop = 2 * 9 * sum(ci * co / 4 ** lvl for (ci, co), lvl in zip(
+            Lr.LAYERS, (0, 0, 1, 1, 2, 2, 3, 3, 2, 2, 1, 1, 0, 0))) * h * w
+        net = Lr.UNet(1, h, w)
+        try:
+            net.set_params(params)
+            net.set_input(rng.normal(size=(1, h, w, 5)).astype(np.float32))
+            z = torch.empty((1, h, w), dtype=torch.float32, device="cuda")
+            r = {}
+            for name, eng in (("tcgen05", 1), ("mma_sync", 0)):
+                net.set_engine(eng)
+                for _ in range(2):
+                    net.forward(z)
+                torch.cuda.synchronize()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                for _ in range(reps):
+                    net.forward(z)
+                b.record()
+                torch.cuda.synchronize()
+                ms = a.elapsed_time(b) / reps
+                r[name] = {"ms": round(ms, 4), "tflops": round(flop / (ms * 1e-3) / 1e12, 1),
+                           "frac_of_bf16_peak": round(flop / (ms * 1e-3) / 1e12 / peak, 4)}
+            net.set_engine(1)
+        finally:
+            net.close()
+        out[f"{h}x{w}"] = {**r, "gflop": round(flop / 1e9, 2),
+                           "speedup_tcgen05": round(r["mma_sync"]["ms"] / r["tcgen05"]["ms"], 3)}
+    out["peak"] = {"bf16_tflops": peak, "source": kind}
+    out["timing"] = ("CUDA events on the default stream around back-to-back forward passes "
+                     "(each ends with a 4-byte status read)")
+    return out
 
 
 class ClockSampler:
@@ -1094,6 +1153,10 @@ def run_ours(args):
                                  "fallback_to_vcycle": bool(learned["fallbacks"]),
                                  "relres_true": learned["relres"][-1],
                                  "speedup_vs_plain_fp64": round(plain["ms"] / learned["ms"], 3)}
+        try:
+            line["unet_forward"] = unet_forward_times()
+        except Exception as e:  # must not hide the headline line
+            line["unet_forward"] = {"error": f"{type(e).__name__}: {e}"}
     print(json.dumps(line), flush=True)
     if pg:
         pg.destroy_process_group()

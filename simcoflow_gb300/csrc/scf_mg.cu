@@ -1015,7 +1015,9 @@ void launch_pupdate_spmv_t<double>(LevelView L0, const double* z, const double* 
 }
 // FP32-direction grid: 32-column bands times row strips, about eight CTAs
 // per SM in all (measured best on the 2048^2 and 4096^2 levels: fewer leave
-// memory latency exposed, more make the last-block reduction longer)
+// memory latency exposed, more make the last-block reduction longer), and at
+// least eight rows per thread (small grids, many of which run side by side in
+// a batch, would otherwise launch a block per eight rows)
 dim3 pupdate_ff_grid(int nx, int ny) {
   static int sms[16];
   int dev = 0;
@@ -1027,7 +1029,8 @@ dim3 pupdate_ff_grid(int nx, int ny) {
   }
   const int gx = (nx + 31) / 32;
   int gy = 8 * n / gx > 1 ? 8 * n / gx : 1;
-  if (gy > (ny + 7) / 8) gy = (ny + 7) / 8;
+  const int gmax = (ny + 63) / 64;
+  if (gy > gmax) gy = gmax;
   return dim3(gx, gy);
 }
 template <>
