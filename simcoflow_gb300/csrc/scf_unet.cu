@@ -666,10 +666,12 @@ void conv_mma(int cin, int cout, const ConvP& p, bool ups, bool bwd, bool mask, 
 }  // namespace
 
 // a layer's convolution on the selected engine (tcgen05 unless a test or a
-// measurement asks for the mma.sync kernel)
+// measurement asks for the mma.sync kernel); map: the input's tensor map
+// (device) for TMA staging, or null
 void conv_dispatch(int engine, int cin, int cout, const ConvP& p, bool ups, bool bwd, bool mask,
-                   int sms, int* err, cudaStream_t s) {
-  if (engine == 1) conv_tc(cin, cout, p, ups, bwd, mask, sms, err, s);
+                   int sms, int* err, const CUtensorMap* map, cudaStream_t s) {
+  if (engine == 1 || engine == 2)
+    conv_tc(cin, cout, p, ups, bwd, mask, sms, err, engine == 1 ? map : nullptr, s);
   else conv_mma(cin, cout, p, ups, bwd, mask, sms, s);
 }
 
@@ -744,6 +746,23 @@ int UNet::create(int n, int h, int w, bool train, int device) {
   const int pc[3] = {16, 32, 64};
   for (int i = 0; i < 3; ++i)
     if (alloc((void**)&pool_[i], px(i + 1) * pc[i] * 2)) return -1;
+  // tensor maps of the forward ReLU layers' inputs (TMA staging); a layer
+  // whose map the driver does not accept stages its rows with its threads
+  has_map_.assign(L.size(), 0);
+  if (alloc((void**)&maps_, L.size() * sizeof(CUtensorMap))) return -1;
+  {
+    std::vector<CUtensorMap> hm(L.size());
+    for (size_t i = 0; i < L.size(); ++i) {
+      if (L[i].ups) continue;
+      const void* in = i == 0 ? (const void*)in_
+                       : (i == 2 || i == 4 || i == 6) ? (const void*)pool_[i / 2 - 1]
+                                                      : (const void*)act_[i - 1];
+      has_map_[i] = conv_tma_map(&hm[i], in, n, h >> L[i].level, w >> L[i].level, L[i].cin) == 0;
+    }
+    if (cudaMemcpy(maps_, hm.data(), L.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice) !=
+        cudaSuccess)
+      return -1;
+  }
   if (train) {
     if (alloc((void**)&grads_, np * 4) || alloc((void**)&m_, np * 4) || alloc((void**)&v_, np * 4) ||
         alloc((void**)&dz_, p0 * 4))
@@ -763,6 +782,8 @@ void UNet::destroy() {
   act_.clear(); pool_.clear(); g_.clear();
   params_ = grads_ = m_ = v_ = z_ = dz_ = red_ = nullptr;
   tc_err_ = nullptr;
+  maps_ = nullptr;
+  has_map_.clear();
   wb_ = wt_ = in_ = nullptr;
 }
 
@@ -829,7 +850,8 @@ void UNet::forward(cudaStream_t s) {
     size_t off = 0;
     for (size_t j = 0; j < i; ++j) off += (size_t)L[j].cout * 9 * L[j].cin;
     p.wt = wb_ + off;
-    conv_dispatch(engine_, l.cin, l.cout, p, l.ups, false, false, sms_, tc_err_, s);
+    conv_dispatch(engine_, l.cin, l.cout, p, l.ups, false, false, sms_, tc_err_,
+                  has_map_[i] ? maps_ + i : nullptr, s);
   }
   k_head<<<grid_for((size_t)n_ * h_ * w_, sms_), 256, 0, s>>>(
       act_.back(), params_ + num_params() - 17, (size_t)n_ * h_ * w_, z_);
@@ -947,7 +969,7 @@ void UNet::backward(cudaStream_t s) {
     p.bias = nullptr;
     p.out = g_[b];
     p.n = n_; p.H = H; p.W = W;
-    conv_dispatch(engine_, l.cout, l.cin, p, false, true, l.relu, sms_, tc_err_, s);
+    conv_dispatch(engine_, l.cout, l.cin, p, false, true, l.relu, sms_, tc_err_, nullptr, s);
     int cur = b;
     if (l.ups) {  // gradient of nearest upsampling: 2x2 sums onto the coarse input
       const int c = other(a, b);
@@ -1084,7 +1106,7 @@ static int tc_status(scf_unet* u) {
 }
 
 int scf_unet_set_engine(scf_unet* u, int engine) {
-  if (!u || (engine != 0 && engine != 1)) return -1;
+  if (!u || engine < 0 || engine > 2) return -1;
   u->net.engine_ = engine;
   return 0;
 }
@@ -1107,7 +1129,7 @@ int scf_unet_forward(scf_unet* u, float* z, int device) {
 int scf_unet_conv(int engine, int cin, int cout, int ups, int bwd, int mask, const void* in,
                   const void* maskp, const void* wt, const float* bias, const void* add,
                   void* out, int n, int H, int W, void* stream) {
-  if ((engine != 0 && engine != 1) || n < 1 || H < 1 || W < 1 || !in || !wt || !out ||
+  if (engine < 0 || engine > 2 || n < 1 || H < 1 || W < 1 || !in || !wt || !out ||
       (ups && (bwd || H % 2 || W % 2 || !add)) || (mask && (!bwd || !maskp)) ||
       (!bwd && !ups && !bias))
     return -1;
@@ -1126,13 +1148,22 @@ int scf_unet_conv(int engine, int cin, int cout, int ups, int bwd, int mask, con
   int* err = nullptr;
   if (cudaMalloc((void**)&err, 4) != cudaSuccess) return -2;
   cudaMemsetAsync(err, 0, 4, s);
-  scf::conv_dispatch(engine, cin, cout, a, ups != 0, bwd != 0, mask != 0, sms, err, s);
+  // forward ReLU layers on engine 1: the input's tensor map for TMA staging
+  CUtensorMap* dmap = nullptr;
+  if (engine == 1 && !ups && !bwd) {
+    CUtensorMap hm;
+    if (scf::conv_tma_map(&hm, in, n, H, W, cin) == 0 &&
+        cudaMalloc((void**)&dmap, sizeof(CUtensorMap)) == cudaSuccess)
+      cudaMemcpy(dmap, &hm, sizeof(CUtensorMap), cudaMemcpyHostToDevice);
+  }
+  scf::conv_dispatch(engine, cin, cout, a, ups != 0, bwd != 0, mask != 0, sms, err, dmap, s);
   int e = 0;
   int rc = (cudaMemcpyAsync(&e, err, 4, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
             cudaStreamSynchronize(s) == cudaSuccess && cudaGetLastError() == cudaSuccess)
                ? 0
                : -2;
   cudaFree(err);
+  if (dmap) cudaFree(dmap);
   if (rc == 0 && e) rc = -3;
   return rc;
 }

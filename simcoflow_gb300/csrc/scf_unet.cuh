@@ -2,6 +2,7 @@
 // C-ABI (training, tests) and by the projection solver (inference inside the
 // flexible PCG).
 #pragma once
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -26,8 +27,13 @@ struct ConvArgs {
 // input masked by the ReLU output.  *err (device int) is set when a bounded
 // wait runs out.  Returns 0, or -1 for a channel pair or variant that the
 // network does not have or a failed launch.
+// map: device copy of the input's tensor map from conv_tma_map, or null.
+// With a map the forward ReLU layers stage their input rows by TMA.
 int conv_tc(int cin, int cout, const ConvArgs& a, bool ups, bool bwd, bool mask, int sms,
-            int* err, cudaStream_t s);
+            int* err, const CUtensorMap* map, cudaStream_t s);
+// Tensor map of an NHWC BF16 tensor [n][H][W][cin] for the TMA-staged
+// convolution (host; 0 on success).
+int conv_tma_map(CUtensorMap* m, const void* in, int n, int H, int W, int cin);
 
 struct UNetLayer {
   int cin, cout;  // channels in / out
@@ -70,10 +76,13 @@ class UNet {
 
   int n_ = 0, h_ = 0, w_ = 0;
   bool train_ = false;
-  // convolution engine: 1 = tcgen05 (TMEM accumulators), 0 = mma.sync (kept
-  // as the comparison for tests and measurements); weight gradients use
-  // mma.sync either way
+  // convolution engine: 1 = tcgen05 (TMEM accumulators) with the forward
+  // ReLU layers' rows staged by TMA, 2 = tcgen05 with every row staged by
+  // the threads, 0 = mma.sync (kept as the comparison for tests and
+  // measurements); weight gradients use mma.sync either way
   int engine_ = 1;
+  CUtensorMap* maps_ = nullptr;  // device: tensor map of each layer's input (forward)
+  std::vector<char> has_map_;    // the layer's map was accepted
   int* tc_err_ = nullptr;  // device flag: a tcgen05 convolution's bounded wait ran out
   int sms_ = 152;
   float *params_ = nullptr, *grads_ = nullptr, *m_ = nullptr, *v_ = nullptr;

@@ -26,6 +26,7 @@
 // pixel's accumulator row from TMEM (thread t = lane t), add bias / skip,
 // apply ReLU and store BF16.  A wait that runs out sets *err, waits once
 // more (bounded) for the MMAs in flight, frees the tensor memory and returns.
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <cstdint>
@@ -337,11 +338,227 @@ __global__ void __launch_bounds__(kTile) k_conv_tc(ConvArgs p, int rows, int* er
   if (warp == 0) tmem_dealloc(tmem, S::TCOLS);
 }
 
+// ---------------------------------------------------------------------------
+// The forward ReLU layers (input at full resolution, no mask, no skip add)
+// with the staged rows copied by the tensor-memory-access unit: one thread
+// issues, per input row, one cp.async.bulk.tensor copy of the 130 pixels
+// x0-1 .. x0+128 times all CIN channels straight into the ring slot's
+// canonical layout, and the copy completes on the slot's own mbarrier.  The
+// tensor map describes the NHWC tensor with its dimensions reordered --
+// (8 channels, pixel, channel group, row, image) -- so that a box of
+// (8, 130, CIN/8, 1, 1) lands as [channel group][pixel][8 channels]: the
+// no-swizzle K-major layout with 16 bytes per pixel and 2080 bytes between
+// channel groups.  Coordinates outside the image (the pixel before and after
+// the row, the rows above and below it) read as zeros: the convolution's
+// padding.  Rows are fetched two tiles ahead (five ring slots: the MMAs of
+// tile y read rows y-1 .. y+1, row y+2 is in flight, row y+3 is issued), so
+// the threads do no staging at all; they only run the epilogue.
+constexpr int kTmaSlots = 5;
+constexpr int kTmaPix = 130;
+constexpr int kTmaThreads = 256;  // two warps per TMEM lane quadrant
+
+template <int CIN, int COUT>
+struct TmaShape {
+  static constexpr int KC = CIN / 8;
+  static constexpr int LBO_A = kTmaPix * 16;                 // between channel groups
+  static constexpr int ROW_BYTES = KC * LBO_A;                // one copy
+  static constexpr int ROWB = (ROW_BYTES + 127) / 128 * 128;  // slot stride (128-byte aligned)
+  static constexpr int LBO_B = COUT * 16;
+  static constexpr int TAPB = CIN * COUT * 2;
+  static constexpr int WB = 9 * TAPB;
+  static constexpr int OFF_RING = (WB + 127) / 128 * 128;
+  static constexpr int OFF_BIAS = OFF_RING + kTmaSlots * ROWB;
+  static constexpr int OFF_BAR = OFF_BIAS + COUT * 4;  // two MMA barriers, then one per slot
+  static constexpr int SMEM = 128 + OFF_BAR + 8 * (2 + kTmaSlots) + 16;
+  // two accumulators of COUT FP32 columns
+  static constexpr unsigned TCOLS = COUT <= 16 ? 32u : COUT <= 32 ? 64u : 128u;
+  static constexpr int HALF = COUT / 2;  // columns drained by one warp
+};
+
+__device__ __forceinline__ void bar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void tma_row(void* dst, const CUtensorMap* map, int x, int row, int img,
+                                        uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(saddr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(x), "r"(0), "r"(row), "r"(img),
+      "r"(saddr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7])
+      : "r"(taddr));
+}
+
+// Per tile y (accumulator buf): thread 0 issues the next tile's MMAs into the
+// other accumulator (its three rows have arrived) and the copy of row y+3,
+// then every warp waits for tile y's MMAs and drains its quarter of the
+// pixels and half of the channels of accumulator buf -- the tensor core
+// works on tile y+1 meanwhile.
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(kTmaThreads) k_conv_tma(ConvArgs p, int rows, int* err,
+                                                          const CUtensorMap* map) {
+  using S = TmaShape<CIN, COUT>;
+  constexpr int KC = S::KC, HALF = S::HALF;
+  extern __shared__ __align__(128) unsigned char tm_raw[];
+  unsigned char* sm = tm_raw + ((128u - (saddr(tm_raw) & 127u)) & 127u);
+  unsigned char* ring = sm + S::OFF_RING;
+  float* bias = reinterpret_cast<float*>(sm + S::OFF_BIAS);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + S::OFF_BAR);  // MMA completion, per accumulator
+  uint64_t* rbar = bar + 2;                                      // row arrival, per slot
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(rbar + kTmaSlots);
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int quad = warp & 3, half = warp >> 2;  // TMEM lanes 32 quad .. , columns half * HALF ..
+
+  for (int i = t; i < COUT * 9 * KC; i += kTmaThreads) {
+    const int co = i % COUT, c = (i / COUT) % KC, tap = i / (COUT * KC);
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(p.wt) + (co * 9 + tap) * KC + c);
+    *reinterpret_cast<uint4*>(sm + tap * S::TAPB + c * S::LBO_B + co * 16) = v;
+  }
+  if (t < COUT) bias[t] = p.bias ? p.bias[t] : 0.0f;
+  if (warp == 0) tmem_alloc(tslot, S::TCOLS);
+  if (t == 0) {
+    bar_init(bar, 1);
+    bar_init(bar + 1, 1);
+    for (int k = 0; k < kTmaSlots; ++k) bar_init(rbar + k, 1);
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+
+  const int H = p.H, W = p.W;
+  const int nseg = (W + kTile - 1) / kTile, chunks = (H + rows - 1) / rows;
+  const int items = p.n * nseg * chunks;
+  const unsigned abase = saddr(ring), wbase = saddr(sm);
+  constexpr uint32_t IDESC = idesc_bf16_m128<COUT>();
+  // per accumulator: the parity of its next commit; thread 0: its commits not
+  // yet waited for
+  unsigned phases = 0u, pend = 0u;
+  // thread 0: the parity of each slot's next arrival, slots with a copy in flight
+  unsigned rphase = 0u, rpend = 0u;
+  bool ok = true;
+  auto slot_of = [](int yy) { return (yy + 1) % kTmaSlots; };
+  auto fetch = [&](int img, int x0, int yy) {  // thread 0
+    const int s = slot_of(yy);
+    bar_expect_tx(rbar + s, (unsigned)S::ROW_BYTES);
+    tma_row(ring + s * S::ROWB, map, x0 - 1, yy, img, rbar + s);
+    rpend |= 1u << s;
+  };
+  auto arrived = [&](int yy) -> bool {  // thread 0, bounded
+    const int s = slot_of(yy);
+    if (!bar_wait_bounded(rbar + s, (rphase >> s) & 1u)) return false;
+    rphase ^= 1u << s;
+    rpend &= ~(1u << s);
+    return true;
+  };
+  auto issue = [&](int y, int buf) {  // thread 0: the MMAs of tile y
+    tc_fence_after();
+    const int s0 = slot_of(y - 1);
+#pragma unroll
+    for (int tap = 0; tap < 9; ++tap) {
+      const int dy = tap / 3, dx = tap % 3;
+      const int slot = s0 + dy < kTmaSlots ? s0 + dy : s0 + dy - kTmaSlots;
+      const unsigned arow = abase + slot * S::ROWB + dx * 16;
+      const unsigned btap = wbase + tap * S::TAPB;
+#pragma unroll
+      for (int ks = 0; ks < CIN / 16; ++ks) {
+        const uint64_t a = sdesc(arow + 2 * ks * S::LBO_A, S::LBO_A, 128);
+        const uint64_t b = sdesc(btap + 2 * ks * S::LBO_B, S::LBO_B, 128);
+        mma_bf16(tmem + buf * COUT, a, b, IDESC, (tap | ks) != 0);
+      }
+    }
+  };
+
+  for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
+    const int ch = item % chunks, seg = (item / chunks) % nseg, img = item / (chunks * nseg);
+    const int x0 = seg * kTile, ya = ch * rows, yb = min(H, ya + rows);
+    bool rows_ok = true;
+    if (t == 0) {  // rows ya-1 .. yb are needed; the first four fetched up front
+      for (int yy = ya - 1; yy <= ya + 2 && yy <= yb; ++yy) fetch(img, x0, yy);
+      rows_ok = arrived(ya - 1) && arrived(ya) && arrived(ya + 1);
+      if (rows_ok) issue(ya, 0);
+      mma_commit(bar);  // arrives at once when no MMA was issued
+      pend |= 1u;
+    }
+    for (int y = ya; y < yb; ++y) {
+      const int buf = (y - ya) & 1;
+      if (t == 0 && rows_ok && y + 1 < yb) {
+        // tile y+1 into the other accumulator, drained by tile y-1
+        rows_ok = arrived(y + 2);
+        if (rows_ok) {
+          issue(y + 1, buf ^ 1);
+          mma_commit(bar + (buf ^ 1));
+          pend |= 1u << (buf ^ 1);
+          // row y+3 into the slot of row y-2, read by no MMA in flight
+          if (y + 3 <= yb) fetch(img, x0, y + 3);
+        }
+      }
+      const bool got = bar_wait_bounded(bar + buf, (phases >> buf) & 1u);
+      if (!__syncthreads_and(got && rows_ok)) {
+        ok = false;
+        break;
+      }
+      phases ^= 1u << buf;
+      pend &= ~(1u << buf);
+      tc_fence_after();
+      uint32_t r[HALF];
+      const uint32_t ta = tmem + ((uint32_t)(quad * 32) << 16) + buf * COUT + half * HALF;
+      if constexpr (HALF == 8) {
+        tmem_ld8(ta, *reinterpret_cast<uint32_t(*)[8]>(&r[0]));
+      } else {
+#pragma unroll
+        for (int j = 0; j < HALF / 16; ++j)
+          tmem_ld16(ta + j * 16, *reinterpret_cast<uint32_t(*)[16]>(&r[j * 16]));
+      }
+      tmem_wait_ld();
+      const int x = x0 + quad * 32 + lane;
+      if (x < W) {
+        const size_t off = (((size_t)img * H + y) * W + x) * COUT + half * HALF;
+#pragma unroll
+        for (int g = 0; g < HALF / 8; ++g) {
+          float f[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+            f[k] = fmaxf(__uint_as_float(r[g * 8 + k]) + bias[half * HALF + g * 8 + k], 0.0f);
+          uint4 o;
+          bf162* ob = reinterpret_cast<bf162*>(&o);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) ob[k] = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+          *(reinterpret_cast<uint4*>(p.out + off) + g) = o;
+        }
+      }
+      tc_fence_before();
+      __syncthreads();  // accumulator buf drained before tile y+2's MMAs
+    }
+  }
+  if (!ok && t == 0) {
+    atomicExch(err, 1);
+    // let the copies and MMAs in flight land (bounded) before the memory goes
+    for (int s = 0; s < kTmaSlots; ++s)
+      if ((rpend >> s) & 1u) bar_wait_bounded(rbar + s, (rphase >> s) & 1u);
+    if (pend & 1u) bar_wait_bounded(bar, phases & 1u);
+    if (pend & 2u) bar_wait_bounded(bar + 1, (phases >> 1) & 1u);
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, S::TCOLS);
+}
+
 // resident CTAs per SM from the kernel's registers and shared memory (the
 // occupancy query does not count these kernels correctly) and the tensor
 // memory: 512 columns per SM
 template <class K>
-int resident_ctas(K k, int smem, unsigned tcols) {
+int resident_ctas(K k, int smem, unsigned tcols, int threads = kTile) {
   cudaFuncAttributes fa{};
   int dev = 0, smem_sm = 0, resv = 0, regs_sm = 0, thr_sm = 0;
   if (cudaFuncGetAttributes(&fa, k) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
@@ -355,8 +572,8 @@ int resident_ctas(K k, int smem, unsigned tcols) {
     return 0;
   const int per_smem = smem_sm / (smem + fa.sharedSizeBytes + resv);
   const int warp_regs = (fa.numRegs * 32 + 255) / 256 * 256;  // allocation unit: 256 per warp
-  const int per_regs = regs_sm / (warp_regs * (kTile / 32));
-  const int per_thr = thr_sm / kTile;
+  const int per_regs = regs_sm / (warp_regs * (threads / 32));
+  const int per_thr = thr_sm / threads;
   const int per_tmem = 512 / (int)tcols;
   int o = per_smem;
   if (per_regs < o) o = per_regs;
@@ -388,6 +605,29 @@ int launch_tc(const ConvArgs& a, int sms, int* err, cudaStream_t s) {
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
+template <int CIN, int COUT>
+int launch_tma(const ConvArgs& a, int sms, int* err, const CUtensorMap* map, cudaStream_t s) {
+  using S = TmaShape<CIN, COUT>;
+  auto k = k_conv_tma<CIN, COUT>;
+  static const int occ = [k] {
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM) !=
+        cudaSuccess)
+      return 0;
+    return resident_ctas(k, S::SMEM, S::TCOLS, kTmaThreads);
+  }();
+  if (occ <= 0) return -1;
+  const long long nseg = (a.W + kTile - 1) / kTile;
+  const long long slots = (long long)sms * occ;
+  const long long total_rows = (long long)a.n * nseg * a.H;
+  int rows = (int)((total_rows + slots - 1) / slots);
+  if (rows < 1) rows = 1;
+  const long long items = (long long)a.n * nseg * ((a.H + rows - 1) / rows);
+  const int grid = (int)(items < slots ? items : slots);
+  k<<<grid, kTmaThreads, S::SMEM, s>>>(a, rows, err, map);
+  ++g_launches;
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
 template <int CI, int CO>
 constexpr bool up_pair() {
   return (CI == 64 && CO == 64) || (CI == 64 && CO == 32) || (CI == 32 && CO == 16);
@@ -403,12 +643,14 @@ constexpr bool relu_pair() {
 // gradient masked by the ReLU output for ReLU layers
 template <int CI, int CO>
 int dispatch_pair(const ConvArgs& a, bool ups, bool bwd, bool mask, int sms, int* err,
-                  cudaStream_t s) {
+                  const CUtensorMap* map, cudaStream_t s) {
   if (!bwd) {
     if constexpr (up_pair<CI, CO>())
       if (ups) return launch_tc<CI, CO, true, false, true, false>(a, sms, err, s);
-    if constexpr (relu_pair<CI, CO>())
+    if constexpr (relu_pair<CI, CO>()) {
+      if (!ups && map) return launch_tma<CI, CO>(a, sms, err, map, s);
       if (!ups) return launch_tc<CI, CO, false, false, false, true>(a, sms, err, s);
+    }
     return -1;
   }
   if constexpr (relu_pair<CO, CI>())
@@ -421,13 +663,51 @@ int dispatch_pair(const ConvArgs& a, bool ups, bool bwd, bool mask, int sms, int
 }  // namespace
 
 int conv_tc(int cin, int cout, const ConvArgs& a, bool ups, bool bwd, bool mask, int sms,
-            int* err, cudaStream_t s) {
+            int* err, const CUtensorMap* map, cudaStream_t s) {
 #define SCF_TC(CI, CO) \
-  if (cin == CI && cout == CO) return dispatch_pair<CI, CO>(a, ups, bwd, mask, sms, err, s);
+  if (cin == CI && cout == CO) return dispatch_pair<CI, CO>(a, ups, bwd, mask, sms, err, map, s);
   SCF_TC(16, 16) SCF_TC(16, 32) SCF_TC(32, 16) SCF_TC(32, 32) SCF_TC(32, 64) SCF_TC(64, 32)
   SCF_TC(64, 64)
 #undef SCF_TC
   return -1;
+}
+
+namespace {
+typedef CUresult (*EncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                             const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                             const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                             CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeFn encoder() {
+  static EncodeFn fn = [] {
+    void* q = nullptr;
+    cudaDriverEntryPointQueryResult r = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &q, 12000, cudaEnableDefault,
+                                         &r) != cudaSuccess ||
+        r != cudaDriverEntryPointSuccess)
+      return (EncodeFn) nullptr;
+    return reinterpret_cast<EncodeFn>(q);
+  }();
+  return fn;
+}
+}  // namespace
+
+int conv_tma_map(CUtensorMap* m, const void* in, int n, int H, int W, int cin) {
+  EncodeFn fn = encoder();
+  if (!fn || (reinterpret_cast<uintptr_t>(in) & 15) || cin % 16 || W < 1 || H < 1 || n < 1)
+    return -1;
+  const cuuint64_t e = 2;  // BF16
+  // (8 channels, pixel, channel group, row, image)
+  const cuuint64_t dims[5] = {8, (cuuint64_t)W, (cuuint64_t)(cin / 8), (cuuint64_t)H,
+                              (cuuint64_t)n};
+  const cuuint64_t strides[4] = {(cuuint64_t)cin * e, 16, (cuuint64_t)W * cin * e,
+                                 (cuuint64_t)H * W * cin * e};
+  const cuuint32_t box[5] = {8, (cuuint32_t)kTmaPix, (cuuint32_t)(cin / 8), 1, 1};
+  const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(in), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS
+             ? 0
+             : -1;
 }
 
 }  // namespace scf

@@ -1,7 +1,7 @@
 """The network's 3x3 convolutions on the tcgen05 tensor cores (TMEM
 accumulators) against a float64 reference computed from the same BF16
-operands, and against the mma.sync kernels, through the C-ABI
-scf_unet_conv.  Every variant the network launches: forward with ReLU,
+operands, against the mma.sync kernels, and with TMA-staged against
+thread-staged input rows, through the C-ABI scf_unet_conv.  Every variant the network launches: forward with ReLU,
 forward with nearest upsampling and the skip add, and the input gradient
 with and without the ReLU mask; shapes with ragged 128-pixel segments,
 rows narrower than a segment and several segments per row."""
@@ -106,6 +106,21 @@ def test_tcgen05_conv_matches_mma_sync_kernel(cuda, kind, ch):
     assert np.all(d <= 2.0 ** -7 * np.maximum(np.abs(g0), np.abs(g1)) + 1e-4 * np.abs(g0).max())
 
 
+@pytest.mark.parametrize("ch", FWD_RELU, ids=[f"{c[0]}x{c[1]}" for c in FWD_RELU])
+def test_tma_staged_rows_match_thread_staged_rows(cuda, ch):
+    """Engine 1 stages the forward ReLU layers' input rows by TMA, engine 2
+    with the CTA's threads: the same MMAs on the same shared-memory layout,
+    so the outputs agree bit for bit (rows of 40, 136 and 256 pixels, a
+    column of images taller than a tile strip)."""
+    import torch
+    cin, cout = ch
+    for (n, H, W) in [(2, 6, 40), (1, 5, 136), (2, 34, 256)]:
+        g1, ref = _run(torch, 1, "relu", cin, cout, n, H, W, seed=cin + cout)
+        g2, _ = _run(torch, 2, "relu", cin, cout, n, H, W, seed=cin + cout)
+        _check(g1, ref)
+        assert np.array_equal(g1, g2)
+
+
 def test_network_forward_same_on_both_engines(cuda):
     from simcoflow_gb300 import learned as Lr
     rng = np.random.Generator(np.random.PCG64(2))
@@ -117,9 +132,12 @@ def test_network_forward_same_on_both_engines(cuda):
         net.set_params(p)
         net.set_input(x5)
         z1 = net.forward()
-        assert Lr.lib().scf_unet_set_engine(net._h, 0) == 0
+        net.set_engine(2)
+        z2 = net.forward()
+        net.set_engine(0)
         z0 = net.forward()
     finally:
         net.close()
     assert np.isfinite(z1).all()
+    assert np.array_equal(z1, z2)  # TMA or thread staging: the same MMAs
     assert np.linalg.norm(z1 - z0) <= 2e-2 * np.linalg.norm(z0)
