@@ -355,7 +355,8 @@ __global__ void __launch_bounds__(kTile) k_conv_tc(ConvArgs p, int rows, int* er
 // the threads do no staging at all; they only run the epilogue.
 constexpr int kTmaSlots = 5;
 constexpr int kTmaPix = 130;
-constexpr int kTmaThreads = 256;  // two warps per TMEM lane quadrant
+constexpr int kTmaDrain = 256;                  // epilogue: two warps per TMEM lane quadrant
+constexpr int kTmaThreads = kTmaDrain + 32;     // + the warp that copies rows and issues MMAs
 
 template <int CIN, int COUT>
 struct TmaShape {
@@ -368,8 +369,11 @@ struct TmaShape {
   static constexpr int WB = 9 * TAPB;
   static constexpr int OFF_RING = (WB + 127) / 128 * 128;
   static constexpr int OFF_BIAS = OFF_RING + kTmaSlots * ROWB;
-  static constexpr int OFF_BAR = OFF_BIAS + COUT * 4;  // two MMA barriers, then one per slot
-  static constexpr int SMEM = 128 + OFF_BAR + 8 * (2 + kTmaSlots) + 16;
+  // barriers: full[2] (MMAs of an accumulator done), empty[2] (accumulator
+  // drained), one per ring slot (row arrived); then the TMEM address and the
+  // abort flag
+  static constexpr int OFF_BAR = OFF_BIAS + COUT * 4;
+  static constexpr int SMEM = 128 + OFF_BAR + 8 * (4 + kTmaSlots) + 16;
   // two accumulators of COUT FP32 columns
   static constexpr unsigned TCOLS = COUT <= 16 ? 32u : COUT <= 32 ? 64u : 128u;
   static constexpr int HALF = COUT / 2;  // columns drained by one warp
@@ -397,11 +401,30 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
       : "r"(taddr));
 }
 
-// Per tile y (accumulator buf): thread 0 issues the next tile's MMAs into the
-// other accumulator (its three rows have arrived) and the copy of row y+3,
-// then every warp waits for tile y's MMAs and drains its quarter of the
-// pixels and half of the channels of accumulator buf -- the tensor core
-// works on tile y+1 meanwhile.
+// One waits on an mbarrier phase, bounded, giving up early once another
+// thread of the CTA has raised the abort flag; a wait that runs out raises it.
+__device__ __forceinline__ bool wait_or_abort(uint64_t* bar, unsigned parity,
+                                              volatile int* abort) {
+  for (int i = 0; i < kSpins; ++i) {
+    if (bar_try_wait(bar, parity)) return true;
+    if (*abort) return false;
+  }
+  *abort = 1;
+  return false;
+}
+__device__ __forceinline__ void bar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(bar)) : "memory");
+}
+
+// Warp roles.  Warp 8 (one thread) copies the rows by TMA and issues the MMAs
+// of tile y into accumulator y mod 2 as soon as the accumulator is drained
+// (its `empty` barrier) and the rows have arrived, then commits them to the
+// accumulator's `full` barrier; warps 0-7 wait on `full`, drain their
+// quarter of the pixels and half of the channels, and arrive on `empty`.
+// Both roles walk the same items and tiles, so the tensor core runs tile
+// y+1 while the epilogue drains tile y, and no block-wide barrier sits in
+// the loop.  A row goes into the slot of the row three below it once the
+// MMAs that read that row (tile y-1) are done.
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(kTmaThreads) k_conv_tma(ConvArgs p, int rows, int* err,
                                                           const CUtensorMap* map) {
@@ -411,11 +434,12 @@ __global__ void __launch_bounds__(kTmaThreads) k_conv_tma(ConvArgs p, int rows, 
   unsigned char* sm = tm_raw + ((128u - (saddr(tm_raw) & 127u)) & 127u);
   unsigned char* ring = sm + S::OFF_RING;
   float* bias = reinterpret_cast<float*>(sm + S::OFF_BIAS);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + S::OFF_BAR);  // MMA completion, per accumulator
-  uint64_t* rbar = bar + 2;                                      // row arrival, per slot
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + S::OFF_BAR);
+  uint64_t* empty = full + 2;
+  uint64_t* rbar = full + 4;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(rbar + kTmaSlots);
+  volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const int quad = warp & 3, half = warp >> 2;  // TMEM lanes 32 quad .. , columns half * HALF ..
 
   for (int i = t; i < COUT * 9 * KC; i += kTmaThreads) {
     const int co = i % COUT, c = (i / COUT) % KC, tap = i / (COUT * KC);
@@ -425,9 +449,12 @@ __global__ void __launch_bounds__(kTmaThreads) k_conv_tma(ConvArgs p, int rows, 
   if (t < COUT) bias[t] = p.bias ? p.bias[t] : 0.0f;
   if (warp == 0) tmem_alloc(tslot, S::TCOLS);
   if (t == 0) {
-    bar_init(bar, 1);
-    bar_init(bar + 1, 1);
+    for (int k = 0; k < 2; ++k) {
+      bar_init(full + k, 1);
+      bar_init(empty + k, kTmaDrain / 32);  // one arrival per draining warp
+    }
     for (int k = 0; k < kTmaSlots; ++k) bar_init(rbar + k, 1);
+    *abort = 0;
   }
   fence_async_smem();
   tc_fence_before();
@@ -438,115 +465,133 @@ __global__ void __launch_bounds__(kTmaThreads) k_conv_tma(ConvArgs p, int rows, 
   const int H = p.H, W = p.W;
   const int nseg = (W + kTile - 1) / kTile, chunks = (H + rows - 1) / rows;
   const int items = p.n * nseg * chunks;
-  const unsigned abase = saddr(ring), wbase = saddr(sm);
-  constexpr uint32_t IDESC = idesc_bf16_m128<COUT>();
-  // per accumulator: the parity of its next commit; thread 0: its commits not
-  // yet waited for
-  unsigned phases = 0u, pend = 0u;
-  // thread 0: the parity of each slot's next arrival, slots with a copy in flight
-  unsigned rphase = 0u, rpend = 0u;
-  bool ok = true;
-  auto slot_of = [](int yy) { return (yy + 1) % kTmaSlots; };
-  auto fetch = [&](int img, int x0, int yy) {  // thread 0
-    const int s = slot_of(yy);
-    bar_expect_tx(rbar + s, (unsigned)S::ROW_BYTES);
-    tma_row(ring + s * S::ROWB, map, x0 - 1, yy, img, rbar + s);
-    rpend |= 1u << s;
-  };
-  auto arrived = [&](int yy) -> bool {  // thread 0, bounded
-    const int s = slot_of(yy);
-    if (!bar_wait_bounded(rbar + s, (rphase >> s) & 1u)) return false;
-    rphase ^= 1u << s;
-    rpend &= ~(1u << s);
-    return true;
-  };
-  auto issue = [&](int y, int buf) {  // thread 0: the MMAs of tile y
-    tc_fence_after();
-    const int s0 = slot_of(y - 1);
-#pragma unroll
-    for (int tap = 0; tap < 9; ++tap) {
-      const int dy = tap / 3, dx = tap % 3;
-      const int slot = s0 + dy < kTmaSlots ? s0 + dy : s0 + dy - kTmaSlots;
-      const unsigned arow = abase + slot * S::ROWB + dx * 16;
-      const unsigned btap = wbase + tap * S::TAPB;
-#pragma unroll
-      for (int ks = 0; ks < CIN / 16; ++ks) {
-        const uint64_t a = sdesc(arow + 2 * ks * S::LBO_A, S::LBO_A, 128);
-        const uint64_t b = sdesc(btap + 2 * ks * S::LBO_B, S::LBO_B, 128);
-        mma_bf16(tmem + buf * COUT, a, b, IDESC, (tap | ks) != 0);
-      }
-    }
-  };
 
-  for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
-    const int ch = item % chunks, seg = (item / chunks) % nseg, img = item / (chunks * nseg);
-    const int x0 = seg * kTile, ya = ch * rows, yb = min(H, ya + rows);
-    bool rows_ok = true;
-    if (t == 0) {  // rows ya-1 .. yb are needed; the first four fetched up front
-      for (int yy = ya - 1; yy <= ya + 2 && yy <= yb; ++yy) fetch(img, x0, yy);
-      rows_ok = arrived(ya - 1) && arrived(ya) && arrived(ya + 1);
-      if (rows_ok) issue(ya, 0);
-      mma_commit(bar);  // arrives at once when no MMA was issued
-      pend |= 1u;
-    }
-    for (int y = ya; y < yb; ++y) {
-      const int buf = (y - ya) & 1;
-      if (t == 0 && rows_ok && y + 1 < yb) {
-        // tile y+1 into the other accumulator, drained by tile y-1
-        rows_ok = arrived(y + 2);
-        if (rows_ok) {
-          issue(y + 1, buf ^ 1);
-          mma_commit(bar + (buf ^ 1));
-          pend |= 1u << (buf ^ 1);
-          // row y+3 into the slot of row y-2, read by no MMA in flight
+  if (warp == kTmaDrain / 32) {
+    if (lane == 0) {  // ---- rows and MMAs ----
+      const unsigned abase = saddr(ring), wbase = saddr(sm);
+      constexpr uint32_t IDESC = idesc_bf16_m128<COUT>();
+      unsigned rphase = 0u, rpend = 0u;  // per slot: next arrival parity, copy in flight
+      unsigned fphase = 0u, ephase = 0u, fpend = 0u;  // per accumulator
+      unsigned used = 0u;  // per accumulator: held a tile before
+      int tile = 0;        // tiles issued by this CTA (accumulator = tile & 1)
+      auto slot_of = [](int yy) { return (yy + 1) % kTmaSlots; };
+      auto fetch = [&](int img, int x0, int yy) {
+        const int s = slot_of(yy);
+        bar_expect_tx(rbar + s, (unsigned)S::ROW_BYTES);
+        tma_row(ring + s * S::ROWB, map, x0 - 1, yy, img, rbar + s);
+        rpend |= 1u << s;
+      };
+      auto arrived = [&](int yy) -> bool {
+        const int s = slot_of(yy);
+        if (!wait_or_abort(rbar + s, (rphase >> s) & 1u, abort)) return false;
+        rphase ^= 1u << s;
+        rpend &= ~(1u << s);
+        return true;
+      };
+      // the MMAs committed to accumulator b are done (every commit is waited
+      // for, in order, so the parities stay in step)
+      auto retire = [&](int b) -> bool {
+        if (!((fpend >> b) & 1u)) return true;
+        if (!wait_or_abort(full + b, (fphase >> b) & 1u, abort)) return false;
+        fphase ^= 1u << b;
+        fpend &= ~(1u << b);
+        return true;
+      };
+      bool go = true;
+      for (int item = blockIdx.x; item < items && go; item += gridDim.x) {
+        const int ch = item % chunks, seg = (item / chunks) % nseg, img = item / (chunks * nseg);
+        const int x0 = seg * kTile, ya = ch * rows, yb = min(H, ya + rows);
+        for (int yy = ya - 1; yy <= ya + 2 && yy <= yb; ++yy) fetch(img, x0, yy);
+        go = arrived(ya - 1) && arrived(ya);
+        for (int y = ya; y < yb && go; ++y, ++tile) {
+          const int b = tile & 1;
+          if (!arrived(y + 1)) { go = false; break; }
+          if ((used >> b) & 1u) {  // the epilogue has drained this accumulator
+            if (!wait_or_abort(empty + b, (ephase >> b) & 1u, abort)) { go = false; break; }
+            ephase ^= 1u << b;
+          }
+          tc_fence_after();
+          const int s0 = slot_of(y - 1);
+#pragma unroll
+          for (int tap = 0; tap < 9; ++tap) {
+            const int dy = tap / 3, dx = tap % 3;
+            const int slot = s0 + dy < kTmaSlots ? s0 + dy : s0 + dy - kTmaSlots;
+            const unsigned arow = abase + slot * S::ROWB + dx * 16;
+            const unsigned btap = wbase + tap * S::TAPB;
+#pragma unroll
+            for (int ks = 0; ks < CIN / 16; ++ks) {
+              const uint64_t a = sdesc(arow + 2 * ks * S::LBO_A, S::LBO_A, 128);
+              const uint64_t bb = sdesc(btap + 2 * ks * S::LBO_B, S::LBO_B, 128);
+              mma_bf16(tmem + b * COUT, a, bb, IDESC, (tap | ks) != 0);
+            }
+          }
+          mma_commit(full + b);
+          used |= 1u << b;
+          fpend |= 1u << b;
+          // tile y-1's MMAs (queued ahead of these) done: rows up to y-2 are
+          // free, and row y+3 takes the slot of row y-2
+          if (!retire(b ^ 1)) { go = false; break; }
           if (y + 3 <= yb) fetch(img, x0, y + 3);
         }
+        // the item's last MMAs are done before the next item refills the slots
+        if (go) go = retire(0) && retire(1);
       }
-      const bool got = bar_wait_bounded(bar + buf, (phases >> buf) & 1u);
-      if (!__syncthreads_and(got && rows_ok)) {
-        ok = false;
-        break;
+      if (!go) {
+        *abort = 1;
+        atomicExch(err, 1);
+        // let the copies and MMAs in flight land (bounded) before the memory goes
+        for (int s = 0; s < kTmaSlots; ++s)
+          if ((rpend >> s) & 1u) bar_wait_bounded(rbar + s, (rphase >> s) & 1u);
+        for (int b = 0; b < 2; ++b)
+          if ((fpend >> b) & 1u) bar_wait_bounded(full + b, (fphase >> b) & 1u);
       }
-      phases ^= 1u << buf;
-      pend &= ~(1u << buf);
-      tc_fence_after();
-      uint32_t r[HALF];
-      const uint32_t ta = tmem + ((uint32_t)(quad * 32) << 16) + buf * COUT + half * HALF;
-      if constexpr (HALF == 8) {
-        tmem_ld8(ta, *reinterpret_cast<uint32_t(*)[8]>(&r[0]));
-      } else {
+    }
+  } else {  // ---- epilogue: warps 0-7 ----
+    const int quad = warp & 3, half = warp >> 2;  // TMEM lanes 32 quad .., columns half * HALF ..
+    float bv[HALF];
 #pragma unroll
-        for (int j = 0; j < HALF / 16; ++j)
-          tmem_ld16(ta + j * 16, *reinterpret_cast<uint32_t(*)[16]>(&r[j * 16]));
-      }
-      tmem_wait_ld();
-      const int x = x0 + quad * 32 + lane;
-      if (x < W) {
-        const size_t off = (((size_t)img * H + y) * W + x) * COUT + half * HALF;
+    for (int k = 0; k < HALF; ++k) bv[k] = bias[half * HALF + k];
+    unsigned fphase = 0u;
+    int tile = 0;
+    bool go = true;
+    for (int item = blockIdx.x; item < items && go; item += gridDim.x) {
+      const int ch = item % chunks, seg = (item / chunks) % nseg, img = item / (chunks * nseg);
+      const int x0 = seg * kTile, ya = ch * rows, yb = min(H, ya + rows);
+      for (int y = ya; y < yb; ++y, ++tile) {
+        const int b = tile & 1;
+        if (!wait_or_abort(full + b, (fphase >> b) & 1u, abort)) { go = false; break; }
+        fphase ^= 1u << b;
+        tc_fence_after();
+        uint32_t r[HALF];
+        const uint32_t ta = tmem + ((uint32_t)(quad * 32) << 16) + b * COUT + half * HALF;
+        if constexpr (HALF == 8) {
+          tmem_ld8(ta, *reinterpret_cast<uint32_t(*)[8]>(&r[0]));
+        } else {
 #pragma unroll
-        for (int g = 0; g < HALF / 8; ++g) {
-          float f[8];
+          for (int j = 0; j < HALF / 16; ++j)
+            tmem_ld16(ta + j * 16, *reinterpret_cast<uint32_t(*)[16]>(&r[j * 16]));
+        }
+        tmem_wait_ld();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) bar_arrive(empty + b);  // the accumulator is free again
+        const int x = x0 + quad * 32 + lane;
+        if (x < W) {
+          const size_t off = (((size_t)img * H + y) * W + x) * COUT + half * HALF;
 #pragma unroll
-          for (int k = 0; k < 8; ++k)
-            f[k] = fmaxf(__uint_as_float(r[g * 8 + k]) + bias[half * HALF + g * 8 + k], 0.0f);
-          uint4 o;
-          bf162* ob = reinterpret_cast<bf162*>(&o);
+          for (int g = 0; g < HALF / 8; ++g) {
+            uint4 o;
+            bf162* ob = reinterpret_cast<bf162*>(&o);
 #pragma unroll
-          for (int k = 0; k < 4; ++k) ob[k] = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
-          *(reinterpret_cast<uint4*>(p.out + off) + g) = o;
+            for (int k = 0; k < 4; ++k)
+              ob[k] = __floats2bfloat162_rn(
+                  fmaxf(__uint_as_float(r[g * 8 + 2 * k]) + bv[g * 8 + 2 * k], 0.0f),
+                  fmaxf(__uint_as_float(r[g * 8 + 2 * k + 1]) + bv[g * 8 + 2 * k + 1], 0.0f));
+            *(reinterpret_cast<uint4*>(p.out + off) + g) = o;
+          }
         }
       }
-      tc_fence_before();
-      __syncthreads();  // accumulator buf drained before tile y+2's MMAs
     }
-  }
-  if (!ok && t == 0) {
-    atomicExch(err, 1);
-    // let the copies and MMAs in flight land (bounded) before the memory goes
-    for (int s = 0; s < kTmaSlots; ++s)
-      if ((rpend >> s) & 1u) bar_wait_bounded(rbar + s, (rphase >> s) & 1u);
-    if (pend & 1u) bar_wait_bounded(bar, phases & 1u);
-    if (pend & 2u) bar_wait_bounded(bar + 1, (phases >> 1) & 1u);
   }
   tc_fence_before();
   __syncthreads();
@@ -648,7 +693,10 @@ int dispatch_pair(const ConvArgs& a, bool ups, bool bwd, bool mask, int sms, int
     if constexpr (up_pair<CI, CO>())
       if (ups) return launch_tc<CI, CO, true, false, true, false>(a, sms, err, s);
     if constexpr (relu_pair<CI, CO>()) {
-      if (!ups && map) return launch_tma<CI, CO>(a, sms, err, map, s);
+      // 16 -> 16: nine small MMAs per tile, so the warp roles' hand-offs
+      // cost more than the thread staging they replace (measured)
+      if constexpr (CI > 16 || CO > 16)
+        if (!ups && map) return launch_tma<CI, CO>(a, sms, err, map, s);
       if (!ups) return launch_tc<CI, CO, false, false, false, true>(a, sms, err, s);
     }
     return -1;
