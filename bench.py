@@ -651,6 +651,35 @@ def extra_momentum(case, local, args):
         out["cpu"] = {"ms_u_plus_v": round(cpu_ms, 1), "cores": threads, "kind": "port",
                       "iters": its, "sample": "one u and one v solve (C restatement, OpenMP)"}
         out["speedup_vs_cpu"] = round(cpu_ms / ms, 1)
+    # the multigrid preconditioner (SCF_MOM_MG) against the diagonal: on this
+    # workload (Re 1e5) and where diffusion dominates (Re 0.01, the u solve)
+    mg = {}
+    for rey, comps in ((1.0e5, ("u", "v")), (0.01, ("u",))):
+        mi_r = {c: synth.momentum_inputs(case, c, rey=rey) for c in comps}
+        for prec in ("diagonal", "multigrid"):
+            sm = M.MomentumSolver(case.nx, case.ny, device_ptrs=True, device=local,
+                                  mg=prec == "multigrid")
+            try:
+                ti = {c: {k: (T(v) if isinstance(v, np.ndarray) else v) for k, v in mi.items()}
+                      for c, mi in mi_r.items()}
+                best, sts = None, []
+                for rep in range(3):
+                    sts = []
+                    w = {c: (T(mi["pred"]), T(mi["Dp"])) for c, mi in mi_r.items()}
+                    torch.cuda.synchronize(dev)
+                    t0 = time.perf_counter()
+                    for c in comps:
+                        sts.append(sm.solve(c, ti[c], w[c][0], w[c][1], rtol=1e-10,
+                                            maxit=20000))
+                    torch.cuda.synchronize(dev)
+                    ms_r = (time.perf_counter() - t0) * 1e3
+                    best = ms_r if best is None else min(best, ms_r)
+            finally:
+                sm.close()
+            mg[f"re_{rey:g}_{prec}"] = {"components": list(comps), "ms": round(best, 2),
+                                        "iters": [st.iters for st in sts],
+                                        "relres": [st.relres for st in sts]}
+    out["preconditioners_rtol_1e-10"] = mg
     return out
 
 

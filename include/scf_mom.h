@@ -10,8 +10,8 @@
  *                                  for v, boundary terms)
  *   SetBasicSolver + HYPRE PCG/BoomerAMG (:507-513, :530-536, :588-620)
  *                                  replaced by FP64 BiCGStab with a diagonal
- *                                  preconditioner to rtol (the operator is not
- *                                  symmetric)
+ *                                  or a multigrid (SCF_MOM_MG) preconditioner
+ *                                  to rtol (the operator is not symmetric)
  *   DeltaGetValues     (:847-885)  solution scattered to the cells
  *   Pred += dt GradP / dx / dy     (:517-522, :540-545)
  *   Dp boundary copies (:552-562) and, for v, the open top of
@@ -51,7 +51,18 @@ typedef struct scf_mom_in {
 
 typedef struct scf_mom scf_mom;
 
-/* flags: 0 or SCF_FLAG_DEVICE_PTRS */
+/* Multigrid preconditioner for the BiCGStab solve (creation flag): one FP64
+ * V-cycle (red-black Gauss-Seidel, 2 + 2 sweeps, Galerkin aggregation
+ * coarsening, coarse correction weighted 1.9, dense coarsest solve) on the
+ * symmetric part of the operator per preconditioner application, on the
+ * right, in place of the diagonal.
+ * The reference preconditions these solves with BoomerAMG
+ * (src/PredictorUV_mod.f90:588-620); the diagonal suffices where dx dy / dt
+ * dominates the operator (high Reynolds numbers, small time steps), the
+ * multigrid where diffusion does. */
+#define SCF_MOM_MG 4
+
+/* flags: SCF_FLAG_DEVICE_PTRS, SCF_MOM_MG, or 0 */
 int scf_mom_create(scf_mom **h, int nx, int ny, int flags, int device);
 void scf_mom_destroy(scf_mom *h);
 /* stream for all work of the handle (cudaStream_t; NULL: the handle's own) */

@@ -21,6 +21,7 @@
 
 #include "../../include/scf_mom.h"
 #include "scf_internal.cuh"
+#include "scf_mgpre.cuh"
 
 namespace scf {
 namespace {
@@ -373,6 +374,95 @@ k_mom_xr(MomOp M, double* x, double* r, const double* rh, const double* y, const
   }
 }
 
+// BiCGStab with a multigrid preconditioner on the right (the projection's
+// FP64 V-cycle on the operator's symmetric part, scf_mgpre.cuh): the same
+// recurrences as k_mom_pv / k_mom_st / k_mom_xr, with y = M^-1 p and
+// z = M^-1 s coming from V-cycles between these kernels instead of the
+// diagonal scaling inside them.  One thread per cell, grid-stride rows.
+__device__ __forceinline__ double apply5(const MomOp& M, const double* y, size_t g) {
+  double v = M.P[g] * y[g];
+  v = fma(M.W[g], y[g - 1], v);
+  v = fma(M.E[g], y[g + 1], v);
+  v = fma(M.S[g], y[g - M.pitch], v);
+  return fma(M.N[g], y[g + M.pitch], v);
+}
+
+// p = r + beta (p_old - omega v_old)
+__global__ void k_momg_p(MomOp M, const double* r, const double* pold, const double* vold,
+                         double* pnew, const MomScalars* sc) {
+  pdl_wait();
+  if (sc->done) return;
+  const double beta = (sc->rho1 / sc->rho) * (sc->alpha / sc->omega), om = sc->omega;
+  const int ix = blockIdx.x * 32 + threadIdx.x;
+  if (ix >= M.nx) return;
+  for (int iy = blockIdx.y * 8 + threadIdx.y; iy < M.ny; iy += gridDim.y * 8) {
+    const size_t g = (size_t)iy * M.pitch + ix;
+    pnew[g] = fma(beta, fma(-om, vold[g], pold[g]), r[g]);
+  }
+}
+
+// v = A y, alpha = rho1 / (r^, v)
+__global__ void k_momg_av(MomOp M, const double* y, double* v, const double* rh, MomScalars* sc,
+                          double* part) {
+  pdl_wait();
+  if (sc->done) return;
+  double acc = 0.0;
+  const int ix = blockIdx.x * 32 + threadIdx.x;
+  if (ix < M.nx)
+    for (int iy = blockIdx.y * 8 + threadIdx.y; iy < M.ny; iy += gridDim.y * 8) {
+      const size_t g = (size_t)iy * M.pitch + ix;
+      const double vv = apply5(M, y, g);
+      v[g] = vv;
+      acc = fma(rh[g], vv, acc);
+    }
+  double tot, dummy;
+  if (gsum2(acc, 0.0, part, &sc->tickets[1], &tot, &dummy) && tl() == 0) {
+    sc->rho = sc->rho1;
+    sc->alpha = sc->rho1 / tot;
+    if (!isfinite(sc->alpha)) {
+      sc->status = kErrNaN;
+      sc->done = 1;
+    }
+  }
+}
+
+// s = r - alpha v
+__global__ void k_momg_s(MomOp M, const double* r, const double* v, double* s,
+                         const MomScalars* sc) {
+  pdl_wait();
+  if (sc->done) return;
+  const double alpha = sc->alpha;
+  const int ix = blockIdx.x * 32 + threadIdx.x;
+  if (ix >= M.nx) return;
+  for (int iy = blockIdx.y * 8 + threadIdx.y; iy < M.ny; iy += gridDim.y * 8) {
+    const size_t g = (size_t)iy * M.pitch + ix;
+    s[g] = fma(-alpha, v[g], r[g]);
+  }
+}
+
+// t = A z, omega = (t, s) / (t, t)
+__global__ void k_momg_at(MomOp M, const double* z, double* t, const double* s, MomScalars* sc,
+                          double* part) {
+  pdl_wait();
+  if (sc->done) return;
+  double a1 = 0.0, a2 = 0.0;
+  const int ix = blockIdx.x * 32 + threadIdx.x;
+  if (ix < M.nx)
+    for (int iy = blockIdx.y * 8 + threadIdx.y; iy < M.ny; iy += gridDim.y * 8) {
+      const size_t g = (size_t)iy * M.pitch + ix;
+      const double tv = apply5(M, z, g);
+      t[g] = tv;
+      a1 = fma(tv, s[g], a1);
+      a2 = fma(tv, tv, a2);
+    }
+  double ts, tt;
+  if (gsum2(a1, a2, part, &sc->tickets[2], &ts, &tt) && tl() == 0) {
+    sc->ts = ts;
+    sc->tt = tt;
+    sc->omega = tt > 0.0 ? ts / tt : 0.0;
+  }
+}
+
 // DeltaGetValues + the gradient update of the component's cells
 __global__ void k_mom_pred(MomIn in, int iu, int iv, int nx, int ny, int pitch, const double* x,
                            double* pred) {
@@ -436,6 +526,7 @@ struct scf_mom {
   double *st_pred = nullptr, *st_Dp = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   bool solved = false;
+  scf_proj* mg = nullptr;  // SCF_MOM_MG: multigrid preconditioner (a projection handle)
 };
 
 namespace {
@@ -467,6 +558,8 @@ int padded(scf_mom* h, double** base) {
 }
 
 void free_all(scf_mom* h) {
+  if (h->mg) scf_proj_destroy(h->mg);
+  h->mg = nullptr;
   for (void* p : h->allocs) cudaFree(p);
   h->allocs.clear();
   if (h->sc_host) cudaFreeHost(h->sc_host);
@@ -526,6 +619,7 @@ int scf_mom_create(scf_mom** out, int nx, int ny, int flags, int device) {
   }
   if (cudaEventCreate(&h->ev[0]) != cudaSuccess || cudaEventCreate(&h->ev[1]) != cudaSuccess)
     return fail(SCF_ERR_CUDA);
+  if ((flags & SCF_MOM_MG) && (rc = mgpre_create(&h->mg, nx, ny, device))) return fail(rc);
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) return fail(SCF_ERR_CUDA);
   *out = h;
   return SCF_OK;
@@ -615,14 +709,32 @@ int scf_mom_solve(scf_mom* h, int comp, const scf_mom_in* in, double* pred, doub
   MCK(cudaMemcpyAsync(h->sc_host, h->sc, sizeof(MomScalars), cudaMemcpyDeviceToHost, s));
   MCK(cudaStreamSynchronize(s));
   // the start was written with maxit from init; keep the host copy's limits
+  if (h->mg) {  // the multigrid on this operator's symmetric part
+    const int rc = mgpre_setup(h->mg, h->op.P, h->op.W, h->op.E, h->op.S, h->op.N, s);
+    if (rc) return rc;
+  }
   while (!h->sc_host->done && it < maxit) {
     for (int c = 0; c < 4 && it < maxit; ++c, ++it) {
       const int nxt = cur ^ 1;
-      launch_k(k_mom_pv, tg, dim3(NTM), 0, s, h->op, (const double*)h->r, (const double*)h->rh,
-               (const double*)h->p[cur], h->p[nxt], (const double*)h->v[cur], h->v[nxt], h->y,
-               h->sc, h->part);
-      launch_k(k_mom_st, tg, dim3(NTM), 0, s, h->op, (const double*)h->r,
-               (const double*)h->v[nxt], h->s, h->z, h->t, h->sc, h->part);
+      if (h->mg) {
+        launch_k(k_momg_p, rg, blk, 0, s, h->op, (const double*)h->r, (const double*)h->p[cur],
+                 (const double*)h->v[cur], h->p[nxt], (const MomScalars*)h->sc);
+        int rc = mgpre_apply(h->mg, h->p[nxt], h->y, s);
+        if (rc) return rc;
+        launch_k(k_momg_av, rg, blk, 0, s, h->op, (const double*)h->y, h->v[nxt],
+                 (const double*)h->rh, h->sc, h->part);
+        launch_k(k_momg_s, rg, blk, 0, s, h->op, (const double*)h->r, (const double*)h->v[nxt],
+                 h->s, (const MomScalars*)h->sc);
+        if ((rc = mgpre_apply(h->mg, h->s, h->z, s))) return rc;
+        launch_k(k_momg_at, rg, blk, 0, s, h->op, (const double*)h->z, h->t, (const double*)h->s,
+                 h->sc, h->part);
+      } else {
+        launch_k(k_mom_pv, tg, dim3(NTM), 0, s, h->op, (const double*)h->r,
+                 (const double*)h->rh, (const double*)h->p[cur], h->p[nxt],
+                 (const double*)h->v[cur], h->v[nxt], h->y, h->sc, h->part);
+        launch_k(k_mom_st, tg, dim3(NTM), 0, s, h->op, (const double*)h->r,
+                 (const double*)h->v[nxt], h->s, h->z, h->t, h->sc, h->part);
+      }
       launch_k(k_mom_xr, tg, dim3(NTM), 0, s, h->op, h->x, h->r, (const double*)h->rh,
                (const double*)h->y, (const double*)h->z, (const double*)h->s,
                (const double*)h->t, h->sc, h->part);

@@ -21,6 +21,7 @@
 #include "scf_geom_gpu.cuh"
 #include "scf_mg.cuh"
 #include "scf_unet.cuh"
+#include "scf_mgpre.cuh"
 
 using namespace scf;
 
@@ -479,6 +480,31 @@ void enqueue_setup(scf_proj* h, Scalars* sc, cudaStream_t s, bool fork = true) {
       }
     }
   }
+}
+
+// ---- the FP64 multigrid as a preconditioner of another 5-point operator ----
+// Fine level from an external operator: the symmetric part of its couplings
+// (clamped at zero, so every level stays an M-matrix) and its diagonal.
+__global__ void k_mgpre_level0(LevelView L, const double* __restrict__ P,
+                               const double* __restrict__ W, const double* __restrict__ E,
+                               const double* __restrict__ S, const double* __restrict__ N) {
+  const int ix = blockIdx.x * 32 + threadIdx.x;
+  if (ix >= L.nx) return;
+  for (int iy = blockIdx.y * 8 + threadIdx.y; iy < L.ny; iy += gridDim.y * 8) {
+    const size_t g = (size_t)iy * L.pitch + ix;
+    const double d = P[g];
+    L.dg[g] = d > 0.0 ? d : -1.0;
+    L.cE[g] = ix + 1 < L.nx ? fmax(0.0, -0.5 * (E[g] + W[g + 1])) : 0.0;
+    L.cN[g] = iy + 1 < L.ny ? fmax(0.0, -0.5 * (N[g] + S[g + L.pitch])) : 0.0;
+  }
+}
+
+// the hierarchy below the fine level (enqueue_setup without the assembly)
+void enqueue_setup_levels(scf_proj* h, Scalars* sc, cudaStream_t s) {
+  const size_t nl = h->lev.size();
+  launch_excess(h->lev[0], h->di64[0], nullptr, (int)nl, sc, s);
+  for (size_t l = 1; l < nl; ++l) launch_coarsen(h->lev[l - 1], h->lev[l], h->di64[l], s);
+  launch_coarse_setup(h->lev.back(), h->Ainv, h->cmap, h->ncoarse, s);
 }
 
 // transposed levels of the line smoother (allocated once, on first use)
@@ -1916,3 +1942,56 @@ int scf_proj_vcycle(scf_proj* h, const double* b, double* x) {
 }
 
 }  // extern "C"
+
+namespace scf {
+
+int mgpre_create(scf_proj** out, int nx, int ny, int device) {
+  scf_opts o;
+  scf_opts_default(&o);
+  o.precision = SCF_PREC_FP64;
+  o.smoother = SCF_SMOOTH_POINT;
+  o.flags = SCF_FLAG_DEVICE_PTRS | SCF_FLAG_NO_GRAPH;
+  o.device = device;
+  o.npre = 2;
+  o.npost = 2;
+  // aggregation's coarse operator is too stiff for smooth errors, as for the
+  // pressure (measured on the 2048^2 u solve at Re 0.01: 111 BiCGStab
+  // iterations at omega 1.0, 26 at 1.5, 19 at 1.8, 17 at 1.9; 4 at every
+  // omega at Re 1e5)
+  o.omega = 1.9;
+  return scf_proj_create(out, nx, ny, &o);
+}
+
+int mgpre_setup(scf_proj* h, const double* P, const double* W, const double* E,
+                const double* S, const double* N, cudaStream_t s) {
+  if (!h || !P || !W || !E || !S || !N) return SCF_ERR_ARG;
+  CK(cudaSetDevice(h->device));
+  const LevelView& L0 = h->lev[0];
+  launch_k(k_mgpre_level0, grid_for(L0.nx, L0.ny, 1), dim3(32, 8), 0, s, L0, P, W, E, S, N);
+  CK(cudaMemsetAsync(h->sc_diag, 0, sizeof(Scalars), s));
+  enqueue_setup_levels(h, h->sc_diag, s);
+  CK(cudaGetLastError());
+  h->assembled = true;
+  return SCF_OK;
+}
+
+int mgpre_apply(scf_proj* h, double* b, double* z, cudaStream_t s) {
+  if (!h || !b || !z || !h->assembled || h->mixed || h->line) return SCF_ERR_STATE;
+  // the V-cycle reads level 0's b and ends in level 0's final buffer: both
+  // are pointed at the caller's arrays for the duration of the enqueue (the
+  // launches take the views by value)
+  const int zf = final_buf(h, 0);
+  double* const b0 = h->lev[0].b;
+  double** xf = zf == 0 ? &h->lev[0].x : &h->x2_64[0];
+  double* const x0 = *xf;
+  h->lev[0].b = b;
+  *xf = z;
+  CK(cudaMemsetAsync(h->sc_diag, 0, sizeof(Scalars), s));
+  enqueue_vcycle(h, h->sc_diag, false, s);
+  h->lev[0].b = b0;
+  *xf = x0;
+  CK(cudaGetLastError());
+  return SCF_OK;
+}
+
+}  // namespace scf

@@ -33,6 +33,9 @@ ARRAYS = [("dx", "1"), ("dy", "1"), ("posnu", "0"), ("vof", "1"), ("vofS", "1"),
 SCALARS = ["dt", "beta_vis", "nua", "nuw", "nuref", "rey", "fr"]
 
 
+MOM_MG = 4  # scf_mom_create flag: multigrid preconditioner (include/scf_mom.h)
+
+
 class MomIn(C.Structure):
     _fields_ = ([(n, C.c_void_p) for n, _ in ARRAYS] + [(n, C.c_double) for n in SCALARS])
 
@@ -59,11 +62,14 @@ def load():
 class MomentumSolver:
     """Implicit momentum solves on an nx-by-ny grid (a handle of the C-ABI)."""
 
-    def __init__(self, nx: int, ny: int, device_ptrs: bool = False, device: int = 0):
+    def __init__(self, nx: int, ny: int, device_ptrs: bool = False, device: int = 0,
+                 mg: bool = False):
+        """mg: precondition the BiCGStab solves with a multigrid V-cycle
+        (SCF_MOM_MG) instead of the diagonal."""
         self.nx, self.ny, self.device_ptrs = nx, ny, device_ptrs
         self._h = C.c_void_p()
-        P._check(load().scf_mom_create(C.byref(self._h), nx, ny,
-                                       P.FLAG_DEVICE_PTRS if device_ptrs else 0, device),
+        flags = (P.FLAG_DEVICE_PTRS if device_ptrs else 0) | (MOM_MG if mg else 0)
+        P._check(load().scf_mom_create(C.byref(self._h), nx, ny, flags, device),
                  "scf_mom_create")
         self._keep = []
 
@@ -129,9 +135,9 @@ class MomentumSolver:
         return matr, rhm
 
 
-def predict(inputs: dict, rtol: float = 1e-13, maxit: int = 200) -> dict:
+def predict(inputs: dict, rtol: float = 1e-13, maxit: int = 200, mg: bool = False) -> dict:
     """One component's implicit step on host arrays (a fresh handle)."""
-    s = MomentumSolver(inputs["nx"], inputs["ny"])
+    s = MomentumSolver(inputs["nx"], inputs["ny"], mg=mg)
     try:
         pred = inputs["pred"].copy(order="F")
         Dp = inputs["Dp"].copy(order="F")

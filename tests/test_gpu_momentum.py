@@ -89,3 +89,34 @@ def test_zero_rhs_and_bad_arguments(cuda):
             s.solve("u", bad, mi["pred"].copy(order="F"), mi["Dp"].copy(order="F"))
     finally:
         s.close()
+
+
+@pytest.mark.parametrize("comp", ["u", "v"])
+@pytest.mark.parametrize("mk", [lambda: synth.c1(n=96), lambda: synth.c4(n=128, instance=3)],
+                         ids=["c1_96", "c4_128"])
+def test_multigrid_preconditioner_where_diffusion_dominates(cuda, oracle, mk, comp):
+    """Reynolds number 0.01: the viscous couplings outweigh dx dy / dt by
+    about a hundred, the diagonal preconditioner needs hundreds of
+    iterations, the multigrid V-cycle (SCF_MOM_MG) a handful; the same
+    operator bit for bit and the same solution as the oracle's direct solve."""
+    mi = synth.momentum_inputs(mk(), comp, rey=0.01)
+    exp = oracle.mom_predict(mi)
+    mg = M.predict(mi, rtol=1e-13, maxit=100, mg=True)
+    diag = M.predict(mi, rtol=1e-13, maxit=3000)
+    for g in (mg, diag):
+        assert np.array_equal(g["matr"], exp["matr"])
+        assert np.array_equal(g["Dp"], exp["Dp"])
+        assert g["stats"]["status"] == 0
+        assert rel(g["pred"], exp["pred"]) <= 1e-10
+    assert mg["stats"]["iters"] * 5 <= diag["stats"]["iters"]
+
+
+def test_multigrid_preconditioner_on_the_predictor_workload(cuda, oracle):
+    """At the benchmark's Reynolds number the diagonal already converges in
+    a few iterations; the multigrid one matches it and the oracle."""
+    mi = synth.momentum_inputs(synth.c4(n=256, instance=3), "u")
+    exp = oracle.mom_predict(mi)
+    g = M.predict(mi, rtol=1e-14, mg=True)
+    assert np.array_equal(g["matr"], exp["matr"])
+    assert rel(g["pred"], exp["pred"]) <= 1e-11
+    assert g["stats"]["status"] == 0 and g["stats"]["iters"] <= 10
