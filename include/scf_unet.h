@@ -68,7 +68,7 @@ int scf_unet_target(scf_unet *u, int i, int nx, int ny, const double *e, const d
 int scf_unet_set_input(scf_unet *u, const float *x);
 
 /* Convolution engine of the forward pass and the input gradients:
- * 1 = tcgen05 with the forward ReLU layers' input rows staged by TMA
+ * 1 = tcgen05 with the forward layers' input rows staged by TMA
  * (default), 2 = tcgen05 with every input row staged by the CTA's threads,
  * 0 = the mma.sync kernels (comparison only). */
 int scf_unet_set_engine(scf_unet *u, int engine);

@@ -753,11 +753,12 @@ int UNet::create(int n, int h, int w, bool train, int device) {
   {
     std::vector<CUtensorMap> hm(L.size());
     for (size_t i = 0; i < L.size(); ++i) {
-      if (L[i].ups) continue;
       const void* in = i == 0 ? (const void*)in_
                        : (i == 2 || i == 4 || i == 6) ? (const void*)pool_[i / 2 - 1]
                                                       : (const void*)act_[i - 1];
-      has_map_[i] = conv_tma_map(&hm[i], in, n, h >> L[i].level, w >> L[i].level, L[i].cin) == 0;
+      // an upsampling layer's input is the level below (half resolution)
+      const int lv = L[i].level + (L[i].ups ? 1 : 0);
+      has_map_[i] = conv_tma_map(&hm[i], in, n, h >> lv, w >> lv, L[i].cin) == 0;
     }
     if (cudaMemcpy(maps_, hm.data(), L.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice) !=
         cudaSuccess)
@@ -1148,11 +1149,11 @@ int scf_unet_conv(int engine, int cin, int cout, int ups, int bwd, int mask, con
   int* err = nullptr;
   if (cudaMalloc((void**)&err, 4) != cudaSuccess) return -2;
   cudaMemsetAsync(err, 0, 4, s);
-  // forward ReLU layers on engine 1: the input's tensor map for TMA staging
+  // forward layers on engine 1: the input's tensor map for TMA staging
   CUtensorMap* dmap = nullptr;
-  if (engine == 1 && !ups && !bwd) {
+  if (engine == 1 && !bwd) {
     CUtensorMap hm;
-    if (scf::conv_tma_map(&hm, in, n, H, W, cin) == 0 &&
+    if (scf::conv_tma_map(&hm, in, n, ups ? H / 2 : H, ups ? W / 2 : W, cin) == 0 &&
         cudaMalloc((void**)&dmap, sizeof(CUtensorMap)) == cudaSuccess)
       cudaMemcpy(dmap, &hm, sizeof(CUtensorMap), cudaMemcpyHostToDevice);
   }

@@ -28,11 +28,13 @@ struct ConvArgs {
 // wait runs out.  Returns 0, or -1 for a channel pair or variant that the
 // network does not have or a failed launch.
 // map: device copy of the input's tensor map from conv_tma_map, or null.
-// With a map the forward ReLU layers stage their input rows by TMA.
+// With a map the forward layers (ReLU layers of 32 or 64 channels on a side,
+// upsampling layers) stage their input rows by TMA.
 int conv_tc(int cin, int cout, const ConvArgs& a, bool ups, bool bwd, bool mask, int sms,
             int* err, const CUtensorMap* map, cudaStream_t s);
 // Tensor map of an NHWC BF16 tensor [n][H][W][cin] for the TMA-staged
-// convolution (host; 0 on success).
+// convolution (host; 0 on success).  The input of an upsampling layer is
+// mapped with its own (half-resolution) dimensions.
 int conv_tma_map(CUtensorMap* m, const void* in, int n, int H, int W, int cin);
 
 struct UNetLayer {

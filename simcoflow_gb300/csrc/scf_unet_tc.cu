@@ -354,11 +354,12 @@ __global__ void __launch_bounds__(kTile) k_conv_tc(ConvArgs p, int rows, int* er
 // tile y read rows y-1 .. y+1, row y+2 is in flight, row y+3 is issued), so
 // the threads do no staging at all; they only run the epilogue.
 constexpr int kTmaSlots = 5;
+constexpr int kTmaAcc = 4;  // TMEM accumulators per CTA (a power of two)
 constexpr int kTmaPix = 130;
 constexpr int kTmaDrain = 256;                  // epilogue: two warps per TMEM lane quadrant
 constexpr int kTmaThreads = kTmaDrain + 32;     // + the warp that copies rows and issues MMAs
 
-template <int CIN, int COUT>
+template <int CIN, int COUT, int SLOTS = kTmaSlots>
 struct TmaShape {
   static constexpr int KC = CIN / 8;
   static constexpr int LBO_A = kTmaPix * 16;                 // between channel groups
@@ -368,14 +369,15 @@ struct TmaShape {
   static constexpr int TAPB = CIN * COUT * 2;
   static constexpr int WB = 9 * TAPB;
   static constexpr int OFF_RING = (WB + 127) / 128 * 128;
-  static constexpr int OFF_BIAS = OFF_RING + kTmaSlots * ROWB;
-  // barriers: full[2] (MMAs of an accumulator done), empty[2] (accumulator
-  // drained), one per ring slot (row arrived); then the TMEM address and the
-  // abort flag
+  static constexpr int OFF_BIAS = OFF_RING + SLOTS * ROWB;
+  // barriers: full[kTmaAcc] (MMAs of an accumulator done), empty[kTmaAcc]
+  // (accumulator drained), one per ring slot (row arrived); then the TMEM
+  // address and the abort flag
   static constexpr int OFF_BAR = OFF_BIAS + COUT * 4;
-  static constexpr int SMEM = 128 + OFF_BAR + 8 * (4 + kTmaSlots) + 16;
-  // two accumulators of COUT FP32 columns
-  static constexpr unsigned TCOLS = COUT <= 16 ? 32u : COUT <= 32 ? 64u : 128u;
+  static constexpr int SMEM = 128 + OFF_BAR + 8 * (2 * kTmaAcc + kTmaSlots) + 16;
+  // kTmaAcc accumulators of COUT FP32 columns
+  static constexpr unsigned TCOLS = COUT <= 16 ? 64u : COUT <= 32 ? 128u : 256u;
+  static_assert(kTmaAcc * COUT <= (int)TCOLS, "accumulators exceed the allocation");
   static constexpr int HALF = COUT / 2;  // columns drained by one warp
 };
 
@@ -417,26 +419,53 @@ __device__ __forceinline__ void bar_arrive(uint64_t* bar) {
 }
 
 // Warp roles.  Warp 8 (one thread) copies the rows by TMA and issues the MMAs
-// of tile y into accumulator y mod 2 as soon as the accumulator is drained
-// (its `empty` barrier) and the rows have arrived, then commits them to the
-// accumulator's `full` barrier; warps 0-7 wait on `full`, drain their
-// quarter of the pixels and half of the channels, and arrive on `empty`.
-// Both roles walk the same items and tiles, so the tensor core runs tile
-// y+1 while the epilogue drains tile y, and no block-wide barrier sits in
-// the loop.  A row goes into the slot of the row three below it once the
-// MMAs that read that row (tile y-1) are done.
-template <int CIN, int COUT>
-__global__ void __launch_bounds__(kTmaThreads) k_conv_tma(ConvArgs p, int rows, int* err,
-                                                          const CUtensorMap* map) {
-  using S = TmaShape<CIN, COUT>;
+// of tile t into accumulator t mod kTmaAcc (four) as soon as the accumulator
+// is drained (its `empty` barrier) and the rows have arrived, then commits
+// them to the accumulator's `full` barrier; warps 0-7 wait on `full`, drain
+// their quarter of the pixels and half of the channels, and arrive on
+// `empty`.  Both roles walk the same items and tiles, so the tensor core runs
+// up to three tiles ahead of the epilogue, and no block-wide barrier sits in
+// the loop.  The producer waits for MMAs only on a row's first tile: when the
+// previous tile is done, the rows below the current one are free, and the
+// row SLOTS-2 ahead is copied into the slot of the row two behind.
+// UPS (the decoder's first convolutions: nearest upsampling of a
+// half-resolution input, then the skip tensor added, no ReLU): the rows,
+// segments and copies are those of the half-resolution input, and each
+// half-resolution row y gives four tiles, output rows 2y + py and pixels
+// 2x + px of one parity (py, px).  Tap (dy, dx) of output pixel
+// (2y + py, 2x + px) reads the upsampled input at (2y + py - 1 + dy,
+// 2x + px - 1 + dx), which is half-resolution pixel
+// (y + ((py - 1 + dy) >> 1), x + ((px - 1 + dx) >> 1)): a shifted window of the
+// staged rows like the plain convolution's, with the same products summed
+// in the same tap order, and the padding row or column of the upsampled
+// input maps to the padding of the half-resolution one.  Four tiles per row
+// leave time to copy a row one row ahead, so the ring has four slots there
+// (the decoder's 64->32 layer fits two CTAs on an SM), and the epilogue loads
+// the next tile's skip values while it finishes the current one.
+// CTAs per SM that shared memory allows, as the register bound of the
+// kernel: 64-channel layers 1, 32->64 and the 64->32 upsampling 2, 32->32 3,
+// 16->32 and the 32->16 upsampling 4
+constexpr int tma_ctas(int cin, int cout, bool ups) {
+  return (cin == 64 && cout == 64)             ? 1
+         : (cout == 64 || (ups && cin == 64)) ? 2
+         : (cin == 32 && !ups)                ? 3
+                                              : 4;
+}
+
+template <int CIN, int COUT, bool UPS>
+__global__ void __launch_bounds__(kTmaThreads, tma_ctas(CIN, COUT, UPS))
+    k_conv_tma(ConvArgs p, int rows, int* err, const CUtensorMap* map) {
+  constexpr int SLOTS = UPS ? 4 : kTmaSlots;  // ring slots; a row is copied SLOTS-2 rows ahead
+  using S = TmaShape<CIN, COUT, SLOTS>;
   constexpr int KC = S::KC, HALF = S::HALF;
+  constexpr int NSUB = UPS ? 4 : 1;  // tiles per staged row
   extern __shared__ __align__(128) unsigned char tm_raw[];
   unsigned char* sm = tm_raw + ((128u - (saddr(tm_raw) & 127u)) & 127u);
   unsigned char* ring = sm + S::OFF_RING;
   float* bias = reinterpret_cast<float*>(sm + S::OFF_BIAS);
   uint64_t* full = reinterpret_cast<uint64_t*>(sm + S::OFF_BAR);
-  uint64_t* empty = full + 2;
-  uint64_t* rbar = full + 4;
+  uint64_t* empty = full + kTmaAcc;
+  uint64_t* rbar = full + 2 * kTmaAcc;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(rbar + kTmaSlots);
   volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -449,7 +478,7 @@ __global__ void __launch_bounds__(kTmaThreads) k_conv_tma(ConvArgs p, int rows, 
   if (t < COUT) bias[t] = p.bias ? p.bias[t] : 0.0f;
   if (warp == 0) tmem_alloc(tslot, S::TCOLS);
   if (t == 0) {
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < kTmaAcc; ++k) {
       bar_init(full + k, 1);
       bar_init(empty + k, kTmaDrain / 32);  // one arrival per draining warp
     }
@@ -463,7 +492,8 @@ __global__ void __launch_bounds__(kTmaThreads) k_conv_tma(ConvArgs p, int rows, 
   const uint32_t tmem = *tslot;
 
   const int H = p.H, W = p.W;
-  const int nseg = (W + kTile - 1) / kTile, chunks = (H + rows - 1) / rows;
+  const int RH = UPS ? H / 2 : H, RW = UPS ? W / 2 : W;  // the staged rows
+  const int nseg = (RW + kTile - 1) / kTile, chunks = (RH + rows - 1) / rows;
   const int items = p.n * nseg * chunks;
 
   if (warp == kTmaDrain / 32) {
@@ -473,8 +503,8 @@ __global__ void __launch_bounds__(kTmaThreads) k_conv_tma(ConvArgs p, int rows, 
       unsigned rphase = 0u, rpend = 0u;  // per slot: next arrival parity, copy in flight
       unsigned fphase = 0u, ephase = 0u, fpend = 0u;  // per accumulator
       unsigned used = 0u;  // per accumulator: held a tile before
-      int tile = 0;        // tiles issued by this CTA (accumulator = tile & 1)
-      auto slot_of = [](int yy) { return (yy + 1) % kTmaSlots; };
+      int tile = 0;        // tiles issued by this CTA (accumulator = tile mod kTmaAcc)
+      auto slot_of = [](int yy) { return (yy + 1) % SLOTS; };
       auto fetch = [&](int img, int x0, int yy) {
         const int s = slot_of(yy);
         bar_expect_tx(rbar + s, (unsigned)S::ROW_BYTES);
@@ -488,8 +518,9 @@ __global__ void __launch_bounds__(kTmaThreads) k_conv_tma(ConvArgs p, int rows, 
         rpend &= ~(1u << s);
         return true;
       };
-      // the MMAs committed to accumulator b are done (every commit is waited
-      // for, in order, so the parities stay in step)
+      // the MMAs committed to accumulator b are done (every commit is
+      // accounted for once, here or when the epilogue has drained the
+      // accumulator, so the parities stay in step)
       auto retire = [&](int b) -> bool {
         if (!((fpend >> b) & 1u)) return true;
         if (!wait_or_abort(full + b, (fphase >> b) & 1u, abort)) return false;
@@ -500,41 +531,54 @@ __global__ void __launch_bounds__(kTmaThreads) k_conv_tma(ConvArgs p, int rows, 
       bool go = true;
       for (int item = blockIdx.x; item < items && go; item += gridDim.x) {
         const int ch = item % chunks, seg = (item / chunks) % nseg, img = item / (chunks * nseg);
-        const int x0 = seg * kTile, ya = ch * rows, yb = min(H, ya + rows);
-        for (int yy = ya - 1; yy <= ya + 2 && yy <= yb; ++yy) fetch(img, x0, yy);
+        const int x0 = seg * kTile, ya = ch * rows, yb = min(RH, ya + rows);
+        for (int yy = ya - 1; yy <= ya + SLOTS - 3 && yy <= yb; ++yy) fetch(img, x0, yy);
         go = arrived(ya - 1) && arrived(ya);
-        for (int y = ya; y < yb && go; ++y, ++tile) {
-          const int b = tile & 1;
+        for (int y = ya; y < yb && go; ++y) {
           if (!arrived(y + 1)) { go = false; break; }
-          if ((used >> b) & 1u) {  // the epilogue has drained this accumulator
-            if (!wait_or_abort(empty + b, (ephase >> b) & 1u, abort)) { go = false; break; }
-            ephase ^= 1u << b;
-          }
-          tc_fence_after();
           const int s0 = slot_of(y - 1);
+          for (int sub = 0; sub < NSUB; ++sub, ++tile) {
+            const int b = tile & (kTmaAcc - 1);
+            if ((used >> b) & 1u) {  // the epilogue has drained this accumulator
+              if (!wait_or_abort(empty + b, (ephase >> b) & 1u, abort)) { go = false; break; }
+              ephase ^= 1u << b;
+              if ((fpend >> b) & 1u) {  // so its last MMAs are done
+                fphase ^= 1u << b;
+                fpend &= ~(1u << b);
+              }
+            }
+            tc_fence_after();
+            const int py = sub >> 1, px = sub & 1;
 #pragma unroll
-          for (int tap = 0; tap < 9; ++tap) {
-            const int dy = tap / 3, dx = tap % 3;
-            const int slot = s0 + dy < kTmaSlots ? s0 + dy : s0 + dy - kTmaSlots;
-            const unsigned arow = abase + slot * S::ROWB + dx * 16;
-            const unsigned btap = wbase + tap * S::TAPB;
+            for (int tap = 0; tap < 9; ++tap) {
+              const int dy = tap / 3, dx = tap % 3;
+              // staged row (0..2 from row y-1) and pixel shift of the tap
+              const int ry = UPS ? 1 + ((py - 1 + dy) >> 1) : dy;
+              const int rx = UPS ? 1 + ((px - 1 + dx) >> 1) : dx;
+              const int slot = s0 + ry < SLOTS ? s0 + ry : s0 + ry - SLOTS;
+              const unsigned arow = abase + slot * S::ROWB + rx * 16;
+              const unsigned btap = wbase + tap * S::TAPB;
 #pragma unroll
-            for (int ks = 0; ks < CIN / 16; ++ks) {
-              const uint64_t a = sdesc(arow + 2 * ks * S::LBO_A, S::LBO_A, 128);
-              const uint64_t bb = sdesc(btap + 2 * ks * S::LBO_B, S::LBO_B, 128);
-              mma_bf16(tmem + b * COUT, a, bb, IDESC, (tap | ks) != 0);
+              for (int ks = 0; ks < CIN / 16; ++ks) {
+                const uint64_t a = sdesc(arow + 2 * ks * S::LBO_A, S::LBO_A, 128);
+                const uint64_t bb = sdesc(btap + 2 * ks * S::LBO_B, S::LBO_B, 128);
+                mma_bf16(tmem + b * COUT, a, bb, IDESC, (tap | ks) != 0);
+              }
+            }
+            mma_commit(full + b);
+            used |= 1u << b;
+            fpend |= 1u << b;
+            // on the row's first tile: the previous tile's MMAs (queued ahead
+            // of these) done finishes row y-1's tiles, so rows up to y-2 are
+            // free and row y+SLOTS-2 takes the slot of row y-2
+            if (sub == 0) {
+              if (!retire((tile - 1) & (kTmaAcc - 1))) { go = false; break; }
+              if (y + SLOTS - 2 <= yb) fetch(img, x0, y + SLOTS - 2);
             }
           }
-          mma_commit(full + b);
-          used |= 1u << b;
-          fpend |= 1u << b;
-          // tile y-1's MMAs (queued ahead of these) done: rows up to y-2 are
-          // free, and row y+3 takes the slot of row y-2
-          if (!retire(b ^ 1)) { go = false; break; }
-          if (y + 3 <= yb) fetch(img, x0, y + 3);
         }
         // the item's last MMAs are done before the next item refills the slots
-        if (go) go = retire(0) && retire(1);
+        for (int b = 0; b < kTmaAcc && go; ++b) go = retire(b);
       }
       if (!go) {
         *abort = 1;
@@ -542,7 +586,7 @@ __global__ void __launch_bounds__(kTmaThreads) k_conv_tma(ConvArgs p, int rows, 
         // let the copies and MMAs in flight land (bounded) before the memory goes
         for (int s = 0; s < kTmaSlots; ++s)
           if ((rpend >> s) & 1u) bar_wait_bounded(rbar + s, (rphase >> s) & 1u);
-        for (int b = 0; b < 2; ++b)
+        for (int b = 0; b < kTmaAcc; ++b)
           if ((fpend >> b) & 1u) bar_wait_bounded(full + b, (fphase >> b) & 1u);
       }
     }
@@ -551,44 +595,96 @@ __global__ void __launch_bounds__(kTmaThreads) k_conv_tma(ConvArgs p, int rows, 
     float bv[HALF];
 #pragma unroll
     for (int k = 0; k < HALF; ++k) bv[k] = bias[half * HALF + k];
-    unsigned fphase = 0u;
-    int tile = 0;
-    bool go = true;
-    for (int item = blockIdx.x; item < items && go; item += gridDim.x) {
-      const int ch = item % chunks, seg = (item / chunks) % nseg, img = item / (chunks * nseg);
-      const int x0 = seg * kTile, ya = ch * rows, yb = min(H, ya + rows);
-      for (int y = ya; y < yb; ++y, ++tile) {
-        const int b = tile & 1;
-        if (!wait_or_abort(full + b, (fphase >> b) & 1u, abort)) { go = false; break; }
-        fphase ^= 1u << b;
-        tc_fence_after();
-        uint32_t r[HALF];
-        const uint32_t ta = tmem + ((uint32_t)(quad * 32) << 16) + b * COUT + half * HALF;
-        if constexpr (HALF == 8) {
-          tmem_ld8(ta, *reinterpret_cast<uint32_t(*)[8]>(&r[0]));
-        } else {
+    // this CTA's tiles in issue order: item, staged row y, parity sub
+    struct Pos {
+      int item, img, x0, y, yb, sub;
+    };
+    auto enter = [&](Pos& q) {  // first tile of item q.item
+      const int ch = q.item % chunks, seg = (q.item / chunks) % nseg;
+      q.img = q.item / (chunks * nseg);
+      q.x0 = seg * kTile;
+      q.y = ch * rows;
+      q.yb = min(RH, q.y + rows);
+      q.sub = 0;
+    };
+    auto advance = [&](Pos& q) {
+      if (++q.sub < NSUB) return;
+      q.sub = 0;
+      if (++q.y < q.yb) return;
+      q.item += gridDim.x;
+      if (q.item < items) enter(q);
+    };
+    // output element offset of this thread's pixel in tile q (-1: beyond the row)
+    auto out_off = [&](const Pos& q) -> long long {
+      const int xs = q.x0 + quad * 32 + lane;  // staged pixel of this thread
+      if (xs >= RW) return -1;
+      const int oy = UPS ? 2 * q.y + (q.sub >> 1) : q.y, ox = UPS ? 2 * xs + (q.sub & 1) : xs;
+      return (((long long)q.img * H + oy) * W + ox) * COUT + half * HALF;
+    };
+    uint4 skip[UPS ? HALF / 8 : 1];
+    auto load_skip = [&](const Pos& q) {
+      if constexpr (UPS) {
+        const long long off = out_off(q);
+        if (off >= 0) {
 #pragma unroll
-          for (int j = 0; j < HALF / 16; ++j)
-            tmem_ld16(ta + j * 16, *reinterpret_cast<uint32_t(*)[16]>(&r[j * 16]));
+          for (int g = 0; g < HALF / 8; ++g)
+            skip[g] = __ldg(reinterpret_cast<const uint4*>(p.add + off) + g);
         }
-        tmem_wait_ld();
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) bar_arrive(empty + b);  // the accumulator is free again
-        const int x = x0 + quad * 32 + lane;
-        if (x < W) {
-          const size_t off = (((size_t)img * H + y) * W + x) * COUT + half * HALF;
+      }
+    };
+    unsigned fphase = 0u;
+    Pos pos{};
+    pos.item = blockIdx.x;
+    if (pos.item < items) {
+      enter(pos);
+      load_skip(pos);
+    }
+    for (int tile = 0; pos.item < items; ++tile) {
+      const int b = tile & (kTmaAcc - 1);
+      if (!wait_or_abort(full + b, (fphase >> b) & 1u, abort)) break;
+      fphase ^= 1u << b;
+      tc_fence_after();
+      uint32_t r[HALF];
+      const uint32_t ta = tmem + ((uint32_t)(quad * 32) << 16) + b * COUT + half * HALF;
+      if constexpr (HALF == 8) {
+        tmem_ld8(ta, *reinterpret_cast<uint32_t(*)[8]>(&r[0]));
+      } else {
 #pragma unroll
-          for (int g = 0; g < HALF / 8; ++g) {
-            uint4 o;
-            bf162* ob = reinterpret_cast<bf162*>(&o);
+        for (int j = 0; j < HALF / 16; ++j)
+          tmem_ld16(ta + j * 16, *reinterpret_cast<uint32_t(*)[16]>(&r[j * 16]));
+      }
+      tmem_wait_ld();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) bar_arrive(empty + b);  // the accumulator is free again
+      const long long off = out_off(pos);
+      uint4 cur[UPS ? HALF / 8 : 1];
 #pragma unroll
-            for (int k = 0; k < 4; ++k)
-              ob[k] = __floats2bfloat162_rn(
-                  fmaxf(__uint_as_float(r[g * 8 + 2 * k]) + bv[g * 8 + 2 * k], 0.0f),
-                  fmaxf(__uint_as_float(r[g * 8 + 2 * k + 1]) + bv[g * 8 + 2 * k + 1], 0.0f));
-            *(reinterpret_cast<uint4*>(p.out + off) + g) = o;
+      for (int g = 0; g < (UPS ? HALF / 8 : 1); ++g) cur[g] = skip[g];
+      advance(pos);
+      if (pos.item < items) load_skip(pos);  // in flight while this tile is stored
+      if (off >= 0) {
+#pragma unroll
+        for (int g = 0; g < HALF / 8; ++g) {
+          float f[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k) f[k] = __uint_as_float(r[g * 8 + k]) + bv[g * 8 + k];
+          if constexpr (UPS) {  // skip tensor added, no ReLU
+            const bf162* ab = reinterpret_cast<const bf162*>(&cur[g]);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              f[2 * k] += __low2float(ab[k]);
+              f[2 * k + 1] += __high2float(ab[k]);
+            }
+          } else {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) f[k] = fmaxf(f[k], 0.0f);
           }
+          uint4 o;
+          bf162* ob = reinterpret_cast<bf162*>(&o);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) ob[k] = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+          *(reinterpret_cast<uint4*>(p.out + off) + g) = o;
         }
       }
     }
@@ -650,10 +746,10 @@ int launch_tc(const ConvArgs& a, int sms, int* err, cudaStream_t s) {
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-template <int CIN, int COUT>
+template <int CIN, int COUT, bool UPS>
 int launch_tma(const ConvArgs& a, int sms, int* err, const CUtensorMap* map, cudaStream_t s) {
-  using S = TmaShape<CIN, COUT>;
-  auto k = k_conv_tma<CIN, COUT>;
+  using S = TmaShape<CIN, COUT, UPS ? 4 : kTmaSlots>;
+  auto k = k_conv_tma<CIN, COUT, UPS>;
   static const int occ = [k] {
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM) !=
         cudaSuccess)
@@ -661,12 +757,14 @@ int launch_tma(const ConvArgs& a, int sms, int* err, const CUtensorMap* map, cud
     return resident_ctas(k, S::SMEM, S::TCOLS, kTmaThreads);
   }();
   if (occ <= 0) return -1;
-  const long long nseg = (a.W + kTile - 1) / kTile;
+  // the staged rows: the input's (half the output's when upsampling)
+  const int RH = UPS ? a.H / 2 : a.H, RW = UPS ? a.W / 2 : a.W;
+  const long long nseg = (RW + kTile - 1) / kTile;
   const long long slots = (long long)sms * occ;
-  const long long total_rows = (long long)a.n * nseg * a.H;
+  const long long total_rows = (long long)a.n * nseg * RH;
   int rows = (int)((total_rows + slots - 1) / slots);
   if (rows < 1) rows = 1;
-  const long long items = (long long)a.n * nseg * ((a.H + rows - 1) / rows);
+  const long long items = (long long)a.n * nseg * ((RH + rows - 1) / rows);
   const int grid = (int)(items < slots ? items : slots);
   k<<<grid, kTmaThreads, S::SMEM, s>>>(a, rows, err, map);
   ++g_launches;
@@ -690,13 +788,15 @@ template <int CI, int CO>
 int dispatch_pair(const ConvArgs& a, bool ups, bool bwd, bool mask, int sms, int* err,
                   const CUtensorMap* map, cudaStream_t s) {
   if (!bwd) {
-    if constexpr (up_pair<CI, CO>())
+    if constexpr (up_pair<CI, CO>()) {
+      if (ups && map) return launch_tma<CI, CO, true>(a, sms, err, map, s);
       if (ups) return launch_tc<CI, CO, true, false, true, false>(a, sms, err, s);
+    }
     if constexpr (relu_pair<CI, CO>()) {
       // 16 -> 16: nine small MMAs per tile, so the warp roles' hand-offs
       // cost more than the thread staging they replace (measured)
       if constexpr (CI > 16 || CO > 16)
-        if (!ups && map) return launch_tma<CI, CO>(a, sms, err, map, s);
+        if (!ups && map) return launch_tma<CI, CO, false>(a, sms, err, map, s);
       if (!ups) return launch_tc<CI, CO, false, false, false, true>(a, sms, err, s);
     }
     return -1;

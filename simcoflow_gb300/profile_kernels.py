@@ -64,8 +64,8 @@ def main():
     ap.add_argument("--kernel", default="sweep", choices=sorted(KERNELS))
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--engine", type=int, default=1, choices=[0, 1],
-                    help="unet: convolutions on tcgen05 (1) or mma.sync (0)")
+    ap.add_argument("--engine", type=int, default=1, choices=[0, 1, 2],
+                    help="unet: tcgen05 with TMA staging (1), with thread staging (2), mma.sync (0)")
     args = ap.parse_args()
     import torch
     dev = torch.device("cuda", 0)

@@ -106,17 +106,21 @@ def test_tcgen05_conv_matches_mma_sync_kernel(cuda, kind, ch):
     assert np.all(d <= 2.0 ** -7 * np.maximum(np.abs(g0), np.abs(g1)) + 1e-4 * np.abs(g0).max())
 
 
-@pytest.mark.parametrize("ch", FWD_RELU, ids=[f"{c[0]}x{c[1]}" for c in FWD_RELU])
-def test_tma_staged_rows_match_thread_staged_rows(cuda, ch):
-    """Engine 1 stages the forward ReLU layers' input rows by TMA, engine 2
-    with the CTA's threads: the same MMAs on the same shared-memory layout,
-    so the outputs agree bit for bit (rows of 40, 136 and 256 pixels, a
-    column of images taller than a tile strip)."""
+FWD_ALL = [("relu", c) for c in FWD_RELU] + [("up", c) for c in FWD_UP]
+
+
+@pytest.mark.parametrize("kind,ch", FWD_ALL, ids=[f"{k}-{c[0]}x{c[1]}" for k, c in FWD_ALL])
+def test_tma_staged_rows_match_thread_staged_rows(cuda, kind, ch):
+    """Engine 1 stages the forward layers' input rows by TMA (an upsampling
+    layer copies the half-resolution row and expands it in shared memory),
+    engine 2 with the CTA's threads: the same MMAs on the same shared-memory
+    layout, so the outputs agree bit for bit (rows of 40, 136 and 256
+    pixels, a column of images taller than a tile strip)."""
     import torch
     cin, cout = ch
-    for (n, H, W) in [(2, 6, 40), (1, 5, 136), (2, 34, 256)]:
-        g1, ref = _run(torch, 1, "relu", cin, cout, n, H, W, seed=cin + cout)
-        g2, _ = _run(torch, 2, "relu", cin, cout, n, H, W, seed=cin + cout)
+    for (n, H, W) in [(2, 6, 40), (1, 6 if kind == "up" else 5, 136), (2, 34, 256)]:
+        g1, ref = _run(torch, 1, kind, cin, cout, n, H, W, seed=cin + cout)
+        g2, _ = _run(torch, 2, kind, cin, cout, n, H, W, seed=cin + cout)
         _check(g1, ref)
         assert np.array_equal(g1, g2)
 
