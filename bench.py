@@ -308,6 +308,26 @@ def _host(t, shape):
     return t.cpu().numpy().reshape(shape, order="F")
 
 
+# the line smoother's coarse-level schedules the autotuner tries: (first
+# level, sweeps) -- two to four alternating steps per side on the
+# latency-bound coarse levels -- or None (the fine level's schedule
+# everywhere)
+LINE_COARSE = [None, (1, 4), (2, 4), (3, 4), (1, 6), (2, 6), (2, 8)]
+
+
+def apply_schedule(s, schedule):
+    """(npre, npost, omega[, extra]) on a solver: extra is the point
+    smoother's sweep tile (an index into TILES) or the line smoother's coarse
+    schedule (first level, sweeps), None for neither."""
+    from simcoflow_gb300 import batch as Bt
+    s.set_schedule(*schedule[:3])
+    extra = schedule[3] if len(schedule) > 3 else None
+    if isinstance(extra, int):
+        s.set_tile(Bt.TILES[extra])
+    else:
+        s.set_coarse_sweeps(*(extra or (0, 0)))
+
+
 def device_arm(case, tdev, local, precision, *, steps, warmup, precond="mg", schedule=None,
                tune=True, sample_clocks=False, stream=None, use_graph=True, pg=None,
                kernels=True):
@@ -346,17 +366,18 @@ def device_arm(case, tdev, local, precision, *, steps, warmup, precond="mg", sch
         st = step()
         smoother = {1: "point", 2: "line"}.get(st.smoother)
         # V-cycle schedule from the project's autotuner, by time to the
-        # tolerance on this workload (the line smoother varies only omega)
+        # tolerance on this workload (the line smoother: omega, and one or
+        # two alternating steps per side on the coarse levels)
         if schedule is None and tune:
             from simcoflow_gb300 import batch as Bt
             # point smoother: every schedule with every sweep tile
             cands = ([(*sc, tn) for tn in Bt.TILES for sc in Bt.SCHEDULES]
-                     if smoother == "point" else sorted({(2, 2, sc[2]) for sc in Bt.SCHEDULES}))
+                     if smoother == "point" else
+                     [(2, 2, om, co) for om in sorted({sc[2] for sc in Bt.SCHEDULES})
+                      for co in LINE_COARSE])
             best = None
             for sch in cands:
-                s.set_schedule(*sch[:3])
-                if len(sch) > 3:
-                    s.set_tile(Bt.TILES[sch[3]])
+                apply_schedule(s, sch)
                 step()
                 torch.cuda.synchronize(dev)
                 t0 = time.perf_counter()
@@ -368,10 +389,7 @@ def device_arm(case, tdev, local, precision, *, steps, warmup, precond="mg", sch
                     best = (ms_t, sch)
             schedule = best[1] if best else None
         if schedule is not None:
-            s.set_schedule(*schedule[:3])
-            if len(schedule) > 3:
-                from simcoflow_gb300 import batch as Bt
-                s.set_tile(Bt.TILES[schedule[3]])
+            apply_schedule(s, schedule)
         for _ in range(warmup):
             st = step()
         if pg:
@@ -462,10 +480,7 @@ def e2e_arm(case, local, stream, *, steps, warmup, schedule, pg=None, solid=Fals
     try:
         hs.set_stream(stream.cuda_stream)
         if schedule:
-            hs.set_schedule(*schedule[:3])
-            if len(schedule) > 3:
-                from simcoflow_gb300 import batch as Bt
-                hs.set_tile(Bt.TILES[schedule[3]])
+            apply_schedule(hs, schedule)
         hs.set_grid(H["dx"], H["dy"], H["dxU"], H["dyV"])
         h2d = (sum(H[k].nbytes for k in geo_keys + ["DpU", "DpV", "ustar", "vstar"]) +
                hu.nbytes + hv.nbytes + hpp.nbytes)
@@ -1163,8 +1178,9 @@ def run_ours(args):
         "iters": mixed["iters"][-1], "relres_true": mixed["relres"][-1],
         "levels": mixed["levels"], "asym_faces": mixed["asym_faces"],
         "schedule": {"npre_npost_omega": mixed["schedule"],
-                     "source": "autotuner (simcoflow_gb300.batch.SCHEDULES, and TILES for the "
-                               "point smoother), per arm"},
+                     "source": "autotuner (simcoflow_gb300.batch.SCHEDULES; TILES for the "
+                               "point smoother; the line smoother's coarse schedule, "
+                               "[first level, sweeps], from bench.LINE_COARSE), per arm"},
         "plain_fp64_mg_pcg": arm_line(plain, "fp64"),
         "speedup_vs_plain_fp64": round(plain["ms"] / ms_step, 3),
         "e2e": {k: v for k, v in e2e.items() if k != "out"},

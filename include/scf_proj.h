@@ -88,7 +88,11 @@ typedef struct scf_opts {
     int coarse_max;  /* coarsest level has at most this many cells (<= 64) */
     int smoother;    /* SCF_SMOOTH_AUTO (default), SCF_SMOOTH_POINT or SCF_SMOOTH_LINE */
     int precond;     /* SCF_PRECOND_MG (default) or SCF_PRECOND_LEARNED */
-    int reserved[6];
+    int coarse_sweeps; /* line smoother: sweeps before / after the coarse correction on
+                          level coarse_from (0: the finest) and every coarser level;
+                          0 (default): npre / npost there too */
+    int coarse_from;
+    int reserved[4];
 } scf_opts;
 
 typedef struct scf_stats {
@@ -134,6 +138,13 @@ int scf_proj_solve_rhs(struct scf_proj *h, const double *b, double *x, double *r
  * the coarse correction, correction scale); rebuilds its graph.  Used by the
  * autotuner. */
 int scf_proj_set_opts(struct scf_proj *h, int npre, int npost, double omega);
+
+/* Line smoother: sweeps (1..8; a step of x-lines then y-lines counts as two)
+ * before and after the coarse correction on level coarse_from (0: the
+ * finest) and every coarser level, 0 for npre / npost there too; rebuilds the
+ * graph.  The coarse levels are latency-bound, so more smoothing there
+ * can cost less than the PCG iterations it saves.  Used by the autotuner. */
+int scf_proj_set_coarse_sweeps(struct scf_proj *h, int coarse_from, int sweeps);
 
 /* Sweep tile of the red-black (point) smoother on an existing handle;
  * rebuilds its graph.  SCF_TILE_64X32 (default): 64 x 32 cells per CTA, the

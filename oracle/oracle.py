@@ -111,6 +111,7 @@ def lib():
                                           C.POINTER(C.c_double)])
         L.oracle_num_threads.restype = C.c_int
         L.oracle_set_threads.argtypes = [C.c_int]
+        L.oracle_set_coarse_sweeps.argtypes = [C.c_int, C.c_int]
         L.oracle_format_many.argtypes = [_P, C.c_int64, C.c_char_p]
         L.oracle_tecplot_pcell.restype = C.c_int64
         L.oracle_tecplot_pcell.argtypes = [C.c_int, C.c_int] + [_P] * 13 + [C.c_char_p]
@@ -264,8 +265,22 @@ def own_west_south(case, matr):
 SMOOTHERS = {"point": 0, "line": 1}
 
 
+class _coarse_sweeps:
+    """The line smoother's coarse schedule (level, sweeps) for the calls in
+    a with-block; None or sweeps 0: npre / npost on every level."""
+
+    def __init__(self, coarse):
+        self.c = coarse or (0, 0)
+
+    def __enter__(self):
+        lib().oracle_set_coarse_sweeps(int(self.c[0]), int(self.c[1]))
+
+    def __exit__(self, *a):
+        lib().oracle_set_coarse_sweeps(0, 0)
+
+
 def mgpcg(case, matr, rhm, rtol=1e-13, maxit=500, npre=2, npost=2, omega=1.9, coarse_max=64,
-          threads=0, smoother="point"):
+          threads=0, smoother="point", coarse=None):
     """CPU FP64 MG-PCG: the PCG applies the assembled rows as written (own
     west / south entries), the V-cycle preconditioner the symmetric storage.
     Returns (Pp-interior x as (nx,ny) Fortran array, iterations, true relres,
@@ -280,23 +295,25 @@ def mgpcg(case, matr, rhm, rtol=1e-13, maxit=500, npre=2, npost=2, omega=1.9, co
     nlev = C.c_int(0)
     if threads:
         lib().oracle_set_threads(threads)
-    it = lib().oracle_mgpcg(nx, ny, cE.ctypes.data_as(_P), cN.ctypes.data_as(_P),
-                            dg.ctypes.data_as(_P), cW.ctypes.data_as(_P), cS.ctypes.data_as(_P),
-                            b.ctypes.data_as(_P), x.ctypes.data_as(_P),
-                            rtol, maxit, npre, npost, omega, coarse_max, C.byref(rel),
-                            C.byref(nlev), SMOOTHERS[smoother])
+    with _coarse_sweeps(coarse):
+        it = lib().oracle_mgpcg(nx, ny, cE.ctypes.data_as(_P), cN.ctypes.data_as(_P),
+                                dg.ctypes.data_as(_P), cW.ctypes.data_as(_P),
+                                cS.ctypes.data_as(_P), b.ctypes.data_as(_P),
+                                x.ctypes.data_as(_P), rtol, maxit, npre, npost, omega,
+                                coarse_max, C.byref(rel), C.byref(nlev), SMOOTHERS[smoother])
     return np.asfortranarray(x.reshape(ny, nx).T), it, rel.value, nlev.value
 
 
 def vcycle(case, matr, b_f, npre=2, npost=2, omega=1.9, coarse_max=64,
-           smoother="point") -> np.ndarray:
+           smoother="point", coarse=None) -> np.ndarray:
     nx, ny = case.nx, case.ny
     cE, cN, dg = symmetric_operator(case, matr)
     b = np.ascontiguousarray(b_f.T).ravel()
     x = np.zeros(nx * ny)
-    lib().oracle_vcycle(nx, ny, cE.ctypes.data_as(_P), cN.ctypes.data_as(_P),
-                        dg.ctypes.data_as(_P), b.ctypes.data_as(_P), x.ctypes.data_as(_P), npre,
-                        npost, omega, coarse_max, SMOOTHERS[smoother])
+    with _coarse_sweeps(coarse):
+        lib().oracle_vcycle(nx, ny, cE.ctypes.data_as(_P), cN.ctypes.data_as(_P),
+                            dg.ctypes.data_as(_P), b.ctypes.data_as(_P), x.ctypes.data_as(_P),
+                            npre, npost, omega, coarse_max, SMOOTHERS[smoother])
     return np.asfortranarray(x.reshape(ny, nx).T)
 
 
@@ -308,7 +325,7 @@ def line_smoother_wanted(case) -> bool:
 
 
 def project_mg(case, rtol=1e-8, maxit=500, npre=2, npost=2, omega=1.9, coarse_max=64,
-               smoother=None, threads=0) -> dict:
+               smoother=None, threads=0, coarse=None) -> dict:
     """The whole projection in C on all host threads, as the timed CPU
     baseline runs it: pocoef, the dense rows, the right-hand side, the FP64
     MG-PCG to rtol (the PCG on the rows as written, the V-cycle on their
@@ -326,9 +343,10 @@ def project_mg(case, rtol=1e-8, maxit=500, npre=2, npost=2, omega=1.9, coarse_ma
     xint = np.zeros((nx, ny), order="F")
     rel = C.c_double(0.0)
     nlev = C.c_int(0)
-    it = lib().oracle_mgpcg_matr(nx, ny, _p(matr), _p(rhm), _p(case["posnu_p"]), _p(xint), rtol,
-                                 maxit, npre, npost, omega, coarse_max, C.byref(rel),
-                                 C.byref(nlev), SMOOTHERS[smoother])
+    with _coarse_sweeps(coarse):
+        it = lib().oracle_mgpcg_matr(nx, ny, _p(matr), _p(rhm), _p(case["posnu_p"]), _p(xint),
+                                     rtol, maxit, npre, npost, omega, coarse_max, C.byref(rel),
+                                     C.byref(nlev), SMOOTHERS[smoother])
     Pp = np.zeros((nx + 2, ny + 2), order="F")
     wb, eb, sb, nb = case.bc
     lib().oracle_scatter_interior(nx, ny, _p(case["posnu_p"]), _p(xint), wb, eb, sb, nb, _p(Pp))

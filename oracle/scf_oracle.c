@@ -545,6 +545,7 @@ typedef struct {
     olevel lev[32];
     double omega;
     int npre, npost;
+    int cfrom, csweeps; /* line smoother: csweeps on levels cfrom and coarser (0: npre/npost) */
     int line;        /* 1: alternating zebra line smoother */
     int nc;          /* coarsest unknowns */
     double *chol;    /* nc x nc lower Cholesky factor */
@@ -813,6 +814,17 @@ static void prolong_add(olevel *F, const olevel *C, double omega) {
         }
 }
 
+/* the coarse line-smoothing schedule of the next MG-PCG or V-cycle call:
+   sweeps (a step of x-lines then y-lines counts as two) on level cfrom (0:
+   the finest) and coarser; sweeps 0 keeps npre / npost everywhere */
+static int g_cfrom = 0, g_csweeps = 0;
+void oracle_set_coarse_sweeps(int cfrom, int sweeps) { g_cfrom = cfrom; g_csweeps = sweeps; }
+
+static int line_steps(const omg *M, int l, int post) {
+    int sw = M->csweeps > 0 && l >= M->cfrom ? M->csweeps : (post ? M->npost : M->npre);
+    return (sw + 1) / 2;
+}
+
 static void vcycle(omg *M, int l) {
     olevel *L = &M->lev[l];
     size_t n = (size_t)L->nx * L->ny;
@@ -820,7 +832,7 @@ static void vcycle(omg *M, int l) {
     pzero(L->x, n);
     if (M->line) {
         /* a line step (x-lines and y-lines) counts as two sweeps */
-        for (int s = 0; s < (M->npre + 1) / 2; ++s) line_step(L, 0);
+        for (int s = 0; s < line_steps(M, l, 0); ++s) line_step(L, 0);
     } else {
         for (int s = 0; s < M->npre; ++s) { rbgs_half(L, 0); rbgs_half(L, 1); }
     }
@@ -829,7 +841,7 @@ static void vcycle(omg *M, int l) {
     vcycle(M, l + 1);
     prolong_add(L, &M->lev[l + 1], M->omega);
     if (M->line) {
-        for (int s = 0; s < (M->npost + 1) / 2; ++s) line_step(L, 1);
+        for (int s = 0; s < line_steps(M, l, 1); ++s) line_step(L, 1);
     } else {
         for (int s = 0; s < M->npost; ++s) { rbgs_half(L, 1); rbgs_half(L, 0); }
     }
@@ -872,6 +884,7 @@ int oracle_mgpcg(int nx, int ny, const double *cE, const double *cN, const doubl
     omg M;
     memset(&M, 0, sizeof(M));
     M.omega = omega; M.npre = npre; M.npost = npost; M.line = smoother == 1;
+    M.cfrom = g_cfrom; M.csweeps = g_csweeps;
     int ncyc = 1;
     if (maxit < 0) { ncyc = (-maxit) / 1000; maxit = (-maxit) % 1000; if (ncyc < 1) ncyc = 1; }
     size_t n = (size_t)nx * ny;
@@ -1006,6 +1019,7 @@ void oracle_vcycle(int nx, int ny, const double *cE, const double *cN, const dou
     omg M;
     memset(&M, 0, sizeof(M));
     M.omega = omega; M.npre = npre; M.npost = npost; M.line = smoother == 1;
+    M.cfrom = g_cfrom; M.csweeps = g_csweeps;
     size_t n = (size_t)nx * ny;
     level_alloc(&M.lev[0], nx, ny);
     memcpy(M.lev[0].cE, cE, n * sizeof(double));

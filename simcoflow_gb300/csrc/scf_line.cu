@@ -1009,9 +1009,13 @@ __global__ void __launch_bounds__(1024) k_line_tail(TailDesc<T, CT> d, Scalars* 
     }
     __syncthreads();
   };
-  const int ns_pre = (d.npre + 1) / 2, ns_post = (d.npost + 1) / 2;
+  // a step (x-lines, then y-lines) counts as two sweeps
+  auto steps = [&](int l, bool post) {
+    return ((l >= d.cfrom ? (post ? d.cpost : d.cpre) : (post ? d.npost : d.npre)) + 1) / 2;
+  };
   const int n = d.n;
   for (int l = 0; l < n - 1; ++l) {
+    const int ns_pre = steps(l, false);
     for (int it = 0; it < ns_pre; ++it) {
       pass(l, 0, 0); pass(l, 0, 1); pass(l, 1, 0); pass(l, 1, 1);
     }
@@ -1073,6 +1077,7 @@ __global__ void __launch_bounds__(1024) k_line_tail(TailDesc<T, CT> d, Scalars* 
       if (G(l)[si] > T(0)) x[si] = fma(d.omega, xc[((iy >> 1) + 1) * wc + (ix >> 1) + 1], x[si]);
     }
     __syncthreads();
+    const int ns_post = steps(l, true);
     for (int it = 0; it < ns_post; ++it) {
       pass(l, 1, 1); pass(l, 1, 0); pass(l, 0, 1); pass(l, 0, 0);
     }

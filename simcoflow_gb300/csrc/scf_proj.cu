@@ -310,6 +310,15 @@ void enqueue_vcycle_t(scf_proj* h, ViewFn view, BufFn buf, const TailDesc<T, CT>
   }
 }
 
+// the coarse line-smoothing schedule of a line tail whose first level is
+// level l0 of the hierarchy (tail levels are numbered from 0)
+constexpr int kNoCoarse = 1 << 20;
+template <class D>
+void set_tail_coarse(D& d, const scf_opts& o, int l0) {
+  d.cfrom = o.coarse_sweeps > 0 ? (o.coarse_from > l0 ? o.coarse_from - l0 : 0) : kNoCoarse;
+  d.cpre = d.cpost = o.coarse_sweeps;
+}
+
 // V-cycle with the alternating zebra line smoother.  A smoothing step is
 // x-lines (even rows, odd rows), then y-lines (even columns, odd columns) on
 // the transposed level; the post-smoothing steps run the same passes in
@@ -321,7 +330,14 @@ void enqueue_vcycle_line_t(scf_proj* h, ViewFn view, TViewFn tview, const TailDe
                            Scalars* sc, bool do_rz, int flexible, cudaStream_t s) {
   using V = MgView<T, CT, T>;
   const int L = (int)h->lev.size();
-  const int npre = (h->opts.npre + 1) / 2, npost = (h->opts.npost + 1) / 2;
+  // steps per level (a step counts as two sweeps); the coarse schedule from
+  // level coarse_from down
+  auto steps = [h](int l, bool post) {
+    const scf_opts& o = h->opts;
+    const int sw = o.coarse_sweeps > 0 && l >= o.coarse_from ? o.coarse_sweeps
+                                                               : (post ? o.npost : o.npre);
+    return (sw + 1) / 2;
+  };
   const double om = h->opts.omega;
   auto to_t = [&](const V& f, const V& ft) {
     launch_transpose<T>(f.x, f.nx, f.ny, f.pitch, ft.x, ft.pitch, sc, s);
@@ -373,6 +389,7 @@ void enqueue_vcycle_line_t(scf_proj* h, ViewFn view, TViewFn tview, const TailDe
     // level 0 gets b from the PCG; coarser levels get both layouts from the
     // restriction
     if (l == 0) launch_transpose<T>(f.b, f.nx, f.ny, f.pitch, ft.b, ft.pitch, sc, s);
+    const int npre = steps(l, false);
     for (int it = 0; it < npre; ++it) step(l, false, it == 0, it == npre - 1);
     launch_resid_restrict_lt(ft, view(l + 1), tview(l + 1), sc, s);
   }
@@ -384,6 +401,7 @@ void enqueue_vcycle_line_t(scf_proj* h, ViewFn view, TViewFn tview, const TailDe
   }
   for (int l = lk - 1; l >= 0; --l) {
     launch_prolong_lt(tview(l), view(l + 1), om, sc, s);
+    const int npost = steps(l, true);
     for (int it = 0; it < npost; ++it)
       step(l, true, false, it == 0, do_rz && l == 0 && it == npost - 1);
   }
@@ -1045,6 +1063,8 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
   if (o.maxit < 1 || o.npre < 1 || o.npost < 1 || o.npre > 8 || o.npost > 8 || !(o.rtol >= 0.0))
     return SCF_ERR_ARG;
   if (o.coarse_max < 1 || o.coarse_max > kMaxCoarse) return SCF_ERR_ARG;
+  if (o.coarse_sweeps < 0 || o.coarse_sweeps > 8 || o.coarse_from < 0 || o.coarse_from > 64)
+    return SCF_ERR_ARG;
   if (!(o.omega > 0.0 && o.omega < 2.0)) return SCF_ERR_ARG;
   if (o.smoother != SCF_SMOOTH_AUTO && o.smoother != SCF_SMOOTH_POINT &&
       o.smoother != SCF_SMOOTH_LINE)
@@ -1163,6 +1183,7 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
         d.n = nlev - l;
         for (int k = 0; k < d.n; ++k) d.lv[k] = view(l + k);
         d.npre = o.npre; d.npost = o.npost;
+        d.cfrom = kNoCoarse; d.cpre = d.cpost = 0;  // the point smoother's tail
         d.omega = (decltype(d.omega))o.omega;
         d.Ainv = h->Ainv; d.cmap = h->cmap; d.nc = h->ncoarse;
         return tail_prepare(d);
@@ -1185,6 +1206,7 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
         d.n = nlev - l;
         for (int k = 0; k < d.n; ++k) d.lv[k] = view(l + k);
         d.npre = o.npre; d.npost = o.npost;
+        set_tail_coarse(d, o, l);
         d.omega = (decltype(d.omega))o.omega;
         d.Ainv = h->Ainv; d.cmap = h->cmap; d.nc = h->ncoarse;
         return line_tail_prepare(d);
@@ -1809,6 +1831,21 @@ int scf_proj_set_opts(scf_proj* h, int npre, int npost, double omega) {
   h->tail32.omega = (float)omega;
   h->ltail64.omega = omega;
   h->ltail32.omega = (float)omega;
+  destroy_graph(h);
+  if (h->assembled && !(h->opts.flags & SCF_FLAG_NO_GRAPH)) return build_graph(h);
+  return SCF_OK;
+}
+
+int scf_proj_set_coarse_sweeps(scf_proj* h, int coarse_from, int sweeps) {
+  if (!h || sweeps < 0 || sweeps > 8 || coarse_from < 0 || coarse_from > 64) return SCF_ERR_ARG;
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  h->opts.coarse_sweeps = sweeps;
+  h->opts.coarse_from = coarse_from;
+  if (h->ltail0 > 0) {  // the line tails carry their own copy of the schedule
+    set_tail_coarse(h->ltail64, h->opts, h->ltail0);
+    set_tail_coarse(h->ltail32, h->opts, h->ltail0);
+  }
   destroy_graph(h);
   if (h->assembled && !(h->opts.flags & SCF_FLAG_NO_GRAPH)) return build_graph(h);
   return SCF_OK;

@@ -45,7 +45,8 @@ EXPORTS = ["scf_opts_default", "scf_proj_create", "scf_proj_destroy", "scf_proj_
            "scf_proj_set_network", "scf_proj_solve_rhs", "scf_proj_set_opts",
            "scf_batch_create", "scf_batch_set_io", "scf_batch_run", "scf_batch_destroy",
            "scf_proj_set_solid", "scf_proj_get_geometry", "scf_diag_divide", "scf_diag_sqrt",
-           "scf_proj_get_matrix", "scf_diag_tma_timeout", "scf_proj_set_tile"]
+           "scf_proj_get_matrix", "scf_diag_tma_timeout", "scf_proj_set_tile",
+           "scf_proj_set_coarse_sweeps"]
 # every symbol declared in include/scf_unet.h
 UNET_EXPORTS = ["scf_unet_num_params", "scf_unet_create", "scf_unet_destroy",
                 "scf_unet_set_stream", "scf_unet_set_params", "scf_unet_get_params",
@@ -58,7 +59,8 @@ class Opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("flags", C.c_int), ("device", C.c_int),
                 ("maxit", C.c_int), ("rtol", C.c_double), ("npre", C.c_int),
                 ("npost", C.c_int), ("omega", C.c_double), ("coarse_max", C.c_int),
-                ("smoother", C.c_int), ("precond", C.c_int), ("reserved", C.c_int * 6)]
+                ("smoother", C.c_int), ("precond", C.c_int), ("coarse_sweeps", C.c_int),
+                ("coarse_from", C.c_int), ("reserved", C.c_int * 4)]
 
 
 class Stats(C.Structure):
@@ -115,6 +117,7 @@ def load():
         L.scf_proj_solve_rhs.argtypes = [vp, dp, dp, dp, C.c_int, C.POINTER(Stats)]
         L.scf_proj_set_opts.argtypes = [vp, C.c_int, C.c_int, C.c_double]
         L.scf_proj_set_tile.argtypes = [vp, C.c_int]
+        L.scf_proj_set_coarse_sweeps.argtypes = [vp, C.c_int, C.c_int]
         L.scf_batch_create.argtypes = [C.POINTER(vp), C.POINTER(vp), C.c_int]
         L.scf_batch_set_io.argtypes = [vp, C.c_int, dp, dp, C.c_double, dp, dp, dp, dp, dp]
         L.scf_batch_run.argtypes = [vp, vp, C.POINTER(Stats)]
@@ -155,7 +158,8 @@ class ProjectionSolver:
     def __init__(self, nx: int, ny: int, precision: str = "fp64", device: int = 0,
                  device_ptrs: bool = False, use_graph: bool = True, maxit: int = 200,
                  rtol: float = 1e-8, npre: int = 2, npost: int = 2, omega: float = 1.9,
-                 coarse_max: int = 64, smoother: str = "auto", precond: str = "mg"):
+                 coarse_max: int = 64, smoother: str = "auto", precond: str = "mg",
+                 coarse_sweeps: int = 0, coarse_from: int = 0):
         L = load()
         o = Opts()
         L.scf_opts_default(C.byref(o))
@@ -165,6 +169,7 @@ class ProjectionSolver:
         o.npre, o.npost, o.omega, o.coarse_max = npre, npost, omega, coarse_max
         o.smoother = SMOOTHERS[smoother]
         o.precond = PRECONDS[precond]
+        o.coarse_sweeps, o.coarse_from = coarse_sweeps, coarse_from
         self.nx, self.ny, self.device_ptrs = nx, ny, device_ptrs
         self.opts = o
         h = C.c_void_p()
@@ -329,6 +334,14 @@ class ProjectionSolver:
         """V-cycle schedule of this handle (rebuilds its graph)."""
         _check(load().scf_proj_set_opts(self._h, npre, npost, omega), "scf_proj_set_opts")
         self.opts.npre, self.opts.npost, self.opts.omega = npre, npost, omega
+
+    def set_coarse_sweeps(self, coarse_from: int, sweeps: int):
+        """Line smoother: sweeps before / after the coarse correction on level
+        coarse_from (0: the finest) and every coarser one, 0 for npre / npost
+        there too (rebuilds the handle's graph)."""
+        _check(load().scf_proj_set_coarse_sweeps(self._h, int(coarse_from), int(sweeps)),
+               "scf_proj_set_coarse_sweeps")
+        self.opts.coarse_from, self.opts.coarse_sweeps = int(coarse_from), int(sweeps)
 
     def set_tile(self, tile: int):
         """Sweep tile of the point smoother: 0 = 64x32 (TMA-staged on large

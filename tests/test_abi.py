@@ -56,19 +56,23 @@ def test_struct_layouts_match_header(tmp_path):
     from simcoflow_gb300 import projection as P
     src = tmp_path / "lay.c"
     fields = [n for n, _ in P.Stats._fields_]
+    ofields = [n for n, _ in P.Opts._fields_]
     src.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "scf_proj.h"\n'
         "int main(void) {\n"
         '  printf("%zu %zu\\n", sizeof(scf_opts), sizeof(scf_stats));\n'
         + "".join(f'  printf("%zu\\n", offsetof(scf_stats, {n}));\n' for n in fields)
+        + "".join(f'  printf("%zu\\n", offsetof(scf_opts, {n}));\n' for n in ofields)
         + "  return 0;\n}\n")
     exe = tmp_path / "lay"
     subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
     assert int(out[0]) == ctypes.sizeof(P.Opts)
     assert int(out[1]) == ctypes.sizeof(P.Stats)
-    for n, off in zip(fields, out[2:]):
+    for n, off in zip(fields, out[2:2 + len(fields)]):
         assert int(off) == getattr(P.Stats, n).offset, n
+    for n, off in zip(ofields, out[2 + len(fields):]):
+        assert int(off) == getattr(P.Opts, n).offset, n
 
 
 def test_host_only_entry_points(built):
@@ -86,6 +90,13 @@ def test_host_only_entry_points(built):
     L.scf_opts_default(ctypes.byref(bad))
     bad.coarse_max = 1000
     assert L.scf_proj_create(ctypes.byref(h), 8, 8, ctypes.byref(bad)) == -1
+    for field, value in (("coarse_sweeps", 9), ("coarse_sweeps", -1), ("coarse_from", -1)):
+        bad = projection.Opts()
+        L.scf_opts_default(ctypes.byref(bad))
+        assert bad.coarse_sweeps == 0 and bad.coarse_from == 0
+        setattr(bad, field, value)
+        assert L.scf_proj_create(ctypes.byref(h), 8, 8, ctypes.byref(bad)) == -1, field
+    assert L.scf_proj_set_coarse_sweeps(None, 1, 4) == -1
     assert L.scf_proj_destroy(None) == 0
 
 

@@ -29,9 +29,12 @@ def _odd_stretched():
                             synth._modes(rng, 8), 1e-3, 800.0)
 
 
+@pytest.mark.parametrize("coarse", [None, (1, 4)], ids=["one_step", "two_steps_from_1"])
 @pytest.mark.parametrize("maker", [lambda: synth.c3(n=128), _odd_stretched],
                          ids=["c3_128", "odd37x29"])
-def test_line_vcycle_matches_oracle(cuda, oracle, maker):
+def test_line_vcycle_matches_oracle(cuda, oracle, maker, coarse):
+    """One alternating step per side everywhere, or two from level 1 down
+    (the per-level kernels and the single-CTA tail)."""
     c = maker()
     matr, _ = oracle.matrix(c)
     rng = np.random.Generator(np.random.PCG64(7))
@@ -39,22 +42,26 @@ def test_line_vcycle_matches_oracle(cuda, oracle, maker):
     s = P.ProjectionSolver(c.nx, c.ny, smoother="line")
     try:
         s.setup_case(c)
+        if coarse:
+            s.set_coarse_sweeps(*coarse)
         xg = s.vcycle(b)
     finally:
         s.close()
-    xo = oracle.vcycle(c, matr, b, npre=2, npost=2, omega=1.9, smoother="line")
+    xo = oracle.vcycle(c, matr, b, npre=2, npost=2, omega=1.9, smoother="line", coarse=coarse)
     # partitioned line solves (Schur complement + cyclic reduction) against
     # the Thomas algorithm: the same exact line solves, other rounding
     assert rel_l2(xg, xo) < 1e-10
 
 
+@pytest.mark.parametrize("coarse", [(0, 0), (1, 4)], ids=["one_step", "two_steps_from_1"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("maker", [lambda: synth.c3(n=256), _odd_stretched],
                          ids=["c3_256", "odd37x29"])
-def test_line_projection_parity(cuda, oracle, maker, precision):
+def test_line_projection_parity(cuda, oracle, maker, precision, coarse):
     c = maker()
     exp = oracle.project(c)
-    g = P.project_case(c, precision=precision, rtol=1e-13, maxit=200)
+    g = P.project_case(c, precision=precision, rtol=1e-13, maxit=200, coarse_from=coarse[0],
+                       coarse_sweeps=coarse[1])
     st = g["stats"]
     assert st["smoother"] == P.SMOOTHERS["line"]  # chosen automatically
     assert st["iters"] < 60
@@ -92,3 +99,18 @@ def test_line_graph_and_graph_free_agree(cuda, precision):
     b = P.project_case(c, precision=precision, rtol=1e-12, maxit=200, use_graph=False)
     for k in ("Pp", "u", "v", "p", "mres"):
         assert np.array_equal(a[k], b[k]), k
+
+
+def test_coarse_steps_cut_iterations(cuda):
+    """Two alternating steps per side on the coarse levels (the latency-bound
+    ones) take fewer PCG iterations to 1e-8 on the stretched grid, in both
+    precisions."""
+    c = synth.c3(n=512)
+    for precision in ("fp64", "mixed"):
+        it = {}
+        for coarse in ((0, 0), (2, 4)):
+            g = P.project_case(c, precision=precision, rtol=1e-8, maxit=200,
+                               coarse_from=coarse[0], coarse_sweeps=coarse[1])
+            assert g["stats"]["status"] == 0
+            it[coarse] = g["stats"]["iters"]
+        assert it[(2, 4)] < it[(0, 0)], (precision, it)

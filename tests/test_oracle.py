@@ -298,6 +298,30 @@ def test_oracle_line_smoother_on_stretched_grid(oracle, built):
     assert all(itp > 3 * itl for itp, itl in its.values())
 
 
+def test_oracle_coarse_line_steps(oracle, built):
+    """The line smoother's coarse schedule: two sweeps (one alternating
+    step) from some level down is the default V-cycle bit for bit; four (two
+    steps) on the coarse levels cut the MG-PCG iterations on the stretched
+    grid and reach the same solution."""
+    c = synth.c3(n=256)
+    r = oracle.project(c)
+    rng = np.random.Generator(np.random.PCG64(3))
+    b = rng.normal(size=(c.nx, c.ny)) * (c["posnu_p"][1:c.nx + 1, 1:c.ny + 1] != -1)
+    x0 = oracle.vcycle(c, r["matr"], b, smoother="line")
+    assert np.array_equal(x0, oracle.vcycle(c, r["matr"], b, smoother="line", coarse=(1, 2)))
+    assert not np.array_equal(x0, oracle.vcycle(c, r["matr"], b, smoother="line",
+                                                coarse=(1, 4)))
+    _, it1, _, _ = oracle.mgpcg(c, r["matr"], r["rhm"], rtol=1e-8, maxit=200, smoother="line")
+    x2, it2, rel, _ = oracle.mgpcg(c, r["matr"], r["rhm"], rtol=1e-12, maxit=200,
+                                   smoother="line", coarse=(1, 4))
+    _, it2e, _, _ = oracle.mgpcg(c, r["matr"], r["rhm"], rtol=1e-8, maxit=200, smoother="line",
+                                 coarse=(1, 4))
+    assert it2e < it1
+    pn = c["posnu_p"][1:c.nx + 1, 1:c.ny + 1] != -1
+    xd = r["Pp"][1:c.nx + 1, 1:c.ny + 1]
+    assert np.linalg.norm((x2 - xd)[pn]) <= 1e-9 * np.linalg.norm(xd[pn])
+
+
 def test_whole_projection_in_c_matches_direct_solve(oracle, built):
     """The timed CPU baseline's path (every stage in C, the dense rows only,
     the MG-PCG on them) gives the direct solve's projection, with the
