@@ -317,12 +317,12 @@ LINE_COARSE = [None, (1, 4), (2, 4), (3, 4), (1, 6), (2, 6), (2, 8)]
 
 def apply_schedule(s, schedule):
     """(npre, npost, omega[, extra]) on a solver: extra is the point
-    smoother's sweep tile (an index into TILES) or the line smoother's coarse
+    smoother's sweep tile (a name in TILES) or the line smoother's coarse
     schedule (first level, sweeps), None for neither."""
     from simcoflow_gb300 import batch as Bt
     s.set_schedule(*schedule[:3])
     extra = schedule[3] if len(schedule) > 3 else None
-    if isinstance(extra, int):
+    if isinstance(extra, str):
         s.set_tile(Bt.TILES[extra])
     else:
         s.set_coarse_sweeps(*(extra or (0, 0)))
