@@ -64,6 +64,10 @@ def main():
     ap.add_argument("--kernel", default="sweep", choices=sorted(KERNELS))
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--omega", type=float, default=1.9, help="coarse-correction weight")
+    ap.add_argument("--coarse", type=int, nargs=2, default=(0, 0), metavar=("LEVEL", "SWEEPS"),
+                    help="line smoother: SWEEPS before / after the coarse correction from "
+                         "LEVEL down (0 0: the fine schedule everywhere)")
     ap.add_argument("--engine", type=int, default=1, choices=[0, 1, 2],
                     help="unet: tcgen05 with TMA staging (1), with thread staging (2), mma.sync (0)")
     args = ap.parse_args()
@@ -174,7 +178,8 @@ def main():
         return
     direct = args.kernel == "projection"
     s = P.ProjectionSolver(c.nx, c.ny, device_ptrs=True, precision=args.precision,
-                           use_graph=not direct)
+                           use_graph=not direct, omega=args.omega,
+                           coarse_from=args.coarse[0], coarse_sweeps=args.coarse[1])
     s.set_grid(t["dx"], t["dy"], t["dxU"], t["dyV"])
     s.set_geometry(**{k: t[k] for k in P.GEOMETRY_ARGS})
     s.assemble(t["DpU"], t["DpV"], c.betaP, c.betaM, c.bc)
