@@ -308,24 +308,27 @@ def _host(t, shape):
     return t.cpu().numpy().reshape(shape, order="F")
 
 
-# the line smoother's coarse-level schedules the autotuner tries: (first
-# level, sweeps) -- two to four alternating steps per side on the
-# latency-bound coarse levels -- or None (the fine level's schedule
+# the coarse-level schedules the autotuner tries: (first level, sweeps) --
+# more sweeps on the latency-bound coarse levels (line smoother: two to four
+# alternating steps per side) -- or None (the fine level's schedule
 # everywhere)
 LINE_COARSE = [None, (1, 4), (2, 4), (3, 4), (1, 6), (2, 6), (2, 8)]
+POINT_COARSE = [None, (1, 4), (2, 4), (2, 6)]
 
 
 def apply_schedule(s, schedule):
-    """(npre, npost, omega[, extra]) on a solver: extra is the point
-    smoother's sweep tile (a name in TILES) or the line smoother's coarse
-    schedule (first level, sweeps), None for neither."""
+    """(npre, npost, omega, extras...) on a solver: an extra is the point
+    smoother's sweep tile (a name in TILES) or the coarse-level schedule
+    (first level, sweeps); without one, npre / npost on every level."""
     from simcoflow_gb300 import batch as Bt
     s.set_schedule(*schedule[:3])
-    extra = schedule[3] if len(schedule) > 3 else None
-    if isinstance(extra, str):
-        s.set_tile(Bt.TILES[extra])
-    else:
-        s.set_coarse_sweeps(*(extra or (0, 0)))
+    coarse = (0, 0)
+    for extra in schedule[3:]:
+        if isinstance(extra, str):
+            s.set_tile(Bt.TILES[extra])
+        elif extra is not None:
+            coarse = tuple(extra)
+    s.set_coarse_sweeps(*coarse)
 
 
 def device_arm(case, tdev, local, precision, *, steps, warmup, precond="mg", schedule=None,
@@ -366,12 +369,13 @@ def device_arm(case, tdev, local, precision, *, steps, warmup, precond="mg", sch
         st = step()
         smoother = {1: "point", 2: "line"}.get(st.smoother)
         # V-cycle schedule from the project's autotuner, by time to the
-        # tolerance on this workload (the line smoother: omega, and one or
-        # two alternating steps per side on the coarse levels)
+        # tolerance on this workload (sweeps, omega, the coarse levels'
+        # sweeps and, for the point smoother, the sweep tile)
         if schedule is None and tune:
             from simcoflow_gb300 import batch as Bt
             # point smoother: every schedule with every sweep tile
-            cands = ([(*sc, tn) for tn in Bt.TILES for sc in Bt.SCHEDULES]
+            cands = ([(*sc, tn, co) for tn in Bt.TILES for sc in Bt.SCHEDULES
+                      for co in POINT_COARSE]
                      if smoother == "point" else
                      [(2, 2, om, co) for om in sorted({sc[2] for sc in Bt.SCHEDULES})
                       for co in LINE_COARSE])
@@ -1179,8 +1183,8 @@ def run_ours(args):
         "levels": mixed["levels"], "asym_faces": mixed["asym_faces"],
         "schedule": {"npre_npost_omega": mixed["schedule"],
                      "source": "autotuner (simcoflow_gb300.batch.SCHEDULES; TILES for the "
-                               "point smoother; the line smoother's coarse schedule, "
-                               "[first level, sweeps], from bench.LINE_COARSE), per arm"},
+                               "point smoother; the coarse levels' schedule, [first level, "
+                               "sweeps], from bench.LINE_COARSE / POINT_COARSE), per arm"},
         "plain_fp64_mg_pcg": arm_line(plain, "fp64"),
         "speedup_vs_plain_fp64": round(plain["ms"] / ms_step, 3),
         "e2e": {k: v for k, v in e2e.items() if k != "out"},

@@ -83,14 +83,16 @@ typedef struct scf_opts {
     int device;      /* CUDA device ordinal */
     int maxit;       /* outer PCG iterations (reference: 50, :108) */
     double rtol;     /* stop at ||b-Ax||_2 <= rtol ||b||_2 (reference: 1e-20, :111) */
-    int npre, npost; /* red-black Gauss-Seidel sweeps before / after coarse correction */
+    int npre, npost; /* sweeps before / after the coarse correction: red-black
+                        Gauss-Seidel iterations (point smoother); line smoother: a step
+                        of x-lines then y-lines counts as two */
     double omega;    /* scale of the coarse-grid correction */
     int coarse_max;  /* coarsest level has at most this many cells (<= 64) */
     int smoother;    /* SCF_SMOOTH_AUTO (default), SCF_SMOOTH_POINT or SCF_SMOOTH_LINE */
     int precond;     /* SCF_PRECOND_MG (default) or SCF_PRECOND_LEARNED */
-    int coarse_sweeps; /* line smoother: sweeps before / after the coarse correction on
-                          level coarse_from (0: the finest) and every coarser level;
-                          0 (default): npre / npost there too */
+    int coarse_sweeps; /* sweeps before / after the coarse correction on level
+                          coarse_from (0: the finest) and every coarser level (as
+                          npre / npost count them); 0 (default): npre / npost there too */
     int coarse_from;
     int reserved[4];
 } scf_opts;
@@ -139,11 +141,12 @@ int scf_proj_solve_rhs(struct scf_proj *h, const double *b, double *x, double *r
  * autotuner. */
 int scf_proj_set_opts(struct scf_proj *h, int npre, int npost, double omega);
 
-/* Line smoother: sweeps (1..8; a step of x-lines then y-lines counts as two)
- * before and after the coarse correction on level coarse_from (0: the
- * finest) and every coarser level, 0 for npre / npost there too; rebuilds the
- * graph.  The coarse levels are latency-bound, so more smoothing there
- * can cost less than the PCG iterations it saves.  Used by the autotuner. */
+/* Sweeps (1..8, counted as npre / npost count them: red-black iterations of
+ * the point smoother, two per alternating step of the line smoother) before
+ * and after the coarse correction on level coarse_from (0: the finest) and
+ * every coarser level, 0 for npre / npost there too; rebuilds the graph.
+ * The coarse levels are latency-bound, so more smoothing there can cost less
+ * than the PCG iterations it saves.  Used by the autotuner. */
 int scf_proj_set_coarse_sweeps(struct scf_proj *h, int coarse_from, int sweeps);
 
 /* Sweep tile of the red-black (point) smoother on an existing handle;

@@ -266,8 +266,8 @@ SMOOTHERS = {"point": 0, "line": 1}
 
 
 class _coarse_sweeps:
-    """The line smoother's coarse schedule (level, sweeps) for the calls in
-    a with-block; None or sweeps 0: npre / npost on every level."""
+    """The coarse-level schedule (level, sweeps) for the calls in a
+    with-block; None or sweeps 0: npre / npost on every level."""
 
     def __init__(self, coarse):
         self.c = coarse or (0, 0)

@@ -545,7 +545,7 @@ typedef struct {
     olevel lev[32];
     double omega;
     int npre, npost;
-    int cfrom, csweeps; /* line smoother: csweeps on levels cfrom and coarser (0: npre/npost) */
+    int cfrom, csweeps; /* csweeps sweeps on levels cfrom and coarser (0: npre / npost) */
     int line;        /* 1: alternating zebra line smoother */
     int nc;          /* coarsest unknowns */
     double *chol;    /* nc x nc lower Cholesky factor */
@@ -814,16 +814,17 @@ static void prolong_add(olevel *F, const olevel *C, double omega) {
         }
 }
 
-/* the coarse line-smoothing schedule of the next MG-PCG or V-cycle call:
-   sweeps (a step of x-lines then y-lines counts as two) on level cfrom (0:
-   the finest) and coarser; sweeps 0 keeps npre / npost everywhere */
+/* the coarse-level schedule of the next MG-PCG or V-cycle call: sweeps on
+   level cfrom (0: the finest) and coarser (point smoother: red-black
+   iterations; line smoother: a step of x-lines then y-lines counts as two);
+   sweeps 0 keeps npre / npost everywhere */
 static int g_cfrom = 0, g_csweeps = 0;
 void oracle_set_coarse_sweeps(int cfrom, int sweeps) { g_cfrom = cfrom; g_csweeps = sweeps; }
 
-static int line_steps(const omg *M, int l, int post) {
-    int sw = M->csweeps > 0 && l >= M->cfrom ? M->csweeps : (post ? M->npost : M->npre);
-    return (sw + 1) / 2;
+static int sweeps_at(const omg *M, int l, int post) {
+    return M->csweeps > 0 && l >= M->cfrom ? M->csweeps : (post ? M->npost : M->npre);
 }
+static int line_steps(const omg *M, int l, int post) { return (sweeps_at(M, l, post) + 1) / 2; }
 
 static void vcycle(omg *M, int l) {
     olevel *L = &M->lev[l];
@@ -834,7 +835,7 @@ static void vcycle(omg *M, int l) {
         /* a line step (x-lines and y-lines) counts as two sweeps */
         for (int s = 0; s < line_steps(M, l, 0); ++s) line_step(L, 0);
     } else {
-        for (int s = 0; s < M->npre; ++s) { rbgs_half(L, 0); rbgs_half(L, 1); }
+        for (int s = 0; s < sweeps_at(M, l, 0); ++s) { rbgs_half(L, 0); rbgs_half(L, 1); }
     }
     residual(L);
     restrict_sum(L, &M->lev[l + 1]);
@@ -843,7 +844,7 @@ static void vcycle(omg *M, int l) {
     if (M->line) {
         for (int s = 0; s < line_steps(M, l, 1); ++s) line_step(L, 1);
     } else {
-        for (int s = 0; s < M->npost; ++s) { rbgs_half(L, 1); rbgs_half(L, 0); }
+        for (int s = 0; s < sweeps_at(M, l, 1); ++s) { rbgs_half(L, 1); rbgs_half(L, 0); }
     }
 }
 

@@ -32,6 +32,9 @@ SCHEDULES = BATCH_SCHEDULES + [(2, 2, 1.97)]
 # sweep tiles of the point smoother (scf_proj_set_tile): 64 x 32 cells per
 # CTA (TMA-staged on the larger FP32 levels) and 32 x 32 (plain loads)
 TILES = {"64x32": 0, "32x32": 1}
+# coarse-level schedules (scf_proj_set_coarse_sweeps): (first level, sweeps)
+# on the latency-bound coarse levels, or None for npre / npost everywhere
+COARSE = [None, (1, 4), (2, 4)]
 
 
 def size_class(nx: int, ny: int) -> int:
@@ -79,10 +82,11 @@ class _Instance:
         self.s.close()
 
 
-def autotune(insts, schedules=BATCH_SCHEDULES, tiles=TILES, reps=3, log=None):
-    """Fastest schedule and sweep tile per size class:
-    {class: (npre, npost, omega, tile name)}.  Every schedule is timed with
-    every tile on one representative instance of the class."""
+def autotune(insts, schedules=BATCH_SCHEDULES, tiles=TILES, coarse=COARSE, reps=3, log=None):
+    """Fastest schedule, sweep tile and coarse-level schedule per size
+    class: {class: (npre, npost, omega, tile name, coarse)}.  Every schedule
+    is timed with every tile and coarse schedule on one representative
+    instance of the class."""
     import torch
     table = {}
     reps_by_class = {}
@@ -92,17 +96,19 @@ def autotune(insts, schedules=BATCH_SCHEDULES, tiles=TILES, reps=3, log=None):
         best = None
         for tname, tile in tiles.items():
             inst.s.set_tile(tile)
-            for sch in schedules:
-                inst.s.set_schedule(*sch)
-                inst.solve_once()  # warm (graph build)
-                torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                for _ in range(reps):
-                    st = inst.solve_once()
-                torch.cuda.synchronize()
-                ms = (time.perf_counter() - t0) / reps * 1e3
-                if st.status == 0 and (best is None or ms < best[0]):
-                    best = (ms, (*sch, tname), st.iters)
+            for co in coarse:
+                inst.s.set_coarse_sweeps(*(co or (0, 0)))
+                for sch in schedules:
+                    inst.s.set_schedule(*sch)
+                    inst.solve_once()  # warm (graph build)
+                    torch.cuda.synchronize()
+                    t0 = time.perf_counter()
+                    for _ in range(reps):
+                        st = inst.solve_once()
+                    torch.cuda.synchronize()
+                    ms = (time.perf_counter() - t0) / reps * 1e3
+                    if st.status == 0 and (best is None or ms < best[0]):
+                        best = (ms, (*sch, tname, co), st.iters)
         table[cls] = best[1]
         if log:
             log(f"autotune class 2^{cls}: {best[1]} {best[0]:.2f} ms, {best[2]} iterations")
@@ -123,6 +129,7 @@ class BatchProjector:
             if sch is not None:
                 inst.s.set_schedule(*sch[:3])
                 inst.s.set_tile(TILES[sch[3]] if len(sch) > 3 else 0)
+                inst.s.set_coarse_sweeps(*((sch[4] if len(sch) > 4 else None) or (0, 0)))
         L = P.load()
         handles = (C.c_void_p * len(self.insts))(*[i.s._h.value for i in self.insts])
         b = C.c_void_p()

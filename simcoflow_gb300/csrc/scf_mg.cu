@@ -795,7 +795,8 @@ __global__ void __launch_bounds__(1024) k_tail(TailDesc<T, CT> d, Scalars* sc) {
   };
   const int n = d.n;
   for (int l = 0; l < n - 1; ++l) {
-    for (int it = 0; it < d.npre; ++it) { relax(l, 0); relax(l, 1); }
+    const int np = l >= d.cfrom ? d.cpre : d.npre;  // the coarse schedule from cfrom down
+    for (int it = 0; it < np; ++it) { relax(l, 0); relax(l, 1); }
     // residual summed 2x2 onto level l+1
     const MgView<T, CT, T>& L = d.lv[l];
     const MgView<T, CT, T>& C = d.lv[l + 1];
@@ -857,7 +858,8 @@ __global__ void __launch_bounds__(1024) k_tail(TailDesc<T, CT> d, Scalars* sc) {
         x[si] = fma(d.omega, xc[((iy >> 1) + 1) * wc + (ix >> 1) + 1], x[si]);
     }
     __syncthreads();
-    for (int it = 0; it < d.npost; ++it) { relax(l, 1); relax(l, 0); }
+    const int nq = l >= d.cfrom ? d.cpost : d.npost;
+    for (int it = 0; it < nq; ++it) { relax(l, 1); relax(l, 0); }
   }
   {  // x of the first tail level back to global memory
     const MgView<T, CT, T>& L = d.lv[0];

@@ -43,7 +43,7 @@ struct TailDesc {
   int total;                // elements of T in shared memory
   int bd_off, smem;         // byte offset of the coarse gather buffer, total bytes
   int npre, npost;
-  // line smoother: tail levels cfrom and coarser use cpre / cpost sweeps
+  // tail levels cfrom and coarser use cpre / cpost sweeps
   int cfrom, cpre, cpost;
   T omega;
   const double* Ainv;

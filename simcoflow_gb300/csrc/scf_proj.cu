@@ -226,6 +226,15 @@ std::vector<int> sweep_launches(int n, bool fused2) {
   return c;
 }
 
+// Sweeps before (post: after) the coarse correction on level l: npre /
+// npost, or the coarse schedule's count from level coarse_from down (point
+// smoother: red-black iterations; line smoother: a step of x-lines then
+// y-lines counts as two)
+int sweeps_at(const scf_proj* h, int l, bool post) {
+  const scf_opts& o = h->opts;
+  return o.coarse_sweeps > 0 && l >= o.coarse_from ? o.coarse_sweeps : (post ? o.npost : o.npre);
+}
+
 // Buffer holding a level's result after its part of the V-cycle: sweep
 // launches alternate buffers (down, then up, starting from buffer 0), the
 // tail and the coarse solve write buffer 0.
@@ -234,8 +243,8 @@ int final_buf(scf_proj* h, int l) {
   const int L = (int)h->lev.size();
   const int lk = h->tail0 > 0 ? h->tail0 : L - 1;
   if (L == 1 || l >= lk) return 0;
-  const int npre = (int)sweep_launches(h->opts.npre, h->mixed).size();
-  const int npost = (int)sweep_launches(h->opts.npost, h->mixed).size();
+  const int npre = (int)sweep_launches(sweeps_at(h, l, false), h->mixed).size();
+  const int npost = (int)sweep_launches(sweeps_at(h, l, true), h->mixed).size();
   return (npre - 1 + npost) % 2;
 }
 
@@ -248,9 +257,6 @@ void enqueue_vcycle_t(scf_proj* h, ViewFn view, BufFn buf, const TailDesc<T, CT>
   using V = MgView<T, CT, T>;
   const int L = (int)h->lev.size();
   const bool fused2 = std::is_same<T, float>::value;
-  const std::vector<int> pre = sweep_launches(h->opts.npre, fused2),
-                         post = sweep_launches(h->opts.npost, fused2);
-  const int npre = (int)pre.size(), npost = (int)post.size();
   const double om = h->opts.omega;
   if (L == 1) {
     V c = view(0);
@@ -269,6 +275,8 @@ void enqueue_vcycle_t(scf_proj* h, ViewFn view, BufFn buf, const TailDesc<T, CT>
   for (int l = 0; l < lk; ++l) {
     V f = view(l);
     const V c = view(l + 1);  // restriction target (its b)
+    const std::vector<int> pre = sweep_launches(sweeps_at(h, l, false), fused2);
+    const int npre = (int)pre.size();
     for (int it = 0; it < npre; ++it) {
       f.xin = it > 0 ? buf(l, (it - 1) % 2) : nullptr;
       f.x = buf(l, it % 2);
@@ -293,6 +301,9 @@ void enqueue_vcycle_t(scf_proj* h, ViewFn view, BufFn buf, const TailDesc<T, CT>
   for (int l = lk - 1; l >= 0; --l) {
     V f = view(l);
     const V c = coarse_result(l + 1);
+    const int npre = (int)sweep_launches(sweeps_at(h, l, false), fused2).size();
+    const std::vector<int> post = sweep_launches(sweeps_at(h, l, true), fused2);
+    const int npost = (int)post.size();
     for (int it = 0; it < npost; ++it) {
       f.xin = buf(l, (npre - 1 + it) % 2);
       f.x = buf(l, (npre + it) % 2);
@@ -310,8 +321,8 @@ void enqueue_vcycle_t(scf_proj* h, ViewFn view, BufFn buf, const TailDesc<T, CT>
   }
 }
 
-// the coarse line-smoothing schedule of a line tail whose first level is
-// level l0 of the hierarchy (tail levels are numbered from 0)
+// the coarse-level schedule of a tail whose first level is level l0 of the
+// hierarchy (tail levels are numbered from 0)
 constexpr int kNoCoarse = 1 << 20;
 template <class D>
 void set_tail_coarse(D& d, const scf_opts& o, int l0) {
@@ -330,14 +341,8 @@ void enqueue_vcycle_line_t(scf_proj* h, ViewFn view, TViewFn tview, const TailDe
                            Scalars* sc, bool do_rz, int flexible, cudaStream_t s) {
   using V = MgView<T, CT, T>;
   const int L = (int)h->lev.size();
-  // steps per level (a step counts as two sweeps); the coarse schedule from
-  // level coarse_from down
-  auto steps = [h](int l, bool post) {
-    const scf_opts& o = h->opts;
-    const int sw = o.coarse_sweeps > 0 && l >= o.coarse_from ? o.coarse_sweeps
-                                                               : (post ? o.npost : o.npre);
-    return (sw + 1) / 2;
-  };
+  // steps per level (a step counts as two sweeps)
+  auto steps = [h](int l, bool post) { return (sweeps_at(h, l, post) + 1) / 2; };
   const double om = h->opts.omega;
   auto to_t = [&](const V& f, const V& ft) {
     launch_transpose<T>(f.x, f.nx, f.ny, f.pitch, ft.x, ft.pitch, sc, s);
@@ -1183,7 +1188,7 @@ int scf_proj_create(scf_proj** out, int nx, int ny, const scf_opts* opts) {
         d.n = nlev - l;
         for (int k = 0; k < d.n; ++k) d.lv[k] = view(l + k);
         d.npre = o.npre; d.npost = o.npost;
-        d.cfrom = kNoCoarse; d.cpre = d.cpost = 0;  // the point smoother's tail
+        set_tail_coarse(d, o, l);
         d.omega = (decltype(d.omega))o.omega;
         d.Ainv = h->Ainv; d.cmap = h->cmap; d.nc = h->ncoarse;
         return tail_prepare(d);
@@ -1842,7 +1847,12 @@ int scf_proj_set_coarse_sweeps(scf_proj* h, int coarse_from, int sweeps) {
   CK(cudaStreamSynchronize(h->stream));
   h->opts.coarse_sweeps = sweeps;
   h->opts.coarse_from = coarse_from;
-  if (h->ltail0 > 0) {  // the line tails carry their own copy of the schedule
+  // the tails carry their own copy of the schedule
+  if (h->tail0 > 0) {
+    set_tail_coarse(h->tail64, h->opts, h->tail0);
+    set_tail_coarse(h->tail32, h->opts, h->tail0);
+  }
+  if (h->ltail0 > 0) {
     set_tail_coarse(h->ltail64, h->opts, h->ltail0);
     set_tail_coarse(h->ltail32, h->opts, h->ltail0);
   }

@@ -336,9 +336,9 @@ class ProjectionSolver:
         self.opts.npre, self.opts.npost, self.opts.omega = npre, npost, omega
 
     def set_coarse_sweeps(self, coarse_from: int, sweeps: int):
-        """Line smoother: sweeps before / after the coarse correction on level
-        coarse_from (0: the finest) and every coarser one, 0 for npre / npost
-        there too (rebuilds the handle's graph)."""
+        """Sweeps before / after the coarse correction on level coarse_from
+        (0: the finest) and every coarser one, counted as npre / npost count
+        them; 0 for npre / npost there too (rebuilds the handle's graph)."""
         _check(load().scf_proj_set_coarse_sweeps(self._h, int(coarse_from), int(sweeps)),
                "scf_proj_set_coarse_sweeps")
         self.opts.coarse_from, self.opts.coarse_sweeps = int(coarse_from), int(sweeps)

@@ -34,7 +34,11 @@ def _apply(schedule):
 def test_point_smoother_schedule_sets_the_tile():
     from simcoflow_gb300 import batch as Bt
     for name, code in Bt.TILES.items():
-        assert _apply((2, 2, 1.9, name)) == [("schedule", (2, 2, 1.9)), ("tile", code)]
+        assert _apply((2, 2, 1.9, name)) == [("schedule", (2, 2, 1.9)), ("tile", code),
+                                             ("coarse", (0, 0))]
+        assert _apply((2, 2, 1.9, name, (1, 4))) == [("schedule", (2, 2, 1.9)), ("tile", code),
+                                                     ("coarse", (1, 4))]
+        assert _apply([2, 2, 1.9, name, None])[-1] == ("coarse", (0, 0))
 
 
 def test_line_smoother_schedule_sets_the_coarse_levels():
@@ -48,7 +52,7 @@ def test_schedule_without_extra_clears_the_coarse_schedule():
         assert _apply(sch) == [("schedule", (2, 2, sch[2])), ("coarse", (0, 0))]
 
 
-def test_every_line_candidate_is_a_valid_coarse_schedule():
+def test_every_candidate_is_a_valid_coarse_schedule():
     import bench
-    for co in bench.LINE_COARSE:
+    for co in bench.LINE_COARSE + bench.POINT_COARSE:
         assert co is None or (0 <= co[0] <= 64 and 1 <= co[1] <= 8)

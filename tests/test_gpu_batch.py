@@ -38,9 +38,10 @@ def test_batch_equals_single_instance_and_oracle(cuda, oracle):
         # a second launch of the same graph gives the same answers
         stats2, _ = bp.run()
         assert [s["iters"] for s in stats2] == [s["iters"] for s in stats]
-        # the autotuner chose a schedule and a sweep tile for every size class
+        # the autotuner chose a schedule, a sweep tile and a coarse-level
+        # schedule for every size class
         for cls, entry in bp.table.items():
-            assert len(entry) == 4 and entry[3] in B.TILES, (cls, entry)
+            assert len(entry) == 5 and entry[3] in B.TILES and entry[4] in B.COARSE, (cls, entry)
     finally:
         bp.close()
 

@@ -110,7 +110,12 @@ def test_odd_rectangular_grid(cuda, oracle):
     _check_solution(c, g, exp)
 
 
-def test_vcycle_matches_oracle(cuda, oracle):
+@pytest.mark.parametrize("coarse", [None, (1, 4), (2, 3)],
+                         ids=["uniform", "four_from_1", "three_from_2"])
+def test_vcycle_matches_oracle(cuda, oracle, coarse):
+    """The point-smoothed V-cycle against the oracle's, with npre / npost on
+    every level or a coarse-level schedule (an odd count changes which of
+    the two iterate buffers holds each level's result)."""
     c = synth.c4(n=128, instance=4)
     matr, _ = oracle.matrix(c)
     rng = np.random.Generator(np.random.PCG64(5))
@@ -118,10 +123,12 @@ def test_vcycle_matches_oracle(cuda, oracle):
     s = P.ProjectionSolver(c.nx, c.ny)
     try:
         s.setup_case(c)
+        if coarse:
+            s.set_coarse_sweeps(*coarse)
         xg = s.vcycle(b)
     finally:
         s.close()
-    xo = oracle.vcycle(c, matr, b, npre=2, npost=2, omega=1.9)
+    xo = oracle.vcycle(c, matr, b, npre=2, npost=2, omega=1.9, coarse=coarse)
     assert rel_l2(xg, xo) < 1e-11
 
 
@@ -246,6 +253,22 @@ def test_mixed_vcycle_is_close_to_fp64(cuda, oracle):
         finally:
             s.close()
     assert rel_l2(out["mixed"], out["fp64"]) < 3e-2
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_coarse_sweeps_point_smoother(cuda, oracle, precision):
+    """More sweeps on the coarse levels: the same solution as the oracle's
+    direct solve, in fewer PCG iterations on the 2048^2 configuration's
+    workload scaled down."""
+    c = synth.c2(n=512)
+    exp = oracle.project(c)
+    it = {}
+    for coarse in ((0, 0), (1, 4)):
+        g = _gpu_project(c, precision=precision, rtol=1e-13, maxit=200, coarse_from=coarse[0],
+                         coarse_sweeps=coarse[1])
+        _check_solution(c, g, exp)
+        it[coarse] = g["stats"]["iters"]
+    assert it[(1, 4)] < it[(0, 0)], it
 
 
 def test_mixed_preconditioner_iterations(cuda):
