@@ -199,8 +199,9 @@ __device__ __forceinline__ double pos_part(double v) {
 // significands from one high product; then the exact remainder corrects the
 // last digit and gives the round-to-nearest-even bit, the closing step of long
 // division (Knuth, TAOCP vol. 2, 4.3.1).  An exact midpoint cannot occur for
-// a quotient of two 53-bit significands.  Zero, subnormal, infinite or NaN
-// operands and results outside the normal range take the IEEE division.
+// a quotient of two 53-bit significands.  A power-of-two divisor gives the
+// exact quotient by exponent arithmetic alone.  Zero, subnormal, infinite or
+// NaN operands and results outside the normal range take the IEEE division.
 __device__ __forceinline__ double div_rn(double a, double b) {
   using u64 = unsigned long long;
   const u64 ua = (u64)__double_as_longlong(a), ub = (u64)__double_as_longlong(b);
@@ -211,6 +212,11 @@ __device__ __forceinline__ double div_rn(double a, double b) {
   const int E = ea - eb + 1022 + (int)ge;   // biased exponent of the result
   if ((unsigned)(ea - 1) >= 2046u || (unsigned)(eb - 1) >= 2046u || (unsigned)(E - 1) >= 2045u)
     return div_rare(a, b);
+  // b a power of two (uniform grid spacings, unit densities): the quotient is
+  // a's significand under the exponent E, exact
+  if ((ub & 0xfffffffffffffull) == 0ull)
+    return __longlong_as_double(
+        (long long)(((ua ^ ub) & (1ull << 63)) | ((u64)E << 52) | (ua & 0xfffffffffffffull)));
   float y0;
   asm("rcp.approx.ftz.f32 %0, %1;"
       : "=f"(y0)

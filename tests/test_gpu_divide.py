@@ -76,6 +76,20 @@ def test_near_exact_quotients():
     check(a.view(np.float64), b)
 
 
+def test_power_of_two_divisors():
+    """Divisors 2^k (uniform grid spacings, unit densities), which take the
+    exponent-only path, over the whole exponent range: quotients in the
+    normal range, next to overflow and down into the subnormals."""
+    rng = np.random.default_rng(16)
+    n = 1_000_000
+    a = rng.uniform(1.0, 2.0, n) * np.exp2(rng.integers(-1000, 1000, n)) * rng.choice([-1, 1], n)
+    b = np.exp2(rng.integers(-1022, 1024, n).astype(np.float64)) * rng.choice([-1, 1], n)
+    check(a, b)
+    k = np.arange(-1074, 1024, dtype=np.float64)
+    check(np.full(k.size, 1.5), np.exp2(k))
+    check(np.full(k.size, 3.0 * 2.0**-1000), np.exp2(k))
+
+
 def test_range_edges():
     """Results next to overflow and underflow, and the special operands."""
     big, tiny = np.finfo(np.float64).max, np.finfo(np.float64).tiny
