@@ -554,7 +554,9 @@ k_pupdate_spmv_t(LevelView L, const double* __restrict__ z, const double* __rest
 // row loop: each thread has all its loads (the direction of the cell and its
 // four neighbours, which mostly hit L1 / L2, and the operator) in flight at
 // once.  Cells outside the grid count as zeros.
-__global__ void __launch_bounds__(NT)
+// (64 registers: four CTAs per SM, so the grid's eight per SM run in two full
+// waves; at 72 registers, three per SM, the kernel took 213 against 175 us at 4096^2)
+__global__ void __launch_bounds__(NT, 4)
 k_pupdate_spmv_ff(LevelView L, const float* __restrict__ z, const float* __restrict__ pold,
                   float* __restrict__ pnew, double* __restrict__ q, Scalars* sc, double* part) {
   pdl_wait();
